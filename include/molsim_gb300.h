@@ -1,0 +1,250 @@
+/*
+ * molsim_gb300.h — C ABI of the GB300 force/energy hot path of MOLSIM.
+ *
+ * The reference (MOLSIM, Fortran 90) exposes this path as argument-less
+ * subroutines that work on module globals.  Each entry point below replaces
+ * one of them; the comment names the subroutine it stands in for
+ * (file:line in the reference's Src/ directory).  A Fortran caller binds
+ * these with ISO_C_BINDING; a Python caller with ctypes (molsim_gb300/).
+ *
+ * Conventions
+ *   - Every function returns an int status: MG_OK (0) or a negative MG_ERR_*.
+ *     The text of the last error (with the offending particle index where
+ *     there is one) is read with mg_last_error().  Where the reference calls
+ *     Stop(), the library returns the matching error instead; a hard-core
+ *     overlap in a trial move is a result (lhsoverlap), not an error.
+ *   - Arrays use the reference's layouts: positions/forces ro(3,np) are
+ *     column-major, i.e. x,y,z of particle 1, then particle 2 ...
+ *     Particle, type and pair indices are 1-based, as in the reference.
+ *   - The library copies every input array it keeps; it never frees or
+ *     retains caller memory.  One handle = one CUDA stream on the current
+ *     device; a handle is not thread safe.  Calls are synchronous: outputs
+ *     are valid when the call returns.
+ */
+#ifndef MOLSIM_GB300_H
+#define MOLSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MG_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define MG_OK                   0
+#define MG_ERR_ARG             -1  /* bad argument or parameter combination      */
+#define MG_ERR_CUDA            -2  /* a CUDA runtime call failed                 */
+#define MG_ERR_TABLE_UNDERRUN  -3  /* r2 < r2umin   (energy.F90:478, Stop)       */
+#define MG_ERR_NEIGH_OVERFLOW  -4  /* nneighpn > maxnneigh (nlist.F90:752, Stop) */
+#define MG_ERR_NAN             -5  /* non-finite force or energy                 */
+#define MG_ERR_TIMEOUT         -6  /* a bounded device wait ran out              */
+#define MG_ERR_IBUF            -7  /* ibuf > nbuf   (energy.F90:484, Stop)       */
+#define MG_ERR_TABLE           -8  /* table build failed (potential.F90:1121,1129) */
+#define MG_ERR_STATE           -9  /* call made out of order                     */
+#define MG_ERR_ALLOC          -10  /* device or host allocation failed           */
+#define MG_ERR_UNSUPPORTED    -11  /* option outside the built path              */
+#define MG_ERR_CELL           -12  /* particle outside the cell grid             */
+
+/* ---- option values ----------------------------------------------------- */
+enum { MG_EWALD_NONE = 0, MG_EWALD_STD = 1, MG_EWALD_SPM = 2 };   /* txewaldrec */
+enum { MG_VLIST = 0, MG_CELLLIST = 1 };                           /* txintlist  */
+enum { MG_MD = 0, MG_MC = 1, MG_BD = 2 };                         /* lmd/lmc/lbd */
+enum { MG_FP64 = 0, MG_MIXED = 1 };                               /* precision form */
+
+/*
+ * System description: the subset of MolModule (mol.F90:1087-1218) and
+ * EnergyModule (energy.F90:98-256) that the hot path reads, for a charged
+ * monoatomic system in a rectangular periodic box (txbc='xyz').
+ */
+typedef struct mg_params {
+    int32_t abi_version;      /* must be MG_ABI_VERSION                          */
+    int32_t np;               /* number of particles (monoatomic: na == np)     */
+    int32_t npt;              /* number of particle types                       */
+    int32_t nptpt;            /* number of type pairs, npt*(npt+1)/2            */
+    const int32_t *iptpn;     /* [np] type of each particle, 1..npt             */
+    const int32_t *iptpt;     /* [npt*npt] iptpt(ipt,jpt), column-major, 1..nptpt */
+    const double  *az;        /* [np] charge of each particle (units of e)      */
+
+    /* tabulated two-body potential (PotTwoBodyTab1, potential.F90:868) */
+    int32_t nbuf;             /* number of doubles in ubuf                      */
+    const double  *ubuf;      /* [nbuf] 12 doubles per interval                 */
+    const int32_t *iubuflow;  /* [nptpt] 1-based start of each pair's table     */
+    const double  *r2umin;    /* [nptpt] lower end of each table                */
+    const double  *r2atat;    /* [nptpt] hard-core distance squared             */
+
+    double  boxlen[3];        /* box edges (Angstrom); box centred at origin    */
+    double  rcut;             /* real-space cutoff                              */
+    double  drnlist;          /* Verlet skin                                    */
+    int32_t txintlist;        /* MG_VLIST or MG_CELLLIST                        */
+    int32_t mode;             /* MG_MD, MG_MC or MG_BD (list kind and MC state) */
+    int32_t form;             /* MG_FP64 or MG_MIXED                            */
+    int32_t maxnneigh;        /* neighbour capacity per particle (0 = automatic) */
+
+    /* Ewald summation (EwaldSetup, energy.F90:6601) */
+    int32_t ewald;            /* MG_EWALD_NONE / _STD / _SPM                    */
+    double  ualpha;           /* Ewald damping parameter (1/Angstrom)           */
+    int32_t ncut;             /* std: k-vector cutoff                           */
+    int32_t ncutregion_cube;  /* std: 0 = 'sphere', 1 = 'cube'                  */
+    int32_t order;            /* SPME: B-spline order                           */
+    int32_t nmesh;            /* SPME: mesh points per edge (even)              */
+    int32_t lsurf;            /* 1 = add the surface term (UEwaldSurf)          */
+    double  epsi_four_pi;     /* EpsiFourPi = Epsi0FourPi/relpermitt            */
+    double  force_fac;        /* (sclene/scllen)/sclfor, force -> forceo        */
+
+    /* chain bonds (UBond, energy.F90:5335): u = k*(r-eq)**p per bond */
+    int32_t nbond;
+    const int32_t *bond_ip;   /* [nbond] first particle, 1-based                */
+    const int32_t *bond_jp;   /* [nbond] second particle, 1-based               */
+    const double  *bond_k;    /* [nbond]                                        */
+    const double  *bond_eq;   /* [nbond]                                        */
+    const int32_t *bond_p;    /* [nbond] integer power                          */
+} mg_params;
+
+/* Parameters of the (1,6,12) potential table (Pot_1_6_12, potential.F90:1349). */
+typedef struct mg_pot_params {
+    int32_t npt;
+    const int32_t *iptpt;     /* [npt*npt] column-major, 1-based                */
+    const double *zat;        /* [npt] charge per type                          */
+    const double *sigat;      /* [npt] LJ sigma per type                        */
+    const double *epsat;      /* [npt] LJ epsilon per type                      */
+    double rcut;
+    double ualpha;
+    double epsi_four_pi;
+    int32_t lcharge_ewald;    /* 1: charges with Ewald (CalcEwaldUfac factors)  */
+    int32_t lljcut;           /* 1: truncate LJ at ljrcut*sig and shift         */
+    double ljrcut;
+    double ljushift;
+    double r2uminin;          /* reference default 0.1                          */
+    double utoltab, ftoltab;  /* reference default 1e-5 (a single-precision literal) */
+    double umaxtab, fmaxtab;  /* reference default 20000                        */
+} mg_pot_params;
+
+typedef struct mg_handle mg_handle;
+
+/* ---- library information ----------------------------------------------- */
+int         mg_abi_version(void);
+const char *mg_status_string(int status);
+/* Text of the last error of this handle (NUL-terminated, truncated to n). */
+int         mg_last_error(const mg_handle *h, char *buf, size_t n);
+
+/* ---- host set-up (once per parameter set) -------------------------------- */
+
+/* PotTwoBodyTab1/2/3 + SetUBuffer + CheckUBuffer (potential.F90:868-1263) for
+ * the (1,6,12) potential.  Writes up to nbuf_cap doubles into ubuf and always
+ * sets *nbuf_used; returns MG_ERR_TABLE if the capacity is too small (call
+ * again with a larger buffer) or the interval search does not converge. */
+int mg_pot_twobody_tab(const mg_pot_params *pp, double *ubuf, int32_t nbuf_cap,
+                       int32_t *nbuf_used, int32_t *iubuflow, double *r2umin,
+                       int32_t *nugrid);
+
+/* RcutToAlpha (energy.F90:7090-7106): alpha from tolerance and cutoff
+ * (iewaldopt = 3, charged system, lq2sum = 0). */
+int mg_rcut_to_alpha(double uewaldtol, double rcut, double q2sum,
+                     double boxlenshort, double epsi_four_pi, double *ualpha);
+
+/* ---- handle ---------------------------------------------------------------- */
+
+/* Copies the system, builds the Ewald arrays (kfac, or meshfac/energyfac/
+ * virfac as EwaldSetup, energy.F90:6601-7018) and allocates device memory. */
+int mg_create(const mg_params *p, mg_handle **h);
+int mg_destroy(mg_handle *h);
+
+/* ro(3,np): upload positions (the ro array of MolModule). */
+int mg_set_positions(mg_handle *h, const double *ro);
+int mg_get_positions(mg_handle *h, double *ro);
+
+/* ---- neighbour lists (A1-A4) --------------------------------------------- */
+
+/* NList(iWriteInput) (nlist.F90:553-596): builds the Verlet list
+ * (SetVListMD / SetVListMC, nlist.F90:724-890) or the cell list
+ * (InitCellList(rcut+drnlist) + SetCellList, celllist.F90:76,384). */
+int mg_nlist_set(mg_handle *h);
+
+/* NList(iSimulationStep) (nlist.F90:598-621): accumulates drostep(3,np) and
+ * rebuilds the Verlet list when sqrt(r2max1)+sqrt(r2max2) > drnlist.
+ * drostep may be NULL to use the displacements of the last device step. */
+int mg_nlist_update(mg_handle *h, const double *drostep, int32_t *rebuilt);
+
+/* Verlet list in the reference's layout: nneighpn(np) and
+ * jpnlist(maxnneigh,np), column-major, 1-based.  MD/BD: half list with the
+ * (ip+jp) parity owner rule (nlist.F90:742-745); MC: full list. */
+int mg_nlist_get(mg_handle *h, int32_t *nneighpn, int32_t *jpnlist,
+                 int32_t maxnneigh);
+
+/* Cell list: ncell[3] = ncellX..Z (InitCellList), and for every particle the
+ * 0-based cell id  ix + iy*ncellX + iz*ncellX*ncellY  (pcellro). */
+int mg_celllist_get(mg_handle *h, int32_t *ncell, int32_t *cellip);
+
+/* ---- energies and forces (A5-A12, A15) ------------------------------------ */
+
+/* UTotal (energy.F90:280-430) for a charged monoatomic system: two-body
+ * (UTwoBodyA / UTwoBodyACellList), Ewald (UEwaldRecStd or UEwaldRecSPM,
+ * UEwaldSelf, UEwaldSurf), UBond and the force epilogue.
+ *   forceo  [3*np]  forces scaled by force_fac (may be NULL)
+ *   u_twob  [nptpt+1] u%twob(0:nptpt)            (may be NULL)
+ *   uout    [4]  u%tot, u%rec, u%bond, virial    (may be NULL)          */
+int mg_utotal(mg_handle *h, double *forceo, double *u_twob, double *uout);
+
+/* ---- Monte Carlo trial moves (A13, A14) ------------------------------------ */
+
+/* DUTotal (denergy.F90:98-215) for nptm moving particles ipnptm(1:nptm)
+ * at trial positions rotm(3,nptm).  Returns du%twob(0:nptpt) in du_twob,
+ * du%rec in *du_rec, du%tot in *du_tot and the hard-core flag. */
+int mg_dutotal(mg_handle *h, int32_t nptm, const int32_t *ipnptm,
+               const double *rotm, double *du_twob, double *du_rec,
+               double *du_tot, int32_t *lhsoverlap);
+
+/* MCUpdate for the last mg_dutotal trial (mc.F90:5203-5235): ro = rotm,
+ * EwaldUpdateArray (denergy.F90:1776) and UpdateCellIp (celllist.F90:366). */
+int mg_accept(mg_handle *h);
+
+/* Many independent single-particle trials against the current
+ * configuration: trial t moves particle ip[t] to rtrial(3,t).  Writes
+ * du_tot[t] (= du%tot) and lhsoverlap[t]. */
+int mg_dutotal_batch(mg_handle *h, int32_t ntrial, const int32_t *ip,
+                     const double *rtrial, double *du_tot, int32_t *lhsoverlap);
+
+/* ---- integrators ------------------------------------------------------------ */
+
+/* Velocity-Verlet (VelVer, md.F90:252-420 + GetLinAcc md.F90:601-625) for a
+ * monoatomic system: massip[np] inverse masses, tstep in ps.  rod/rodd
+ * velocity and acceleration arrays (3*np) are uploaded by mg_md_setup. */
+int mg_md_setup(mg_handle *h, double tstep, const double *massip,
+                const double *rod, const double *rodd);
+/* nstep velocity-Verlet steps on the device, each with the Verlet-list
+ * check of NList(iSimulationStep).  Outputs as mg_utotal for the last step;
+ * rod/rodd (may be NULL) receive the final velocities and accelerations. */
+int mg_md_run(mg_handle *h, int32_t nstep, double *forceo, double *uout,
+              double *rod, double *rodd);
+
+/* Brownian dynamics (BDStep, bd.F90:120-155): fac1, fac2 per type as the
+ * reference computes them; iseed is the GauRandom seed (mollib.F90:2739). */
+int mg_bd_setup(mg_handle *h, const double *fac1, const double *fac2,
+                int32_t iseed);
+/* nstep BD steps on the device (BDStep, then UTotal, then the list check).
+ * The first call computes forceo from the current positions before the
+ * first step, as BDDriver does at its initial stage. */
+int mg_bd_run(mg_handle *h, int32_t nstep, double *forceo, double *uout);
+/* One BD step as the host caller sees it: ro_io (3*np, host) is uploaded,
+ * one step is taken, and ro_io and forceo (host) are written back. */
+int mg_bd_step_host(mg_handle *h, double *ro_io, double *forceo, double *uout);
+/* GauRandom state after the BD steps run so far. */
+int mg_bd_get_seed(mg_handle *h, int32_t *iseed);
+
+/* ---- timing ------------------------------------------------------------------ */
+
+/* Average device time per call (ms) of each phase since the last reset,
+ * measured with CUDA events on the handle's stream; names in *names
+ * (comma separated).  Used for the roofline. */
+int mg_phase_times(mg_handle *h, double *ms, int32_t nmax, int32_t *nphase,
+                   char *names, size_t names_len);
+int mg_phase_reset(mg_handle *h, int32_t enable);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOLSIM_GB300_H */

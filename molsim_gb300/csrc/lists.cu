@@ -1,0 +1,554 @@
+// lists.cu — cell list and Verlet list on the device (rows A1-A5).
+//
+// Reference: InitCellList / pcellro / SetCellList (celllist.F90:76-410),
+// SetVListMD / SetVListMC (nlist.F90:724-890), the rebuild rule of
+// NList(iSimulationStep) (nlist.F90:598-621) and PBCr2 (molaux.F90:149-184).
+//
+// GB300 form: the reference's per-cell linked lists become a counting sort of
+// particles into cell order (slot space); the Verlet list is built per slot
+// from the 27 neighbour cells and stored column-major (nbr[k*np+slot]) so a
+// warp reading neighbour k of 32 consecutive slots touches one 128-byte line.
+// Inside a cell particles are ordered by index, so lists are deterministic.
+// Membership decisions (cell index, r^2 < (rcut+drnlist)^2) use round-to-
+// nearest FP64 without contraction, giving the reference's sets bit-exactly.
+#include <algorithm>
+#include <cstdio>
+
+#include "mg_internal.cuh"
+
+namespace {
+
+__global__ void k_cell_assign(const double *__restrict__ ro, int np, double3 half, double3 csi,
+                              int3 nc, int *__restrict__ cellof, int *__restrict__ count,
+                              int *__restrict__ err, const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    // i = floor((ro + boxlen2) * cellSizei)   (celllist.F90:303)
+    int ix = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 0], half.x), csi.x));
+    int iy = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 1], half.y), csi.y));
+    int iz = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 2], half.z), csi.z));
+    if (ix < 0 || ix >= nc.x || iy < 0 || iy >= nc.y || iz < 0 || iz >= nc.z) {
+        // outside the grid (the reference indexes out of bounds here): report
+        // it and clamp so the sort below stays a permutation
+        mg_dev_error(err, MG_ERR_CELL, p + 1, 0, 0);
+        ix = min(max(ix, 0), nc.x - 1);
+        iy = min(max(iy, 0), nc.y - 1);
+        iz = min(max(iz, 0), nc.z - 1);
+    }
+    int c = ix + iy * nc.x + iz * nc.x * nc.y;
+    cellof[p] = c;
+    atomicAdd(&count[c], 1);
+}
+
+// single-block exclusive scan: out[i] = sum(in[0..i)), out[n] = total
+__global__ void k_scan1(const int *__restrict__ in, int *__restrict__ out, int n,
+                        const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    __shared__ int warp_sums[32];
+    int t = threadIdx.x, nt = blockDim.x;
+    int chunk = (n + nt - 1) / nt;
+    int b = t * chunk, e = min(n, b + chunk);
+    int s = 0;
+    for (int i = b; i < e; ++i) s += in[i];
+    // block exclusive scan of s
+    int lane = t & 31, w = t >> 5;
+    int v = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) warp_sums[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int nw = nt >> 5;
+        int x = (lane < nw) ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < nw) warp_sums[lane] = x;
+    }
+    __syncthreads();
+    int excl = v - s + (w > 0 ? warp_sums[w - 1] : 0);
+    for (int i = b; i < e; ++i) {
+        out[i] = excl;
+        excl += in[i];
+    }
+    if (t == nt - 1) out[n] = excl;
+}
+
+__global__ void k_cell_scatter(const int *__restrict__ cellof, int np, const int *__restrict__ start,
+                               int *__restrict__ fill, int *__restrict__ perm,
+                               const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int c = cellof[p];
+    int slot = start[c] + atomicAdd(&fill[c], 1);
+    perm[slot] = p;
+}
+
+// order each cell's particles by index (insertion sort; cells are small)
+__global__ void k_cell_sort(int ncell, const int *__restrict__ start, int *__restrict__ perm,
+                            const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    int b = start[c], e = start[c + 1];
+    for (int i = b + 1; i < e; ++i) {
+        int v = perm[i], j = i - 1;
+        while (j >= b && perm[j] > v) {
+            perm[j + 1] = perm[j];
+            --j;
+        }
+        perm[j + 1] = v;
+    }
+}
+
+__global__ void k_slot_of(const int *__restrict__ perm, int np, int *__restrict__ slot,
+                          const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < np) slot[perm[s]] = s;
+}
+
+struct StencilArgs {
+    int3 nc;
+    int lo[3], hi[3];   // neighbour offset range per dimension ({-1..1} or {0..0})
+};
+
+// Verlet list of slot i: all slots j != i in the neighbour cells with
+// r^2 < rs2cut (SetVListMD/MC membership; the half-list ownership rule is
+// applied only when the list is exported in the reference layout).
+__global__ void k_vlist(const double *__restrict__ ro, const int *__restrict__ perm,
+                        const int *__restrict__ cellof, const int *__restrict__ start, int np,
+                        StencilArgs sa, mg_box box, double rs2cut, int maxnb,
+                        int *__restrict__ nnb, int *__restrict__ nbr, int *__restrict__ err,
+                        const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    int p = perm[i];
+    double xi = ro[3 * p], yi = ro[3 * p + 1], zi = ro[3 * p + 2];
+    int c = cellof[p];
+    int cx = c % sa.nc.x, cy = (c / sa.nc.x) % sa.nc.y, cz = c / (sa.nc.x * sa.nc.y);
+    int cnt = 0;
+    for (int dz = sa.lo[2]; dz <= sa.hi[2]; ++dz) {
+        int z = cz + dz;
+        z += (z < 0) ? sa.nc.z : 0;
+        z -= (z >= sa.nc.z) ? sa.nc.z : 0;
+        for (int dy = sa.lo[1]; dy <= sa.hi[1]; ++dy) {
+            int y = cy + dy;
+            y += (y < 0) ? sa.nc.y : 0;
+            y -= (y >= sa.nc.y) ? sa.nc.y : 0;
+            for (int dx = sa.lo[0]; dx <= sa.hi[0]; ++dx) {
+                int x = cx + dx;
+                x += (x < 0) ? sa.nc.x : 0;
+                x -= (x >= sa.nc.x) ? sa.nc.x : 0;
+                int cc = x + y * sa.nc.x + z * sa.nc.x * sa.nc.y;
+                int b = start[cc], e = start[cc + 1];
+                for (int j = b; j < e; ++j) {
+                    if (j == i) continue;
+                    int q = perm[j];
+                    double ddx = mg_pbc1(__dsub_rn(xi, ro[3 * q]), box.half[0], box.len[0]);
+                    double ddy = mg_pbc1(__dsub_rn(yi, ro[3 * q + 1]), box.half[1], box.len[1]);
+                    double ddz = mg_pbc1(__dsub_rn(zi, ro[3 * q + 2]), box.half[2], box.len[2]);
+                    double r2 = mg_r2_exact(ddx, ddy, ddz);
+                    if (r2 < rs2cut) {
+                        if (cnt < maxnb) nbr[(size_t)cnt * np + i] = j;
+                        ++cnt;
+                    }
+                }
+            }
+        }
+    }
+    if (cnt > maxnb) {
+        mg_dev_error(err, MG_ERR_NEIGH_OVERFLOW, p + 1, cnt, maxnb);
+        cnt = maxnb;
+    }
+    nnb[i] = cnt;
+}
+
+// ---- NList(iSimulationStep) rebuild rule (nlist.F90:598-621) ---------------
+// The reference scans particles in order keeping r2max1 (running maximum) and
+// r2max2 (largest value that was not a new running maximum when met).  The
+// device reproduces that exactly: pass 1 accumulates drosum and block maxima,
+// pass 2 finds per block the non-record values given the maximum of all
+// earlier blocks, pass 3 combines.
+__global__ void k_chk_accum(const double *__restrict__ drostep, double *__restrict__ drosum,
+                            double *__restrict__ r2out, double *__restrict__ blkmax, int np,
+                            const int *__restrict__ flag) {
+    __shared__ double red[32];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool reset = (*flag != 0);   // a rebuild happened at the previous check
+    double r2 = 0.0;
+    if (p < np) {
+        double s0, s1, s2;
+        if (reset) {
+            s0 = 0.0 + drostep[3 * p];
+            s1 = 0.0 + drostep[3 * p + 1];
+            s2 = 0.0 + drostep[3 * p + 2];
+        } else {
+            s0 = __dadd_rn(drosum[3 * p], drostep[3 * p]);
+            s1 = __dadd_rn(drosum[3 * p + 1], drostep[3 * p + 1]);
+            s2 = __dadd_rn(drosum[3 * p + 2], drostep[3 * p + 2]);
+        }
+        drosum[3 * p] = s0;
+        drosum[3 * p + 1] = s1;
+        drosum[3 * p + 2] = s2;
+        r2 = mg_r2_exact(s0, s1, s2);
+        r2out[p] = r2;
+    }
+    double m = r2;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int nw = blockDim.x >> 5;
+        double x = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if (threadIdx.x == 0) blkmax[blockIdx.x] = x;
+    }
+}
+
+__global__ void k_chk_second(const double *__restrict__ r2in, const double *__restrict__ blkmax,
+                             double *__restrict__ blk2, int np) {
+    __shared__ double wmax[32], red[32];
+    __shared__ double pb;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int b = 0; b < (int)blockIdx.x; ++b) m = fmax(m, blkmax[b]);
+        pb = m;
+    }
+    double r2 = (p < np) ? r2in[p] : 0.0;
+    // inclusive prefix max within the warp
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double v = r2;
+    for (int o = 1; o < 32; o <<= 1) {
+        double y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = fmax(v, y);
+    }
+    if (lane == 31) wmax[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        double x = (lane < nw) ? wmax[lane] : 0.0;
+        for (int o = 1; o < 32; o <<= 1) {
+            double y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = fmax(x, y);
+        }
+        if (lane < nw) wmax[lane] = x;
+    }
+    __syncthreads();
+    double excl = __shfl_up_sync(0xffffffffu, v, 1);
+    if (lane == 0) excl = 0.0;
+    if (w > 0) excl = fmax(excl, wmax[w - 1]);
+    double prev = fmax(pb, excl);   // running maximum before this particle
+    double cand = (p < np && !(r2 > prev)) ? r2 : 0.0;
+    for (int o = 16; o > 0; o >>= 1) cand = fmax(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+    if (lane == 0) red[w] = cand;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int nw = blockDim.x >> 5;
+        double x = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if (threadIdx.x == 0) blk2[blockIdx.x] = x;
+    }
+}
+
+__global__ void k_chk_final(const double *__restrict__ blkmax, const double *__restrict__ blk2,
+                            int nblk, double drnlist, int *__restrict__ flag) {
+    if (threadIdx.x != 0) return;
+    double m1 = 0.0, m2 = 0.0;
+    for (int b = 0; b < nblk; ++b) {
+        m1 = fmax(m1, blkmax[b]);
+        m2 = fmax(m2, blk2[b]);
+    }
+    flag[0] = (sqrt(m1) + sqrt(m2) > drnlist) ? 1 : 0;
+}
+
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+// ---- MC cell list: the reference's doubly linked lists on the device -------
+__global__ void k_mc_cells_set(const double *__restrict__ ro, int np, double3 half, double3 csi,
+                               int3 nc, int *__restrict__ iphead, int *__restrict__ npart,
+                               int *__restrict__ ipnext, int *__restrict__ ipprev,
+                               int *__restrict__ cellof, int *__restrict__ err) {
+    // SetCellList: add ip = 1..np in order (head insertion); one thread keeps
+    // the reference's list order
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int p = 0; p < np; ++p) {
+        int ix = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 0], half.x), csi.x));
+        int iy = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 1], half.y), csi.y));
+        int iz = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 2], half.z), csi.z));
+        if (ix < 0 || ix >= nc.x || iy < 0 || iy >= nc.y || iz < 0 || iz >= nc.z) {
+            mg_dev_error(err, MG_ERR_CELL, p + 1, 0, 0);
+            return;
+        }
+        int c = ix + iy * nc.x + iz * nc.x * nc.y;
+        int ip = p + 1;
+        npart[c] += 1;
+        int jp = iphead[c];
+        iphead[c] = ip;
+        if (jp != 0) {
+            ipprev[jp - 1] = ip;
+            ipnext[ip - 1] = jp;
+        } else {
+            ipnext[ip - 1] = 0;
+        }
+        ipprev[ip - 1] = 0;
+        cellof[p] = c;
+    }
+}
+
+// UpdateCellIp (celllist.F90:366-382) for one particle (1-based ip)
+__global__ void k_mc_cells_update(const double *__restrict__ ro, int ip, double3 half, double3 csi,
+                                  int3 nc, int *__restrict__ iphead, int *__restrict__ npart,
+                                  int *__restrict__ ipnext, int *__restrict__ ipprev,
+                                  int *__restrict__ cellof, int *__restrict__ err) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int p = ip - 1;
+    int ix = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 0], half.x), csi.x));
+    int iy = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 1], half.y), csi.y));
+    int iz = (int)floor(__dmul_rn(__dadd_rn(ro[3 * p + 2], half.z), csi.z));
+    if (ix < 0 || ix >= nc.x || iy < 0 || iy >= nc.y || iz < 0 || iz >= nc.z) {
+        mg_dev_error(err, MG_ERR_CELL, ip, 0, 0);
+        return;
+    }
+    int cnew = ix + iy * nc.x + iz * nc.x * nc.y, cold = cellof[p];
+    if (cnew == cold) return;
+    // RmIpFromCell
+    npart[cold] -= 1;
+    int nextp = ipnext[p], prevp = ipprev[p];
+    if (nextp == 0) {
+        if (iphead[cold] == ip) iphead[cold] = 0;
+        else ipnext[prevp - 1] = 0;
+    } else {
+        if (iphead[cold] == ip) {
+            iphead[cold] = nextp;
+            ipprev[nextp - 1] = 0;
+        } else {
+            ipprev[nextp - 1] = prevp;
+            ipnext[prevp - 1] = nextp;
+        }
+    }
+    ipprev[p] = 0;
+    ipnext[p] = 0;
+    // AddIpToCell
+    npart[cnew] += 1;
+    int jp = iphead[cnew];
+    iphead[cnew] = ip;
+    if (jp != 0) {
+        ipprev[jp - 1] = ip;
+        ipnext[p] = jp;
+    } else {
+        ipnext[p] = 0;
+    }
+    ipprev[p] = 0;
+    cellof[p] = cnew;
+}
+
+StencilArgs make_stencil(const mg_handle *h) {
+    StencilArgs sa;
+    sa.nc = make_int3(h->ncell[0], h->ncell[1], h->ncell[2]);
+    for (int m = 0; m < 3; ++m) {
+        // a collapsed dimension (one cell) has only the cell itself;
+        // otherwise there are >= 3 cells and -1, 0, +1 are distinct
+        sa.lo[m] = (h->ncell[m] >= 3) ? -1 : 0;
+        sa.hi[m] = (h->ncell[m] >= 3) ? 1 : 0;
+    }
+    return sa;
+}
+
+mg_box make_box(const mg_handle *h) {
+    mg_box b;
+    for (int m = 0; m < 3; ++m) {
+        b.len[m] = h->boxlen[m];
+        b.half[m] = h->boxlen2[m];
+        b.inv[m] = h->boxleni[m];
+    }
+    return b;
+}
+
+}  // namespace
+
+void mg_scan_exclusive(mg_handle *h, const int *in, int *out, int n, const int *gate) {
+    k_scan1<<<1, 1024, 0, h->st>>>(in, out, n, gate);
+    h->launches++;
+}
+
+// InitCellList(rcut + drnlist) (celllist.F90:76-152): grid and stencil range
+int mg_lists_init(mg_handle *h) {
+    double rcell = h->rcut + h->drnlist;
+    if (!(rcell > 0)) return mg_fail(h, MG_ERR_ARG, "rcut + drnlist must be > 0");
+    double ircell = 1.0 / rcell;
+    for (int m = 0; m < 3; ++m) {
+        int n = (int)floor(h->boxlen[m] * ircell);
+        if (n < 1) n = 1;
+        h->ncell[m] = n;
+        h->cellSize[m] = h->boxlen[m] / n;
+        h->cellSizei[m] = 1.0 / h->cellSize[m];
+    }
+    for (int m = 0; m < 3; ++m) {
+        int dir = (int)ceil(h->rcut * h->cellSizei[m]);
+        if (2 * dir + 1 > h->ncell[m]) {
+            h->ncell[m] = 1;
+            h->cellSize[m] = h->boxlen[m];
+            h->cellSizei[m] = h->boxleni[m];
+        }
+    }
+    h->ncelltot = h->ncell[0] * h->ncell[1] * h->ncell[2];
+    int np = h->np;
+    if (h->maxnb <= 0) {
+        // automatic capacity: twice the expected number within rcut+drnlist,
+        // at least 64, at most np-1 (the reference's own maxnneigh is >= np-1)
+        double dens = np / h->vol;
+        double expect = 4.0 / 3.0 * 3.141592653589793 * rcell * rcell * rcell * dens;
+        int cap = (int)(2.0 * expect + 64);
+        if (cap > np - 1) cap = np - 1;
+        if (cap < 1) cap = 1;
+        h->maxnb = cap;
+    }
+    size_t nc = (size_t)h->ncelltot;
+    MG_CUDA(h, cudaMalloc(&h->d_cellof, sizeof(int) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_cellcount, sizeof(int) * nc));
+    MG_CUDA(h, cudaMalloc(&h->d_cellfill, sizeof(int) * nc));
+    MG_CUDA(h, cudaMalloc(&h->d_cellstart, sizeof(int) * (nc + 1)));
+    MG_CUDA(h, cudaMalloc(&h->d_perm, sizeof(int) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_slot, sizeof(int) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_nnb, sizeof(int) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_nbr, sizeof(int) * (size_t)h->maxnb * np));
+    MG_CUDA(h, cudaMalloc(&h->d_pos_s, sizeof(double4) * np));
+    h->nblk_chk = (np + 1023) / 1024;
+    MG_CUDA(h, cudaMalloc(&h->d_drostep, sizeof(double) * 3 * np));
+    MG_CUDA(h, cudaMalloc(&h->d_drosum, sizeof(double) * 3 * np));
+    MG_CUDA(h, cudaMalloc(&h->d_blkmax, sizeof(double) * (2 * h->nblk_chk + np)));
+    MG_CUDA(h, cudaMalloc(&h->d_rebuild, sizeof(int) * 2));
+    MG_CUDA(h, cudaMemsetAsync(h->d_drosum, 0, sizeof(double) * 3 * np, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_drostep, 0, sizeof(double) * 3 * np, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_rebuild, 0, sizeof(int) * 2, h->st));
+    if (h->mode == MG_MC && h->txintlist == MG_CELLLIST) {
+        MG_CUDA(h, cudaMalloc(&h->d_iphead, sizeof(int) * nc));
+        MG_CUDA(h, cudaMalloc(&h->d_npart, sizeof(int) * nc));
+        MG_CUDA(h, cudaMalloc(&h->d_ipnext, sizeof(int) * np));
+        MG_CUDA(h, cudaMalloc(&h->d_ipprev, sizeof(int) * np));
+    }
+    return MG_OK;
+}
+
+// Cell sort + Verlet list.  With `conditional`, every kernel first reads the
+// device rebuild flag and returns when it is 0 (graph-friendly rebuild).
+int mg_lists_build(mg_handle *h, bool conditional) {
+    int np = h->np;
+    const int *gate = conditional ? h->d_rebuild : nullptr;
+    double3 half = make_double3(h->boxlen2[0], h->boxlen2[1], h->boxlen2[2]);
+    double3 csi = make_double3(h->cellSizei[0], h->cellSizei[1], h->cellSizei[2]);
+    int3 nc = make_int3(h->ncell[0], h->ncell[1], h->ncell[2]);
+    int tb = 256, gb = (np + tb - 1) / tb;
+    MG_CUDA(h, cudaMemsetAsync(h->d_cellcount, 0, sizeof(int) * h->ncelltot, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_cellfill, 0, sizeof(int) * h->ncelltot, h->st));
+    k_cell_assign<<<gb, tb, 0, h->st>>>(h->d_ro, np, half, csi, nc, h->d_cellof, h->d_cellcount,
+                                        h->d_err, gate);
+    mg_scan_exclusive(h, h->d_cellcount, h->d_cellstart, h->ncelltot, gate);
+    k_cell_scatter<<<gb, tb, 0, h->st>>>(h->d_cellof, np, h->d_cellstart, h->d_cellfill, h->d_perm,
+                                         gate);
+    k_cell_sort<<<(h->ncelltot + tb - 1) / tb, tb, 0, h->st>>>(h->ncelltot, h->d_cellstart,
+                                                               h->d_perm, gate);
+    k_slot_of<<<gb, tb, 0, h->st>>>(h->d_perm, np, h->d_slot, gate);
+    k_vlist<<<gb, 128, 0, h->st>>>(h->d_ro, h->d_perm, h->d_cellof, h->d_cellstart, np,
+                                   make_stencil(h), make_box(h), h->rs2cut, h->maxnb, h->d_nnb,
+                                   h->d_nbr, h->d_err, gate);
+    h->launches += 6;
+    MG_CUDA(h, cudaGetLastError());
+    h->list_valid = true;
+    return MG_OK;
+}
+
+// NList(iSimulationStep): accumulate drostep (already on the device in
+// d_drostep) and set the rebuild flag; the caller then runs a conditional build.
+int mg_lists_check(mg_handle *h) {
+    int np = h->np, nb = h->nblk_chk;
+    double *r2 = h->d_blkmax + 2 * nb;
+    k_chk_accum<<<nb, 1024, 0, h->st>>>(h->d_drostep, h->d_drosum, r2, h->d_blkmax, np,
+                                        h->d_rebuild);
+    k_chk_second<<<nb, 1024, 0, h->st>>>(r2, h->d_blkmax, h->d_blkmax + nb, np);
+    k_chk_final<<<1, 32, 0, h->st>>>(h->d_blkmax, h->d_blkmax + nb, nb, h->drnlist, h->d_rebuild);
+    h->launches += 3;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+int mg_mc_cells_set(mg_handle *h) {
+    double3 half = make_double3(h->boxlen2[0], h->boxlen2[1], h->boxlen2[2]);
+    double3 csi = make_double3(h->cellSizei[0], h->cellSizei[1], h->cellSizei[2]);
+    int3 nc = make_int3(h->ncell[0], h->ncell[1], h->ncell[2]);
+    MG_CUDA(h, cudaMemsetAsync(h->d_iphead, 0, sizeof(int) * h->ncelltot, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_npart, 0, sizeof(int) * h->ncelltot, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_ipnext, 0, sizeof(int) * h->np, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_ipprev, 0, sizeof(int) * h->np, h->st));
+    k_mc_cells_set<<<1, 32, 0, h->st>>>(h->d_ro, h->np, half, csi, nc, h->d_iphead, h->d_npart,
+                                        h->d_ipnext, h->d_ipprev, h->d_cellof, h->d_err);
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+int mg_mc_cells_update(mg_handle *h, int ip) {
+    double3 half = make_double3(h->boxlen2[0], h->boxlen2[1], h->boxlen2[2]);
+    double3 csi = make_double3(h->cellSizei[0], h->cellSizei[1], h->cellSizei[2]);
+    int3 nc = make_int3(h->ncell[0], h->ncell[1], h->ncell[2]);
+    k_mc_cells_update<<<1, 32, 0, h->st>>>(h->d_ro, ip, half, csi, nc, h->d_iphead, h->d_npart,
+                                           h->d_ipnext, h->d_ipprev, h->d_cellof, h->d_err);
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+// Export the Verlet list in the reference layout (1-based, column-major
+// jpnlist(maxnneigh, np)).  MD/BD: SetVListMD's ownership rule (pair (i<j)
+// listed under i when i+j is odd, under j when even, 1-based); MC: full list.
+// Neighbours are listed in increasing particle order, as the reference's jp
+// loops produce them.
+int mg_lists_export(mg_handle *h, int32_t *nneighpn, int32_t *jpnlist, int32_t maxnneigh) {
+    if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "no Verlet list has been built");
+    MG_TRY(mg_check_device_error(h));
+    int np = h->np;
+    std::vector<int> nnb(np), perm(np), nbr((size_t)h->maxnb * np);
+    MG_CUDA(h, cudaMemcpy(nnb.data(), h->d_nnb, sizeof(int) * np, cudaMemcpyDeviceToHost));
+    MG_CUDA(h, cudaMemcpy(perm.data(), h->d_perm, sizeof(int) * np, cudaMemcpyDeviceToHost));
+    MG_CUDA(h, cudaMemcpy(nbr.data(), h->d_nbr, sizeof(int) * nbr.size(), cudaMemcpyDeviceToHost));
+    std::vector<std::vector<int>> out(np);
+    for (int i = 0; i < np; ++i) {
+        int ip = perm[i] + 1;
+        for (int k = 0; k < nnb[i]; ++k) {
+            int jp = perm[nbr[(size_t)k * np + i]] + 1;
+            bool keep;
+            if (h->mode == MG_MC) keep = true;
+            else {
+                int odd = (ip + jp) % 2;
+                keep = (ip < jp) ? (odd != 0) : (odd == 0);
+            }
+            if (keep) out[ip - 1].push_back(jp);
+        }
+    }
+    for (int p = 0; p < np; ++p) {
+        std::vector<int> &v = out[p];
+        std::sort(v.begin(), v.end());
+        nneighpn[p] = (int32_t)v.size();
+        if ((int)v.size() > maxnneigh)
+            return mg_fail(h, MG_ERR_NEIGH_OVERFLOW, "particle %d has %d neighbours > %d", p + 1,
+                           (int)v.size(), maxnneigh);
+        for (size_t k = 0; k < v.size(); ++k) jpnlist[(size_t)p * maxnneigh + k] = v[k];
+    }
+    return MG_OK;
+}
+
+int mg_cells_export(mg_handle *h, int32_t *ncell, int32_t *cellip) {
+    if (!h->list_valid && !h->d_iphead) return mg_fail(h, MG_ERR_STATE, "no cell list");
+    MG_TRY(mg_check_device_error(h));
+    for (int m = 0; m < 3; ++m) ncell[m] = h->ncell[m];
+    MG_CUDA(h, cudaMemcpy(cellip, h->d_cellof, sizeof(int) * h->np, cudaMemcpyDeviceToHost));
+    return MG_OK;
+}

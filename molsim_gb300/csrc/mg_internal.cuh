@@ -1,0 +1,240 @@
+// mg_internal.cuh — internal declarations of the GB300 hot-path library.
+//
+// Device data layout (one handle = one system on one GPU):
+//   ro        double[3*np]   positions, reference layout ro(3,np)
+//   perm      int[np]        cell-sorted slot -> particle (0-based)
+//   pos_s     double4[np]    (x,y,z,charge) in slot order, refreshed per call
+//   nbr       int[maxnb*np]  Verlet list in slot space, column-major
+//                            (neighbour k of slot i at nbr[k*np+i])
+//   force     double[3*np]   FP64 accumulator (plain form), reference layout
+//   ffx       long long[3*np] 64-bit fixed-point accumulator (mixed form)
+//   mesh      SPME real mesh Q[z][y][x] and half spectrum F[z][y][kx]
+//   part      double[]       per-block partial sums, reduced in fixed order
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/molsim_gb300.h"
+
+#define MG_MAX_ORDER 12
+#define MG_MAX_NPTPT 10
+#define MG_FX_SCALE 4294967296.0          // 2^32: fixed-point force / mesh scale
+#define MG_FX_INV (1.0 / 4294967296.0)
+
+struct mg_phase {
+    std::string name;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double total_ms = 0;
+    long count = 0;
+    bool pending = false;
+};
+
+struct mg_handle {
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    std::string err;
+
+    // ---- parameters ---------------------------------------------------
+    int np = 0, npt = 0, nptpt = 0, form = 0, mode = 0, txintlist = 0;
+    int ewald = 0, ncut = 0, ncut2 = 0, order = 0, nmesh = 0, lsurf = 0, nbond = 0;
+    int maxnb = 0;
+    double boxlen[3], boxlen2[3], boxleni[3], TwoPiBoxi[3], vol = 0;
+    double rcut = 0, rcut2 = 0, drnlist = 0, rs2cut = 0, ualpha = 0, EpsiFourPi = 0;
+    double force_fac = 0, u_self = 0;
+    std::vector<int> h_type;          // 0-based particle types
+    std::vector<int> h_pairidx;       // [npt*npt] 1-based pair index
+    std::vector<double> h_az;
+
+    // ---- device: system ------------------------------------------------
+    double *d_ro = nullptr, *d_az = nullptr;
+    int *d_type = nullptr, *d_pairidx = nullptr;
+    double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_r2atat = nullptr;
+    float *d_ubuf_f = nullptr;
+    int *d_tab_start = nullptr, *d_tab_n = nullptr;   // per pair: first record (0-based double offset / 12), count
+    int nbuf = 0;
+
+    // ---- cells and Verlet list -----------------------------------------
+    int ncell[3] = {1, 1, 1}, ncelltot = 1;
+    double cellSize[3], cellSizei[3];
+    int *d_cellof = nullptr, *d_cellcount = nullptr, *d_cellstart = nullptr, *d_cellfill = nullptr;
+    int *d_perm = nullptr, *d_slot = nullptr;
+    int *d_nnb = nullptr, *d_nbr = nullptr;
+    double4 *d_pos_s = nullptr;
+    bool list_valid = false;
+    // MC cell list (doubly linked lists, reference layout; 1-based, 0 = none)
+    int *d_iphead = nullptr, *d_npart = nullptr, *d_ipnext = nullptr, *d_ipprev = nullptr;
+    int *d_neighcells = nullptr, nneighcell_max = 0;   // [ncelltot * 27]
+    int *d_nneighcell = nullptr;
+
+    // ---- forces and reductions ----------------------------------------
+    double *d_force = nullptr, *d_forceo = nullptr;
+    long long *d_ffx = nullptr;
+    double *d_part = nullptr;      // partial sums
+    int part_pair = 0, part_rec = 0, part_bond = 0, part_surf = 0;   // offsets
+    int nblk_pair = 0, nblk_rec = 0, nblk_bond = 0, nblk_surf = 0;
+    double *d_uout = nullptr;      // [nptpt+1] u_twob, then u_tot,u_rec,u_bond,virial, then surf sums (3)
+    int *d_err = nullptr;          // [4] code, info1, info2, info3
+    double *h_pinned = nullptr;    // pinned staging for outputs
+    size_t h_pinned_bytes = 0;
+
+    // ---- bonds -----------------------------------------------------------
+    int *d_bond_ij = nullptr, *d_bond_p = nullptr;   // [2*nbond] (0-based), [nbond]
+    double *d_bond_k = nullptr, *d_bond_eq = nullptr;
+    int *d_bond_off = nullptr, *d_bond_list = nullptr;  // CSR per particle: entries b*2 + (0 first, 1 second)
+
+    // ---- standard Ewald ----------------------------------------------------
+    int nkvec = 0;
+    int4 *d_kvec = nullptr;         // (nx, ny, nz, -)
+    double *d_kfac = nullptr;
+    double2 *d_eik = nullptr;       // [3][ncut+1][np]
+    double2 *d_S = nullptr;         // [nkvec][4]
+    double2 *d_Stm = nullptr;
+
+    // ---- SPME ------------------------------------------------------------
+    int nh = 0;                     // nmesh/2 + 1
+    double dkdr[3];
+    void *d_Q = nullptr;            // real mesh (double or float)
+    void *d_F = nullptr;            // half spectrum (double2 or float2)
+    unsigned long long *d_Qfx = nullptr;  // fixed-point spread mesh (mixed form)
+    double *d_mf = nullptr, *d_ew = nullptr, *d_vw = nullptr;   // octant tables [nh^3]
+    float *d_mf_f = nullptr, *d_ew_f = nullptr, *d_vw_f = nullptr;
+    void *d_tw = nullptr;           // twiddles exp(-2 pi i m/n), m < n
+    int fft_tx = 0, fft_tiles = 0;
+    double *d_Qref = nullptr;       // MC: charge mesh of the accepted state (FP64)
+    double *d_phi = nullptr;        // MC: potential mesh of the accepted state
+    double *d_gker = nullptr;       // MC: real-space kernel g (nmesh^3)
+    double urecold = 0;
+
+    // ---- MC trial ------------------------------------------------------------
+    int nptm = 0;
+    int *d_ipnptm = nullptr;
+    double *d_rotm = nullptr, *d_du = nullptr;
+    std::vector<int> h_ipnptm;
+    std::vector<double> h_rotm;
+    bool trial_ok = false;
+    bool have_rec = false;
+    double h_du_tot = 0, h_du_rec = 0;
+
+    // ---- list check ---------------------------------------------------------
+    double *d_drostep = nullptr, *d_drosum = nullptr, *d_blkmax = nullptr;
+    int *d_rebuild = nullptr;       // [2]: current flag, flag of the previous step
+    int nblk_chk = 0;
+
+    // ---- MD / BD ----------------------------------------------------------------
+    double tstep = 0;
+    double *d_massip = nullptr, *d_rod = nullptr, *d_rodd = nullptr;
+    bool md_ready = false, bd_ready = false, have_force = false;
+    double *d_fac1 = nullptr, *d_fac2 = nullptr;
+    int *d_rng = nullptr;            // [4] iseed, flag, ncand_short, -
+    double *d_rng_save = nullptr;    // [1]
+    int ncand = 0;
+    unsigned *d_cflag = nullptr;     // candidate acceptance scan
+    int *d_cidx = nullptr;           // accepted candidate index by rank
+    double *d_cval = nullptr;        // [2*ncand] rx, ry per candidate
+    int *d_scan_tmp = nullptr;
+    int scan_cap = 0;
+
+    // ---- graphs and timing -----------------------------------------------------
+    cudaGraphExec_t g_bd = nullptr, g_md = nullptr;
+    bool timing = false;
+    std::vector<mg_phase> phases;
+    long launches = 0;
+};
+
+// ---- error helpers ----------------------------------------------------------
+int mg_fail(mg_handle *h, int code, const char *fmt, ...);
+#define MG_CUDA(h, call)                                                                   \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return mg_fail((h), MG_ERR_CUDA, "%s failed: %s (%s:%d)", #call,              \
+                           cudaGetErrorString(e_), __FILE__, __LINE__);                    \
+    } while (0)
+#define MG_TRY(x)                  \
+    do {                           \
+        int s_ = (x);              \
+        if (s_ != MG_OK) return s_; \
+    } while (0)
+
+// device error word: first error wins
+__device__ __forceinline__ void mg_dev_error(int *err, int code, int a, int b, int c) {
+    if (atomicCAS(err, 0, code) == 0) {
+        err[1] = a;
+        err[2] = b;
+        err[3] = c;
+    }
+}
+
+// ---- exact FP64 helpers (no FMA contraction where the result decides a
+//      branch: list membership, table interval, cell index) -------------------
+__device__ __forceinline__ double mg_r2_exact(double dx, double dy, double dz) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+// PBCr2 (molaux.F90:159-162) for a box: single conditional image shift
+__device__ __forceinline__ double mg_pbc1(double d, double half, double len) {
+    return (fabs(d) > half) ? __dsub_rn(d, copysign(len, d)) : d;
+}
+
+struct mg_box {
+    double len[3], half[3], inv[3];
+};
+
+// ---- phase timing -------------------------------------------------------------
+int mg_phase_begin(mg_handle *h, const char *name);
+int mg_phase_end(mg_handle *h, const char *name);
+void mg_phase_collect(mg_handle *h);
+
+// ---- module entry points (host side) ----------------------------------------------
+int mg_lists_init(mg_handle *h);
+int mg_lists_build(mg_handle *h, bool conditional);   // cell sort + Verlet list
+int mg_lists_check(mg_handle *h);                      // NList(iSimulationStep) rule on device
+int mg_lists_export(mg_handle *h, int32_t *nneighpn, int32_t *jpnlist, int32_t maxnneigh);
+int mg_cells_export(mg_handle *h, int32_t *ncell, int32_t *cellip);
+int mg_mc_cells_set(mg_handle *h);
+int mg_mc_cells_update(mg_handle *h, int ip);
+
+int mg_forces_init(mg_handle *h);
+int mg_utotal_launch(mg_handle *h);                    // queue a full UTotal on the stream
+int mg_utotal_fetch(mg_handle *h, double *forceo, double *u_twob, double *uout);
+
+int mg_spme_init(mg_handle *h);
+int mg_spme_launch(mg_handle *h);                      // spread, FFT, influence, gather
+int mg_ewald_std_init(mg_handle *h);
+int mg_ewald_std_launch(mg_handle *h);
+
+int mg_mc_init(mg_handle *h);
+int mg_mc_dutotal(mg_handle *h, int nptm, const int32_t *ipnptm, const double *rotm,
+                  double *du_twob, double *du_rec, double *du_tot, int32_t *lhsoverlap);
+int mg_mc_accept(mg_handle *h);
+int mg_mc_after_utotal(mg_handle *h);
+int mg_mc_batch(mg_handle *h, int ntrial, const int32_t *ip, const double *rt, double *du,
+                int32_t *ovl);
+
+int mg_integrate_bd_step_launch(mg_handle *h);
+int mg_integrate_md_step_launch(mg_handle *h);
+int mg_integrate_bd_setup(mg_handle *h, const double *fac1, const double *fac2, int32_t iseed);
+int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, const double *rod,
+                          const double *rodd);
+
+int mg_check_device_error(mg_handle *h);               // sync + read the device error word
+
+// host set-up (host_setup.cu)
+int mg_host_table(const mg_pot_params *pp, double *ubuf, int32_t nbuf_cap, int32_t *nbuf_used,
+                  int32_t *iubuflow, double *r2umin, int32_t *nugrid);
+int mg_host_rcut_to_alpha(double uewaldtol, double rcut, double q2sum, double boxlenshort,
+                          double epsi_four_pi, double *ualpha);
+void mg_host_spme_tables(int n, int order, const double boxlen[3], const double TwoPiBoxi[3],
+                         double vol, double ualpha, std::vector<double> &mf,
+                         std::vector<double> &ew, std::vector<double> &vw);
+void mg_host_kvectors(int ncut, int ncut2, const double TwoPiBoxi[3], double vol, double ualpha,
+                      std::vector<int> &kv, std::vector<double> &kfac);
+int mg_host_bspline(int order, double pos, int *kmax, double *values, double *derivs);
+
+// kernels shared between modules
+void mg_scan_exclusive(mg_handle *h, const int *in, int *out, int n, const int *gate);
+
+template <typename T> struct mg_cplx;
+template <> struct mg_cplx<double> { typedef double2 type; };
+template <> struct mg_cplx<float> { typedef float2 type; };

@@ -1,0 +1,38 @@
+"""TEST INFRASTRUCTURE ONLY: load the CPU oracle through ctypes.
+
+The oracle exports orc_* entry points with the same arguments as the
+library's mg_* entry points, so molsim_gb300.Engine(system, lib=oracle(),
+prefix="orc_") runs the reference's algorithm on the CPU.
+"""
+import ctypes as C
+
+from molsim_gb300 import abi
+
+from .build_oracle import build
+
+_lib = None
+
+
+def oracle():
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(build())
+        abi.declare(lib, "orc_", abi.SIGNATURES)
+        lib.orc_erf2.restype = C.c_double
+        lib.orc_erf2.argtypes = [C.c_double]
+        lib.orc_random.restype = C.c_double
+        lib.orc_random.argtypes = [C.POINTER(C.c_int32)]
+        lib.orc_gau_random.restype = C.c_double
+        lib.orc_gau_random.argtypes = [C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        lib.orc_fft_r2c_3d.restype = C.c_int
+        lib.orc_fft_r2c_3d.argtypes = [C.c_int, abi.PF64, abi.PF64]
+        lib.orc_fft_c2r_3d.restype = C.c_int
+        lib.orc_fft_c2r_3d.argtypes = [C.c_int, abi.PF64, abi.PF64]
+        lib.orc_cardinal_bspline.restype = C.c_int
+        lib.orc_cardinal_bspline.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_int), abi.PF64, abi.PF64]
+        lib.orc_celllist_test.restype = C.c_int
+        lib.orc_celllist_test.argtypes = [C.c_void_p]
+        lib.orc_get_qmesh.restype = C.c_int
+        lib.orc_get_qmesh.argtypes = [C.c_void_p, abi.PF64]
+        _lib = lib
+    return _lib

@@ -1,0 +1,1840 @@
+/*
+ * molsim_oracle.c — TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain-C restatement of MOLSIM's force/energy hot path (reference:
+ * joakimstenhammar/molsim, Fortran 90).  Every routine follows the Fortran
+ * loop order and expression order of the reference routine it names, so that
+ * the GPU library can be compared with it at the 1e-10 level and, for lists,
+ * bit-exactly.  Compiled with -ffp-contract=off (no fused multiply-add), as a
+ * baseline x86-64 gfortran -O2 build of the reference would evaluate it.
+ * Integer powers follow gfortran's -O2 expansion (x**6 = x**3 * x**3).
+ *
+ * Used only by tests/, __graft_entry__.smoke() and bench.py's CPU baseline.
+ * Parity status: unpinned against reference outputs (none ship, and the
+ * Fortran cannot be built here); pinned against known answers in tests.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <complex.h>
+#include "molsim_oracle.h"
+
+#define Zero 0.0
+#define Half 0.5
+#define One 1.0
+#define Two 2.0
+#define Three 3.0
+#define Four 4.0
+static const double Pi = 3.1415926535897932;   /* mol.F90:63 */
+#define TwoPi (Two * Pi)
+#define FourPi (Four * Pi)
+
+typedef struct { double re, im; } zc;   /* complex(8) */
+
+static inline zc zmul(zc a, zc b) { zc r; r.re = a.re * b.re - a.im * b.im; r.im = a.re * b.im + a.im * b.re; return r; }
+static inline zc zconj(zc a) { a.im = -a.im; return a; }
+static inline zc zscale(double s, zc a) { zc r; r.re = s * a.re; r.im = s * a.im; return r; }
+static inline zc zadd(zc a, zc b) { zc r; r.re = a.re + b.re; r.im = a.im + b.im; return r; }
+static inline zc zsub(zc a, zc b) { zc r; r.re = a.re - b.re; r.im = a.im - b.im; return r; }
+
+static inline double pow2(double x) { return x * x; }
+static inline double pow3(double x) { return (x * x) * x; }
+static inline double pow6(double x) { double x3 = (x * x) * x; return x3 * x3; }
+/* gfortran -O2 expands x**n (integer n) with an optimal multiplication chain;
+   the chains for the small n used by UBond are written out here. */
+static double powi(double x, int n) {
+    switch (n) {
+    case 0: return One;
+    case 1: return x;
+    case 2: return x * x;
+    case 3: return (x * x) * x;
+    case 4: { double x2 = x * x; return x2 * x2; }
+    default: { double r = One; for (int i = 0; i < n; ++i) r *= x; return r; }
+    }
+}
+static inline double fsign(double a, double b) { return copysign(fabs(a), b); }   /* Fortran sign(a,b) */
+
+/* ======================================================================
+ * mollib.F90
+ * ====================================================================== */
+
+/* Erf2, mollib.F90:215-274.  The reference's second branch iterates j from
+   ncfd-1 (not ncfc-1) down to 2 after starting from c(ncfc), so c(17) is never
+   used and the last term uses c(1) (the loop index ends at 1); both are kept.
+   At |x| == xup exactly no branch assigns the result in the reference; sign(1,x)
+   is returned there. */
+double orc_erf2(double x) {
+    static const double sqrtpi = 1.7724538509055160;
+    static const double xup = 6.25;
+    static const double c[18] = {
+        1.9449071068178803, 4.20186582324414e-2, -1.86866103976769e-2,
+        5.1281061839107e-3, -1.0683107461726e-3, 1.744737872522e-4,
+        -2.15642065714e-5, 1.7282657974e-6, -2.00479241e-8,
+        -1.64782105e-8, 2.0008475e-9, 2.57716e-11,
+        -3.06343e-11, 1.9158e-12, 3.703e-13,
+        -5.43e-14, -4.0e-15, 1.2e-15};
+    static const double d[17] = {
+        1.4831105640848036, -3.010710733865950e-1, 6.89948306898316e-2,
+        -1.39162712647222e-2, 2.4207995224335e-3, -3.658639685849e-4,
+        4.86209844323e-5, -5.7492565580e-6, 6.113243578e-7,
+        -5.89910153e-8, 5.2070091e-9, -4.232976e-10,
+        3.18811e-11, -2.2361e-12, 1.467e-13,
+        -9.0e-15, 5.0e-16};
+    const int ncfc = 18, ncfd = 17;
+    double xv = fabs(x), bj, bjp1, bjp2, x2;
+    int j;
+    if (xv <= Two) {
+        x2 = x * x - Two;
+        bjp2 = Zero;
+        bjp1 = d[ncfd - 1];
+        for (j = ncfd - 1; j >= 2; --j) {
+            bj = x2 * bjp1 - bjp2 + d[j - 1];
+            bjp2 = bjp1;
+            bjp1 = bj;
+        }
+        bj = x2 * bjp1 - bjp2 + d[0];
+        return Half * (bj - bjp2) * x;
+    } else if (Two < xv && xv < xup) {
+        x2 = Two - 20.0 / (xv + Three);
+        bjp2 = Zero;
+        bjp1 = c[ncfc - 1];
+        for (j = ncfd - 1; j >= 2; --j) {
+            bj = x2 * bjp1 - bjp2 + c[j - 1];
+            bjp2 = bjp1;
+            bjp1 = bj;
+        }
+        /* j == 1 here */
+        bj = x2 * bjp1 - bjp2 + c[j - 1];
+        x2 = Half * (bj - bjp2) / xv * exp(-x * x) / sqrtpi;
+        return (One - x2) * fsign(One, x);
+    }
+    return fsign(One, x);
+}
+
+/* CardinalBSpline, mollib.F90:1629-1685 (values and first derivatives). */
+int orc_cardinal_bspline(int order, double pos, int *kmax, double *values, double *derivs) {
+    double lastvals[64];
+    int v, n, i;
+    double x, a;
+    if (order < 1 || order > 64) return -1;
+    v = (int)floor(pos);
+    x = pos - v;
+    *kmax = v;
+    for (i = 0; i < order; ++i) lastvals[i] = 0.0;
+    values[0] = x;
+    if (order > 1) {
+        values[1] = (1.0 - x);
+        for (n = 3; n <= order; ++n) {
+            for (i = 0; i < order; ++i) lastvals[i] = values[i];
+            values[0] = x * lastvals[0] / (n - 1);
+            for (i = 1; i <= n - 2; ++i) {
+                a = i + x;
+                values[i] = (a * lastvals[i] + (n - a) * lastvals[i - 1]) / (n - 1);
+            }
+            values[n - 1] = (1 - x) * lastvals[n - 2] / (n - 1);
+        }
+        n = order;
+        if (derivs) {
+            derivs[0] = lastvals[0];
+            for (i = 1; i <= n - 2; ++i) derivs[i] = lastvals[i] - lastvals[i - 1];
+            derivs[n - 1] = -lastvals[n - 2];
+        }
+    }
+    return 0;
+}
+
+/* Random, mollib.F90:2689-2709 (Park-Miller with a Marsaglia shift). */
+static double rnd_am;
+static int32_t rnd_ix = -1, rnd_iy = -1;
+double orc_random(int32_t *idum) {
+    const int32_t ia = 16807, im = 2147483647, iq = 127773, ir = 2836;
+    int32_t k;
+    if (*idum <= 0 || rnd_iy < 0) {
+        rnd_am = (double)nextafterf(1.0f, -1.0f) / im;
+        rnd_iy = ((888889999 ^ abs(*idum)) | 1);
+        rnd_ix = 777755555 ^ abs(*idum);
+        *idum = abs(*idum) + 1;
+    }
+    uint32_t ux = (uint32_t)rnd_ix;
+    ux ^= ux << 13;
+    ux ^= ux >> 17;   /* ishft(ix,-17) is a logical shift */
+    ux ^= ux << 5;
+    rnd_ix = (int32_t)ux;
+    k = rnd_iy / iq;
+    rnd_iy = ia * (rnd_iy - k * iq) - ir * k;
+    if (rnd_iy < 0) rnd_iy += im;
+    return rnd_am * (double)((im & (rnd_ix ^ rnd_iy)) | 1);
+}
+
+/* GauRandom, mollib.F90:2739-2766: polar Box-Muller over the 31-bit LCG
+   iseed = ibclr(iseed*16087, 31) (32-bit wrapping product).  The reference
+   keeps flag/save as SAVE variables; they are explicit state here. */
+double orc_gau_random(int32_t *iseed, int32_t *flag, double *save) {
+    const double f = 1.0 / 2147483648.0;   /* 2**(-31) */
+    double rx, ry, r, fac;
+    if (*flag) {
+        for (;;) {
+            *iseed = (int32_t)(((uint32_t)*iseed * 16087u) & 0x7fffffffu);
+            rx = Two * (f * *iseed - Half);
+            *iseed = (int32_t)(((uint32_t)*iseed * 16087u) & 0x7fffffffu);
+            ry = Two * (f * *iseed - Half);
+            r = rx * rx + ry * ry;
+            if (r < One) break;
+        }
+        fac = sqrt(-Two * log(r) / r);
+        *save = ry * fac;
+        *flag = 0;
+        return rx * fac;
+    }
+    *flag = 1;
+    return *save;
+}
+
+/* HeapSortIndex, mollib.F90:1749-1796 (1-based index output). */
+static void heap_sort_index(int n, const double *vec, int *index) {
+    int l, i, j, ir, indext;
+    double vect;
+    for (i = 1; i <= n; ++i) index[i - 1] = i;
+    if (n <= 1) return;
+#define V(k) vec[(k) - 1]
+#define IX(k) index[(k) - 1]
+    l = n / 2 + 1;
+    ir = n;
+    for (;;) {
+        if (l > 1) {
+            l = l - 1;
+            indext = IX(l);
+            vect = V(indext);
+        } else {
+            indext = IX(ir);
+            vect = V(indext);
+            IX(ir) = IX(1);
+            ir = ir - 1;
+            if (ir == 1) { IX(1) = indext; return; }
+        }
+        i = l;
+        j = l + l;
+        while (j <= ir) {
+            if (j < ir) {
+                if (V(IX(j)) < V(IX(j + 1))) j = j + 1;
+            }
+            if (vect < V(IX(j))) {
+                IX(i) = IX(j);
+                i = j;
+                j = j + j;
+            } else {
+                j = ir + 1;
+            }
+        }
+        IX(i) = indext;
+    }
+#undef V
+#undef IX
+}
+
+/* ======================================================================
+ * potential.F90 : table construction
+ * ====================================================================== */
+
+/* CalcEwaldUfac, potential.F90:2938-2966 */
+void orc_calc_ewald_ufac(double r1, double ualpha, double *c0fac, double *c1fac, double *c2fac) {
+    const double fac = 1.12837916709;
+    double ra = ualpha * r1;
+    double er = orc_erf2(ra);
+    double ex = fac * exp(-(ra * ra));
+    *c0fac = One - (er);
+    *c1fac = One - (er - ra * ex);
+    *c2fac = One - (er - ra * (One + ra * ra) * ex);
+}
+
+static inline int iptpt_of(const int32_t *iptpt, int npt, int ipt, int jpt) {   /* 1-based in/out */
+    return iptpt[(jpt - 1) * npt + (ipt - 1)];
+}
+
+/* Pot_1_6_12 'calc', potential.F90:1386-1428 (one atom per particle type). */
+void orc_pot_1_6_12(const mg_pot_params *pp, int iat, int jat, double r1,
+                    double *u0, double *u1, double *u2) {
+    double qq = pp->zat[iat - 1] * pp->zat[jat - 1] * pp->epsi_four_pi;
+    double sig = 0.5 * (pp->sigat[iat - 1] + pp->sigat[jat - 1]);
+    double eps = sqrt(pp->epsat[iat - 1] * pp->epsat[jat - 1]);
+    double r1i = One / r1;
+    double fac = pow6(sig * r1i);
+    double c0fac, c1fac, c2fac;
+    if (pp->lcharge_ewald) orc_calc_ewald_ufac(r1, pp->ualpha, &c0fac, &c1fac, &c2fac);
+    else { c0fac = One; c1fac = One; c2fac = One; }
+    double ushort0 = +Four * eps * (fac * fac - fac);
+    double ushort1 = -(24.0 * eps * (Two * (fac * fac) - fac) * r1i);
+    double ushort2 = +24.0 * eps * (26.0 * (fac * fac) - 7.0 * fac) * (r1i * r1i);
+    if (pp->lljcut) {
+        if (r1 < pp->ljrcut * sig) {
+            ushort0 = ushort0 + pp->ljushift * eps;
+        } else {
+            ushort0 = Zero; ushort1 = Zero; ushort2 = Zero;
+        }
+    }
+    *u0 = qq * c0fac * r1i + ushort0;
+    *u1 = -(qq * c1fac * (r1i * r1i)) + ushort1;
+    *u2 = Two * qq * c2fac * pow3(r1i) + ushort2;
+}
+
+/* SetUBuffer, potential.F90:1139-1221 */
+static void set_ubuffer(double zlow, double u0low, double u1low, double u2low,
+                        double zupp, double u0upp, double u1upp, double u2upp, double *ubuft) {
+    double dz1, dz2, dz3, rlow, rupp, w0low, w1low, w2low, w0upp, w1upp, w2upp, a, b, c;
+    if ((u0low == Zero) && (u0upp == Zero)) {
+        ubuft[0] = zlow;
+        for (int i = 1; i < 12; ++i) ubuft[i] = Zero;
+        return;
+    }
+    rlow = sqrt(zlow);
+    rupp = sqrt(zupp);
+    dz1 = zupp - zlow;
+    dz2 = dz1 * dz1;
+    dz3 = dz2 * dz1;
+    w0low = u0low;
+    w0upp = u0upp;
+    w1low = 0.50 * u1low / rlow;
+    w1upp = 0.50 * u1upp / rupp;
+    w2low = 0.25 * (u2low - u1low / rlow) / zlow;
+    w2upp = 0.25 * (u2upp - u1upp / rupp) / zupp;
+    a = 6.0 * (w0upp - w0low - w1low * dz1 - 0.5 * w2low * dz2) / dz3;
+    b = 2.0 * (w1upp - w1low - w2low * dz1) / dz2;
+    c = (w2upp - w2low) / dz1;
+    ubuft[0] = zlow;
+    ubuft[1] = w0low;
+    ubuft[2] = w1low;
+    ubuft[3] = 0.5 * w2low;
+    ubuft[4] = (10.0 * a - 12.0 * b + 3.0 * c) / (6.0);
+    ubuft[5] = (-15.0 * a + 21.0 * b - 6.0 * c) / (6.0 * dz1);
+    ubuft[6] = (2.0 * a - 3.0 * b + c) / (2.0 * dz2);
+    ubuft[7] = -2.0 * ubuft[2];
+    ubuft[8] = -4.0 * ubuft[3];
+    ubuft[9] = -6.0 * ubuft[4];
+    ubuft[10] = -8.0 * ubuft[5];
+    ubuft[11] = -10.0 * ubuft[6];
+}
+
+/* CheckUBuffer, potential.F90:1224-1263 */
+static void check_ubuffer(const mg_pot_params *pp, int iat, int jat, double rlow, double rupp,
+                          const double *ubuft, int *ok, int *repul) {
+    const int ncheck = 11;
+    double dr, dz, r1, u0, u1, u2, usum, fsum;
+    *ok = 0;
+    *repul = 0;
+    dr = (rupp - rlow) / (ncheck - 1);
+    for (int icheck = 1; icheck <= ncheck; ++icheck) {
+        r1 = rlow + dr * (icheck - 1);
+        orc_pot_1_6_12(pp, iat, jat, r1, &u0, &u1, &u2);
+        dz = r1 * r1 - rlow * rlow;
+        usum = ubuft[1] + dz * (ubuft[2] + dz * (ubuft[3] + dz * (ubuft[4] + dz * (ubuft[5] + dz * ubuft[6]))));
+        fsum = ubuft[7] + dz * (ubuft[8] + dz * (ubuft[9] + dz * (ubuft[10] + dz * ubuft[11])));
+        fsum = r1 * fsum;
+        if (fabs(usum - u0) > pp->utoltab) return;
+        if (fabs(fsum + u1) > pp->ftoltab) return;
+        if (fabs(usum) > pp->umaxtab) *repul = 1;
+        if (fabs(fsum) > pp->fmaxtab) *repul = 1;
+    }
+    *ok = 1;
+}
+
+/* PotTwoBodyTab1/2/3, potential.F90:868-1136, for the (1,6,12) potential of a
+   monoatomic system (atom type == particle type, racom = 0). */
+int orc_pot_twobody_tab(const mg_pot_params *pp, double *ubuf, int32_t nbuf_cap,
+                        int32_t *nbuf_used, int32_t *iubuflow, double *r2umin,
+                        int32_t *nugrid) {
+    const int mnugrid = 1200, ndr = 100;
+    const double drfac = 0.9, rumaxfac = 1.1;
+    int npt = pp->npt, nptpt = npt * (npt + 1) / 2;
+    int cap = 12 * mnugrid * nptpt;
+    double *buf = calloc((size_t)cap, sizeof(double));
+    int *lset = calloc((size_t)nptpt, sizeof(int));
+    int ibuf = 1;
+    int status = 0;
+    if (!buf || !lset) { free(buf); free(lset); return MG_ERR_ALLOC; }
+    for (int ipt = 1; ipt <= npt && !status; ++ipt) {
+        for (int jpt = ipt; jpt <= npt && !status; ++jpt) {
+            int iatjat = iptpt_of(pp->iptpt, npt, ipt, jpt);
+            double r2uminv = pp->r2uminin;                               /* 'init' */
+            double r2umaxv = pow2(rumaxfac * (pp->rcut + 0.0 + 0.0));
+            if (lset[iatjat - 1]) continue;
+            double rumax = sqrt(r2umaxv);
+            double rumin = sqrt(r2uminv);
+            /* PotTwoBodyTab3 */
+            int igrid, idr = 0;
+            double rupp, rlow = 0, zlow, zupp, dr, ubuft[12];
+            double u0low, u1low, u2low, u0upp, u1upp, u2upp;
+            iubuflow[iatjat - 1] = ibuf;
+            rupp = rumax;
+            dr = Half * (rumax - rumin);
+            for (igrid = 1; igrid <= mnugrid; ++igrid) {
+                int ok = 0, repul = 0;
+                zupp = rupp * rupp;
+                for (idr = 1; idr <= ndr; ++idr) {
+                    rlow = rupp - dr;
+                    rlow = (rumin > rlow) ? rumin : rlow;
+                    zlow = rlow * rlow;
+                    orc_pot_1_6_12(pp, ipt, jpt, rlow, &u0low, &u1low, &u2low);
+                    orc_pot_1_6_12(pp, ipt, jpt, rupp, &u0upp, &u1upp, &u2upp);
+                    set_ubuffer(zlow, u0low, u1low, u2low, zupp, u0upp, u1upp, u2upp, ubuft);
+                    check_ubuffer(pp, ipt, jpt, rlow, rupp, ubuft, &ok, &repul);
+                    if (ok) {
+                        rupp = rlow;
+                        if (pp->lljcut) dr = Two * dr;
+                        break;
+                    }
+                    dr = dr * drfac;
+                }
+                if (idr >= ndr + 1) { status = MG_ERR_TABLE; break; }
+                if (ibuf + 11 > cap) { status = MG_ERR_TABLE; break; }
+                memcpy(buf + ibuf - 1, ubuft, sizeof(ubuft));
+                ibuf = ibuf + 12;
+                if (repul) rumin = rlow;
+                if (rlow <= rumin) break;
+                if (repul) break;
+            }
+            if (status) break;
+            if (igrid >= mnugrid + 1) { status = MG_ERR_TABLE; break; }
+            nugrid[iatjat - 1] = igrid;
+            r2umin[iatjat - 1] = rumin * rumin;
+            lset[iatjat - 1] = 1;
+        }
+    }
+    *nbuf_used = ibuf - 1;
+    if (!status) {
+        if (ibuf - 1 > nbuf_cap || !ubuf) status = MG_ERR_TABLE;
+        else memcpy(ubuf, buf, sizeof(double) * (size_t)(ibuf - 1));
+    }
+    free(buf);
+    free(lset);
+    return status;
+}
+
+/* RcutToAlpha, energy.F90:7090-7106 (lq2sum == 0) */
+int orc_rcut_to_alpha(double uewaldtol, double rcut, double q2sum, double boxlenshort,
+                      double epsi_four_pi, double *ualpha) {
+    double y, xold, xnew = 0;
+    int i;
+    y = (uewaldtol / (q2sum * epsi_four_pi)) * sqrt(Two * pow3(boxlenshort * rcut));
+    xold = 1.0e-1;
+    for (i = 1; i <= 40; ++i) {
+        xnew = (One / rcut) * sqrt(-log(y * (xold * xold)));
+        if (fabs(xold - xnew) / xnew < 1.0e-6) break;
+        xold = xnew;
+    }
+    if (i > 40) return MG_ERR_ARG;
+    *ualpha = xnew;
+    return 0;
+}
+
+/* ======================================================================
+ * System state (MolModule / EnergyModule / CellListModule globals)
+ * ====================================================================== */
+
+typedef struct { int npart, nneighcell, iphead; int *neigh; } orc_cell;
+
+struct orc_sys {
+    int np, npt, nptpt;
+    int *iptpn, *iptpt;
+    double *az;
+    int nbuf;
+    double *ubuf, *r2umin, *r2atat;
+    int *iubuflow;
+    double boxlen[3], boxlen2[3], boxleni[3], dpbc[3], TwoPiBoxi[3], vol, boxlenshort;
+    double rcut, rcut2, drnlist;
+    int txintlist, mode, maxnneigh;
+    int ewald, ncut, ncut2, nkvec, order, nmesh, lsurf;
+    double ualpha, ualpha2, EpsiFourPi, force_fac;
+    /* bonds */
+    int nbond;
+    int *bond_ip, *bond_jp, *bond_p;
+    double *bond_k, *bond_eq;
+    /* state */
+    double *ro, *force, *forceo, *u_twob, *utwobnew, *utwobold;
+    double u_tot, u_rec, u_bond, virial;
+    /* vlist */
+    int *nneighpn, *jpnlist;
+    double *drosum;
+    /* cell list */
+    int ncellX, ncellY, ncellZ, maxneighcell;
+    double cellSize[3], cellSizei[3];
+    orc_cell *cell;
+    int *ipnext, *ipprev, *cellip;   /* cellip: 0-based cell id, -1 if none */
+    /* std Ewald */
+    double *kfac;
+    zc *eikx, *eiky, *eikz, *eikyzm, *eikyzp, *eikr, *sumeikr;     /* eik*(na,0:ncut), sumeikr(nkvec,4) */
+    zc *eikxtm, *eikytm, *eikztm, *eikyzmtm, *eikyzptm, *sumeikrtm;
+    /* SPME */
+    int s[3];
+    double dkdr[3];
+    double *meshfac, *energyfac, *virfac;   /* (0:s/2)^3, x fastest */
+    double *Qmesh, *QmeshTM, *FQmesh, *Qspread;
+    double *spline, *deriv;                 /* (0:order-1, 3, na) */
+    int *meshmax;                           /* (3, na) */
+    double *splinetm, *derivtm;
+    int *meshmaxtm;
+    double urecold, urecnew;
+    int have_rec;                           /* a UTotal has set the MC Ewald state */
+    /* MC trial */
+    int nptm;
+    int *ipnptm, *lptm;
+    double *rotm;
+    double du_twob0, du_rec, du_tot;
+    int trial_ok;
+    /* MD */
+    double tstep, *massip, *rod, *rodd, *roddo, *drostep;
+    /* BD */
+    double *fac1, *fac2;
+    int32_t iseed, gflag;
+    double gsave;
+    int bd_have_force;
+};
+
+#define RO(m, ip) s->ro[3 * ((ip) - 1) + (m) - 1]
+#define FORCE(m, ia) s->force[3 * ((ia) - 1) + (m) - 1]
+#define AZ(ia) s->az[(ia) - 1]
+#define IPTPN(ip) s->iptpn[(ip) - 1]
+#define IPTPT(i, j) s->iptpt[((j) - 1) * s->npt + ((i) - 1)]
+#define UBUF(k) s->ubuf[(k) - 1]
+
+static void *xcalloc(size_t n, size_t sz) { return calloc(n ? n : 1, sz); }
+
+/* PBCr2, molaux.F90:149-184 (lbcbox) */
+static inline void pbcr2(const orc_sys *s, double *dx, double *dy, double *dz, double *r2) {
+    if (fabs(*dx) > s->boxlen2[0]) *dx = *dx - fsign(s->dpbc[0], *dx);
+    if (fabs(*dy) > s->boxlen2[1]) *dy = *dy - fsign(s->dpbc[1], *dy);
+    if (fabs(*dz) > s->boxlen2[2]) *dz = *dz - fsign(s->dpbc[2], *dz);
+    *r2 = *dx * *dx + *dy * *dy + *dz * *dz;
+}
+
+/* PBC, molaux.F90:104-146 (lbcbox): ANINT rounds half away from zero */
+static inline void pbc(const orc_sys *s, double *dx, double *dy, double *dz) {
+    if (fabs(*dx) > s->boxlen2[0]) *dx = *dx - s->dpbc[0] * round(*dx * s->boxleni[0]);
+    if (fabs(*dy) > s->boxlen2[1]) *dy = *dy - s->dpbc[1] * round(*dy * s->boxleni[1]);
+    if (fabs(*dz) > s->boxlen2[2]) *dz = *dz - s->dpbc[2] * round(*dz * s->boxleni[2]);
+}
+
+/* ======================================================================
+ * EwaldSetup, energy.F90:6601-7049
+ * ====================================================================== */
+static int ewald_setup(orc_sys *s) {
+    if (s->ewald == MG_EWALD_STD) {
+        int ncut = s->ncut, nk = 0;
+        s->nkvec = (ncut + 1) * (ncut + 1) * (ncut + 1);
+        s->kfac = xcalloc((size_t)s->nkvec, sizeof(double));
+        double fac0 = TwoPi / s->vol;
+        for (int nz = 0; nz <= ncut; ++nz) {
+            double facz = Two;
+            if (nz == 0) facz = One;
+            for (int ny = 0; ny <= ncut; ++ny) {
+                double facy = One;
+                if (ny == 0) facy = Half;
+                for (int nx = 0; nx <= ncut; ++nx) {
+                    if (nx * nx + ny * ny + nz * nz > s->ncut2) continue;
+                    if (nx == 0 && ny == 0 && nz == 0) continue;
+                    nk = nk + 1;
+                    double facx = One;
+                    if (nx == 0) facx = Half;
+                    double k2 = pow2(nx * s->TwoPiBoxi[0]) + pow2(ny * s->TwoPiBoxi[1]) + pow2(nz * s->TwoPiBoxi[2]);
+                    s->kfac[nk - 1] = fac0 * facz * facy * facx * exp(-k2 / (Four * (s->ualpha * s->ualpha))) / k2;
+                }
+            }
+        }
+        s->nkvec = nk;
+        size_t na = (size_t)s->np, nc = (size_t)ncut + 1;
+        s->eikx = xcalloc(na * nc, sizeof(zc)); s->eiky = xcalloc(na * nc, sizeof(zc)); s->eikz = xcalloc(na * nc, sizeof(zc));
+        s->eikyzm = xcalloc(na, sizeof(zc)); s->eikyzp = xcalloc(na, sizeof(zc));
+        s->eikr = xcalloc(na * 4, sizeof(zc));
+        s->sumeikr = xcalloc((size_t)nk * 4, sizeof(zc));
+        s->eikxtm = xcalloc(na * nc, sizeof(zc)); s->eikytm = xcalloc(na * nc, sizeof(zc)); s->eikztm = xcalloc(na * nc, sizeof(zc));
+        s->eikyzmtm = xcalloc(na, sizeof(zc)); s->eikyzptm = xcalloc(na, sizeof(zc));
+        s->sumeikrtm = xcalloc((size_t)nk * 4, sizeof(zc));
+    } else if (s->ewald == MG_EWALD_SPM) {
+        int order = s->order, n = s->nmesh;
+        if (n <= 0 || order <= 0 || n % 2 != 0) return MG_ERR_ARG;
+        s->s[0] = s->s[1] = s->s[2] = n;
+        size_t m3 = (size_t)n * n * n, nh = (size_t)(n / 2 + 1);
+        s->Qmesh = xcalloc(m3, sizeof(double));
+        s->QmeshTM = xcalloc(m3, sizeof(double));
+        s->Qspread = xcalloc(m3, sizeof(double));
+        s->FQmesh = xcalloc(2 * nh * n * n, sizeof(double));
+        s->meshfac = xcalloc(nh * nh * nh, sizeof(double));
+        s->energyfac = xcalloc(nh * nh * nh, sizeof(double));
+        s->virfac = xcalloc(nh * nh * nh, sizeof(double));
+        s->spline = xcalloc((size_t)order * 3 * s->np, sizeof(double));
+        s->deriv = xcalloc((size_t)order * 3 * s->np, sizeof(double));
+        s->meshmax = xcalloc((size_t)3 * s->np, sizeof(int));
+        s->splinetm = xcalloc((size_t)order * 3 * s->np, sizeof(double));
+        s->derivtm = xcalloc((size_t)order * 3 * s->np, sizeof(double));
+        s->meshmaxtm = xcalloc((size_t)3 * s->np, sizeof(int));
+        for (int m = 0; m < 3; ++m) s->dkdr[m] = s->s[m] / s->boxlen[m];
+        /* b(m)**2, eq (4.4) of JCP 1995, 103, 8577.  cmplx(0, x) without a KIND
+           argument is single-precision complex in Fortran, so the phase is
+           rounded to float and its exponential is a float: reproduced as
+           float(angle) and correctly rounded float cos/sin. */
+        double spl[64];
+        int z;
+        double *b2 = xcalloc((size_t)3 * n, sizeof(double));
+        orc_cardinal_bspline(order, Zero, &z, spl, NULL);
+        for (int i = 0; i < 3; ++i) {
+            for (int m = 0; m < s->s[i]; ++m) {
+                if ((order % 2 == 1) && (2 * m == s->s[i])) continue;
+                double are = Zero, aim = Zero;
+                for (int k = 0; k <= order - 2; ++k) {
+                    float th = (float)(TwoPi * m * k / s->s[i]);
+                    float ce = (float)cos((double)th), se = (float)sin((double)th);
+                    /* a = a + spl(k+1)*cmplx(ce,se): real(8) times complex(4) */
+                    are = are + spl[k + 1] * (double)ce;
+                    aim = aim + spl[k + 1] * (double)se;
+                }
+                b2[i * n + m] = One / (are * are + aim * aim);
+            }
+        }
+        double fac0 = FourPi / s->vol;
+        double expf_ = -One / (Four * (s->ualpha * s->ualpha));
+        for (int nz = 0; nz <= n / 2; ++nz)
+            for (int ny = 0; ny <= n / 2; ++ny)
+                for (int nx = 0; nx <= n / 2; ++nx) {
+                    size_t id = ((size_t)nz * nh + ny) * nh + nx;
+                    if (nx == 0 && ny == 0 && nz == 0) {
+                        s->meshfac[id] = Zero; s->energyfac[id] = Zero; s->virfac[id] = Zero;
+                    } else {
+                        double m2 = pow2(nx * s->TwoPiBoxi[0]) + pow2(ny * s->TwoPiBoxi[1]) + pow2(nz * s->TwoPiBoxi[2]);
+                        double c = exp(m2 * expf_) / m2;
+                        double mf = fac0 * c * b2[nx] * b2[n + ny] * b2[2 * n + nz];
+                        s->meshfac[id] = mf;
+                        if (nx == (n - nx) % n) mf = mf / 2;
+                        if (ny == (n - ny) % n) mf = mf / 2;
+                        if (nz == (n - nz) % n) mf = mf / 2;
+                        s->energyfac[id] = mf;
+                        s->virfac[id] = (One + 2 * m2 * expf_) * mf;
+                    }
+                }
+        free(b2);
+    }
+    s->ualpha2 = s->ualpha * s->ualpha;
+    return 0;
+}
+
+int orc_create(const mg_params *p, orc_sys **out) {
+    if (!p || !out || p->abi_version != MG_ABI_VERSION || p->np < 1 || p->npt < 1) return MG_ERR_ARG;
+    orc_sys *s = xcalloc(1, sizeof(orc_sys));
+    int np = p->np;
+    s->np = np; s->npt = p->npt; s->nptpt = p->nptpt;
+    s->iptpn = xcalloc(np, sizeof(int)); memcpy(s->iptpn, p->iptpn, sizeof(int) * np);
+    s->iptpt = xcalloc((size_t)p->npt * p->npt, sizeof(int)); memcpy(s->iptpt, p->iptpt, sizeof(int) * p->npt * p->npt);
+    s->az = xcalloc(np, sizeof(double)); memcpy(s->az, p->az, sizeof(double) * np);
+    s->nbuf = p->nbuf;
+    s->ubuf = xcalloc(p->nbuf, sizeof(double)); memcpy(s->ubuf, p->ubuf, sizeof(double) * p->nbuf);
+    s->iubuflow = xcalloc(p->nptpt, sizeof(int)); memcpy(s->iubuflow, p->iubuflow, sizeof(int) * p->nptpt);
+    s->r2umin = xcalloc(p->nptpt, sizeof(double)); memcpy(s->r2umin, p->r2umin, sizeof(double) * p->nptpt);
+    s->r2atat = xcalloc(p->nptpt, sizeof(double)); memcpy(s->r2atat, p->r2atat, sizeof(double) * p->nptpt);
+    for (int m = 0; m < 3; ++m) {
+        s->boxlen[m] = p->boxlen[m];
+        s->boxlen2[m] = p->boxlen[m] / Two;
+        s->boxleni[m] = One / p->boxlen[m];
+        s->TwoPiBoxi[m] = TwoPi * s->boxleni[m];
+        s->dpbc[m] = p->boxlen[m];
+    }
+    s->vol = p->boxlen[0] * p->boxlen[1] * p->boxlen[2];
+    s->boxlenshort = fmin(fmin(p->boxlen[0], p->boxlen[1]), p->boxlen[2]);
+    s->rcut = p->rcut; s->rcut2 = p->rcut * p->rcut; s->drnlist = p->drnlist;
+    s->txintlist = p->txintlist; s->mode = p->mode;
+    s->maxnneigh = p->maxnneigh > 0 ? p->maxnneigh : np - 1;
+    if (s->maxnneigh < 1) s->maxnneigh = 1;
+    s->ewald = p->ewald; s->ualpha = p->ualpha; s->ncut = p->ncut;
+    s->ncut2 = p->ncutregion_cube ? 3 * p->ncut * p->ncut : p->ncut * p->ncut;
+    s->order = p->order; s->nmesh = p->nmesh; s->lsurf = p->lsurf;
+    s->EpsiFourPi = p->epsi_four_pi; s->force_fac = p->force_fac;
+    s->nbond = p->nbond;
+    if (s->nbond > 0) {
+        s->bond_ip = xcalloc(s->nbond, sizeof(int)); memcpy(s->bond_ip, p->bond_ip, sizeof(int) * s->nbond);
+        s->bond_jp = xcalloc(s->nbond, sizeof(int)); memcpy(s->bond_jp, p->bond_jp, sizeof(int) * s->nbond);
+        s->bond_p = xcalloc(s->nbond, sizeof(int)); memcpy(s->bond_p, p->bond_p, sizeof(int) * s->nbond);
+        s->bond_k = xcalloc(s->nbond, sizeof(double)); memcpy(s->bond_k, p->bond_k, sizeof(double) * s->nbond);
+        s->bond_eq = xcalloc(s->nbond, sizeof(double)); memcpy(s->bond_eq, p->bond_eq, sizeof(double) * s->nbond);
+    }
+    s->ro = xcalloc((size_t)3 * np, sizeof(double));
+    s->force = xcalloc((size_t)3 * np, sizeof(double));
+    s->forceo = xcalloc((size_t)3 * np, sizeof(double));
+    s->u_twob = xcalloc((size_t)s->nptpt + 1, sizeof(double));
+    s->utwobnew = xcalloc((size_t)s->nptpt + 1, sizeof(double));
+    s->utwobold = xcalloc((size_t)s->nptpt + 1, sizeof(double));
+    s->drosum = xcalloc((size_t)3 * np, sizeof(double));
+    s->drostep = xcalloc((size_t)3 * np, sizeof(double));
+    s->ipnptm = xcalloc(np, sizeof(int));
+    s->lptm = xcalloc(np, sizeof(int));
+    s->rotm = xcalloc((size_t)3 * np, sizeof(double));
+    s->cellip = xcalloc(np, sizeof(int));
+    s->ipnext = xcalloc(np, sizeof(int));
+    s->ipprev = xcalloc(np, sizeof(int));
+    s->gflag = 1;
+    int st = ewald_setup(s);
+    if (st) { orc_destroy(s); return st; }
+    *out = s;
+    return 0;
+}
+
+void orc_destroy(orc_sys *s) {
+    if (!s) return;
+    void *ptrs[] = {s->iptpn, s->iptpt, s->az, s->ubuf, s->r2umin, s->r2atat, s->iubuflow,
+                    s->bond_ip, s->bond_jp, s->bond_p, s->bond_k, s->bond_eq,
+                    s->ro, s->force, s->forceo, s->u_twob, s->utwobnew, s->utwobold,
+                    s->nneighpn, s->jpnlist, s->drosum, s->ipnext, s->ipprev, s->cellip,
+                    s->kfac, s->eikx, s->eiky, s->eikz, s->eikyzm, s->eikyzp, s->eikr, s->sumeikr,
+                    s->eikxtm, s->eikytm, s->eikztm, s->eikyzmtm, s->eikyzptm, s->sumeikrtm,
+                    s->meshfac, s->energyfac, s->virfac, s->Qmesh, s->QmeshTM, s->FQmesh, s->Qspread,
+                    s->spline, s->deriv, s->meshmax, s->splinetm, s->derivtm, s->meshmaxtm,
+                    s->ipnptm, s->lptm, s->rotm, s->massip, s->rod, s->rodd, s->roddo, s->drostep,
+                    s->fac1, s->fac2};
+    for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
+    if (s->cell) {
+        int nc = s->ncellX * s->ncellY * s->ncellZ;
+        for (int i = 0; i < nc; ++i) free(s->cell[i].neigh);
+        free(s->cell);
+    }
+    free(s);
+}
+
+int orc_set_positions(orc_sys *s, const double *ro) {
+    memcpy(s->ro, ro, sizeof(double) * 3 * s->np);
+    return 0;
+}
+int orc_get_positions(orc_sys *s, double *ro) {
+    memcpy(ro, s->ro, sizeof(double) * 3 * s->np);
+    return 0;
+}
+
+/* ======================================================================
+ * celllist.F90
+ * ====================================================================== */
+
+static inline int id_cell_pos(const orc_sys *s, int ix, int iy, int iz) {   /* 0-based id */
+    return ix + iy * s->ncellX + iz * (s->ncellX * s->ncellY);
+}
+
+/* InitCellList, celllist.F90:76-265 */
+static int init_cell_list(orc_sys *s, double rcell) {
+    int dirRange[3];
+    if (rcell <= 0.0) return MG_ERR_ARG;
+    int oldX = s->ncellX, oldY = s->ncellY, oldZ = s->ncellZ;
+    double ircell = 1.0 / rcell;
+    int nc[3];
+    for (int m = 0; m < 3; ++m) {
+        nc[m] = (int)floor(s->boxlen[m] * ircell);
+        if (nc[m] < 1) nc[m] = 1;
+        s->cellSize[m] = s->boxlen[m] / nc[m];
+        s->cellSizei[m] = 1.0 / s->cellSize[m];
+    }
+    for (int m = 0; m < 3; ++m) dirRange[m] = (int)ceil(s->rcut * s->cellSizei[m]);
+    for (int m = 0; m < 3; ++m) {
+        if (2 * dirRange[m] + 1 > nc[m]) {
+            nc[m] = 1;
+            dirRange[m] = 0;
+            s->cellSize[m] = s->boxlen[m];
+            s->cellSizei[m] = s->boxleni[m];
+        }
+    }
+    s->ncellX = nc[0]; s->ncellY = nc[1]; s->ncellZ = nc[2];
+    if (oldX == nc[0] && oldY == nc[1] && oldZ == nc[2] && s->cell) return 0;
+    if (s->cell) {
+        int ncold = oldX * oldY * oldZ;
+        for (int i = 0; i < ncold; ++i) free(s->cell[i].neigh);
+        free(s->cell);
+        s->cell = NULL;
+    }
+    int maxdir = (2 * dirRange[0] + 1) * (2 * dirRange[1] + 1) * (2 * dirRange[2] + 1);
+    int *dirs = xcalloc((size_t)3 * maxdir, sizeof(int));
+    int *dsorted = xcalloc((size_t)3 * maxdir, sizeof(int));
+    int *dindex = xcalloc(maxdir, sizeof(int));
+    double *l1 = xcalloc(maxdir, sizeof(double));
+    int idir = 0;
+    for (int ixd = -dirRange[0]; ixd <= dirRange[0]; ++ixd)
+        for (int iyd = -dirRange[1]; iyd <= dirRange[1]; ++iyd)
+            for (int izd = -dirRange[2]; izd <= dirRange[2]; ++izd) {
+                int d3[3] = {ixd, iyd, izd};
+                double dr[3], sum = 0;
+                for (int m = 0; m < 3; ++m) {
+                    int a = abs(d3[m]) - 1;
+                    if (a < 0) a = 0;
+                    dr[m] = a * s->cellSize[m];
+                }
+                sum = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+                if (sum > s->rcut2) continue;
+                dirs[3 * idir] = ixd; dirs[3 * idir + 1] = iyd; dirs[3 * idir + 2] = izd;
+                idir++;
+            }
+    s->maxneighcell = idir;
+    for (int i = 0; i < idir; ++i) l1[i] = (double)(abs(dirs[3 * i]) + abs(dirs[3 * i + 1]) + abs(dirs[3 * i + 2]));
+    heap_sort_index(idir, l1, dindex);
+    for (int i = 0; i < idir; ++i)
+        for (int m = 0; m < 3; ++m) dsorted[3 * i + m] = dirs[3 * (dindex[i] - 1) + m];
+    int ncell = nc[0] * nc[1] * nc[2];
+    s->cell = xcalloc(ncell, sizeof(orc_cell));
+    for (int ix = 0; ix < nc[0]; ++ix)
+        for (int iy = 0; iy < nc[1]; ++iy)
+            for (int iz = 0; iz < nc[2]; ++iz) {
+                orc_cell *c = &s->cell[id_cell_pos(s, ix, iy, iz)];
+                c->neigh = xcalloc(idir, sizeof(int));
+                int ineigh = 0;
+                for (int k = 0; k < idir; ++k) {
+                    int ng[3] = {ix + dsorted[3 * k], iy + dsorted[3 * k + 1], iz + dsorted[3 * k + 2]};
+                    for (int m = 0; m < 3; ++m) {
+                        if ((ng[m] >= nc[m] || ng[m] < 0) && (s->dpbc[m] == s->boxlen[m])) {
+                            ng[m] = ((ng[m] % nc[m]) + nc[m]) % nc[m];   /* Fortran modulo */
+                        }
+                    }
+                    if (ng[0] >= nc[0] || ng[0] < 0 || ng[1] >= nc[1] || ng[1] < 0 || ng[2] >= nc[2] || ng[2] < 0) continue;
+                    c->neigh[ineigh++] = id_cell_pos(s, ng[0], ng[1], ng[2]);
+                }
+                c->nneighcell = ineigh;
+            }
+    free(dirs); free(dsorted); free(dindex); free(l1);
+    return 0;
+}
+
+/* pcellro, celllist.F90:295-305 (0-based id; -1 outside the grid) */
+static int pcellro(const orc_sys *s, const double *r) {
+    int i[3];
+    int nc[3] = {s->ncellX, s->ncellY, s->ncellZ};
+    for (int m = 0; m < 3; ++m) {
+        i[m] = (int)floor((r[m] + s->boxlen2[m]) * s->cellSizei[m]);
+        if (i[m] < 0 || i[m] >= nc[m]) return -1;
+    }
+    return id_cell_pos(s, i[0], i[1], i[2]);
+}
+
+/* AddIpToCell, celllist.F90:307-327 (ip 1-based; ipnext/ipprev 0 = none) */
+static void add_ip_to_cell(orc_sys *s, int ip, int icell) {
+    orc_cell *c = &s->cell[icell];
+    c->npart = c->npart + 1;
+    int jp = c->iphead;
+    c->iphead = ip;
+    if (jp != 0) {
+        s->ipprev[jp - 1] = ip;
+        s->ipnext[ip - 1] = jp;
+    } else {
+        s->ipnext[ip - 1] = 0;
+    }
+    s->ipprev[ip - 1] = 0;
+    s->cellip[ip - 1] = icell;
+}
+
+/* RmIpFromCell, celllist.F90:329-364 */
+static void rm_ip_from_cell(orc_sys *s, int ip, int icell) {
+    orc_cell *c = &s->cell[icell];
+    c->npart = c->npart - 1;
+    int nextp = s->ipnext[ip - 1], prevp = s->ipprev[ip - 1];
+    if (nextp == 0) {
+        if (c->iphead == ip) c->iphead = 0;
+        else s->ipnext[prevp - 1] = 0;
+    } else {
+        if (c->iphead == ip) {
+            c->iphead = nextp;
+            s->ipprev[nextp - 1] = 0;
+        } else {
+            s->ipprev[nextp - 1] = prevp;
+            s->ipnext[prevp - 1] = nextp;
+        }
+    }
+    s->ipprev[ip - 1] = 0;
+    s->ipnext[ip - 1] = 0;
+    s->cellip[ip - 1] = -1;
+}
+
+/* UpdateCellIp, celllist.F90:366-382 */
+static int update_cell_ip(orc_sys *s, int ip) {
+    int cold = s->cellip[ip - 1];
+    int cnew = pcellro(s, &RO(1, ip));
+    if (cnew < 0) return MG_ERR_CELL;
+    if (cold != cnew) {
+        rm_ip_from_cell(s, ip, cold);
+        add_ip_to_cell(s, ip, cnew);
+    }
+    return 0;
+}
+
+/* SetCellList, celllist.F90:384-410 */
+static int set_cell_list(orc_sys *s) {
+    int nc = s->ncellX * s->ncellY * s->ncellZ;
+    for (int i = 0; i < nc; ++i) { s->cell[i].npart = 0; s->cell[i].iphead = 0; }
+    memset(s->ipnext, 0, sizeof(int) * s->np);
+    memset(s->ipprev, 0, sizeof(int) * s->np);
+    for (int ip = 1; ip <= s->np; ++ip) {
+        int c = pcellro(s, &RO(1, ip));
+        if (c < 0) return MG_ERR_CELL;
+        add_ip_to_cell(s, ip, c);
+    }
+    return 0;
+}
+
+/* TestCellList, celllist.F90:447-476: every pair within rcut of a particle
+   must be in one of the neighbour cells of its cell.  Returns the number of
+   missing pairs. */
+int orc_celllist_test(orc_sys *s) {
+    int missing = 0;
+    for (int ip = 1; ip <= s->np; ++ip) {
+        orc_cell *ci = &s->cell[s->cellip[ip - 1]];
+        for (int jp = 1; jp <= s->np; ++jp) {
+            if (jp == ip) continue;
+            double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2;
+            pbcr2(s, &dx, &dy, &dz, &r2);
+            if (r2 >= s->rcut2) continue;
+            int found = 0;
+            for (int k = 0; k < ci->nneighcell && !found; ++k)
+                if (ci->neigh[k] == s->cellip[jp - 1]) found = 1;
+            if (!found) missing++;
+        }
+    }
+    return missing;
+}
+
+/* ======================================================================
+ * nlist.F90
+ * ====================================================================== */
+
+/* SetVListMD, nlist.F90:724-765 (serial: ipmyid = 1..np) */
+static int set_vlist_md(orc_sys *s) {
+    double rs2cut = pow2(s->rcut + s->drnlist);
+    for (int ip = 1; ip <= s->np; ++ip) {
+        int *nn = &s->nneighpn[ip - 1];
+        *nn = 0;
+        for (int jp = 1; jp <= s->np; ++jp) {
+            int itemp = (ip + jp) % 2;
+            if (ip < jp && itemp == 0) continue;
+            if (ip > jp && itemp != 0) continue;
+            if (ip == jp) continue;
+            double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2;
+            pbcr2(s, &dx, &dy, &dz, &r2);
+            if (r2 < rs2cut) {
+                *nn = *nn + 1;
+                if (*nn > s->maxnneigh) return MG_ERR_NEIGH_OVERFLOW;
+                s->jpnlist[(size_t)(ip - 1) * s->maxnneigh + (*nn - 1)] = jp;
+            }
+        }
+    }
+    return 0;
+}
+
+/* SetVListMC, nlist.F90:820-890 (serial branch) */
+static int set_vlist_mc(orc_sys *s) {
+    double rs2cut = pow2(s->rcut + s->drnlist);
+    for (int ip = 1; ip <= s->np; ++ip) s->nneighpn[ip - 1] = 0;
+    for (int ip = 1; ip <= s->np; ++ip) {
+        for (int jp = ip + 1; jp <= s->np; ++jp) {
+            double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2;
+            pbcr2(s, &dx, &dy, &dz, &r2);
+            if (r2 < rs2cut) {
+                int ni = ++s->nneighpn[ip - 1], nj = ++s->nneighpn[jp - 1];
+                if (ni > s->maxnneigh || nj > s->maxnneigh) return MG_ERR_NEIGH_OVERFLOW;
+                s->jpnlist[(size_t)(ip - 1) * s->maxnneigh + (ni - 1)] = jp;
+                s->jpnlist[(size_t)(jp - 1) * s->maxnneigh + (nj - 1)] = ip;
+            }
+        }
+    }
+    return 0;
+}
+
+static int set_vlist(orc_sys *s) {
+    if (!s->nneighpn) {
+        s->nneighpn = xcalloc(s->np, sizeof(int));
+        s->jpnlist = xcalloc((size_t)s->np * s->maxnneigh, sizeof(int));
+    }
+    if (s->mode == MG_MC) return set_vlist_mc(s);
+    return set_vlist_md(s);
+}
+
+/* NList(iWriteInput), nlist.F90:568-589 */
+int orc_nlist_set(orc_sys *s) {
+    int st;
+    if (s->txintlist == MG_VLIST) {
+        st = set_vlist(s);
+    } else {
+        st = init_cell_list(s, s->rcut + s->drnlist);
+        if (!st) st = set_cell_list(s);
+    }
+    memset(s->drosum, 0, sizeof(double) * 3 * s->np);
+    return st;
+}
+
+/* NList(iSimulationStep), nlist.F90:598-621 (inlist == 0).  With the cell
+   list the reference relies on UpdateCellIp after MC moves and never
+   refreshes cells in MD/BD; here the cell list is refreshed on the same
+   displacement rule in MD/BD (the reference's cells would be stale). */
+int orc_nlist_update(orc_sys *s, const double *drostep, int32_t *rebuilt) {
+    double r2, r2max1 = Zero, r2max2 = Zero;
+    const double *d = drostep ? drostep : s->drostep;
+    *rebuilt = 0;
+    if (s->txintlist == MG_CELLLIST && s->mode == MG_MC) return 0;
+    for (int ip = 1; ip <= s->np; ++ip) {
+        double *ds = &s->drosum[3 * (ip - 1)];
+        ds[0] = ds[0] + d[3 * (ip - 1)];
+        ds[1] = ds[1] + d[3 * (ip - 1) + 1];
+        ds[2] = ds[2] + d[3 * (ip - 1) + 2];
+        r2 = ds[0] * ds[0] + ds[1] * ds[1] + ds[2] * ds[2];
+        if (r2 > r2max1) r2max1 = r2;
+        else if (r2 > r2max2) r2max2 = r2;
+    }
+    if (sqrt(r2max1) + sqrt(r2max2) > s->drnlist) {
+        memset(s->drosum, 0, sizeof(double) * 3 * s->np);
+        *rebuilt = 1;
+        if (s->txintlist == MG_VLIST) return set_vlist(s);
+        return set_cell_list(s);
+    }
+    return 0;
+}
+
+int orc_nlist_get(orc_sys *s, int32_t *nneighpn, int32_t *jpnlist, int32_t maxnneigh) {
+    if (!s->nneighpn) return MG_ERR_STATE;
+    for (int ip = 0; ip < s->np; ++ip) {
+        int n = s->nneighpn[ip];
+        nneighpn[ip] = n;
+        if (n > maxnneigh) return MG_ERR_NEIGH_OVERFLOW;
+        for (int k = 0; k < n; ++k) jpnlist[(size_t)ip * maxnneigh + k] = s->jpnlist[(size_t)ip * s->maxnneigh + k];
+    }
+    return 0;
+}
+
+int orc_celllist_get(orc_sys *s, int32_t *ncell, int32_t *cellip) {
+    if (!s->cell) return MG_ERR_STATE;
+    ncell[0] = s->ncellX; ncell[1] = s->ncellY; ncell[2] = s->ncellZ;
+    for (int ip = 0; ip < s->np; ++ip) cellip[ip] = s->cellip[ip];
+    return 0;
+}
+
+/* ======================================================================
+ * energy.F90 : two-body
+ * ====================================================================== */
+
+/* table lookup shared by the pair routines: energy.F90:481-490 */
+static inline int table_eval(const orc_sys *s, int iptjpt, double r2, double *usum, double *fsum) {
+    int ibuf = s->iubuflow[iptjpt - 1];
+    for (;;) {
+        if (r2 >= UBUF(ibuf)) break;
+        ibuf = ibuf + 12;
+        if (ibuf > s->nbuf) return MG_ERR_IBUF;
+    }
+    double d = r2 - UBUF(ibuf);
+    *usum = UBUF(ibuf + 1) + d * (UBUF(ibuf + 2) + d * (UBUF(ibuf + 3) + d * (UBUF(ibuf + 4) + d * (UBUF(ibuf + 5) + d * UBUF(ibuf + 6)))));
+    if (fsum) *fsum = UBUF(ibuf + 7) + d * (UBUF(ibuf + 8) + d * (UBUF(ibuf + 9) + d * (UBUF(ibuf + 10) + d * UBUF(ibuf + 11))));
+    return 0;
+}
+
+/* UTwoBodyA, energy.F90:445-544 (Verlet list) */
+static int utwobody_a(orc_sys *s) {
+    double virtwob = Zero, fsum = Zero, usum;
+    for (int k = 0; k <= s->nptpt; ++k) s->u_twob[k] = Zero;
+    for (int ip = 1; ip <= s->np; ++ip) {
+        int ipt = IPTPN(ip);
+        for (int jploc = 1; jploc <= s->nneighpn[ip - 1]; ++jploc) {
+            int jp = s->jpnlist[(size_t)(ip - 1) * s->maxnneigh + jploc - 1];
+            if (s->mode == MG_MC && jp < ip) continue;
+            int jpt = IPTPN(jp);
+            int iptjpt = IPTPT(ipt, jpt);
+            double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2;
+            pbcr2(s, &dx, &dy, &dz, &r2);
+            if (r2 > s->rcut2) continue;
+            if (r2 < s->r2atat[iptjpt - 1]) {
+                usum = 1e10;   /* fsum keeps its previous value, as in the reference */
+            } else if (r2 < s->r2umin[iptjpt - 1]) {
+                return MG_ERR_TABLE_UNDERRUN;
+            } else {
+                int st = table_eval(s, iptjpt, r2, &usum, &fsum);
+                if (st) return st;
+            }
+            s->u_twob[iptjpt] = s->u_twob[iptjpt] + usum;
+            FORCE(1, ip) = FORCE(1, ip) + (fsum * dx);
+            FORCE(2, ip) = FORCE(2, ip) + (fsum * dy);
+            FORCE(3, ip) = FORCE(3, ip) + (fsum * dz);
+            FORCE(1, jp) = FORCE(1, jp) - (fsum * dx);
+            FORCE(2, jp) = FORCE(2, jp) - (fsum * dy);
+            FORCE(3, jp) = FORCE(3, jp) - (fsum * dz);
+            virtwob = virtwob - (fsum * r2);
+        }
+    }
+    double t = Zero;
+    for (int k = 1; k <= s->nptpt; ++k) t = t + s->u_twob[k];
+    s->u_twob[0] = t;
+    s->u_tot = s->u_tot + s->u_twob[0];
+    s->virial = s->virial + virtwob;
+    return 0;
+}
+
+/* UTwoBodyACellList, energy.F90:669-777 */
+static int utwobody_a_celllist(orc_sys *s) {
+    double virtwob = Zero, usum, fsum;
+    for (int k = 0; k <= s->nptpt; ++k) s->u_twob[k] = Zero;
+    for (int ip = 1; ip <= s->np; ++ip) {
+        int ipt = IPTPN(ip);
+        orc_cell *ic = &s->cell[s->cellip[ip - 1]];
+        for (int incell = 0; incell < ic->nneighcell; ++incell) {
+            orc_cell *nc = &s->cell[ic->neigh[incell]];
+            int jp = nc->iphead;
+            for (int jploc = 1; jploc <= nc->npart; ++jploc) {
+                if (jp > ip) {
+                    int jpt = IPTPN(jp);
+                    int iptjpt = IPTPT(ipt, jpt);
+                    double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2;
+                    pbcr2(s, &dx, &dy, &dz, &r2);
+                    if (r2 < s->rcut2) {
+                        if (r2 < s->r2atat[iptjpt - 1]) {
+                            usum = 1e10;
+                            fsum = 1e10;
+                        } else if (r2 < s->r2umin[iptjpt - 1]) {
+                            return MG_ERR_TABLE_UNDERRUN;
+                        } else {
+                            int st = table_eval(s, iptjpt, r2, &usum, &fsum);
+                            if (st) return st;
+                        }
+                        s->u_twob[iptjpt] = s->u_twob[iptjpt] + usum;
+                        FORCE(1, ip) = FORCE(1, ip) + (fsum * dx);
+                        FORCE(2, ip) = FORCE(2, ip) + (fsum * dy);
+                        FORCE(3, ip) = FORCE(3, ip) + (fsum * dz);
+                        FORCE(1, jp) = FORCE(1, jp) - (fsum * dx);
+                        FORCE(2, jp) = FORCE(2, jp) - (fsum * dy);
+                        FORCE(3, jp) = FORCE(3, jp) - (fsum * dz);
+                        virtwob = virtwob - (fsum * r2);
+                    }
+                }
+                jp = s->ipnext[jp - 1];
+            }
+        }
+    }
+    double t = Zero;
+    for (int k = 1; k <= s->nptpt; ++k) t = t + s->u_twob[k];
+    s->u_twob[0] = t;
+    s->u_tot = s->u_tot + s->u_twob[0];
+    s->virial = s->virial + virtwob;
+    return 0;
+}
+
+/* ======================================================================
+ * energy.F90 : Ewald
+ * ====================================================================== */
+
+#define EIK(a, ia, n) (a)[(size_t)(n) * s->np + ((ia) - 1)]
+
+/* EwaldSetArray, energy.F90:1401-1425 */
+static void ewald_set_array(orc_sys *s, int ialow, int iaupp) {
+    for (int ia = ialow; ia <= iaupp; ++ia) {
+        zc one = {One, Zero};
+        EIK(s->eikx, ia, 0) = one; EIK(s->eiky, ia, 0) = one; EIK(s->eikz, ia, 0) = one;
+        double ax = s->TwoPiBoxi[0] * RO(1, ia), ay = s->TwoPiBoxi[1] * RO(2, ia), az = s->TwoPiBoxi[2] * RO(3, ia);
+        zc ex = {cos(ax), sin(ax)}, ey = {cos(ay), sin(ay)}, ez = {cos(az), sin(az)};
+        if (s->ncut >= 1) { EIK(s->eikx, ia, 1) = ex; EIK(s->eiky, ia, 1) = ey; EIK(s->eikz, ia, 1) = ez; }
+    }
+    for (int icut = 2; icut <= s->ncut; ++icut)
+        for (int ia = ialow; ia <= iaupp; ++ia) {
+            EIK(s->eikx, ia, icut) = zmul(EIK(s->eikx, ia, icut - 1), EIK(s->eikx, ia, 1));
+            EIK(s->eiky, ia, icut) = zmul(EIK(s->eiky, ia, icut - 1), EIK(s->eiky, ia, 1));
+            EIK(s->eikz, ia, icut) = zmul(EIK(s->eikz, ia, icut - 1), EIK(s->eikz, ia, 1));
+        }
+}
+
+/* UEwaldRecStd, energy.F90:964-1102 (serial branch, :1046-1096) */
+static void uewald_rec_std(orc_sys *s, double *virrec) {
+    int na = s->np, kn = 0;
+    ewald_set_array(s, 1, na);
+    for (int i = 0; i < s->nkvec * 4; ++i) { s->sumeikr[i].re = Zero; s->sumeikr[i].im = Zero; }
+    for (int nz = 0; nz <= s->ncut; ++nz) {
+        for (int ny = 0; ny <= s->ncut; ++ny) {
+            if (ny * ny + nz * nz > s->ncut2) continue;
+            for (int ia = 1; ia <= na; ++ia) {
+                s->eikyzm[ia - 1] = zmul(zconj(EIK(s->eiky, ia, ny)), EIK(s->eikz, ia, nz));
+                s->eikyzp[ia - 1] = zmul(EIK(s->eiky, ia, ny), EIK(s->eikz, ia, nz));
+            }
+            for (int nx = 0; nx <= s->ncut; ++nx) {
+                if (nx * nx + ny * ny + nz * nz > s->ncut2) continue;
+                if (nx == 0 && ny == 0 && nz == 0) continue;
+                kn = kn + 1;
+                zc *S = &s->sumeikr[(size_t)(kn - 1) * 4];
+                for (int ia = 1; ia <= na; ++ia) {
+                    zc ex = EIK(s->eikx, ia, nx);
+                    zc *er = &s->eikr[(size_t)(ia - 1) * 4];
+                    er[0] = zmul(zscale(AZ(ia), zconj(ex)), s->eikyzm[ia - 1]);
+                    er[1] = zmul(zscale(AZ(ia), zconj(ex)), s->eikyzp[ia - 1]);
+                    er[2] = zmul(zscale(AZ(ia), ex), s->eikyzm[ia - 1]);
+                    er[3] = zmul(zscale(AZ(ia), ex), s->eikyzp[ia - 1]);
+                    for (int c = 0; c < 4; ++c) S[c] = zadd(S[c], er[c]);
+                }
+                double term = Zero;
+                for (int c = 0; c < 4; ++c) term = term + (S[c].re * S[c].re + S[c].im * S[c].im);
+                term = s->kfac[kn - 1] * term;
+                s->u_rec = s->u_rec + term;
+                double kfac2 = s->EpsiFourPi * Two * s->kfac[kn - 1];
+                double kx = kfac2 * nx * s->TwoPiBoxi[0];
+                double ky = kfac2 * ny * s->TwoPiBoxi[1];
+                double kz = kfac2 * nz * s->TwoPiBoxi[2];
+                for (int ia = 1; ia <= na; ++ia) {
+                    zc *er = &s->eikr[(size_t)(ia - 1) * 4];
+                    double facmm = -er[0].re * S[0].im + er[0].im * S[0].re;
+                    double facmp = -er[1].re * S[1].im + er[1].im * S[1].re;
+                    double facpm = -er[2].re * S[2].im + er[2].im * S[2].re;
+                    double facpp = -er[3].re * S[3].im + er[3].im * S[3].re;
+                    FORCE(1, ia) = FORCE(1, ia) + kx * (-facmm - facmp + facpm + facpp);
+                    FORCE(2, ia) = FORCE(2, ia) + ky * (-facmm + facmp - facpm + facpp);
+                    FORCE(3, ia) = FORCE(3, ia) + kz * (+facmm + facmp + facpm + facpp);
+                }
+                double k2 = pow2(nx * s->TwoPiBoxi[0]) + pow2(ny * s->TwoPiBoxi[1]) + pow2(nz * s->TwoPiBoxi[2]);
+                *virrec = *virrec - (One - k2 / (Two * s->ualpha2)) * term;
+            }
+        }
+    }
+}
+
+/* SPMFFTRec, energy.F90:6525-6587 */
+static int spm_fft_rec(orc_sys *s, int lsave, double *uloc, double *virloc) {
+    int n = s->nmesh, nh = n / 2 + 1;
+    zc *F = (zc *)s->FQmesh;
+    if (orc_fft_r2c_3d(n, s->Qmesh, s->FQmesh)) return MG_ERR_ALLOC;
+    if (lsave) memcpy(s->QmeshTM, s->Qmesh, sizeof(double) * (size_t)n * n * n);
+    *uloc = Zero;
+#define FQ(x, y, z) F[((size_t)(z) * n + (y)) * nh + (x)]
+    for (int nz = 0; nz <= n / 2; ++nz) {
+        int nza = (n - nz) % n;
+        for (int ny = 0; ny <= n / 2; ++ny) {
+            int nya = (n - ny) % n;
+            for (int nx = 0; nx <= n / 2; ++nx) {
+                size_t id = ((size_t)nz * nh + ny) * nh + nx;
+                zc v1 = FQ(nx, ny, nz), v2 = FQ(nx, ny, nza), v3 = FQ(nx, nya, nz), v4 = FQ(nx, nya, nza);
+                double Qsum = v1.re * v1.re + v1.im * v1.im
+                            + v2.re * v2.re + v2.im * v2.im
+                            + v3.re * v3.re + v3.im * v3.im
+                            + v4.re * v4.re + v4.im * v4.im;
+                *uloc = *uloc + Qsum * s->energyfac[id];
+                *virloc = *virloc - Qsum * s->virfac[id];
+                double mf = s->meshfac[id];
+                FQ(nx, ny, nz) = zscale(mf, v1);
+                FQ(nx, ny, nza) = zscale(mf, v2);
+                FQ(nx, nya, nz) = zscale(mf, v3);
+                FQ(nx, nya, nza) = zscale(mf, v4);
+            }
+        }
+    }
+#undef FQ
+    if (orc_fft_c2r_3d(n, s->FQmesh, s->Qmesh)) return MG_ERR_ALLOC;
+    return 0;
+}
+
+#define SPL(arr, i, m, ia) (arr)[((size_t)((ia) - 1) * 3 + (m) - 1) * s->order + (i)]
+#define MESHMAX(arr, m, ia) (arr)[(size_t)((ia) - 1) * 3 + (m) - 1]
+#define QM(arr, x, y, z) (arr)[((size_t)(z) * s->s[1] + (y)) * s->s[0] + (x)]
+
+/* UEwaldRecSPM, energy.F90:1207-1297 */
+static int uewald_rec_spm(orc_sys *s, double *virrec) {
+    int order = s->order, *S3 = s->s;
+    memset(s->Qmesh, 0, sizeof(double) * (size_t)S3[0] * S3[1] * S3[2]);
+    for (int ia = 1; ia <= s->np; ++ia) {
+        for (int m = 1; m <= 3; ++m) {
+            int kmax;
+            orc_cardinal_bspline(order, s->dkdr[m - 1] * RO(m, ia), &kmax, &SPL(s->spline, 0, m, ia), &SPL(s->deriv, 0, m, ia));
+            MESHMAX(s->meshmax, m, ia) = (kmax + S3[m - 1]) % S3[m - 1];
+        }
+        for (int iz = 0; iz <= order - 1; ++iz) {
+            int nz = (S3[2] + MESHMAX(s->meshmax, 3, ia) - iz) % S3[2];
+            double qz = AZ(ia) * SPL(s->spline, iz, 3, ia);
+            for (int iy = 0; iy <= order - 1; ++iy) {
+                int ny = (S3[1] + MESHMAX(s->meshmax, 2, ia) - iy) % S3[1];
+                double qyz = qz * SPL(s->spline, iy, 2, ia);
+                for (int ix = 0; ix <= order - 1; ++ix) {
+                    int nx = (S3[0] + MESHMAX(s->meshmax, 1, ia) - ix) % S3[0];
+                    double q = qyz * SPL(s->spline, ix, 1, ia);
+                    QM(s->Qmesh, nx, ny, nz) = QM(s->Qmesh, nx, ny, nz) + q;
+                }
+            }
+        }
+    }
+    memcpy(s->Qspread, s->Qmesh, sizeof(double) * (size_t)S3[0] * S3[1] * S3[2]);
+    double urec;
+    int st = spm_fft_rec(s, s->mode == MG_MC, &urec, virrec);
+    if (st) return st;
+    s->u_rec = urec;
+    for (int ia = 1; ia <= s->np; ++ia) {
+        double esum[3] = {Zero, Zero, Zero};
+        for (int iz = 0; iz <= order - 1; ++iz) {
+            int nz = (S3[2] + MESHMAX(s->meshmax, 3, ia) - iz) % S3[2];
+            double splz = SPL(s->spline, iz, 3, ia), dsdz = SPL(s->deriv, iz, 3, ia);
+            for (int iy = 0; iy <= order - 1; ++iy) {
+                int ny = (S3[1] + MESHMAX(s->meshmax, 2, ia) - iy) % S3[1];
+                double sply = SPL(s->spline, iy, 2, ia), dsdy = SPL(s->deriv, iy, 2, ia);
+                for (int ix = 0; ix <= order - 1; ++ix) {
+                    int nx = (S3[0] + MESHMAX(s->meshmax, 1, ia) - ix) % S3[0];
+                    double splx = SPL(s->spline, ix, 1, ia), dsdx = SPL(s->deriv, ix, 1, ia);
+                    double Qval = QM(s->Qmesh, nx, ny, nz);
+                    esum[0] = esum[0] + dsdx * sply * splz * Qval;
+                    esum[1] = esum[1] + splx * dsdy * splz * Qval;
+                    esum[2] = esum[2] + splx * sply * dsdz * Qval;
+                }
+            }
+        }
+        for (int m = 1; m <= 3; ++m)
+            FORCE(m, ia) = FORCE(m, ia) - AZ(ia) * esum[m - 1] * s->dkdr[m - 1] * s->EpsiFourPi;
+    }
+    if (s->mode == MG_MC) {
+        memcpy(s->Qmesh, s->QmeshTM, sizeof(double) * (size_t)S3[0] * S3[1] * S3[2]);
+        s->urecold = s->u_rec;
+    }
+    return 0;
+}
+
+/* UEwaldSelf, energy.F90:1301-1345 (atomic contribution; monoatomic) */
+static void uewald_self(orc_sys *s) {
+    double fac = s->ualpha / sqrt(Pi), t = Zero;
+    for (int ia = 1; ia <= s->np; ++ia) t = t + AZ(ia) * AZ(ia);
+    s->u_rec = s->u_rec - fac * t;
+}
+
+/* UEwaldSurf, energy.F90:1349-1371 (3d-periodic) */
+static void uewald_surf(orc_sys *s, double *virrec) {
+    double fac = TwoPi / (Three * s->vol);
+    double sx = Zero, sy = Zero, sz = Zero;
+    for (int ia = 1; ia <= s->np; ++ia) sx = sx + AZ(ia) * RO(1, ia);
+    for (int ia = 1; ia <= s->np; ++ia) sy = sy + AZ(ia) * RO(2, ia);
+    for (int ia = 1; ia <= s->np; ++ia) sz = sz + AZ(ia) * RO(3, ia);
+    double term = fac * (sx * sx + sy * sy + sz * sz);
+    s->u_rec = s->u_rec + term;
+    for (int ia = 1; ia <= s->np; ++ia) {
+        FORCE(1, ia) = FORCE(1, ia) - s->EpsiFourPi * (Two * fac) * AZ(ia) * sx;
+        FORCE(2, ia) = FORCE(2, ia) - s->EpsiFourPi * (Two * fac) * AZ(ia) * sy;
+        FORCE(3, ia) = FORCE(3, ia) - s->EpsiFourPi * (Two * fac) * AZ(ia) * sz;
+    }
+    *virrec = *virrec - term;
+}
+
+/* UEwald, energy.F90:905-960 */
+static int uewald(orc_sys *s) {
+    double virrec = Zero;
+    s->u_rec = Zero;
+    if (s->ewald == MG_EWALD_STD) uewald_rec_std(s, &virrec);
+    else {
+        int st = uewald_rec_spm(s, &virrec);
+        if (st) return st;
+    }
+    uewald_self(s);
+    if (s->lsurf) uewald_surf(s, &virrec);
+    s->u_rec = s->EpsiFourPi * s->u_rec;
+    s->u_tot = s->u_tot + s->u_rec;
+    s->virial = s->virial + s->EpsiFourPi * virrec;
+    s->have_rec = 1;
+    return 0;
+}
+
+/* UBond, energy.F90:5335-5386 (the bonds in chain order) */
+static void ubond(orc_sys *s) {
+    double virbond = Zero;
+    s->u_bond = Zero;
+    for (int b = 0; b < s->nbond; ++b) {
+        int ip = s->bond_ip[b], jp = s->bond_jp[b];
+        double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2;
+        pbcr2(s, &dx, &dy, &dz, &r2);
+        double r1 = sqrt(r2);
+        double term = r1 - s->bond_eq[b];
+        double fac = s->bond_k[b] * powi(term, s->bond_p[b] - 1);
+        s->u_bond = s->u_bond + fac * term;
+        fac = -s->bond_p[b] * fac / r1;
+        FORCE(1, ip) = FORCE(1, ip) + (fac * dx);
+        FORCE(2, ip) = FORCE(2, ip) + (fac * dy);
+        FORCE(3, ip) = FORCE(3, ip) + (fac * dz);
+        FORCE(1, jp) = FORCE(1, jp) - (fac * dx);
+        FORCE(2, jp) = FORCE(2, jp) - (fac * dy);
+        FORCE(3, jp) = FORCE(3, jp) - (fac * dz);
+        virbond = virbond - (fac * r2);
+    }
+    s->u_tot = s->u_tot + s->u_bond;
+    s->virial = s->virial + virbond;
+}
+
+/* UTotal, energy.F90:280-430 (charged monoatomic branch) */
+static int utotal_core(orc_sys *s) {
+    int st = 0;
+    s->u_tot = Zero;
+    for (int k = 0; k <= s->nptpt; ++k) s->u_twob[k] = Zero;
+    memset(s->force, 0, sizeof(double) * 3 * s->np);
+    s->virial = Zero;
+    s->u_bond = Zero;
+    if (s->txintlist == MG_VLIST) {
+        if (!s->nneighpn) return MG_ERR_STATE;
+        st = utwobody_a(s);
+    } else {
+        if (!s->cell) return MG_ERR_STATE;
+        st = utwobody_a_celllist(s);
+    }
+    if (st) return st;
+    if (s->ewald != MG_EWALD_NONE) { st = uewald(s); if (st) return st; }
+    if (s->nbond > 0) ubond(s);
+    double fac = s->force_fac;
+    for (int ia = 1; ia <= s->np; ++ia) {
+        /* monoatomic: r == ro, so the molecular virial term is zero */
+        for (int m = 1; m <= 3; ++m) {
+            FORCE(m, ia) = FORCE(m, ia) * fac;
+            s->forceo[3 * (ia - 1) + m - 1] = Zero + FORCE(m, ia);
+        }
+    }
+    return 0;
+}
+
+static void copy_out(orc_sys *s, double *forceo, double *u_twob, double *uout) {
+    if (forceo) memcpy(forceo, s->forceo, sizeof(double) * 3 * s->np);
+    if (u_twob) memcpy(u_twob, s->u_twob, sizeof(double) * (s->nptpt + 1));
+    if (uout) { uout[0] = s->u_tot; uout[1] = s->u_rec; uout[2] = s->u_bond; uout[3] = s->virial; }
+}
+
+int orc_utotal(orc_sys *s, double *forceo, double *u_twob, double *uout) {
+    int st = utotal_core(s);
+    if (st) return st;
+    copy_out(s, forceo, u_twob, uout);
+    return 0;
+}
+
+int orc_get_qmesh(orc_sys *s, double *q) {
+    if (s->ewald != MG_EWALD_SPM) return MG_ERR_STATE;
+    memcpy(q, s->Qspread, sizeof(double) * (size_t)s->nmesh * s->nmesh * s->nmesh);
+    return 0;
+}
+
+/* ======================================================================
+ * denergy.F90
+ * ====================================================================== */
+
+/* UTwoBodyANew / UTwoBodyAOld (Verlet list), denergy.F90:289-504, and the
+   cell-list versions, denergy.F90:728-935. Returns 1 on overlap. */
+static int utwobody_new(orc_sys *s, int *err) {
+    for (int k = 0; k <= s->nptpt; ++k) s->utwobnew[k] = Zero;
+    for (int iploc = 1; iploc <= s->nptm; ++iploc) {
+        int ip = s->ipnptm[iploc - 1], ipt = IPTPN(ip);
+        const double *rt = &s->rotm[3 * (iploc - 1)];
+        if (s->txintlist == MG_VLIST) {
+            for (int jploc = 1; jploc <= s->nneighpn[ip - 1]; ++jploc) {
+                int jp = s->jpnlist[(size_t)(ip - 1) * s->maxnneigh + jploc - 1];
+                if (s->lptm[jp - 1]) continue;
+                int iptjpt = IPTPT(ipt, IPTPN(jp));
+                double dx = rt[0] - RO(1, jp), dy = rt[1] - RO(2, jp), dz = rt[2] - RO(3, jp), r2, usum;
+                pbcr2(s, &dx, &dy, &dz, &r2);
+                if (r2 > s->rcut2) continue;
+                if (r2 < s->r2atat[iptjpt - 1]) return 1;
+                if (r2 < s->r2umin[iptjpt - 1]) return 1;
+                if ((*err = table_eval(s, iptjpt, r2, &usum, NULL))) return 1;
+                s->utwobnew[iptjpt] = s->utwobnew[iptjpt] + usum;
+            }
+        } else {
+            int icell = pcellro(s, rt);
+            if (icell < 0) { *err = MG_ERR_CELL; return 1; }
+            orc_cell *ic = &s->cell[icell];
+            for (int incell = 0; incell < ic->nneighcell; ++incell) {
+                orc_cell *nc = &s->cell[ic->neigh[incell]];
+                int jp = nc->iphead;
+                for (int jploc = 1; jploc <= nc->npart; ++jploc) {
+                    if (!s->lptm[jp - 1]) {
+                        int iptjpt = IPTPT(ipt, IPTPN(jp));
+                        double dx = rt[0] - RO(1, jp), dy = rt[1] - RO(2, jp), dz = rt[2] - RO(3, jp), r2, usum;
+                        pbcr2(s, &dx, &dy, &dz, &r2);
+                        if (r2 < s->rcut2) {
+                            if (r2 < s->r2atat[iptjpt - 1]) return 1;
+                            if (r2 < s->r2umin[iptjpt - 1]) return 1;
+                            if ((*err = table_eval(s, iptjpt, r2, &usum, NULL))) return 1;
+                            s->utwobnew[iptjpt] = s->utwobnew[iptjpt] + usum;
+                        }
+                    }
+                    jp = s->ipnext[jp - 1];
+                }
+            }
+        }
+    }
+    /* pairs where both particles move (lptmdutwob) */
+    for (int iploc = 1; iploc <= s->nptm; ++iploc) {
+        int ip = s->ipnptm[iploc - 1], ipt = IPTPN(ip);
+        for (int jploc = iploc + 1; jploc <= s->nptm; ++jploc) {
+            int jp = s->ipnptm[jploc - 1];
+            int iptjpt = IPTPT(ipt, IPTPN(jp));
+            const double *ri = &s->rotm[3 * (iploc - 1)], *rj = &s->rotm[3 * (jploc - 1)];
+            double dx = ri[0] - rj[0], dy = ri[1] - rj[1], dz = ri[2] - rj[2], r2, usum;
+            pbcr2(s, &dx, &dy, &dz, &r2);
+            if (s->txintlist == MG_VLIST ? (r2 > s->rcut2) : !(r2 < s->rcut2)) continue;
+            if (r2 < s->r2atat[iptjpt - 1]) return 1;
+            if (r2 < s->r2umin[iptjpt - 1]) return 1;
+            if ((*err = table_eval(s, iptjpt, r2, &usum, NULL))) return 1;
+            s->utwobnew[iptjpt] = s->utwobnew[iptjpt] + usum;
+        }
+    }
+    double t = Zero;
+    for (int k = 1; k <= s->nptpt; ++k) t = t + s->utwobnew[k];
+    s->utwobnew[0] = t;
+    return 0;
+}
+
+static int utwobody_old(orc_sys *s) {
+    for (int k = 0; k <= s->nptpt; ++k) s->utwobold[k] = Zero;
+    for (int iploc = 1; iploc <= s->nptm; ++iploc) {
+        int ip = s->ipnptm[iploc - 1], ipt = IPTPN(ip);
+        if (s->txintlist == MG_VLIST) {
+            for (int jploc = 1; jploc <= s->nneighpn[ip - 1]; ++jploc) {
+                int jp = s->jpnlist[(size_t)(ip - 1) * s->maxnneigh + jploc - 1];
+                if (s->lptm[jp - 1]) continue;
+                int iptjpt = IPTPT(ipt, IPTPN(jp));
+                double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2, usum;
+                pbcr2(s, &dx, &dy, &dz, &r2);
+                if (r2 > s->rcut2) continue;
+                if (r2 < s->r2umin[iptjpt - 1]) return 1;
+                int st = table_eval(s, iptjpt, r2, &usum, NULL);
+                if (st) return st;
+                s->utwobold[iptjpt] = s->utwobold[iptjpt] + usum;
+            }
+        } else {
+            orc_cell *ic = &s->cell[s->cellip[ip - 1]];
+            for (int incell = 0; incell < ic->nneighcell; ++incell) {
+                orc_cell *nc = &s->cell[ic->neigh[incell]];
+                int jp = nc->iphead;
+                for (int jploc = 1; jploc <= nc->npart; ++jploc) {
+                    if (!s->lptm[jp - 1]) {
+                        int iptjpt = IPTPT(ipt, IPTPN(jp));
+                        double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2, usum;
+                        pbcr2(s, &dx, &dy, &dz, &r2);
+                        if (r2 < s->rcut2) {
+                            int st = table_eval(s, iptjpt, r2, &usum, NULL);
+                            if (st) return st;
+                            s->utwobold[iptjpt] = s->utwobold[iptjpt] + usum;
+                        }
+                    }
+                    jp = s->ipnext[jp - 1];
+                }
+            }
+        }
+    }
+    for (int iploc = 1; iploc <= s->nptm; ++iploc) {
+        int ip = s->ipnptm[iploc - 1], ipt = IPTPN(ip);
+        for (int jploc = iploc + 1; jploc <= s->nptm; ++jploc) {
+            int jp = s->ipnptm[jploc - 1];
+            int iptjpt = IPTPT(ipt, IPTPN(jp));
+            double dx = RO(1, ip) - RO(1, jp), dy = RO(2, ip) - RO(2, jp), dz = RO(3, ip) - RO(3, jp), r2, usum;
+            pbcr2(s, &dx, &dy, &dz, &r2);
+            if (s->txintlist == MG_VLIST ? (r2 > s->rcut2) : !(r2 < s->rcut2)) continue;
+            int st = table_eval(s, iptjpt, r2, &usum, NULL);
+            if (st) return st;
+            s->utwobold[iptjpt] = s->utwobold[iptjpt] + usum;
+        }
+    }
+    double t = Zero;
+    for (int k = 1; k <= s->nptpt; ++k) t = t + s->utwobold[k];
+    s->utwobold[0] = t;
+    return 0;
+}
+
+/* EwaldSetArrayTM, denergy.F90:1708-1737 */
+#define EIKTM(a, ialoc, n) (a)[(size_t)(n) * s->np + ((ialoc) - 1)]
+static void ewald_set_array_tm(orc_sys *s) {
+    for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+        const double *rt = &s->rotm[3 * (ialoc - 1)];
+        zc one = {One, Zero};
+        EIKTM(s->eikxtm, ialoc, 0) = one; EIKTM(s->eikytm, ialoc, 0) = one; EIKTM(s->eikztm, ialoc, 0) = one;
+        double ax = s->TwoPiBoxi[0] * rt[0], ay = s->TwoPiBoxi[1] * rt[1], az = s->TwoPiBoxi[2] * rt[2];
+        zc ex = {cos(ax), sin(ax)}, ey = {cos(ay), sin(ay)}, ez = {cos(az), sin(az)};
+        if (s->ncut >= 1) { EIKTM(s->eikxtm, ialoc, 1) = ex; EIKTM(s->eikytm, ialoc, 1) = ey; EIKTM(s->eikztm, ialoc, 1) = ez; }
+    }
+    for (int icut = 2; icut <= s->ncut; ++icut)
+        for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+            EIKTM(s->eikxtm, ialoc, icut) = zmul(EIKTM(s->eikxtm, ialoc, icut - 1), EIKTM(s->eikxtm, ialoc, 1));
+            EIKTM(s->eikytm, ialoc, icut) = zmul(EIKTM(s->eikytm, ialoc, icut - 1), EIKTM(s->eikytm, ialoc, 1));
+            EIKTM(s->eikztm, ialoc, icut) = zmul(EIKTM(s->eikztm, ialoc, icut - 1), EIKTM(s->eikztm, ialoc, 1));
+        }
+}
+
+/* DUTwoBodyEwaldRecStd, denergy.F90:1275-1337 */
+static void du_ewald_rec_std(orc_sys *s) {
+    int kn = 0;
+    ewald_set_array_tm(s);
+    for (int nz = 0; nz <= s->ncut; ++nz) {
+        for (int ny = 0; ny <= s->ncut; ++ny) {
+            if (ny * ny + nz * nz > s->ncut2) continue;
+            for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+                int ia = s->ipnptm[ialoc - 1];
+                s->eikyzm[ia - 1] = zmul(zconj(EIK(s->eiky, ia, ny)), EIK(s->eikz, ia, nz));
+                s->eikyzp[ia - 1] = zmul(EIK(s->eiky, ia, ny), EIK(s->eikz, ia, nz));
+                s->eikyzmtm[ialoc - 1] = zmul(zconj(EIKTM(s->eikytm, ialoc, ny)), EIKTM(s->eikztm, ialoc, nz));
+                s->eikyzptm[ialoc - 1] = zmul(EIKTM(s->eikytm, ialoc, ny), EIKTM(s->eikztm, ialoc, nz));
+            }
+            for (int nx = 0; nx <= s->ncut; ++nx) {
+                if (nx * nx + ny * ny + nz * nz > s->ncut2) continue;
+                if (nx == 0 && ny == 0 && nz == 0) continue;
+                kn = kn + 1;
+                zc *St = &s->sumeikrtm[(size_t)(kn - 1) * 4], *S = &s->sumeikr[(size_t)(kn - 1) * 4];
+                for (int c = 0; c < 4; ++c) St[c] = S[c];
+                for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+                    int ia = s->ipnptm[ialoc - 1];
+                    zc ext = EIKTM(s->eikxtm, ialoc, nx), ex = EIK(s->eikx, ia, nx);
+                    double q = AZ(ia);
+                    St[0] = zadd(St[0], zscale(q, zsub(zmul(zconj(ext), s->eikyzmtm[ialoc - 1]), zmul(zconj(ex), s->eikyzm[ia - 1]))));
+                    St[1] = zadd(St[1], zscale(q, zsub(zmul(zconj(ext), s->eikyzptm[ialoc - 1]), zmul(zconj(ex), s->eikyzp[ia - 1]))));
+                    St[2] = zadd(St[2], zscale(q, zsub(zmul(ext, s->eikyzmtm[ialoc - 1]), zmul(ex, s->eikyzm[ia - 1]))));
+                    St[3] = zadd(St[3], zscale(q, zsub(zmul(ext, s->eikyzptm[ialoc - 1]), zmul(ex, s->eikyzp[ia - 1]))));
+                }
+                double termnew = St[0].re * St[0].re + St[0].im * St[0].im + St[1].re * St[1].re + St[1].im * St[1].im
+                               + St[2].re * St[2].re + St[2].im * St[2].im + St[3].re * St[3].re + St[3].im * St[3].im;
+                double termold = S[0].re * S[0].re + S[0].im * S[0].im + S[1].re * S[1].re + S[1].im * S[1].im
+                               + S[2].re * S[2].re + S[2].im * S[2].im + S[3].re * S[3].re + S[3].im * S[3].im;
+                double term = s->kfac[kn - 1] * (termnew - termold);
+                s->du_rec = s->du_rec + term;
+            }
+        }
+    }
+}
+
+/* DUTwoBodyEwaldRecSPM, denergy.F90:1413-1495 */
+static int du_ewald_rec_spm(orc_sys *s) {
+    int order = s->order, *S3 = s->s, n = s->nmesh, nh = n / 2 + 1;
+    s->urecnew = Zero;
+    memcpy(s->QmeshTM, s->Qmesh, sizeof(double) * (size_t)n * n * n);
+    for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+        int ia = s->ipnptm[ialoc - 1];
+        const double *rt = &s->rotm[3 * (ialoc - 1)];
+        for (int m = 1; m <= 3; ++m) {
+            int kmax;
+            orc_cardinal_bspline(order, s->dkdr[m - 1] * rt[m - 1], &kmax, &SPL(s->splinetm, 0, m, ialoc), &SPL(s->derivtm, 0, m, ialoc));
+            MESHMAX(s->meshmaxtm, m, ialoc) = (kmax + S3[m - 1]) % S3[m - 1];
+        }
+        for (int iz = 0; iz <= order - 1; ++iz) {
+            int nz = (S3[2] + MESHMAX(s->meshmax, 3, ia) - iz) % S3[2];
+            double qz = AZ(ia) * SPL(s->spline, iz, 3, ia);
+            int nztm = (S3[2] + MESHMAX(s->meshmaxtm, 3, ialoc) - iz) % S3[2];
+            double qztm = AZ(ia) * SPL(s->splinetm, iz, 3, ialoc);
+            for (int iy = 0; iy <= order - 1; ++iy) {
+                int ny = (S3[1] + MESHMAX(s->meshmax, 2, ia) - iy) % S3[1];
+                double qyz = qz * SPL(s->spline, iy, 2, ia);
+                int nytm = (S3[1] + MESHMAX(s->meshmaxtm, 2, ialoc) - iy) % S3[1];
+                double qyztm = qztm * SPL(s->splinetm, iy, 2, ialoc);
+                for (int ix = 0; ix <= order - 1; ++ix) {
+                    int nx = (S3[0] + MESHMAX(s->meshmax, 1, ia) - ix) % S3[0];
+                    double q = qyz * SPL(s->spline, ix, 1, ia);
+                    int nxtm = (S3[0] + MESHMAX(s->meshmaxtm, 1, ialoc) - ix) % S3[0];
+                    double qtm = qyztm * SPL(s->splinetm, ix, 1, ialoc);
+                    QM(s->QmeshTM, nx, ny, nz) = QM(s->QmeshTM, nx, ny, nz) - q;
+                    QM(s->QmeshTM, nxtm, nytm, nztm) = QM(s->QmeshTM, nxtm, nytm, nztm) + qtm;
+                }
+            }
+        }
+    }
+    if (orc_fft_r2c_3d(n, s->QmeshTM, s->FQmesh)) return MG_ERR_ALLOC;
+    zc *F = (zc *)s->FQmesh;
+#define FQ(x, y, z) F[((size_t)(z) * n + (y)) * nh + (x)]
+    for (int nz = 0; nz <= n / 2; ++nz) {
+        int nza = (n - nz) % n;
+        for (int ny = 0; ny <= n / 2; ++ny) {
+            int nya = (n - ny) % n;
+            for (int nx = 0; nx <= n / 2; ++nx) {
+                zc v[4] = {FQ(nx, ny, nz), FQ(nx, ny, nza), FQ(nx, nya, nz), FQ(nx, nya, nza)};
+                double Qsum = Zero;
+                for (int c = 0; c < 4; ++c) Qsum = Qsum + (v[c].re * v[c].re + v[c].im * v[c].im);
+                s->urecnew = s->urecnew + Qsum * s->energyfac[((size_t)nz * nh + ny) * nh + nx];
+            }
+        }
+    }
+#undef FQ
+    s->du_rec = s->urecnew - s->urecold;
+    return 0;
+}
+
+/* DUTwoBodyEwaldSurf, denergy.F90:1504-1548 */
+static void du_ewald_surf(orc_sys *s) {
+    double fac = TwoPi / (Three * s->vol);
+    double sx = Zero, sy = Zero, sz = Zero;
+    for (int ia = 1; ia <= s->np; ++ia) sx = sx + AZ(ia) * RO(1, ia);
+    for (int ia = 1; ia <= s->np; ++ia) sy = sy + AZ(ia) * RO(2, ia);
+    for (int ia = 1; ia <= s->np; ++ia) sz = sz + AZ(ia) * RO(3, ia);
+    double sxt = sx, syt = sy, szt = sz;
+    for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+        int ia = s->ipnptm[ialoc - 1];
+        const double *rt = &s->rotm[3 * (ialoc - 1)];
+        sxt = sxt + AZ(ia) * (rt[0] - RO(1, ia));
+        syt = syt + AZ(ia) * (rt[1] - RO(2, ia));
+        szt = szt + AZ(ia) * (rt[2] - RO(3, ia));
+    }
+    double term = fac * ((sxt * sxt + syt * syt + szt * szt) - (sx * sx + sy * sy + sz * sz));
+    s->du_rec = s->du_rec + term;
+}
+
+/* DUTotal, denergy.F90:98-215 with DUTwoBody (:246-286) and DUTwoBodyEwald
+   (:1240-1270), charged monoatomic branch. */
+int orc_dutotal(orc_sys *s, int32_t nptm, const int32_t *ipnptm, const double *rotm,
+                double *du_twob, double *du_rec, double *du_tot, int32_t *lhsoverlap) {
+    if (nptm < 1 || nptm > s->np) return MG_ERR_ARG;
+    if (s->txintlist == MG_VLIST && !s->nneighpn) return MG_ERR_STATE;
+    if (s->txintlist == MG_CELLLIST && !s->cell) return MG_ERR_STATE;
+    if (s->ewald != MG_EWALD_NONE && !s->have_rec) return MG_ERR_STATE;
+    for (int i = 0; i < s->nptm; ++i) s->lptm[s->ipnptm[i] - 1] = 0;
+    s->nptm = nptm;
+    for (int i = 0; i < nptm; ++i) {
+        s->ipnptm[i] = ipnptm[i];
+        s->lptm[ipnptm[i] - 1] = 1;
+        for (int m = 0; m < 3; ++m) s->rotm[3 * i + m] = rotm[3 * i + m];
+    }
+    s->du_tot = Zero;
+    s->du_rec = Zero;
+    double du_tw[64];
+    int ntw = s->nptpt + 1;
+    for (int k = 0; k < ntw && k < 64; ++k) du_tw[k] = Zero;
+    int err = 0;
+    int overlap = utwobody_new(s, &err);
+    if (err) return err;
+    s->trial_ok = 0;
+    if (!overlap) {
+        for (int k = 0; k < ntw; ++k) du_tw[k] = du_tw[k] + s->utwobnew[k];
+        int st = utwobody_old(s);
+        if (st < 0) return st;
+        if (st == 1) return MG_ERR_TABLE_UNDERRUN;
+        for (int k = 0; k < ntw; ++k) du_tw[k] = du_tw[k] - s->utwobold[k];
+        s->du_tot = s->du_tot + du_tw[0];
+        if (s->ewald != MG_EWALD_NONE) {
+            if (s->ewald == MG_EWALD_STD) du_ewald_rec_std(s);
+            else { st = du_ewald_rec_spm(s); if (st) return st; }
+            if (s->lsurf) du_ewald_surf(s);
+            s->du_rec = s->EpsiFourPi * s->du_rec;
+            s->du_tot = s->du_tot + s->du_rec;
+        }
+        s->trial_ok = 1;
+    }
+    if (du_twob) for (int k = 0; k < ntw; ++k) du_twob[k] = overlap ? Zero : du_tw[k];
+    if (du_rec) *du_rec = s->du_rec;
+    if (du_tot) *du_tot = s->du_tot;
+    if (lhsoverlap) *lhsoverlap = overlap;
+    return 0;
+}
+
+/* MCUpdate, mc.F90:5203-5235: ro = rotm, EwaldUpdateArray
+   (denergy.F90:1776-1820), UpdateCellIp. */
+int orc_accept(orc_sys *s) {
+    if (!s->trial_ok) return MG_ERR_STATE;
+    if (s->ewald == MG_EWALD_STD) {
+        for (int icut = 0; icut <= s->ncut; ++icut)
+            for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+                int ia = s->ipnptm[ialoc - 1];
+                EIK(s->eikx, ia, icut) = EIKTM(s->eikxtm, ialoc, icut);
+                EIK(s->eiky, ia, icut) = EIKTM(s->eikytm, ialoc, icut);
+                EIK(s->eikz, ia, icut) = EIKTM(s->eikztm, ialoc, icut);
+            }
+        memcpy(s->sumeikr, s->sumeikrtm, sizeof(zc) * 4 * (size_t)s->nkvec);
+    } else if (s->ewald == MG_EWALD_SPM) {
+        memcpy(s->Qmesh, s->QmeshTM, sizeof(double) * (size_t)s->nmesh * s->nmesh * s->nmesh);
+        s->urecold = s->urecnew;
+        for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+            int ia = s->ipnptm[ialoc - 1];
+            for (int m = 1; m <= 3; ++m) {
+                for (int i = 0; i < s->order; ++i) {
+                    SPL(s->spline, i, m, ia) = SPL(s->splinetm, i, m, ialoc);
+                    SPL(s->deriv, i, m, ia) = SPL(s->derivtm, i, m, ialoc);
+                }
+                MESHMAX(s->meshmax, m, ia) = MESHMAX(s->meshmaxtm, m, ialoc);
+            }
+        }
+    }
+    for (int ialoc = 1; ialoc <= s->nptm; ++ialoc) {
+        int ip = s->ipnptm[ialoc - 1];
+        for (int m = 1; m <= 3; ++m) RO(m, ip) = s->rotm[3 * (ialoc - 1) + m - 1];
+        if (s->txintlist == MG_CELLLIST) {
+            int st = update_cell_ip(s, ip);
+            if (st) return st;
+        }
+    }
+    s->u_tot = s->u_tot + s->du_tot;
+    s->trial_ok = 0;
+    return 0;
+}
+
+/* ======================================================================
+ * md.F90 / bd.F90
+ * ====================================================================== */
+
+int orc_md_setup(orc_sys *s, double tstep, const double *massip, const double *rod, const double *rodd) {
+    size_t n3 = (size_t)3 * s->np;
+    if (!s->massip) {
+        s->massip = xcalloc(s->np, sizeof(double));
+        s->rod = xcalloc(n3, sizeof(double));
+        s->rodd = xcalloc(n3, sizeof(double));
+        s->roddo = xcalloc(n3, sizeof(double));
+    }
+    s->tstep = tstep;
+    memcpy(s->massip, massip, sizeof(double) * s->np);
+    memcpy(s->rod, rod, sizeof(double) * n3);
+    memcpy(s->rodd, rodd, sizeof(double) * n3);
+    return 0;
+}
+
+/* VelVer, md.F90:252-420, with GetLinAcc (md.F90:601-625) and the list check
+   of NListDriver(iSimulationStep) after the step. */
+int orc_md_run(orc_sys *s, int32_t nstep, double *forceo, double *uout, double *rod, double *rodd) {
+    if (!s->massip) return MG_ERR_STATE;
+    double tstep = s->tstep;
+    for (int step = 0; step < nstep; ++step) {
+        double fac = Half * tstep * tstep;
+        for (int ip = 1; ip <= s->np; ++ip) {
+            double *d = &s->drostep[3 * (ip - 1)];
+            double *v = &s->rod[3 * (ip - 1)], *a = &s->rodd[3 * (ip - 1)];
+            d[0] = tstep * v[0] + fac * a[0];
+            d[1] = tstep * v[1] + fac * a[1];
+            d[2] = tstep * v[2] + fac * a[2];
+            RO(1, ip) = RO(1, ip) + d[0];
+            RO(2, ip) = RO(2, ip) + d[1];
+            RO(3, ip) = RO(3, ip) + d[2];
+            pbc(s, &RO(1, ip), &RO(2, ip), &RO(3, ip));
+        }
+        int st = utotal_core(s);
+        if (st) return st;
+        for (int i = 0; i < 3 * s->np; ++i) s->roddo[i] = s->rodd[i];
+        for (int ip = 1; ip <= s->np; ++ip)
+            for (int m = 0; m < 3; ++m)
+                s->rodd[3 * (ip - 1) + m] = s->massip[ip - 1] * s->forceo[3 * (ip - 1) + m];
+        for (int i = 0; i < 3 * s->np; ++i) s->rod[i] = s->rod[i] + Half * tstep * (s->rodd[i] + s->roddo[i]);
+        int32_t rebuilt;
+        st = orc_nlist_update(s, s->drostep, &rebuilt);
+        if (st) return st;
+    }
+    copy_out(s, forceo, NULL, uout);
+    if (rod) memcpy(rod, s->rod, sizeof(double) * 3 * s->np);
+    if (rodd) memcpy(rodd, s->rodd, sizeof(double) * 3 * s->np);
+    return 0;
+}
+
+int orc_bd_setup(orc_sys *s, const double *fac1, const double *fac2, int32_t iseed) {
+    if (!s->fac1) { s->fac1 = xcalloc(s->npt, sizeof(double)); s->fac2 = xcalloc(s->npt, sizeof(double)); }
+    memcpy(s->fac1, fac1, sizeof(double) * s->npt);
+    memcpy(s->fac2, fac2, sizeof(double) * s->npt);
+    s->iseed = iseed;
+    s->gflag = 1;
+    s->gsave = 0;
+    s->bd_have_force = 0;
+    return 0;
+}
+
+/* BDDriver(iSimulationStep), bd.F90:53-59: BDStep (bd.F90:120-155) then
+   UTotal, then the list check. */
+int orc_bd_run(orc_sys *s, int32_t nstep, double *forceo, double *uout) {
+    if (!s->fac1) return MG_ERR_STATE;
+    if (!s->bd_have_force) {
+        int st = utotal_core(s);
+        if (st) return st;
+        s->bd_have_force = 1;
+    }
+    for (int step = 0; step < nstep; ++step) {
+        for (int ip = 1; ip <= s->np; ++ip) {
+            int ipt = IPTPN(ip);
+            double *d = &s->drostep[3 * (ip - 1)];
+            const double *f = &s->forceo[3 * (ip - 1)];
+            for (int m = 0; m < 3; ++m)
+                d[m] = s->fac1[ipt - 1] * f[m] + s->fac2[ipt - 1] * orc_gau_random(&s->iseed, &s->gflag, &s->gsave);
+            RO(1, ip) = RO(1, ip) + d[0];
+            RO(2, ip) = RO(2, ip) + d[1];
+            RO(3, ip) = RO(3, ip) + d[2];
+            pbc(s, &RO(1, ip), &RO(2, ip), &RO(3, ip));
+        }
+        int st = utotal_core(s);
+        if (st) return st;
+        int32_t rebuilt;
+        st = orc_nlist_update(s, s->drostep, &rebuilt);
+        if (st) return st;
+    }
+    copy_out(s, forceo, NULL, uout);
+    return 0;
+}
+
+int orc_bd_get_seed(orc_sys *s, int32_t *iseed) {
+    *iseed = s->iseed;
+    return 0;
+}

@@ -1,0 +1,62 @@
+"""Shared helpers for parity tests: systems, comparisons, tolerances."""
+import numpy as np
+
+from molsim_gb300 import Engine, abi, configs
+
+# Tolerances.  Plain FP64 form against the oracle: energies and virial within
+# 1e-10 relative; forces within 1e-10 of the largest force magnitude (a
+# per-component relative test is meaningless for components near zero).
+# Mixed form: force RMS error <= 1e-5 of the RMS force.
+TOL_FP64 = 1e-10
+TOL_MIXED_RMS = 1e-5
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def force_err(f, fref):
+    d = np.asarray(f) - np.asarray(fref)
+    return np.abs(d).max() / np.abs(fref).max()
+
+
+def force_rms_err(f, fref):
+    d = np.asarray(f) - np.asarray(fref)
+    return np.sqrt((d * d).sum() / (np.asarray(fref) ** 2).sum())
+
+
+def prepared(system, orc):
+    """System with its table built by the oracle (the library's own table
+    builder is checked against this one separately)."""
+    system.build_table(orc.orc_pot_twobody_tab)
+    return system
+
+
+def run_pair(system, orc, form=abi.MG_FP64):
+    """UTotal from the oracle and from the GPU for the same system."""
+    ref = Engine(system, lib=orc, prefix="orc_")
+    ref.SetPositions(system.ro_flat())
+    ref.NList("write")
+    r = ref.UTotal()
+    gpu = Engine(system, form=form)
+    gpu.SetPositions(system.ro_flat())
+    gpu.NList("write")
+    g = gpu.UTotal()
+    return r, g, ref, gpu
+
+
+def small_cases():
+    """(name, factory) for the UTotal parity matrix."""
+    return [
+        ("spme_vlist_md", lambda: configs.small_system(seed=11)),
+        ("spme_cell_md", lambda: configs.small_system(seed=12, txintlist=abi.MG_CELLLIST)),
+        ("spme_surf", lambda: configs.small_system(seed=13, lsurf=1)),
+        ("spme_bonds", lambda: configs.small_system(seed=14, chains=4, nseg=12)),
+        ("spme_order4_n32", lambda: configs.small_system(seed=15, nmesh=32, order=4, n=600, L=50.0)),
+        ("std_vlist", lambda: configs.small_system(seed=16, ewald=abi.MG_EWALD_STD, ncut=6)),
+        ("std_cell_surf", lambda: configs.small_system(seed=17, ewald=abi.MG_EWALD_STD, ncut=5,
+                                                       txintlist=abi.MG_CELLLIST, lsurf=1)),
+        ("no_ewald", lambda: configs.small_system(seed=18, ewald=abi.MG_EWALD_NONE)),
+        ("wca_lljcut", lambda: configs.small_system(seed=19, lljcut=1)),
+        ("mc_mode", lambda: configs.small_system(seed=20, mode=abi.MG_MC)),
+    ]
