@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair(PairArgs a) {
             if (r2 < a.r2atat[pair - 1]) {
                 // hard-core overlap: u = 1e10 (the cell-list routine also sets
                 // fsum = 1e10; the Verlet-list routine keeps a stale value)
-                acc[pair] += 0.5 * 1e10;
+                acc[pair - 1] += 0.5 * 1e10;
                 if (MIXED) {
                     gx += 1e10f * (float)dx; gy += 1e10f * (float)dy; gz += 1e10f * (float)dz;
                 } else {
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair(PairArgs a) {
                 gx += fs * (float)dx;
                 gy += fs * (float)dy;
                 gz += fs * (float)dz;
-                acc[pair] += 0.5 * (double)us;
+                acc[pair - 1] += 0.5 * (double)us;
                 acc[a.nptpt] -= 0.5 * (double)(fs * r2f);
             } else {
                 int rec = table_interval(a.ubuf, st, n, r2);
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair(PairArgs a) {
                 fx += fsum * dx;
                 fy += fsum * dy;
                 fz += fsum * dz;
-                acc[pair] += 0.5 * us;
+                acc[pair - 1] += 0.5 * us;
                 acc[a.nptpt] -= 0.5 * (fsum * r2);
             }
         }

@@ -457,7 +457,7 @@ int mg_lists_build(mg_handle *h, bool conditional) {
     k_cell_sort<<<(h->ncelltot + tb - 1) / tb, tb, 0, h->st>>>(h->ncelltot, h->d_cellstart,
                                                                h->d_perm, gate);
     k_slot_of<<<gb, tb, 0, h->st>>>(h->d_perm, np, h->d_slot, gate);
-    k_vlist<<<gb, 128, 0, h->st>>>(h->d_ro, h->d_perm, h->d_cellof, h->d_cellstart, np,
+    k_vlist<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_ro, h->d_perm, h->d_cellof, h->d_cellstart, np,
                                    make_stencil(h), make_box(h), h->rs2cut, h->maxnb, h->d_nnb,
                                    h->d_nbr, h->d_err, gate);
     h->launches += 6;

@@ -60,3 +60,18 @@ def small_cases():
         ("wca_lljcut", lambda: configs.small_system(seed=19, lljcut=1)),
         ("mc_mode", lambda: configs.small_system(seed=20, mode=abi.MG_MC)),
     ]
+
+
+def utotal_errors(g, r, nptpt):
+    """Relative errors of every UTotal output (energies against their own
+    magnitude, forces against the largest force)."""
+    e = {}
+    for k in range(nptpt + 1):
+        e[f"u_twob[{k}]"] = abs(g["u_twob"][k] - r["u_twob"][k]) / max(abs(r["u_twob"][k]), 1e-12)
+    e["u_rec"] = abs(g["u_rec"] - r["u_rec"]) / max(abs(r["u_rec"]), 1.0)
+    e["u_bond"] = abs(g["u_bond"] - r["u_bond"]) / max(abs(r["u_bond"]), 1e-12)
+    e["u_tot"] = rel(g["u_tot"], r["u_tot"])
+    e["virial"] = rel(g["virial"], r["virial"])
+    e["force_max"] = force_err(g["forceo"], r["forceo"])
+    e["force_rms"] = force_rms_err(g["forceo"], r["forceo"])
+    return e
