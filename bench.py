@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""bench.py — throughput of the GB300 force/energy hot path.
+
+Workload: the polyelectrolyte solution (64 chains x 200 beads, 12800
+counterions, 20000 salt pairs; N = 65600 ions, L = 700 A, SPME order 6 on a
+128^3 mesh, r_c = 12 A, Verlet skin 2 A), overdamped BD (BDStep + UTotal +
+list check per step, dt = 0.01 ps).  A step is one BD step of the whole
+system.  Inputs are seeded synthetic configurations (no dataset exists).
+
+Timing: W untimed warm-up steps, then K device steps; before every step an
+untimed write of 512 MiB evicts the L2 cache (the system fits in L2, so it is
+flushed rather than outgrown); CUDA events on the library's stream bracket
+each step; the per-step times are summed.  `value` is the mixed form
+(FP32 arithmetic, 64-bit fixed-point accumulation); the plain FP64 form is
+reported beside it.  `e2e` runs the same steps through the C ABI with host
+buffers (positions in, positions and forces out every step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With --impl reference the CPU oracle (the C restatement of the reference's
+Fortran, one thread, as the reference's serial build) runs BD steps of the
+same workload; each step is timed on the host.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MD steps/s @65k-ion SPME: mixed vs FP64 GPU at force RMS≤1e-5; host-CPU ref"
+FLUSH_BYTES = 512 << 20
+BD_DT = 0.01
+BD_SEED = 1234567
+WORKLOAD = "polyelectrolyte N=65600 (64x200 beads, 12800 counterions, 20000 salt pairs) L=700A SPME p=6 128^3 r_c=12A BD"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def make_system(seed):
+    from molsim_gb300 import configs
+    t = time.time()
+    s = configs.polyelectrolyte(seed=seed)
+    log(f"[bench] workload generated in {time.time() - t:.1f}s (N={s.np_})")
+    return s
+
+
+# ---- algorithmic bytes per launch (mixed form), see the design doc -----------------
+def algorithmic_bytes(kernel, n, k, pairs, nbond):
+    nh = k // 2 + 1
+    k3, spec = k ** 3, nh * k * k
+    return {
+        "prepare": n * (24 + 4 + 4 + 32),
+        "pair": n * 32 + pairs * 4 + n * 4 + n * 24,
+        "spread": n * 32 + k3 * 8,
+        "mesh_convert": k3 * 8 + k3 * 4,
+        "fft_x_r2c": k3 * 4 + spec * 8,
+        "fft_y_fwd": 2 * spec * 8,
+        "fft_z_conv": 2 * spec * 8 + 3 * nh ** 3 * 4,
+        "fft_y_inv": 2 * spec * 8,
+        "fft_x_c2r": spec * 8 + k3 * 4,
+        "gather": k3 * 4 + n * 32 + 2 * n * 24,
+        "bond+reduce": nbond * 2 * 24 + n * 24 * 2,
+        "bd_move": n * (24 + 24 + 24 + 4),
+        "list": n * (24 + 24 + 8),
+    }.get(kernel)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+        return False
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def traffic_from_profiles(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/*.md lines 'traffic_bytes_per_launch <kernel>: <bytes>')."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for f in sorted(os.listdir(d)):
+        if not f.endswith(".md"):
+            continue
+        for line in open(os.path.join(d, f)):
+            if line.startswith("traffic_bytes_per_launch ") and line.split()[1].rstrip(":") == kernel:
+                try:
+                    return float(line.split(":")[1].split()[0])
+                except (IndexError, ValueError):
+                    return None
+    return None
+
+
+def cpu_baseline(seed, budget_s=20.0, max_steps=12):
+    """The oracle (one thread) on BD steps of the same workload; cell-list
+    mode so that set-up is O(N) (the Verlet-list build is O(N^2))."""
+    from molsim_gb300 import Engine, abi
+    from oracle.loader import oracle
+    orc = oracle()
+    s = make_system(seed)
+    s.txintlist = abi.MG_CELLLIST
+    s.build_table(orc.orc_pot_twobody_tab)
+    e = Engine(s, lib=orc, prefix="orc_")
+    e.SetPositions(s.ro_flat())
+    e.NList("write")
+    e.BDSetup(BD_DT, BD_SEED)
+    e.BDRun(0)  # initial forces, untimed
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_steps and time.perf_counter() - t_all < budget_s:
+        t0 = time.perf_counter()
+        e.BDRun(1)
+        times.append(time.perf_counter() - t0)
+    e.close()
+    return times
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    times = cpu_baseline(args.seed, budget_s=min(60.0, 2.0 * max(args.steps, 1)), max_steps=max(args.steps, 1))
+    v = len(times) / sum(times)
+    sample = f"{len(times)} BD steps of the full N=65600 workload (oracle, cell-list mode), host wall clock per step"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": len(times), "warmup": 1, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "form": "reference CPU FP64 (oracle port, 1 thread)"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import molsim_gb300
+    from molsim_gb300 import Engine, abi
+
+    rank, local_rank, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev_index = torch.cuda.current_device()
+    molsim_gb300.build()
+    s = make_system(args.seed + rank)
+    s.build_table()
+    K, W = args.steps, args.warmup
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def engine(form):
+        e = Engine(s, form=form)
+        e.SetPositions(s.ro_flat())
+        e.NList("write")
+        e.BDSetup(BD_DT, BD_SEED)
+        return e
+
+    # accuracy of the mixed form on this workload (same configuration)
+    e64, emx = engine(abi.MG_FP64), engine(abi.MG_MIXED)
+    r64, rmx = e64.UTotal(), emx.UTotal()
+    d = rmx["forceo"] - r64["forceo"]
+    force_rms = float(np.sqrt((d * d).sum() / (r64["forceo"] ** 2).sum()))
+    energy_rel = abs(rmx["u_tot"] - r64["u_tot"]) / abs(r64["u_tot"])
+
+    results = {}
+    clocks = None
+    for name, e in (("fp64", e64), ("mixed", emx)):
+        e.BenchSteps(1, W, FLUSH_BYTES)
+        barrier()
+        if name == "mixed":
+            with ClockSampler(dev_index) as cs:
+                ms = e.BenchSteps(1, K, FLUSH_BYTES)
+            clocks = cs.summary()
+        else:
+            ms = e.BenchSteps(1, K, FLUSH_BYTES)
+        barrier()
+        ms = max_over_ranks(ms)
+        results[name] = {"ms_per_step": ms / K, "steps_per_s": world * K / (ms * 1e-3)}
+    kernels_per_step = emx.StepKernels(1)
+
+    # per-kernel device times (uncaptured launches, same flush regime)
+    emx.PhaseReset(True)
+    emx.BenchSteps(1, min(50, max(K, 5)), FLUSH_BYTES)
+    phases = emx.PhaseTimes()
+    emx.PhaseReset(False)
+    nn, _ = emx.VList(maxnneigh=256)
+    pairs = int(2 * nn.sum())
+    nbond = 0 if s.bond_ip is None else len(s.bond_ip)
+    dom = max(phases, key=phases.get)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    ab = algorithmic_bytes(dom, s.np_, s.nmesh, pairs, nbond)
+    achieved = ab / (phases[dom] * 1e-3) / 1e9 if ab else None
+    traffic = traffic_from_profiles(dom)
+
+    # end to end through the C ABI with host buffers
+    lib = abi.load_library()
+    n3 = 3 * s.np_
+    ro_h = torch.empty(n3, dtype=torch.float64, pin_memory=True)
+    f_h = torch.empty(n3, dtype=torch.float64, pin_memory=True)
+    u_h = torch.empty(4, dtype=torch.float64, pin_memory=True)
+    ro_h.copy_(torch.from_numpy(emx.GetPositions().reshape(-1)))
+    p_ro = C.cast(ro_h.data_ptr(), abi.PF64)
+    p_f = C.cast(f_h.data_ptr(), abi.PF64)
+    p_u = C.cast(u_h.data_ptr(), abi.PF64)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    ke = max(1, min(K, 500))
+    for _ in range(min(W, 10)):
+        assert lib.mg_bd_step_host(emx.h, p_ro, p_f, p_u) == 0
+    tsum = 0.0
+    barrier()
+    for i in range(ke):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = lib.mg_bd_step_host(emx.h, p_ro, p_f, p_u)
+        tsum += time.perf_counter() - t0
+        if st != 0:
+            raise RuntimeError(f"mg_bd_step_host failed: {st}")
+    tsum = max_over_ranks(tsum)
+    e2e = world * ke / tsum
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        times = cpu_baseline(args.seed)
+        cpu = {"value": len(times) / sum(times), "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": f"{len(times)} BD steps of the full N=65600 workload on one host core "
+                         "(oracle, cell-list mode), wall clock per step"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": results["mixed"]["steps_per_s"], "unit": "steps/s",
+            "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": results["mixed"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
+            "data": "synthetic (seeded polyelectrolyte configuration)",
+            "config": {"workload": WORKLOAD, "form": "mixed (FP32 arithmetic, int64 fixed-point accumulation)",
+                       "l2": "flushed (512 MiB write) before every timed step",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "fp64": results["fp64"],
+            "mixed_over_fp64": results["mixed"]["steps_per_s"] / results["fp64"]["steps_per_s"],
+            "accuracy": {"force_rms_mixed_vs_fp64": force_rms, "energy_rel_mixed_vs_fp64": energy_rel},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "peak_source": peak_src, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "algorithmic_bytes": ab, "kernel_ms": phases[dom]},
+            "phases_ms": phases,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 24 * s.np_,
+                    "d2h_bytes_per_step": 48 * s.np_ + 32},
+            "clocks": clocks,
+            "gpu_launches": kernels_per_step * K,
+        }
+        print(json.dumps(out), flush=True)
+    for e in (e64, emx):
+        e.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

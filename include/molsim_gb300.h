@@ -243,6 +243,18 @@ int mg_phase_times(mg_handle *h, double *ms, int32_t nmax, int32_t *nphase,
                    char *names, size_t names_len);
 int mg_phase_reset(mg_handle *h, int32_t enable);
 
+/* Benchmark helper: nstep device steps of the set-up integrator (kind 0 =
+ * velocity Verlet, 1 = BD).  Before every step a buffer of flush_bytes is
+ * written on the handle's stream (0 = no flush) to evict the L2 cache; CUDA
+ * events on the same stream bracket each step (not the flush).  *ms_sum
+ * receives the summed device time of the steps.  With phase timing enabled
+ * the steps run uncaptured so every kernel can be timed. */
+int mg_bench_steps(mg_handle *h, int32_t kind, int32_t nstep, int64_t flush_bytes,
+                   double *ms_sum);
+/* Number of kernel launches in one captured device step (0 before the first
+ * mg_md_run / mg_bd_run / mg_bench_steps). */
+int mg_step_kernels(mg_handle *h, int32_t kind, int32_t *nkernels);
+
 #ifdef __cplusplus
 }
 #endif

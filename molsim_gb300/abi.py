@@ -83,6 +83,8 @@ LIB_ONLY = [
     ("bd_step_host", C.c_int, [H, PF64, PF64, PF64]),
     ("phase_times", C.c_int, [H, PF64, C.c_int32, PI32, C.c_char_p, C.c_size_t]),
     ("phase_reset", C.c_int, [H, C.c_int32]),
+    ("bench_steps", C.c_int, [H, C.c_int32, C.c_int32, C.c_int64, PF64]),
+    ("step_kernels", C.c_int, [H, C.c_int32, PI32]),
 ]
 
 # every function the header declares (checked against the .so in tests)

@@ -395,6 +395,31 @@ int mg_md_setup(mg_handle *h, double tstep, const double *massip, const double *
     return mg_integrate_md_setup(h, tstep, massip, rod, rodd);
 }
 
+static int capture_step(mg_handle *h, bool bd) {
+    cudaGraphExec_t &g = bd ? h->g_bd : h->g_md;
+    if (g) return MG_OK;
+    cudaGraph_t graph;
+    MG_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int st = bd ? mg_integrate_bd_step_launch(h) : mg_integrate_md_step_launch(h);
+    cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
+    if (st != MG_OK) return st;
+    if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    size_t nn = 0;
+    cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(graph, nodes.data(), &nn);
+    int nk = 0;
+    for (auto &n : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(n, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+    }
+    (bd ? h->kernels_bd : h->kernels_md) = nk;
+    ce = cudaGraphInstantiate(&g, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    return MG_OK;
+}
+
 static int run_steps(mg_handle *h, int nstep, bool bd) {
     cudaGraphExec_t &g = bd ? h->g_bd : h->g_md;
     if (h->timing) {   // uncaptured launches so every phase can be timed
@@ -404,17 +429,7 @@ static int run_steps(mg_handle *h, int nstep, bool bd) {
         }
         return MG_OK;
     }
-    if (!g) {
-        cudaGraph_t graph;
-        MG_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-        int st = bd ? mg_integrate_bd_step_launch(h) : mg_integrate_md_step_launch(h);
-        cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
-        if (st != MG_OK) return st;
-        if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-        ce = cudaGraphInstantiate(&g, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-    }
+    MG_TRY(capture_step(h, bd));
     for (int s = 0; s < nstep; ++s) MG_CUDA(h, cudaGraphLaunch(g, h->st));
     return MG_OK;
 }
@@ -433,6 +448,8 @@ int mg_md_run(mg_handle *h, int32_t nstep, double *forceo, double *uout, double 
 
 int mg_bd_setup(mg_handle *h, const double *fac1, const double *fac2, int32_t iseed) {
     if (!h || !fac1 || !fac2) return MG_ERR_ARG;
+    // GauRandom's LCG stays at 0 from a seed that is 0 modulo 2^31
+    if (((uint32_t)iseed & 0x7fffffffu) == 0) return mg_fail(h, MG_ERR_ARG, "iseed must be nonzero modulo 2^31");
     return mg_integrate_bd_setup(h, fac1, fac2, iseed);
 }
 
@@ -485,6 +502,54 @@ int mg_phase_times(mg_handle *h, double *ms, int32_t nmax, int32_t *nphase, char
     }
     *nphase = k;
     if (names && names_len) std::snprintf(names, names_len, "%s", all.c_str());
+    return MG_OK;
+}
+
+int mg_bench_steps(mg_handle *h, int32_t kind, int32_t nstep, int64_t flush_bytes, double *ms_sum) {
+    if (!h || !ms_sum || nstep < 0 || flush_bytes < 0) return MG_ERR_ARG;
+    bool bd = kind == 1;
+    if (bd ? !h->bd_ready : !h->md_ready) return mg_fail(h, MG_ERR_STATE, "integrator not set up");
+    if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_nlist_set has not been called");
+    if (bd && !h->have_force) {
+        MG_TRY(mg_utotal_launch(h));
+        MG_TRY(mg_check_device_error(h));
+        h->have_force = true;
+    }
+    void *flush = nullptr;
+    if (flush_bytes) MG_CUDA(h, cudaMalloc(&flush, (size_t)flush_bytes));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double total = 0.0;
+    int st = MG_OK;
+    if (!h->timing) st = capture_step(h, bd);
+    for (int s = 0; s < nstep && st == MG_OK; ++s) {
+        if (flush) cudaMemsetAsync(flush, s & 0xff, (size_t)flush_bytes, h->st);
+        cudaEventRecord(e0, h->st);
+        if (h->timing) st = bd ? mg_integrate_bd_step_launch(h) : mg_integrate_md_step_launch(h);
+        else if (cudaGraphLaunch(bd ? h->g_bd : h->g_md, h->st) != cudaSuccess)
+            st = mg_fail(h, MG_ERR_CUDA, "graph launch failed");
+        cudaEventRecord(e1, h->st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = mg_fail(h, MG_ERR_CUDA, "step %d failed: %s", s, cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total += ms;
+        if (h->timing) mg_phase_collect(h);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (flush) cudaFree(flush);
+    if (st != MG_OK) return st;
+    *ms_sum = total;
+    return mg_check_device_error(h);
+}
+
+int mg_step_kernels(mg_handle *h, int32_t kind, int32_t *nkernels) {
+    if (!h || !nkernels) return MG_ERR_ARG;
+    *nkernels = (kind == 1) ? h->kernels_bd : h->kernels_md;
     return MG_OK;
 }
 

@@ -348,9 +348,11 @@ int mg_forces_init(mg_handle *h) {
 int mg_utotal_launch(mg_handle *h) {
     int np = h->np;
     bool mixed = h->form == MG_MIXED;
-    MG_TRY(mg_phase_begin(h, "pair"));
+    MG_TRY(mg_phase_begin(h, "prepare"));
     k_prepare<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(h->d_ro, h->d_perm, h->d_type,
                                                                      np, h->d_pos_s);
+    MG_TRY(mg_phase_end(h, "prepare"));
+    MG_TRY(mg_phase_begin(h, "pair"));
     PairArgs a;
     a.pos_s = h->d_pos_s;
     a.perm = h->d_perm;

@@ -138,6 +138,7 @@ struct mg_handle {
 
     // ---- graphs and timing -----------------------------------------------------
     cudaGraphExec_t g_bd = nullptr, g_md = nullptr;
+    int kernels_bd = 0, kernels_md = 0;
     bool timing = false;
     std::vector<mg_phase> phases;
     long launches = 0;

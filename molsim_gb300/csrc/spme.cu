@@ -421,14 +421,22 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv) {
     dim3 gc(h->fft_tiles, n);
     size_t ystride = nh, yother = (size_t)n * nh;   // y pass: t -> y, other -> z
     size_t zstride = (size_t)n * nh, zother = nh;   // z pass: t -> z, other -> y
-    MG_TRY(mg_phase_begin(h, "fft"));
+    MG_TRY(mg_phase_begin(h, "fft_x_r2c"));
     k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>(Q, F, n, logn, lp, tw);
+    MG_TRY(mg_phase_end(h, "fft_x_r2c"));
+    MG_TRY(mg_phase_begin(h, "fft_y_fwd"));
     k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, -1, tw, cv);
+    MG_TRY(mg_phase_end(h, "fft_y_fwd"));
+    MG_TRY(mg_phase_begin(h, "fft_z_conv"));
     k_fft_col<T, true><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, zstride, zother, -1, tw, cv);
+    MG_TRY(mg_phase_end(h, "fft_z_conv"));
+    MG_TRY(mg_phase_begin(h, "fft_y_inv"));
     k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, +1, tw, cv);
+    MG_TRY(mg_phase_end(h, "fft_y_inv"));
+    MG_TRY(mg_phase_begin(h, "fft_x_c2r"));
     k_fft_x_c2r<T><<<gx, thx, smx, h->st>>>(F, Q, n, logn, lp, tw);
+    MG_TRY(mg_phase_end(h, "fft_x_c2r"));
     h->launches += 5;
-    MG_TRY(mg_phase_end(h, "fft"));
     return MG_OK;
 }
 
@@ -516,9 +524,11 @@ int mg_spme_launch(mg_handle *h) {
     if (h->form == MG_MIXED) {
         MG_TRY(mg_phase_begin(h, "spread"));
         k_spread_fx<<<gb, tb, 0, h->st>>>(sa, h->d_Qfx);
-        k_fx_to_float<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>(h->d_Qfx, (float *)h->d_Q, n3);
-        h->launches += 2;
         MG_TRY(mg_phase_end(h, "spread"));
+        MG_TRY(mg_phase_begin(h, "mesh_convert"));
+        k_fx_to_float<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>(h->d_Qfx, (float *)h->d_Q, n3);
+        MG_TRY(mg_phase_end(h, "mesh_convert"));
+        h->launches += 2;
         cv.mf = h->d_mf_f;
         cv.ew = h->d_ew_f;
         cv.vw = h->d_vw_f;
@@ -529,8 +539,10 @@ int mg_spme_launch(mg_handle *h) {
         h->launches++;
         MG_TRY(mg_phase_end(h, "gather"));
     } else {
-        MG_TRY(mg_phase_begin(h, "spread"));
+        MG_TRY(mg_phase_begin(h, "mesh_clear"));
         MG_CUDA(h, cudaMemsetAsync(h->d_Q, 0, sizeof(double) * n3, h->st));
+        MG_TRY(mg_phase_end(h, "mesh_clear"));
+        MG_TRY(mg_phase_begin(h, "spread"));
         k_spread_f64<<<gb, tb, 0, h->st>>>(sa, (double *)h->d_Q);
         h->launches++;
         MG_TRY(mg_phase_end(h, "spread"));

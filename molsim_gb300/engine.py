@@ -178,6 +178,19 @@ class Engine:
         self._check(self._fn("bd_get_seed")(self.h, abi.i32(s)), "bd_get_seed")
         return int(s[0])
 
+    def BenchSteps(self, kind, nstep, flush_bytes=0):
+        """Summed device ms of nstep integrator steps (kind 0 = MD, 1 = BD),
+        L2 flushed before each step when flush_bytes > 0."""
+        ms = np.zeros(1)
+        self._check(self.lib.mg_bench_steps(self.h, int(kind), int(nstep), int(flush_bytes),
+                                            abi.f64(ms)), "bench_steps")
+        return float(ms[0])
+
+    def StepKernels(self, kind):
+        n = np.zeros(1, dtype=np.int32)
+        self._check(self.lib.mg_step_kernels(self.h, int(kind), abi.i32(n)), "step_kernels")
+        return int(n[0])
+
     # ---- timing ---------------------------------------------------------------------
     def PhaseReset(self, enable=True):
         self._check(self.lib.mg_phase_reset(self.h, int(enable)), "phase_reset")

@@ -1793,6 +1793,8 @@ int orc_md_run(orc_sys *s, int32_t nstep, double *forceo, double *uout, double *
 }
 
 int orc_bd_setup(orc_sys *s, const double *fac1, const double *fac2, int32_t iseed) {
+    /* a seed that is 0 modulo 2^31 never leaves 0 and GauRandom would loop forever */
+    if (((uint32_t)iseed & 0x7fffffffu) == 0) return MG_ERR_ARG;
     if (!s->fac1) { s->fac1 = xcalloc(s->npt, sizeof(double)); s->fac2 = xcalloc(s->npt, sizeof(double)); }
     memcpy(s->fac1, fac1, sizeof(double) * s->npt);
     memcpy(s->fac2, fac2, sizeof(double) * s->npt);
