@@ -254,10 +254,14 @@ def run_ours(args):
     kernels_per_step = emx.StepKernels(1)
 
     # per-kernel device times (uncaptured launches, same flush regime)
-    emx.PhaseReset(True)
-    emx.BenchSteps(1, min(50, max(K, 5)), FLUSH_BYTES)
-    phases = emx.PhaseTimes()
-    emx.PhaseReset(False)
+    def phase_pass(e):
+        e.PhaseReset(True)
+        e.BenchSteps(1, min(50, max(K, 5)), FLUSH_BYTES)
+        ph = e.PhaseTimes()
+        e.PhaseReset(False)
+        return ph
+    phases = phase_pass(emx)
+    phases64 = phase_pass(e64)
     nn, _ = emx.VList(maxnneigh=256)
     pairs = int(2 * nn.sum())
     nbond = 0 if s.bond_ip is None else len(s.bond_ip)
@@ -324,6 +328,7 @@ def run_ours(args):
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "algorithmic_bytes": ab, "kernel_ms": phases[dom]},
             "phases_ms": phases,
+            "phases_ms_fp64": phases64,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 24 * s.np_,
                     "d2h_bytes_per_step": 48 * s.np_ + 32},

@@ -107,7 +107,10 @@ static void free_all(mg_handle *h) {
                     h->d_Qref, h->d_phi, h->d_gker, h->d_ipnptm, h->d_rotm, h->d_du, h->d_drostep,
                     h->d_drosum, h->d_blkmax, h->d_rebuild, h->d_massip, h->d_rod, h->d_rodd,
                     h->d_fac1, h->d_fac2, h->d_rng, h->d_rng_save, h->d_cflag, h->d_cidx, h->d_cval,
-                    h->d_scan_tmp};
+                    h->d_scan_tmp, h->d_zlow, h->d_coef, h->d_coef_f, h->d_bin_z0, h->d_bin_inv,
+                    h->d_bin_kstart, h->d_brick_count, h->d_brick_perm, h->d_brick_rank,
+                    h->d_brick_of, h->d_brick_start, h->d_tiles, h->d_f32_tabs, h->d_pos_f,
+                    h->d_cell_s, h->d_corner, h->d_spl_w, h->d_spl_dw};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -248,7 +251,7 @@ static int create_impl(const mg_params *p, mg_handle *h) {
     else if (h->ewald == MG_EWALD_STD) MG_TRY(mg_ewald_std_init(h));
     else if (h->ewald != MG_EWALD_NONE) return mg_fail(h, MG_ERR_ARG, "ewald = %d", h->ewald);
     MG_TRY(mg_lists_init(h));
-    MG_TRY(mg_forces_init(h));
+    MG_TRY(mg_forces_init(h, p->ubuf, start.data(), count.data()));
     if (h->mode == MG_MC) MG_TRY(mg_mc_init(h));
     MG_CUDA(h, cudaStreamSynchronize(h->st));
     return MG_OK;
@@ -398,12 +401,61 @@ int mg_md_setup(mg_handle *h, double tstep, const double *massip, const double *
 static int capture_step(mg_handle *h, bool bd) {
     cudaGraphExec_t &g = bd ? h->g_bd : h->g_md;
     if (g) return MG_OK;
-    cudaGraph_t graph;
+    // The step is captured with the Verlet-list rebuild in the body of a
+    // conditional (IF) node whose condition the list check sets on the
+    // device, so steps without a rebuild launch none of its kernels.
+    cudaGraph_t graph = nullptr;
     MG_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    int st = bd ? mg_integrate_bd_step_launch(h) : mg_integrate_md_step_launch(h);
-    cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
-    if (st != MG_OK) return st;
-    if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    cudaError_t ce = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &cg, nullptr, nullptr, nullptr);
+    if (ce == cudaSuccess) ce = cudaGraphConditionalHandleCreate(&h->cond, cg, 0, cudaGraphCondAssignDefault);
+    int st = MG_OK;
+    if (ce == cudaSuccess) {
+        h->use_cond = true;
+        st = bd ? mg_integrate_bd_step_launch(h) : mg_integrate_md_step_launch(h);
+        h->use_cond = false;
+    }
+    if (ce == cudaSuccess && st == MG_OK) {
+        const cudaGraphNode_t *deps = nullptr;
+        const cudaGraphEdgeData *edges = nullptr;
+        size_t ndeps = 0;
+        ce = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &cg, &deps, &edges, &ndeps);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h->cond;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn = nullptr;
+        if (ce == cudaSuccess) ce = cudaGraphAddNode(&cn, cg, deps, edges, ndeps, &cp);
+        if (ce == cudaSuccess) ce = cudaStreamUpdateCaptureDependencies(h->st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (ce == cudaSuccess) {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            cudaStream_t side = nullptr;
+            ce = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+            if (ce == cudaSuccess) ce = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if (ce == cudaSuccess) {
+                cudaStream_t keep = h->st;
+                h->st = side;
+                st = mg_lists_build(h, false);
+                h->st = keep;
+                cudaGraph_t b2 = nullptr;
+                cudaError_t ce2 = cudaStreamEndCapture(side, &b2);
+                if (ce2 != cudaSuccess) ce = ce2;
+            }
+            if (side) cudaStreamDestroy(side);
+        }
+    }
+    cudaError_t ce3 = cudaStreamEndCapture(h->st, &graph);
+    if (st != MG_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (ce == cudaSuccess) ce = ce3;
+    if (ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    }
     size_t nn = 0;
     cudaGraphGetNodes(graph, nullptr, &nn);
     std::vector<cudaGraphNode_t> nodes(nn);

@@ -15,6 +15,8 @@
 //
 // Mixed form: the cutoff decision stays FP64; table arithmetic is FP32 and each
 // particle's force is stored as 64-bit fixed point (scale 2^32).
+#include <algorithm>
+
 #include "mg_internal.cuh"
 
 namespace {
@@ -48,15 +50,48 @@ __global__ void k_prepare(const double *__restrict__ ro, const int *__restrict__
     pos_s[s] = make_double4(ro[3 * p], ro[3 * p + 1], ro[3 * p + 2], (double)type[p]);
 }
 
+// mixed form: FP32 offset from the centre of the particle's cell (the cell
+// of the last list build) and the cell's coordinates packed in 10-bit
+// fields, so pair distances need no FP64 arithmetic
+struct CellGeom {
+    int nc[3];
+    double size[3], half[3];
+    float sizef[3], lenf[3], halff[3];
+};
+
+__global__ void k_prepare_f32(const double *__restrict__ ro, const int *__restrict__ perm,
+                              const int *__restrict__ type, const int *__restrict__ cellof, int np,
+                              CellGeom g, float4 *__restrict__ pos_f, int *__restrict__ cell_s) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= np) return;
+    int p = perm[s];
+    int c = cellof[p];
+    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    // offsets wrapped to the nearest image, so a particle that crossed the
+    // box since the list build keeps a small offset
+    double d[3];
+    int cc[3] = {cx, cy, cz};
+    for (int m = 0; m < 3; ++m) {
+        d[m] = ro[3 * p + m] - ((cc[m] + 0.5) * g.size[m] - g.half[m]);
+        if (fabs(d[m]) > g.half[m]) d[m] -= copysign(2.0 * g.half[m], d[m]);
+    }
+    float ox = (float)d[0], oy = (float)d[1], oz = (float)d[2];
+    pos_f[s] = make_float4(ox, oy, oz, __int_as_float(type[p]));
+    cell_s[s] = cx | (cy << 10) | (cz << 20);
+}
+
 struct PairArgs {
     const double4 *pos_s;
     const int *perm, *nnb, *nbr;
-    int np, npt, nptpt;
+    int np, npt, nptpt, nrec, nbins;
     const int *pairidx;          // [npt*npt] 1-based, column-major
-    const double *ubuf;
-    const float *ubuf_f;
+    const double *zlow;          // [nrec] lower end (r^2) of every table interval
+    const double *coef;          // [nrec*11] FP64 coefficients (usum 6, fsum 5)
+    const float *coef_f;         // [nrec*11] FP32 coefficients (mixed form)
     const int *tab_start, *tab_n;
-    const double *r2umin, *r2atat;
+    const double *r2umin, *r2atat, *bin_z0, *bin_inv;
+    const unsigned short *bin_kstart;   // [nptpt*nbins] first interval to scan from
+    int tab_in_smem;             // coefficient table staged in shared memory
     mg_box box;
     double rcut2;
     int cellcut;                 // 1: r2 < rcut2 (cell list), 0: r2 <= rcut2 (Verlet list)
@@ -66,106 +101,330 @@ struct PairArgs {
     int *err;
 };
 
-__device__ __forceinline__ int table_interval(const double *__restrict__ ubuf, int start, int n,
-                                              double r2) {
-    // smallest k with z_low(k) <= r2; z_low strictly decreasing in k
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (r2 >= ubuf[(size_t)(start + mid) * 12]) hi = mid;
-        else lo = mid + 1;
-    }
-    return start + lo;
-}
-
-__device__ __forceinline__ int table_interval_f(const float *__restrict__ ubuf, int start, int n,
-                                                float r2) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (r2 >= ubuf[(size_t)(start + mid) * 12]) hi = mid;
-        else lo = mid + 1;
-    }
-    return start + lo;
-}
+// shared-memory image of the small per-pair data and (optionally) the table
+struct PairShared {
+    int *pairidx, *start, *n;
+    double *r2atat, *r2umin, *z0, *inv, *zlow;
+    unsigned short *kstart;
+    void *coef;
+    double *u;   // per-thread energy slots [nptpt][blockDim]
+};
 
 template <bool MIXED>
+__host__ __device__ size_t pair_smem_layout(const PairArgs &a, unsigned char *base, PairShared &s, int nthr) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t r = o;
+        o = (o + bytes + 15) & ~(size_t)15;
+        return base ? (void *)(base + r) : nullptr;
+    };
+    s.r2atat = (double *)take(sizeof(double) * a.nptpt);
+    s.r2umin = (double *)take(sizeof(double) * a.nptpt);
+    s.z0 = (double *)take(sizeof(double) * a.nptpt);
+    s.inv = (double *)take(sizeof(double) * a.nptpt);
+    s.u = (double *)take(sizeof(double) * a.nptpt * nthr);
+    s.zlow = (double *)take(sizeof(double) * a.nrec);
+    s.pairidx = (int *)take(sizeof(int) * a.npt * a.npt);
+    s.start = (int *)take(sizeof(int) * a.nptpt);
+    s.n = (int *)take(sizeof(int) * a.nptpt);
+    s.kstart = (unsigned short *)take(sizeof(unsigned short) * a.nptpt * a.nbins);
+    s.coef = a.tab_in_smem ? take((MIXED ? sizeof(float) : sizeof(double)) * 11 * a.nrec) : nullptr;
+    return o;
+}
+
+// table interval containing r2 (first k with zlow(k) <= r2, as the reference's
+// linear search from iubuflow finds it): start from the bin's first
+// candidate and step forward; exact by construction of kstart
+__device__ __forceinline__ int find_interval(const PairShared &s, int pair, double r2, int nbins) {
+    int b = (int)((r2 - s.z0[pair]) * s.inv[pair]);
+    b = min(max(b, 0), nbins - 1);
+    int k = s.kstart[pair * nbins + b];
+    int last = s.n[pair] - 1;
+    const double *z = s.zlow + s.start[pair];
+    while (k < last && z[k] > r2) ++k;
+    return s.start[pair] + k;
+}
+
+// One pair (i, j) of the Verlet list; returns false when it is beyond rcut.
+template <bool MIXED>
+__device__ __forceinline__ void pair_term(const PairArgs &a, const PairShared &s, double4 pi, int ti,
+                                          double4 pj, int p, int j, double &fx, double &fy, double &fz,
+                                          float &gx, float &gy, float &gz, double *u, double &vir) {
+    double dx = mg_pbc1(__dsub_rn(pi.x, pj.x), a.box.half[0], a.box.len[0]);
+    double dy = mg_pbc1(__dsub_rn(pi.y, pj.y), a.box.half[1], a.box.len[1]);
+    double dz = mg_pbc1(__dsub_rn(pi.z, pj.z), a.box.half[2], a.box.len[2]);
+    double r2 = mg_r2_exact(dx, dy, dz);
+    if (a.cellcut ? !(r2 < a.rcut2) : (r2 > a.rcut2)) return;
+    int tj = (int)pj.w;
+    int pair = s.pairidx[tj * a.npt + ti] - 1;   // iptpt(ipt,jpt) - 1
+    if (r2 < s.r2atat[pair]) {
+        // hard-core overlap: u = 1e10 (the cell-list routine also sets
+        // fsum = 1e10; the Verlet-list routine keeps a stale value)
+        u[pair * blockDim.x] += 0.5 * 1e10;
+        if (MIXED) { gx += 1e10f * (float)dx; gy += 1e10f * (float)dy; gz += 1e10f * (float)dz; }
+        else { fx += 1e10 * dx; fy += 1e10 * dy; fz += 1e10 * dz; }
+        vir -= 0.5 * (1e10 * r2);
+        return;
+    }
+    if (r2 < s.r2umin[pair]) {
+        mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, p + 1, a.perm[j] + 1, pair + 1);
+        return;
+    }
+    int rec = find_interval(s, pair, r2, a.nbins);
+    double d = r2 - s.zlow[rec];
+    if (MIXED) {
+        const float *c = a.tab_in_smem ? (const float *)s.coef + (size_t)rec * 11 : a.coef_f + (size_t)rec * 11;
+        float df = (float)d;
+        float us = c[0] + df * (c[1] + df * (c[2] + df * (c[3] + df * (c[4] + df * c[5]))));
+        float fs = c[6] + df * (c[7] + df * (c[8] + df * (c[9] + df * c[10])));
+        gx += fs * (float)dx;
+        gy += fs * (float)dy;
+        gz += fs * (float)dz;
+        u[pair * blockDim.x] += 0.5 * (double)us;
+        vir -= 0.5 * (double)fs * r2;
+    } else {
+        const double *c = a.tab_in_smem ? (const double *)s.coef + (size_t)rec * 11 : a.coef + (size_t)rec * 11;
+        double us = c[0] + d * (c[1] + d * (c[2] + d * (c[3] + d * (c[4] + d * c[5]))));
+        double fs = c[6] + d * (c[7] + d * (c[8] + d * (c[9] + d * c[10])));
+        fx += fs * dx;
+        fy += fs * dy;
+        fz += fs * dz;
+        u[pair * blockDim.x] += 0.5 * us;
+        vir -= 0.5 * (fs * r2);
+    }
+}
+
+// WARP: one warp per slot (dense systems); otherwise one thread per slot.
+template <bool MIXED, bool WARP>
 __global__ void __launch_bounds__(kPairThreads) k_pair(PairArgs a) {
-    __shared__ double sh[(MG_MAX_NPTPT + 1) * (kPairThreads / 32)];
-    double acc[MG_MAX_NPTPT + 1];
-    for (int v = 0; v <= a.nptpt; ++v) acc[v] = 0.0;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[(MG_MAX_NPTPT + 1) * (kPairThreads / 32)];
+    PairShared s;
+    pair_smem_layout<MIXED>(a, smem, s, blockDim.x);
+    for (int k = threadIdx.x; k < a.npt * a.npt; k += blockDim.x) s.pairidx[k] = a.pairidx[k];
+    for (int k = threadIdx.x; k < a.nptpt; k += blockDim.x) {
+        s.r2atat[k] = a.r2atat[k];
+        s.r2umin[k] = a.r2umin[k];
+        s.z0[k] = a.bin_z0[k];
+        s.inv[k] = a.bin_inv[k];
+        s.start[k] = a.tab_start[k];
+        s.n[k] = a.tab_n[k];
+    }
+    for (int k = threadIdx.x; k < a.nptpt * (int)blockDim.x; k += blockDim.x) s.u[k] = 0.0;
+    for (int k = threadIdx.x; k < a.nrec; k += blockDim.x) s.zlow[k] = a.zlow[k];
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.bin_kstart);
+        uint4 *dst = reinterpret_cast<uint4 *>(s.kstart);
+        int nv = (a.nptpt * a.nbins * 2) / 16;
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) dst[k] = src[k];
+    }
+    if (a.tab_in_smem) {
+        if (MIXED) {
+            float *dst = (float *)s.coef;
+            for (int k = threadIdx.x; k < 11 * a.nrec; k += blockDim.x) dst[k] = a.coef_f[k];
+        } else {
+            double *dst = (double *)s.coef;
+            for (int k = threadIdx.x; k < 11 * a.nrec; k += blockDim.x) dst[k] = a.coef[k];
+        }
+    }
+    __syncthreads();
+    double *u = s.u + threadIdx.x;
+    double vir = 0.0;
+    int lane = threadIdx.x & 31;
+    int i = WARP ? (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5)
+                 : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < a.np) {
         double4 pi = a.pos_s[i];
         int ti = (int)pi.w;
         int p = a.perm[i];
         double fx = 0.0, fy = 0.0, fz = 0.0;
         float gx = 0.f, gy = 0.f, gz = 0.f;
-        double fsum = 0.0;
         int nn = a.nnb[i];
-        for (int k = 0; k < nn; ++k) {
-            int j = a.nbr[(size_t)k * a.np + i];
-            double4 pj = a.pos_s[j];
-            double dx = mg_pbc1(__dsub_rn(pi.x, pj.x), a.box.half[0], a.box.len[0]);
-            double dy = mg_pbc1(__dsub_rn(pi.y, pj.y), a.box.half[1], a.box.len[1]);
-            double dz = mg_pbc1(__dsub_rn(pi.z, pj.z), a.box.half[2], a.box.len[2]);
-            double r2 = mg_r2_exact(dx, dy, dz);
-            if (a.cellcut ? !(r2 < a.rcut2) : (r2 > a.rcut2)) continue;
-            int tj = (int)pj.w;
-            int pair = a.pairidx[tj * a.npt + ti];   // iptpt(ipt,jpt), 1-based
-            if (r2 < a.r2atat[pair - 1]) {
-                // hard-core overlap: u = 1e10 (the cell-list routine also sets
-                // fsum = 1e10; the Verlet-list routine keeps a stale value)
-                acc[pair - 1] += 0.5 * 1e10;
-                if (MIXED) {
-                    gx += 1e10f * (float)dx; gy += 1e10f * (float)dy; gz += 1e10f * (float)dz;
-                } else {
-                    fx += 1e10 * dx; fy += 1e10 * dy; fz += 1e10 * dz;
-                }
-                acc[a.nptpt] -= 0.5 * (1e10 * r2);
-                continue;
+        int k0 = WARP ? lane : 0, ks = WARP ? 32 : 1;
+        // software pipelining: the next neighbour's index and position are
+        // requested before the current pair is evaluated
+        int k = k0;
+        int jn = (k < nn) ? a.nbr[(size_t)k * a.np + i] : 0;
+        double4 pn = (k < nn) ? a.pos_s[jn] : make_double4(0, 0, 0, 0);
+        for (; k < nn; k += ks) {
+            int j = jn;
+            double4 pj = pn;
+            if (k + ks < nn) {
+                jn = a.nbr[(size_t)(k + ks) * a.np + i];
+                pn = a.pos_s[jn];
             }
-            if (r2 < a.r2umin[pair - 1]) {
-                mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, p + 1, a.perm[j] + 1, pair);
-                continue;
-            }
-            int st = a.tab_start[pair - 1], n = a.tab_n[pair - 1];
-            if (MIXED) {
-                float r2f = (float)r2;
-                int rec = table_interval_f(a.ubuf_f, st, n, r2f);
-                const float *c = a.ubuf_f + (size_t)rec * 12;
-                float d = r2f - c[0];
-                float us = c[1] + d * (c[2] + d * (c[3] + d * (c[4] + d * (c[5] + d * c[6]))));
-                float fs = c[7] + d * (c[8] + d * (c[9] + d * (c[10] + d * c[11])));
-                gx += fs * (float)dx;
-                gy += fs * (float)dy;
-                gz += fs * (float)dz;
-                acc[pair - 1] += 0.5 * (double)us;
-                acc[a.nptpt] -= 0.5 * (double)(fs * r2f);
-            } else {
-                int rec = table_interval(a.ubuf, st, n, r2);
-                const double *c = a.ubuf + (size_t)rec * 12;
-                double d = r2 - c[0];
-                double us = c[1] + d * (c[2] + d * (c[3] + d * (c[4] + d * (c[5] + d * c[6]))));
-                fsum = c[7] + d * (c[8] + d * (c[9] + d * (c[10] + d * c[11])));
-                fx += fsum * dx;
-                fy += fsum * dy;
-                fz += fsum * dz;
-                acc[pair - 1] += 0.5 * us;
-                acc[a.nptpt] -= 0.5 * (fsum * r2);
+            pair_term<MIXED>(a, s, pi, ti, pj, p, j, fx, fy, fz, gx, gy, gz, u, vir);
+        }
+        if (WARP) {
+            for (int o = 16; o > 0; o >>= 1) {
+                fx += __shfl_down_sync(0xffffffffu, fx, o);
+                fy += __shfl_down_sync(0xffffffffu, fy, o);
+                fz += __shfl_down_sync(0xffffffffu, fz, o);
+                gx += __shfl_down_sync(0xffffffffu, gx, o);
+                gy += __shfl_down_sync(0xffffffffu, gy, o);
+                gz += __shfl_down_sync(0xffffffffu, gz, o);
             }
         }
-        if (MIXED) {
-            a.ffx[3 * p + 0] = __double2ll_rn((double)gx * MG_FX_SCALE);
-            a.ffx[3 * p + 1] = __double2ll_rn((double)gy * MG_FX_SCALE);
-            a.ffx[3 * p + 2] = __double2ll_rn((double)gz * MG_FX_SCALE);
-        } else {
-            a.force[3 * p + 0] = fx;
-            a.force[3 * p + 1] = fy;
-            a.force[3 * p + 2] = fz;
+        if (!WARP || lane == 0) {
+            if (MIXED) {
+                a.ffx[3 * p + 0] = __double2ll_rn((double)gx * MG_FX_SCALE);
+                a.ffx[3 * p + 1] = __double2ll_rn((double)gy * MG_FX_SCALE);
+                a.ffx[3 * p + 2] = __double2ll_rn((double)gz * MG_FX_SCALE);
+            } else {
+                a.force[3 * p + 0] = fx;
+                a.force[3 * p + 1] = fy;
+                a.force[3 * p + 2] = fz;
+            }
         }
     }
-    block_sum<kPairThreads>(acc, a.nptpt + 1, a.part + (size_t)blockIdx.x * (a.nptpt + 1), sh);
+    double acc[MG_MAX_NPTPT + 1];
+    for (int v = 0; v < a.nptpt; ++v) acc[v] = u[v * blockDim.x];
+    acc[a.nptpt] = vir;
+    block_sum<kPairThreads>(acc, a.nptpt + 1, a.part + (size_t)blockIdx.x * (a.nptpt + 1), red);
+}
+
+// ---- mixed-form pair kernel: FP32 only ------------------------------------------
+struct PairArgsF {
+    const float4 *pos_f;
+    const int *cell_s, *perm, *nnb, *nbr;
+    int np, npt, nptpt, nrec, nbins;
+    const int *pairidx, *tab_start, *tab_n;
+    const float *zlow_f, *coef_f, *r2umin_f, *r2atat_f, *bin_z0_f, *bin_inv_f;
+    const unsigned short *bin_kstart;
+    int tab_in_smem;
+    CellGeom g;
+    float rcut2;
+    int cellcut;
+    long long *ffx;
+    double *part;
+    int *err;
+};
+
+struct PairSharedF {
+    int *pairidx, *start, *n;
+    float *r2atat, *r2umin, *z0, *inv, *zlow, *coef, *u;
+    unsigned short *kstart;
+};
+
+__host__ __device__ size_t pair_smem_layout_f(const PairArgsF &a, unsigned char *base, PairSharedF &s, int nthr) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t r = o;
+        o = (o + bytes + 15) & ~(size_t)15;
+        return base ? (void *)(base + r) : nullptr;
+    };
+    s.r2atat = (float *)take(sizeof(float) * a.nptpt);
+    s.r2umin = (float *)take(sizeof(float) * a.nptpt);
+    s.z0 = (float *)take(sizeof(float) * a.nptpt);
+    s.inv = (float *)take(sizeof(float) * a.nptpt);
+    s.u = (float *)take(sizeof(float) * a.nptpt * nthr);
+    s.zlow = (float *)take(sizeof(float) * a.nrec);
+    s.pairidx = (int *)take(sizeof(int) * a.npt * a.npt);
+    s.start = (int *)take(sizeof(int) * a.nptpt);
+    s.n = (int *)take(sizeof(int) * a.nptpt);
+    s.kstart = (unsigned short *)take(sizeof(unsigned short) * a.nptpt * a.nbins);
+    s.coef = a.tab_in_smem ? (float *)take(sizeof(float) * 11 * a.nrec) : nullptr;
+    return o;
+}
+
+__device__ __forceinline__ int wrap_cell(int d, int n) {
+    int h = n >> 1;
+    d += (d < -h) ? n : 0;
+    d -= (d > h) ? n : 0;
+    return d;
+}
+
+// A team of TEAM lanes per slot walks the slot's Verlet list with stride
+// TEAM; the team's force is combined with shuffles.  Tables are read through
+// the read-only path (they stay in L1); per-lane energies sit in shared slots.
+template <int TEAM>
+__global__ void __launch_bounds__(kPairThreads) k_pair_f32(PairArgsF a) {
+    __shared__ float su[MG_MAX_NPTPT * kPairThreads];
+    __shared__ double red[(MG_MAX_NPTPT + 1) * (kPairThreads / 32)];
+    for (int k = threadIdx.x; k < a.nptpt * kPairThreads; k += kPairThreads) su[k] = 0.f;
+    __syncthreads();
+    float *u = su + threadIdx.x;
+    float vir = 0.f;
+    int j0 = threadIdx.x & (TEAM - 1);
+    int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) / TEAM);
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    if (i < a.np) {
+        float4 pi = __ldg(&a.pos_f[i]);
+        int ci = __ldg(&a.cell_s[i]);
+        int ti = __float_as_int(pi.w);
+        int nn = __ldg(&a.nnb[i]);
+        for (int k = j0; k < nn; k += TEAM) {
+            int j = __ldg(&a.nbr[(size_t)k * a.np + i]);
+            float4 pj = __ldg(&a.pos_f[j]);
+            int cj = __ldg(&a.cell_s[j]);
+            int dcx = wrap_cell((ci & 1023) - (cj & 1023), a.g.nc[0]);
+            int dcy = wrap_cell(((ci >> 10) & 1023) - ((cj >> 10) & 1023), a.g.nc[1]);
+            int dcz = wrap_cell((ci >> 20) - (cj >> 20), a.g.nc[2]);
+            float dx = (float)dcx * a.g.sizef[0] + (pi.x - pj.x);
+            float dy = (float)dcy * a.g.sizef[1] + (pi.y - pj.y);
+            float dz = (float)dcz * a.g.sizef[2] + (pi.z - pj.z);
+            if (fabsf(dx) > a.g.halff[0]) dx -= copysignf(a.g.lenf[0], dx);
+            if (fabsf(dy) > a.g.halff[1]) dy -= copysignf(a.g.lenf[1], dy);
+            if (fabsf(dz) > a.g.halff[2]) dz -= copysignf(a.g.lenf[2], dz);
+            float r2 = dx * dx + dy * dy + dz * dz;
+            if (a.cellcut ? !(r2 < a.rcut2) : (r2 > a.rcut2)) continue;
+            int pair = __ldg(&a.pairidx[__float_as_int(pj.w) * a.npt + ti]) - 1;
+            if (r2 < __ldg(&a.r2atat_f[pair])) {
+                u[pair * kPairThreads] += 0.5e10f;
+                gx += 1e10f * dx; gy += 1e10f * dy; gz += 1e10f * dz;
+                vir -= 0.5e10f * r2;
+                continue;
+            }
+            if (r2 < __ldg(&a.r2umin_f[pair])) {
+                mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, a.perm[i] + 1, a.perm[j] + 1, pair + 1);
+                continue;
+            }
+            int b = (int)((r2 - __ldg(&a.bin_z0_f[pair])) * __ldg(&a.bin_inv_f[pair]));
+            b = min(max(b, 0), a.nbins - 1);
+            int start = __ldg(&a.tab_start[pair]);
+            int kk = __ldg(&a.bin_kstart[pair * a.nbins + b]), last = __ldg(&a.tab_n[pair]) - 1;
+            const float *z = a.zlow_f + start;
+            while (kk < last && __ldg(&z[kk]) > r2) ++kk;
+            int rec = start + kk;
+            const float *c = a.coef_f + (size_t)rec * 11;
+            float d = r2 - __ldg(&z[kk]);
+            float us = __ldg(&c[0]) + d * (__ldg(&c[1]) + d * (__ldg(&c[2]) + d * (__ldg(&c[3]) + d * (__ldg(&c[4]) + d * __ldg(&c[5])))));
+            float fs = __ldg(&c[6]) + d * (__ldg(&c[7]) + d * (__ldg(&c[8]) + d * (__ldg(&c[9]) + d * __ldg(&c[10]))));
+            gx += fs * dx;
+            gy += fs * dy;
+            gz += fs * dz;
+            u[pair * kPairThreads] += 0.5f * us;
+            vir -= 0.5f * fs * r2;
+        }
+    }
+    // every lane takes part (teams past np hold zeros)
+#pragma unroll
+    for (int o = TEAM / 2; o > 0; o >>= 1) {
+        gx += __shfl_xor_sync(0xffffffffu, gx, o, TEAM);
+        gy += __shfl_xor_sync(0xffffffffu, gy, o, TEAM);
+        gz += __shfl_xor_sync(0xffffffffu, gz, o, TEAM);
+    }
+    if (i < a.np && j0 == 0) {
+        int p = a.perm[i];
+        a.ffx[3 * p + 0] = __double2ll_rn((double)gx * MG_FX_SCALE);
+        a.ffx[3 * p + 1] = __double2ll_rn((double)gy * MG_FX_SCALE);
+        a.ffx[3 * p + 2] = __double2ll_rn((double)gz * MG_FX_SCALE);
+    }
+    __syncthreads();
+    // warp sums in FP32, FP64 across the block's warps
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int NW = kPairThreads / 32;
+    for (int v = 0; v <= a.nptpt; ++v) {
+        float x = (v < a.nptpt) ? u[v * kPairThreads] : vir;
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[v * NW + wid] = (double)x;
+    }
+    __syncthreads();
+    if (threadIdx.x <= a.nptpt) {
+        double sum = 0.0;
+        for (int k = 0; k < NW; ++k) sum += red[threadIdx.x * NW + k];
+        a.part[(size_t)blockIdx.x * (a.nptpt + 1) + threadIdx.x] = sum;
+    }
 }
 
 // UBond: every particle adds the forces of its (at most a few) bonds; the
@@ -319,9 +578,123 @@ __global__ void k_epilogue(const double *__restrict__ force, const long long *__
 
 }  // namespace
 
-int mg_forces_init(mg_handle *h) {
+// Direct-index table lookup: per type pair a uniform grid of nbins bins over
+// [r2umin, max(rcut^2, z_low(1))]; kstart(bin) is the first interval whose
+// lower end lies at or below the bin's upper edge (with a margin), so a
+// forward scan from it stops at the reference's interval.
+static int pair_tables(mg_handle *h, const double *ubuf, const int *start, const int *count) {
+    int nptpt = h->nptpt;
+    h->nrec = h->nbuf / 12;
+    h->nbins = 1024;
+    std::vector<double> zlow(h->nrec), coef(11 * (size_t)h->nrec), z0(nptpt), inv(nptpt);
+    std::vector<float> coef_f(11 * (size_t)h->nrec);
+    std::vector<unsigned short> kst((size_t)nptpt * h->nbins);
+    for (int r = 0; r < h->nrec; ++r) {
+        zlow[r] = ubuf[12 * (size_t)r];
+        for (int c = 0; c < 11; ++c) {
+            coef[11 * (size_t)r + c] = ubuf[12 * (size_t)r + 1 + c];
+            coef_f[11 * (size_t)r + c] = (float)ubuf[12 * (size_t)r + 1 + c];
+        }
+    }
+    for (int p = 0; p < nptpt; ++p) {
+        const double *z = zlow.data() + start[p];
+        int n = count[p];
+        if (n > 65535) return mg_fail(h, MG_ERR_UNSUPPORTED, "table of pair %d has %d intervals", p + 1, n);
+        double lo = z[n - 1], hi = std::max(h->rcut2, z[0]);
+        double width = (hi - lo) / h->nbins;
+        if (!(width > 0)) width = 1.0;
+        z0[p] = lo;
+        inv[p] = 1.0 / width;
+        for (int b = 0; b < h->nbins; ++b) {
+            int k = 0;
+            if (b < h->nbins - 1) {
+                double upper = lo + (b + 1.001) * width;
+                while (k < n - 1 && z[k] > upper) ++k;
+            }
+            kst[(size_t)p * h->nbins + b] = (unsigned short)k;
+        }
+    }
+    MG_CUDA(h, cudaMalloc(&h->d_zlow, sizeof(double) * h->nrec));
+    MG_CUDA(h, cudaMalloc(&h->d_coef, sizeof(double) * coef.size()));
+    MG_CUDA(h, cudaMalloc(&h->d_coef_f, sizeof(float) * coef_f.size()));
+    MG_CUDA(h, cudaMalloc(&h->d_bin_z0, sizeof(double) * nptpt));
+    MG_CUDA(h, cudaMalloc(&h->d_bin_inv, sizeof(double) * nptpt));
+    MG_CUDA(h, cudaMalloc(&h->d_bin_kstart, sizeof(unsigned short) * kst.size()));
+    MG_CUDA(h, cudaMemcpy(h->d_zlow, zlow.data(), sizeof(double) * h->nrec, cudaMemcpyHostToDevice));
+    MG_CUDA(h, cudaMemcpy(h->d_coef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(h, cudaMemcpy(h->d_coef_f, coef_f.data(), sizeof(float) * coef_f.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(h, cudaMemcpy(h->d_bin_z0, z0.data(), sizeof(double) * nptpt, cudaMemcpyHostToDevice));
+    MG_CUDA(h, cudaMemcpy(h->d_bin_inv, inv.data(), sizeof(double) * nptpt, cudaMemcpyHostToDevice));
+    MG_CUDA(h, cudaMemcpy(h->d_bin_kstart, kst.data(), sizeof(unsigned short) * kst.size(), cudaMemcpyHostToDevice));
+    {   // FP32 copies for the mixed form (interval lower ends, bins, limits)
+        std::vector<float> zf(h->nrec), r2u(nptpt), r2a(nptpt), z0f(nptpt), invf(nptpt);
+        for (int r = 0; r < h->nrec; ++r) zf[r] = (float)zlow[r];
+        for (int p = 0; p < nptpt; ++p) {
+            z0f[p] = (float)z0[p];
+            invf[p] = (float)inv[p];
+        }
+        std::vector<double> r2u_d(nptpt), r2a_d(nptpt);
+        MG_CUDA(h, cudaMemcpy(r2u_d.data(), h->d_r2umin, sizeof(double) * nptpt, cudaMemcpyDeviceToHost));
+        MG_CUDA(h, cudaMemcpy(r2a_d.data(), h->d_r2atat, sizeof(double) * nptpt, cudaMemcpyDeviceToHost));
+        for (int p = 0; p < nptpt; ++p) {
+            r2u[p] = (float)r2u_d[p];
+            r2a[p] = (float)r2a_d[p];
+        }
+        MG_CUDA(h, cudaMalloc(&h->d_f32_tabs, sizeof(float) * (h->nrec + 4 * nptpt)));
+        float *d = h->d_f32_tabs;
+        MG_CUDA(h, cudaMemcpy(d, zf.data(), sizeof(float) * h->nrec, cudaMemcpyHostToDevice));
+        MG_CUDA(h, cudaMemcpy(d + h->nrec, r2u.data(), sizeof(float) * nptpt, cudaMemcpyHostToDevice));
+        MG_CUDA(h, cudaMemcpy(d + h->nrec + nptpt, r2a.data(), sizeof(float) * nptpt, cudaMemcpyHostToDevice));
+        MG_CUDA(h, cudaMemcpy(d + h->nrec + 2 * nptpt, z0f.data(), sizeof(float) * nptpt, cudaMemcpyHostToDevice));
+        MG_CUDA(h, cudaMemcpy(d + h->nrec + 3 * nptpt, invf.data(), sizeof(float) * nptpt, cudaMemcpyHostToDevice));
+    }
+    // shared-memory budget: stage the coefficient table when it is small
+    PairArgs a{};
+    a.nptpt = nptpt;
+    a.npt = h->npt;
+    a.nrec = h->nrec;
+    a.nbins = h->nbins;
+    bool mixed = h->form == MG_MIXED;
+    size_t base, full;
+    if (mixed) {
+        PairArgsF af{};
+        af.nptpt = nptpt;
+        af.npt = h->npt;
+        af.nrec = h->nrec;
+        af.nbins = h->nbins;
+        PairSharedF sf;
+        af.tab_in_smem = 0;
+        base = pair_smem_layout_f(af, nullptr, sf, kPairThreads);
+        af.tab_in_smem = 1;
+        full = pair_smem_layout_f(af, nullptr, sf, kPairThreads);
+    } else {
+        PairShared s;
+        a.tab_in_smem = 0;
+        base = pair_smem_layout<false>(a, nullptr, s, kPairThreads);
+        a.tab_in_smem = 1;
+        full = pair_smem_layout<false>(a, nullptr, s, kPairThreads);
+    }
+    h->pair_tab_smem = (full <= 64 * 1024) ? 1 : 0;
+    h->pair_smem = h->pair_tab_smem ? full : base;
+    if (h->pair_smem > 200 * 1024) return mg_fail(h, MG_ERR_UNSUPPORTED, "pair tables need %zu bytes of shared memory", h->pair_smem);
+    cudaFuncSetAttribute(k_pair<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_pair<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return MG_OK;
+}
+
+int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int *count) {
     int np = h->np;
-    h->nblk_pair = (np + kPairThreads - 1) / kPairThreads;
+    MG_TRY(pair_tables(h, ubuf, start, count));
+    // warp per particle when the expected list is long (dense systems)
+    double dens = np / h->vol, rc = h->rcut + h->drnlist;
+    double expect = 4.0 / 3.0 * 3.141592653589793 * rc * rc * rc * dens;
+    h->pair_warp = expect > 24.0 ? 1 : 0;
+    // mixed form: a team of lanes per slot sized to the expected full list
+    // (~2x the half-sphere count), so short lists still fill the GPU
+    h->pair_team = expect < 1.0 ? 1 : expect < 3.0 ? 2 : expect < 10.0 ? 4 : expect < 20.0 ? 8 : expect < 40.0 ? 16 : 32;
+    int per_block = h->pair_warp ? kPairThreads / 32 : kPairThreads;
+    h->nblk_pair = (np + per_block - 1) / per_block;
+    if (h->form == MG_MIXED) h->nblk_pair = (int)(((long)np * h->pair_team + kPairThreads - 1) / kPairThreads);
     h->nblk_bond = (np + kThreads - 1) / kThreads;
     h->nblk_surf = (np + kThreads - 1) / kThreads;
     // rec partials: SPME z-pass blocks or std k-vectors; sized by the caller
@@ -337,6 +710,10 @@ int mg_forces_init(mg_handle *h) {
     MG_CUDA(h, cudaMemsetAsync(h->d_uout, 0, sizeof(double) * (h->nptpt + 1 + 8), h->st));
     MG_CUDA(h, cudaMalloc(&h->d_forceo, sizeof(double) * 3 * np));
     if (h->form == MG_MIXED) {
+        for (int m = 0; m < 3; ++m)
+            if (h->ncell[m] >= 1024) return mg_fail(h, MG_ERR_UNSUPPORTED, "more than 1023 cells per edge");
+        MG_CUDA(h, cudaMalloc(&h->d_pos_f, sizeof(float4) * np));
+        MG_CUDA(h, cudaMalloc(&h->d_cell_s, sizeof(int) * np));
         MG_CUDA(h, cudaMalloc(&h->d_ffx, sizeof(long long) * 3 * np));
     } else {
         MG_CUDA(h, cudaMalloc(&h->d_force, sizeof(double) * 3 * np));
@@ -348,9 +725,22 @@ int mg_forces_init(mg_handle *h) {
 int mg_utotal_launch(mg_handle *h) {
     int np = h->np;
     bool mixed = h->form == MG_MIXED;
+    CellGeom cg;
+    for (int m = 0; m < 3; ++m) {
+        cg.nc[m] = h->ncell[m];
+        cg.size[m] = h->cellSize[m];
+        cg.half[m] = h->boxlen2[m];
+        cg.sizef[m] = (float)h->cellSize[m];
+        cg.lenf[m] = (float)h->boxlen[m];
+        cg.halff[m] = (float)h->boxlen2[m];
+    }
     MG_TRY(mg_phase_begin(h, "prepare"));
-    k_prepare<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(h->d_ro, h->d_perm, h->d_type,
-                                                                     np, h->d_pos_s);
+    if (mixed)
+        k_prepare_f32<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
+            h->d_ro, h->d_perm, h->d_type, h->d_cellof, np, cg, h->d_pos_f, h->d_cell_s);
+    else
+        k_prepare<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(h->d_ro, h->d_perm, h->d_type,
+                                                                         np, h->d_pos_s);
     MG_TRY(mg_phase_end(h, "prepare"));
     MG_TRY(mg_phase_begin(h, "pair"));
     PairArgs a;
@@ -361,13 +751,19 @@ int mg_utotal_launch(mg_handle *h) {
     a.np = np;
     a.npt = h->npt;
     a.nptpt = h->nptpt;
+    a.nrec = h->nrec;
+    a.nbins = h->nbins;
     a.pairidx = h->d_pairidx;
-    a.ubuf = h->d_ubuf;
-    a.ubuf_f = h->d_ubuf_f;
+    a.zlow = h->d_zlow;
+    a.coef = h->d_coef;
+    a.coef_f = h->d_coef_f;
     a.tab_start = h->d_tab_start;
     a.tab_n = h->d_tab_n;
     a.r2umin = h->d_r2umin;
     a.r2atat = h->d_r2atat;
+    a.bin_z0 = h->d_bin_z0;
+    a.bin_inv = h->d_bin_inv;
+    a.bin_kstart = h->d_bin_kstart;
     for (int m = 0; m < 3; ++m) {
         a.box.len[m] = h->boxlen[m];
         a.box.half[m] = h->boxlen2[m];
@@ -379,8 +775,51 @@ int mg_utotal_launch(mg_handle *h) {
     a.ffx = h->d_ffx;
     a.part = h->d_part + h->part_pair;
     a.err = h->d_err;
-    if (mixed) k_pair<true><<<h->nblk_pair, kPairThreads, 0, h->st>>>(a);
-    else k_pair<false><<<h->nblk_pair, kPairThreads, 0, h->st>>>(a);
+    a.tab_in_smem = h->pair_tab_smem;
+    size_t sm = h->pair_smem;
+    int nb = h->nblk_pair;
+    if (mixed) {
+        PairArgsF f;
+        f.pos_f = h->d_pos_f;
+        f.cell_s = h->d_cell_s;
+        f.perm = h->d_perm;
+        f.nnb = h->d_nnb;
+        f.nbr = h->d_nbr;
+        f.np = np;
+        f.npt = h->npt;
+        f.nptpt = h->nptpt;
+        f.nrec = h->nrec;
+        f.nbins = h->nbins;
+        f.pairidx = h->d_pairidx;
+        f.tab_start = h->d_tab_start;
+        f.tab_n = h->d_tab_n;
+        f.zlow_f = h->d_f32_tabs;
+        f.r2umin_f = h->d_f32_tabs + h->nrec;
+        f.r2atat_f = h->d_f32_tabs + h->nrec + h->nptpt;
+        f.bin_z0_f = h->d_f32_tabs + h->nrec + 2 * h->nptpt;
+        f.bin_inv_f = h->d_f32_tabs + h->nrec + 3 * h->nptpt;
+        f.coef_f = h->d_coef_f;
+        f.bin_kstart = h->d_bin_kstart;
+        f.tab_in_smem = h->pair_tab_smem;
+        f.g = cg;
+        f.rcut2 = (float)h->rcut2;
+        f.cellcut = a.cellcut;
+        f.ffx = h->d_ffx;
+        f.part = h->d_part + h->part_pair;
+        f.err = h->d_err;
+        int team = h->pair_team, nbt = (int)(((long)np * team + kPairThreads - 1) / kPairThreads);
+        switch (team) {
+        case 1: k_pair_f32<1><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        case 2: k_pair_f32<2><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        case 4: k_pair_f32<4><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        case 8: k_pair_f32<8><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        case 16: k_pair_f32<16><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        default: k_pair_f32<32><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        }
+    } else {
+        if (h->pair_warp) k_pair<false, true><<<nb, kPairThreads, sm, h->st>>>(a);
+        else k_pair<false, false><<<nb, kPairThreads, sm, h->st>>>(a);
+    }
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "pair"));
 

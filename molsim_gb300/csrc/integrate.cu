@@ -37,33 +37,60 @@ __device__ __forceinline__ double pbc_wrap(double d, double half, double len, do
     return d;
 }
 
-// candidate pairs: flag, rx, ry (state of the stream is rng[0])
-__global__ void k_bd_cand(const int *__restrict__ rng, int ncand, unsigned *__restrict__ flag,
-                          double2 *__restrict__ val) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncand) return;
+constexpr int kCandBlock = 1024;   // candidates per block
+
+// Candidate pairs c = blockIdx.x*1024 + threadIdx.x use LCG states 2c+1, 2c+2
+// after rng[0].  Each block compacts its accepted pairs in candidate order
+// and stores the two deviates (rx*fac, ry*fac) of each, its accepted count
+// in blkcnt and the candidate index of each accepted pair in cidx.
+template <bool F32>
+__global__ void __launch_bounds__(kCandBlock) k_bd_cand(const int *__restrict__ rng, int ncand,
+                                                         double2 *__restrict__ gval,
+                                                         int *__restrict__ cidx,
+                                                         int *__restrict__ blkcnt) {
+    __shared__ int wcount[kCandBlock / 32];
+    int c = blockIdx.x * kCandBlock + threadIdx.x;
     const double f = 1.0 / 2147483648.0;
-    unsigned s0 = (unsigned)rng[0];
-    unsigned s1 = (unsigned)(((unsigned long long)s0 * lcg_pow(2ull * c + 1)) & kMask31);
-    unsigned s2 = (s1 * kLcgA) & kMask31;
-    double rx = 2.0 * (f * (double)s1 - 0.5);
-    double ry = 2.0 * (f * (double)s2 - 0.5);
-    double r = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry));
-    flag[c] = (r < 1.0) ? 1u : 0u;
-    val[c] = make_double2(rx, ry);
-}
-
-__global__ void k_bd_compact(const unsigned *__restrict__ flag, const int *__restrict__ rank,
-                             int ncand, int *__restrict__ cidx) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncand && flag[c]) cidx[rank[c]] = c;
-}
-
-__device__ __forceinline__ double gauss_of_pair(const double2 *__restrict__ val, int c, int comp) {
-    double2 v = val[c];
-    double r = __dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y));
-    double fac = sqrt(-2.0 * log(r) / r);
-    return (comp == 0 ? v.x : v.y) * fac;
+    bool acc = false;
+    double rx = 0.0, ry = 0.0, r = 2.0;
+    if (c < ncand) {
+        unsigned s0 = (unsigned)rng[0];
+        unsigned s1 = (unsigned)(((unsigned long long)s0 * lcg_pow(2ull * c + 1)) & kMask31);
+        unsigned s2 = (s1 * kLcgA) & kMask31;
+        rx = 2.0 * (f * (double)s1 - 0.5);
+        ry = 2.0 * (f * (double)s2 - 0.5);
+        r = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry));
+        acc = r < 1.0;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned ball = __ballot_sync(0xffffffffu, acc);
+    if (lane == 0) wcount[w] = __popc(ball);
+    __syncthreads();
+    if (w == 0) {
+        int x = wcount[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        wcount[lane] = x;   // inclusive prefix over warps
+        if (lane == 31) blkcnt[blockIdx.x] = x;
+    }
+    __syncthreads();
+    if (acc) {
+        int rank = (w ? wcount[w - 1] : 0) + __popc(ball & ((1u << lane) - 1u));
+        size_t o = (size_t)blockIdx.x * kCandBlock + rank;
+        double2 g;
+        if (F32) {   // mixed form: the Box-Muller transform in FP32
+            float rf = (float)r;
+            float fac = sqrtf(-2.0f * __logf(rf) / rf);
+            g = make_double2((double)((float)rx * fac), (double)((float)ry * fac));
+        } else {     // GauRandom: fac = sqrt(-two*log(r)/r)
+            double fac = sqrt(-2.0 * log(r) / r);
+            g = make_double2(rx * fac, ry * fac);
+        }
+        gval[o] = g;
+        cidx[o] = c;
+    }
 }
 
 struct BdArgs {
@@ -71,21 +98,53 @@ struct BdArgs {
     const double *forceo, *fac1, *fac2;
     const int *type;
     int np;
-    int *rng;               // [0] iseed, [1] flag
+    int *rng;               // [0] iseed, [1] flag (1: next call draws a new pair)
     double *save;
-    const int *cidx, *rank_total;   // rank_total = scan out[ncand]
-    const double2 *val;
-    int ncand;
+    const double2 *gval;
+    const int *cidx, *blkcnt;
+    int nblk;
     mg_box box;
     int *err;
 };
 
+// prefix of the per-block accepted counts in shared memory (inclusive)
+__device__ __forceinline__ void load_block_prefix(const int *__restrict__ blkcnt, int nblk, int *sp) {
+    if (threadIdx.x < 32) {
+        int carry = 0;
+        for (int b0 = 0; b0 < nblk; b0 += 32) {
+            int b = b0 + threadIdx.x;
+            int x = (b < nblk) ? blkcnt[b] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if ((int)threadIdx.x >= o) x += y;
+            }
+            if (b < nblk) sp[b] = carry + x;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+    }
+    __syncthreads();
+}
+
+// accepted pair j -> offset of its stored deviates (-1 if the stream ran short)
+__device__ __forceinline__ long pair_slot(const int *sp, int nblk, int j) {
+    if (nblk == 0 || j >= sp[nblk - 1]) return -1;
+    int lo = 0, hi = nblk - 1;   // first block with inclusive prefix > j
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (sp[mid] > j) hi = mid;
+        else lo = mid + 1;
+    }
+    int before = lo ? sp[lo - 1] : 0;
+    return (long)lo * kCandBlock + (j - before);
+}
+
 // BDStep: drostep = fac1*forceo + fac2*GauRandom; ro += drostep; PBC
 __global__ void k_bd_move(BdArgs a) {
+    extern __shared__ int sp[];
+    load_block_prefix(a.blkcnt, a.nblk, sp);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.np) return;
     int off = (a.rng[1] == 0) ? 1 : 0;   // a saved deviate is pending
-    int naccept = *a.rank_total;
     int t = a.type[p];
     double f1 = a.fac1[t], f2 = a.fac2[t];
     for (int m = 0; m < 3; ++m) {
@@ -94,12 +153,14 @@ __global__ void k_bd_move(BdArgs a) {
         if (off && g == 0) {
             dev = *a.save;
         } else {
-            int hh = g - off, j = hh >> 1;
-            if (j >= naccept) {
-                mg_dev_error(a.err, MG_ERR_TIMEOUT, p + 1, j, naccept);
+            int hh = g - off;
+            long slot = pair_slot(sp, a.nblk, hh >> 1);
+            if (slot < 0) {
+                mg_dev_error(a.err, MG_ERR_TIMEOUT, p + 1, hh >> 1, a.nblk);
                 dev = 0.0;
             } else {
-                dev = gauss_of_pair(a.val, a.cidx[j], hh & 1);
+                double2 v = a.gval[slot];
+                dev = (hh & 1) ? v.y : v.x;
             }
         }
         double d = __dadd_rn(__dmul_rn(f1, a.forceo[3 * p + m]), __dmul_rn(f2, dev));
@@ -109,20 +170,22 @@ __global__ void k_bd_move(BdArgs a) {
     }
 }
 
-// advance the GauRandom state past this step's deviates (one thread)
+// advance the GauRandom state past this step's deviates (one warp)
 __global__ void k_bd_state(BdArgs a) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    extern __shared__ int sp[];
+    load_block_prefix(a.blkcnt, a.nblk, sp);
+    if (threadIdx.x != 0) return;
     int off = (a.rng[1] == 0) ? 1 : 0;
-    int G = 3 * a.np, need = G - off;
+    int need = 3 * a.np - off;
     int J = (need + 1) / 2;
-    int naccept = *a.rank_total;
-    if (J > naccept) return;   // k_bd_move has flagged the error
-    int clast = a.cidx[J - 1];
+    long slot = pair_slot(sp, a.nblk, J - 1);
+    if (slot < 0) return;   // k_bd_move has flagged the error
+    int clast = a.cidx[slot];
     unsigned s0 = (unsigned)a.rng[0];
     unsigned sn = (unsigned)(((unsigned long long)s0 * lcg_pow(2ull * (clast + 1))) & kMask31);
     a.rng[0] = (int)sn;
     if (need & 1) {
-        *a.save = gauss_of_pair(a.val, clast, 1);
+        *a.save = a.gval[slot].y;
         a.rng[1] = 0;
     } else {
         a.rng[1] = 1;
@@ -185,11 +248,13 @@ int mg_integrate_bd_setup(mg_handle *h, const double *fac1, const double *fac2, 
         MG_CUDA(h, cudaMalloc(&h->d_rng, sizeof(int) * 4));
         MG_CUDA(h, cudaMalloc(&h->d_rng_save, sizeof(double)));
         int J = (3 * np + 1) / 2 + 1;
-        h->ncand = (int)(J * 1.35) + 4096;
-        MG_CUDA(h, cudaMalloc(&h->d_cflag, sizeof(unsigned) * h->ncand));
+        // acceptance is pi/4: 1.35 J + 4096 candidates leave a margin of
+        // hundreds of standard deviations
+        int nblk = ((int)(J * 1.35) + 4096 + kCandBlock - 1) / kCandBlock;
+        h->ncand = nblk * kCandBlock;
         MG_CUDA(h, cudaMalloc(&h->d_cval, sizeof(double2) * h->ncand));
         MG_CUDA(h, cudaMalloc(&h->d_cidx, sizeof(int) * h->ncand));
-        MG_CUDA(h, cudaMalloc(&h->d_scan_tmp, sizeof(int) * (h->ncand + 1)));
+        MG_CUDA(h, cudaMalloc(&h->d_scan_tmp, sizeof(int) * nblk));
     }
     MG_CUDA(h, cudaMemcpy(h->d_fac1, fac1, sizeof(double) * npt, cudaMemcpyHostToDevice));
     MG_CUDA(h, cudaMemcpy(h->d_fac2, fac2, sizeof(double) * npt, cudaMemcpyHostToDevice));
@@ -220,7 +285,7 @@ int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, cons
 
 // one BD step (BDStep, UTotal, list check) queued on the stream
 int mg_integrate_bd_step_launch(mg_handle *h) {
-    int np = h->np, nc = h->ncand;
+    int np = h->np, nc = h->ncand, nblk = nc / kCandBlock;
     BdArgs a;
     a.ro = h->d_ro;
     a.drostep = h->d_drostep;
@@ -231,24 +296,28 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     a.np = np;
     a.rng = h->d_rng;
     a.save = h->d_rng_save;
+    a.gval = (const double2 *)h->d_cval;
     a.cidx = h->d_cidx;
-    a.rank_total = h->d_scan_tmp + nc;
-    a.val = (const double2 *)h->d_cval;
-    a.ncand = nc;
+    a.blkcnt = h->d_scan_tmp;
+    a.nblk = nblk;
     a.box = box_of(h);
     a.err = h->d_err;
+    size_t sm = sizeof(int) * nblk;
+    MG_TRY(mg_phase_begin(h, "bd_rng"));
+    if (h->form == MG_MIXED)
+        k_bd_cand<true><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
+    else
+        k_bd_cand<false><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
+    MG_TRY(mg_phase_end(h, "bd_rng"));
     MG_TRY(mg_phase_begin(h, "bd_move"));
-    k_bd_cand<<<(nc + 255) / 256, 256, 0, h->st>>>(h->d_rng, nc, h->d_cflag, (double2 *)h->d_cval);
-    mg_scan_exclusive(h, (const int *)h->d_cflag, h->d_scan_tmp, nc, nullptr);
-    k_bd_compact<<<(nc + 255) / 256, 256, 0, h->st>>>(h->d_cflag, h->d_scan_tmp, nc, h->d_cidx);
-    k_bd_move<<<(np + 255) / 256, 256, 0, h->st>>>(a);
-    k_bd_state<<<1, 32, 0, h->st>>>(a);
-    h->launches += 4;
+    k_bd_move<<<(np + 255) / 256, 256, sm, h->st>>>(a);
+    k_bd_state<<<1, 32, sm, h->st>>>(a);
+    h->launches += 3;
     MG_TRY(mg_phase_end(h, "bd_move"));
     MG_TRY(mg_utotal_launch(h));
     MG_TRY(mg_phase_begin(h, "list"));
     MG_TRY(mg_lists_check(h));
-    MG_TRY(mg_lists_build(h, true));
+    if (!h->use_cond) MG_TRY(mg_lists_build(h, true));
     MG_TRY(mg_phase_end(h, "list"));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
@@ -277,7 +346,7 @@ int mg_integrate_md_step_launch(mg_handle *h) {
     h->launches++;
     MG_TRY(mg_phase_begin(h, "list"));
     MG_TRY(mg_lists_check(h));
-    MG_TRY(mg_lists_build(h, true));
+    if (!h->use_cond) MG_TRY(mg_lists_build(h, true));
     MG_TRY(mg_phase_end(h, "list"));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;

@@ -212,19 +212,27 @@ __global__ void k_chk_accum(const double *__restrict__ drostep, double *__restri
     }
 }
 
+// Pass 2 per block: the largest value that was not a new running maximum,
+// given the maximum of all earlier blocks.  The last block to finish
+// combines the blocks (threadfence + counter) and sets the rebuild flag and,
+// inside a captured step, the graph condition that runs the rebuild.
 __global__ void k_chk_second(const double *__restrict__ r2in, const double *__restrict__ blkmax,
-                             double *__restrict__ blk2, int np) {
+                             double *__restrict__ blk2, int np, int nblk, double drnlist,
+                             int *__restrict__ flag, int *__restrict__ counter, int use_cond,
+                             cudaGraphConditionalHandle cond) {
     __shared__ double wmax[32], red[32];
     __shared__ double pb;
+    __shared__ bool last;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (threadIdx.x == 0) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w == 0) {   // maximum over all earlier blocks, one warp
         double m = 0.0;
-        for (int b = 0; b < (int)blockIdx.x; ++b) m = fmax(m, blkmax[b]);
-        pb = m;
+        for (int b = lane; b < (int)blockIdx.x; b += 32) m = fmax(m, blkmax[b]);
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) pb = m;
     }
     double r2 = (p < np) ? r2in[p] : 0.0;
     // inclusive prefix max within the warp
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     double v = r2;
     for (int o = 1; o < 32; o <<= 1) {
         double y = __shfl_up_sync(0xffffffffu, v, o);
@@ -250,23 +258,32 @@ __global__ void k_chk_second(const double *__restrict__ r2in, const double *__re
     for (int o = 16; o > 0; o >>= 1) cand = fmax(cand, __shfl_xor_sync(0xffffffffu, cand, o));
     if (lane == 0) red[w] = cand;
     __syncthreads();
-    if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) {
         int nw = blockDim.x >> 5;
-        double x = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-        if (threadIdx.x == 0) blk2[blockIdx.x] = x;
+        double x = 0.0;
+        for (int k = 0; k < nw; ++k) x = fmax(x, red[k]);
+        blk2[blockIdx.x] = x;
+        __threadfence();
+        last = (atomicAdd(counter, 1) == nblk - 1);
     }
-}
-
-__global__ void k_chk_final(const double *__restrict__ blkmax, const double *__restrict__ blk2,
-                            int nblk, double drnlist, int *__restrict__ flag) {
-    if (threadIdx.x != 0) return;
+    __syncthreads();
+    if (!last || threadIdx.x >= 32) return;
+    __threadfence();
     double m1 = 0.0, m2 = 0.0;
-    for (int b = 0; b < nblk; ++b) {
-        m1 = fmax(m1, blkmax[b]);
-        m2 = fmax(m2, blk2[b]);
+    for (int b = lane; b < nblk; b += 32) {
+        m1 = fmax(m1, ((volatile const double *)blkmax)[b]);
+        m2 = fmax(m2, ((volatile const double *)blk2)[b]);
     }
-    flag[0] = (sqrt(m1) + sqrt(m2) > drnlist) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+        m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    }
+    if (lane == 0) {
+        int f = (sqrt(m1) + sqrt(m2) > drnlist) ? 1 : 0;
+        flag[0] = f;
+        *counter = 0;
+        if (use_cond) cudaGraphSetConditional(cond, (unsigned)f);
+    }
 }
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
@@ -473,9 +490,10 @@ int mg_lists_check(mg_handle *h) {
     double *r2 = h->d_blkmax + 2 * nb;
     k_chk_accum<<<nb, 1024, 0, h->st>>>(h->d_drostep, h->d_drosum, r2, h->d_blkmax, np,
                                         h->d_rebuild);
-    k_chk_second<<<nb, 1024, 0, h->st>>>(r2, h->d_blkmax, h->d_blkmax + nb, np);
-    k_chk_final<<<1, 32, 0, h->st>>>(h->d_blkmax, h->d_blkmax + nb, nb, h->drnlist, h->d_rebuild);
-    h->launches += 3;
+    k_chk_second<<<nb, 1024, 0, h->st>>>(r2, h->d_blkmax, h->d_blkmax + nb, np, nb, h->drnlist,
+                                         h->d_rebuild, h->d_rebuild + 1, h->use_cond ? 1 : 0,
+                                         h->cond);
+    h->launches += 2;
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }

@@ -54,6 +54,15 @@ struct mg_handle {
     float *d_ubuf_f = nullptr;
     int *d_tab_start = nullptr, *d_tab_n = nullptr;   // per pair: first record (0-based double offset / 12), count
     int nbuf = 0;
+    // pair kernel tables: interval lower ends, coefficients, direct-index bins
+    int nrec = 0, nbins = 0, pair_tab_smem = 0, pair_warp = 0, pair_team = 1;
+    size_t pair_smem = 0;
+    double *d_zlow = nullptr, *d_coef = nullptr, *d_bin_z0 = nullptr, *d_bin_inv = nullptr;
+    float *d_coef_f = nullptr;
+    unsigned short *d_bin_kstart = nullptr;
+    float *d_f32_tabs = nullptr;     // mixed: zlow, r2umin, r2atat, bin z0, bin inverse width
+    float4 *d_pos_f = nullptr;       // mixed: cell-relative FP32 positions in slot order
+    int *d_cell_s = nullptr;         // mixed: packed cell coordinates in slot order
 
     // ---- cells and Verlet list -----------------------------------------
     int ncell[3] = {1, 1, 1}, ncelltot = 1;
@@ -102,6 +111,16 @@ struct mg_handle {
     float *d_mf_f = nullptr, *d_ew_f = nullptr, *d_vw_f = nullptr;
     void *d_tw = nullptr;           // twiddles exp(-2 pi i m/n), m < n
     int fft_tx = 0, fft_tiles = 0;
+    int brick = 0, nbrick_edge = 0, nbricks = 0;
+    size_t spread_smem = 0, gather_smem = 0;
+    int fx_shift = 30;
+    int spread_wpb = 4;             // spread: bricks (warps) per block
+    int spread_chunk = 256;         // particles staged per pass of the spread              // mixed spread: weights scaled by 2^fx_shift into int32
+    int *d_brick_count = nullptr, *d_brick_perm = nullptr, *d_brick_rank = nullptr, *d_brick_of = nullptr;
+    int *d_brick_start = nullptr;
+    void *d_tiles = nullptr;        // per-brick spread tiles (mesh type)
+    int *d_corner = nullptr;        // [3][np] stamp corner per particle and dimension
+    void *d_spl_w = nullptr, *d_spl_dw = nullptr;   // [3][order][np] B-spline values, derivatives
     double *d_Qref = nullptr;       // MC: charge mesh of the accepted state (FP64)
     double *d_phi = nullptr;        // MC: potential mesh of the accepted state
     double *d_gker = nullptr;       // MC: real-space kernel g (nmesh^3)
@@ -138,6 +157,10 @@ struct mg_handle {
 
     // ---- graphs and timing -----------------------------------------------------
     cudaGraphExec_t g_bd = nullptr, g_md = nullptr;
+    // while a step is captured, the list check sets a graph condition that
+    // runs the (otherwise skipped) rebuild body
+    bool use_cond = false;
+    cudaGraphConditionalHandle cond = 0;
     int kernels_bd = 0, kernels_md = 0;
     bool timing = false;
     std::vector<mg_phase> phases;
@@ -196,7 +219,7 @@ int mg_cells_export(mg_handle *h, int32_t *ncell, int32_t *cellip);
 int mg_mc_cells_set(mg_handle *h);
 int mg_mc_cells_update(mg_handle *h, int ip);
 
-int mg_forces_init(mg_handle *h);
+int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int *count);
 int mg_utotal_launch(mg_handle *h);                    // queue a full UTotal on the stream
 int mg_utotal_fetch(mg_handle *h, double *forceo, double *u_twob, double *uout);
 

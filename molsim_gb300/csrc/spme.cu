@@ -6,18 +6,24 @@
 // file has its own FFT.
 //
 // Pipeline per UTotal (mesh Q[z][y][x], half spectrum F[z][y][kx], kx<=n/2):
-//   spread   B-spline stamp of every charge into Q (FP64 atomics, or 64-bit
-//            fixed point in the mixed form, which makes the mesh and
-//            everything after it bit-reproducible)
+//   bricks   particles binned by the mesh brick (B^3 points) that holds the
+//            upper corner of their B-spline stamp (count, prefix, scatter)
+//   spread   one CTA per brick: every thread owns one row of the brick's tile
+//            (the brick plus an order-1 halo) in shared memory and adds the
+//            stamps crossing it, without atomics; 64-bit fixed point in the
+//            mixed form (bit-reproducible), FP64 in the plain form
+//   fold     each mesh point sums the (at most 8) tiles covering it
 //   x pass   r2c along x; two real lines are packed into one complex line
 //   y pass   complex FFT along y, tiles of TX consecutive kx columns
 //   z pass   complex FFT along z, then the influence function (energy, virial,
 //            multiply by meshfac) and the inverse z FFT while the column is
 //            still in shared memory
 //   y pass   inverse; x pass c2r inverse (FFTW's unnormalised convention)
-//   gather   force from the potential mesh with separable B-spline sums
+//   gather   one CTA per brick stages the potential tile in shared memory;
+//            separable B-spline sums per particle
 // The FFTs are radix-4 Stockham (one radix-2 stage when log2 n is odd) in
 // shared memory; twiddles come from a host table computed in long double.
+#include <algorithm>
 #include <cmath>
 
 #include "mg_internal.cuh"
@@ -203,7 +209,7 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
         const T *mf = (const T *)cv.mf, *ew = (const T *)cv.ew, *vw = (const T *)cv.vw;
         int ky = blockIdx.y;
         int fy = min(ky, n - ky);
-        double e_acc = 0.0, v_acc = 0.0;
+        T e_t = 0, v_t = 0;   // per-thread sums in the mesh type, block sums in FP64
         for (int e = threadIdx.x; e < tx * n; e += blockDim.x) {
             int t = e / tx, c = e % tx;
             int kx = kx0 + c;
@@ -212,19 +218,19 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
             size_t id = ((size_t)fz * nh + fy) * nh + kx;
             V f = R[t * tx + c];
             T p2 = f.x * f.x + f.y * f.y;
-            e_acc += (double)(p2 * ew[id]);
-            v_acc -= (double)(p2 * vw[id]);
+            e_t += p2 * ew[id];
+            v_t -= p2 * vw[id];
             T m = mf[id];
             f.x *= m;
             f.y *= m;
             R[t * tx + c] = f;
         }
         int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-        for (int o = 16; o > 0; o >>= 1) {
-            e_acc += __shfl_down_sync(0xffffffffu, e_acc, o);
-            v_acc += __shfl_down_sync(0xffffffffu, v_acc, o);
+        for (int o = 16; o > 0; o >>= 1) {   // warp sums in the mesh type, FP64 across warps
+            e_t += __shfl_down_sync(0xffffffffu, e_t, o);
+            v_t += __shfl_down_sync(0xffffffffu, v_t, o);
         }
-        if (lane == 0) { red[w] = e_acc; red[32 + w] = v_acc; }
+        if (lane == 0) { red[w] = (double)e_t; red[32 + w] = (double)v_t; }
         __syncthreads();
         if (threadIdx.x == 0) {
             double se = 0.0, sv = 0.0;
@@ -244,162 +250,356 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
 }
 
 // ---- B-spline (CardinalBSpline, mollib.F90:1629-1685) -----------------------
-template <typename T>
-__device__ __forceinline__ int bspline(int order, T pos_frac, int kmax_in, T *v, T *dv) {
-    T x = pos_frac;
-    T last[MG_MAX_ORDER];
+// values v[i] = M(x + i) ... in the reference's order (v[0] = x for order 2)
+// and first derivatives dv, for the fractional mesh coordinate x
+template <typename T, int ORDER>
+__device__ __forceinline__ void bspline_o(T x, T *v, T *dv) {
+    T last[ORDER];
     v[0] = x;
     v[1] = (T)1 - x;
-    for (int i = 2; i < order; ++i) v[i] = (T)0;
-    for (int i = 0; i < order; ++i) last[i] = (T)0;
-    for (int nn = 3; nn <= order; ++nn) {
+#pragma unroll
+    for (int i = 2; i < ORDER; ++i) v[i] = (T)0;
+#pragma unroll
+    for (int i = 0; i < ORDER; ++i) last[i] = (T)0;
+#pragma unroll
+    for (int nn = 3; nn <= ORDER; ++nn) {
+#pragma unroll
         for (int i = 0; i < nn - 1; ++i) last[i] = v[i];
-        T inv = (T)1 / (T)(nn - 1);
+        const T inv = (T)1 / (T)(nn - 1);
         v[0] = x * last[0] * inv;
+#pragma unroll
         for (int i = 1; i <= nn - 2; ++i) {
-            T a = (T)i + x;
-            v[i] = (a * last[i] + ((T)nn - a) * last[i - 1]) * inv;
+            T aa = (T)i + x;
+            v[i] = (aa * last[i] + ((T)nn - aa) * last[i - 1]) * inv;
         }
         v[nn - 1] = ((T)1 - x) * last[nn - 2] * inv;
     }
     dv[0] = last[0];
-    for (int i = 1; i <= order - 2; ++i) dv[i] = last[i] - last[i - 1];
-    dv[order - 1] = -last[order - 2];
-    return kmax_in;
+#pragma unroll
+    for (int i = 1; i <= ORDER - 2; ++i) dv[i] = last[i] - last[i - 1];
+    dv[ORDER - 1] = -last[ORDER - 2];
 }
 
 struct SplineArgs {
     const double *ro, *az;
-    int np, order, n;
+    int np, order, n, n_log;
     double dkdr[3];
 };
 
-// stamp origin and spline weights of particle p in dimension m
+// Spline data of every particle, once per call (the only FP64 of the mesh
+// path: position -> mesh coordinate).  Layout: corner[m*np + p] (stamp
+// upper corner, meshmax of the reference), w and dw[(m*ORDER + i)*np + p].
+template <typename T, int ORDER>
+__global__ void k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__restrict__ w,
+                                 T *__restrict__ dw) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.np) return;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        double pos = a.dkdr[m] * a.ro[3 * p + m];
+        double fl = floor(pos);
+        int mm = (int)fl % a.n;
+        corner[m * a.np + p] = mm < 0 ? mm + a.n : mm;
+        T v[ORDER], d[ORDER];
+        bspline_o<T, ORDER>((T)(pos - fl), v, d);
+#pragma unroll
+        for (int i = 0; i < ORDER; ++i) {
+            w[(size_t)(m * ORDER + i) * a.np + p] = v[i];
+            dw[(size_t)(m * ORDER + i) * a.np + p] = d[i];
+        }
+    }
+}
+
+// ---- brick-sorted spread -------------------------------------------------------
+// The mesh is cut into bricks of B^3 points.  A particle belongs to the brick
+// holding the upper corner of its stamp; the stamp then lies in that brick's
+// tile (the brick extended by order-1 points towards lower indices).
+struct BrickArgs {
+    int n, B, nb;          // mesh edge, brick edge, bricks per edge (powers of 2)
+    int ln, lB, lnb;       // their log2
+    int tile;              // B + order - 1
+    int nbricks;
+    float fx_scale;        // mixed form: stamp weights to 32-bit integers (2^k)
+    float fx_inv;
+    int *count, *start, *perm, *rank, *brick;
+};
+
+__global__ void k_brick_count(const int *__restrict__ corner, int np, BrickArgs b) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int bx = corner[p] >> b.lB, by = corner[np + p] >> b.lB, bz = corner[2 * np + p] >> b.lB;
+    int id = (((bz << b.lnb) + by) << b.lnb) + bx;
+    b.brick[p] = id;
+    b.rank[p] = atomicAdd(&b.count[id], 1);
+}
+
+// exclusive prefix of the brick counts (one block of 1024 threads); the
+// counts are cleared for the next call
+__global__ void __launch_bounds__(1024) k_brick_prefix(BrickArgs b) {
+    __shared__ int wsum[32];
+    int nb = b.nbricks, per = (nb + 1023) / 1024;
+    int lo = threadIdx.x * per, hi = min(nb, lo + per);
+    int s = 0;
+    for (int i = lo; i < hi; ++i) s += b.count[i];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int x = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        wsum[lane] = x;
+    }
+    __syncthreads();
+    int run = v - s + (w ? wsum[w - 1] : 0);
+    for (int i = lo; i < hi; ++i) {
+        b.start[i] = run;
+        run += b.count[i];
+        b.count[i] = 0;
+    }
+    if (threadIdx.x == 1023) b.start[nb] = run;
+}
+
+__global__ void k_brick_scatter(int np, BrickArgs b) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < np) b.perm[b.start[b.brick[p]] + b.rank[p]] = p;
+}
+
+constexpr int kSpreadWarps = 4;   // bricks (warps) per block
+
+// spread: one warp per brick owns the brick's tile in shared memory and adds
+// the particles one after another, its lanes covering the order^3 points of
+// a stamp (all distinct), so plain read-modify-writes are race free.  ACC is
+// a 64-bit fixed-point integer in the mixed form (exact, independent of the
+// particle order) or double.  The tile is written to scratch in the mesh type.
+template <typename T, typename ACC, int ORDER, int B>
+__global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, const int *__restrict__ corner,
+                                                                   const T *__restrict__ w,
+                                                                   const double *__restrict__ az, int np,
+                                                                   T *__restrict__ tiles) {
+    constexpr int t = B + ORDER - 1, t3 = t * t * t, O3 = ORDER * ORDER * ORDER;
+    // per warp: the tile, then a staging area of 32 particles (corner
+    // offsets packed in one int, charge-weighted x, y and z weights)
+    struct Stage {
+        int off[32];
+        T wx[ORDER][32], wy[ORDER][32], wz[ORDER][32];
+    };
+    extern __shared__ __align__(16) unsigned char smem_sw[];
+    int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+    ACC *tile = reinterpret_cast<ACC *>(smem_sw) + (size_t)wib * t3;
+    Stage *stg = reinterpret_cast<Stage *>(smem_sw + (((size_t)nwb * t3 * sizeof(ACC) + 15) & ~(size_t)15)) + wib;
+    int brick = blockIdx.x * nwb + wib;
+    if (brick >= b.nbricks) return;
+    for (int k = lane; k < t3; k += 32) tile[k] = (ACC)0;
+    int mnb = b.nb - 1;
+    int bx = brick & mnb, by = (brick >> b.lnb) & mnb, bz = brick >> (2 * b.lnb);
+    int ox = bx * B - (ORDER - 1), oy = by * B - (ORDER - 1), oz = bz * B - (ORDER - 1);
+    int first = b.start[brick], last = b.start[brick + 1];
+    for (int q0 = first; q0 < last; q0 += 32) {
+        int cnt = min(32, last - q0);
+        __syncwarp();
+        if (lane < cnt) {   // stage one particle per lane
+            int p = b.perm[q0 + lane];
+            int cx = corner[p] - ox, cy = corner[np + p] - oy, cz = corner[2 * np + p] - oz;
+            stg->off[lane] = cx | (cy << 8) | (cz << 16);
+            T qp = (T)az[p];
+#pragma unroll
+            for (int i = 0; i < ORDER; ++i) {
+                stg->wx[i][lane] = qp * w[(size_t)i * np + p];
+                stg->wy[i][lane] = w[(size_t)(ORDER + i) * np + p];
+                stg->wz[i][lane] = w[(size_t)(2 * ORDER + i) * np + p];
+            }
+        }
+        __syncwarp();
+        for (int e = 0; e < cnt; ++e) {
+            int off = stg->off[e];
+            int base = ((off >> 16) * t + ((off >> 8) & 255)) * t + (off & 255);
+#pragma unroll
+            for (int pass = 0; pass < (O3 + 31) / 32; ++pass) {
+                int k = lane + 32 * pass;
+                if (k < O3) {
+                    int ix = k % ORDER, iy = (k / ORDER) % ORDER, iz = k / (ORDER * ORDER);
+                    T wt = stg->wx[ix][e] * stg->wy[iy][e] * stg->wz[iz][e];
+                    ACC *dst = tile + base - (iz * t + iy) * t - ix;
+                    if (sizeof(ACC) == 8 && sizeof(T) == 4)   // |wt * fx_scale| < 2^31 by choice of scale
+                        *dst += (ACC)(long long)__float2int_rn(wt * b.fx_scale);
+                    else
+                        *dst += (ACC)wt;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    T *out = tiles + (size_t)brick * t3;
+    for (int k = lane; k < t3; k += 32) {
+        ACC v = tile[k];
+        if (sizeof(ACC) == 8 && sizeof(T) == 4) {
+            long long x = (long long)v;   // 64-bit integer to float without the FP64 pipe
+            float hi = (float)(int)(x >> 32), lo = (float)(unsigned)(x & 0xffffffffll);
+            out[k] = (T)((hi * 4294967296.0f + lo) * b.fx_inv);
+        } else {
+            out[k] = (T)v;
+        }
+    }
+}
+
+// fold: every mesh point adds the tiles that cover it (its own brick and the
+// low halos of up to seven following bricks) in a fixed order
 template <typename T>
-__device__ __forceinline__ int particle_spline(const SplineArgs &a, int p, int m, T *v, T *dv) {
-    double pos = a.dkdr[m] * a.ro[3 * p + m];
-    double fl = floor(pos);
-    int kmax = (int)fl;
-    T x = (T)(pos - fl);
-    bspline<T>(a.order, x, kmax, v, dv);
-    int mm = kmax % a.n;
-    return mm < 0 ? mm + a.n : mm;
-}
-
-__global__ void k_spread_f64(SplineArgs a, double *__restrict__ Q) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.np) return;
-    double v[3][MG_MAX_ORDER], dv[MG_MAX_ORDER];
-    int mm[3];
-    for (int m = 0; m < 3; ++m) mm[m] = particle_spline<double>(a, p, m, v[m], dv);
-    int n = a.n, o = a.order;
-    double q = a.az[p];
-    for (int iz = 0; iz < o; ++iz) {
-        int nz = mm[2] - iz;
-        nz += (nz < 0) ? n : 0;
-        double qz = q * v[2][iz];
-        for (int iy = 0; iy < o; ++iy) {
-            int ny = mm[1] - iy;
-            ny += (ny < 0) ? n : 0;
-            double qyz = qz * v[1][iy];
-            double *row = Q + ((size_t)nz * n + ny) * n;
-            for (int ix = 0; ix < o; ++ix) {
-                int nx = mm[0] - ix;
-                nx += (nx < 0) ? n : 0;
-                atomicAdd(row + nx, qyz * v[0][ix]);
+__global__ void k_fold_tiles(const T *__restrict__ tiles, BrickArgs b, int order, T *__restrict__ Q) {
+    int B = b.B, t = b.tile, h = order - 1, mB = B - 1, mnb = b.nb - 1;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ((size_t)1 << (3 * b.ln))) return;
+    int mn = b.n - 1;
+    int x = (int)idx & mn, y = (int)(idx >> b.ln) & mn, z = (int)(idx >> (2 * b.ln));
+    int bx = x >> b.lB, by = y >> b.lB, bz = z >> b.lB, lx = x & mB, ly = y & mB, lz = z & mB;
+    size_t t3 = (size_t)t * t * t;
+    T sum = (T)0;
+    for (int ez = 0; ez < 2; ++ez) {
+        if (ez && lz < B - h) break;
+        int cz = ez ? lz - B + h : lz + h, kz = (bz + ez) & mnb;
+        for (int ey = 0; ey < 2; ++ey) {
+            if (ey && ly < B - h) break;
+            int cy = ey ? ly - B + h : ly + h, ky = (by + ey) & mnb;
+            for (int ex = 0; ex < 2; ++ex) {
+                if (ex && lx < B - h) break;
+                int cx = ex ? lx - B + h : lx + h, kx = (bx + ex) & mnb;
+                int brick = (((kz << b.lnb) + ky) << b.lnb) + kx;
+                sum += tiles[(size_t)brick * t3 + ((size_t)cz * t + cy) * t + cx];
             }
         }
     }
+    Q[idx] = sum;
 }
 
-__global__ void k_spread_fx(SplineArgs a, unsigned long long *__restrict__ Q) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.np) return;
-    float v[3][MG_MAX_ORDER], dv[MG_MAX_ORDER];
-    int mm[3];
-    for (int m = 0; m < 3; ++m) mm[m] = particle_spline<float>(a, p, m, v[m], dv);
-    int n = a.n, o = a.order;
-    float q = (float)a.az[p];
-    for (int iz = 0; iz < o; ++iz) {
-        int nz = mm[2] - iz;
-        nz += (nz < 0) ? n : 0;
-        float qz = q * v[2][iz];
-        for (int iy = 0; iy < o; ++iy) {
-            int ny = mm[1] - iy;
-            ny += (ny < 0) ? n : 0;
-            float qyz = qz * v[1][iy];
-            unsigned long long *row = Q + ((size_t)nz * n + ny) * n;
-            for (int ix = 0; ix < o; ++ix) {
-                int nx = mm[0] - ix;
-                nx += (nx < 0) ? n : 0;
-                long long fx = __float2ll_rn(qyz * v[0][ix] * 4294967296.0f);
-                atomicAdd(row + nx, (unsigned long long)fx);
-            }
-        }
-    }
-}
-
-// fixed-point mesh -> float mesh, clearing the accumulator for the next call
-__global__ void k_fx_to_float(unsigned long long *__restrict__ Qfx, float *__restrict__ Q, size_t n3) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n3) return;
-    long long v = (long long)Qfx[i];
-    Q[i] = (float)((double)v * MG_FX_INV);
-    Qfx[i] = 0ull;
-}
-
-// gather: esum = sum dM*M*M*phi over the stamp (energy.F90:1255-1285),
-// evaluated as separable row sums; force -= q*esum*dkdr*EpsiFourPi
-template <typename T, bool MIXED>
-__global__ void k_gather(SplineArgs a, const T *__restrict__ Q, double efp,
-                         double *__restrict__ force, long long *__restrict__ ffx) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.np) return;
-    T v[3][MG_MAX_ORDER], d[3][MG_MAX_ORDER];
-    int mm[3];
-    for (int m = 0; m < 3; ++m) mm[m] = particle_spline<T>(a, p, m, v[m], d[m]);
-    int n = a.n, o = a.order;
-    int xs[MG_MAX_ORDER];
-    for (int ix = 0; ix < o; ++ix) {
-        int nx = mm[0] - ix;
-        xs[ix] = nx + ((nx < 0) ? n : 0);
-    }
+// gather: a group of G lanes per particle (G = 8 for orders up to 8, else
+// 16; particles in cell-sorted order for mesh locality).  Lane j < ORDER of a
+// group owns the stamp plane iz = j: for each row iy it sums dM*phi and M*phi
+// along x; the group then combines.  E = sum dM*M*M*phi
+// (energy.F90:1255-1285); force -= q*E*dkdr*EpsiFourPi.
+template <typename T, bool MIXED, int ORDER>
+__global__ void __launch_bounds__(256) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
+                                                    const int *__restrict__ corner, const T *__restrict__ w,
+                                                    const T *__restrict__ dw, const T *__restrict__ Q,
+                                                    double efp, double *__restrict__ force,
+                                                    long long *__restrict__ ffx) {
+    constexpr int G = ORDER <= 8 ? 8 : 16;
+    int g = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G);
+    int j = threadIdx.x & (G - 1);
+    bool valid = g < a.np;
+    bool act = valid && j < ORDER;
+    int p = valid ? perm[g] : 0;
+    int np = a.np, n = a.n, mn = n - 1;
     T e0 = 0, e1 = 0, e2 = 0;
-    for (int iz = 0; iz < o; ++iz) {
-        int nz = mm[2] - iz;
-        nz += (nz < 0) ? n : 0;
-        T e0z = 0, e1z = 0, e2z = 0;
-        for (int iy = 0; iy < o; ++iy) {
-            int ny = mm[1] - iy;
-            ny += (ny < 0) ? n : 0;
-            const T *row = Q + ((size_t)nz * n + ny) * n;
-            T sx = 0, s0 = 0;
-            for (int ix = 0; ix < o; ++ix) {
-                T q = row[xs[ix]];
-                sx += d[0][ix] * q;
-                s0 += v[0][ix] * q;
-            }
-            e0z += v[1][iy] * sx;
-            e1z += d[1][iy] * s0;
-            e2z += v[1][iy] * s0;
+    if (act) {
+        T vx[ORDER], dx[ORDER];
+#pragma unroll
+        for (int i = 0; i < ORDER; ++i) {
+            vx[i] = w[(size_t)i * np + p];
+            dx[i] = dw[(size_t)i * np + p];
         }
-        e0 += v[2][iz] * e0z;
-        e1 += v[2][iz] * e1z;
-        e2 += d[2][iz] * e2z;
+        T vz = w[(size_t)(2 * ORDER + j) * np + p], dz = dw[(size_t)(2 * ORDER + j) * np + p];
+        int c0 = corner[p], c1 = corner[np + p], c2 = corner[2 * np + p];
+        const T *plane = Q + ((size_t)((c2 - j) & mn) << (2 * a.n_log));
+        T a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll
+        for (int iy = 0; iy < ORDER; ++iy) {
+            T vy = w[(size_t)(ORDER + iy) * np + p], dy = dw[(size_t)(ORDER + iy) * np + p];
+            const T *rw = plane + (size_t)((c1 - iy) & mn) * n;
+            T sx = 0, s0 = 0;
+#pragma unroll
+            for (int ix = 0; ix < ORDER; ++ix) {
+                T q = rw[(c0 - ix) & mn];
+                sx += dx[ix] * q;
+                s0 += vx[ix] * q;
+            }
+            a0 += vy * sx;
+            a1 += dy * s0;
+            a2 += vy * s0;
+        }
+        e0 = vz * a0;
+        e1 = vz * a1;
+        e2 = dz * a2;
     }
-    double q = a.az[p];
-    double f0 = -q * (double)e0 * a.dkdr[0] * efp;
-    double f1 = -q * (double)e1 * a.dkdr[1] * efp;
-    double f2 = -q * (double)e2 * a.dkdr[2] * efp;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        e0 += __shfl_xor_sync(0xffffffffu, e0, o, G);
+        e1 += __shfl_xor_sync(0xffffffffu, e1, o, G);
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o, G);
+    }
+    if (j != 0 || !valid) return;
     if (MIXED) {
-        ffx[3 * p + 0] += __double2ll_rn(f0 * MG_FX_SCALE);
-        ffx[3 * p + 1] += __double2ll_rn(f1 * MG_FX_SCALE);
-        ffx[3 * p + 2] += __double2ll_rn(f2 * MG_FX_SCALE);
+        float qk = (float)(-a.az[p] * efp);
+        ffx[3 * p + 0] += __double2ll_rn((double)(qk * (float)a.dkdr[0] * (float)e0) * MG_FX_SCALE);
+        ffx[3 * p + 1] += __double2ll_rn((double)(qk * (float)a.dkdr[1] * (float)e1) * MG_FX_SCALE);
+        ffx[3 * p + 2] += __double2ll_rn((double)(qk * (float)a.dkdr[2] * (float)e2) * MG_FX_SCALE);
     } else {
-        force[3 * p + 0] += f0;
-        force[3 * p + 1] += f1;
-        force[3 * p + 2] += f2;
+        double qp = a.az[p];
+        force[3 * p + 0] += -qp * (double)e0 * a.dkdr[0] * efp;
+        force[3 * p + 1] += -qp * (double)e1 * a.dkdr[1] * efp;
+        force[3 * p + 2] += -qp * (double)e2 * a.dkdr[2] * efp;
     }
+}
+
+// launch one of the order-templated mesh kernels: 0 = splines, 1 = spread, 2 = gather
+template <typename T, typename ACC, int ORDER>
+void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const BrickArgs &bk) {
+    int np = h->np;
+    int *corner = h->d_corner;
+    T *w = (T *)h->d_spl_w, *dw = (T *)h->d_spl_dw;
+    if (which == 0) {
+        k_spline_prepare<T, ORDER><<<(np + 255) / 256, 256, 0, h->st>>>(sa, corner, w, dw);
+    } else if (which == 1) {
+        int wpb = h->spread_wpb;
+        int grid = (h->nbricks + wpb - 1) / wpb;
+        if (h->brick == 8)
+            k_spread_warp<T, ACC, ORDER, 8><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
+                bk, corner, w, h->d_az, np, (T *)h->d_tiles);
+        else
+            k_spread_warp<T, ACC, ORDER, 16><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
+                bk, corner, w, h->d_az, np, (T *)h->d_tiles);
+    } else {
+        constexpr int G = ORDER <= 8 ? 8 : 16;
+        k_gather_grp<T, sizeof(T) == 4, ORDER><<<(unsigned)(((long)np * G + 255) / 256), 256, 0, h->st>>>(
+            sa, h->d_perm, corner, w, (const T *)h->d_spl_dw, (const T *)h->d_Q, h->EpsiFourPi, h->d_force,
+            h->d_ffx);
+    }
+}
+
+template <typename T, typename ACC>
+int mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const BrickArgs &bk) {
+    switch (h->order) {
+    case 4: launch_mesh_kernel<T, ACC, 4>(h, which, sa, bk); break;
+    case 5: launch_mesh_kernel<T, ACC, 5>(h, which, sa, bk); break;
+    case 6: launch_mesh_kernel<T, ACC, 6>(h, which, sa, bk); break;
+    case 7: launch_mesh_kernel<T, ACC, 7>(h, which, sa, bk); break;
+    case 8: launch_mesh_kernel<T, ACC, 8>(h, which, sa, bk); break;
+    case 9: launch_mesh_kernel<T, ACC, 9>(h, which, sa, bk); break;
+    case 10: launch_mesh_kernel<T, ACC, 10>(h, which, sa, bk); break;
+    case 11: launch_mesh_kernel<T, ACC, 11>(h, which, sa, bk); break;
+    case 12: launch_mesh_kernel<T, ACC, 12>(h, which, sa, bk); break;
+    default: return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d (supported: 4..12)", h->order);
+    }
+    h->launches++;
+    return MG_OK;
+}
+
+template <typename T, typename ACC, int ORDER> void spread_attr_o() {
+    cudaFuncSetAttribute(k_spread_warp<T, ACC, ORDER, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(k_spread_warp<T, ACC, ORDER, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+}
+
+template <typename T, typename ACC> void spread_attrs() {
+    spread_attr_o<T, ACC, 4>(); spread_attr_o<T, ACC, 5>(); spread_attr_o<T, ACC, 6>();
+    spread_attr_o<T, ACC, 7>(); spread_attr_o<T, ACC, 8>(); spread_attr_o<T, ACC, 9>();
+    spread_attr_o<T, ACC, 10>(); spread_attr_o<T, ACC, 11>(); spread_attr_o<T, ACC, 12>();
 }
 
 int ilog2(int n) {
@@ -464,6 +664,44 @@ int mg_spme_init(mg_handle *h) {
     h->fft_tiles = tiles;
     h->fft_tx = (h->nh + tiles - 1) / tiles;
     h->nblk_rec = tiles * n;
+    // bricks of 8^3 points (16^3 for orders above 9, whose halo would
+    // otherwise reach beyond the next brick)
+    if (h->order < 4) return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d (supported: 4..12)", h->order);
+    h->brick = (h->order - 1 > 8) ? 16 : 8;
+    if (h->brick > n) h->brick = n;
+    if (h->order - 1 > h->brick)
+        return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d too large for mesh %d", h->order, n);
+    h->nbrick_edge = n / h->brick;
+    h->nbricks = h->nbrick_edge * h->nbrick_edge * h->nbrick_edge;
+    int tile = h->brick + h->order - 1;
+    size_t acc = (h->form == MG_MIXED) ? sizeof(unsigned long long) : sizeof(double);
+    size_t tsz = (h->form == MG_MIXED) ? sizeof(float) : sizeof(double);
+    size_t t3 = (size_t)tile * tile * tile;
+    // warps (bricks) per block: as many tiles as fit, at most kSpreadWarps
+    size_t stage = 32 * sizeof(int) + 3 * (size_t)h->order * 32 * tsz;   // per-warp particle staging
+    h->spread_wpb = (int)std::min<size_t>(kSpreadWarps, (size_t)(200 * 1024) / (acc * t3 + stage + 16));
+    if (h->spread_wpb < 1)
+        return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME spread tile does not fit in shared memory");
+    h->spread_smem = ((h->spread_wpb * acc * t3 + 15) & ~(size_t)15) + h->spread_wpb * stage;
+    MG_CUDA(h, cudaMalloc(&h->d_brick_count, sizeof(int) * h->nbricks));
+    MG_CUDA(h, cudaMemset(h->d_brick_count, 0, sizeof(int) * h->nbricks));
+    MG_CUDA(h, cudaMalloc(&h->d_brick_start, sizeof(int) * (h->nbricks + 1)));
+    MG_CUDA(h, cudaMalloc(&h->d_brick_perm, sizeof(int) * h->np));
+    MG_CUDA(h, cudaMalloc(&h->d_brick_rank, sizeof(int) * h->np));
+    MG_CUDA(h, cudaMalloc(&h->d_brick_of, sizeof(int) * h->np));
+    MG_CUDA(h, cudaMalloc(&h->d_tiles, tsz * (size_t)h->nbricks * t3));
+    MG_CUDA(h, cudaMalloc(&h->d_corner, sizeof(int) * 3 * (size_t)h->np));
+    MG_CUDA(h, cudaMalloc(&h->d_spl_w, tsz * 3 * h->order * (size_t)h->np));
+    MG_CUDA(h, cudaMalloc(&h->d_spl_dw, tsz * 3 * h->order * (size_t)h->np));
+    spread_attrs<float, unsigned long long>();
+    spread_attrs<double, double>();
+    // stamp weights q*Mx*My*Mz are below max|q| in magnitude (cardinal
+    // B-spline values are < 1); the integer scale keeps them below 2^31
+    double qmax = 1.0;
+    for (double q : h->h_az) qmax = std::max(qmax, std::fabs(q));
+    int k = 30;
+    while (k > 8 && std::ldexp(qmax, k) >= 2147483648.0 * 0.99) --k;
+    h->fx_shift = k;
     bool mixed = h->form == MG_MIXED;
     size_t n3 = (size_t)n * n * n, nc = (size_t)h->nh * n * n, no = (size_t)h->nh * h->nh * h->nh;
     std::vector<double> mf, ew, vw;
@@ -479,8 +717,6 @@ int mg_spme_init(mg_handle *h) {
     if (mixed) {
         MG_CUDA(h, cudaMalloc(&h->d_Q, sizeof(float) * n3));
         MG_CUDA(h, cudaMalloc(&h->d_F, sizeof(float2) * nc));
-        MG_CUDA(h, cudaMalloc(&h->d_Qfx, sizeof(unsigned long long) * n3));
-        MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(unsigned long long) * n3, h->st));
         std::vector<float> a(no), b(no), c(no);
         for (size_t i = 0; i < no; ++i) { a[i] = (float)mf[i]; b[i] = (float)ew[i]; c[i] = (float)vw[i]; }
         MG_CUDA(h, cudaMalloc(&h->d_mf_f, sizeof(float) * no));
@@ -517,45 +753,67 @@ int mg_spme_launch(mg_handle *h) {
     sa.np = np;
     sa.order = h->order;
     sa.n = n;
+    sa.n_log = ilog2(n);
     for (int m = 0; m < 3; ++m) sa.dkdr[m] = h->dkdr[m];
     ConvArgs cv;
     cv.part = h->d_part + h->part_rec;
-    int tb = 128, gb = (np + tb - 1) / tb;
-    if (h->form == MG_MIXED) {
-        MG_TRY(mg_phase_begin(h, "spread"));
-        k_spread_fx<<<gb, tb, 0, h->st>>>(sa, h->d_Qfx);
-        MG_TRY(mg_phase_end(h, "spread"));
-        MG_TRY(mg_phase_begin(h, "mesh_convert"));
-        k_fx_to_float<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>(h->d_Qfx, (float *)h->d_Q, n3);
-        MG_TRY(mg_phase_end(h, "mesh_convert"));
-        h->launches += 2;
+    int tb = 256, gb = (np + tb - 1) / tb;
+    BrickArgs bk;
+    bk.n = n;
+    bk.B = h->brick;
+    bk.nb = h->nbrick_edge;
+    bk.ln = ilog2(n);
+    bk.lB = ilog2(h->brick);
+    bk.lnb = ilog2(h->nbrick_edge);
+    bk.fx_scale = std::ldexp(1.0f, h->fx_shift);
+    bk.fx_inv = std::ldexp(1.0f, -h->fx_shift);
+    bk.tile = h->brick + h->order - 1;
+    bk.nbricks = h->nbricks;
+    bk.count = h->d_brick_count;
+    bk.perm = h->d_brick_perm;
+    bk.rank = h->d_brick_rank;
+    bk.brick = h->d_brick_of;
+    bk.start = h->d_brick_start;
+    size_t n3t = (size_t)n * n * n;
+    bool mixed = h->form == MG_MIXED;
+    MG_TRY(mg_phase_begin(h, "splines"));
+    if (mixed) MG_TRY((mesh_kernel<float, unsigned long long>(h, 0, sa, bk)));
+    else MG_TRY((mesh_kernel<double, double>(h, 0, sa, bk)));
+    MG_TRY(mg_phase_end(h, "splines"));
+    MG_TRY(mg_phase_begin(h, "brick_sort"));
+    k_brick_count<<<gb, tb, 0, h->st>>>(h->d_corner, np, bk);
+    k_brick_prefix<<<1, 1024, 0, h->st>>>(bk);
+    k_brick_scatter<<<gb, tb, 0, h->st>>>(np, bk);
+    h->launches += 3;
+    MG_TRY(mg_phase_end(h, "brick_sort"));
+    MG_TRY(mg_phase_begin(h, "spread"));
+    if (mixed) MG_TRY((mesh_kernel<float, unsigned long long>(h, 1, sa, bk)));
+    else MG_TRY((mesh_kernel<double, double>(h, 1, sa, bk)));
+    MG_TRY(mg_phase_end(h, "spread"));
+    MG_TRY(mg_phase_begin(h, "mesh_fold"));
+    if (mixed)
+        k_fold_tiles<float><<<(unsigned)((n3t + 255) / 256), 256, 0, h->st>>>((const float *)h->d_tiles, bk,
+                                                                            h->order, (float *)h->d_Q);
+    else
+        k_fold_tiles<double><<<(unsigned)((n3t + 255) / 256), 256, 0, h->st>>>((const double *)h->d_tiles, bk,
+                                                                             h->order, (double *)h->d_Q);
+    h->launches++;
+    MG_TRY(mg_phase_end(h, "mesh_fold"));
+    if (mixed) {
         cv.mf = h->d_mf_f;
         cv.ew = h->d_ew_f;
         cv.vw = h->d_vw_f;
         MG_TRY(fft_launch<float>(h, (float *)h->d_Q, (float2 *)h->d_F, (const float2 *)h->d_tw, cv));
-        MG_TRY(mg_phase_begin(h, "gather"));
-        k_gather<float, true><<<gb, tb, 0, h->st>>>(sa, (const float *)h->d_Q, h->EpsiFourPi,
-                                                    h->d_force, h->d_ffx);
-        h->launches++;
-        MG_TRY(mg_phase_end(h, "gather"));
     } else {
-        MG_TRY(mg_phase_begin(h, "mesh_clear"));
-        MG_CUDA(h, cudaMemsetAsync(h->d_Q, 0, sizeof(double) * n3, h->st));
-        MG_TRY(mg_phase_end(h, "mesh_clear"));
-        MG_TRY(mg_phase_begin(h, "spread"));
-        k_spread_f64<<<gb, tb, 0, h->st>>>(sa, (double *)h->d_Q);
-        h->launches++;
-        MG_TRY(mg_phase_end(h, "spread"));
         cv.mf = h->d_mf;
         cv.ew = h->d_ew;
         cv.vw = h->d_vw;
         MG_TRY(fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv));
-        MG_TRY(mg_phase_begin(h, "gather"));
-        k_gather<double, false><<<gb, tb, 0, h->st>>>(sa, (const double *)h->d_Q, h->EpsiFourPi,
-                                                      h->d_force, h->d_ffx);
-        h->launches++;
-        MG_TRY(mg_phase_end(h, "gather"));
     }
+    MG_TRY(mg_phase_begin(h, "gather"));
+    if (mixed) MG_TRY((mesh_kernel<float, unsigned long long>(h, 2, sa, bk)));
+    else MG_TRY((mesh_kernel<double, double>(h, 2, sa, bk)));
+    MG_TRY(mg_phase_end(h, "gather"));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }

@@ -59,6 +59,9 @@ def small_cases():
         ("no_ewald", lambda: configs.small_system(seed=18, ewald=abi.MG_EWALD_NONE)),
         ("wca_lljcut", lambda: configs.small_system(seed=19, lljcut=1)),
         ("mc_mode", lambda: configs.small_system(seed=20, mode=abi.MG_MC)),
+        ("spme_order8_n64", lambda: configs.small_system(seed=21, nmesh=64, order=8)),
+        ("spme_order10_n128", lambda: configs.small_system(seed=22, nmesh=128, order=10, n=500, L=45.0)),
+        ("spme_order4_n128", lambda: configs.small_system(seed=23, nmesh=128, order=4, n=600, L=50.0)),
     ]
 
 

@@ -39,7 +39,7 @@ def test_bd_stream_and_positions(seed, nstep, orc, gpu_lib):
 
 def test_bd_odd_deviate_count_carries_saved_value(orc, gpu_lib):
     """3*np odd: each step leaves one Box-Muller deviate saved for the next."""
-    s = prepared(configs.small_system(seed=52, n=301, L=36.0, mode=abi.MG_BD), orc)
+    s = prepared(configs.small_system(seed=52, n=310, L=36.0, mode=abi.MG_BD), orc)
     assert (3 * s.np_) % 2 == 1
     ref, gpu = _pair(s, orc)
     for e in (ref, gpu):
