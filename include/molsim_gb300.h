@@ -255,6 +255,35 @@ int mg_bench_steps(mg_handle *h, int32_t kind, int32_t nstep, int64_t flush_byte
  * mg_md_run / mg_bd_run / mg_bench_steps). */
 int mg_step_kernels(mg_handle *h, int32_t kind, int32_t *nkernels);
 
+/* ---- allocation-free entry point ----------------------------------------------- */
+
+/* Largest ncut that mg_ewald_rec_std_noalloc accepts. */
+#define MG_NOALLOC_MAX_NCUT 24
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- a host code whose device memory all belongs to its own pool, or
+ * one that must not let cudaMalloc/cudaFree synchronise the device inside its
+ * step -- the reciprocal part of mg_utotal for standard Ewald
+ * (UEwaldRecStd + UEwaldSelf, no surface term), with no handle and no
+ * allocation.  Every buffer is caller-owned DEVICE memory:
+ *   d_ro [3*np] positions, d_az [np] charges (read)
+ *   d_force [3*np]  the reciprocal force is ADDED (EpsiFourPi applied;
+ *                   force_fac is not)
+ *   d_uout [2]      EpsiFourPi (Urec + Uself), EpsiFourPi Virrec (written)
+ * The k-vector set is that of mg_create for the same ncut, ncutregion_cube.
+ * Work is queued on `stream` (a cudaStream_t; NULL = default stream) and the
+ * call returns without waiting for it.  The working memory is a fixed device
+ * array of about 1.2 MB inside the library, held by every GPU that loads it:
+ * ncut above MG_NOALLOC_MAX_NCUT is rejected (MG_ERR_ARG).  All calls share
+ * that array, so calls that overlap on the GPU (other streams, other threads)
+ * race.  The first call on a device looks up the array's device address; make
+ * that first call before any stream capture begins.  On error a message is
+ * written to err (if non-NULL). */
+int mg_ewald_rec_std_noalloc(int32_t np, const double *d_ro, const double *d_az,
+                             const double boxlen[3], double ualpha, int32_t ncut,
+                             int32_t ncutregion_cube, double epsi_four_pi, double *d_force,
+                             double *d_uout, void *stream, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif
