@@ -50,6 +50,30 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
 
+def replica_seed(seed, rank):
+    """Replicas only: every rank runs its own independent system."""
+    return seed + rank
+
+
+def barrier(world):
+    """All ranks reach this point, then the local device is idle."""
+    import torch
+    if world > 1:
+        torch.distributed.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(x, world, device="cuda"):
+    """Max of a per-rank float over all ranks (the slowest rank sets the time)."""
+    if world == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_system(seed):
     from molsim_gb300 import configs
     t = time.time()
@@ -207,21 +231,9 @@ def run_ours(args):
         torch.cuda.set_device(0)
     dev_index = torch.cuda.current_device()
     molsim_gb300.build()
-    s = make_system(args.seed + rank)
+    s = make_system(replica_seed(args.seed, rank))
     s.build_table()
     K, W = args.steps, args.warmup
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
 
     def engine(form):
         e = Engine(s, form=form)
@@ -241,15 +253,15 @@ def run_ours(args):
     clocks = None
     for name, e in (("fp64", e64), ("mixed", emx)):
         e.BenchSteps(1, W, FLUSH_BYTES)
-        barrier()
+        barrier(world)
         if name == "mixed":
             with ClockSampler(dev_index) as cs:
                 ms = e.BenchSteps(1, K, FLUSH_BYTES)
             clocks = cs.summary()
         else:
             ms = e.BenchSteps(1, K, FLUSH_BYTES)
-        barrier()
-        ms = max_over_ranks(ms)
+        barrier(world)
+        ms = max_over_ranks(ms, world)
         results[name] = {"ms_per_step": ms / K, "steps_per_s": world * K / (ms * 1e-3)}
     kernels_per_step = emx.StepKernels(1)
 
@@ -291,7 +303,7 @@ def run_ours(args):
     for _ in range(min(W, 10)):
         assert lib.mg_bd_step_host(emx.h, p_ro, p_f, p_u) == 0
     tsum = 0.0
-    barrier()
+    barrier(world)
     for i in range(ke):
         flush.fill_(float(i))
         torch.cuda.synchronize()
@@ -300,7 +312,7 @@ def run_ours(args):
         tsum += time.perf_counter() - t0
         if st != 0:
             raise RuntimeError(f"mg_bd_step_host failed: {st}")
-    tsum = max_over_ranks(tsum)
+    tsum = max_over_ranks(tsum, world)
     e2e = world * ke / tsum
 
     cpu = None
