@@ -82,24 +82,34 @@ def make_system(seed):
     return s
 
 
-# ---- algorithmic bytes per launch (mixed form), see the design doc -----------------
-def algorithmic_bytes(kernel, n, k, pairs, nbond):
+# ---- algorithmic bytes per launch of each phase (mixed form) -------------------
+# Each logical array counts once per launch at the form's element size: N
+# particles, P stored neighbour pairs, K the mesh edge, p the spline order, nb
+# bonds.  Positions 24 B (FP64 xyz), charges 8 B, fixed-point forces 24 B (read
+# and written where they accumulate), spline values 4 B, the real mesh 4 B and
+# the half spectrum 8 B per point.  Tile halos, re-reads and atomics are not
+# algorithmic and are not counted.
+def algorithmic_bytes(kernel, n, k, pairs, nbond, order=6):
     nh = k // 2 + 1
     k3, spec = k ** 3, nh * k * k
+    spl = 3 * order * 4                       # one set of spline values per particle
     return {
-        "prepare": n * (24 + 4 + 4 + 32),
-        "pair": n * 32 + pairs * 4 + n * 4 + n * 24,
-        "spread": n * 32 + k3 * 8,
-        "mesh_convert": k3 * 8 + k3 * 4,
+        "bd_rng": n * 12,                                     # 3 deviates out
+        "bd_move": n * (24 + 24 + 12 + 24),                   # ro, force, deviates in; ro out
+        "list": n * 24,                                       # displacement check
+        "prepare": n * (24 + 4 + 16),                         # ro, type in; cell slot out
+        "pair": n * 16 + pairs * 4 + n * 48,                  # slots, list in; forces in+out
+        "splines": n * 24 + n * (12 + 2 * spl),               # ro in; corner, w, dw out
+        "brick_sort": n * (12 + 12),                          # corner in; brick, rank, perm out
+        "spread": n * (4 + 12 + spl + 8) + k3 * 4,            # perm, corner, w, q in; mesh out
+        "mesh_fold": k3 * 4,                                  # mesh out
         "fft_x_r2c": k3 * 4 + spec * 8,
         "fft_y_fwd": 2 * spec * 8,
-        "fft_z_conv": 2 * spec * 8 + 3 * nh ** 3 * 4,
+        "fft_z_conv": 2 * spec * 8 + 3 * nh ** 3 * 4,         # spectrum in+out, influence tables
         "fft_y_inv": 2 * spec * 8,
         "fft_x_c2r": spec * 8 + k3 * 4,
-        "gather": k3 * 4 + n * 32 + 2 * n * 24,
-        "bond+reduce": nbond * 2 * 24 + n * 24 * 2,
-        "bd_move": n * (24 + 24 + 24 + 4),
-        "list": n * (24 + 24 + 8),
+        "gather": k3 * 4 + n * (4 + 12 + 2 * spl + 8) + n * 48,
+        "bond+reduce": nbond * 48 + n * 48,
     }.get(kernel)
 
 
@@ -277,14 +287,16 @@ def run_ours(args):
     nn, _ = emx.VList(maxnneigh=256)
     pairs = int(2 * nn.sum())
     nbond = 0 if s.bond_ip is None else len(s.bond_ip)
-    dom = max(phases, key=phases.get)
+    # the Verlet-list rebuild runs on a small fraction of the steps; its
+    # per-call time is reported but does not pick the dominant kernel
+    dom = max((k for k in phases if k != "list_build"), key=phases.get)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
-    ab = algorithmic_bytes(dom, s.np_, s.nmesh, pairs, nbond)
+    ab = algorithmic_bytes(dom, s.np_, s.nmesh, pairs, nbond, s.order)
     achieved = ab / (phases[dom] * 1e-3) / 1e9 if ab else None
     traffic = traffic_from_profiles(dom)
 
@@ -355,6 +367,31 @@ def run_ours(args):
     return 0
 
 
+def run_profile(args):
+    """A short, quiet run for ncu: the workload in one form, W warm-up steps
+    and K steps through the captured step graph, no flush, no other work."""
+    import torch
+
+    import molsim_gb300
+    from molsim_gb300 import Engine, abi
+    torch.cuda.set_device(0)
+    molsim_gb300.build()
+    s = make_system(args.seed)
+    s.build_table()
+    e = Engine(s, form=abi.MG_MIXED if args.profile == "mixed" else abi.MG_FP64)
+    e.SetPositions(s.ro_flat())
+    e.NList("write")
+    e.BDSetup(BD_DT, BD_SEED)
+    # phase timing runs the steps as plain launches: ncu does not profile the
+    # kernels of a graph that holds a conditional node
+    e.PhaseReset(True)
+    ms = e.BenchSteps(1, args.warmup + args.steps, 0)
+    log(f"[profile] {args.profile}: {args.warmup + args.steps} steps, {ms:.3f} ms, "
+        f"{e.StepKernels(1)} kernels per step")
+    e.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -363,7 +400,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile", choices=["mixed", "fp64"],
+                    help="profiling run for ncu: only W + K BD steps of one form, nothing else")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

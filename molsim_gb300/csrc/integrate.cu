@@ -283,6 +283,8 @@ int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, cons
     return MG_OK;
 }
 
+static int list_step(mg_handle *h);
+
 // one BD step (BDStep, UTotal, list check) queued on the stream
 int mg_integrate_bd_step_launch(mg_handle *h) {
     int np = h->np, nc = h->ncand, nblk = nc / kCandBlock;
@@ -315,11 +317,29 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     h->launches += 3;
     MG_TRY(mg_phase_end(h, "bd_move"));
     MG_TRY(mg_utotal_launch(h));
+    MG_TRY(list_step(h));
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+// NList(iSimulationStep) inside a device step.  In a captured step the
+// rebuild sits in the graph's conditional node.  Uncaptured (phase timing,
+// profiling) the host reads the rebuild flag after the check and launches the
+// build only when it is due, so that uncaptured steps run the same kernels as
+// the graph does.
+static int list_step(mg_handle *h) {
     MG_TRY(mg_phase_begin(h, "list"));
     MG_TRY(mg_lists_check(h));
-    if (!h->use_cond) MG_TRY(mg_lists_build(h, true));
     MG_TRY(mg_phase_end(h, "list"));
-    MG_CUDA(h, cudaGetLastError());
+    if (h->use_cond) return MG_OK;
+    int flag = 0;
+    MG_CUDA(h, cudaMemcpyAsync(&flag, h->d_rebuild, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    MG_CUDA(h, cudaStreamSynchronize(h->st));
+    if (flag) {
+        MG_TRY(mg_phase_begin(h, "list_build"));
+        MG_TRY(mg_lists_build(h, false));
+        MG_TRY(mg_phase_end(h, "list_build"));
+    }
     return MG_OK;
 }
 
@@ -344,10 +364,7 @@ int mg_integrate_md_step_launch(mg_handle *h) {
     MG_TRY(mg_utotal_launch(h));
     k_md_vel<<<gb, 256, 0, h->st>>>(a);
     h->launches++;
-    MG_TRY(mg_phase_begin(h, "list"));
-    MG_TRY(mg_lists_check(h));
-    if (!h->use_cond) MG_TRY(mg_lists_build(h, true));
-    MG_TRY(mg_phase_end(h, "list"));
+    MG_TRY(list_step(h));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }

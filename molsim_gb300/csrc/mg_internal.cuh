@@ -106,18 +106,20 @@ struct mg_handle {
     double dkdr[3];
     void *d_Q = nullptr;            // real mesh (double or float)
     void *d_F = nullptr;            // half spectrum (double2 or float2)
-    unsigned long long *d_Qfx = nullptr;  // fixed-point spread mesh (mixed form)
+    unsigned long long *d_Qfx = nullptr;  // spread mesh in 64-bit fixed point (cleared by the FFT x pass)
     double *d_mf = nullptr, *d_ew = nullptr, *d_vw = nullptr;   // octant tables [nh^3]
     float *d_mf_f = nullptr, *d_ew_f = nullptr, *d_vw_f = nullptr;
     void *d_tw = nullptr;           // twiddles exp(-2 pi i m/n), m < n
     int fft_tx = 0, fft_tiles = 0;
     int brick = 0, nbrick_edge = 0, nbricks = 0;
     size_t spread_smem = 0, gather_smem = 0;
-    int fx_shift = 30;
+    int fx_shift = 30, fx_shift64 = 48;
     int spread_wpb = 4;             // spread: bricks (warps) per block
     int spread_chunk = 256;         // particles staged per pass of the spread              // mixed spread: weights scaled by 2^fx_shift into int32
     int *d_brick_count = nullptr, *d_brick_perm = nullptr, *d_brick_rank = nullptr, *d_brick_of = nullptr;
     int *d_brick_start = nullptr;
+    int *d_brick_istart = nullptr, *d_item_brick = nullptr;   // spread work items per brick
+    int spread_m = 32, max_items = 0;
     void *d_tiles = nullptr;        // per-brick spread tiles (mesh type)
     int *d_corner = nullptr;        // [3][np] stamp corner per particle and dimension
     void *d_spl_w = nullptr, *d_spl_dw = nullptr;   // [3][order][np] B-spline values, derivatives

@@ -26,6 +26,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <type_traits>
+
 #include "mg_internal.cuh"
 
 namespace {
@@ -111,8 +113,16 @@ __device__ __forceinline__ void load_tw(V2<T> *s_tw, const V2<T> *__restrict__ t
 }
 
 // ---- x pass: r2c, two real lines per complex line ---------------------------
+// 64-bit fixed point to the mesh type: double directly; float through two
+// 32-bit halves so that the mixed form stays off the FP64 pipe
+template <typename T> __device__ __forceinline__ T fx_to_real(long long x);
+template <> __device__ __forceinline__ double fx_to_real<double>(long long x) { return (double)x; }
+template <> __device__ __forceinline__ float fx_to_real<float>(long long x) {
+    return (float)(int)(x >> 32) * 4294967296.0f + (float)(unsigned)(x & 0xffffffffll);
+}
+
 template <typename T>
-__global__ void k_fft_x_r2c(const T *__restrict__ Q, V2<T> *__restrict__ F, int n, int logn,
+__global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *__restrict__ F, int n, int logn,
                             int lp, const V2<T> *__restrict__ tw) {
     typedef V2<T> V;
     extern __shared__ unsigned char smem_raw[];
@@ -123,9 +133,11 @@ __global__ void k_fft_x_r2c(const T *__restrict__ Q, V2<T> *__restrict__ F, int 
     size_t line0 = (size_t)blockIdx.x * 2 * lp;
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
         int c = e / n, t = e % n;
+        // the spread's fixed-point mesh (cleared after this pass)
+        long long q0 = Qfx[(line0 + 2 * c) * n + t], q1 = Qfx[(line0 + 2 * c + 1) * n + t];
         V v;
-        v.x = Q[(line0 + 2 * c) * n + t];
-        v.y = Q[(line0 + 2 * c + 1) * n + t];
+        v.x = fx_to_real<T>(q0) * fx_inv;
+        v.y = fx_to_real<T>(q1) * fx_inv;
         A[c * n + t] = v;
     }
     __syncthreads();
@@ -321,7 +333,11 @@ struct BrickArgs {
     int nbricks;
     float fx_scale;        // mixed form: stamp weights to 32-bit integers (2^k)
     float fx_inv;
+    double fx_scale64;     // FP64 form: stamp weights to 64-bit integers
+    int M;                 // particles per spread work item
     int *count, *start, *perm, *rank, *brick;
+    int *istart;           // first work item of each brick (nbricks + 1)
+    int *item_brick;       // brick of each work item
 };
 
 __global__ void k_brick_count(const int *__restrict__ corner, int np, BrickArgs b) {
@@ -333,38 +349,48 @@ __global__ void k_brick_count(const int *__restrict__ corner, int np, BrickArgs 
     b.rank[p] = atomicAdd(&b.count[id], 1);
 }
 
-// exclusive prefix of the brick counts (one block of 1024 threads); the
-// counts are cleared for the next call
+// exclusive prefixes of the brick counts and of the work items per brick
+// (ceil(count / M)), one block of 1024 threads; the item -> brick map is
+// filled and the counts are cleared for the next call
 __global__ void __launch_bounds__(1024) k_brick_prefix(BrickArgs b) {
-    __shared__ int wsum[32];
+    __shared__ int wsum[2][32];
     int nb = b.nbricks, per = (nb + 1023) / 1024;
     int lo = threadIdx.x * per, hi = min(nb, lo + per);
-    int s = 0;
-    for (int i = lo; i < hi; ++i) s += b.count[i];
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int v = s;
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += y;
+    int s = 0, si = 0;
+    for (int i = lo; i < hi; ++i) {
+        int c = b.count[i];
+        s += c;
+        si += (c + b.M - 1) / b.M;
     }
-    if (lane == 31) wsum[w] = v;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v = s, vi = si;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, v, o), yi = __shfl_up_sync(0xffffffffu, vi, o);
+        if (lane >= o) { v += y; vi += yi; }
+    }
+    if (lane == 31) { wsum[0][w] = v; wsum[1][w] = vi; }
     __syncthreads();
-    if (w == 0) {
-        int x = wsum[lane];
+    if (w < 2) {
+        int x = wsum[w][lane];
         for (int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
-        wsum[lane] = x;
+        wsum[w][lane] = x;
     }
     __syncthreads();
-    int run = v - s + (w ? wsum[w - 1] : 0);
+    int run = v - s + (w ? wsum[0][w - 1] : 0);
+    int irun = vi - si + (w ? wsum[1][w - 1] : 0);
     for (int i = lo; i < hi; ++i) {
+        int c = b.count[i], ni = (c + b.M - 1) / b.M;
         b.start[i] = run;
-        run += b.count[i];
+        b.istart[i] = irun;
+        for (int k = 0; k < ni; ++k) b.item_brick[irun + k] = i;
+        run += c;
+        irun += ni;
         b.count[i] = 0;
     }
-    if (threadIdx.x == 1023) b.start[nb] = run;
+    if (threadIdx.x == 1023) { b.start[nb] = run; b.istart[nb] = irun; }
 }
 
 __global__ void k_brick_scatter(int np, BrickArgs b) {
@@ -372,36 +398,57 @@ __global__ void k_brick_scatter(int np, BrickArgs b) {
     if (p < np) b.perm[b.start[b.brick[p]] + b.rank[p]] = p;
 }
 
-constexpr int kSpreadWarps = 4;   // bricks (warps) per block
+constexpr int kSpreadWarps = 8;   // most work items (warps) per block
+constexpr int kSpreadItem = 32;   // most particles per spread work item
 
-// spread: one warp per brick owns the brick's tile in shared memory and adds
-// the particles one after another, its lanes covering the order^3 points of
-// a stamp (all distinct), so plain read-modify-writes are race free.  ACC is
-// a 64-bit fixed-point integer in the mixed form (exact, independent of the
-// particle order) or double.  The tile is written to scratch in the mesh type.
+// spread: one warp per work item (up to M particles of one brick, so that a
+// brick crowded by a polymer coil does not hold up the grid) owns a tile of
+// the brick plus its halo in shared memory and adds the particles one after
+// another, its lanes covering the order^3 points of a stamp (all distinct),
+// so plain read-modify-writes are race free.  ACC is fixed point: 32-bit in
+// the mixed form (the scale keeps M stamps below 2^31), 64-bit in the FP64
+// form (scale 2^48 or finer, far below FP64 rounding of the energies).  The
+// tile is then added into the 64-bit fixed-point mesh with integer atomics:
+// exact, so the mesh does not depend on how particles fall into items or on
+// the order in which items run.
 template <typename T, typename ACC, int ORDER, int B>
 __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, const int *__restrict__ corner,
                                                                    const T *__restrict__ w,
                                                                    const double *__restrict__ az, int np,
-                                                                   T *__restrict__ tiles) {
+                                                                   long long *__restrict__ Qfx) {
     constexpr int t = B + ORDER - 1, t3 = t * t * t, O3 = ORDER * ORDER * ORDER;
+    constexpr int NPASS = (O3 + 31) / 32;
+    constexpr int REC = 3 * ORDER + 1;   // odd record length: lanes reading one record hit distinct banks
     // per warp: the tile, then a staging area of 32 particles (corner
-    // offsets packed in one int, charge-weighted x, y and z weights)
+    // offsets packed in one int; per particle the charge-weighted x weights,
+    // then the y and z weights)
     struct Stage {
         int off[32];
-        T wx[ORDER][32], wy[ORDER][32], wz[ORDER][32];
+        T w[32][REC];
     };
     extern __shared__ __align__(16) unsigned char smem_sw[];
     int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
     ACC *tile = reinterpret_cast<ACC *>(smem_sw) + (size_t)wib * t3;
     Stage *stg = reinterpret_cast<Stage *>(smem_sw + (((size_t)nwb * t3 * sizeof(ACC) + 15) & ~(size_t)15)) + wib;
-    int brick = blockIdx.x * nwb + wib;
-    if (brick >= b.nbricks) return;
+    int item = blockIdx.x * nwb + wib;
+    if (item >= b.istart[b.nbricks]) return;
+    int brick = b.item_brick[item];
     for (int k = lane; k < t3; k += 32) tile[k] = (ACC)0;
     int mnb = b.nb - 1;
     int bx = brick & mnb, by = (brick >> b.lnb) & mnb, bz = brick >> (2 * b.lnb);
     int ox = bx * B - (ORDER - 1), oy = by * B - (ORDER - 1), oz = bz * B - (ORDER - 1);
-    int first = b.start[brick], last = b.start[brick + 1];
+    int first = b.start[brick] + (item - b.istart[brick]) * b.M;
+    int last = min(first + b.M, b.start[brick + 1]);
+    // this lane's stamp points, one per pass: tile offset relative to the
+    // particle's corner and the packed (ix, iy, iz) weight indices
+    int rel[NPASS], wix[NPASS];
+#pragma unroll
+    for (int pass = 0; pass < NPASS; ++pass) {
+        int k = min(lane + 32 * pass, O3 - 1);
+        int ix = k % ORDER, iy = (k / ORDER) % ORDER, iz = k / (ORDER * ORDER);
+        rel[pass] = -((iz * t + iy) * t + ix);
+        wix[pass] = ix | ((ORDER + iy) << 8) | ((2 * ORDER + iz) << 16);
+    }
     for (int q0 = first; q0 < last; q0 += 32) {
         int cnt = min(32, last - q0);
         __syncwarp();
@@ -410,73 +457,57 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
             int cx = corner[p] - ox, cy = corner[np + p] - oy, cz = corner[2 * np + p] - oz;
             stg->off[lane] = cx | (cy << 8) | (cz << 16);
             T qp = (T)az[p];
+            T *rec = stg->w[lane];
 #pragma unroll
             for (int i = 0; i < ORDER; ++i) {
-                stg->wx[i][lane] = qp * w[(size_t)i * np + p];
-                stg->wy[i][lane] = w[(size_t)(ORDER + i) * np + p];
-                stg->wz[i][lane] = w[(size_t)(2 * ORDER + i) * np + p];
+                rec[i] = qp * w[(size_t)i * np + p];
+                rec[ORDER + i] = w[(size_t)(ORDER + i) * np + p];
+                rec[2 * ORDER + i] = w[(size_t)(2 * ORDER + i) * np + p];
             }
         }
         __syncwarp();
         for (int e = 0; e < cnt; ++e) {
             int off = stg->off[e];
             int base = ((off >> 16) * t + ((off >> 8) & 255)) * t + (off & 255);
+            const T *rec = stg->w[e];
+            // the order^3 points of one stamp are distinct: every lane issues
+            // all of its loads before any store
+            ACC old[NPASS];
+            T val[NPASS];
 #pragma unroll
-            for (int pass = 0; pass < (O3 + 31) / 32; ++pass) {
-                int k = lane + 32 * pass;
-                if (k < O3) {
-                    int ix = k % ORDER, iy = (k / ORDER) % ORDER, iz = k / (ORDER * ORDER);
-                    T wt = stg->wx[ix][e] * stg->wy[iy][e] * stg->wz[iz][e];
-                    ACC *dst = tile + base - (iz * t + iy) * t - ix;
-                    if (sizeof(ACC) == 8 && sizeof(T) == 4)   // |wt * fx_scale| < 2^31 by choice of scale
-                        *dst += (ACC)(long long)__float2int_rn(wt * b.fx_scale);
+            for (int pass = 0; pass < NPASS; ++pass) {
+                if (lane + 32 * pass < O3) {
+                    int q = wix[pass];
+                    val[pass] = rec[q & 255] * rec[(q >> 8) & 255] * rec[q >> 16];
+                    old[pass] = tile[base + rel[pass]];
+                }
+            }
+#pragma unroll
+            for (int pass = 0; pass < NPASS; ++pass) {
+                if (lane + 32 * pass < O3) {
+                    if (sizeof(T) == 4)   // |sum of M stamps * fx_scale| < 2^31 by choice of scale
+                        tile[base + rel[pass]] = old[pass] + __float2int_rn((float)val[pass] * b.fx_scale);
                     else
-                        *dst += (ACC)wt;
+                        tile[base + rel[pass]] = old[pass] + __double2ll_rn((double)val[pass] * b.fx_scale64);
                 }
             }
             __syncwarp();
         }
     }
-    T *out = tiles + (size_t)brick * t3;
-    for (int k = lane; k < t3; k += 32) {
-        ACC v = tile[k];
-        if (sizeof(ACC) == 8 && sizeof(T) == 4) {
-            long long x = (long long)v;   // 64-bit integer to float without the FP64 pipe
-            float hi = (float)(int)(x >> 32), lo = (float)(unsigned)(x & 0xffffffffll);
-            out[k] = (T)((hi * 4294967296.0f + lo) * b.fx_inv);
-        } else {
-            out[k] = (T)v;
+    // add the tile into the mesh, row by row: 64-bit integer adds are exact,
+    // so the result does not depend on the order in which items arrive
+    constexpr int XL = t <= 16 ? 16 : 32, RPI = 32 / XL;
+    int mn = b.n - 1, cx = lane & (XL - 1);
+    if (cx < t) {
+        size_t gx = (size_t)((ox + cx) & mn);
+        for (int row = lane / XL; row < t * t; row += RPI) {
+            long long v = (long long)tile[row * t + cx];
+            if (v == 0) continue;
+            int cy = row % t, cz = row / t;
+            size_t idx = ((((size_t)((oz + cz) & mn) << b.ln) + (size_t)((oy + cy) & mn)) << b.ln) | gx;
+            atomicAdd(reinterpret_cast<unsigned long long *>(Qfx) + idx, (unsigned long long)v);
         }
     }
-}
-
-// fold: every mesh point adds the tiles that cover it (its own brick and the
-// low halos of up to seven following bricks) in a fixed order
-template <typename T>
-__global__ void k_fold_tiles(const T *__restrict__ tiles, BrickArgs b, int order, T *__restrict__ Q) {
-    int B = b.B, t = b.tile, h = order - 1, mB = B - 1, mnb = b.nb - 1;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= ((size_t)1 << (3 * b.ln))) return;
-    int mn = b.n - 1;
-    int x = (int)idx & mn, y = (int)(idx >> b.ln) & mn, z = (int)(idx >> (2 * b.ln));
-    int bx = x >> b.lB, by = y >> b.lB, bz = z >> b.lB, lx = x & mB, ly = y & mB, lz = z & mB;
-    size_t t3 = (size_t)t * t * t;
-    T sum = (T)0;
-    for (int ez = 0; ez < 2; ++ez) {
-        if (ez && lz < B - h) break;
-        int cz = ez ? lz - B + h : lz + h, kz = (bz + ez) & mnb;
-        for (int ey = 0; ey < 2; ++ey) {
-            if (ey && ly < B - h) break;
-            int cy = ey ? ly - B + h : ly + h, ky = (by + ey) & mnb;
-            for (int ex = 0; ex < 2; ++ex) {
-                if (ex && lx < B - h) break;
-                int cx = ex ? lx - B + h : lx + h, kx = (bx + ex) & mnb;
-                int brick = (((kz << b.lnb) + ky) << b.lnb) + kx;
-                sum += tiles[(size_t)brick * t3 + ((size_t)cz * t + cy) * t + cx];
-            }
-        }
-    }
-    Q[idx] = sum;
 }
 
 // gather: a group of G lanes per particle (G = 8 for orders up to 8, else
@@ -558,13 +589,13 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
         k_spline_prepare<T, ORDER><<<(np + 255) / 256, 256, 0, h->st>>>(sa, corner, w, dw);
     } else if (which == 1) {
         int wpb = h->spread_wpb;
-        int grid = (h->nbricks + wpb - 1) / wpb;
+        int grid = (h->max_items + wpb - 1) / wpb;
         if (h->brick == 8)
             k_spread_warp<T, ACC, ORDER, 8><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
-                bk, corner, w, h->d_az, np, (T *)h->d_tiles);
+                bk, corner, w, h->d_az, np, (long long *)h->d_Qfx);
         else
             k_spread_warp<T, ACC, ORDER, 16><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
-                bk, corner, w, h->d_az, np, (T *)h->d_tiles);
+                bk, corner, w, h->d_az, np, (long long *)h->d_Qfx);
     } else {
         constexpr int G = ORDER <= 8 ? 8 : 16;
         k_gather_grp<T, sizeof(T) == 4, ORDER><<<(unsigned)(((long)np * G + 255) / 256), 256, 0, h->st>>>(
@@ -609,7 +640,7 @@ int ilog2(int n) {
 }
 
 template <typename T>
-int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv) {
+int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_inv) {
     int n = h->nmesh, logn = ilog2(n), nh = h->nh;
     int lp = 4;                                  // line pairs per CTA in the x passes
     size_t vsz = sizeof(V2<T>);
@@ -622,7 +653,9 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv) {
     size_t ystride = nh, yother = (size_t)n * nh;   // y pass: t -> y, other -> z
     size_t zstride = (size_t)n * nh, zother = nh;   // z pass: t -> z, other -> y
     MG_TRY(mg_phase_begin(h, "fft_x_r2c"));
-    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>(Q, F, n, logn, lp, tw);
+    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, fx_inv, F, n, logn, lp, tw);
+    // the next spread accumulates into a cleared mesh
+    MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n, h->st));
     MG_TRY(mg_phase_end(h, "fft_x_r2c"));
     MG_TRY(mg_phase_begin(h, "fft_y_fwd"));
     k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, -1, tw, cv);
@@ -674,34 +707,67 @@ int mg_spme_init(mg_handle *h) {
     h->nbrick_edge = n / h->brick;
     h->nbricks = h->nbrick_edge * h->nbrick_edge * h->nbrick_edge;
     int tile = h->brick + h->order - 1;
-    size_t acc = (h->form == MG_MIXED) ? sizeof(unsigned long long) : sizeof(double);
+    size_t acc = (h->form == MG_MIXED) ? sizeof(int) : sizeof(double);
     size_t tsz = (h->form == MG_MIXED) ? sizeof(float) : sizeof(double);
     size_t t3 = (size_t)tile * tile * tile;
-    // warps (bricks) per block: as many tiles as fit, at most kSpreadWarps
-    size_t stage = 32 * sizeof(int) + 3 * (size_t)h->order * 32 * tsz;   // per-warp particle staging
-    h->spread_wpb = (int)std::min<size_t>(kSpreadWarps, (size_t)(200 * 1024) / (acc * t3 + stage + 16));
+    // warps (work items) per block: the count that keeps the most warps
+    // resident per SM (228 KB of shared memory, 1 KB reserved per block)
+    size_t stage = 32 * sizeof(int) + 32 * (3 * (size_t)h->order + 1) * tsz;   // per-warp particle staging
+    size_t per_warp = acc * t3 + stage;
+    int best = 0;
+    h->spread_wpb = 0;
+    for (int wpb = 1; wpb <= kSpreadWarps; ++wpb) {
+        size_t blk = ((wpb * acc * t3 + 15) & ~(size_t)15) + wpb * stage;
+        if (blk > (size_t)200 * 1024) break;
+        int blocks = std::min<int>(32, (int)((size_t)228 * 1024 / (blk + 1024)));
+        if (blocks * wpb >= best) { best = blocks * wpb; h->spread_wpb = wpb; }
+    }
     if (h->spread_wpb < 1)
         return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME spread tile does not fit in shared memory");
     h->spread_smem = ((h->spread_wpb * acc * t3 + 15) & ~(size_t)15) + h->spread_wpb * stage;
+    (void)per_warp;
+    h->spread_m = kSpreadItem;
+    h->max_items = h->nbricks + (h->np + kSpreadItem - 1) / kSpreadItem;
     MG_CUDA(h, cudaMalloc(&h->d_brick_count, sizeof(int) * h->nbricks));
     MG_CUDA(h, cudaMemset(h->d_brick_count, 0, sizeof(int) * h->nbricks));
     MG_CUDA(h, cudaMalloc(&h->d_brick_start, sizeof(int) * (h->nbricks + 1)));
     MG_CUDA(h, cudaMalloc(&h->d_brick_perm, sizeof(int) * h->np));
     MG_CUDA(h, cudaMalloc(&h->d_brick_rank, sizeof(int) * h->np));
     MG_CUDA(h, cudaMalloc(&h->d_brick_of, sizeof(int) * h->np));
-    MG_CUDA(h, cudaMalloc(&h->d_tiles, tsz * (size_t)h->nbricks * t3));
+    MG_CUDA(h, cudaMalloc(&h->d_brick_istart, sizeof(int) * (h->nbricks + 1)));
+    MG_CUDA(h, cudaMalloc(&h->d_item_brick, sizeof(int) * h->max_items));
+    MG_CUDA(h, cudaMalloc(&h->d_Qfx, sizeof(long long) * (size_t)n * n * n));
+    MG_CUDA(h, cudaMemset(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n));
     MG_CUDA(h, cudaMalloc(&h->d_corner, sizeof(int) * 3 * (size_t)h->np));
     MG_CUDA(h, cudaMalloc(&h->d_spl_w, tsz * 3 * h->order * (size_t)h->np));
     MG_CUDA(h, cudaMalloc(&h->d_spl_dw, tsz * 3 * h->order * (size_t)h->np));
-    spread_attrs<float, unsigned long long>();
-    spread_attrs<double, double>();
+    spread_attrs<float, int>();
+    spread_attrs<double, long long>();
     // stamp weights q*Mx*My*Mz are below max|q| in magnitude (cardinal
     // B-spline values are < 1); the integer scale keeps them below 2^31
     double qmax = 1.0;
     for (double q : h->h_az) qmax = std::max(qmax, std::fabs(q));
+    // The mixed spread sums up to kSpreadItem stamps per tile point in int32:
+    // the scale keeps kSpreadItem * max|q| * (max B-spline value)^3 below 2^31.
+    double mmax = 0.0;
+    {
+        std::vector<double> v(h->order), d(h->order);
+        int km;
+        mg_host_bspline(h->order, 0.5 * h->order + 0.5, &km, v.data(), d.data());
+        for (double x : v) mmax = std::max(mmax, x);
+        mg_host_bspline(h->order, 0.5 * h->order, &km, v.data(), d.data());
+        for (double x : v) mmax = std::max(mmax, x);
+    }
+    double bound = kSpreadItem * qmax * mmax * mmax * mmax * 1.01;
     int k = 30;
-    while (k > 8 && std::ldexp(qmax, k) >= 2147483648.0 * 0.99) --k;
+    while (k > 4 && std::ldexp(bound, k) >= 2147483648.0 * 0.99) --k;
     h->fx_shift = k;
+    // FP64 form: the whole mesh sums in 64 bits; no point can hold more than
+    // np * max|q| * (max B-spline value)^3
+    double bound64 = (double)h->np * qmax * mmax * mmax * mmax * 1.01;
+    int k64 = 52;
+    while (k64 > 20 && std::ldexp(bound64, k64) >= 9.2e18 * 0.5) --k64;
+    h->fx_shift64 = k64;
     bool mixed = h->form == MG_MIXED;
     size_t n3 = (size_t)n * n * n, nc = (size_t)h->nh * n * n, no = (size_t)h->nh * h->nh * h->nh;
     std::vector<double> mf, ew, vw;
@@ -767,6 +833,7 @@ int mg_spme_launch(mg_handle *h) {
     bk.lnb = ilog2(h->nbrick_edge);
     bk.fx_scale = std::ldexp(1.0f, h->fx_shift);
     bk.fx_inv = std::ldexp(1.0f, -h->fx_shift);
+    bk.fx_scale64 = std::ldexp(1.0, h->fx_shift64);
     bk.tile = h->brick + h->order - 1;
     bk.nbricks = h->nbricks;
     bk.count = h->d_brick_count;
@@ -774,11 +841,13 @@ int mg_spme_launch(mg_handle *h) {
     bk.rank = h->d_brick_rank;
     bk.brick = h->d_brick_of;
     bk.start = h->d_brick_start;
-    size_t n3t = (size_t)n * n * n;
+    bk.M = h->spread_m;
+    bk.istart = h->d_brick_istart;
+    bk.item_brick = h->d_item_brick;
     bool mixed = h->form == MG_MIXED;
     MG_TRY(mg_phase_begin(h, "splines"));
-    if (mixed) MG_TRY((mesh_kernel<float, unsigned long long>(h, 0, sa, bk)));
-    else MG_TRY((mesh_kernel<double, double>(h, 0, sa, bk)));
+    if (mixed) MG_TRY((mesh_kernel<float, int>(h, 0, sa, bk)));
+    else MG_TRY((mesh_kernel<double, long long>(h, 0, sa, bk)));
     MG_TRY(mg_phase_end(h, "splines"));
     MG_TRY(mg_phase_begin(h, "brick_sort"));
     k_brick_count<<<gb, tb, 0, h->st>>>(h->d_corner, np, bk);
@@ -787,32 +856,24 @@ int mg_spme_launch(mg_handle *h) {
     h->launches += 3;
     MG_TRY(mg_phase_end(h, "brick_sort"));
     MG_TRY(mg_phase_begin(h, "spread"));
-    if (mixed) MG_TRY((mesh_kernel<float, unsigned long long>(h, 1, sa, bk)));
-    else MG_TRY((mesh_kernel<double, double>(h, 1, sa, bk)));
+    if (mixed) MG_TRY((mesh_kernel<float, int>(h, 1, sa, bk)));
+    else MG_TRY((mesh_kernel<double, long long>(h, 1, sa, bk)));
     MG_TRY(mg_phase_end(h, "spread"));
-    MG_TRY(mg_phase_begin(h, "mesh_fold"));
-    if (mixed)
-        k_fold_tiles<float><<<(unsigned)((n3t + 255) / 256), 256, 0, h->st>>>((const float *)h->d_tiles, bk,
-                                                                            h->order, (float *)h->d_Q);
-    else
-        k_fold_tiles<double><<<(unsigned)((n3t + 255) / 256), 256, 0, h->st>>>((const double *)h->d_tiles, bk,
-                                                                             h->order, (double *)h->d_Q);
-    h->launches++;
-    MG_TRY(mg_phase_end(h, "mesh_fold"));
     if (mixed) {
         cv.mf = h->d_mf_f;
         cv.ew = h->d_ew_f;
         cv.vw = h->d_vw_f;
-        MG_TRY(fft_launch<float>(h, (float *)h->d_Q, (float2 *)h->d_F, (const float2 *)h->d_tw, cv));
+        MG_TRY(fft_launch<float>(h, (float *)h->d_Q, (float2 *)h->d_F, (const float2 *)h->d_tw, cv, bk.fx_inv));
     } else {
         cv.mf = h->d_mf;
         cv.ew = h->d_ew;
         cv.vw = h->d_vw;
-        MG_TRY(fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv));
+        MG_TRY(fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv,
+                                  1.0 / bk.fx_scale64));
     }
     MG_TRY(mg_phase_begin(h, "gather"));
-    if (mixed) MG_TRY((mesh_kernel<float, unsigned long long>(h, 2, sa, bk)));
-    else MG_TRY((mesh_kernel<double, double>(h, 2, sa, bk)));
+    if (mixed) MG_TRY((mesh_kernel<float, int>(h, 2, sa, bk)));
+    else MG_TRY((mesh_kernel<double, long long>(h, 2, sa, bk)));
     MG_TRY(mg_phase_end(h, "gather"));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
