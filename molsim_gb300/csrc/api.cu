@@ -96,6 +96,7 @@ void mg_phase_collect(mg_handle *h) {
 
 // ---- handle ------------------------------------------------------------------
 static void free_all(mg_handle *h) {
+    mg_mc_free(h);
     void *ptrs[] = {h->d_ro, h->d_az, h->d_type, h->d_pairidx, h->d_ubuf, h->d_r2umin, h->d_r2atat,
                     h->d_ubuf_f, h->d_tab_start, h->d_tab_n, h->d_cellof, h->d_cellcount,
                     h->d_cellstart, h->d_cellfill, h->d_perm, h->d_slot, h->d_nnb, h->d_nbr,
@@ -366,6 +367,10 @@ int mg_celllist_get(mg_handle *h, int32_t *ncell, int32_t *cellip) {
 int mg_utotal(mg_handle *h, double *forceo, double *u_twob, double *uout) {
     if (!h) return MG_ERR_ARG;
     if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_nlist_set has not been called");
+    if (h->list_stale) {   // MC with a cell list: the reference's pair sum sees the current cells
+        MG_TRY(mg_lists_build(h, false));
+        h->list_stale = false;
+    }
     MG_TRY(mg_utotal_launch(h));
     MG_TRY(mg_utotal_fetch(h, forceo, u_twob, uout));
     h->have_force = true;

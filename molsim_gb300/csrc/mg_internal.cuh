@@ -72,6 +72,7 @@ struct mg_handle {
     int *d_nnb = nullptr, *d_nbr = nullptr;
     double4 *d_pos_s = nullptr;
     bool list_valid = false;
+    bool list_stale = false;        // MC + cell list: particles moved since the last build
     // MC cell list (doubly linked lists, reference layout; 1-based, 0 = none)
     int *d_iphead = nullptr, *d_npart = nullptr, *d_ipnext = nullptr, *d_ipprev = nullptr;
     int *d_neighcells = nullptr, nneighcell_max = 0;   // [ncelltot * 27]
@@ -129,6 +130,7 @@ struct mg_handle {
     double urecold = 0;
 
     // ---- MC trial ------------------------------------------------------------
+    void *mc = nullptr;             // trial buffers (mc.cu)
     int nptm = 0;
     int *d_ipnptm = nullptr;
     double *d_rotm = nullptr, *d_du = nullptr;
@@ -230,7 +232,12 @@ int mg_spme_launch(mg_handle *h);                      // spread, FFT, influence
 int mg_ewald_std_init(mg_handle *h);
 int mg_ewald_std_launch(mg_handle *h);
 
+double mg_spme_fx_scale(const mg_handle *h);
+int mg_spme_potential(mg_handle *h);
+int mg_spme_load_mesh(mg_handle *h, const double *q);
+int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul);
 int mg_mc_init(mg_handle *h);
+void mg_mc_free(mg_handle *h);
 int mg_mc_dutotal(mg_handle *h, int nptm, const int32_t *ipnptm, const double *rotm,
                   double *du_twob, double *du_rec, double *du_tot, int32_t *lhsoverlap);
 int mg_mc_accept(mg_handle *h);

@@ -579,6 +579,23 @@ __global__ void __launch_bounds__(256) k_gather_grp(SplineArgs a, const int *__r
     }
 }
 
+// ---- conversions between the fixed-point, FP64 and mesh-type meshes (MC) ----
+__global__ void k_fx_to_f64(const long long *__restrict__ fx, double *__restrict__ q, size_t n, double inv) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = (double)fx[i] * inv;
+}
+
+__global__ void k_f64_to_fx(const double *__restrict__ q, long long *__restrict__ fx, size_t n, double scale) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) fx[i] = __double2ll_rn(q[i] * scale);
+}
+
+template <typename T>
+__global__ void k_mesh_to_f64(const T *__restrict__ Q, double *__restrict__ out, size_t n, double mul) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)Q[i] * mul;
+}
+
 // launch one of the order-templated mesh kernels: 0 = splines, 1 = spread, 2 = gather
 template <typename T, typename ACC, int ORDER>
 void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const BrickArgs &bk) {
@@ -810,6 +827,51 @@ int mg_spme_init(mg_handle *h) {
     return MG_OK;
 }
 
+double mg_spme_fx_scale(const mg_handle *h) {
+    return std::ldexp(1.0, h->form == MG_MIXED ? h->fx_shift : h->fx_shift64);
+}
+
+// The fixed-point charge mesh (d_Qfx) -> forward FFT, energy and virial
+// partial sums, influence function, inverse FFT -> potential mesh in d_Q
+// (the derivative of the reciprocal energy by the mesh charges).  d_Qfx is
+// cleared for the next spread.
+int mg_spme_potential(mg_handle *h) {
+    ConvArgs cv;
+    cv.part = h->d_part + h->part_rec;
+    if (h->form == MG_MIXED) {
+        cv.mf = h->d_mf_f;
+        cv.ew = h->d_ew_f;
+        cv.vw = h->d_vw_f;
+        return fft_launch<float>(h, (float *)h->d_Q, (float2 *)h->d_F, (const float2 *)h->d_tw, cv,
+                                 (float)(1.0 / mg_spme_fx_scale(h)));
+    }
+    cv.mf = h->d_mf;
+    cv.ew = h->d_ew;
+    cv.vw = h->d_vw;
+    return fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv,
+                              1.0 / mg_spme_fx_scale(h));
+}
+
+// FP64 charge mesh -> the fixed-point mesh the FFT reads
+int mg_spme_load_mesh(mg_handle *h, const double *q) {
+    size_t n3 = (size_t)h->nmesh * h->nmesh * h->nmesh;
+    k_f64_to_fx<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>(q, (long long *)h->d_Qfx, n3, mg_spme_fx_scale(h));
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+// potential mesh d_Q (mesh type) -> FP64 copy scaled by mul
+int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul) {
+    size_t n3 = (size_t)h->nmesh * h->nmesh * h->nmesh;
+    unsigned g = (unsigned)((n3 + 255) / 256);
+    if (h->form == MG_MIXED) k_mesh_to_f64<float><<<g, 256, 0, h->st>>>((const float *)h->d_Q, out, n3, mul);
+    else k_mesh_to_f64<double><<<g, 256, 0, h->st>>>((const double *)h->d_Q, out, n3, mul);
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
 int mg_spme_launch(mg_handle *h) {
     int n = h->nmesh, np = h->np;
     size_t n3 = (size_t)n * n * n;
@@ -859,18 +921,12 @@ int mg_spme_launch(mg_handle *h) {
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 1, sa, bk)));
     else MG_TRY((mesh_kernel<double, long long>(h, 1, sa, bk)));
     MG_TRY(mg_phase_end(h, "spread"));
-    if (mixed) {
-        cv.mf = h->d_mf_f;
-        cv.ew = h->d_ew_f;
-        cv.vw = h->d_vw_f;
-        MG_TRY(fft_launch<float>(h, (float *)h->d_Q, (float2 *)h->d_F, (const float2 *)h->d_tw, cv, bk.fx_inv));
-    } else {
-        cv.mf = h->d_mf;
-        cv.ew = h->d_ew;
-        cv.vw = h->d_vw;
-        MG_TRY(fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv,
-                                  1.0 / bk.fx_scale64));
+    if (h->d_Qref) {   // MC: keep the charge mesh of the accepted state in FP64
+        k_fx_to_f64<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>((const long long *)h->d_Qfx, h->d_Qref, n3,
+                                                                    1.0 / mg_spme_fx_scale(h));
+        h->launches++;
     }
+    MG_TRY(mg_spme_potential(h));
     MG_TRY(mg_phase_begin(h, "gather"));
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 2, sa, bk)));
     else MG_TRY((mesh_kernel<double, long long>(h, 2, sa, bk)));

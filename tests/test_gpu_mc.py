@@ -1,0 +1,142 @@
+"""MC trial-move energy differences on the GPU against the oracle.
+
+DUTotal (denergy.F90:98-215) and MCUpdate (mc.F90:5203-5235): the same
+sequence of trials -- single and multi-particle moves, some of them
+overlapping -- runs on the oracle and on the GPU, and every accepted trial
+is accepted on both.  Tolerances (plain FP64 form): the two-body and
+reciprocal differences within 1e-10 of the corresponding total energies
+(the reference forms them as differences of such sums, so its own rounding
+floor is ~1e-16 of them); overlap flags equal; positions after the sequence
+bit for bit.  The ucheck invariant of the reference (molsim.F90:1728-1745)
+then holds on the GPU: UTotal after the moves equals UTotal before plus the
+accepted du%tot.
+"""
+import numpy as np
+import pytest
+
+from molsim_gb300 import Engine, abi, configs
+from tests.helpers import prepared, rel
+
+pytestmark = pytest.mark.gpu
+
+MC = abi.MG_MC
+CASES = [
+    ("spme_vlist", dict(seed=61)),
+    ("spme_cell", dict(seed=62, txintlist=abi.MG_CELLLIST)),
+    ("spme_order8_surf", dict(seed=63, nmesh=32, order=8, lsurf=1)),
+    ("std_vlist_surf", dict(seed=64, ewald=abi.MG_EWALD_STD, ncut=5, lsurf=1)),
+    ("std_cell", dict(seed=65, ewald=abi.MG_EWALD_STD, ncut=5, txintlist=abi.MG_CELLLIST)),
+    ("no_ewald_cell", dict(seed=66, ewald=abi.MG_EWALD_NONE, txintlist=abi.MG_CELLLIST)),
+    ("spme_bonds_vlist", dict(seed=67, chains=3, nseg=8)),
+]
+
+
+def _pair(s, orc, form=abi.MG_FP64):
+    ref = Engine(s, lib=orc, prefix="orc_")
+    gpu = Engine(s, form=form)
+    out = []
+    for e in (ref, gpu):
+        e.SetPositions(s.ro_flat())
+        e.NList("write")
+        out.append(e.UTotal())
+    return ref, gpu, out[0], out[1]
+
+
+def _trial(rng, s, ro, nptm, step):
+    ips = rng.choice(s.np_, size=nptm, replace=False)
+    L = s.boxlen[0]
+    new = ro[ips] + rng.uniform(-step, step, (nptm, 3))
+    new -= L * np.round(new / L)
+    return ips + 1, new
+
+
+@pytest.mark.parametrize("name,kw", CASES, ids=[c[0] for c in CASES])
+def test_dutotal_and_accept_match_oracle(name, kw, orc, gpu_lib):
+    s = prepared(configs.small_system(mode=MC, **kw), orc)
+    ref, gpu, u_ref, u_gpu = _pair(s, orc)
+    scale_tw = max(abs(u_ref["u_twob"][0]), 1.0)
+    scale_rec = max(abs(u_ref["u_rec"]), 1.0)
+    rng = np.random.default_rng(kw["seed"])
+    ro = s.ro.copy()
+    acc, nacc, novl = 0.0, 0, 0
+    for it in range(40):
+        nptm = 3 if it % 5 == 4 else 1
+        ips, new = _trial(rng, s, ro, nptm, 2.5)
+        r, ovl_r = ref.DUTotal(ips, new)
+        g, ovl_g = gpu.DUTotal(ips, new)
+        assert ovl_g == ovl_r, it
+        if ovl_r:
+            novl += 1
+            continue
+        for k in range(s.nptpt + 1):
+            assert abs(g["du_twob"][k] - r["du_twob"][k]) <= 1e-10 * scale_tw, (it, k)
+        assert abs(g["du_rec"] - r["du_rec"]) <= 1e-10 * scale_rec, it
+        assert abs(g["du_tot"] - r["du_tot"]) <= 1e-10 * (scale_tw + scale_rec), it
+        if rng.random() < 0.6:
+            ref.MCUpdate()
+            gpu.MCUpdate()
+            ro[ips - 1] = new
+            acc += g["du_tot"]
+            nacc += 1
+    assert nacc >= 10
+    assert np.array_equal(gpu.GetPositions(), ref.GetPositions())
+    # ucheck on the GPU: a fresh UTotal of the moved configuration
+    u1 = gpu.UTotal()
+    assert abs((u_gpu["u_tot"] + acc) - u1["u_tot"]) <= 1e-9 * (scale_tw + scale_rec)
+    u1_ref = ref.UTotal()
+    assert rel(u1["u_tot"], u1_ref["u_tot"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name,kw", [CASES[0], CASES[1], CASES[3], CASES[5]], ids=lambda x: str(x)[:12])
+def test_batch_trials_match_single_oracle_trials(name, kw, orc, gpu_lib):
+    s = prepared(configs.small_system(mode=MC, **kw), orc)
+    ref, gpu, u_ref, _ = _pair(s, orc)
+    scale = max(abs(u_ref["u_twob"][0]), 1.0) + max(abs(u_ref["u_rec"]), 1.0)
+    rng = np.random.default_rng(kw["seed"] + 100)
+    n = 64
+    ips = rng.integers(s.np_, size=n) + 1
+    L = s.boxlen[0]
+    new = s.ro[ips - 1] + rng.uniform(-2.5, 2.5, (n, 3))
+    new -= L * np.round(new / L)
+    du, ovl = gpu.DUTotalBatch(ips, new)
+    for t in range(n):
+        r, o = ref.DUTotal([ips[t]], new[t:t + 1])
+        assert bool(ovl[t]) == o, t
+        if not o:
+            assert abs(du[t] - r["du_tot"]) <= 1e-10 * scale, t
+    assert ovl.sum() < n
+
+
+def test_batch_leaves_state_unchanged(orc, gpu_lib):
+    s = prepared(configs.small_system(mode=MC, seed=68), orc)
+    _, gpu, _, u0 = _pair(s, orc)
+    rng = np.random.default_rng(68)
+    ips = rng.integers(s.np_, size=200) + 1
+    new = s.ro[ips - 1] + rng.uniform(-1.0, 1.0, (200, 3))
+    new -= s.boxlen[0] * np.round(new / s.boxlen[0])
+    du1, o1 = gpu.DUTotalBatch(ips, new)
+    du2, o2 = gpu.DUTotalBatch(ips, new)
+    assert np.array_equal(du1, du2) and np.array_equal(o1, o2)
+    assert np.array_equal(gpu.GetPositions(), s.ro)
+    with pytest.raises(Exception):
+        gpu.MCUpdate()            # a batch leaves no trial to accept
+
+
+def test_mixed_form_trials_near_fp64(orc, gpu_lib):
+    s = prepared(configs.small_system(mode=MC, seed=69), orc)
+    g64 = Engine(s)
+    gmx = Engine(s, form=abi.MG_MIXED)
+    for e in (g64, gmx):
+        e.SetPositions(s.ro_flat())
+        e.NList("write")
+        e.UTotal()
+    rng = np.random.default_rng(69)
+    ips = rng.integers(s.np_, size=128) + 1
+    new = s.ro[ips - 1] + rng.uniform(-1.0, 1.0, (128, 3))
+    new -= s.boxlen[0] * np.round(new / s.boxlen[0])
+    d64, o64 = g64.DUTotalBatch(ips, new)
+    dmx, omx = gmx.DUTotalBatch(ips, new)
+    assert np.array_equal(o64, omx)
+    ok = ~o64
+    err = np.abs(dmx[ok] - d64[ok])
+    assert np.sqrt((err ** 2).mean()) <= 1e-5 * np.sqrt((d64[ok] ** 2).mean())
