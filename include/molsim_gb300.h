@@ -207,6 +207,22 @@ int mg_accept(mg_handle *h);
 int mg_dutotal_batch(mg_handle *h, int32_t ntrial, const int32_t *ip,
                      const double *rtrial, double *du_tot, int32_t *lhsoverlap);
 
+/* ---- gradients (adjoint form) ------------------------------------------------ */
+
+/* UTotal at the current positions and its gradients with respect to the
+ * parameters (the site potentials are the reference's reciprocal-space
+ * potential, cf. FieldStatEwaldRecSPM energy.F90:2845-2940, plus the
+ * real-space, self and surface parts; the rest has no reference counterpart):
+ *   phi     [np]     dU/dq_i per particle (EpsiFourPi applied)
+ *   du_deps [nptpt]  dU/d eps_ab of every type pair (Pot_1_6_12 with
+ *   du_dsig [nptpt]  sig_ab = (sig_a+sig_b)/2, eps_ab = sqrt(eps_a eps_b))
+ *   du_dbox [3]      dU/dL_a for an affine stretch of the box along a;
+ *                    sum_a L_a du_dbox[a] equals the scalar virial
+ * pp holds the species' sigma, epsilon and lljcut settings the table was
+ * built from.  Any output may be NULL. */
+int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps,
+            double *du_dsig, double *du_dbox);
+
 /* ---- integrators ------------------------------------------------------------ */
 
 /* Velocity-Verlet (VelVer, md.F90:252-420 + GetLinAcc md.F90:601-625) for a

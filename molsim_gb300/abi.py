@@ -85,6 +85,7 @@ LIB_ONLY = [
     ("phase_reset", C.c_int, [H, C.c_int32]),
     ("bench_steps", C.c_int, [H, C.c_int32, C.c_int32, C.c_int64, PF64]),
     ("step_kernels", C.c_int, [H, C.c_int32, PI32]),
+    ("grad", C.c_int, [H, C.POINTER(MgPotParams), PF64, PF64, PF64, PF64]),
     ("ewald_rec_std_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, PF64, C.c_double, C.c_int32,
                                         C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_char_p, C.c_size_t]),

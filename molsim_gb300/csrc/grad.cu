@@ -1,0 +1,438 @@
+// grad.cu — gradients of UTotal with respect to its parameters (row A16 and
+// the adjoint form).
+//
+//   phi(i)     = dU/dq_i, the site potential: real-space Coulomb over the
+//                Verlet list (erfc(alpha r)/r with Ewald, 1/r without), the
+//                reciprocal potential at the site (SPME: the B-spline gather
+//                of the potential mesh with spline values, as
+//                FieldStatEwaldRecSPM, energy.F90:2845-2940, does for
+//                fields; standard Ewald: the k-sum with the structure
+//                factors), the self term and the surface term
+//   dU/deps_ab, dU/dsig_ab
+//                for the (1,6,12) pair parameters of every type pair
+//                (Pot_1_6_12, potential.F90:1349-1434: sig_ab = (sig_a +
+//                sig_b)/2, eps_ab = sqrt(eps_a eps_b), with lljcut's cut and
+//                shift) from the analytic Lennard-Jones form
+//   dU/dL_a    for an affine stretch of the box along a (positions scaled
+//                with it): pairs and bonds through their radial derivative,
+//                the reciprocal sum through the L-dependence of meshfac /
+//                kfac, the surface term through its volume and dipole;
+//                sum_a L_a dU/dL_a is the reference's scalar virial.
+// All arithmetic is FP64 in both forms (the mixed form reads its FP32
+// potential mesh).
+#include <cmath>
+#include <vector>
+
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int kGradThreads = 128;
+
+struct GradArgs {
+    const double *ro, *az;
+    const int *type, *pairidx, *perm, *nnb, *nbr;
+    int np, npt, nptpt, cellcut, ewald;
+    const double *ubuf, *r2atat, *r2umin;
+    const int *tab_start, *tab_n;
+    mg_box box;
+    double rcut2, efp, alpha;
+    const double *sig, *eps, *ljrc;   // per pair type: sigma_ab, eps_ab, ljrcut * sigma_ab
+    int lljcut;
+    double ljushift;
+    double *phi;                      // [np]
+    double *part;                     // per block: deps[nptpt], dsig[nptpt], dL[3]
+};
+
+__global__ void __launch_bounds__(kGradThreads) k_grad_pairs(GradArgs a) {
+    __shared__ double red[2 * MG_MAX_NPTPT + 3][kGradThreads / 32];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double de[MG_MAX_NPTPT], ds[MG_MAX_NPTPT], w0 = 0.0, w1 = 0.0, w2 = 0.0;
+    for (int k = 0; k < a.nptpt; ++k) { de[k] = 0.0; ds[k] = 0.0; }
+    if (i < a.np) {
+        int p = a.perm[i], ti = a.type[p];
+        const double *ri = a.ro + 3 * (size_t)p;
+        double site = 0.0;
+        int nn = a.nnb[i];
+        for (int k = 0; k < nn; ++k) {
+            int q = a.perm[a.nbr[(size_t)k * a.np + i]];
+            const double *rj = a.ro + 3 * (size_t)q;
+            double dx = mg_pbc1(__dsub_rn(ri[0], rj[0]), a.box.half[0], a.box.len[0]);
+            double dy = mg_pbc1(__dsub_rn(ri[1], rj[1]), a.box.half[1], a.box.len[1]);
+            double dz = mg_pbc1(__dsub_rn(ri[2], rj[2]), a.box.half[2], a.box.len[2]);
+            double r2 = mg_r2_exact(dx, dy, dz);
+            if (a.cellcut ? !(r2 < a.rcut2) : (r2 > a.rcut2)) continue;
+            int pair = a.pairidx[a.type[q] * a.npt + ti] - 1;
+            if (r2 < a.r2atat[pair] || r2 < a.r2umin[pair]) continue;   // constant 1e10 / outside the table
+            double r = sqrt(r2);
+            // real-space Coulomb kernel at the site
+            site += a.az[q] * a.efp * (a.ewald != MG_EWALD_NONE ? erfc(a.alpha * r) / r : 1.0 / r);
+            // Lennard-Jones parameter derivatives (each pair is met twice)
+            double sg = a.sig[pair], x = sg * sg / r2;
+            x = x * x * x;
+            bool lj = !a.lljcut || r < a.ljrc[pair];
+            if (lj) {
+                de[pair] += 0.5 * (4.0 * (x * x - x) + (a.lljcut ? a.ljushift : 0.0));
+                ds[pair] += 0.5 * (24.0 * a.eps[pair] / sg) * (2.0 * x * x - x);
+            }
+            // table force: dU/dL_a = -sum fsum dx_a^2 / L_a
+            int rr = a.tab_start[pair], nr = a.tab_n[pair], kk = 0;
+            while (kk + 1 < nr && r2 < a.ubuf[12 * (size_t)(rr + kk)]) ++kk;
+            const double *c = a.ubuf + 12 * (size_t)(rr + kk);
+            double d = r2 - c[0];
+            double fsum = c[7] + d * (c[8] + d * (c[9] + d * (c[10] + d * c[11])));
+            w0 -= 0.5 * fsum * dx * dx;
+            w1 -= 0.5 * fsum * dy * dy;
+            w2 -= 0.5 * fsum * dz * dz;
+        }
+        a.phi[p] = site;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int nv = 2 * a.nptpt + 3;
+    for (int v = 0; v < nv; ++v) {
+        double x = v < a.nptpt ? de[v] : v < 2 * a.nptpt ? ds[v - a.nptpt] : (v == 2 * a.nptpt ? w0 : v == 2 * a.nptpt + 1 ? w1 : w2);
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[v][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double s = 0.0;
+        for (int k = 0; k < kGradThreads / 32; ++k) s += red[threadIdx.x][k];
+        a.part[(size_t)blockIdx.x * nv + threadIdx.x] = s;
+    }
+}
+
+// bonds: dU/dL_a = sum du/dr dx_a^2 / r (divided by L_a at the end)
+__global__ void k_grad_bonds(const double *__restrict__ ro, const int *__restrict__ ij,
+                             const double *__restrict__ bk, const double *__restrict__ beq,
+                             const int *__restrict__ bp, int nbond, mg_box box, double *__restrict__ part) {
+    __shared__ double red[3][8];
+    double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbond; b += gridDim.x * blockDim.x) {
+        int i = ij[2 * b], j = ij[2 * b + 1];
+        double dx = mg_pbc1(ro[3 * (size_t)i] - ro[3 * (size_t)j], box.half[0], box.len[0]);
+        double dy = mg_pbc1(ro[3 * (size_t)i + 1] - ro[3 * (size_t)j + 1], box.half[1], box.len[1]);
+        double dz = mg_pbc1(ro[3 * (size_t)i + 2] - ro[3 * (size_t)j + 2], box.half[2], box.len[2]);
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        int pw = bp[b];
+        double du = bk[b] * pw * pow(r - beq[b], pw - 1) / r;
+        w0 += du * dx * dx;
+        w1 += du * dy * dy;
+        w2 += du * dz * dz;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        w0 += __shfl_down_sync(0xffffffffu, w0, o);
+        w1 += __shfl_down_sync(0xffffffffu, w1, o);
+        w2 += __shfl_down_sync(0xffffffffu, w2, o);
+    }
+    if (lane == 0) { red[0][w] = w0; red[1][w] = w1; red[2][w] = w2; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double x = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x += red[threadIdx.x][k];
+        part[3 * blockIdx.x + threadIdx.x] = x;
+    }
+}
+
+// CardinalBSpline values (mollib.F90:1625-1687)
+__device__ void grad_bspline(int order, double x, double *v) {
+    double last[MG_MAX_ORDER];
+    v[0] = x;
+    v[1] = 1.0 - x;
+    for (int i = 2; i < order; ++i) v[i] = 0.0;
+    for (int nn = 3; nn <= order; ++nn) {
+        for (int i = 0; i < nn - 1; ++i) last[i] = v[i];
+        v[0] = x * last[0] / (nn - 1);
+        for (int i = 1; i <= nn - 2; ++i) {
+            double aa = i + x;
+            v[i] = (aa * last[i] + (nn - aa) * last[i - 1]) / (nn - 1);
+        }
+        v[nn - 1] = (1.0 - x) * last[nn - 2] / (nn - 1);
+    }
+}
+
+// reciprocal, self and surface parts of the site potentials
+struct SiteArgs {
+    const double *ro, *az;
+    int np, ewald, lsurf;
+    double efp, alpha, surf2;          // surf2 = 2 * 2 pi / (3 V)
+    const double *dip;                 // [3] sum q r (UTotal's surface sums)
+    // SPME
+    int n, order, mixed;
+    double dkdr[3];
+    const void *mesh;                  // potential mesh dE/dQ (mesh type)
+    // standard Ewald
+    const int4 *kv;
+    const double *kfac;
+    const double2 *S;
+    int nk;
+    double3 tpbi;
+    double *phi;
+};
+
+__global__ void k_grad_site(SiteArgs a) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.np || a.ewald == MG_EWALD_NONE) return;
+    const double *r = a.ro + 3 * (size_t)p;
+    double rec = 0.0;
+    if (a.ewald == MG_EWALD_SPM) {
+        double w[3][MG_MAX_ORDER];
+        int c[3];
+        for (int d = 0; d < 3; ++d) {
+            double pos = a.dkdr[d] * r[d], fl = floor(pos);
+            int mm = (int)fl % a.n;
+            c[d] = mm < 0 ? mm + a.n : mm;
+            grad_bspline(a.order, pos - fl, w[d]);
+        }
+        int mn = a.n - 1;
+        for (int iz = 0; iz < a.order; ++iz)
+            for (int iy = 0; iy < a.order; ++iy) {
+                size_t row = ((size_t)((c[2] - iz) & mn) * a.n + ((c[1] - iy) & mn)) * a.n;
+                double wyz = w[2][iz] * w[1][iy], s = 0.0;
+                for (int ix = 0; ix < a.order; ++ix) {
+                    size_t idx = row + ((c[0] - ix) & mn);
+                    double v = a.mixed ? (double)((const float *)a.mesh)[idx] : ((const double *)a.mesh)[idx];
+                    s += w[0][ix] * v;
+                }
+                rec += wyz * s;
+            }
+    } else {
+        // d/dq_i sum_k kfac sum_c |S_c|^2 = sum_k kfac sum_c 2 Re(conj(S_c) e_c)
+        for (int k = 0; k < a.nk; ++k) {
+            int4 n = a.kv[k];
+            double sx, cx, sy, cy, sz, cz;
+            sincos(n.x * a.tpbi.x * r[0], &sx, &cx);
+            sincos(n.y * a.tpbi.y * r[1], &sy, &cy);
+            sincos(n.z * a.tpbi.z * r[2], &sz, &cz);
+            // e_c = e^{i(sx kx x + sy ky y + kz z)} for (sx, sy) = (-,-), (-,+), (+,-), (+,+)
+            double acc = 0.0;
+            for (int cmb = 0; cmb < 4; ++cmb) {
+                double ax = (cmb & 2) ? sx : -sx, ay = (cmb & 1) ? sy : -sy;
+                // (cx + i ax)(cy + i ay)(cz + i sz)
+                double re1 = cx * cy - ax * ay, im1 = cx * ay + ax * cy;
+                double re = re1 * cz - im1 * sz, im = re1 * sz + im1 * cz;
+                double2 S = a.S[4 * k + cmb];
+                acc += S.x * re + S.y * im;
+            }
+            rec += 2.0 * a.kfac[k] * acc;
+        }
+    }
+    double q = a.az[p];
+    double v = rec - 2.0 * a.alpha / sqrt(3.1415926535897932) * q;   // UEwaldSelf
+    if (a.lsurf) v += a.surf2 * (a.dip[0] * r[0] + a.dip[1] * r[1] + a.dip[2] * r[2]);
+    a.phi[p] += a.efp * v;
+}
+
+// standard Ewald: dE/dL_a = sum_k kfac g_a(k) sum_c |S_c|^2
+__global__ void k_grad_box_std(const int4 *__restrict__ kv, const double *__restrict__ kfac,
+                               const double2 *__restrict__ S, int nk, double3 tpbi, double3 li, double ia2,
+                               double *__restrict__ out3) {
+    __shared__ double red[3][8];
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+        int4 n = kv[k];
+        double s2 = 0.0;
+        for (int c = 0; c < 4; ++c) s2 += S[4 * k + c].x * S[4 * k + c].x + S[4 * k + c].y * S[4 * k + c].y;
+        double mx = n.x * tpbi.x, my = n.y * tpbi.y, mz = n.z * tpbi.z;
+        mx *= mx;
+        my *= my;
+        mz *= mz;
+        double c = ia2 + 1.0 / (mx + my + mz), e = kfac[k] * s2;
+        g0 += e * (-1.0 + 2.0 * mx * c) * li.x;
+        g1 += e * (-1.0 + 2.0 * my * c) * li.y;
+        g2 += e * (-1.0 + 2.0 * mz * c) * li.z;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        g0 += __shfl_down_sync(0xffffffffu, g0, o);
+        g1 += __shfl_down_sync(0xffffffffu, g1, o);
+        g2 += __shfl_down_sync(0xffffffffu, g2, o);
+    }
+    if (lane == 0) { red[0][w] = g0; red[1][w] = g1; red[2][w] = g2; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double x = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x += red[threadIdx.x][k];
+        out3[threadIdx.x] = x;
+    }
+}
+
+// fixed-order totals: out = [deps(nptpt), dsig(nptpt), dL(3)]
+struct FinalGrad {
+    const double *pair_part;
+    int nblk_pair, nptpt;
+    const double *bond_part;
+    int nblk_bond;
+    const double *rec3;      // dE_rec/dL (before EpsiFourPi) or null
+    const double *dip;       // surface sums or null
+    double efp, surf_fac;
+    double L[3];
+    double *out;
+};
+
+__global__ void k_grad_final(FinalGrad f) {
+    int v = threadIdx.x, nv = 2 * f.nptpt + 3;
+    if (v >= nv) return;
+    double s = 0.0;
+    for (int b = 0; b < f.nblk_pair; ++b) s += f.pair_part[(size_t)b * nv + v];
+    if (v >= 2 * f.nptpt) {
+        int d = v - 2 * f.nptpt;
+        for (int b = 0; b < f.nblk_bond; ++b) s += f.bond_part[3 * b + d];
+        s /= f.L[d];                       // pair and bond sums are L_a dU/dL_a
+        double r = f.rec3 ? f.rec3[d] : 0.0;
+        if (f.dip) {
+            double m2 = f.dip[0] * f.dip[0] + f.dip[1] * f.dip[1] + f.dip[2] * f.dip[2];
+            r += f.surf_fac * (2.0 * f.dip[d] * f.dip[d] - m2) / f.L[d];
+        }
+        s += f.efp * r;
+    }
+    f.out[v] = s;
+}
+
+}  // namespace
+
+int mg_spme_box_grad(mg_handle *h, double *out3, double *scratch);
+
+extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps, double *du_dsig,
+                       double *du_dbox) {
+    if (!h || !pp || !pp->sigat || !pp->epsat) return MG_ERR_ARG;
+    if (pp->npt != h->npt) return mg_fail(h, MG_ERR_ARG, "pot params npt %d != %d", pp->npt, h->npt);
+    if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_nlist_set has not been called");
+    int np = h->np, nptpt = h->nptpt, npt = h->npt;
+    // per pair type: Lorentz-Berthelot sigma_ab, eps_ab and the LJ cut
+    std::vector<double> ab(3 * (size_t)nptpt, 0.0);
+    for (int a = 0; a < npt; ++a)
+        for (int b = 0; b < npt; ++b) {
+            int pair = h->h_pairidx[b * npt + a] - 1;
+            double sg = 0.5 * (pp->sigat[a] + pp->sigat[b]);
+            ab[pair] = sg;
+            ab[nptpt + pair] = std::sqrt(pp->epsat[a] * pp->epsat[b]);
+            ab[2 * nptpt + pair] = pp->ljrcut * sg;
+        }
+    if (h->list_stale) {
+        MG_TRY(mg_lists_build(h, false));
+        h->list_stale = false;
+    }
+    MG_TRY(mg_utotal_launch(h));   // energies, structure factors / potential mesh, surface sums
+    int nblk_pair = (np + kGradThreads - 1) / kGradThreads, nv = 2 * nptpt + 3;
+    int nblk_bond = h->nbond > 0 ? std::min(304, (h->nbond + 255) / 256) : 0;
+    size_t need = (size_t)np + 3 * nptpt + (size_t)nblk_pair * nv + 3 * (size_t)std::max(nblk_bond, 1) + 3 +
+                  3 * 304 + (size_t)nv;
+    if (need > h->grad_cap) {
+        if (h->d_grad) cudaFree(h->d_grad);
+        h->d_grad = nullptr;
+        MG_CUDA(h, cudaMalloc(&h->d_grad, sizeof(double) * need));
+        h->grad_cap = need;
+    }
+    double *d_phi = h->d_grad, *d_ab = d_phi + np, *d_pp = d_ab + 3 * nptpt;
+    double *d_bp = d_pp + (size_t)nblk_pair * nv, *d_rec3 = d_bp + 3 * (size_t)std::max(nblk_bond, 1);
+    double *d_scr = d_rec3 + 3, *d_out = d_scr + 3 * 304;
+    MG_CUDA(h, cudaMemcpyAsync(d_ab, ab.data(), sizeof(double) * 3 * nptpt, cudaMemcpyHostToDevice, h->st));
+    GradArgs a;
+    a.ro = h->d_ro;
+    a.az = h->d_az;
+    a.type = h->d_type;
+    a.pairidx = h->d_pairidx;
+    a.perm = h->d_perm;
+    a.nnb = h->d_nnb;
+    a.nbr = h->d_nbr;
+    a.np = np;
+    a.npt = npt;
+    a.nptpt = nptpt;
+    a.cellcut = h->txintlist == MG_CELLLIST ? 1 : 0;
+    a.ewald = h->ewald;
+    a.ubuf = h->d_ubuf;
+    a.r2atat = h->d_r2atat;
+    a.r2umin = h->d_r2umin;
+    a.tab_start = h->d_tab_start;
+    a.tab_n = h->d_tab_n;
+    for (int d = 0; d < 3; ++d) {
+        a.box.len[d] = h->boxlen[d];
+        a.box.half[d] = h->boxlen2[d];
+        a.box.inv[d] = h->boxleni[d];
+    }
+    a.rcut2 = h->rcut2;
+    a.efp = h->EpsiFourPi;
+    a.alpha = h->ualpha;
+    a.sig = d_ab;
+    a.eps = d_ab + nptpt;
+    a.ljrc = d_ab + 2 * nptpt;
+    a.lljcut = pp->lljcut;
+    a.ljushift = pp->ljushift;
+    a.phi = d_phi;
+    a.part = d_pp;
+    k_grad_pairs<<<nblk_pair, kGradThreads, 0, h->st>>>(a);
+    h->launches++;
+    bool surf = h->lsurf && h->ewald != MG_EWALD_NONE;
+    const double *d_dip = surf ? h->d_uout + nptpt + 1 + 4 : nullptr;
+    if (h->ewald != MG_EWALD_NONE) {
+        SiteArgs s = {};
+        s.ro = h->d_ro;
+        s.az = h->d_az;
+        s.np = np;
+        s.ewald = h->ewald;
+        s.lsurf = surf ? 1 : 0;
+        s.efp = h->EpsiFourPi;
+        s.alpha = h->ualpha;
+        s.surf2 = 2.0 * (2.0 * 3.1415926535897932 / (3.0 * h->vol));
+        s.dip = d_dip;
+        s.n = h->nmesh;
+        s.order = h->order;
+        s.mixed = h->form == MG_MIXED;
+        for (int d = 0; d < 3; ++d) s.dkdr[d] = h->dkdr[d];
+        s.mesh = h->d_Q;
+        s.kv = h->d_kvec;
+        s.kfac = h->d_kfac;
+        s.S = h->d_S;
+        s.nk = h->nkvec;
+        s.tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
+        s.phi = d_phi;
+        k_grad_site<<<(np + 127) / 128, 128, 0, h->st>>>(s);
+        h->launches++;
+    }
+    if (nblk_bond > 0) {
+        mg_box box = a.box;
+        k_grad_bonds<<<nblk_bond, 256, 0, h->st>>>(h->d_ro, h->d_bond_ij, h->d_bond_k, h->d_bond_eq, h->d_bond_p,
+                                                    h->nbond, box, d_bp);
+        h->launches++;
+    }
+    const double *rec3 = nullptr;
+    double3 li = make_double3(1.0 / h->boxlen[0], 1.0 / h->boxlen[1], 1.0 / h->boxlen[2]);
+    if (h->ewald == MG_EWALD_STD) {
+        k_grad_box_std<<<1, 256, 0, h->st>>>(h->d_kvec, h->d_kfac, h->d_S, h->nkvec,
+                                             make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]), li,
+                                             1.0 / (4.0 * h->ualpha * h->ualpha), d_rec3);
+        h->launches++;
+        rec3 = d_rec3;
+    } else if (h->ewald == MG_EWALD_SPM) {
+        MG_TRY(mg_spme_box_grad(h, d_rec3, d_scr));
+        rec3 = d_rec3;
+    }
+    FinalGrad f;
+    f.pair_part = d_pp;
+    f.nblk_pair = nblk_pair;
+    f.nptpt = nptpt;
+    f.bond_part = d_bp;
+    f.nblk_bond = nblk_bond;
+    f.rec3 = rec3;
+    f.dip = d_dip;
+    f.efp = h->EpsiFourPi;
+    f.surf_fac = 2.0 * 3.1415926535897932 / (3.0 * h->vol);
+    for (int d = 0; d < 3; ++d) f.L[d] = h->boxlen[d];
+    f.out = d_out;
+    k_grad_final<<<1, 32, 0, h->st>>>(f);
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
+    std::vector<double> out(nv);
+    if (phi) MG_CUDA(h, cudaMemcpyAsync(phi, d_phi, sizeof(double) * np, cudaMemcpyDeviceToHost, h->st));
+    MG_CUDA(h, cudaMemcpyAsync(out.data(), d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, h->st));
+    MG_TRY(mg_check_device_error(h));
+    if (du_deps)
+        for (int k = 0; k < nptpt; ++k) du_deps[k] = out[k];
+    if (du_dsig)
+        for (int k = 0; k < nptpt; ++k) du_dsig[k] = out[nptpt + k];
+    if (du_dbox)
+        for (int d = 0; d < 3; ++d) du_dbox[d] = out[2 * nptpt + d];
+    return MG_OK;
+}

@@ -129,6 +129,10 @@ struct mg_handle {
     double *d_gker = nullptr;       // MC: real-space kernel g (nmesh^3)
     double urecold = 0;
 
+    // ---- gradients (grad.cu) ----------------------------------------------
+    double *d_grad = nullptr;       // site potentials, pair parameters, partial sums
+    size_t grad_cap = 0;
+
     // ---- MC trial ------------------------------------------------------------
     void *mc = nullptr;             // trial buffers (mc.cu)
     int nptm = 0;

@@ -872,21 +872,15 @@ int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul) {
     return MG_OK;
 }
 
-int mg_spme_launch(mg_handle *h) {
-    int n = h->nmesh, np = h->np;
-    size_t n3 = (size_t)n * n * n;
-    SplineArgs sa;
+static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
+    int n = h->nmesh;
     sa.ro = h->d_ro;
     sa.az = h->d_az;
-    sa.np = np;
+    sa.np = h->np;
     sa.order = h->order;
     sa.n = n;
     sa.n_log = ilog2(n);
     for (int m = 0; m < 3; ++m) sa.dkdr[m] = h->dkdr[m];
-    ConvArgs cv;
-    cv.part = h->d_part + h->part_rec;
-    int tb = 256, gb = (np + tb - 1) / tb;
-    BrickArgs bk;
     bk.n = n;
     bk.B = h->brick;
     bk.nb = h->nbrick_edge;
@@ -906,6 +900,11 @@ int mg_spme_launch(mg_handle *h) {
     bk.M = h->spread_m;
     bk.istart = h->d_brick_istart;
     bk.item_brick = h->d_item_brick;
+}
+
+// splines, brick sort and spread: the charge mesh in d_Qfx
+static int spme_spread(mg_handle *h, const SplineArgs &sa, const BrickArgs &bk) {
+    int np = h->np, tb = 256, gb = (np + tb - 1) / tb;
     bool mixed = h->form == MG_MIXED;
     MG_TRY(mg_phase_begin(h, "splines"));
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 0, sa, bk)));
@@ -921,6 +920,106 @@ int mg_spme_launch(mg_handle *h) {
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 1, sa, bk)));
     else MG_TRY((mesh_kernel<double, long long>(h, 1, sa, bk)));
     MG_TRY(mg_phase_end(h, "spread"));
+    return MG_OK;
+}
+
+// d(E_rec)/dL_a for an affine stretch of the box along a (positions scaled
+// with it, so the mesh charges do not change): sum over the half spectrum of
+// |F|^2 ew(k) g_a(k), g_a = (1/L_a) (-1 + 2 m_a^2 (1/(4 alpha^2) + 1/m^2)),
+// the derivative of meshfac = 4 pi/V exp(-m^2/4alpha^2)/m^2 b2 by L_a.
+template <typename T>
+__global__ void __launch_bounds__(256) k_box_grad(const V2<T> *__restrict__ F, const T *__restrict__ ew, int n,
+                                                  double3 tpbi, double3 li, double ia2, double *__restrict__ part) {
+    __shared__ double red[3][8];
+    int nh = n / 2 + 1;
+    size_t total = (size_t)nh * n * n;
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        int kx = (int)(e % nh), ky = (int)((e / nh) % n), kz = (int)(e / ((size_t)nh * n));
+        int fy = min(ky, n - ky), fz = min(kz, n - kz);
+        if (kx == 0 && fy == 0 && fz == 0) continue;
+        double w = (double)ew[((size_t)fz * nh + fy) * nh + kx];
+        if (w == 0.0) continue;
+        V2<T> f = F[e];
+        double p2 = (double)f.x * f.x + (double)f.y * f.y;
+        double mx = kx * tpbi.x, my = fy * tpbi.y, mz = fz * tpbi.z;
+        mx *= mx;
+        my *= my;
+        mz *= mz;
+        double c = ia2 + 1.0 / (mx + my + mz), pw = p2 * w;
+        g0 += pw * (-1.0 + 2.0 * mx * c) * li.x;
+        g1 += pw * (-1.0 + 2.0 * my * c) * li.y;
+        g2 += pw * (-1.0 + 2.0 * mz * c) * li.z;
+    }
+    int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        g0 += __shfl_down_sync(0xffffffffu, g0, o);
+        g1 += __shfl_down_sync(0xffffffffu, g1, o);
+        g2 += __shfl_down_sync(0xffffffffu, g2, o);
+    }
+    if (lane == 0) { red[0][wp] = g0; red[1][wp] = g1; red[2][wp] = g2; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double x = 0.0;
+        for (int k = 0; k < 8; ++k) x += red[threadIdx.x][k];
+        part[3 * blockIdx.x + threadIdx.x] = x;
+    }
+}
+
+__global__ void k_sum3(const double *__restrict__ part, int nblk, double *__restrict__ out) {
+    if (threadIdx.x >= 3) return;
+    double x = 0.0;
+    for (int b = 0; b < nblk; ++b) x += part[3 * b + threadIdx.x];
+    out[threadIdx.x] = x;
+}
+
+template <typename T> static int box_grad_t(mg_handle *h, double *out3, double *scratch, int nblk) {
+    int n = h->nmesh, logn = ilog2(n), nh = h->nh;
+    int lp = 4;
+    size_t vsz = sizeof(V2<T>);
+    size_t smx = vsz * (n + 2 * (size_t)lp * n);
+    int thx = max(32, min(1024, lp * n / 4));
+    int gx = n * n / (2 * lp);
+    size_t smc = vsz * (n + 2 * (size_t)h->fft_tx * n);
+    int thc = max(32, min(1024, ((h->fft_tx * n / 4) + 31) / 32 * 32));
+    dim3 gc(h->fft_tiles, n);
+    ConvArgs cv = {};
+    V2<T> *F = (V2<T> *)h->d_F;
+    const V2<T> *tw = (const V2<T> *)h->d_tw;
+    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, (T)(1.0 / mg_spme_fx_scale(h)), F, n,
+                                            logn, lp, tw);
+    MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n, h->st));
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, nh, (size_t)n * nh, -1, tw, cv);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, (size_t)n * nh, nh, -1, tw, cv);
+    const T *ew = (const T *)(h->form == MG_MIXED ? (const void *)h->d_ew_f : (const void *)h->d_ew);
+    double3 tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
+    double3 li = make_double3(1.0 / h->boxlen[0], 1.0 / h->boxlen[1], 1.0 / h->boxlen[2]);
+    k_box_grad<T><<<nblk, 256, 0, h->st>>>(F, ew, n, tpbi, li, 1.0 / (4.0 * h->ualpha * h->ualpha), scratch);
+    k_sum3<<<1, 32, 0, h->st>>>(scratch, nblk, out3);
+    h->launches += 6;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+// d(E_rec)/dL (before EpsiFourPi) into the device array out3; scratch holds
+// 3 * 304 doubles
+int mg_spme_box_grad(mg_handle *h, double *out3, double *scratch) {
+    SplineArgs sa;
+    BrickArgs bk;
+    spme_args(h, sa, bk);
+    MG_TRY(spme_spread(h, sa, bk));
+    if (h->form == MG_MIXED) return box_grad_t<float>(h, out3, scratch, 304);
+    return box_grad_t<double>(h, out3, scratch, 304);
+}
+
+int mg_spme_launch(mg_handle *h) {
+    int n = h->nmesh;
+    size_t n3 = (size_t)n * n * n;
+    SplineArgs sa;
+    BrickArgs bk;
+    spme_args(h, sa, bk);
+    bool mixed = h->form == MG_MIXED;
+    MG_TRY(spme_spread(h, sa, bk));
     if (h->d_Qref) {   // MC: keep the charge mesh of the accepted state in FP64
         k_fx_to_f64<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>((const long long *)h->d_Qfx, h->d_Qref, n3,
                                                                     1.0 / mg_spme_fx_scale(h));

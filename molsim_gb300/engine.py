@@ -144,6 +144,19 @@ class Engine:
                                               abi.i32(ovl)), "dutotal_batch")
         return du, ovl.astype(bool)
 
+    def Grad(self):
+        """UTotal at the current positions with its parameter gradients:
+        phi (dU/dq_i), du_deps and du_dsig per type pair, du_dbox (dU/dL_a
+        for an affine stretch of the box)."""
+        pp, keep = self.system.pot_params()
+        phi = np.zeros(self.np)
+        de = np.zeros(self.nptpt)
+        ds = np.zeros(self.nptpt)
+        db = np.zeros(3)
+        self._check(self.lib.mg_grad(self.h, C.byref(pp), abi.f64(phi), abi.f64(de), abi.f64(ds), abi.f64(db)),
+                    "grad")
+        return dict(phi=phi, du_deps=de, du_dsig=ds, du_dbox=db)
+
     # ---- integrators ------------------------------------------------------------
     def MDSetup(self, tstep, rod, rodd=None):
         massip = self.system.massip()
