@@ -250,6 +250,26 @@ int mg_bd_step_host(mg_handle *h, double *ro_io, double *forceo, double *uout);
 /* GauRandom state after the BD steps run so far. */
 int mg_bd_get_seed(mg_handle *h, int32_t *iseed);
 
+/* ---- ensembles of independent replicas -------------------------------------- */
+
+/* No counterpart in the reference (it runs one system per process).  nrep
+ * handles on one device, each set up for MD (mg_md_setup) or BD
+ * (mg_bd_setup) after mg_nlist_set, are stepped together: one CUDA graph
+ * holds one step of every replica (a branch per replica, each with its own
+ * conditional list rebuild), so one launch advances all of them.  A replica
+ * follows the same trajectory as when it runs alone.  The handles stay
+ * owned by the caller and must outlive the ensemble; read a replica's state
+ * with mg_md_run / mg_bd_run (nstep = 0) and mg_get_positions. */
+typedef struct mg_ensemble mg_ensemble;
+int mg_ensemble_create(int32_t nrep, mg_handle *const *handles, mg_ensemble **e);
+/* nstep steps of every replica (kind 0 = velocity Verlet, 1 = BD); *ms (may
+ * be NULL) receives the device time of the nstep graph launches. */
+int mg_ensemble_run(mg_ensemble *e, int32_t kind, int32_t nstep, double *ms);
+/* Kernel launches in one ensemble step (0 before the first run). */
+int mg_ensemble_kernels(mg_ensemble *e, int32_t kind, int32_t *nkernels);
+int mg_ensemble_last_error(const mg_ensemble *e, char *buf, size_t n);
+int mg_ensemble_destroy(mg_ensemble *e);
+
 /* ---- timing ------------------------------------------------------------------ */
 
 /* Average device time per call (ms) of each phase since the last reset,

@@ -86,6 +86,11 @@ LIB_ONLY = [
     ("bench_steps", C.c_int, [H, C.c_int32, C.c_int32, C.c_int64, PF64]),
     ("step_kernels", C.c_int, [H, C.c_int32, PI32]),
     ("grad", C.c_int, [H, C.POINTER(MgPotParams), PF64, PF64, PF64, PF64]),
+    ("ensemble_create", C.c_int, [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    ("ensemble_run", C.c_int, [H, C.c_int32, C.c_int32, PF64]),
+    ("ensemble_kernels", C.c_int, [H, C.c_int32, PI32]),
+    ("ensemble_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
+    ("ensemble_destroy", C.c_int, [H]),
     ("ewald_rec_std_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, PF64, C.c_double, C.c_int32,
                                         C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_char_p, C.c_size_t]),

@@ -10,6 +10,8 @@ SetChainRandom (coordinate.F90:1609-1676: random walks of fixed step).
   electrolyte_spme  N=32768 ions, L=817, SPME order 6, 64^3
   polyelectrolyte   64x200-bead chains + 12800 counterions + 20000 salt
                     pairs (N=65600), L=700, SPME order 6, 128^3, BD
+  replica_set       independent electrolyte boxes of uneven size and salt
+                    concentration for the batched (ensemble) form
   small_system      a scaled-down charged LJ system for parity tests
 """
 import math
@@ -248,3 +250,36 @@ def small_system(seed=7, n=400, L=40.0, ewald=abi.MG_EWALD_SPM, nmesh=16, order=
                   txintlist=txintlist, mode=mode, ewald=ewald, ualpha=alpha_for_erfc(1e-5, rcut),
                   ncut=ncut, order=order, nmesh=nmesh, lsurf=lsurf, lljcut=lljcut,
                   name=f"small_N{len(types)}", **kw)
+
+
+AVOGADRO = 6.02214076e23
+
+
+def replica_set(seed=5, nrep=256, nmin=500, nmax=8000, cmin=0.01, cmax=1.0, rcut=12.0, order=5,
+                spacing=1.6, mode=abi.MG_MD):
+    """nrep electrolyte boxes: N log-uniform in [nmin, nmax] rounded to even,
+    salt concentration c uniform in [cmin, cmax] mol/L setting each box edge
+    (N/2 ion pairs in V = N/(2 c N_A)), charges +-1 e, LJ sigma = 4 A,
+    eps = 0.1 kT truncated at r_c, SPME of the given order on the power-of-
+    two mesh with spacing at most `spacing` A (autotune.tune_spme refines
+    both).  Returns a list of Systems."""
+    T = 298.0
+    kt = units.kT(T)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for r in range(nrep):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax))) / 2)) * 2
+        c = rng.uniform(cmin, cmax)
+        vol = (n / 2) / (c * AVOGADRO) * 1e27          # A^3 (1 L = 1e27 A^3)
+        L = vol ** (1.0 / 3.0)
+        k = 8
+        while L / k > spacing:
+            k *= 2
+        sp = [Species("Na", +1.0, 4.0, 0.1 * kt, mass=23.0), Species("Cl", -1.0, 4.0, 0.1 * kt, mass=35.45)]
+        ro, types = _ions(L, n // 2, n - n // 2, int(rng.integers(1 << 30)))
+        out.append(System(species=sp, iptpn=types, ro=ro, boxlen=np.array([L, L, L]), temp=T,
+                          relpermitt=units.relpermitt_from_bjerrum(7.1, T), rcut=rcut, drnlist=2.0,
+                          txintlist=abi.MG_VLIST, mode=mode, ewald=abi.MG_EWALD_SPM,
+                          ualpha=alpha_for_erfc(1e-5, rcut), order=order, nmesh=k, lsurf=0, lljcut=0,
+                          name=f"replica{r}_N{n}_c{c:.3f}"))
+    return out

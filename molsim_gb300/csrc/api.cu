@@ -10,6 +10,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <new>
+#include <string>
 
 #include "mg_internal.cuh"
 
@@ -403,14 +405,11 @@ int mg_md_setup(mg_handle *h, double tstep, const double *massip, const double *
     return mg_integrate_md_setup(h, tstep, massip, rod, rodd);
 }
 
-static int capture_step(mg_handle *h, bool bd) {
-    cudaGraphExec_t &g = bd ? h->g_bd : h->g_md;
-    if (g) return MG_OK;
-    // The step is captured with the Verlet-list rebuild in the body of a
-    // conditional (IF) node whose condition the list check sets on the
-    // device, so steps without a rebuild launch none of its kernels.
-    cudaGraph_t graph = nullptr;
-    MG_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+// Append one device step of handle h to the graph that h->st is being
+// captured into.  The Verlet-list rebuild goes into the body of a
+// conditional (IF) node whose condition the list check sets on the device,
+// so steps without a rebuild launch none of its kernels.
+static int capture_step_body(mg_handle *h, bool bd) {
     cudaStreamCaptureStatus cs;
     cudaGraph_t cg = nullptr;
     cudaError_t ce = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &cg, nullptr, nullptr, nullptr);
@@ -451,16 +450,12 @@ static int capture_step(mg_handle *h, bool bd) {
             if (side) cudaStreamDestroy(side);
         }
     }
-    cudaError_t ce3 = cudaStreamEndCapture(h->st, &graph);
-    if (st != MG_OK) {
-        if (graph) cudaGraphDestroy(graph);
-        return st;
-    }
-    if (ce == cudaSuccess) ce = ce3;
-    if (ce != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-    }
+    if (st != MG_OK) return st;
+    if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    return MG_OK;
+}
+
+static int count_kernels(cudaGraph_t graph) {
     size_t nn = 0;
     cudaGraphGetNodes(graph, nullptr, &nn);
     std::vector<cudaGraphNode_t> nodes(nn);
@@ -470,7 +465,22 @@ static int capture_step(mg_handle *h, bool bd) {
         cudaGraphNodeType t;
         if (cudaGraphNodeGetType(n, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
     }
-    (bd ? h->kernels_bd : h->kernels_md) = nk;
+    return nk;
+}
+
+static int capture_step(mg_handle *h, bool bd) {
+    cudaGraphExec_t &g = bd ? h->g_bd : h->g_md;
+    if (g) return MG_OK;
+    cudaGraph_t graph = nullptr;
+    MG_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int st = capture_step_body(h, bd);
+    cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
+    if (st != MG_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (st != MG_OK) return st;
+        return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    }
+    (bd ? h->kernels_bd : h->kernels_md) = count_kernels(graph);
     ce = cudaGraphInstantiate(&g, graph, 0);
     cudaGraphDestroy(graph);
     if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
@@ -624,3 +634,157 @@ int mg_phase_reset(mg_handle *h, int32_t enable) {
 }
 
 }  // extern "C"
+
+// ---- ensembles of independent systems --------------------------------------
+//
+// Every replica keeps its own handle (arrays, stream, lists); the ensemble
+// captures one step of all of them into a single CUDA graph -- one branch per
+// replica, forked from and joined to the ensemble's stream -- so one graph
+// launch advances every replica by one step and the replicas' small kernels
+// run side by side.  Each branch is the replica's own step, so a replica in
+// an ensemble follows the same trajectory as when it runs alone.
+
+struct mg_ensemble {
+    std::vector<mg_handle *> hs;
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    int kernels[2] = {0, 0};
+    std::string err;
+};
+
+#define MG_TRY_E(e, x)                  \
+    do {                                \
+        int _s = (x);                   \
+        if (_s != MG_OK) return _s;     \
+    } while (0)
+
+static int ens_fail(mg_ensemble *e, int code, const char *msg) {
+    if (e) e->err = msg;
+    return code;
+}
+
+int mg_ensemble_create(int32_t nrep, mg_handle *const *handles, mg_ensemble **out) {
+    if (nrep < 1 || !handles || !out) return MG_ERR_ARG;
+    *out = nullptr;
+    mg_ensemble *e = new (std::nothrow) mg_ensemble();
+    if (!e) return MG_ERR_ALLOC;
+    int dev = handles[0] ? handles[0]->dev : 0;
+    for (int r = 0; r < nrep; ++r) {
+        if (!handles[r] || handles[r]->dev != dev) {
+            delete e;
+            return MG_ERR_ARG;
+        }
+        e->hs.push_back(handles[r]);
+    }
+    cudaSetDevice(dev);
+    if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
+        mg_ensemble_destroy(e);
+        return MG_ERR_CUDA;
+    }
+    e->join.resize(nrep, nullptr);
+    for (int r = 0; r < nrep; ++r)
+        if (cudaEventCreateWithFlags(&e->join[r], cudaEventDisableTiming) != cudaSuccess) {
+            mg_ensemble_destroy(e);
+            return MG_ERR_CUDA;
+        }
+    *out = e;
+    return MG_OK;
+}
+
+int mg_ensemble_destroy(mg_ensemble *e) {
+    if (!e) return MG_OK;
+    for (int k = 0; k < 2; ++k)
+        if (e->g[k]) cudaGraphExecDestroy(e->g[k]);
+    for (cudaEvent_t ev : e->join)
+        if (ev) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->st) cudaStreamDestroy(e->st);
+    delete e;
+    return MG_OK;
+}
+
+static int ens_capture(mg_ensemble *e, int kind) {
+    if (e->g[kind]) return MG_OK;
+    bool bd = kind == 1;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return ens_fail(e, MG_ERR_CUDA, "ensemble: begin capture failed");
+    cudaError_t ce = cudaEventRecord(e->fork, e->st);
+    int st = MG_OK;
+    for (size_t r = 0; r < e->hs.size() && ce == cudaSuccess && st == MG_OK; ++r) {
+        mg_handle *h = e->hs[r];
+        ce = cudaStreamWaitEvent(h->st, e->fork, 0);   // the replica's stream joins the capture
+        if (ce == cudaSuccess) st = capture_step_body(h, bd);
+        if (ce == cudaSuccess && st == MG_OK) ce = cudaEventRecord(e->join[r], h->st);
+        if (ce == cudaSuccess && st == MG_OK) ce = cudaStreamWaitEvent(e->st, e->join[r], 0);
+        if (st != MG_OK) e->err = "replica " + std::to_string(r) + ": " + h->err;
+    }
+    cudaError_t ce2 = cudaStreamEndCapture(e->st, &graph);
+    if (st != MG_OK || ce != cudaSuccess || ce2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (st != MG_OK) return st;
+        e->err = std::string("ensemble capture: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ce2);
+        return MG_ERR_CUDA;
+    }
+    e->kernels[kind] = count_kernels(graph);
+    ce = cudaGraphInstantiate(&e->g[kind], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return ens_fail(e, MG_ERR_CUDA, "ensemble: graph instantiate failed");
+    return MG_OK;
+}
+
+int mg_ensemble_run(mg_ensemble *e, int32_t kind, int32_t nstep, double *ms) {
+    if (!e || nstep < 0 || (kind != 0 && kind != 1)) return MG_ERR_ARG;
+    for (size_t r = 0; r < e->hs.size(); ++r) {
+        mg_handle *h = e->hs[r];
+        if (!(kind ? h->bd_ready : h->md_ready) || !h->list_valid)
+            return ens_fail(e, MG_ERR_STATE, "every replica needs mg_md_setup / mg_bd_setup and mg_nlist_set");
+        if (h->timing) return ens_fail(e, MG_ERR_STATE, "phase timing must be off in an ensemble");
+        if (kind == 1 && !h->have_force) {   // BD: forces of the starting configuration, as mg_bd_run
+            MG_TRY(mg_utotal_launch(h));
+            h->have_force = true;
+        }
+        if (cudaStreamSynchronize(h->st) != cudaSuccess) return ens_fail(e, MG_ERR_CUDA, "replica stream");
+    }
+    MG_TRY_E(e, ens_capture(e, kind));
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ms) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, e->st);
+    }
+    for (int s = 0; s < nstep; ++s)
+        if (cudaGraphLaunch(e->g[kind], e->st) != cudaSuccess) return ens_fail(e, MG_ERR_CUDA, "graph launch");
+    if (ms) cudaEventRecord(t1, e->st);
+    if (cudaStreamSynchronize(e->st) != cudaSuccess) return ens_fail(e, MG_ERR_CUDA, "ensemble step failed");
+    if (ms) {
+        float f = 0.0f;
+        cudaEventElapsedTime(&f, t0, t1);
+        *ms = f;
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    for (size_t r = 0; r < e->hs.size(); ++r) {
+        int st = mg_check_device_error(e->hs[r]);
+        if (st != MG_OK) {
+            e->err = "replica " + std::to_string(r) + ": " + e->hs[r]->err;
+            return st;
+        }
+    }
+    return MG_OK;
+}
+
+int mg_ensemble_kernels(mg_ensemble *e, int32_t kind, int32_t *nkernels) {
+    if (!e || !nkernels || (kind != 0 && kind != 1)) return MG_ERR_ARG;
+    *nkernels = e->kernels[kind];
+    return MG_OK;
+}
+
+int mg_ensemble_last_error(const mg_ensemble *e, char *buf, size_t n) {
+    if (!e || !buf || n == 0) return MG_ERR_ARG;
+    std::snprintf(buf, n, "%s", e->err.c_str());
+    return MG_OK;
+}
