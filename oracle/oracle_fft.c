@@ -7,8 +7,11 @@
  * with x fastest is transformed to FQ(0:n/2, y, z).  FFTW's published
  * conventions: forward = sum_j x_j exp(-2 pi i jk/n), backward = exp(+...),
  * both unnormalised; c2r assumes Hermitian input.  This file restates those
- * conventions with a plain recursive mixed-radix (2, 3, 5, generic) DFT in
- * double precision; it is checked against numpy.fft in tests.
+ * conventions: power-of-two lengths (every mesh here) by an iterative
+ * radix-2 FFT with two real lines packed into one complex transform, other
+ * lengths by a plain recursive mixed-radix (2, 3, 5, generic) DFT, all in
+ * double precision with long-double twiddles; it is checked against
+ * numpy.fft in tests.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -89,39 +92,82 @@ static void dft_rec(int n, const cpx *in, int stride, cpx *out, int sign, cpx *t
     memcpy(out, tmp, sizeof(cpx) * n);
 }
 
+/* ---- power-of-two lengths: iterative radix-2 (decimation in time) ------- */
+
+static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+/* in-place FFT of a power-of-two length n with the table w of length n
+   (w[j] = exp(-2 pi i j / n)); sign -1 forward, +1 backward */
+static void fft_pow2(int n, cpx *a, int sign, const cpx *w) {
+    for (int i = 1, j = 0; i < n; ++i) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) { cpx t = a[i]; a[i] = a[j]; a[j] = t; }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1, step = n / len;
+        for (int i = 0; i < n; i += len)
+            for (int k = 0; k < half; ++k) {
+                cpx t = w[k * step];
+                if (sign > 0) t.im = -t.im;
+                cpx u = a[i + k], v = a[i + k + half];
+                cpx x = {v.re * t.re - v.im * t.im, v.re * t.im + v.im * t.re};
+                a[i + k].re = u.re + x.re; a[i + k].im = u.im + x.im;
+                a[i + k + half].re = u.re - x.re; a[i + k + half].im = u.im - x.im;
+            }
+    }
+}
+
 static void dft_line(int n, cpx *line, int sign, cpx *work) {
+    if (is_pow2(n)) { fft_pow2(n, line, sign, get_twiddles(n)); return; }
     cpx *in = work, *tmp = work + n;
     memcpy(in, line, sizeof(cpx) * n);
     dft_rec(n, in, 1, line, sign, tmp, get_twiddles(n), n);
+}
+
+/* complex FFTs of the columns c of a (n, ncol) array of stride `stride`
+   between rows, in blocks of adjacent columns for cache locality */
+#define COLBLK 8
+static void fft_columns(int n, cpx *base, size_t stride, int ncol, int sign, cpx *buf, cpx *work) {
+    for (int c0 = 0; c0 < ncol; c0 += COLBLK) {
+        int nc = ncol - c0 < COLBLK ? ncol - c0 : COLBLK;
+        for (int t = 0; t < n; ++t)
+            for (int c = 0; c < nc; ++c) buf[(size_t)c * n + t] = base[(size_t)t * stride + c0 + c];
+        for (int c = 0; c < nc; ++c) dft_line(n, buf + (size_t)c * n, sign, work);
+        for (int t = 0; t < n; ++t)
+            for (int c = 0; c < nc; ++c) base[(size_t)t * stride + c0 + c] = buf[(size_t)c * n + t];
+    }
 }
 
 int orc_fft_r2c_3d(int n, const double *q, double *fqd) {
     int nh = n / 2 + 1;
     cpx *fq = (cpx *)fqd;
     cpx *line = malloc(sizeof(cpx) * n), *work = malloc(sizeof(cpx) * 2 * n);
-    if (!line || !work) { free(line); free(work); return -1; }
-    /* x: real -> half spectrum */
-    for (int z = 0; z < n; ++z)
-        for (int y = 0; y < n; ++y) {
-            for (int x = 0; x < n; ++x) { line[x].re = q[((size_t)z * n + y) * n + x]; line[x].im = 0; }
-            dft_line(n, line, -1, work);
-            for (int kx = 0; kx < nh; ++kx) fq[((size_t)z * n + y) * nh + kx] = line[kx];
+    cpx *buf = malloc(sizeof(cpx) * COLBLK * (size_t)n);
+    if (!line || !work || !buf) { free(line); free(work); free(buf); return -1; }
+    /* x: real -> half spectrum, two real lines per complex transform
+       (A + iB; X_A = (Z_k + conj Z_{n-k})/2, X_B = (Z_k - conj Z_{n-k})/2i) */
+    size_t nl = (size_t)n * n;
+    for (size_t l = 0; l < nl; l += 2) {
+        const double *a = q + l * n, *b = (l + 1 < nl) ? q + (l + 1) * n : NULL;
+        for (int x = 0; x < n; ++x) { line[x].re = a[x]; line[x].im = b ? b[x] : 0.0; }
+        dft_line(n, line, -1, work);
+        cpx *fa = fq + l * nh, *fb = fq + (l + 1) * nh;
+        for (int k = 0; k < nh; ++k) {
+            cpx z = line[k], zc = line[(n - k) % n];
+            fa[k].re = 0.5 * (z.re + zc.re);
+            fa[k].im = 0.5 * (z.im - zc.im);
+            if (b) {
+                fb[k].re = 0.5 * (z.im + zc.im);
+                fb[k].im = -0.5 * (z.re - zc.re);
+            }
         }
-    /* y */
-    for (int z = 0; z < n; ++z)
-        for (int kx = 0; kx < nh; ++kx) {
-            for (int y = 0; y < n; ++y) line[y] = fq[((size_t)z * n + y) * nh + kx];
-            dft_line(n, line, -1, work);
-            for (int y = 0; y < n; ++y) fq[((size_t)z * n + y) * nh + kx] = line[y];
-        }
-    /* z */
-    for (int y = 0; y < n; ++y)
-        for (int kx = 0; kx < nh; ++kx) {
-            for (int z = 0; z < n; ++z) line[z] = fq[((size_t)z * n + y) * nh + kx];
-            dft_line(n, line, -1, work);
-            for (int z = 0; z < n; ++z) fq[((size_t)z * n + y) * nh + kx] = line[z];
-        }
-    free(line); free(work);
+    }
+    /* y and z: columns of the half spectrum */
+    for (int z = 0; z < n; ++z) fft_columns(n, fq + (size_t)z * n * nh, nh, nh, -1, buf, work);
+    for (int y = 0; y < n; ++y) fft_columns(n, fq + (size_t)y * nh, (size_t)n * nh, nh, -1, buf, work);
+    free(line); free(work); free(buf);
     return 0;
 }
 
@@ -130,31 +176,35 @@ int orc_fft_c2r_3d(int n, const double *fqd, double *q) {
     size_t nc = (size_t)nh * n * n;
     cpx *fq = malloc(sizeof(cpx) * nc);
     cpx *line = malloc(sizeof(cpx) * n), *work = malloc(sizeof(cpx) * 2 * n);
-    if (!fq || !line || !work) { free(fq); free(line); free(work); return -1; }
+    cpx *buf = malloc(sizeof(cpx) * COLBLK * (size_t)n);
+    if (!fq || !line || !work || !buf) { free(fq); free(line); free(work); free(buf); return -1; }
     memcpy(fq, fqd, sizeof(cpx) * nc);
     /* z, then y: complex backward */
-    for (int y = 0; y < n; ++y)
-        for (int kx = 0; kx < nh; ++kx) {
-            for (int z = 0; z < n; ++z) line[z] = fq[((size_t)z * n + y) * nh + kx];
-            dft_line(n, line, +1, work);
-            for (int z = 0; z < n; ++z) fq[((size_t)z * n + y) * nh + kx] = line[z];
+    for (int y = 0; y < n; ++y) fft_columns(n, fq + (size_t)y * nh, (size_t)n * nh, nh, +1, buf, work);
+    for (int z = 0; z < n; ++z) fft_columns(n, fq + (size_t)z * n * nh, nh, nh, +1, buf, work);
+    /* x: two Hermitian lines per complex transform, Z = X_A + i X_B over the
+       completed spectra; the imaginary parts of the k = 0 and k = n/2 terms
+       are dropped, as a Hermitian-input c2r does */
+    size_t nl = (size_t)n * n;
+    for (size_t l = 0; l < nl; l += 2) {
+        const cpx *ha = fq + l * nh, *hb = (l + 1 < nl) ? fq + (l + 1) * nh : NULL;
+        for (int k = 0; k < n; ++k) {
+            cpx xa, xb = {0.0, 0.0};
+            int kk = k < nh ? k : n - k;
+            double sg = k < nh ? 1.0 : -1.0;
+            xa.re = ha[kk].re; xa.im = sg * ha[kk].im;
+            if (hb) { xb.re = hb[kk].re; xb.im = sg * hb[kk].im; }
+            if (kk == 0 || 2 * kk == n) { xa.im = 0.0; xb.im = 0.0; }
+            line[k].re = xa.re - xb.im;
+            line[k].im = xa.im + xb.re;
         }
-    for (int z = 0; z < n; ++z)
-        for (int kx = 0; kx < nh; ++kx) {
-            for (int y = 0; y < n; ++y) line[y] = fq[((size_t)z * n + y) * nh + kx];
-            dft_line(n, line, +1, work);
-            for (int y = 0; y < n; ++y) fq[((size_t)z * n + y) * nh + kx] = line[y];
+        dft_line(n, line, +1, work);
+        double *qa = q + l * n, *qb = hb ? q + (l + 1) * n : NULL;
+        for (int x = 0; x < n; ++x) {
+            qa[x] = line[x].re;
+            if (qb) qb[x] = line[x].im;
         }
-    /* x: Hermitian completion, backward, real part (the imaginary parts of
-       the k=0 and k=n/2 terms drop out, as for a Hermitian-input c2r) */
-    for (int z = 0; z < n; ++z)
-        for (int y = 0; y < n; ++y) {
-            const cpx *h = fq + ((size_t)z * n + y) * nh;
-            for (int k = 0; k < nh; ++k) line[k] = h[k];
-            for (int k = nh; k < n; ++k) { line[k].re = h[n - k].re; line[k].im = -h[n - k].im; }
-            dft_line(n, line, +1, work);
-            for (int x = 0; x < n; ++x) q[((size_t)z * n + y) * n + x] = line[x].re;
-        }
-    free(fq); free(line); free(work);
+    }
+    free(fq); free(line); free(work); free(buf);
     return 0;
 }
