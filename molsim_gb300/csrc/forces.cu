@@ -406,9 +406,9 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_f32(PairArgsF a) {
     }
     if (i < a.np && j0 == 0) {
         int p = a.perm[i];
-        a.ffx[3 * p + 0] = __double2ll_rn((double)gx * MG_FX_SCALE);
-        a.ffx[3 * p + 1] = __double2ll_rn((double)gy * MG_FX_SCALE);
-        a.ffx[3 * p + 2] = __double2ll_rn((double)gz * MG_FX_SCALE);
+        a.ffx[3 * p + 0] = mg_f2fx(gx);
+        a.ffx[3 * p + 1] = mg_f2fx(gy);
+        a.ffx[3 * p + 2] = mg_f2fx(gz);
     }
     __syncthreads();
     // warp sums in FP32, FP64 across the block's warps
@@ -506,8 +506,9 @@ struct ReduceArgs {
     double *uout;
 };
 
-// one warp per value, lane-strided sums combined by a fixed shuffle tree
-__global__ void k_reduce(ReduceArgs a) {
+// one warp per value (launched with a warp for every value), lane-strided
+// sums combined by a fixed shuffle tree
+__global__ void __launch_bounds__(1024) k_reduce(ReduceArgs a) {
     __shared__ double vals[MG_MAX_NPTPT + 1 + 2 + 2 + 3];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int nv_pair = a.nptpt + 1;
@@ -519,8 +520,17 @@ __global__ void k_reduce(ReduceArgs a) {
         else if (v < nv_pair + 2) { src = a.part + a.off_rec; stride = 2; nblk = a.nblk_rec; comp = v - nv_pair; }
         else if (v < nv_pair + 4) { src = a.part + a.off_bond; stride = 2; nblk = a.nblk_bond; comp = v - nv_pair - 2; }
         else { src = a.part + a.off_surf; stride = 3; nblk = a.nblk_surf; comp = v - nv_pair - 4; }
-        double s = 0.0;
-        for (int b = lane; b < nblk; b += 32) s += src[(size_t)b * stride + comp];
+        // the first 48 partials of each lane are loaded together (independent
+        // guarded loads, one memory round trip), summed into eight
+        // accumulators and combined in a fixed order
+        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 48; ++k) {
+            int b = lane + 32 * k;
+            acc[k & 7] += (b < nblk) ? src[(size_t)b * stride + comp] : 0.0;
+        }
+        for (int b = lane + 32 * 48; b < nblk; b += 32) acc[0] += src[(size_t)b * stride + comp];
+        double s = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0) vals[v] = s;
     }
@@ -861,7 +871,7 @@ int mg_utotal_launch(mg_handle *h) {
     r.u_self = h->u_self;
     r.surf_fac = 2.0 * 3.1415926535897932 / (3.0 * h->vol);
     r.uout = h->d_uout;
-    k_reduce<<<1, 256, 0, h->st>>>(r);
+    k_reduce<<<1, 32 * (h->nptpt + 1 + 2 + 2 + 3), 0, h->st>>>(r);
     double surf_k = h->EpsiFourPi * (2.0 * r.surf_fac);
     int lsurf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? 1 : 0;
     if (mixed)

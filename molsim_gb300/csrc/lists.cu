@@ -18,6 +18,9 @@
 
 namespace {
 
+constexpr int kChkThreads = 256;   // list check: threads per block
+
+
 __global__ void k_cell_assign(const double *__restrict__ ro, int np, double3 half, double3 csi,
                               int3 nc, int *__restrict__ cellof, int *__restrict__ count,
                               int *__restrict__ err, const int *__restrict__ gate) {
@@ -176,10 +179,15 @@ __global__ void k_vlist(const double *__restrict__ ro, const int *__restrict__ p
 // device reproduces that exactly: pass 1 accumulates drosum and block maxima,
 // pass 2 finds per block the non-record values given the maximum of all
 // earlier blocks, pass 3 combines.
-__global__ void k_chk_accum(const double *__restrict__ drostep, double *__restrict__ drosum,
-                            double *__restrict__ r2out, double *__restrict__ blkmax, int np,
-                            const int *__restrict__ flag) {
-    __shared__ double red[32];
+// r^2 >= 0, and non-negative doubles order as their 64-bit patterns, so the
+// maxima and the prefix maximum below run on integers (no FP64 pipe)
+__device__ __forceinline__ long long chk_max(long long a, long long b) { return a > b ? a : b; }
+
+__global__ void __launch_bounds__(kChkThreads) k_chk_accum(const double *__restrict__ drostep,
+                                                           double *__restrict__ drosum, double *__restrict__ r2out,
+                                                           double *__restrict__ blkmax, int np,
+                                                           const int *__restrict__ flag) {
+    __shared__ long long red[kChkThreads / 32];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool reset = (*flag != 0);   // a rebuild happened at the previous check
     double r2 = 0.0;
@@ -200,15 +208,15 @@ __global__ void k_chk_accum(const double *__restrict__ drostep, double *__restri
         r2 = mg_r2_exact(s0, s1, s2);
         r2out[p] = r2;
     }
-    double m = r2;
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    long long m = __double_as_longlong(r2);
+    for (int o = 16; o > 0; o >>= 1) m = chk_max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x < 32) {
         int nw = blockDim.x >> 5;
-        double x = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-        if (threadIdx.x == 0) blkmax[blockIdx.x] = x;
+        long long x = (threadIdx.x < nw) ? red[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1) x = chk_max(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if (threadIdx.x == 0) blkmax[blockIdx.x] = __longlong_as_double(x);
     }
 }
 
@@ -216,70 +224,72 @@ __global__ void k_chk_accum(const double *__restrict__ drostep, double *__restri
 // given the maximum of all earlier blocks.  The last block to finish
 // combines the blocks (threadfence + counter) and sets the rebuild flag and,
 // inside a captured step, the graph condition that runs the rebuild.
-__global__ void k_chk_second(const double *__restrict__ r2in, const double *__restrict__ blkmax,
-                             double *__restrict__ blk2, int np, int nblk, double drnlist,
-                             int *__restrict__ flag, int *__restrict__ counter, int use_cond,
-                             cudaGraphConditionalHandle cond) {
-    __shared__ double wmax[32], red[32];
-    __shared__ double pb;
+__global__ void __launch_bounds__(kChkThreads) k_chk_second(const double *__restrict__ r2in,
+                                                            const double *__restrict__ blkmax,
+                                                            double *__restrict__ blk2, int np, int nblk,
+                                                            double drnlist, int *__restrict__ flag,
+                                                            int *__restrict__ counter, int use_cond,
+                                                            cudaGraphConditionalHandle cond) {
+    __shared__ long long wmax[32], red[32];
+    __shared__ long long pb;
     __shared__ bool last;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (w == 0) {   // maximum over all earlier blocks, one warp
-        double m = 0.0;
-        for (int b = lane; b < (int)blockIdx.x; b += 32) m = fmax(m, blkmax[b]);
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        long long m = 0;
+        for (int b = lane; b < (int)blockIdx.x; b += 32) m = chk_max(m, __double_as_longlong(blkmax[b]));
+        for (int o = 16; o > 0; o >>= 1) m = chk_max(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (lane == 0) pb = m;
     }
-    double r2 = (p < np) ? r2in[p] : 0.0;
+    long long r2 = (p < np) ? __double_as_longlong(r2in[p]) : 0;
     // inclusive prefix max within the warp
-    double v = r2;
+    long long v = r2;
     for (int o = 1; o < 32; o <<= 1) {
-        double y = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v = fmax(v, y);
+        long long y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = chk_max(v, y);
     }
     if (lane == 31) wmax[w] = v;
     __syncthreads();
     if (w == 0) {
         int nw = blockDim.x >> 5;
-        double x = (lane < nw) ? wmax[lane] : 0.0;
+        long long x = (lane < nw) ? wmax[lane] : 0;
         for (int o = 1; o < 32; o <<= 1) {
-            double y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x = fmax(x, y);
+            long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = chk_max(x, y);
         }
         if (lane < nw) wmax[lane] = x;
     }
     __syncthreads();
-    double excl = __shfl_up_sync(0xffffffffu, v, 1);
-    if (lane == 0) excl = 0.0;
-    if (w > 0) excl = fmax(excl, wmax[w - 1]);
-    double prev = fmax(pb, excl);   // running maximum before this particle
-    double cand = (p < np && !(r2 > prev)) ? r2 : 0.0;
-    for (int o = 16; o > 0; o >>= 1) cand = fmax(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+    long long excl = __shfl_up_sync(0xffffffffu, v, 1);
+    if (lane == 0) excl = 0;
+    if (w > 0) excl = chk_max(excl, wmax[w - 1]);
+    long long prev = chk_max(pb, excl);   // running maximum before this particle
+    long long cand = (p < np && !(r2 > prev)) ? r2 : 0;
+    for (int o = 16; o > 0; o >>= 1) cand = chk_max(cand, __shfl_xor_sync(0xffffffffu, cand, o));
     if (lane == 0) red[w] = cand;
     __syncthreads();
     if (threadIdx.x == 0) {
         int nw = blockDim.x >> 5;
-        double x = 0.0;
-        for (int k = 0; k < nw; ++k) x = fmax(x, red[k]);
-        blk2[blockIdx.x] = x;
+        long long x = 0;
+        for (int k = 0; k < nw; ++k) x = chk_max(x, red[k]);
+        blk2[blockIdx.x] = __longlong_as_double(x);
         __threadfence();
         last = (atomicAdd(counter, 1) == nblk - 1);
     }
     __syncthreads();
     if (!last || threadIdx.x >= 32) return;
     __threadfence();
-    double m1 = 0.0, m2 = 0.0;
+    long long m1 = 0, m2 = 0;
     for (int b = lane; b < nblk; b += 32) {
-        m1 = fmax(m1, ((volatile const double *)blkmax)[b]);
-        m2 = fmax(m2, ((volatile const double *)blk2)[b]);
+        m1 = chk_max(m1, __double_as_longlong(((volatile const double *)blkmax)[b]));
+        m2 = chk_max(m2, __double_as_longlong(((volatile const double *)blk2)[b]));
     }
     for (int o = 16; o > 0; o >>= 1) {
-        m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-        m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+        m1 = chk_max(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+        m2 = chk_max(m2, __shfl_xor_sync(0xffffffffu, m2, o));
     }
     if (lane == 0) {
-        int f = (sqrt(m1) + sqrt(m2) > drnlist) ? 1 : 0;
+        int f = (sqrt(__longlong_as_double(m1)) + sqrt(__longlong_as_double(m2)) > drnlist) ? 1 : 0;
         flag[0] = f;
         *counter = 0;
         if (use_cond) cudaGraphSetConditional(cond, (unsigned)f);
@@ -438,7 +448,7 @@ int mg_lists_init(mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_nnb, sizeof(int) * np));
     MG_CUDA(h, cudaMalloc(&h->d_nbr, sizeof(int) * (size_t)h->maxnb * np));
     MG_CUDA(h, cudaMalloc(&h->d_pos_s, sizeof(double4) * np));
-    h->nblk_chk = (np + 1023) / 1024;
+    h->nblk_chk = (np + kChkThreads - 1) / kChkThreads;
     MG_CUDA(h, cudaMalloc(&h->d_drostep, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMalloc(&h->d_drosum, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMalloc(&h->d_blkmax, sizeof(double) * (2 * h->nblk_chk + np)));
@@ -488,9 +498,9 @@ int mg_lists_build(mg_handle *h, bool conditional) {
 int mg_lists_check(mg_handle *h) {
     int np = h->np, nb = h->nblk_chk;
     double *r2 = h->d_blkmax + 2 * nb;
-    k_chk_accum<<<nb, 1024, 0, h->st>>>(h->d_drostep, h->d_drosum, r2, h->d_blkmax, np,
+    k_chk_accum<<<nb, kChkThreads, 0, h->st>>>(h->d_drostep, h->d_drosum, r2, h->d_blkmax, np,
                                         h->d_rebuild);
-    k_chk_second<<<nb, 1024, 0, h->st>>>(r2, h->d_blkmax, h->d_blkmax + nb, np, nb, h->drnlist,
+    k_chk_second<<<nb, kChkThreads, 0, h->st>>>(r2, h->d_blkmax, h->d_blkmax + nb, np, nb, h->drnlist,
                                          h->d_rebuild, h->d_rebuild + 1, h->use_cond ? 1 : 0,
                                          h->cond);
     h->launches += 2;

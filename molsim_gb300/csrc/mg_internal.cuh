@@ -209,6 +209,18 @@ __device__ __forceinline__ double mg_pbc1(double d, double half, double len) {
     return (fabs(d) > half) ? __dsub_rn(d, copysign(len, d)) : d;
 }
 
+// round(v * 2^32) as a 64-bit integer without the FP64 pipe (the mixed
+// form's fixed-point forces): integer part and fraction are converted
+// separately, both exactly.  |v| >= 2^31 (only the 1e10 hard-core overlap
+// force reaches it) saturates.
+__device__ __forceinline__ long long mg_f2fx(float v) {
+    v = fminf(fmaxf(v, -2147483648.0f), 2147483520.0f);
+    float hi = floorf(v);
+    float fr = v - hi;                                    // exact, in [0, 1)
+    unsigned lo = __float2uint_rn(fr * 4294967296.0f);   // fr * 2^32 < 2^32, exact scaling
+    return ((long long)(int)hi << 32) + (long long)lo;
+}
+
 struct mg_box {
     double len[3], half[3], inv[3];
 };

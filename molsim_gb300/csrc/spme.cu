@@ -296,6 +296,10 @@ struct SplineArgs {
     const double *ro, *az;
     int np, order, n, n_log;
     double dkdr[3];
+    // brick sort, first pass: brick of each particle and its rank among the
+    // brick's particles (log2 of the brick edge and of the bricks per edge)
+    int lB, lnb;
+    int *count, *rank, *brick;
 };
 
 // Spline data of every particle, once per call (the only FP64 of the mesh
@@ -306,12 +310,14 @@ __global__ void k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__re
                                  T *__restrict__ dw) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.np) return;
+    int c[3];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         double pos = a.dkdr[m] * a.ro[3 * p + m];
         double fl = floor(pos);
         int mm = (int)fl % a.n;
-        corner[m * a.np + p] = mm < 0 ? mm + a.n : mm;
+        c[m] = mm < 0 ? mm + a.n : mm;
+        corner[m * a.np + p] = c[m];
         T v[ORDER], d[ORDER];
         bspline_o<T, ORDER>((T)(pos - fl), v, d);
 #pragma unroll
@@ -320,6 +326,9 @@ __global__ void k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__re
             dw[(size_t)(m * ORDER + i) * a.np + p] = d[i];
         }
     }
+    int id = ((((c[2] >> a.lB) << a.lnb) + (c[1] >> a.lB)) << a.lnb) + (c[0] >> a.lB);
+    a.brick[p] = id;
+    a.rank[p] = atomicAdd(&a.count[id], 1);
 }
 
 // ---- brick-sorted spread -------------------------------------------------------
@@ -340,24 +349,25 @@ struct BrickArgs {
     int *item_brick;       // brick of each work item
 };
 
-__global__ void k_brick_count(const int *__restrict__ corner, int np, BrickArgs b) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
-    int bx = corner[p] >> b.lB, by = corner[np + p] >> b.lB, bz = corner[2 * np + p] >> b.lB;
-    int id = (((bz << b.lnb) + by) << b.lnb) + bx;
-    b.brick[p] = id;
-    b.rank[p] = atomicAdd(&b.count[id], 1);
-}
 
 // exclusive prefixes of the brick counts and of the work items per brick
 // (ceil(count / M)), one block of 1024 threads; the item -> brick map is
 // filled and the counts are cleared for the next call
 __global__ void __launch_bounds__(1024) k_brick_prefix(BrickArgs b) {
     __shared__ int wsum[2][32];
+    constexpr int KMAX = 8;   // counts held in registers (one memory round trip) up to 8192 bricks
     int nb = b.nbricks, per = (nb + 1023) / 1024;
     int lo = threadIdx.x * per, hi = min(nb, lo + per);
+    int cnt[KMAX];
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) cnt[k] = (lo + k < hi) ? b.count[lo + k] : 0;
     int s = 0, si = 0;
-    for (int i = lo; i < hi; ++i) {
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) {
+        s += cnt[k];
+        si += (cnt[k] + b.M - 1) / b.M;
+    }
+    for (int i = lo + KMAX; i < hi; ++i) {   // meshes above 8192 bricks
         int c = b.count[i];
         s += c;
         si += (c + b.M - 1) / b.M;
@@ -382,7 +392,7 @@ __global__ void __launch_bounds__(1024) k_brick_prefix(BrickArgs b) {
     int run = v - s + (w ? wsum[0][w - 1] : 0);
     int irun = vi - si + (w ? wsum[1][w - 1] : 0);
     for (int i = lo; i < hi; ++i) {
-        int c = b.count[i], ni = (c + b.M - 1) / b.M;
+        int c = (i - lo < KMAX) ? cnt[i - lo] : b.count[i], ni = (c + b.M - 1) / b.M;
         b.start[i] = run;
         b.istart[i] = irun;
         for (int k = 0; k < ni; ++k) b.item_brick[irun + k] = i;
@@ -519,7 +529,7 @@ template <typename T, bool MIXED, int ORDER>
 __global__ void __launch_bounds__(256) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
                                                     const int *__restrict__ corner, const T *__restrict__ w,
                                                     const T *__restrict__ dw, const T *__restrict__ Q,
-                                                    double efp, double *__restrict__ force,
+                                                    T kx, T ky, T kz, double *__restrict__ force,
                                                     long long *__restrict__ ffx) {
     constexpr int G = ORDER <= 8 ? 8 : 16;
     int g = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G);
@@ -566,16 +576,15 @@ __global__ void __launch_bounds__(256) k_gather_grp(SplineArgs a, const int *__r
         e2 += __shfl_xor_sync(0xffffffffu, e2, o, G);
     }
     if (j != 0 || !valid) return;
+    T qk = -(T)a.az[p];   // kx, ky, kz = dkdr * EpsiFourPi
     if (MIXED) {
-        float qk = (float)(-a.az[p] * efp);
-        ffx[3 * p + 0] += __double2ll_rn((double)(qk * (float)a.dkdr[0] * (float)e0) * MG_FX_SCALE);
-        ffx[3 * p + 1] += __double2ll_rn((double)(qk * (float)a.dkdr[1] * (float)e1) * MG_FX_SCALE);
-        ffx[3 * p + 2] += __double2ll_rn((double)(qk * (float)a.dkdr[2] * (float)e2) * MG_FX_SCALE);
+        ffx[3 * p + 0] += mg_f2fx((float)(qk * kx * e0));
+        ffx[3 * p + 1] += mg_f2fx((float)(qk * ky * e1));
+        ffx[3 * p + 2] += mg_f2fx((float)(qk * kz * e2));
     } else {
-        double qp = a.az[p];
-        force[3 * p + 0] += -qp * (double)e0 * a.dkdr[0] * efp;
-        force[3 * p + 1] += -qp * (double)e1 * a.dkdr[1] * efp;
-        force[3 * p + 2] += -qp * (double)e2 * a.dkdr[2] * efp;
+        force[3 * p + 0] += (double)qk * (double)e0 * (double)kx;
+        force[3 * p + 1] += (double)qk * (double)e1 * (double)ky;
+        force[3 * p + 2] += (double)qk * (double)e2 * (double)kz;
     }
 }
 
@@ -614,9 +623,12 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
             k_spread_warp<T, ACC, ORDER, 16><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
                 bk, corner, w, h->d_az, np, (long long *)h->d_Qfx);
     } else {
+        // force factors dkdr * EpsiFourPi per direction
+        T kx = (T)(h->dkdr[0] * h->EpsiFourPi), ky = (T)(h->dkdr[1] * h->EpsiFourPi),
+          kz = (T)(h->dkdr[2] * h->EpsiFourPi);
         constexpr int G = ORDER <= 8 ? 8 : 16;
         k_gather_grp<T, sizeof(T) == 4, ORDER><<<(unsigned)(((long)np * G + 255) / 256), 256, 0, h->st>>>(
-            sa, h->d_perm, corner, w, (const T *)h->d_spl_dw, (const T *)h->d_Q, h->EpsiFourPi, h->d_force,
+            sa, h->d_perm, corner, w, (const T *)h->d_spl_dw, (const T *)h->d_Q, kx, ky, kz, h->d_force,
             h->d_ffx);
     }
 }
@@ -881,6 +893,11 @@ static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
     sa.n = n;
     sa.n_log = ilog2(n);
     for (int m = 0; m < 3; ++m) sa.dkdr[m] = h->dkdr[m];
+    sa.lB = ilog2(h->brick);
+    sa.lnb = ilog2(h->nbrick_edge);
+    sa.count = h->d_brick_count;
+    sa.rank = h->d_brick_rank;
+    sa.brick = h->d_brick_of;
     bk.n = n;
     bk.B = h->brick;
     bk.nb = h->nbrick_edge;
@@ -911,10 +928,9 @@ static int spme_spread(mg_handle *h, const SplineArgs &sa, const BrickArgs &bk) 
     else MG_TRY((mesh_kernel<double, long long>(h, 0, sa, bk)));
     MG_TRY(mg_phase_end(h, "splines"));
     MG_TRY(mg_phase_begin(h, "brick_sort"));
-    k_brick_count<<<gb, tb, 0, h->st>>>(h->d_corner, np, bk);
-    k_brick_prefix<<<1, 1024, 0, h->st>>>(bk);
+    k_brick_prefix<<<1, 1024, 0, h->st>>>(bk);   // the counts come from the spline kernel
     k_brick_scatter<<<gb, tb, 0, h->st>>>(np, bk);
-    h->launches += 3;
+    h->launches += 2;
     MG_TRY(mg_phase_end(h, "brick_sort"));
     MG_TRY(mg_phase_begin(h, "spread"));
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 1, sa, bk)));
