@@ -520,17 +520,18 @@ __global__ void __launch_bounds__(1024) k_reduce(ReduceArgs a) {
         else if (v < nv_pair + 2) { src = a.part + a.off_rec; stride = 2; nblk = a.nblk_rec; comp = v - nv_pair; }
         else if (v < nv_pair + 4) { src = a.part + a.off_bond; stride = 2; nblk = a.nblk_bond; comp = v - nv_pair - 2; }
         else { src = a.part + a.off_surf; stride = 3; nblk = a.nblk_surf; comp = v - nv_pair - 4; }
-        // the first 48 partials of each lane are loaded together (independent
-        // guarded loads, one memory round trip), summed into eight
-        // accumulators and combined in a fixed order
-        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-        for (int k = 0; k < 48; ++k) {
-            int b = lane + 32 * k;
-            acc[k & 7] += (b < nblk) ? src[(size_t)b * stride + comp] : 0.0;
+        // four independent partial sums per lane (loads in flight together),
+        // combined in a fixed order
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int b = lane;
+        for (; b + 96 < nblk; b += 128) {
+            s0 += src[(size_t)b * stride + comp];
+            s1 += src[(size_t)(b + 32) * stride + comp];
+            s2 += src[(size_t)(b + 64) * stride + comp];
+            s3 += src[(size_t)(b + 96) * stride + comp];
         }
-        for (int b = lane + 32 * 48; b < nblk; b += 32) acc[0] += src[(size_t)b * stride + comp];
-        double s = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+        for (; b < nblk; b += 32) s0 += src[(size_t)b * stride + comp];
+        double s = (s0 + s1) + (s2 + s3);
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0) vals[v] = s;
     }
