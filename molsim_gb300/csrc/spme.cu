@@ -6,21 +6,24 @@
 // file has its own FFT.
 //
 // Pipeline per UTotal (mesh Q[z][y][x], half spectrum F[z][y][kx], kx<=n/2):
-//   bricks   particles binned by the mesh brick (B^3 points) that holds the
-//            upper corner of their B-spline stamp (count, prefix, scatter)
-//   spread   one CTA per brick: every thread owns one row of the brick's tile
-//            (the brick plus an order-1 halo) in shared memory and adds the
-//            stamps crossing it, without atomics; 64-bit fixed point in the
-//            mixed form (bit-reproducible), FP64 in the plain form
-//   fold     each mesh point sums the (at most 8) tiles covering it
-//   x pass   r2c along x; two real lines are packed into one complex line
+//   splines  B-spline values and derivatives per particle; the particle's
+//            brick (B^3 mesh points holding the upper corner of its stamp)
+//            and its rank in that brick (atomic count)
+//   bricks   prefix of the brick counts and of the work items (at most 32
+//            particles of one brick each); particles scattered in brick order
+//   spread   one warp per work item adds its particles' stamps into a
+//            fixed-point tile (the brick plus an order-1 halo) in shared
+//            memory, then adds the tile into the 64-bit fixed-point mesh with
+//            integer atomics (exact, so independent of the order)
+//   x pass   r2c along x from the fixed-point mesh; two real lines are
+//            packed into one complex line; the mesh is then cleared
 //   y pass   complex FFT along y, tiles of TX consecutive kx columns
 //   z pass   complex FFT along z, then the influence function (energy, virial,
 //            multiply by meshfac) and the inverse z FFT while the column is
 //            still in shared memory
 //   y pass   inverse; x pass c2r inverse (FFTW's unnormalised convention)
-//   gather   one CTA per brick stages the potential tile in shared memory;
-//            separable B-spline sums per particle
+//   gather   a group of lanes per particle (lane = stamp plane), separable
+//            B-spline sums over the potential mesh
 // The FFTs are radix-4 Stockham (one radix-2 stage when log2 n is odd) in
 // shared memory; twiddles come from a host table computed in long double.
 #include <algorithm>
