@@ -1,0 +1,143 @@
+"""Gradient of the mean potential energy of a velocity-Verlet trajectory.
+
+L(x0, v0) = 1/(n+1) sum_{k=0..n} U(x_k), where x_k follows the reference's
+velocity Verlet (VelVer, md.F90:252-357) from positions x0 and velocities v0:
+
+    x' = x + dt v + dt^2/2 a,   a' = forceo(x') / m,   v' = v + dt/2 (a + a')
+
+The backward pass is the adjoint of these updates, run from the last step to
+the first.  It needs the forces at every step and Hessian-vector products:
+- The states (x, v, a) are stored every `checkpoint` steps on the forward
+  pass. The backward pass recomputes one segment at a time from its
+  checkpoint, so memory holds one segment, not the whole trajectory.
+- The Hessian-vector products are central differences of the device forces,
+  (forceo(x + eps u) - forceo(x - eps u)) / 2 eps, with eps scaled so that
+  the largest displacement is 1e-5 A.
+
+`TrajectoryFunction` exposes this to torch.autograd; its gradients are
+dL/dx0 and dL/dv0.
+"""
+import numpy as np
+
+from . import abi, units
+from .engine import Engine
+
+
+class Trajectory:
+    """Velocity Verlet of a System through the GPU forces (FP64 form)."""
+
+    def __init__(self, system, dt=0.002, nsteps=50, checkpoint=10, hvp_disp=1e-5):
+        if system.ubuf is None:
+            system.build_table()
+        self.s = system
+        self.dt, self.n, self.ck, self.hvp_disp = dt, nsteps, checkpoint, hvp_disp
+        self.e = Engine(system, form=abi.MG_FP64)
+        self.im = np.repeat(system.massip(), 3)          # inverse masses per coordinate
+        self.L = system.boxlen
+
+    def _wrap(self, x):
+        x = x.reshape(-1, 3)
+        return (x - self.L * np.round(x / self.L)).reshape(-1)
+
+    def forces(self, x):
+        """forceo (reference force scale) and U at positions x (flat)."""
+        self.e.SetPositions(self._wrap(x))
+        self.e.NList("write")
+        r = self.e.UTotal()
+        return r["forceo"].reshape(-1), r["u_tot"]
+
+    def _step(self, x, v, a):
+        dt = self.dt
+        x1 = x + dt * v + 0.5 * dt * dt * a
+        f1, u1 = self.forces(x1)
+        a1 = f1 * self.im
+        v1 = v + 0.5 * dt * (a + a1)
+        return x1, v1, a1, u1
+
+    def forward(self, x0, v0):
+        """L and the checkpoints (x, v, a) every `checkpoint` steps."""
+        f0, u0 = self.forces(x0)
+        x, v, a = x0.copy(), v0.copy(), f0 * self.im
+        usum, cks = u0, {0: (x.copy(), v.copy(), a.copy())}
+        for k in range(1, self.n + 1):
+            x, v, a, u = self._step(x, v, a)
+            usum += u
+            if k % self.ck == 0 and k < self.n:
+                cks[k] = (x.copy(), v.copy(), a.copy())
+        return usum / (self.n + 1), cks
+
+    def _jtv(self, x, lam):
+        """(d acc / dx)^T lam at x: acc = forceo * im and d forceo/dx is
+        symmetric, so this is the force derivative along im * lam."""
+        u = self.im * lam
+        nrm = np.abs(u).max()
+        if nrm == 0.0:
+            return np.zeros_like(lam)
+        eps = self.hvp_disp / nrm
+        fp, _ = self.forces(x + eps * u)
+        fm, _ = self.forces(x - eps * u)
+        return (fp - fm) / (2.0 * eps)
+
+    def backward(self, cks):
+        """dL/dx0 and dL/dv0 by the adjoint of velocity Verlet."""
+        dt, w = self.dt, 1.0 / (self.n + 1)
+        gx = np.zeros_like(cks[0][0])   # adjoints of x, v, a after the step being undone
+        gv = np.zeros_like(gx)
+        ga = np.zeros_like(gx)
+        starts = sorted(cks)
+        for si in range(len(starts) - 1, -1, -1):
+            k0 = starts[si]
+            k1 = starts[si + 1] if si + 1 < len(starts) else self.n
+            # the segment's states, recomputed from its checkpoint
+            xs, vs, as_ = [cks[k0][0]], [cks[k0][1]], [cks[k0][2]]
+            for _ in range(k0, k1):
+                x, v, a, _u = self._step(xs[-1], vs[-1], as_[-1])
+                xs.append(x)
+                vs.append(v)
+                as_.append(a)
+            for j in range(k1 - k0, 0, -1):
+                xk = xs[j]
+                # the loss term U(x_k): dU/dx = -forceo / FORCE_FAC
+                f, _ = self.forces(xk)
+                gx = gx - w * f / units.FORCE_FAC
+                # v' = v + dt/2 a + dt/2 a'
+                ga_tot = ga + 0.5 * dt * gv
+                gv_prev = gv.copy()
+                ga_prev = 0.5 * dt * gv
+                # a' = acc(x')
+                gx = gx + self._jtv(xk, ga_tot)
+                # x' = x + dt v + dt^2/2 a
+                gv_prev = gv_prev + dt * gx
+                ga_prev = ga_prev + 0.5 * dt * dt * gx
+                gv, ga = gv_prev, ga_prev
+                # gx carries over unchanged (dx'/dx = I)
+        # step 0: the loss term U(x0) and a0 = acc(x0)
+        x0 = cks[0][0]
+        f0, _ = self.forces(x0)
+        gx = gx - w * f0 / units.FORCE_FAC + self._jtv(x0, ga)
+        return gx, gv
+
+    def close(self):
+        self.e.close()
+
+
+def trajectory_function():
+    """torch.autograd.Function over (x0, v0) for a Trajectory (imports torch
+    lazily: only the Python side uses it)."""
+    import torch
+
+    class TrajectoryFunction(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x0, v0, traj):
+            L, cks = traj.forward(x0.detach().cpu().numpy().reshape(-1).copy(),
+                                  v0.detach().cpu().numpy().reshape(-1).copy())
+            ctx.traj, ctx.cks, ctx.shape = traj, cks, x0.shape
+            return torch.as_tensor(L, dtype=x0.dtype, device=x0.device)
+
+        @staticmethod
+        def backward(ctx, gout):
+            gx, gv = ctx.traj.backward(ctx.cks)
+            t = lambda g: torch.as_tensor(g, dtype=gout.dtype, device=gout.device).reshape(ctx.shape)
+            return gout * t(gx), gout * t(gv), None
+
+    return TrajectoryFunction
