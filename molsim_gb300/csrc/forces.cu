@@ -23,6 +23,9 @@ namespace {
 
 constexpr int kPairThreads = 128;
 constexpr int kThreads = 256;
+// bonds: the chain beads come first in the particle order, so small blocks
+// spread their FP64 bond work over many SMs
+constexpr int kBondThreads = 64;
 
 // block reduction of nv doubles per thread into out[0..nv) (thread 0 writes)
 template <int BS>
@@ -430,7 +433,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_f32(PairArgsF a) {
 // UBond: every particle adds the forces of its (at most a few) bonds; the
 // bond's first particle counts its energy and virial.
 template <bool MIXED>
-__global__ void __launch_bounds__(kThreads) k_bond(const double *__restrict__ ro, int np,
+__global__ void __launch_bounds__(kBondThreads) k_bond(const double *__restrict__ ro, int np,
                                                    const int *__restrict__ off,
                                                    const int *__restrict__ list,
                                                    const int *__restrict__ ij,
@@ -440,7 +443,7 @@ __global__ void __launch_bounds__(kThreads) k_bond(const double *__restrict__ ro
                                                    double *__restrict__ force,
                                                    long long *__restrict__ ffx,
                                                    double *__restrict__ part) {
-    __shared__ double sh[2 * (kThreads / 32)];
+    __shared__ double sh[2 * (kBondThreads / 32)];
     double acc[2] = {0.0, 0.0};
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < np) {
@@ -476,7 +479,7 @@ __global__ void __launch_bounds__(kThreads) k_bond(const double *__restrict__ ro
             }
         }
     }
-    block_sum<kThreads>(acc, 2, part + (size_t)blockIdx.x * 2, sh);
+    block_sum<kBondThreads>(acc, 2, part + (size_t)blockIdx.x * 2, sh);
 }
 
 // sum of az*r per block (UEwaldSurf, energy.F90:1352-1355)
@@ -706,7 +709,7 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
     int per_block = h->pair_warp ? kPairThreads / 32 : kPairThreads;
     h->nblk_pair = (np + per_block - 1) / per_block;
     if (h->form == MG_MIXED) h->nblk_pair = (int)(((long)np * h->pair_team + kPairThreads - 1) / kPairThreads);
-    h->nblk_bond = (np + kThreads - 1) / kThreads;
+    h->nblk_bond = (np + kBondThreads - 1) / kBondThreads;
     h->nblk_surf = (np + kThreads - 1) / kThreads;
     // rec partials: SPME z-pass blocks or std k-vectors; sized by the caller
     // of mg_forces_init (nblk_rec set before)
@@ -840,12 +843,12 @@ int mg_utotal_launch(mg_handle *h) {
     MG_TRY(mg_phase_begin(h, "bond+reduce"));
     if (h->nbond > 0) {
         if (mixed)
-            k_bond<true><<<h->nblk_bond, kThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
+            k_bond<true><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
                                                                h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
                                                                h->d_bond_p, a.box, h->d_force, h->d_ffx,
                                                                h->d_part + h->part_bond);
         else
-            k_bond<false><<<h->nblk_bond, kThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
+            k_bond<false><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
                                                                 h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
                                                                 h->d_bond_p, a.box, h->d_force, h->d_ffx,
                                                                 h->d_part + h->part_bond);

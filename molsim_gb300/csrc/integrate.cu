@@ -98,7 +98,7 @@ struct BdArgs {
     const double *forceo, *fac1, *fac2;
     const int *type;
     int np;
-    int *rng;               // [0] iseed, [1] flag (1: next call draws a new pair)
+    int *rng;               // [0] iseed, [1] flag (1: next call draws a new pair), [3] block counter
     double *save;
     const double2 *gval;
     const int *cidx, *blkcnt;
@@ -107,22 +107,39 @@ struct BdArgs {
     int *err;
 };
 
-// prefix of the per-block accepted counts in shared memory (inclusive)
+// prefix of the per-block accepted counts in shared memory (inclusive): all
+// threads load (one memory round trip per blockDim counts), warps scan, the
+// warp totals are scanned by warp 0
 __device__ __forceinline__ void load_block_prefix(const int *__restrict__ blkcnt, int nblk, int *sp) {
-    if (threadIdx.x < 32) {
-        int carry = 0;
-        for (int b0 = 0; b0 < nblk; b0 += 32) {
-            int b = b0 + threadIdx.x;
-            int x = (b < nblk) ? blkcnt[b] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, x, o);
-                if ((int)threadIdx.x >= o) x += y;
-            }
-            if (b < nblk) sp[b] = carry + x;
-            carry += __shfl_sync(0xffffffffu, x, 31);
-        }
-    }
+    __shared__ int wtot[32];
+    __shared__ int carry_s;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (threadIdx.x == 0) carry_s = 0;
     __syncthreads();
+    for (int base = 0; base < nblk; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int x = (i < nblk) ? blkcnt[i] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wtot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int t = (lane < nw) ? wtot[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            if (lane < nw) wtot[lane] = t;
+        }
+        __syncthreads();
+        int c = carry_s;
+        if (i < nblk) sp[i] = c + x + (w ? wtot[w - 1] : 0);
+        __syncthreads();
+        if (threadIdx.x == 0) carry_s = c + wtot[nw - 1];
+        __syncthreads();
+    }
 }
 
 // accepted pair j -> offset of its stored deviates (-1 if the stream ran short)
@@ -138,48 +155,52 @@ __device__ __forceinline__ long pair_slot(const int *sp, int nblk, int j) {
     return (long)lo * kCandBlock + (j - before);
 }
 
-// BDStep: drostep = fac1*forceo + fac2*GauRandom; ro += drostep; PBC
+// BDStep: drostep = fac1*forceo + fac2*GauRandom; ro += drostep; PBC.  The
+// last block to finish also advances the GauRandom state past this step's
+// deviates (every block has read the old state by then).
 __global__ void k_bd_move(BdArgs a) {
     extern __shared__ int sp[];
+    __shared__ bool last;
     load_block_prefix(a.blkcnt, a.nblk, sp);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.np) return;
     int off = (a.rng[1] == 0) ? 1 : 0;   // a saved deviate is pending
-    int t = a.type[p];
-    double f1 = a.fac1[t], f2 = a.fac2[t];
-    for (int m = 0; m < 3; ++m) {
-        int g = 3 * p + m;
-        double dev;
-        if (off && g == 0) {
-            dev = *a.save;
-        } else {
-            int hh = g - off;
-            long slot = pair_slot(sp, a.nblk, hh >> 1);
-            if (slot < 0) {
-                mg_dev_error(a.err, MG_ERR_TIMEOUT, p + 1, hh >> 1, a.nblk);
-                dev = 0.0;
+    if (p < a.np) {
+        int t = a.type[p];
+        double f1 = a.fac1[t], f2 = a.fac2[t];
+        for (int m = 0; m < 3; ++m) {
+            int g = 3 * p + m;
+            double dev;
+            if (off && g == 0) {
+                dev = *a.save;
             } else {
-                double2 v = a.gval[slot];
-                dev = (hh & 1) ? v.y : v.x;
+                int hh = g - off;
+                long slot = pair_slot(sp, a.nblk, hh >> 1);
+                if (slot < 0) {
+                    mg_dev_error(a.err, MG_ERR_TIMEOUT, p + 1, hh >> 1, a.nblk);
+                    dev = 0.0;
+                } else {
+                    double2 v = a.gval[slot];
+                    dev = (hh & 1) ? v.y : v.x;
+                }
             }
+            double d = __dadd_rn(__dmul_rn(f1, a.forceo[3 * p + m]), __dmul_rn(f2, dev));
+            a.drostep[3 * p + m] = d;
+            double r = __dadd_rn(a.ro[3 * p + m], d);
+            a.ro[3 * p + m] = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
         }
-        double d = __dadd_rn(__dmul_rn(f1, a.forceo[3 * p + m]), __dmul_rn(f2, dev));
-        a.drostep[3 * p + m] = d;
-        double r = __dadd_rn(a.ro[3 * p + m], d);
-        a.ro[3 * p + m] = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
     }
-}
-
-// advance the GauRandom state past this step's deviates (one warp)
-__global__ void k_bd_state(BdArgs a) {
-    extern __shared__ int sp[];
-    load_block_prefix(a.blkcnt, a.nblk, sp);
-    if (threadIdx.x != 0) return;
-    int off = (a.rng[1] == 0) ? 1 : 0;
+    __syncthreads();   // this block has read the state (rng, save)
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = (atomicAdd(&a.rng[3], 1) == (int)gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    a.rng[3] = 0;
     int need = 3 * a.np - off;
     int J = (need + 1) / 2;
     long slot = pair_slot(sp, a.nblk, J - 1);
-    if (slot < 0) return;   // k_bd_move has flagged the error
+    if (slot < 0) return;   // the move has flagged the error
     int clast = a.cidx[slot];
     unsigned s0 = (unsigned)a.rng[0];
     unsigned sn = (unsigned)(((unsigned long long)s0 * lcg_pow(2ull * (clast + 1))) & kMask31);
@@ -312,9 +333,8 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
         k_bd_cand<false><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
     MG_TRY(mg_phase_end(h, "bd_rng"));
     MG_TRY(mg_phase_begin(h, "bd_move"));
-    k_bd_move<<<(np + 255) / 256, 256, sm, h->st>>>(a);
-    k_bd_state<<<1, 32, sm, h->st>>>(a);
-    h->launches += 3;
+    k_bd_move<<<(np + 255) / 256, 256, sm, h->st>>>(a);   // advances the GauRandom state too
+    h->launches += 2;
     MG_TRY(mg_phase_end(h, "bd_move"));
     MG_TRY(mg_utotal_launch(h));
     MG_TRY(list_step(h));

@@ -46,22 +46,49 @@ template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
 template <typename V> __device__ __forceinline__ V cadd(V a, V b) { V r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename V> __device__ __forceinline__ V csub(V a, V b) { V r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 
+// Unsigned division by a divisor fixed for a whole launch (the half-spectrum
+// width n/2+1, the column-tile width) by one multiply-high and two shifts:
+// Granlund and Montgomery, "Division by invariant integers using
+// multiplication" (1994), the round-up method; exact for every 32-bit n.
+struct FastDiv {
+    unsigned d, m, s1, s2;
+};
+
+static FastDiv make_fastdiv(unsigned d) {
+    unsigned l = 0;
+    while ((1ull << l) < d) ++l;
+    FastDiv f;
+    f.d = d;
+    f.m = (unsigned)(((((unsigned long long)1 << l) - d) << 32) / d + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 0 ? l - 1 : 0;
+    return f;
+}
+
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv &f) {
+    unsigned t = __umulhi(n, f.m);
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 // Stockham FFT of nl lines of length n = 2^logn held in shared memory.  Element
 // (line c, index t) is at buf[c*cs + t*ts].  LINE_MAJOR (ts == 1): threads run
 // along t; otherwise (cs == 1) threads run along c.  Returns the buffer that
 // holds the result.  sign = -1 forward, +1 backward (unnormalised).
 template <typename T, bool LINE_MAJOR>
 __device__ V2<T> *smem_fft(V2<T> *A, V2<T> *B, int n, int logn, int nl, int cs, int ts, int sign,
-                           const V2<T> *__restrict__ tw) {
+                           const V2<T> *__restrict__ tw, const FastDiv &fnl) {
     typedef V2<T> V;
     V *in = A, *out = B;
     int tid = threadIdx.x, nthr = blockDim.x;
-    int Ns = 1;
+    int Ns = 1, logNs = 0;
+    // (line c, index j) of work item b: shifts along a line, the invariant
+    // divider across lines
     if (logn & 1) {
         int nb = n >> 1;
         for (int b = tid; b < nl * nb; b += nthr) {
-            int c = LINE_MAJOR ? b / nb : b % nl;
-            int j = LINE_MAJOR ? b % nb : b / nl;
+            int c, j;
+            if (LINE_MAJOR) { c = b >> (logn - 1); j = b & (nb - 1); }
+            else { j = (int)fdiv((unsigned)b, fnl); c = b - j * nl; }
             V v0 = in[c * cs + j * ts], v1 = in[c * cs + (j + nb) * ts];
             out[c * cs + (2 * j) * ts] = cadd(v0, v1);
             out[c * cs + (2 * j + 1) * ts] = csub(v0, v1);
@@ -69,13 +96,15 @@ __device__ V2<T> *smem_fft(V2<T> *A, V2<T> *B, int n, int logn, int nl, int cs, 
         __syncthreads();
         V *t = in; in = out; out = t;
         Ns = 2;
+        logNs = 1;
     }
     int nq = n >> 2;
     while (Ns < n) {
-        int stride = n / (4 * Ns);
+        int stride = nq >> logNs;   // n / (4 Ns)
         for (int b = tid; b < nl * nq; b += nthr) {
-            int c = LINE_MAJOR ? b / nq : b % nl;
-            int j = LINE_MAJOR ? b % nq : b / nl;
+            int c, j;
+            if (LINE_MAJOR) { c = b >> (logn - 2); j = b & (nq - 1); }
+            else { j = (int)fdiv((unsigned)b, fnl); c = b - j * nl; }
             int k = j & (Ns - 1);
             const V *src = in + c * cs;
             V v0 = src[j * ts], v1 = src[(j + nq) * ts], v2 = src[(j + 2 * nq) * ts],
@@ -106,6 +135,7 @@ __device__ V2<T> *smem_fft(V2<T> *A, V2<T> *B, int n, int logn, int nl, int cs, 
         __syncthreads();
         V *t = in; in = out; out = t;
         Ns <<= 2;
+        logNs += 2;
     }
     return in;
 }
@@ -126,7 +156,7 @@ template <> __device__ __forceinline__ float fx_to_real<float>(long long x) {
 
 template <typename T>
 __global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *__restrict__ F, int n, int logn,
-                            int lp, const V2<T> *__restrict__ tw) {
+                            int lp, const V2<T> *__restrict__ tw, FastDiv fnh) {
     typedef V2<T> V;
     extern __shared__ unsigned char smem_raw[];
     V *s_tw = reinterpret_cast<V *>(smem_raw);
@@ -135,7 +165,7 @@ __global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *
     load_tw<T>(s_tw, tw, n);
     size_t line0 = (size_t)blockIdx.x * 2 * lp;
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
-        int c = e / n, t = e % n;
+        int c = e >> logn, t = e & (n - 1);
         // the spread's fixed-point mesh (cleared after this pass)
         long long q0 = Qfx[(line0 + 2 * c) * n + t], q1 = Qfx[(line0 + 2 * c + 1) * n + t];
         V v;
@@ -144,9 +174,9 @@ __global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *
         A[c * n + t] = v;
     }
     __syncthreads();
-    V *Z = smem_fft<T, true>(A, B, n, logn, lp, n, 1, -1, s_tw);
+    V *Z = smem_fft<T, true>(A, B, n, logn, lp, n, 1, -1, s_tw, fnh);
     for (int e = threadIdx.x; e < lp * nh; e += blockDim.x) {
-        int c = e / nh, k = e % nh;
+        int c = (int)fdiv((unsigned)e, fnh), k = e - c * nh;
         V z = Z[c * n + k], zc = Z[c * n + ((n - k) & (n - 1))];
         V a, b;
         // X_A = (Z_k + conj Z_{n-k})/2,  X_B = (Z_k - conj Z_{n-k})/(2i)
@@ -171,7 +201,7 @@ __global__ void k_fft_x_c2r(const V2<T> *__restrict__ F, T *__restrict__ Q, int 
     load_tw<T>(s_tw, tw, n);
     size_t line0 = (size_t)blockIdx.x * 2 * lp;
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
-        int c = e / n, k = e % n;
+        int c = e >> logn, k = e & (n - 1);
         int kk = (k < nh) ? k : n - k;
         V a = F[(line0 + 2 * c) * nh + kk], b = F[(line0 + 2 * c + 1) * nh + kk];
         if (kk == 0 || kk == n / 2) { a.y = (T)0; b.y = (T)0; }
@@ -182,9 +212,9 @@ __global__ void k_fft_x_c2r(const V2<T> *__restrict__ F, T *__restrict__ Q, int 
         A[c * n + k] = z;
     }
     __syncthreads();
-    V *Z = smem_fft<T, true>(A, B, n, logn, lp, n, 1, +1, s_tw);
+    V *Z = smem_fft<T, true>(A, B, n, logn, lp, n, 1, +1, s_tw, FastDiv{});
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
-        int c = e / n, t = e % n;
+        int c = e >> logn, t = e & (n - 1);
         V z = Z[c * n + t];
         Q[(line0 + 2 * c) * n + t] = z.x;
         Q[(line0 + 2 * c + 1) * n + t] = z.y;
@@ -200,7 +230,7 @@ struct ConvArgs {
 //      inverse transform follow the forward one -------------------------------
 template <typename T, bool CONV>
 __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx, size_t tstride,
-                          size_t ostride, int sign, const V2<T> *__restrict__ tw, ConvArgs cv) {
+                          size_t ostride, int sign, const V2<T> *__restrict__ tw, ConvArgs cv, FastDiv ftx) {
     typedef V2<T> V;
     extern __shared__ unsigned char smem_raw[];
     __shared__ double red[2 * 32];
@@ -210,7 +240,7 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
     int kx0 = blockIdx.x * tx;
     size_t base = (size_t)blockIdx.y * ostride;
     for (int e = threadIdx.x; e < tx * n; e += blockDim.x) {
-        int t = e / tx, c = e % tx;
+        int t = (int)fdiv((unsigned)e, ftx), c = e - t * tx;
         int kx = kx0 + c;
         V v;
         v.x = (T)0;
@@ -219,14 +249,14 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
         A[t * tx + c] = v;
     }
     __syncthreads();
-    V *R = smem_fft<T, false>(A, B, n, logn, tx, 1, tx, sign, s_tw);
+    V *R = smem_fft<T, false>(A, B, n, logn, tx, 1, tx, sign, s_tw, ftx);
     if (CONV) {
         const T *mf = (const T *)cv.mf, *ew = (const T *)cv.ew, *vw = (const T *)cv.vw;
         int ky = blockIdx.y;
         int fy = min(ky, n - ky);
         T e_t = 0, v_t = 0;   // per-thread sums in the mesh type, block sums in FP64
         for (int e = threadIdx.x; e < tx * n; e += blockDim.x) {
-            int t = e / tx, c = e % tx;
+            int t = (int)fdiv((unsigned)e, ftx), c = e - t * tx;
             int kx = kx0 + c;
             if (kx >= nh) continue;
             int fz = min(t, n - t);
@@ -255,10 +285,10 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
             cv.part[2 * blk + 1] = sv;
         }
         V *other = (R == A) ? B : A;
-        R = smem_fft<T, false>(R, other, n, logn, tx, 1, tx, +1, s_tw);
+        R = smem_fft<T, false>(R, other, n, logn, tx, 1, tx, +1, s_tw, ftx);
     }
     for (int e = threadIdx.x; e < tx * n; e += blockDim.x) {
-        int t = e / tx, c = e % tx;
+        int t = (int)fdiv((unsigned)e, ftx), c = e - t * tx;
         int kx = kx0 + c;
         if (kx < nh) F[base + t * tstride + kx] = R[t * tx + c];
     }
@@ -685,18 +715,19 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_
     size_t ystride = nh, yother = (size_t)n * nh;   // y pass: t -> y, other -> z
     size_t zstride = (size_t)n * nh, zother = nh;   // z pass: t -> z, other -> y
     MG_TRY(mg_phase_begin(h, "fft_x_r2c"));
-    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, fx_inv, F, n, logn, lp, tw);
+    FastDiv fnh = make_fastdiv((unsigned)nh), ftx = make_fastdiv((unsigned)h->fft_tx);
+    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, fx_inv, F, n, logn, lp, tw, fnh);
     // the next spread accumulates into a cleared mesh
     MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n, h->st));
     MG_TRY(mg_phase_end(h, "fft_x_r2c"));
     MG_TRY(mg_phase_begin(h, "fft_y_fwd"));
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, -1, tw, cv);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, -1, tw, cv, ftx);
     MG_TRY(mg_phase_end(h, "fft_y_fwd"));
     MG_TRY(mg_phase_begin(h, "fft_z_conv"));
-    k_fft_col<T, true><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, zstride, zother, -1, tw, cv);
+    k_fft_col<T, true><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, zstride, zother, -1, tw, cv, ftx);
     MG_TRY(mg_phase_end(h, "fft_z_conv"));
     MG_TRY(mg_phase_begin(h, "fft_y_inv"));
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, +1, tw, cv);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, +1, tw, cv, ftx);
     MG_TRY(mg_phase_end(h, "fft_y_inv"));
     MG_TRY(mg_phase_begin(h, "fft_x_c2r"));
     k_fft_x_c2r<T><<<gx, thx, smx, h->st>>>(F, Q, n, logn, lp, tw);
@@ -1005,11 +1036,12 @@ template <typename T> static int box_grad_t(mg_handle *h, double *out3, double *
     ConvArgs cv = {};
     V2<T> *F = (V2<T> *)h->d_F;
     const V2<T> *tw = (const V2<T> *)h->d_tw;
+    FastDiv fnh = make_fastdiv((unsigned)nh), ftx = make_fastdiv((unsigned)h->fft_tx);
     k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, (T)(1.0 / mg_spme_fx_scale(h)), F, n,
-                                            logn, lp, tw);
+                                            logn, lp, tw, fnh);
     MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n, h->st));
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, nh, (size_t)n * nh, -1, tw, cv);
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, (size_t)n * nh, nh, -1, tw, cv);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, nh, (size_t)n * nh, -1, tw, cv, ftx);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, (size_t)n * nh, nh, -1, tw, cv, ftx);
     const T *ew = (const T *)(h->form == MG_MIXED ? (const void *)h->d_ew_f : (const void *)h->d_ew);
     double3 tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
     double3 li = make_double3(1.0 / h->boxlen[0], 1.0 / h->boxlen[1], 1.0 / h->boxlen[2]);
