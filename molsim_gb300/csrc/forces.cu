@@ -705,7 +705,11 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
     h->pair_warp = expect > 24.0 ? 1 : 0;
     // mixed form: a team of lanes per slot sized to the expected full list
     // (~2x the half-sphere count), so short lists still fill the GPU
-    h->pair_team = expect < 1.0 ? 1 : expect < 3.0 ? 2 : expect < 10.0 ? 4 : expect < 20.0 ? 8 : expect < 40.0 ? 16 : 32;
+    // lanes per particle: at sparse densities the per-particle latency chain
+    // (list index, neighbour slot, table) dominates, and more lanes per
+    // particle hide it (measured at ~2 neighbours: 1 lane 52 us, 2 lanes
+    // 34 us, 4 lanes 26 us for 65 600 particles)
+    h->pair_team = expect < 1.0 ? 2 : expect < 10.0 ? 4 : expect < 20.0 ? 8 : expect < 40.0 ? 16 : 32;
     int per_block = h->pair_warp ? kPairThreads / 32 : kPairThreads;
     h->nblk_pair = (np + per_block - 1) / per_block;
     if (h->form == MG_MIXED) h->nblk_pair = (int)(((long)np * h->pair_team + kPairThreads - 1) / kPairThreads);

@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
 // along x; the group then combines.  E = sum dM*M*M*phi
 // (energy.F90:1255-1285); force -= q*E*dkdr*EpsiFourPi.
 template <typename T, bool MIXED, int ORDER>
-__global__ void __launch_bounds__(256) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
+__global__ void __launch_bounds__(256, 4) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
                                                     const int *__restrict__ corner, const T *__restrict__ w,
                                                     const T *__restrict__ dw, const T *__restrict__ Q,
                                                     T kx, T ky, T kz, double *__restrict__ force,
