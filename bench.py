@@ -108,6 +108,8 @@ def algorithmic_bytes(kernel, n, k, pairs, nbond, order=6):
         "fft_z_conv": 2 * spec * 8 + 3 * nh ** 3 * 4,         # spectrum in+out, influence tables
         "fft_y_inv": 2 * spec * 8,
         "fft_x_c2r": spec * 8 + k3 * 4,
+        "fft_xy_fwd": k3 * 8 * 2 + spec * 8,                  # fixed-point mesh in and cleared; spectrum out
+        "fft_yx_inv": spec * 8 + k3 * 4,                      # spectrum in; potential mesh out
         "gather": k3 * 4 + n * (4 + 12 + 2 * spl + 8) + n * 48,
         "bond+reduce": nbond * 48 + n * 48,
     }.get(kernel)

@@ -500,44 +500,94 @@ __global__ void __launch_bounds__(kThreads) k_surf_sums(const double *__restrict
 struct ReduceArgs {
     const double *part;
     int nptpt;
-    int off_pair, nblk_pair;
-    int off_rec, nblk_rec;
-    int off_bond, nblk_bond;
-    int off_surf, nblk_surf;
+    int off[4], nblk[4];    // partial arrays: pair, reciprocal, bonds, surface
+    int blk0[5];            // first stage-1 block of each array (blk0[4] = grid)
+    int row0[4];            // first scratch entry of each array
     int ewald, lsurf;
     double EpsiFourPi, u_self, surf_fac;
     double *uout;
+    double *rows;           // stage-1 sums, one row per block
+    unsigned *ticket;       // blocks finished (zero between launches)
 };
 
-// one warp per value (launched with a warp for every value), lane-strided
-// sums combined by a fixed shuffle tree
-__global__ void __launch_bounds__(1024) k_reduce(ReduceArgs a) {
+// Partial sums of the energies and virials -> the UTotal outputs.  The
+// partials are four arrays of rows (pair: nptpt + 1 values per row,
+// reciprocal 2, bonds 2, surface 3).  Stage 1: each block sums
+// kRedThreads / stride consecutive rows of one array (one load per thread)
+// into a scratch row.  Stage 2, in the block that finishes last (a ticket
+// counter): the scratch rows of each array, by its own warps.  Thread t of a
+// group sums the entries t, t + S, ... of its array, S a multiple of the row
+// length, so that one thread always meets the same component; per-thread
+// sums are combined per component by one warp.  Every sum runs in a fixed
+// order.
+constexpr int kRedThreads = 256;
+
+__host__ __device__ __forceinline__ int red_stride(int g, int nv_pair) {
+    return g == 0 ? nv_pair : g == 3 ? 3 : 2;
+}
+
+// sum of component comp over the per-thread sums tsum[t0 + i], i < S
+__device__ __forceinline__ double red_comp(const double *tsum, int t0, int S, int stride, int comp, int lane) {
+    double sv = 0.0;
+    for (int i = comp + stride * lane; i < S; i += 32 * stride) sv += tsum[t0 + i];
+    for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xffffffffu, sv, o);
+    return sv;
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
+    __shared__ double tsum[kRedThreads];
     __shared__ double vals[MG_MAX_NPTPT + 1 + 2 + 2 + 3];
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ int is_last;
+    int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    constexpr int nwarp = kRedThreads / 32;
     int nv_pair = a.nptpt + 1;
-    int nv = nv_pair + 2 + 2 + 3;
-    for (int v = w; v < nv; v += nw) {
-        const double *src;
-        int stride, nblk, comp;
-        if (v < nv_pair) { src = a.part + a.off_pair; stride = nv_pair; nblk = a.nblk_pair; comp = v; }
-        else if (v < nv_pair + 2) { src = a.part + a.off_rec; stride = 2; nblk = a.nblk_rec; comp = v - nv_pair; }
-        else if (v < nv_pair + 4) { src = a.part + a.off_bond; stride = 2; nblk = a.nblk_bond; comp = v - nv_pair - 2; }
-        else { src = a.part + a.off_surf; stride = 3; nblk = a.nblk_surf; comp = v - nv_pair - 4; }
-        // four independent partial sums per lane (loads in flight together),
-        // combined in a fixed order
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        int b = lane;
-        for (; b + 96 < nblk; b += 128) {
-            s0 += src[(size_t)b * stride + comp];
-            s1 += src[(size_t)(b + 32) * stride + comp];
-            s2 += src[(size_t)(b + 64) * stride + comp];
-            s3 += src[(size_t)(b + 96) * stride + comp];
+    {   // stage 1: block -> (array g, its block index within g)
+        int b = blockIdx.x, g = 0;
+        while (g < 3 && b >= a.blk0[g + 1]) ++g;
+        int stride = red_stride(g, nv_pair), rows = kRedThreads / stride, S = rows * stride;
+        const double *src = a.part + a.off[g];
+        size_t r0 = (size_t)(b - a.blk0[g]) * rows, r1 = min(r0 + rows, (size_t)a.nblk[g]);
+        size_t f = r0 * stride + t;
+        tsum[t] = (t < S && f < r1 * stride) ? src[f] : 0.0;
+        __syncthreads();
+        for (int c = w; c < stride; c += nwarp) {
+            double sv = red_comp(tsum, 0, S, stride, c, lane);
+            if (lane == 0) a.rows[a.row0[g] + (size_t)(b - a.blk0[g]) * stride + c] = sv;
         }
-        for (; b < nblk; b += 32) s0 += src[(size_t)b * stride + comp];
-        double s = (s0 + s1) + (s2 + s3);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) vals[v] = s;
     }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) is_last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // stage 2: warps 0-3 the pair rows, 4-5 reciprocal, 6 bonds, 7 surface
+    const int t0s[4] = {0, 128, 192, 224}, nts[4] = {128, 64, 32, 32};
+    int g = w < 4 ? 0 : w < 6 ? 1 : w < 7 ? 2 : 3;
+    int stride = red_stride(g, nv_pair);
+    int S = stride * (nts[g] / stride), tl = t - t0s[g];
+    size_t total = (size_t)(a.blk0[g + 1] - a.blk0[g]) * stride;
+    const double *src = a.rows + a.row0[g];
+    double s0 = 0.0, s1 = 0.0;
+    if (tl < S) {
+        size_t f = tl;
+        for (; f + S < total; f += 2 * (size_t)S) {
+            s0 += __ldcg(src + f);
+            s1 += __ldcg(src + f + S);
+        }
+        if (f < total) s0 += __ldcg(src + f);
+    }
+    tsum[t] = s0 + s1;
+    __syncthreads();
+    int nv = nv_pair + 2 + 2 + 3;
+    for (int v = w; v < nv; v += nwarp) {
+        int gv = v < nv_pair ? 0 : v < nv_pair + 2 ? 1 : v < nv_pair + 4 ? 2 : 3;
+        int comp = gv == 0 ? v : gv == 1 ? v - nv_pair : gv == 2 ? v - nv_pair - 2 : v - nv_pair - 4;
+        int sg = red_stride(gv, nv_pair);
+        double sv = red_comp(tsum, t0s[gv], sg * (nts[gv] / sg), sg, comp, lane);
+        if (lane == 0) vals[v] = sv;
+    }
+    if (t == 0) *a.ticket = 0u;   // for the next launch (graph replays)
     __syncthreads();
     if (threadIdx.x != 0) return;
     double *u = a.uout;
@@ -721,7 +771,9 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
     h->part_rec = h->part_pair + h->nblk_pair * (h->nptpt + 1);
     h->part_bond = h->part_rec + 2 * (h->nblk_rec > 0 ? h->nblk_rec : 1);
     h->part_surf = h->part_bond + 2 * h->nblk_bond;
-    size_t npart = (size_t)h->part_surf + 3 * h->nblk_surf;
+    // k_reduce: its stage-1 rows (at most one per partial row) and its ticket
+    h->part_red = h->part_surf + 3 * h->nblk_surf;
+    size_t npart = 2 * (size_t)h->part_red + 1;
     MG_CUDA(h, cudaMalloc(&h->d_part, sizeof(double) * npart));
     MG_CUDA(h, cudaMemsetAsync(h->d_part, 0, sizeof(double) * npart, h->st));
     MG_CUDA(h, cudaMalloc(&h->d_uout, sizeof(double) * (h->nptpt + 1 + 8)));
@@ -865,21 +917,32 @@ int mg_utotal_launch(mg_handle *h) {
     ReduceArgs r;
     r.part = h->d_part;
     r.nptpt = h->nptpt;
-    r.off_pair = h->part_pair;
-    r.nblk_pair = h->nblk_pair;
-    r.off_rec = h->part_rec;
-    r.nblk_rec = (h->ewald != MG_EWALD_NONE) ? h->nblk_rec : 0;
-    r.off_bond = h->part_bond;
-    r.nblk_bond = (h->nbond > 0) ? h->nblk_bond : 0;
-    r.off_surf = h->part_surf;
-    r.nblk_surf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? h->nblk_surf : 0;
+    r.off[0] = h->part_pair;
+    r.nblk[0] = h->nblk_pair;
+    r.off[1] = h->part_rec;
+    r.nblk[1] = (h->ewald != MG_EWALD_NONE) ? h->nblk_rec : 0;
+    r.off[2] = h->part_bond;
+    r.nblk[2] = (h->nbond > 0) ? h->nblk_bond : 0;
+    r.off[3] = h->part_surf;
+    r.nblk[3] = (h->ewald != MG_EWALD_NONE && h->lsurf) ? h->nblk_surf : 0;
+    r.blk0[0] = 0;
+    r.row0[0] = 0;
+    for (int g = 0; g < 4; ++g) {
+        int stride = red_stride(g, h->nptpt + 1), rows = kRedThreads / stride;
+        int nb = (r.nblk[g] + rows - 1) / rows;
+        r.blk0[g + 1] = r.blk0[g] + nb;
+        if (g < 3) r.row0[g + 1] = r.row0[g] + nb * stride;
+    }
+    if (r.blk0[4] == 0) r.blk0[4] = r.blk0[3] = r.blk0[2] = r.blk0[1] = 1;   // one (empty) pair block
     r.ewald = h->ewald;
     r.lsurf = h->lsurf;
     r.EpsiFourPi = h->EpsiFourPi;
     r.u_self = h->u_self;
     r.surf_fac = 2.0 * 3.1415926535897932 / (3.0 * h->vol);
     r.uout = h->d_uout;
-    k_reduce<<<1, 32 * (h->nptpt + 1 + 2 + 2 + 3), 0, h->st>>>(r);
+    r.rows = h->d_part + h->part_red;
+    r.ticket = reinterpret_cast<unsigned *>(h->d_part + 2 * (size_t)h->part_red);
+    k_reduce<<<r.blk0[4], kRedThreads, 0, h->st>>>(r);
     double surf_k = h->EpsiFourPi * (2.0 * r.surf_fac);
     int lsurf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? 1 : 0;
     if (mixed)

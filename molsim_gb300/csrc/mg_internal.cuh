@@ -84,6 +84,7 @@ struct mg_handle {
     double *d_part = nullptr;      // partial sums
     int part_pair = 0, part_rec = 0, part_bond = 0, part_surf = 0;   // offsets
     int nblk_pair = 0, nblk_rec = 0, nblk_bond = 0, nblk_surf = 0;
+    int part_red = 0;                   // energy reduction: its scratch rows in d_part
     double *d_uout = nullptr;      // [nptpt+1] u_twob, then u_tot,u_rec,u_bond,virial, then surf sums (3)
     int *d_err = nullptr;          // [4] code, info1, info2, info3
     double *h_pinned = nullptr;    // pinned staging for outputs
@@ -112,6 +113,7 @@ struct mg_handle {
     float *d_mf_f = nullptr, *d_ew_f = nullptr, *d_vw_f = nullptr;
     void *d_tw = nullptr;           // twiddles exp(-2 pi i m/n), m < n
     int fft_tx = 0, fft_tiles = 0;
+    int fft_plane = 0, fft_warps = 0;   // mixed form, 32 <= nmesh <= 128: three plane/slab passes
     int brick = 0, nbrick_edge = 0, nbricks = 0;
     size_t spread_smem = 0, gather_smem = 0;
     int fx_shift = 30, fx_shift64 = 48;

@@ -555,11 +555,13 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
 
 // gather: a group of G lanes per particle (G = 8 for orders up to 8, else
 // 16; particles in cell-sorted order for mesh locality).  Lane j < ORDER of a
-// group owns the stamp plane iz = j: for each row iy it sums dM*phi and M*phi
-// along x; the group then combines.  E = sum dM*M*M*phi
-// (energy.F90:1255-1285); force -= q*E*dkdr*EpsiFourPi.
+// group owns the stamp column ix = j, so that the group reads each mesh row
+// segment of its stamp as ORDER consecutive values: per plane iz it sums
+// M_y*phi and dM_y*phi over the rows, then weights them by M_z and dM_z; the
+// x weight of the lane's column and the group sum follow.  E = sum
+// dM*M*M*phi (energy.F90:1255-1285); force -= q*E*dkdr*EpsiFourPi.
 template <typename T, bool MIXED, int ORDER>
-__global__ void __launch_bounds__(256, 4) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
+__global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
                                                     const int *__restrict__ corner, const T *__restrict__ w,
                                                     const T *__restrict__ dw, const T *__restrict__ Q,
                                                     T kx, T ky, T kz, double *__restrict__ force,
@@ -573,34 +575,34 @@ __global__ void __launch_bounds__(256, 4) k_gather_grp(SplineArgs a, const int *
     int np = a.np, n = a.n, mn = n - 1;
     T e0 = 0, e1 = 0, e2 = 0;
     if (act) {
-        T vx[ORDER], dx[ORDER];
+        T vy[ORDER], dy[ORDER];
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            vx[i] = w[(size_t)i * np + p];
-            dx[i] = dw[(size_t)i * np + p];
+            vy[i] = w[(size_t)(ORDER + i) * np + p];
+            dy[i] = dw[(size_t)(ORDER + i) * np + p];
         }
-        T vz = w[(size_t)(2 * ORDER + j) * np + p], dz = dw[(size_t)(2 * ORDER + j) * np + p];
+        T vx = w[(size_t)j * np + p], dx = dw[(size_t)j * np + p];
         int c0 = corner[p], c1 = corner[np + p], c2 = corner[2 * np + p];
-        const T *plane = Q + ((size_t)((c2 - j) & mn) << (2 * a.n_log));
-        T a0 = 0, a1 = 0, a2 = 0;
+        const T *col = Q + ((c0 - j) & mn);
+        T A = 0, B = 0, C = 0;
 #pragma unroll
-        for (int iy = 0; iy < ORDER; ++iy) {
-            T vy = w[(size_t)(ORDER + iy) * np + p], dy = dw[(size_t)(ORDER + iy) * np + p];
-            const T *rw = plane + (size_t)((c1 - iy) & mn) * n;
-            T sx = 0, s0 = 0;
+        for (int iz = 0; iz < ORDER; ++iz) {
+            T vz = w[(size_t)(2 * ORDER + iz) * np + p], dz = dw[(size_t)(2 * ORDER + iz) * np + p];
+            const T *pl = col + ((size_t)((c2 - iz) & mn) << (2 * a.n_log));
+            T r0 = 0, r1 = 0;
 #pragma unroll
-            for (int ix = 0; ix < ORDER; ++ix) {
-                T q = rw[(c0 - ix) & mn];
-                sx += dx[ix] * q;
-                s0 += vx[ix] * q;
+            for (int iy = 0; iy < ORDER; ++iy) {
+                T q = pl[(size_t)((c1 - iy) & mn) * n];
+                r0 += vy[iy] * q;
+                r1 += dy[iy] * q;
             }
-            a0 += vy * sx;
-            a1 += dy * s0;
-            a2 += vy * s0;
+            A += vz * r0;
+            B += vz * r1;
+            C += dz * r0;
         }
-        e0 = vz * a0;
-        e1 = vz * a1;
-        e2 = dz * a2;
+        e0 = dx * A;
+        e1 = vx * B;
+        e2 = vx * C;
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
@@ -701,8 +703,395 @@ int ilog2(int n) {
     return l;
 }
 
+// ---- plane passes (mixed form, n = 32 P for P = 1, 2, 4) --------------------
+// Three kernels replace the five line passes when a whole mesh plane fits in
+// shared memory: one CTA per z plane does the x r2c and the forward y FFT
+// (and clears the fixed-point mesh it read); one CTA per ky slab does the
+// forward z FFT, the influence function and the inverse z FFT; one CTA per
+// z plane does the inverse y FFT and the x c2r.  Each line is transformed
+// by one warp in registers:
+//   lane l holds elements x[l + 32 j], j < P.  Forward: a P-point DFT in the
+//   lane's registers, the twiddle w_n^(l k1), then a 32-point transform
+//   across the lanes by decimation in frequency (shuffles), after which lane
+//   l holds X[k1 + P bitrev5(l)].  The backward transform starts from that
+//   layout (decimation in time across the lanes, conjugate twiddle, P-point
+//   DFT) and ends with x[l + 32 j], unnormalised.
+// Twiddles come from the table w_n^m = exp(-2 pi i m / n) in shared memory.
+
+template <typename T> __device__ __forceinline__ V2<T> shfl_xor_c(V2<T> v, int m) {
+    v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+    v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+    return v;
+}
+
+template <typename T> __device__ __forceinline__ V2<T> conj_c(V2<T> t) {
+    t.y = -t.y;
+    return t;
+}
+
+__device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
+
+// in-place P-point DFT in registers (natural order in and out): iterative
+// radix-2 with the bit reversal as compile-time register renaming
+template <typename T, int P, bool INV>
+__device__ __forceinline__ void reg_dft(V2<T> *v, const V2<T> *tw, int n) {
+    typedef V2<T> V;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+        int r = 0;
+#pragma unroll
+        for (int b = 1, x = i; b < P; b <<= 1, x >>= 1) r = (r << 1) | (x & 1);
+        if (r > i) { V t = v[i]; v[i] = v[r]; v[r] = t; }
+    }
+#pragma unroll
+    for (int len = 2; len <= P; len <<= 1) {
+        const int half = len >> 1;
+#pragma unroll
+        for (int i = 0; i < P; i += len) {
+#pragma unroll
+            for (int e = 0; e < half; ++e) {
+                V u = v[i + e], t = v[i + e + half];
+                if (e) {
+                    V w = tw[e * (n / len)];
+                    t = cmul(t, INV ? conj_c<T>(w) : w);
+                }
+                v[i + e] = cadd(u, t);
+                v[i + e + half] = csub(u, t);
+            }
+        }
+    }
+}
+
+// Per-lane twiddle tables (bank-conflict free): tl[h - 1 + e] = w_2h^e for the
+// cross-lane stage h (e < h), tk[32 (k1 - 1) + l] = w_n^(l k1).
+template <typename T, int P>
+__device__ __forceinline__ void load_lane_tw(V2<T> *tl, V2<T> *tk, const V2<T> *__restrict__ tw) {
+    constexpr int n = 32 * P;
+    for (int m = threadIdx.x; m < 32 + 32 * (P - 1); m += blockDim.x) {
+        if (m < 31) {
+            int h = 1;
+            while (2 * h - 1 <= m) h <<= 1;
+            tl[m] = tw[(m - (h - 1)) * (n / (2 * h))];
+        } else if (m >= 32) {
+            int mm = m - 32, k1 = mm / 32 + 1, l = mm & 31;
+            tk[mm] = tw[(l * k1) & (n - 1)];
+        }
+    }
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void warp_fft_fwd(V2<T> *v, const V2<T> *tw, const V2<T> *tl, const V2<T> *tk,
+                                             int lane) {
+    constexpr int n = 32 * P;
+    reg_dft<T, P, false>(v, tw, n);
+#pragma unroll
+    for (int k1 = 1; k1 < P; ++k1) v[k1] = cmul(v[k1], tk[32 * (k1 - 1) + lane]);
+#pragma unroll
+    for (int h = 16; h > 0; h >>= 1) {
+        V2<T> w = tl[h - 1 + (lane & (h - 1))];
+        const T s = (lane & h) ? (T)-1 : (T)1;   // lower lane: a + b, upper lane: (a - b) w
+        if (!(lane & h)) { w.x = (T)1; w.y = (T)0; }
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+            V2<T> p = shfl_xor_c<T>(v[k1], h), t;
+            t.x = p.x + s * v[k1].x;
+            t.y = p.y + s * v[k1].y;
+            v[k1] = cmul(t, w);
+        }
+    }
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void warp_fft_inv(V2<T> *v, const V2<T> *tw, const V2<T> *tl, const V2<T> *tk,
+                                             int lane) {
+    constexpr int n = 32 * P;
+#pragma unroll
+    for (int h = 1; h <= 16; h <<= 1) {
+        const V2<T> w = conj_c<T>(tl[h - 1 + (lane & (h - 1))]);
+        const bool up = lane & h;   // lower lane: a + w b, upper lane: a - w b
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+            V2<T> p = shfl_xor_c<T>(v[k1], h);
+            V2<T> b = cmul(up ? v[k1] : p, w), a = up ? p : v[k1];
+            v[k1] = up ? csub(a, b) : cadd(a, b);
+        }
+    }
+#pragma unroll
+    for (int k1 = 1; k1 < P; ++k1) v[k1] = cmul(v[k1], conj_c<T>(tk[32 * (k1 - 1) + lane]));
+    reg_dft<T, P, true>(v, tw, n);
+}
+
+// shared-memory row of wave number ky after the forward y pass: lane l's
+// register k1 holds ky = k1 + P bitrev5(l) and is kept in row 32 k1 + l
+template <int P> __device__ __forceinline__ int perm_row(int ky) { return (ky % P) * 32 + brev5(ky / P); }
+
+// skewed index into a warp's line buffer: one pad entry per 16, so that the
+// strided writes k1 + P bitrev5(l) and the natural reads are conflict free
+__device__ __forceinline__ int zsk(int i) { return i + (i >> 4); }
+
+// twiddle part of the plane kernels' shared memory: tw[n] | tl[32] | tk[32 (P - 1)]
+template <int P> __host__ __device__ constexpr int plane_tw_entries() { return 32 * P + 32 + 32 * (P - 1); }
+
+// x r2c + forward y FFT of plane z; clears the fixed-point plane it reads.
+// Shared memory: twiddles | S[n][nh] (plane, row = y) | Zs[warps][n + n/16]
+template <typename T, int P>
+__global__ void __launch_bounds__(1024) k_plane_fwd(unsigned long long *__restrict__ Qfx, T fx_inv,
+                                                    V2<T> *__restrict__ F, const V2<T> *__restrict__ tw,
+                                                    FastDiv fnh) {
+    typedef V2<T> V;
+    constexpr int n = 32 * P, nh = n / 2 + 1;
+    extern __shared__ unsigned char smem_raw[];
+    V *s_tw = reinterpret_cast<V *>(smem_raw), *s_tl = s_tw + n, *s_tk = s_tl + 32;
+    V *S = s_tw + plane_tw_entries<P>();
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    V *Zs = S + n * nh + w * (n + n / 16);
+    load_tw<T>(s_tw, tw, n);
+    load_lane_tw<T, P>(s_tl, s_tk, tw);
+    __syncthreads();
+    const size_t z = blockIdx.x;
+    const int bl = brev5(lane);
+    long long *Qp = reinterpret_cast<long long *>(Qfx) + z * n * n;
+    // every line pair of this warp is loaded before the first transform
+    constexpr int MP = (P + 1) / 2;   // pairs per warp at 32 warps
+    long long raw[MP][2 * P];
+#pragma unroll
+    for (int r = 0; r < MP; ++r) {
+        int pr = w + 32 * r;
+        if (pr < n / 2) {
+            long long *qa = Qp + (size_t)(2 * pr) * n, *qb = qa + n;
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                raw[r][2 * j] = qa[lane + 32 * j];
+                raw[r][2 * j + 1] = qb[lane + 32 * j];
+            }
+#pragma unroll
+            for (int j = 0; j < P; ++j) {   // the next spread accumulates into a cleared mesh
+                qa[lane + 32 * j] = 0;
+                qb[lane + 32 * j] = 0;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < MP; ++r) {
+        int pr = w + 32 * r;
+        if (pr >= n / 2) break;
+        V v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            v[j].x = fx_to_real<T>(raw[r][2 * j]) * fx_inv;
+            v[j].y = fx_to_real<T>(raw[r][2 * j + 1]) * fx_inv;
+        }
+        warp_fft_fwd<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) Zs[zsk(k1 + P * bl)] = v[k1];
+        __syncwarp();
+        V *Sa = S + (2 * pr) * nh, *Sb = Sa + nh;
+        for (int k = lane; k < nh; k += 32) {
+            V zk = Zs[zsk(k)], zc = Zs[zsk((n - k) & (n - 1))];
+            V a, b;
+            // X_A = (Z_k + conj Z_{n-k})/2,  X_B = (Z_k - conj Z_{n-k})/(2i)
+            a.x = (T)0.5 * (zk.x + zc.x);
+            a.y = (T)0.5 * (zk.y - zc.y);
+            b.x = (T)0.5 * (zk.y + zc.y);
+            b.y = (T)-0.5 * (zk.x - zc.x);
+            Sa[k] = a;
+            Sb[k] = b;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int c = w; c < nh; c += nw) {   // forward y FFT of column kx = c
+        V v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) v[j] = S[(lane + 32 * j) * nh + c];
+        warp_fft_fwd<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) S[(32 * k1 + lane) * nh + c] = v[k1];
+    }
+    __syncthreads();
+    V *Fp = F + z * n * nh;
+    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
+        int ky = (int)fdiv((unsigned)e, fnh), kx = e - ky * nh;
+        Fp[e] = S[perm_row<P>(ky) * nh + kx];
+    }
+}
+
+// forward z FFT, influence function (energy and virial partial sums, times
+// meshfac) and inverse z FFT of the slab ky.  Shared memory: twiddles |
+// S[n][nh] (row = z) | mf, ew, vw of the octant row fy, [nh][nh] each
+template <typename T, int P>
+__global__ void __launch_bounds__(1024) k_slab_conv(V2<T> *__restrict__ F, const V2<T> *__restrict__ tw,
+                                                    ConvArgs cv, FastDiv fnh) {
+    typedef V2<T> V;
+    constexpr int n = 32 * P, nh = n / 2 + 1;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ double red[2 * 32];
+    V *s_tw = reinterpret_cast<V *>(smem_raw), *s_tl = s_tw + n, *s_tk = s_tl + 32;
+    V *S = s_tw + plane_tw_entries<P>();
+    T *s_mf = reinterpret_cast<T *>(S + n * nh), *s_ew = s_mf + nh * nh, *s_vw = s_ew + nh * nh;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    load_tw<T>(s_tw, tw, n);
+    load_lane_tw<T, P>(s_tl, s_tk, tw);
+    const int ky = blockIdx.x, fy = min(ky, n - ky);
+    const T *mf = (const T *)cv.mf, *ew = (const T *)cv.ew, *vw = (const T *)cv.vw;
+    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
+        int zz = (int)fdiv((unsigned)e, fnh), kx = e - zz * nh;
+        S[e] = F[((size_t)zz * n + ky) * nh + kx];
+    }
+    for (int e = threadIdx.x; e < nh * nh; e += blockDim.x) {
+        int fz = (int)fdiv((unsigned)e, fnh), kx = e - fz * nh;
+        size_t id = ((size_t)fz * nh + fy) * nh + kx;
+        s_mf[e] = mf[id];
+        s_ew[e] = ew[id];
+        s_vw[e] = vw[id];
+    }
+    __syncthreads();
+    const int bl = brev5(lane);
+    T e_t = 0, v_t = 0;
+    for (int c = w; c < nh; c += nw) {
+        V v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) v[j] = S[(lane + 32 * j) * nh + c];
+        warp_fft_fwd<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+            int kz = k1 + P * bl;
+            int id = min(kz, n - kz) * nh + c;
+            T p2 = v[k1].x * v[k1].x + v[k1].y * v[k1].y;
+            e_t += p2 * s_ew[id];
+            v_t -= p2 * s_vw[id];
+            T m = s_mf[id];
+            v[k1].x *= m;
+            v[k1].y *= m;
+        }
+        warp_fft_inv<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int j = 0; j < P; ++j) S[(lane + 32 * j) * nh + c] = v[j];
+    }
+    for (int o = 16; o > 0; o >>= 1) {   // warp sums in the mesh type, FP64 across warps
+        e_t += __shfl_down_sync(0xffffffffu, e_t, o);
+        v_t += __shfl_down_sync(0xffffffffu, v_t, o);
+    }
+    if (lane == 0) { red[w] = (double)e_t; red[32 + w] = (double)v_t; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double se = 0.0, sv = 0.0;
+        for (int k = 0; k < nw; ++k) { se += red[k]; sv += red[32 + k]; }
+        cv.part[2 * blockIdx.x] = se;
+        cv.part[2 * blockIdx.x + 1] = sv;
+    }
+    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
+        int zz = (int)fdiv((unsigned)e, fnh), kx = e - zz * nh;
+        F[((size_t)zz * n + ky) * nh + kx] = S[e];
+    }
+}
+
+// inverse y FFT + x c2r of plane z (Hermitian input: imaginary parts of
+// kx = 0 and n/2 dropped).  Shared memory as k_plane_fwd.
+template <typename T, int P>
+__global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F, T *__restrict__ Q,
+                                                    const V2<T> *__restrict__ tw, FastDiv fnh) {
+    typedef V2<T> V;
+    constexpr int n = 32 * P, nh = n / 2 + 1;
+    extern __shared__ unsigned char smem_raw[];
+    V *s_tw = reinterpret_cast<V *>(smem_raw), *s_tl = s_tw + n, *s_tk = s_tl + 32;
+    V *S = s_tw + plane_tw_entries<P>();
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    V *Zs = S + n * nh + w * (n + n / 16);
+    load_tw<T>(s_tw, tw, n);
+    load_lane_tw<T, P>(s_tl, s_tk, tw);
+    const size_t z = blockIdx.x;
+    const V *Fp = F + z * n * nh;
+    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
+        int ky = (int)fdiv((unsigned)e, fnh), kx = e - ky * nh;
+        S[perm_row<P>(ky) * nh + kx] = Fp[e];
+    }
+    __syncthreads();
+    for (int c = w; c < nh; c += nw) {   // inverse y FFT of column kx = c
+        V v[P];
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) v[k1] = S[(32 * k1 + lane) * nh + c];
+        warp_fft_inv<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int j = 0; j < P; ++j) S[(lane + 32 * j) * nh + c] = v[j];
+    }
+    __syncthreads();
+    const int bl = brev5(lane);
+    T *Qp = Q + z * n * n;
+    for (int pr = w; pr < n / 2; pr += nw) {
+        const V *Sa = S + (2 * pr) * nh, *Sb = Sa + nh;
+        for (int k = lane; k < n; k += 32) {
+            int kk = (k < nh) ? k : n - k;
+            V a = Sa[kk], b = Sb[kk];
+            if (kk == 0 || 2 * kk == n) { a.y = (T)0; b.y = (T)0; }
+            if (k >= nh) { a.y = -a.y; b.y = -b.y; }
+            V zz;
+            zz.x = a.x - b.y;
+            zz.y = a.y + b.x;
+            Zs[zsk(k)] = zz;
+        }
+        __syncwarp();
+        V v[P];
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) v[k1] = Zs[zsk(k1 + P * bl)];
+        __syncwarp();
+        warp_fft_inv<T, P>(v, s_tw, s_tl, s_tk, lane);
+        T *qa = Qp + (size_t)(2 * pr) * n, *qb = qa + n;
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            qa[lane + 32 * j] = v[j].x;
+            qb[lane + 32 * j] = v[j].y;
+        }
+    }
+}
+
+template <int P> static size_t plane_smem(int warps) {
+    const int n = 32 * P, nh = n / 2 + 1;
+    return sizeof(float2) * ((size_t)plane_tw_entries<P>() + (size_t)n * nh + (size_t)warps * (n + n / 16));
+}
+template <int P> static size_t slab_smem() {
+    const int n = 32 * P, nh = n / 2 + 1;
+    return sizeof(float2) * ((size_t)plane_tw_entries<P>() + (size_t)n * nh) + 3 * sizeof(float) * (size_t)nh * nh;
+}
+
+template <int P>
+static int plane_passes(mg_handle *h, float *Q, float2 *F, const float2 *tw, ConvArgs cv, float fx_inv) {
+    const int n = 32 * P, thr = 32 * h->fft_warps;
+    FastDiv fnh = make_fastdiv((unsigned)h->nh);
+    MG_TRY(mg_phase_begin(h, "fft_xy_fwd"));
+    k_plane_fwd<float, P><<<n, thr, plane_smem<P>(h->fft_warps), h->st>>>(h->d_Qfx, fx_inv, F, tw, fnh);
+    MG_TRY(mg_phase_end(h, "fft_xy_fwd"));
+    MG_TRY(mg_phase_begin(h, "fft_z_conv"));
+    k_slab_conv<float, P><<<n, thr, slab_smem<P>(), h->st>>>(F, tw, cv, fnh);
+    MG_TRY(mg_phase_end(h, "fft_z_conv"));
+    MG_TRY(mg_phase_begin(h, "fft_yx_inv"));
+    k_plane_inv<float, P><<<n, thr, plane_smem<P>(h->fft_warps), h->st>>>(F, Q, tw, fnh);
+    MG_TRY(mg_phase_end(h, "fft_yx_inv"));
+    h->launches += 3;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+static int plane_dispatch(mg_handle *h, float *Q, float2 *F, const float2 *tw, ConvArgs cv, float fx_inv) {
+    switch (h->nmesh) {
+    case 32: return plane_passes<1>(h, Q, F, tw, cv, fx_inv);
+    case 64: return plane_passes<2>(h, Q, F, tw, cv, fx_inv);
+    case 128: return plane_passes<4>(h, Q, F, tw, cv, fx_inv);
+    default: return mg_fail(h, MG_ERR_UNSUPPORTED, "plane FFT for nmesh = %d", h->nmesh);
+    }
+}
+
+template <int P> static void set_plane_limits() {
+    cudaFuncSetAttribute(k_plane_fwd<float, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_slab_conv<float, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_plane_inv<float, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
 template <typename T>
 int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_inv) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (h->fft_plane) return plane_dispatch(h, Q, F, tw, cv, fx_inv);
+    }
     int n = h->nmesh, logn = ilog2(n), nh = h->nh;
     int lp = 4;                                  // line pairs per CTA in the x passes
     size_t vsz = sizeof(V2<T>);
@@ -741,6 +1130,11 @@ template <typename T> void set_smem_limits() {
     cudaFuncSetAttribute(k_fft_x_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_fft_col<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_fft_col<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if constexpr (std::is_same<T, float>::value) {
+        set_plane_limits<1>();
+        set_plane_limits<2>();
+        set_plane_limits<4>();
+    }
 }
 
 }  // namespace
@@ -760,6 +1154,13 @@ int mg_spme_init(mg_handle *h) {
     h->fft_tiles = tiles;
     h->fft_tx = (h->nh + tiles - 1) / tiles;
     h->nblk_rec = tiles * n;
+    // mixed form, 32 <= n <= 128: plane passes, 32 warps per plane, one
+    // partial sum per ky slab
+    h->fft_plane = (h->form == MG_MIXED && n >= 32 && n <= 128) ? 1 : 0;
+    if (h->fft_plane) {
+        h->fft_warps = 32;
+        h->nblk_rec = n;
+    }
     // bricks of 8^3 points (16^3 for orders above 9, whose halo would
     // otherwise reach beyond the next brick)
     if (h->order < 4) return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d (supported: 4..12)", h->order);
