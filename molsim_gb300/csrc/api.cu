@@ -113,7 +113,7 @@ static void free_all(mg_handle *h) {
                     h->d_scan_tmp, h->d_zlow, h->d_coef, h->d_coef_f, h->d_bin_z0, h->d_bin_inv,
                     h->d_bin_kstart, h->d_brick_count, h->d_brick_perm, h->d_brick_rank,
                     h->d_brick_of, h->d_brick_start, h->d_brick_istart, h->d_item_brick, h->d_tiles, h->d_grad, h->d_f32_tabs, h->d_pos_f,
-                    h->d_cell_s, h->d_corner, h->d_spl_w, h->d_spl_dw};
+                    h->d_cell_s, h->d_corner, h->d_spl_w, h->d_spl_dw, h->d_ffx2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -123,6 +123,9 @@ static void free_all(mg_handle *h) {
         cudaEventDestroy(p.e0);
         cudaEventDestroy(p.e1);
     }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->st2) cudaStreamDestroy(h->st2);
     if (h->st) cudaStreamDestroy(h->st);
 }
 
@@ -208,6 +211,9 @@ static int create_impl(const mg_params *p, mg_handle *h) {
     for (int i = 0; i < p->nbuf; ++i) ubf[i] = (float)p->ubuf[i];
 
     MG_CUDA(h, cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    MG_CUDA(h, cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
+    MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     MG_CUDA(h, cudaMalloc(&h->d_ro, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMemset(h->d_ro, 0, sizeof(double) * 3 * np));
     MG_TRY(upload(h, &h->d_az, p->az, np));

@@ -628,13 +628,15 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
 // force -> forceo with the surface force and the unit factor (energy.F90:405-424)
 template <bool MIXED>
 __global__ void k_epilogue(const double *__restrict__ force, const long long *__restrict__ ffx,
-                           const double *__restrict__ az, const double *__restrict__ uout, int o,
+                           const long long *__restrict__ ffx2, const double *__restrict__ az,
+                           const double *__restrict__ uout, int o,
                            int np, int lsurf, double surf_k, double fac,
                            double *__restrict__ forceo) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     for (int m = 0; m < 3; ++m) {
-        double f = MIXED ? (double)ffx[3 * p + m] * MG_FX_INV : force[3 * p + m];
+        double f = MIXED ? (double)(ffx[3 * p + m] + (ffx2 ? ffx2[3 * p + m] : 0ll)) * MG_FX_INV
+                         : force[3 * p + m];
         if (lsurf) f = f - surf_k * az[p] * uout[o + 4 + m];
         forceo[3 * p + m] = f * fac;
     }
@@ -785,6 +787,7 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
         MG_CUDA(h, cudaMalloc(&h->d_pos_f, sizeof(float4) * np));
         MG_CUDA(h, cudaMalloc(&h->d_cell_s, sizeof(int) * np));
         MG_CUDA(h, cudaMalloc(&h->d_ffx, sizeof(long long) * 3 * np));
+        if (h->ewald == MG_EWALD_SPM) MG_CUDA(h, cudaMalloc(&h->d_ffx2, sizeof(long long) * 3 * np));
     } else {
         MG_CUDA(h, cudaMalloc(&h->d_force, sizeof(double) * 3 * np));
     }
@@ -804,9 +807,20 @@ int mg_utotal_launch(mg_handle *h) {
         cg.lenf[m] = (float)h->boxlen[m];
         cg.halff[m] = (float)h->boxlen2[m];
     }
+    // mixed form with SPME (uncaptured phase timing aside): the short-range
+    // forces run on the second stream into d_ffx2 while the mesh path runs here
+    bool par = mixed && h->ewald == MG_EWALD_SPM && h->d_ffx2 && !h->timing;
+    cudaStream_t ss = h->st;
+    long long *ffx_sr = h->d_ffx;
+    if (par) {
+        MG_CUDA(h, cudaEventRecord(h->ev_fork, h->st));
+        MG_CUDA(h, cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+        ss = h->st2;
+        ffx_sr = h->d_ffx2;
+    }
     MG_TRY(mg_phase_begin(h, "prepare"));
     if (mixed)
-        k_prepare_f32<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
+        k_prepare_f32<<<(np + kThreads - 1) / kThreads, kThreads, 0, ss>>>(
             h->d_ro, h->d_perm, h->d_type, h->d_cellof, np, cg, h->d_pos_f, h->d_cell_s);
     else
         k_prepare<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(h->d_ro, h->d_perm, h->d_type,
@@ -874,18 +888,26 @@ int mg_utotal_launch(mg_handle *h) {
         f.g = cg;
         f.rcut2 = (float)h->rcut2;
         f.cellcut = a.cellcut;
-        f.ffx = h->d_ffx;
+        f.ffx = ffx_sr;
         f.part = h->d_part + h->part_pair;
         f.err = h->d_err;
         int team = h->pair_team, nbt = (int)(((long)np * team + kPairThreads - 1) / kPairThreads);
         switch (team) {
-        case 1: k_pair_f32<1><<<nbt, kPairThreads, 0, h->st>>>(f); break;
-        case 2: k_pair_f32<2><<<nbt, kPairThreads, 0, h->st>>>(f); break;
-        case 4: k_pair_f32<4><<<nbt, kPairThreads, 0, h->st>>>(f); break;
-        case 8: k_pair_f32<8><<<nbt, kPairThreads, 0, h->st>>>(f); break;
-        case 16: k_pair_f32<16><<<nbt, kPairThreads, 0, h->st>>>(f); break;
-        default: k_pair_f32<32><<<nbt, kPairThreads, 0, h->st>>>(f); break;
+        case 1: k_pair_f32<1><<<nbt, kPairThreads, 0, ss>>>(f); break;
+        case 2: k_pair_f32<2><<<nbt, kPairThreads, 0, ss>>>(f); break;
+        case 4: k_pair_f32<4><<<nbt, kPairThreads, 0, ss>>>(f); break;
+        case 8: k_pair_f32<8><<<nbt, kPairThreads, 0, ss>>>(f); break;
+        case 16: k_pair_f32<16><<<nbt, kPairThreads, 0, ss>>>(f); break;
+        default: k_pair_f32<32><<<nbt, kPairThreads, 0, ss>>>(f); break;
         }
+        if (par && h->nbond > 0) {   // bonds follow the pairs on the second stream
+            k_bond<true><<<h->nblk_bond, kBondThreads, 0, ss>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
+                                                            h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
+                                                            h->d_bond_p, a.box, h->d_force, ffx_sr,
+                                                            h->d_part + h->part_bond);
+            h->launches++;
+        }
+        if (par) MG_CUDA(h, cudaEventRecord(h->ev_join, ss));
     } else {
         if (h->pair_warp) k_pair<false, true><<<nb, kPairThreads, sm, h->st>>>(a);
         else k_pair<false, false><<<nb, kPairThreads, sm, h->st>>>(a);
@@ -893,11 +915,16 @@ int mg_utotal_launch(mg_handle *h) {
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "pair"));
 
-    if (h->ewald == MG_EWALD_SPM) MG_TRY(mg_spme_launch(h));
-    else if (h->ewald == MG_EWALD_STD) MG_TRY(mg_ewald_std_launch(h));
+    h->par_forces = par;
+    int spst = MG_OK;
+    if (h->ewald == MG_EWALD_SPM) spst = mg_spme_launch(h);
+    else if (h->ewald == MG_EWALD_STD) spst = mg_ewald_std_launch(h);
+    h->par_forces = false;
+    if (par) MG_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_join, 0));   // join before any return
+    MG_TRY(spst);
 
     MG_TRY(mg_phase_begin(h, "bond+reduce"));
-    if (h->nbond > 0) {
+    if (h->nbond > 0 && !par) {
         if (mixed)
             k_bond<true><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
                                                                h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
@@ -947,12 +974,12 @@ int mg_utotal_launch(mg_handle *h) {
     int lsurf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? 1 : 0;
     if (mixed)
         k_epilogue<true><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
-            h->d_force, h->d_ffx, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf, surf_k, h->force_fac,
-            h->d_forceo);
+            h->d_force, h->d_ffx, par ? h->d_ffx2 : nullptr, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf,
+            surf_k, h->force_fac, h->d_forceo);
     else
         k_epilogue<false><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
-            h->d_force, h->d_ffx, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf, surf_k, h->force_fac,
-            h->d_forceo);
+            h->d_force, h->d_ffx, nullptr, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf, surf_k,
+            h->force_fac, h->d_forceo);
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "bond+reduce"));
     MG_CUDA(h, cudaGetLastError());

@@ -105,6 +105,7 @@ struct BdArgs {
     int nblk;
     mg_box box;
     int *err;
+    mg_chk_args chk;        // the list check's first pass runs here
 };
 
 // prefix of the per-block accepted counts in shared memory (inclusive): all
@@ -155,15 +156,18 @@ __device__ __forceinline__ long pair_slot(const int *sp, int nblk, int j) {
     return (long)lo * kCandBlock + (j - before);
 }
 
-// BDStep: drostep = fac1*forceo + fac2*GauRandom; ro += drostep; PBC.  The
-// last block to finish also advances the GauRandom state past this step's
-// deviates (every block has read the old state by then).
-__global__ void k_bd_move(BdArgs a) {
+// BDStep: drostep = fac1*forceo + fac2*GauRandom; ro += drostep; PBC; then
+// the first pass of the list check on drostep.  The last block to finish
+// also advances the GauRandom state past this step's deviates (every block
+// has read the old state by then).
+__global__ void __launch_bounds__(kChkThreads) k_bd_move(BdArgs a) {
     extern __shared__ int sp[];
     __shared__ bool last;
     load_block_prefix(a.blkcnt, a.nblk, sp);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int off = (a.rng[1] == 0) ? 1 : 0;   // a saved deviate is pending
+    bool reset = (*a.chk.flag != 0);
+    double dd[3] = {0.0, 0.0, 0.0};
     if (p < a.np) {
         int t = a.type[p];
         double f1 = a.fac1[t], f2 = a.fac2[t];
@@ -185,10 +189,12 @@ __global__ void k_bd_move(BdArgs a) {
             }
             double d = __dadd_rn(__dmul_rn(f1, a.forceo[3 * p + m]), __dmul_rn(f2, dev));
             a.drostep[3 * p + m] = d;
+            dd[m] = d;
             double r = __dadd_rn(a.ro[3 * p + m], d);
             a.ro[3 * p + m] = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
         }
     }
+    mg_chk_accum(p, a.np, dd[0], dd[1], dd[2], reset, a.chk.drosum, a.chk.r2out, a.chk.blkmax);
     __syncthreads();   // this block has read the state (rng, save)
     if (threadIdx.x == 0) {
         __threadfence();
@@ -219,19 +225,26 @@ struct MdArgs {
     int np;
     double tstep, fac;
     mg_box box;
+    mg_chk_args chk;        // the list check's first pass runs in k_md_pos
 };
 
-// VelVer positions: drostep = tstep*rod + fac*rodd; ro += drostep; PBC
-__global__ void k_md_pos(MdArgs a) {
+// VelVer positions: drostep = tstep*rod + fac*rodd; ro += drostep; PBC; then
+// the first pass of the list check on drostep
+__global__ void __launch_bounds__(kChkThreads) k_md_pos(MdArgs a) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.np) return;
-    for (int m = 0; m < 3; ++m) {
-        int i = 3 * p + m;
-        double d = __dadd_rn(__dmul_rn(a.tstep, a.rod[i]), __dmul_rn(a.fac, a.rodd[i]));
-        a.drostep[i] = d;
-        double r = __dadd_rn(a.ro[i], d);
-        a.ro[i] = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
+    bool reset = (*a.chk.flag != 0);
+    double dd[3] = {0.0, 0.0, 0.0};
+    if (p < a.np) {
+        for (int m = 0; m < 3; ++m) {
+            int i = 3 * p + m;
+            double d = __dadd_rn(__dmul_rn(a.tstep, a.rod[i]), __dmul_rn(a.fac, a.rodd[i]));
+            a.drostep[i] = d;
+            dd[m] = d;
+            double r = __dadd_rn(a.ro[i], d);
+            a.ro[i] = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
+        }
     }
+    mg_chk_accum(p, a.np, dd[0], dd[1], dd[2], reset, a.chk.drosum, a.chk.r2out, a.chk.blkmax);
 }
 
 // GetLinAcc and the velocity half-kick: rodd = massip*forceo;
@@ -304,7 +317,7 @@ int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, cons
     return MG_OK;
 }
 
-static int list_step(mg_handle *h);
+static int list_step(mg_handle *h, bool accum_done);
 
 // one BD step (BDStep, UTotal, list check) queued on the stream
 int mg_integrate_bd_step_launch(mg_handle *h) {
@@ -325,6 +338,7 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     a.nblk = nblk;
     a.box = box_of(h);
     a.err = h->d_err;
+    a.chk = mg_lists_chk_args(h);
     size_t sm = sizeof(int) * nblk;
     MG_TRY(mg_phase_begin(h, "bd_rng"));
     if (h->form == MG_MIXED)
@@ -333,11 +347,11 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
         k_bd_cand<false><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
     MG_TRY(mg_phase_end(h, "bd_rng"));
     MG_TRY(mg_phase_begin(h, "bd_move"));
-    k_bd_move<<<(np + 255) / 256, 256, sm, h->st>>>(a);   // advances the GauRandom state too
+    k_bd_move<<<(np + kChkThreads - 1) / kChkThreads, kChkThreads, sm, h->st>>>(a);   // advances the GauRandom state too
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "bd_move"));
     MG_TRY(mg_utotal_launch(h));
-    MG_TRY(list_step(h));
+    MG_TRY(list_step(h, true));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }
@@ -347,9 +361,9 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
 // profiling) the host reads the rebuild flag after the check and launches the
 // build only when it is due, so that uncaptured steps run the same kernels as
 // the graph does.
-static int list_step(mg_handle *h) {
+static int list_step(mg_handle *h, bool accum_done) {
     MG_TRY(mg_phase_begin(h, "list"));
-    MG_TRY(mg_lists_check(h));
+    MG_TRY(mg_lists_check(h, accum_done));
     MG_TRY(mg_phase_end(h, "list"));
     if (h->use_cond) return MG_OK;
     int flag = 0;
@@ -376,15 +390,16 @@ int mg_integrate_md_step_launch(mg_handle *h) {
     a.tstep = h->tstep;
     a.fac = 0.5 * (h->tstep * h->tstep);
     a.box = box_of(h);
-    int gb = (h->np + 255) / 256;
+    a.chk = mg_lists_chk_args(h);
+    int gb = (h->np + kChkThreads - 1) / kChkThreads;
     MG_TRY(mg_phase_begin(h, "md_pos"));
-    k_md_pos<<<gb, 256, 0, h->st>>>(a);
+    k_md_pos<<<gb, kChkThreads, 0, h->st>>>(a);
     h->launches++;
     MG_TRY(mg_phase_end(h, "md_pos"));
     MG_TRY(mg_utotal_launch(h));
-    k_md_vel<<<gb, 256, 0, h->st>>>(a);
+    k_md_vel<<<gb, kChkThreads, 0, h->st>>>(a);
     h->launches++;
-    MG_TRY(list_step(h));
+    MG_TRY(list_step(h, true));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }

@@ -18,7 +18,6 @@
 
 namespace {
 
-constexpr int kChkThreads = 256;   // list check: threads per block
 
 
 __global__ void k_cell_assign(const double *__restrict__ ro, int np, double3 half, double3 csi,
@@ -187,37 +186,15 @@ __global__ void __launch_bounds__(kChkThreads) k_chk_accum(const double *__restr
                                                            double *__restrict__ drosum, double *__restrict__ r2out,
                                                            double *__restrict__ blkmax, int np,
                                                            const int *__restrict__ flag) {
-    __shared__ long long red[kChkThreads / 32];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool reset = (*flag != 0);   // a rebuild happened at the previous check
-    double r2 = 0.0;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
     if (p < np) {
-        double s0, s1, s2;
-        if (reset) {
-            s0 = 0.0 + drostep[3 * p];
-            s1 = 0.0 + drostep[3 * p + 1];
-            s2 = 0.0 + drostep[3 * p + 2];
-        } else {
-            s0 = __dadd_rn(drosum[3 * p], drostep[3 * p]);
-            s1 = __dadd_rn(drosum[3 * p + 1], drostep[3 * p + 1]);
-            s2 = __dadd_rn(drosum[3 * p + 2], drostep[3 * p + 2]);
-        }
-        drosum[3 * p] = s0;
-        drosum[3 * p + 1] = s1;
-        drosum[3 * p + 2] = s2;
-        r2 = mg_r2_exact(s0, s1, s2);
-        r2out[p] = r2;
+        d0 = drostep[3 * p];
+        d1 = drostep[3 * p + 1];
+        d2 = drostep[3 * p + 2];
     }
-    long long m = __double_as_longlong(r2);
-    for (int o = 16; o > 0; o >>= 1) m = chk_max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        int nw = blockDim.x >> 5;
-        long long x = (threadIdx.x < nw) ? red[threadIdx.x] : 0;
-        for (int o = 16; o > 0; o >>= 1) x = chk_max(x, __shfl_xor_sync(0xffffffffu, x, o));
-        if (threadIdx.x == 0) blkmax[blockIdx.x] = __longlong_as_double(x);
-    }
+    mg_chk_accum(p, np, d0, d1, d2, reset, drosum, r2out, blkmax);
 }
 
 // Pass 2 per block: the largest value that was not a new running maximum,
@@ -495,15 +472,29 @@ int mg_lists_build(mg_handle *h, bool conditional) {
 
 // NList(iSimulationStep): accumulate drostep (already on the device in
 // d_drostep) and set the rebuild flag; the caller then runs a conditional build.
-int mg_lists_check(mg_handle *h) {
+mg_chk_args mg_lists_chk_args(mg_handle *h) {
+    mg_chk_args c;
+    c.drosum = h->d_drosum;
+    c.r2out = h->d_blkmax + 2 * h->nblk_chk;
+    c.blkmax = h->d_blkmax;
+    c.flag = h->d_rebuild;
+    return c;
+}
+
+// accum_done: the move kernel of this step ran the first pass (blocks of
+// kChkThreads particles)
+int mg_lists_check(mg_handle *h, bool accum_done) {
     int np = h->np, nb = h->nblk_chk;
     double *r2 = h->d_blkmax + 2 * nb;
-    k_chk_accum<<<nb, kChkThreads, 0, h->st>>>(h->d_drostep, h->d_drosum, r2, h->d_blkmax, np,
-                                        h->d_rebuild);
+    if (!accum_done) {
+        k_chk_accum<<<nb, kChkThreads, 0, h->st>>>(h->d_drostep, h->d_drosum, r2, h->d_blkmax, np,
+                                                   h->d_rebuild);
+        h->launches++;
+    }
     k_chk_second<<<nb, kChkThreads, 0, h->st>>>(r2, h->d_blkmax, h->d_blkmax + nb, np, nb, h->drnlist,
                                          h->d_rebuild, h->d_rebuild + 1, h->use_cond ? 1 : 0,
                                          h->cond);
-    h->launches += 2;
+    h->launches += 1;
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }

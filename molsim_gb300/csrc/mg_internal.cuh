@@ -34,6 +34,12 @@ struct mg_phase {
 struct mg_handle {
     int dev = 0;
     cudaStream_t st = nullptr;
+    // mixed form with SPME: the short-range forces (prepare, pair, bonds) run
+    // on st2 beside the mesh path on st, into their own accumulator d_ffx2
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    long long *d_ffx2 = nullptr;
+    bool par_forces = false;        // set while a forked UTotal queues its mesh path
     std::string err;
 
     // ---- parameters ---------------------------------------------------
@@ -206,6 +212,58 @@ __device__ __forceinline__ void mg_dev_error(int *err, int code, int a, int b, i
 __device__ __forceinline__ double mg_r2_exact(double dx, double dy, double dz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
+// First pass of the NList(iSimulationStep) rebuild rule (nlist.F90:598-621)
+// for particle p of a block of kChkThreads threads: drosum += d (drosum
+// restarts after a rebuild), r2 = |drosum|^2 into r2out[p], the block's
+// largest r2 into blkmax[blockIdx.x].  r2 >= 0, and non-negative doubles
+// order as their 64-bit patterns, so the maximum runs on integers.  Every
+// thread of the block calls it (it holds a barrier).
+constexpr int kChkThreads = 256;
+__device__ __forceinline__ void mg_chk_accum(int p, int np, double d0, double d1, double d2, bool reset,
+                                             double *__restrict__ drosum, double *__restrict__ r2out,
+                                             double *__restrict__ blkmax) {
+    __shared__ long long chk_red[kChkThreads / 32];
+    double r2 = 0.0;
+    if (p < np) {
+        double s0, s1, s2;
+        if (reset) {
+            s0 = 0.0 + d0;
+            s1 = 0.0 + d1;
+            s2 = 0.0 + d2;
+        } else {
+            s0 = __dadd_rn(drosum[3 * p], d0);
+            s1 = __dadd_rn(drosum[3 * p + 1], d1);
+            s2 = __dadd_rn(drosum[3 * p + 2], d2);
+        }
+        drosum[3 * p] = s0;
+        drosum[3 * p + 1] = s1;
+        drosum[3 * p + 2] = s2;
+        r2 = __dadd_rn(__dadd_rn(__dmul_rn(s0, s0), __dmul_rn(s1, s1)), __dmul_rn(s2, s2));
+        r2out[p] = r2;
+    }
+    long long m = __double_as_longlong(r2);
+    for (int o = 16; o > 0; o >>= 1) {
+        long long y = __shfl_xor_sync(0xffffffffu, m, o);
+        m = y > m ? y : m;
+    }
+    if ((threadIdx.x & 31) == 0) chk_red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        long long x = (threadIdx.x < kChkThreads / 32) ? chk_red[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            long long y = __shfl_xor_sync(0xffffffffu, x, o);
+            x = y > x ? y : x;
+        }
+        if (threadIdx.x == 0) blkmax[blockIdx.x] = __longlong_as_double(x);
+    }
+}
+
+// the list check's device arrays, for move kernels that run its first pass
+struct mg_chk_args {
+    double *drosum, *r2out, *blkmax;
+    const int *flag;   // nonzero: a rebuild happened at the previous check
+};
+
 // PBCr2 (molaux.F90:159-162) for a box: single conditional image shift
 __device__ __forceinline__ double mg_pbc1(double d, double half, double len) {
     return (fabs(d) > half) ? __dsub_rn(d, copysign(len, d)) : d;
@@ -235,7 +293,8 @@ void mg_phase_collect(mg_handle *h);
 // ---- module entry points (host side) ----------------------------------------------
 int mg_lists_init(mg_handle *h);
 int mg_lists_build(mg_handle *h, bool conditional);   // cell sort + Verlet list
-int mg_lists_check(mg_handle *h);                      // NList(iSimulationStep) rule on device
+int mg_lists_check(mg_handle *h, bool accum_done = false);   // NList(iSimulationStep) rule on device
+mg_chk_args mg_lists_chk_args(mg_handle *h);          // arrays for a move kernel's first pass
 int mg_lists_export(mg_handle *h, int32_t *nneighpn, int32_t *jpnlist, int32_t maxnneigh);
 int mg_cells_export(mg_handle *h, int32_t *ncell, int32_t *cellip);
 int mg_mc_cells_set(mg_handle *h);

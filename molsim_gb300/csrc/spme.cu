@@ -333,6 +333,7 @@ struct SplineArgs {
     // brick's particles (log2 of the brick edge and of the bricks per edge)
     int lB, lnb;
     int *count, *rank, *brick;
+    int assign;            // gather: the first writer of the force accumulator
 };
 
 // Spline data of every particle, once per call (the only FP64 of the mesh
@@ -613,9 +614,17 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     if (j != 0 || !valid) return;
     T qk = -(T)a.az[p];   // kx, ky, kz = dkdr * EpsiFourPi
     if (MIXED) {
-        ffx[3 * p + 0] += mg_f2fx((float)(qk * kx * e0));
-        ffx[3 * p + 1] += mg_f2fx((float)(qk * ky * e1));
-        ffx[3 * p + 2] += mg_f2fx((float)(qk * kz * e2));
+        long long f0 = mg_f2fx((float)(qk * kx * e0)), f1 = mg_f2fx((float)(qk * ky * e1)),
+                  f2 = mg_f2fx((float)(qk * kz * e2));
+        if (a.assign) {   // the short-range forces went to their own accumulator
+            ffx[3 * p + 0] = f0;
+            ffx[3 * p + 1] = f1;
+            ffx[3 * p + 2] = f2;
+        } else {
+            ffx[3 * p + 0] += f0;
+            ffx[3 * p + 1] += f1;
+            ffx[3 * p + 2] += f2;
+        }
     } else {
         force[3 * p + 0] += (double)qk * (double)e0 * (double)kx;
         force[3 * p + 1] += (double)qk * (double)e1 * (double)ky;
@@ -1333,6 +1342,7 @@ static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
     sa.count = h->d_brick_count;
     sa.rank = h->d_brick_rank;
     sa.brick = h->d_brick_of;
+    sa.assign = h->par_forces ? 1 : 0;
     bk.n = n;
     bk.B = h->brick;
     bk.nb = h->nbrick_edge;
