@@ -124,6 +124,8 @@ struct mg_handle {
     size_t spread_smem = 0, gather_smem = 0;
     int fx_shift = 30, fx_shift64 = 48;
     int spread_wpb = 4;             // spread: bricks (warps) per block
+    int spread_wpb_lane = 4;        // the same for the lane-per-particle spread
+    size_t spread_smem_lane = 0;
     int spread_chunk = 256;         // particles staged per pass of the spread              // mixed spread: weights scaled by 2^fx_shift into int32
     int *d_brick_count = nullptr, *d_brick_perm = nullptr, *d_brick_rank = nullptr, *d_brick_of = nullptr;
     int *d_brick_start = nullptr;

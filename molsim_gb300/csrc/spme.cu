@@ -543,15 +543,92 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
     constexpr int XL = t <= 16 ? 16 : 32, RPI = 32 / XL;
     int mn = b.n - 1, cx = lane & (XL - 1);
     if (cx < t) {
-        size_t gx = (size_t)((ox + cx) & mn);
-        for (int row = lane / XL; row < t * t; row += RPI) {
-            long long v = (long long)tile[row * t + cx];
-            if (v == 0) continue;
-            int cy = row % t, cz = row / t;
-            size_t idx = ((((size_t)((oz + cz) & mn) << b.ln) + (size_t)((oy + cy) & mn)) << b.ln) | gx;
-            atomicAdd(reinterpret_cast<unsigned long long *>(Qfx) + idx, (unsigned long long)v);
+        unsigned long long *qx = reinterpret_cast<unsigned long long *>(Qfx) + ((ox + cx) & mn);
+        const ACC *tz = tile + cx;
+        for (int cz = 0; cz < t; ++cz, tz += t * t) {
+            unsigned long long *qz = qx + ((size_t)((oz + cz) & mn) << (2 * b.ln));
+            for (int cy = lane / XL; cy < t; cy += RPI) {
+                long long v = (long long)tz[cy * t];
+                if (v != 0) atomicAdd(qz + ((size_t)((oy + cy) & mn) << b.ln), (unsigned long long)v);
+            }
         }
     }
+}
+
+// spread, mixed form: one warp per work item (up to 32 particles of one
+// brick), one lane per particle.  The lane holds its particle's B-spline
+// weights in registers (the x weights times charge and scale) and adds the
+// order^3 stamp values into the warp's 32-bit fixed-point tile with
+// shared-memory integer atomics (exact, so the tile does not depend on the
+// order of the adds; the scale keeps 32 stamps below 2^31).  The tile is then
+// added into the 64-bit fixed-point mesh with integer atomics, as in
+// k_spread_warp.
+template <int ORDER, int B>
+__global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, const int *__restrict__ corner,
+                                                                   const float *__restrict__ w,
+                                                                   const double *__restrict__ az, int np,
+                                                                   long long *__restrict__ Qfx) {
+    constexpr int t = B + ORDER - 1, t3 = t * t * t;
+    extern __shared__ __align__(16) int tile_l[];
+    int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+    int *tile = tile_l + (size_t)wib * t3;
+    int item = blockIdx.x * nwb + wib;
+    if (item >= b.istart[b.nbricks]) return;
+    int brick = b.item_brick[item];
+    for (int k = lane; k < t3; k += 32) tile[k] = 0;
+    int mnb = b.nb - 1;
+    int bx = brick & mnb, by = (brick >> b.lnb) & mnb, bz = brick >> (2 * b.lnb);
+    int ox = bx * B - (ORDER - 1), oy = by * B - (ORDER - 1), oz = bz * B - (ORDER - 1);
+    int first = b.start[brick] + (item - b.istart[brick]) * b.M;
+    int last = min(first + b.M, b.start[brick + 1]);
+    int q = first + lane;
+    bool act = q < last;
+    float wx[ORDER], wy[ORDER], wz[ORDER];
+    int base = 0;
+    if (act) {
+        int p = b.perm[q];
+        int cx = corner[p] - ox, cy = corner[np + p] - oy, cz = corner[2 * np + p] - oz;
+        base = (cz * t + cy) * t + cx;
+        float qs = (float)az[p] * b.fx_scale;
+#pragma unroll
+        for (int i = 0; i < ORDER; ++i) {
+            wx[i] = qs * w[(size_t)i * np + p];
+            wy[i] = w[(size_t)(ORDER + i) * np + p];
+            wz[i] = w[(size_t)(2 * ORDER + i) * np + p];
+        }
+    }
+    __syncwarp();
+    if (act) {
+#pragma unroll
+        for (int iz = 0; iz < ORDER; ++iz) {
+#pragma unroll
+            for (int iy = 0; iy < ORDER; ++iy) {
+                float wyz = wy[iy] * wz[iz];
+                int *row = tile + base - (iz * t + iy) * t;
+#pragma unroll
+                for (int ix = 0; ix < ORDER; ++ix) atomicAdd(row - ix, __float2int_rn(wx[ix] * wyz));
+            }
+        }
+    }
+    __syncwarp();
+    constexpr int XL = t <= 16 ? 16 : 32, RPI = 32 / XL;
+    int mn = b.n - 1, cx = lane & (XL - 1);
+    if (cx < t) {
+        unsigned long long *qx = reinterpret_cast<unsigned long long *>(Qfx) + ((ox + cx) & mn);
+        const int *tz = tile + cx;
+        for (int cz = 0; cz < t; ++cz, tz += t * t) {
+            unsigned long long *qz = qx + ((size_t)((oz + cz) & mn) << (2 * b.ln));
+            for (int cy = lane / XL; cy < t; cy += RPI) {
+                long long v = (long long)tz[cy * t];
+                if (v != 0) atomicAdd(qz + ((size_t)((oy + cy) & mn) << b.ln), (unsigned long long)v);
+            }
+        }
+    }
+}
+
+template <int ORDER> void spread_lane_attr() {
+    cudaFuncSetAttribute(k_spread_lane<ORDER, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_spread_lane<ORDER, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 // gather: a group of G lanes per particle (G = 8 for orders up to 8, else
@@ -657,6 +734,16 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
     T *w = (T *)h->d_spl_w, *dw = (T *)h->d_spl_dw;
     if (which == 0) {
         k_spline_prepare<T, ORDER><<<(np + 255) / 256, 256, 0, h->st>>>(sa, corner, w, dw);
+    } else if (which == 1 && sizeof(T) == 4) {   // mixed form
+        int wpb = h->spread_wpb_lane;
+        int grid = (h->max_items + wpb - 1) / wpb;
+        const float *wf = (const float *)w;
+        if (h->brick == 8)
+            k_spread_lane<ORDER, 8><<<grid, 32 * wpb, h->spread_smem_lane, h->st>>>(
+                bk, corner, wf, h->d_az, np, (long long *)h->d_Qfx);
+        else
+            k_spread_lane<ORDER, 16><<<grid, 32 * wpb, h->spread_smem_lane, h->st>>>(
+                bk, corner, wf, h->d_az, np, (long long *)h->d_Qfx);
     } else if (which == 1) {
         int wpb = h->spread_wpb;
         int grid = (h->max_items + wpb - 1) / wpb;
@@ -1199,6 +1286,18 @@ int mg_spme_init(mg_handle *h) {
         return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME spread tile does not fit in shared memory");
     h->spread_smem = ((h->spread_wpb * acc * t3 + 15) & ~(size_t)15) + h->spread_wpb * stage;
     (void)per_warp;
+    // lane-per-particle spread (mixed form): a 32-bit tile per warp, no staging
+    {
+        int bestl = 0;
+        h->spread_wpb_lane = 1;
+        for (int wpb = 1; wpb <= kSpreadWarps; ++wpb) {
+            size_t blk = wpb * sizeof(int) * t3;
+            if (blk > (size_t)200 * 1024) break;
+            int blocks = std::min<int>(32, (int)((size_t)228 * 1024 / (blk + 1024)));
+            if (blocks * wpb >= bestl) { bestl = blocks * wpb; h->spread_wpb_lane = wpb; }
+        }
+        h->spread_smem_lane = h->spread_wpb_lane * sizeof(int) * t3;
+    }
     h->spread_m = kSpreadItem;
     h->max_items = h->nbricks + (h->np + kSpreadItem - 1) / kSpreadItem;
     MG_CUDA(h, cudaMalloc(&h->d_brick_count, sizeof(int) * h->nbricks));
@@ -1216,6 +1315,8 @@ int mg_spme_init(mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_spl_dw, tsz * 3 * h->order * (size_t)h->np));
     spread_attrs<float, int>();
     spread_attrs<double, long long>();
+    spread_lane_attr<4>(); spread_lane_attr<5>(); spread_lane_attr<6>(); spread_lane_attr<7>(); spread_lane_attr<8>();
+    spread_lane_attr<9>(); spread_lane_attr<10>(); spread_lane_attr<11>(); spread_lane_attr<12>();
     // stamp weights q*Mx*My*Mz are below max|q| in magnitude (cardinal
     // B-spline values are < 1); the integer scale keeps them below 2^31
     double qmax = 1.0;
