@@ -627,8 +627,9 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
 
 // force -> forceo with the surface force and the unit factor (energy.F90:405-424)
 template <bool MIXED>
-__global__ void k_epilogue(const double *__restrict__ force, const long long *__restrict__ ffx,
-                           const long long *__restrict__ ffx2, const double *__restrict__ az,
+__global__ void k_epilogue(const double *__restrict__ force, const double *__restrict__ force2,
+                           const long long *__restrict__ ffx, const long long *__restrict__ ffx2,
+                           const double *__restrict__ az,
                            const double *__restrict__ uout, int o,
                            int np, int lsurf, double surf_k, double fac,
                            double *__restrict__ forceo) {
@@ -636,7 +637,7 @@ __global__ void k_epilogue(const double *__restrict__ force, const long long *__
     if (p >= np) return;
     for (int m = 0; m < 3; ++m) {
         double f = MIXED ? (double)(ffx[3 * p + m] + (ffx2 ? ffx2[3 * p + m] : 0ll)) * MG_FX_INV
-                         : force[3 * p + m];
+                         : (force2 ? __dadd_rn(force[3 * p + m], force2[3 * p + m]) : force[3 * p + m]);
         if (lsurf) f = f - surf_k * az[p] * uout[o + 4 + m];
         forceo[3 * p + m] = f * fac;
     }
@@ -790,6 +791,7 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
         if (h->ewald == MG_EWALD_SPM) MG_CUDA(h, cudaMalloc(&h->d_ffx2, sizeof(long long) * 3 * np));
     } else {
         MG_CUDA(h, cudaMalloc(&h->d_force, sizeof(double) * 3 * np));
+        if (h->ewald == MG_EWALD_SPM) MG_CUDA(h, cudaMalloc(&h->d_force2, sizeof(double) * 3 * np));
     }
     return MG_OK;
 }
@@ -807,24 +809,27 @@ int mg_utotal_launch(mg_handle *h) {
         cg.lenf[m] = (float)h->boxlen[m];
         cg.halff[m] = (float)h->boxlen2[m];
     }
-    // mixed form with SPME (uncaptured phase timing aside): the short-range
-    // forces run on the second stream into d_ffx2 while the mesh path runs here
-    bool par = mixed && h->ewald == MG_EWALD_SPM && h->d_ffx2 && !h->timing;
+    // SPME (uncaptured phase timing aside): the short-range forces run on the
+    // second stream into their own accumulator while the mesh path runs here
+    bool par = h->ewald == MG_EWALD_SPM && (mixed ? h->d_ffx2 != nullptr : h->d_force2 != nullptr) &&
+               !h->timing;
     cudaStream_t ss = h->st;
     long long *ffx_sr = h->d_ffx;
+    double *force_sr = h->d_force;
     if (par) {
         MG_CUDA(h, cudaEventRecord(h->ev_fork, h->st));
         MG_CUDA(h, cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
         ss = h->st2;
         ffx_sr = h->d_ffx2;
+        force_sr = h->d_force2;
     }
     MG_TRY(mg_phase_begin(h, "prepare"));
     if (mixed)
         k_prepare_f32<<<(np + kThreads - 1) / kThreads, kThreads, 0, ss>>>(
             h->d_ro, h->d_perm, h->d_type, h->d_cellof, np, cg, h->d_pos_f, h->d_cell_s);
     else
-        k_prepare<<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(h->d_ro, h->d_perm, h->d_type,
-                                                                         np, h->d_pos_s);
+        k_prepare<<<(np + kThreads - 1) / kThreads, kThreads, 0, ss>>>(h->d_ro, h->d_perm, h->d_type,
+                                                                      np, h->d_pos_s);
     MG_TRY(mg_phase_end(h, "prepare"));
     MG_TRY(mg_phase_begin(h, "pair"));
     PairArgs a;
@@ -855,7 +860,7 @@ int mg_utotal_launch(mg_handle *h) {
     }
     a.rcut2 = h->rcut2;
     a.cellcut = (h->txintlist == MG_CELLLIST) ? 1 : 0;
-    a.force = h->d_force;
+    a.force = force_sr;
     a.ffx = h->d_ffx;
     a.part = h->d_part + h->part_pair;
     a.err = h->d_err;
@@ -900,18 +905,33 @@ int mg_utotal_launch(mg_handle *h) {
         case 16: k_pair_f32<16><<<nbt, kPairThreads, 0, ss>>>(f); break;
         default: k_pair_f32<32><<<nbt, kPairThreads, 0, ss>>>(f); break;
         }
-        if (par && h->nbond > 0) {   // bonds follow the pairs on the second stream
+    } else {
+        if (h->pair_warp) k_pair<false, true><<<nb, kPairThreads, sm, ss>>>(a);
+        else k_pair<false, false><<<nb, kPairThreads, sm, ss>>>(a);
+    }
+    if (par && h->nbond > 0) {   // bonds follow the pairs on the second stream
+        if (mixed)
             k_bond<true><<<h->nblk_bond, kBondThreads, 0, ss>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
                                                             h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                            h->d_bond_p, a.box, h->d_force, ffx_sr,
+                                                            h->d_bond_p, a.box, force_sr, ffx_sr,
                                                             h->d_part + h->part_bond);
-            h->launches++;
-        }
-        if (par) MG_CUDA(h, cudaEventRecord(h->ev_join, ss));
-    } else {
-        if (h->pair_warp) k_pair<false, true><<<nb, kPairThreads, sm, h->st>>>(a);
-        else k_pair<false, false><<<nb, kPairThreads, sm, h->st>>>(a);
+        else
+            k_bond<false><<<h->nblk_bond, kBondThreads, 0, ss>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
+                                                             h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
+                                                             h->d_bond_p, a.box, force_sr, ffx_sr,
+                                                             h->d_part + h->part_bond);
+        h->launches++;
     }
+    h->chk_queued = false;
+    if (par && h->chk_side) {   // the list check overlaps the mesh path too
+        cudaStream_t keep = h->st;
+        h->st = ss;
+        int cst = mg_lists_check(h, true);
+        h->st = keep;
+        MG_TRY(cst);
+        h->chk_queued = true;
+    }
+    if (par) MG_CUDA(h, cudaEventRecord(h->ev_join, ss));
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "pair"));
 
@@ -974,12 +994,12 @@ int mg_utotal_launch(mg_handle *h) {
     int lsurf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? 1 : 0;
     if (mixed)
         k_epilogue<true><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
-            h->d_force, h->d_ffx, par ? h->d_ffx2 : nullptr, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf,
+            h->d_force, nullptr, h->d_ffx, par ? h->d_ffx2 : nullptr, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf,
             surf_k, h->force_fac, h->d_forceo);
     else
         k_epilogue<false><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
-            h->d_force, h->d_ffx, nullptr, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf, surf_k,
-            h->force_fac, h->d_forceo);
+            h->d_force, par ? h->d_force2 : nullptr, h->d_ffx, nullptr, h->d_az, h->d_uout, h->nptpt + 1, np,
+            lsurf, surf_k, h->force_fac, h->d_forceo);
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "bond+reduce"));
     MG_CUDA(h, cudaGetLastError());

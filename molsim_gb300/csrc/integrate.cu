@@ -350,7 +350,10 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     k_bd_move<<<(np + kChkThreads - 1) / kChkThreads, kChkThreads, sm, h->st>>>(a);   // advances the GauRandom state too
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "bd_move"));
-    MG_TRY(mg_utotal_launch(h));
+    h->chk_side = true;
+    int ust = mg_utotal_launch(h);
+    h->chk_side = false;
+    MG_TRY(ust);
     MG_TRY(list_step(h, true));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
@@ -362,9 +365,12 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
 // build only when it is due, so that uncaptured steps run the same kernels as
 // the graph does.
 static int list_step(mg_handle *h, bool accum_done) {
-    MG_TRY(mg_phase_begin(h, "list"));
-    MG_TRY(mg_lists_check(h, accum_done));
-    MG_TRY(mg_phase_end(h, "list"));
+    if (!h->chk_queued) {   // else UTotal queued it beside the mesh path
+        MG_TRY(mg_phase_begin(h, "list"));
+        MG_TRY(mg_lists_check(h, accum_done));
+        MG_TRY(mg_phase_end(h, "list"));
+    }
+    h->chk_queued = false;
     if (h->use_cond) return MG_OK;
     int flag = 0;
     MG_CUDA(h, cudaMemcpyAsync(&flag, h->d_rebuild, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -396,7 +402,10 @@ int mg_integrate_md_step_launch(mg_handle *h) {
     k_md_pos<<<gb, kChkThreads, 0, h->st>>>(a);
     h->launches++;
     MG_TRY(mg_phase_end(h, "md_pos"));
-    MG_TRY(mg_utotal_launch(h));
+    h->chk_side = true;
+    int ust = mg_utotal_launch(h);
+    h->chk_side = false;
+    MG_TRY(ust);
     k_md_vel<<<gb, kChkThreads, 0, h->st>>>(a);
     h->launches++;
     MG_TRY(list_step(h, true));

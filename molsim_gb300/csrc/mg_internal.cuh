@@ -34,12 +34,17 @@ struct mg_phase {
 struct mg_handle {
     int dev = 0;
     cudaStream_t st = nullptr;
-    // mixed form with SPME: the short-range forces (prepare, pair, bonds) run
-    // on st2 beside the mesh path on st, into their own accumulator d_ffx2
+    // SPME: the short-range forces (prepare, pair, bonds) run on st2 beside
+    // the mesh path on st, into their own accumulator (d_ffx2 in the mixed
+    // form, d_force2 in the FP64 form)
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long *d_ffx2 = nullptr;
+    double *d_force2 = nullptr;
     bool par_forces = false;        // set while a forked UTotal queues its mesh path
+    // a device step asks UTotal to queue the list check's second pass on st2
+    // (it needs only the move's displacements); chk_queued reports that it did
+    bool chk_side = false, chk_queued = false;
     std::string err;
 
     // ---- parameters ---------------------------------------------------

@@ -703,9 +703,17 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
             ffx[3 * p + 2] += f2;
         }
     } else {
-        force[3 * p + 0] += (double)qk * (double)e0 * (double)kx;
-        force[3 * p + 1] += (double)qk * (double)e1 * (double)ky;
-        force[3 * p + 2] += (double)qk * (double)e2 * (double)kz;
+        double f0 = (double)qk * (double)e0 * (double)kx, f1 = (double)qk * (double)e1 * (double)ky,
+               f2 = (double)qk * (double)e2 * (double)kz;
+        if (a.assign) {
+            force[3 * p + 0] = f0;
+            force[3 * p + 1] = f1;
+            force[3 * p + 2] = f2;
+        } else {
+            force[3 * p + 0] += f0;
+            force[3 * p + 1] += f1;
+            force[3 * p + 2] += f2;
+        }
     }
 }
 
