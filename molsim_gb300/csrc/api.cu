@@ -503,6 +503,7 @@ static int run_steps(mg_handle *h, int nstep, bool bd) {
         return MG_OK;
     }
     MG_TRY(capture_step(h, bd));
+    if (bd && nstep > 0) MG_TRY(mg_integrate_bd_prime(h));
     for (int s = 0; s < nstep; ++s) MG_CUDA(h, cudaGraphLaunch(g, h->st));
     return MG_OK;
 }
@@ -596,6 +597,7 @@ int mg_bench_steps(mg_handle *h, int32_t kind, int32_t nstep, int64_t flush_byte
     double total = 0.0;
     int st = MG_OK;
     if (!h->timing) st = capture_step(h, bd);
+    if (st == MG_OK && bd && !h->timing) st = mg_integrate_bd_prime(h);
     for (int s = 0; s < nstep && st == MG_OK; ++s) {
         if (flush) cudaMemsetAsync(flush, s & 0xff, (size_t)flush_bytes, h->st);
         cudaEventRecord(e0, h->st);
@@ -753,6 +755,7 @@ int mg_ensemble_run(mg_ensemble *e, int32_t kind, int32_t nstep, double *ms) {
             MG_TRY(mg_utotal_launch(h));
             h->have_force = true;
         }
+        if (kind == 1) MG_TRY(mg_integrate_bd_prime(h));
         if (cudaStreamSynchronize(h->st) != cudaSuccess) return ens_fail(e, MG_ERR_CUDA, "replica stream");
     }
     MG_TRY_E(e, ens_capture(e, kind));

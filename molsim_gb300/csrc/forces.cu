@@ -923,6 +923,15 @@ int mg_utotal_launch(mg_handle *h) {
         h->launches++;
     }
     h->chk_queued = false;
+    h->cand_queued = false;
+    if (par && h->cand_side) {   // the next BD step's candidates (after this step's move)
+        cudaStream_t keep = h->st;
+        h->st = ss;
+        int cst = mg_integrate_bd_cand(h);
+        h->st = keep;
+        MG_TRY(cst);
+        h->cand_queued = true;
+    }
     if (par && h->chk_side) {   // the list check overlaps the mesh path too
         cudaStream_t keep = h->st;
         h->st = ss;

@@ -298,6 +298,7 @@ int mg_integrate_bd_setup(mg_handle *h, const double *fac1, const double *fac2, 
     MG_CUDA(h, cudaMemcpy(h->d_rng_save, &zero, sizeof(double), cudaMemcpyHostToDevice));
     h->bd_ready = true;
     h->have_force = false;
+    h->cand_ready = false;
     return MG_OK;
 }
 
@@ -319,8 +320,30 @@ int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, cons
 
 static int list_step(mg_handle *h, bool accum_done);
 
-// one BD step (BDStep, UTotal, list check) queued on the stream
+// GauRandom candidate pairs from the generator state in d_rng, on h->st
+int mg_integrate_bd_cand(mg_handle *h) {
+    int nc = h->ncand, nblk = nc / kCandBlock;
+    if (h->form == MG_MIXED)
+        k_bd_cand<true><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
+    else
+        k_bd_cand<false><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+int mg_integrate_bd_prime(mg_handle *h) {
+    if (!h->cand_ready) MG_TRY(mg_integrate_bd_cand(h));
+    h->cand_ready = true;
+    return MG_OK;
+}
+
+// one BD step (BDStep, UTotal, list check) queued on the stream.  Uncaptured,
+// the step draws its own candidates first; captured into a graph (use_cond),
+// it finds them drawn (mg_integrate_bd_prime, or the previous step) and
+// draws the next step's after its move, beside the UTotal where it can.
 int mg_integrate_bd_step_launch(mg_handle *h) {
+    bool prefetch = h->use_cond;
     int np = h->np, nc = h->ncand, nblk = nc / kCandBlock;
     BdArgs a;
     a.ro = h->d_ro;
@@ -340,20 +363,24 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     a.err = h->d_err;
     a.chk = mg_lists_chk_args(h);
     size_t sm = sizeof(int) * nblk;
-    MG_TRY(mg_phase_begin(h, "bd_rng"));
-    if (h->form == MG_MIXED)
-        k_bd_cand<true><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
-    else
-        k_bd_cand<false><<<nblk, kCandBlock, 0, h->st>>>(h->d_rng, nc, (double2 *)h->d_cval, h->d_cidx, h->d_scan_tmp);
-    MG_TRY(mg_phase_end(h, "bd_rng"));
+    if (!prefetch) {
+        MG_TRY(mg_phase_begin(h, "bd_rng"));
+        MG_TRY(mg_integrate_bd_cand(h));
+        MG_TRY(mg_phase_end(h, "bd_rng"));
+    }
     MG_TRY(mg_phase_begin(h, "bd_move"));
     k_bd_move<<<(np + kChkThreads - 1) / kChkThreads, kChkThreads, sm, h->st>>>(a);   // advances the GauRandom state too
-    h->launches += 2;
+    h->launches += 1;
     MG_TRY(mg_phase_end(h, "bd_move"));
     h->chk_side = true;
+    h->cand_side = prefetch;
     int ust = mg_utotal_launch(h);
     h->chk_side = false;
+    h->cand_side = false;
     MG_TRY(ust);
+    if (prefetch && !h->cand_queued) MG_TRY(mg_integrate_bd_cand(h));   // UTotal did not fork
+    h->cand_queued = false;
+    if (!prefetch) h->cand_ready = false;   // consumed, none drawn ahead
     MG_TRY(list_step(h, true));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;

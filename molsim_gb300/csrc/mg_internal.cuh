@@ -168,6 +168,10 @@ struct mg_handle {
     double tstep = 0;
     double *d_massip = nullptr, *d_rod = nullptr, *d_rodd = nullptr;
     bool md_ready = false, bd_ready = false, have_force = false;
+    // BD deviates: a captured step draws the next step's GauRandom candidates
+    // beside its UTotal (they depend only on the generator state after the
+    // move); cand_ready: the candidate buffers hold those of the next step
+    bool cand_ready = false, cand_side = false, cand_queued = false;
     double *d_fac1 = nullptr, *d_fac2 = nullptr;
     int *d_rng = nullptr;            // [4] iseed, flag, ncand_short, -
     double *d_rng_save = nullptr;    // [1]
@@ -301,6 +305,8 @@ void mg_phase_collect(mg_handle *h);
 int mg_lists_init(mg_handle *h);
 int mg_lists_build(mg_handle *h, bool conditional);   // cell sort + Verlet list
 int mg_lists_check(mg_handle *h, bool accum_done = false);   // NList(iSimulationStep) rule on device
+int mg_integrate_bd_cand(mg_handle *h);              // GauRandom candidates from the current state (h->st)
+int mg_integrate_bd_prime(mg_handle *h);             // candidates for a captured step, if not ready
 mg_chk_args mg_lists_chk_args(mg_handle *h);          // arrays for a move kernel's first pass
 int mg_lists_export(mg_handle *h, int32_t *nneighpn, int32_t *jpnlist, int32_t maxnneigh);
 int mg_cells_export(mg_handle *h, int32_t *ncell, int32_t *cellip);
