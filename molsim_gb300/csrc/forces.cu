@@ -535,6 +535,7 @@ __device__ __forceinline__ double red_comp(const double *tsum, int t0, int S, in
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
+    mg_pdl_begin();
     __shared__ double tsum[kRedThreads];
     __shared__ double vals[MG_MAX_NPTPT + 1 + 2 + 2 + 3];
     __shared__ int is_last;
@@ -633,6 +634,7 @@ __global__ void k_epilogue(const double *__restrict__ force, const double *__res
                            const double *__restrict__ uout, int o,
                            int np, int lsurf, double surf_k, double fac,
                            double *__restrict__ forceo) {
+    mg_pdl_begin();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     for (int m = 0; m < 3; ++m) {
@@ -998,13 +1000,14 @@ int mg_utotal_launch(mg_handle *h) {
     r.uout = h->d_uout;
     r.rows = h->d_part + h->part_red;
     r.ticket = reinterpret_cast<unsigned *>(h->d_part + 2 * (size_t)h->part_red);
-    k_reduce<<<r.blk0[4], kRedThreads, 0, h->st>>>(r);
+    mg_launch_pdl(k_reduce, r.blk0[4], kRedThreads, 0, h->st, r);
     double surf_k = h->EpsiFourPi * (2.0 * r.surf_fac);
     int lsurf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? 1 : 0;
     if (mixed)
-        k_epilogue<true><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
-            h->d_force, nullptr, h->d_ffx, par ? h->d_ffx2 : nullptr, h->d_az, h->d_uout, h->nptpt + 1, np, lsurf,
-            surf_k, h->force_fac, h->d_forceo);
+        mg_launch_pdl(k_epilogue<true>, (np + kThreads - 1) / kThreads, kThreads, 0, h->st, (const double *)h->d_force,
+                      (const double *)nullptr, (const long long *)h->d_ffx,
+                      (const long long *)(par ? h->d_ffx2 : nullptr), (const double *)h->d_az,
+                      (const double *)h->d_uout, h->nptpt + 1, np, lsurf, surf_k, h->force_fac, h->d_forceo);
     else
         k_epilogue<false><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
             h->d_force, par ? h->d_force2 : nullptr, h->d_ffx, nullptr, h->d_az, h->d_uout, h->nptpt + 1, np,

@@ -223,6 +223,29 @@ __device__ __forceinline__ void mg_dev_error(int *err, int code, int a, int b, i
 __device__ __forceinline__ double mg_r2_exact(double dx, double dy, double dz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
+// Programmatic dependent launch.  A kernel launched by mg_launch_pdl may
+// start while the kernel before it in the stream drains (its blocks take the
+// places that the finished blocks of the predecessor free); it waits for the
+// completion and memory of its predecessor (griddepcontrol.wait) before it
+// reads anything.  Launched without the attribute, the wait is a no-op.
+__device__ __forceinline__ void mg_pdl_begin() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t mg_launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                 Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // First pass of the NList(iSimulationStep) rebuild rule (nlist.F90:598-621)
 // for particle p of a block of kChkThreads threads: drosum += d (drosum
 // restarts after a rebuild), r2 = |drosum|^2 into r2out[p], the block's

@@ -342,6 +342,7 @@ struct SplineArgs {
 template <typename T, int ORDER>
 __global__ void k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__restrict__ w,
                                  T *__restrict__ dw) {
+    mg_pdl_begin();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.np) return;
     int c[3];
@@ -388,6 +389,7 @@ struct BrickArgs {
 // (ceil(count / M)), one block of 1024 threads; the item -> brick map is
 // filled and the counts are cleared for the next call
 __global__ void __launch_bounds__(1024) k_brick_prefix(BrickArgs b) {
+    mg_pdl_begin();
     __shared__ int wsum[2][32];
     constexpr int KMAX = 8;   // counts held in registers (one memory round trip) up to 8192 bricks
     int nb = b.nbricks, per = (nb + 1023) / 1024;
@@ -438,6 +440,7 @@ __global__ void __launch_bounds__(1024) k_brick_prefix(BrickArgs b) {
 }
 
 __global__ void k_brick_scatter(int np, BrickArgs b) {
+    mg_pdl_begin();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < np) b.perm[b.start[b.brick[p]] + b.rank[p]] = p;
 }
@@ -568,6 +571,7 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, 
                                                                    const float *__restrict__ w,
                                                                    const double *__restrict__ az, int np,
                                                                    long long *__restrict__ Qfx) {
+    mg_pdl_begin();
     constexpr int t = B + ORDER - 1, t3 = t * t * t;
     extern __shared__ __align__(16) int tile_l[];
     int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
@@ -644,6 +648,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
                                                     const T *__restrict__ dw, const T *__restrict__ Q,
                                                     T kx, T ky, T kz, double *__restrict__ force,
                                                     long long *__restrict__ ffx) {
+    mg_pdl_begin();
     constexpr int G = ORDER <= 8 ? 8 : 16;
     int g = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G);
     int j = threadIdx.x & (G - 1);
@@ -741,17 +746,17 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
     int *corner = h->d_corner;
     T *w = (T *)h->d_spl_w, *dw = (T *)h->d_spl_dw;
     if (which == 0) {
-        k_spline_prepare<T, ORDER><<<(np + 255) / 256, 256, 0, h->st>>>(sa, corner, w, dw);
+        mg_launch_pdl(k_spline_prepare<T, ORDER>, (np + 255) / 256, 256, 0, h->st, sa, corner, w, dw);
     } else if (which == 1 && sizeof(T) == 4) {   // mixed form
         int wpb = h->spread_wpb_lane;
         int grid = (h->max_items + wpb - 1) / wpb;
         const float *wf = (const float *)w;
         if (h->brick == 8)
-            k_spread_lane<ORDER, 8><<<grid, 32 * wpb, h->spread_smem_lane, h->st>>>(
-                bk, corner, wf, h->d_az, np, (long long *)h->d_Qfx);
+            mg_launch_pdl(k_spread_lane<ORDER, 8>, grid, 32 * wpb, h->spread_smem_lane, h->st, bk, corner, wf,
+                          h->d_az, np, (long long *)h->d_Qfx);
         else
-            k_spread_lane<ORDER, 16><<<grid, 32 * wpb, h->spread_smem_lane, h->st>>>(
-                bk, corner, wf, h->d_az, np, (long long *)h->d_Qfx);
+            mg_launch_pdl(k_spread_lane<ORDER, 16>, grid, 32 * wpb, h->spread_smem_lane, h->st, bk, corner, wf,
+                          h->d_az, np, (long long *)h->d_Qfx);
     } else if (which == 1) {
         int wpb = h->spread_wpb;
         int grid = (h->max_items + wpb - 1) / wpb;
@@ -766,9 +771,9 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
         T kx = (T)(h->dkdr[0] * h->EpsiFourPi), ky = (T)(h->dkdr[1] * h->EpsiFourPi),
           kz = (T)(h->dkdr[2] * h->EpsiFourPi);
         constexpr int G = ORDER <= 8 ? 8 : 16;
-        k_gather_grp<T, sizeof(T) == 4, ORDER><<<(unsigned)(((long)np * G + 255) / 256), 256, 0, h->st>>>(
-            sa, h->d_perm, corner, w, (const T *)h->d_spl_dw, (const T *)h->d_Q, kx, ky, kz, h->d_force,
-            h->d_ffx);
+        mg_launch_pdl(k_gather_grp<T, sizeof(T) == 4, ORDER>, (unsigned)(((long)np * G + 255) / 256), 256, 0,
+                      h->st, sa, h->d_perm, corner, w, (const T *)h->d_spl_dw, (const T *)h->d_Q, kx, ky, kz,
+                      h->d_force, h->d_ffx);
     }
 }
 
@@ -942,6 +947,7 @@ template <typename T, int P>
 __global__ void __launch_bounds__(1024) k_plane_fwd(unsigned long long *__restrict__ Qfx, T fx_inv,
                                                     V2<T> *__restrict__ F, const V2<T> *__restrict__ tw,
                                                     FastDiv fnh) {
+    mg_pdl_begin();
     typedef V2<T> V;
     constexpr int n = 32 * P, nh = n / 2 + 1;
     extern __shared__ unsigned char smem_raw[];
@@ -1026,6 +1032,7 @@ __global__ void __launch_bounds__(1024) k_plane_fwd(unsigned long long *__restri
 template <typename T, int P>
 __global__ void __launch_bounds__(1024) k_slab_conv(V2<T> *__restrict__ F, const V2<T> *__restrict__ tw,
                                                     ConvArgs cv, FastDiv fnh) {
+    mg_pdl_begin();
     typedef V2<T> V;
     constexpr int n = 32 * P, nh = n / 2 + 1;
     extern __shared__ unsigned char smem_raw[];
@@ -1095,6 +1102,7 @@ __global__ void __launch_bounds__(1024) k_slab_conv(V2<T> *__restrict__ F, const
 template <typename T, int P>
 __global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F, T *__restrict__ Q,
                                                     const V2<T> *__restrict__ tw, FastDiv fnh) {
+    mg_pdl_begin();
     typedef V2<T> V;
     constexpr int n = 32 * P, nh = n / 2 + 1;
     extern __shared__ unsigned char smem_raw[];
@@ -1163,13 +1171,13 @@ static int plane_passes(mg_handle *h, float *Q, float2 *F, const float2 *tw, Con
     const int n = 32 * P, thr = 32 * h->fft_warps;
     FastDiv fnh = make_fastdiv((unsigned)h->nh);
     MG_TRY(mg_phase_begin(h, "fft_xy_fwd"));
-    k_plane_fwd<float, P><<<n, thr, plane_smem<P>(h->fft_warps), h->st>>>(h->d_Qfx, fx_inv, F, tw, fnh);
+    mg_launch_pdl(k_plane_fwd<float, P>, n, thr, plane_smem<P>(h->fft_warps), h->st, h->d_Qfx, fx_inv, F, tw, fnh);
     MG_TRY(mg_phase_end(h, "fft_xy_fwd"));
     MG_TRY(mg_phase_begin(h, "fft_z_conv"));
-    k_slab_conv<float, P><<<n, thr, slab_smem<P>(), h->st>>>(F, tw, cv, fnh);
+    mg_launch_pdl(k_slab_conv<float, P>, n, thr, slab_smem<P>(), h->st, F, tw, cv, fnh);
     MG_TRY(mg_phase_end(h, "fft_z_conv"));
     MG_TRY(mg_phase_begin(h, "fft_yx_inv"));
-    k_plane_inv<float, P><<<n, thr, plane_smem<P>(h->fft_warps), h->st>>>(F, Q, tw, fnh);
+    mg_launch_pdl(k_plane_inv<float, P>, n, thr, plane_smem<P>(h->fft_warps), h->st, (const float2 *)F, Q, tw, fnh);
     MG_TRY(mg_phase_end(h, "fft_yx_inv"));
     h->launches += 3;
     MG_CUDA(h, cudaGetLastError());
@@ -1482,8 +1490,8 @@ static int spme_spread(mg_handle *h, const SplineArgs &sa, const BrickArgs &bk) 
     else MG_TRY((mesh_kernel<double, long long>(h, 0, sa, bk)));
     MG_TRY(mg_phase_end(h, "splines"));
     MG_TRY(mg_phase_begin(h, "brick_sort"));
-    k_brick_prefix<<<1, 1024, 0, h->st>>>(bk);   // the counts come from the spline kernel
-    k_brick_scatter<<<gb, tb, 0, h->st>>>(np, bk);
+    mg_launch_pdl(k_brick_prefix, 1, 1024, 0, h->st, bk);   // the counts come from the spline kernel
+    mg_launch_pdl(k_brick_scatter, gb, tb, 0, h->st, np, bk);
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "brick_sort"));
     MG_TRY(mg_phase_begin(h, "spread"));
