@@ -12,11 +12,11 @@ SRCS = [os.path.join(HERE, f) for f in ("molsim_oracle.c", "oracle_fft.c")]
 
 
 def build(force=False):
-    deps = SRCS + [os.path.join(HERE, "molsim_oracle.h"),
+    deps = SRCS + [os.path.join(HERE, "molsim_oracle.h"), os.path.join(HERE, "oracle_par.h"),
                    os.path.join(HERE, "..", "include", "molsim_gb300.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
-    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", LIB, *SRCS, "-lm"]
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-Wall", "-o", LIB, *SRCS, "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stderr)

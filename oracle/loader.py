@@ -34,5 +34,7 @@ def oracle():
         lib.orc_celllist_test.argtypes = [C.c_void_p]
         lib.orc_get_qmesh.restype = C.c_int
         lib.orc_get_qmesh.argtypes = [C.c_void_p, abi.PF64]
+        lib.orc_set_threads.restype = C.c_int
+        lib.orc_set_threads.argtypes = [C.c_int]
         _lib = lib
     return _lib

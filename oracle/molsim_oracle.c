@@ -19,6 +19,7 @@
 #include <string.h>
 #include <complex.h>
 #include "molsim_oracle.h"
+#include "oracle_par.h"
 
 #define Zero 0.0
 #define Half 0.5
@@ -31,6 +32,15 @@ static const double Pi = 3.1415926535897932;   /* mol.F90:63 */
 #define FourPi (Four * Pi)
 
 typedef struct { double re, im; } zc;   /* complex(8) */
+
+/* threads standing in for molsim_par's MPI ranks (oracle_par.h) */
+static int g_orc_threads = 1;
+int orc_threads(void) { return g_orc_threads; }
+int orc_set_threads(int n) {
+    if (n < 1 || n > ORC_MAX_THREADS) return MG_ERR_ARG;
+    g_orc_threads = n;
+    return 0;
+}
 
 static inline zc zmul(zc a, zc b) { zc r; r.re = a.re * b.re - a.im * b.im; r.im = a.re * b.im + a.im * b.re; return r; }
 static inline zc zconj(zc a) { a.im = -a.im; return a; }
@@ -488,7 +498,30 @@ struct orc_sys {
     int32_t iseed, gflag;
     double gsave;
     int bd_have_force;
+    /* private arrays of the threads (the MPI ranks' replicated arrays) */
+    int nthr_alloc;
+    double *thr_force, *thr_u, *thr_mesh;
 };
+
+/* private arrays for nt threads: force (3 np) and energies (nptpt + 1) per
+   thread, and with SPME a charge mesh per thread */
+static int thr_arrays(orc_sys *s, int nt) {
+    if (s->nthr_alloc >= nt) return 0;
+    free(s->thr_force);
+    free(s->thr_u);
+    free(s->thr_mesh);
+    s->thr_force = (double *)malloc(sizeof(double) * (size_t)nt * 3 * s->np);
+    s->thr_u = (double *)malloc(sizeof(double) * (size_t)nt * (s->nptpt + 1));
+    s->thr_mesh = NULL;
+    if (s->ewald == MG_EWALD_SPM)
+        s->thr_mesh = (double *)malloc(sizeof(double) * (size_t)nt * s->nmesh * s->nmesh * s->nmesh);
+    if (!s->thr_force || !s->thr_u || (s->ewald == MG_EWALD_SPM && !s->thr_mesh)) {
+        s->nthr_alloc = 0;
+        return MG_ERR_ALLOC;
+    }
+    s->nthr_alloc = nt;
+    return 0;
+}
 
 #define RO(m, ip) s->ro[3 * ((ip) - 1) + (m) - 1]
 #define FORCE(m, ia) s->force[3 * ((ia) - 1) + (m) - 1]
@@ -686,7 +719,7 @@ void orc_destroy(orc_sys *s) {
                     s->meshfac, s->energyfac, s->virfac, s->Qmesh, s->QmeshTM, s->FQmesh, s->Qspread,
                     s->spline, s->deriv, s->meshmax, s->splinetm, s->derivtm, s->meshmaxtm,
                     s->ipnptm, s->lptm, s->rotm, s->massip, s->rod, s->rodd, s->roddo, s->drostep,
-                    s->fac1, s->fac2};
+                    s->fac1, s->fac2, s->thr_force, s->thr_u, s->thr_mesh};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
     if (s->cell) {
         int nc = s->ncellX * s->ncellY * s->ncellZ;
@@ -1020,11 +1053,16 @@ static inline int table_eval(const orc_sys *s, int iptjpt, double r2, double *us
     return 0;
 }
 
-/* UTwoBodyA, energy.F90:445-544 (Verlet list) */
-static int utwobody_a(orc_sys *s) {
+/* The pair loops run over an ip range [lo, hi) (1-based ip = lo+1 .. hi),
+   accumulating into the force array F, the per-pair-type energies U and the
+   virial *vir: one range and the handle's own arrays is the serial
+   reference; several ranges with private arrays are its MPI ranks. */
+#define FRC(F, m, ia) (F)[3 * ((ia) - 1) + (m) - 1]
+
+/* UTwoBodyA, energy.F90:445-544 (Verlet list: the MD half list or the MC full list) */
+static int utwobody_a_range(orc_sys *s, long lo, long hi, double *F, double *U, double *vir) {
     double virtwob = Zero, fsum = Zero, usum;
-    for (int k = 0; k <= s->nptpt; ++k) s->u_twob[k] = Zero;
-    for (int ip = 1; ip <= s->np; ++ip) {
+    for (int ip = (int)lo + 1; ip <= (int)hi; ++ip) {
         int ipt = IPTPN(ip);
         for (int jploc = 1; jploc <= s->nneighpn[ip - 1]; ++jploc) {
             int jp = s->jpnlist[(size_t)(ip - 1) * s->maxnneigh + jploc - 1];
@@ -1042,29 +1080,24 @@ static int utwobody_a(orc_sys *s) {
                 int st = table_eval(s, iptjpt, r2, &usum, &fsum);
                 if (st) return st;
             }
-            s->u_twob[iptjpt] = s->u_twob[iptjpt] + usum;
-            FORCE(1, ip) = FORCE(1, ip) + (fsum * dx);
-            FORCE(2, ip) = FORCE(2, ip) + (fsum * dy);
-            FORCE(3, ip) = FORCE(3, ip) + (fsum * dz);
-            FORCE(1, jp) = FORCE(1, jp) - (fsum * dx);
-            FORCE(2, jp) = FORCE(2, jp) - (fsum * dy);
-            FORCE(3, jp) = FORCE(3, jp) - (fsum * dz);
+            U[iptjpt] = U[iptjpt] + usum;
+            FRC(F, 1, ip) = FRC(F, 1, ip) + (fsum * dx);
+            FRC(F, 2, ip) = FRC(F, 2, ip) + (fsum * dy);
+            FRC(F, 3, ip) = FRC(F, 3, ip) + (fsum * dz);
+            FRC(F, 1, jp) = FRC(F, 1, jp) - (fsum * dx);
+            FRC(F, 2, jp) = FRC(F, 2, jp) - (fsum * dy);
+            FRC(F, 3, jp) = FRC(F, 3, jp) - (fsum * dz);
             virtwob = virtwob - (fsum * r2);
         }
     }
-    double t = Zero;
-    for (int k = 1; k <= s->nptpt; ++k) t = t + s->u_twob[k];
-    s->u_twob[0] = t;
-    s->u_tot = s->u_tot + s->u_twob[0];
-    s->virial = s->virial + virtwob;
+    *vir = virtwob;
     return 0;
 }
 
 /* UTwoBodyACellList, energy.F90:669-777 */
-static int utwobody_a_celllist(orc_sys *s) {
+static int utwobody_a_celllist_range(orc_sys *s, long lo, long hi, double *F, double *U, double *vir) {
     double virtwob = Zero, usum, fsum;
-    for (int k = 0; k <= s->nptpt; ++k) s->u_twob[k] = Zero;
-    for (int ip = 1; ip <= s->np; ++ip) {
+    for (int ip = (int)lo + 1; ip <= (int)hi; ++ip) {
         int ipt = IPTPN(ip);
         orc_cell *ic = &s->cell[s->cellip[ip - 1]];
         for (int incell = 0; incell < ic->nneighcell; ++incell) {
@@ -1086,19 +1119,84 @@ static int utwobody_a_celllist(orc_sys *s) {
                             int st = table_eval(s, iptjpt, r2, &usum, &fsum);
                             if (st) return st;
                         }
-                        s->u_twob[iptjpt] = s->u_twob[iptjpt] + usum;
-                        FORCE(1, ip) = FORCE(1, ip) + (fsum * dx);
-                        FORCE(2, ip) = FORCE(2, ip) + (fsum * dy);
-                        FORCE(3, ip) = FORCE(3, ip) + (fsum * dz);
-                        FORCE(1, jp) = FORCE(1, jp) - (fsum * dx);
-                        FORCE(2, jp) = FORCE(2, jp) - (fsum * dy);
-                        FORCE(3, jp) = FORCE(3, jp) - (fsum * dz);
+                        U[iptjpt] = U[iptjpt] + usum;
+                        FRC(F, 1, ip) = FRC(F, 1, ip) + (fsum * dx);
+                        FRC(F, 2, ip) = FRC(F, 2, ip) + (fsum * dy);
+                        FRC(F, 3, ip) = FRC(F, 3, ip) + (fsum * dz);
+                        FRC(F, 1, jp) = FRC(F, 1, jp) - (fsum * dx);
+                        FRC(F, 2, jp) = FRC(F, 2, jp) - (fsum * dy);
+                        FRC(F, 3, jp) = FRC(F, 3, jp) - (fsum * dz);
                         virtwob = virtwob - (fsum * r2);
                     }
                 }
                 jp = s->ipnext[jp - 1];
             }
         }
+    }
+    *vir = virtwob;
+    return 0;
+}
+
+/* the pair loop of either list over the threads' ranges; the private force
+   arrays and energies are summed in thread order (the allreduce) */
+typedef struct {
+    orc_sys *s;
+    int cell;
+    double *F;     /* nt x 3 np */
+    double *U;     /* nt x (nptpt + 1) */
+    double vir[ORC_MAX_THREADS];
+    int err[ORC_MAX_THREADS];
+} pair_job;
+
+static void pair_job_run(void *ctx, int t, int nt) {
+    pair_job *j = (pair_job *)ctx;
+    long lo, hi;
+    orc_range(j->s->np, t, nt, &lo, &hi);
+    double *F = j->F + (size_t)t * 3 * j->s->np, *U = j->U + (size_t)t * (j->s->nptpt + 1);
+    memset(F, 0, sizeof(double) * 3 * j->s->np);
+    memset(U, 0, sizeof(double) * (j->s->nptpt + 1));
+    j->err[t] = j->cell ? utwobody_a_celllist_range(j->s, lo, hi, F, U, &j->vir[t])
+                        : utwobody_a_range(j->s, lo, hi, F, U, &j->vir[t]);
+}
+
+static void force_sum_run(void *ctx, int t, int nt) {
+    pair_job *j = (pair_job *)ctx;
+    long n3 = 3L * j->s->np, lo, hi;
+    orc_range(n3, t, nt, &lo, &hi);
+    int ntot = orc_threads();
+    for (long i = lo; i < hi; ++i) {
+        double f = j->s->force[i];
+        for (int k = 0; k < ntot; ++k) f = f + j->F[(size_t)k * n3 + i];
+        j->s->force[i] = f;
+    }
+}
+
+static int utwobody(orc_sys *s, int cell) {
+    double virtwob = Zero;
+    for (int k = 0; k <= s->nptpt; ++k) s->u_twob[k] = Zero;
+    int nt = orc_threads();
+    if (nt == 1) {
+        int st = cell ? utwobody_a_celllist_range(s, 0, s->np, s->force, s->u_twob, &virtwob)
+                      : utwobody_a_range(s, 0, s->np, s->force, s->u_twob, &virtwob);
+        if (st) return st;
+    } else {
+        if (thr_arrays(s, nt)) return MG_ERR_ALLOC;
+        pair_job j;
+        j.s = s;
+        j.cell = cell;
+        j.F = s->thr_force;
+        j.U = s->thr_u;
+        orc_par_run(pair_job_run, &j, nt);
+        int st = 0;
+        for (int t = 0; t < nt && !st; ++t) st = j.err[t];
+        if (!st) {
+            orc_par_run(force_sum_run, &j, nt);
+            for (int t = 0; t < nt; ++t) {
+                for (int k = 1; k <= s->nptpt; ++k) s->u_twob[k] = s->u_twob[k] + j.U[(size_t)t * (s->nptpt + 1) + k];
+                virtwob = virtwob + j.vir[t];
+            }
+        }
+        if (st) return st;
     }
     double t = Zero;
     for (int k = 1; k <= s->nptpt; ++k) t = t + s->u_twob[k];
@@ -1182,15 +1280,13 @@ static void uewald_rec_std(orc_sys *s, double *virrec) {
     }
 }
 
-/* SPMFFTRec, energy.F90:6525-6587 */
-static int spm_fft_rec(orc_sys *s, int lsave, double *uloc, double *virloc) {
+/* the influence function over the planes nz in [nz0, nz1) of the octant:
+   energy and virial sums, then the spectrum times meshfac */
+static void spm_influence_range(orc_sys *s, int nz0, int nz1, double *uloc, double *virloc) {
     int n = s->nmesh, nh = n / 2 + 1;
     zc *F = (zc *)s->FQmesh;
-    if (orc_fft_r2c_3d(n, s->Qmesh, s->FQmesh)) return MG_ERR_ALLOC;
-    if (lsave) memcpy(s->QmeshTM, s->Qmesh, sizeof(double) * (size_t)n * n * n);
-    *uloc = Zero;
 #define FQ(x, y, z) F[((size_t)(z) * n + (y)) * nh + (x)]
-    for (int nz = 0; nz <= n / 2; ++nz) {
+    for (int nz = nz0; nz < nz1; ++nz) {
         int nza = (n - nz) % n;
         for (int ny = 0; ny <= n / 2; ++ny) {
             int nya = (n - ny) % n;
@@ -1212,6 +1308,41 @@ static int spm_fft_rec(orc_sys *s, int lsave, double *uloc, double *virloc) {
         }
     }
 #undef FQ
+}
+
+typedef struct {
+    orc_sys *s;
+    double u[ORC_MAX_THREADS], v[ORC_MAX_THREADS];
+} infl_job;
+
+static void infl_job_run(void *ctx, int t, int nt) {
+    infl_job *j = (infl_job *)ctx;
+    long lo, hi;
+    orc_range(j->s->nmesh / 2 + 1, t, nt, &lo, &hi);
+    j->u[t] = Zero;
+    j->v[t] = Zero;
+    spm_influence_range(j->s, (int)lo, (int)hi, &j->u[t], &j->v[t]);
+}
+
+/* SPMFFTRec, energy.F90:6525-6587 */
+static int spm_fft_rec(orc_sys *s, int lsave, double *uloc, double *virloc) {
+    int n = s->nmesh;
+    if (orc_fft_r2c_3d(n, s->Qmesh, s->FQmesh)) return MG_ERR_ALLOC;
+    if (lsave) memcpy(s->QmeshTM, s->Qmesh, sizeof(double) * (size_t)n * n * n);
+    *uloc = Zero;
+    int nt = orc_threads();
+    if (nt > n / 2 + 1) nt = n / 2 + 1;
+    if (nt == 1) {
+        spm_influence_range(s, 0, n / 2 + 1, uloc, virloc);
+    } else {   /* partial sums per thread, combined in thread order */
+        infl_job j;
+        j.s = s;
+        orc_par_run(infl_job_run, &j, nt);
+        for (int t = 0; t < nt; ++t) {
+            *uloc = *uloc + j.u[t];
+            *virloc = *virloc + j.v[t];
+        }
+    }
     if (orc_fft_c2r_3d(n, s->FQmesh, s->Qmesh)) return MG_ERR_ALLOC;
     return 0;
 }
@@ -1220,11 +1351,10 @@ static int spm_fft_rec(orc_sys *s, int lsave, double *uloc, double *virloc) {
 #define MESHMAX(arr, m, ia) (arr)[(size_t)((ia) - 1) * 3 + (m) - 1]
 #define QM(arr, x, y, z) (arr)[((size_t)(z) * s->s[1] + (y)) * s->s[0] + (x)]
 
-/* UEwaldRecSPM, energy.F90:1207-1297 */
-static int uewald_rec_spm(orc_sys *s, double *virrec) {
+/* splines of particles (lo, hi] (1-based) and their stamps added into Q */
+static void spm_spread_range(orc_sys *s, long lo, long hi, double *Q) {
     int order = s->order, *S3 = s->s;
-    memset(s->Qmesh, 0, sizeof(double) * (size_t)S3[0] * S3[1] * S3[2]);
-    for (int ia = 1; ia <= s->np; ++ia) {
+    for (int ia = (int)lo + 1; ia <= (int)hi; ++ia) {
         for (int m = 1; m <= 3; ++m) {
             int kmax;
             orc_cardinal_bspline(order, s->dkdr[m - 1] * RO(m, ia), &kmax, &SPL(s->spline, 0, m, ia), &SPL(s->deriv, 0, m, ia));
@@ -1239,17 +1369,17 @@ static int uewald_rec_spm(orc_sys *s, double *virrec) {
                 for (int ix = 0; ix <= order - 1; ++ix) {
                     int nx = (S3[0] + MESHMAX(s->meshmax, 1, ia) - ix) % S3[0];
                     double q = qyz * SPL(s->spline, ix, 1, ia);
-                    QM(s->Qmesh, nx, ny, nz) = QM(s->Qmesh, nx, ny, nz) + q;
+                    QM(Q, nx, ny, nz) = QM(Q, nx, ny, nz) + q;
                 }
             }
         }
     }
-    memcpy(s->Qspread, s->Qmesh, sizeof(double) * (size_t)S3[0] * S3[1] * S3[2]);
-    double urec;
-    int st = spm_fft_rec(s, s->mode == MG_MC, &urec, virrec);
-    if (st) return st;
-    s->u_rec = urec;
-    for (int ia = 1; ia <= s->np; ++ia) {
+}
+
+/* the mesh forces of particles (lo, hi] (1-based) */
+static void spm_gather_range(orc_sys *s, long lo, long hi) {
+    int order = s->order, *S3 = s->s;
+    for (int ia = (int)lo + 1; ia <= (int)hi; ++ia) {
         double esum[3] = {Zero, Zero, Zero};
         for (int iz = 0; iz <= order - 1; ++iz) {
             int nz = (S3[2] + MESHMAX(s->meshmax, 3, ia) - iz) % S3[2];
@@ -1270,8 +1400,64 @@ static int uewald_rec_spm(orc_sys *s, double *virrec) {
         for (int m = 1; m <= 3; ++m)
             FORCE(m, ia) = FORCE(m, ia) - AZ(ia) * esum[m - 1] * s->dkdr[m - 1] * s->EpsiFourPi;
     }
+}
+
+typedef struct {
+    orc_sys *s;
+    double *Qt;   /* nt private meshes */
+    size_t n3;
+    int nt;
+} spread_job;
+
+static void spread_job_run(void *ctx, int t, int nt) {
+    spread_job *j = (spread_job *)ctx;
+    long lo, hi;
+    orc_range(j->s->np, t, nt, &lo, &hi);
+    memset(j->Qt + (size_t)t * j->n3, 0, sizeof(double) * j->n3);
+    spm_spread_range(j->s, lo, hi, j->Qt + (size_t)t * j->n3);
+}
+
+static void mesh_sum_run(void *ctx, int t, int nt) {   /* Q = sum of the private meshes, thread order */
+    spread_job *j = (spread_job *)ctx;
+    long lo, hi;
+    orc_range((long)j->n3, t, nt, &lo, &hi);
+    for (long i = lo; i < hi; ++i) {
+        double q = j->Qt[i];
+        for (int k = 1; k < j->nt; ++k) q = q + j->Qt[(size_t)k * j->n3 + i];
+        j->s->Qmesh[i] = q;
+    }
+}
+
+static void gather_job_run(void *ctx, int t, int nt) {
+    spread_job *j = (spread_job *)ctx;
+    long lo, hi;
+    orc_range(j->s->np, t, nt, &lo, &hi);
+    spm_gather_range(j->s, lo, hi);
+}
+
+/* UEwaldRecSPM, energy.F90:1207-1297 */
+static int uewald_rec_spm(orc_sys *s, double *virrec) {
+    int *S3 = s->s;
+    size_t n3 = (size_t)S3[0] * S3[1] * S3[2];
+    int nt = orc_threads();
+    spread_job j = {s, NULL, n3, nt};
+    if (nt == 1) {
+        memset(s->Qmesh, 0, sizeof(double) * n3);
+        spm_spread_range(s, 0, s->np, s->Qmesh);
+    } else {
+        if (thr_arrays(s, nt)) return MG_ERR_ALLOC;
+        j.Qt = s->thr_mesh;
+        orc_par_run(spread_job_run, &j, nt);
+        orc_par_run(mesh_sum_run, &j, nt);
+    }
+    memcpy(s->Qspread, s->Qmesh, sizeof(double) * n3);
+    double urec;
+    int st = spm_fft_rec(s, s->mode == MG_MC, &urec, virrec);
+    if (st) return st;
+    s->u_rec = urec;
+    orc_par_run(gather_job_run, &j, nt);   /* each thread its own particles */
     if (s->mode == MG_MC) {
-        memcpy(s->Qmesh, s->QmeshTM, sizeof(double) * (size_t)S3[0] * S3[1] * S3[2]);
+        memcpy(s->Qmesh, s->QmeshTM, sizeof(double) * n3);
         s->urecold = s->u_rec;
     }
     return 0;
@@ -1354,10 +1540,10 @@ static int utotal_core(orc_sys *s) {
     s->u_bond = Zero;
     if (s->txintlist == MG_VLIST) {
         if (!s->nneighpn) return MG_ERR_STATE;
-        st = utwobody_a(s);
+        st = utwobody(s, 0);
     } else {
         if (!s->cell) return MG_ERR_STATE;
-        st = utwobody_a_celllist(s);
+        st = utwobody(s, 1);
     }
     if (st) return st;
     if (s->ewald != MG_EWALD_NONE) { st = uewald(s); if (st) return st; }

@@ -43,6 +43,9 @@ void   orc_pot_1_6_12(const mg_pot_params *pp, int iat, int jat, double r1,
                       double *u0, double *u1, double *u2);
 
 /* FFT with FFTW's conventions (forward e^{-i}, unnormalised), mesh q[z][y][x] */
+/* threads standing in for the reference's MPI ranks (oracle_par.h); 1 = serial */
+int orc_set_threads(int n);
+
 int orc_fft_r2c_3d(int n, const double *q, double *fq /* (n/2+1)*n*n complex */);
 int orc_fft_c2r_3d(int n, const double *fq, double *q);
 

@@ -17,6 +17,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include "molsim_oracle.h"
+#include "oracle_par.h"
 
 typedef struct { double re, im; } cpx;
 
@@ -140,34 +141,105 @@ static void fft_columns(int n, cpx *base, size_t stride, int ncol, int sign, cpx
     }
 }
 
-int orc_fft_r2c_3d(int n, const double *q, double *fqd) {
-    int nh = n / 2 + 1;
-    cpx *fq = (cpx *)fqd;
-    cpx *line = malloc(sizeof(cpx) * n), *work = malloc(sizeof(cpx) * 2 * n);
-    cpx *buf = malloc(sizeof(cpx) * COLBLK * (size_t)n);
-    if (!line || !work || !buf) { free(line); free(work); free(buf); return -1; }
-    /* x: real -> half spectrum, two real lines per complex transform
-       (A + iB; X_A = (Z_k + conj Z_{n-k})/2, X_B = (Z_k - conj Z_{n-k})/2i) */
+/* The 3D transforms split their independent lines among the oracle's threads
+   (oracle_par.h); every line is transformed the same way, so the result does
+   not depend on the thread count. */
+typedef struct {
+    int n, sign, pass;   /* pass 0: x lines, 1: columns per z plane, 2: columns per y row */
+    const double *q;     /* r2c input */
+    double *qo;          /* c2r output */
+    cpx *fq;
+    int err;
+} fft_task;
+
+static void fft_x_r2c(fft_task *k, long p0, long p1, cpx *line, cpx *work) {
+    int n = k->n, nh = n / 2 + 1;
     size_t nl = (size_t)n * n;
-    for (size_t l = 0; l < nl; l += 2) {
-        const double *a = q + l * n, *b = (l + 1 < nl) ? q + (l + 1) * n : NULL;
+    for (long pr = p0; pr < p1; ++pr) {
+        size_t l = 2 * (size_t)pr;
+        const double *a = k->q + l * n, *b = (l + 1 < nl) ? k->q + (l + 1) * n : NULL;
         for (int x = 0; x < n; ++x) { line[x].re = a[x]; line[x].im = b ? b[x] : 0.0; }
         dft_line(n, line, -1, work);
-        cpx *fa = fq + l * nh, *fb = fq + (l + 1) * nh;
-        for (int k = 0; k < nh; ++k) {
-            cpx z = line[k], zc = line[(n - k) % n];
-            fa[k].re = 0.5 * (z.re + zc.re);
-            fa[k].im = 0.5 * (z.im - zc.im);
+        cpx *fa = k->fq + l * nh, *fb = k->fq + (l + 1) * nh;
+        for (int kk = 0; kk < nh; ++kk) {
+            cpx z = line[kk], zc = line[(n - kk) % n];
+            fa[kk].re = 0.5 * (z.re + zc.re);
+            fa[kk].im = 0.5 * (z.im - zc.im);
             if (b) {
-                fb[k].re = 0.5 * (z.im + zc.im);
-                fb[k].im = -0.5 * (z.re - zc.re);
+                fb[kk].re = 0.5 * (z.im + zc.im);
+                fb[kk].im = -0.5 * (z.re - zc.re);
             }
         }
     }
-    /* y and z: columns of the half spectrum */
-    for (int z = 0; z < n; ++z) fft_columns(n, fq + (size_t)z * n * nh, nh, nh, -1, buf, work);
-    for (int y = 0; y < n; ++y) fft_columns(n, fq + (size_t)y * nh, (size_t)n * nh, nh, -1, buf, work);
+}
+
+static void fft_x_c2r(fft_task *k, long p0, long p1, cpx *line, cpx *work) {
+    int n = k->n, nh = n / 2 + 1;
+    size_t nl = (size_t)n * n;
+    for (long pr = p0; pr < p1; ++pr) {
+        size_t l = 2 * (size_t)pr;
+        const cpx *ha = k->fq + l * nh, *hb = (l + 1 < nl) ? k->fq + (l + 1) * nh : NULL;
+        for (int kq = 0; kq < n; ++kq) {
+            cpx xa, xb = {0.0, 0.0};
+            int kk = kq < nh ? kq : n - kq;
+            double sg = kq < nh ? 1.0 : -1.0;
+            xa.re = ha[kk].re; xa.im = sg * ha[kk].im;
+            if (hb) { xb.re = hb[kk].re; xb.im = sg * hb[kk].im; }
+            if (kk == 0 || 2 * kk == n) { xa.im = 0.0; xb.im = 0.0; }
+            line[kq].re = xa.re - xb.im;
+            line[kq].im = xa.im + xb.re;
+        }
+        dft_line(n, line, +1, work);
+        double *qa = k->qo + l * n, *qb = hb ? k->qo + (l + 1) * n : NULL;
+        for (int x = 0; x < n; ++x) {
+            qa[x] = line[x].re;
+            if (qb) qb[x] = line[x].im;
+        }
+    }
+}
+
+static void fft_task_run(void *ctx, int t, int nt) {
+    fft_task *k = (fft_task *)ctx;
+    int n = k->n, nh = n / 2 + 1;
+    cpx *line = malloc(sizeof(cpx) * n), *work = malloc(sizeof(cpx) * 2 * n);
+    cpx *buf = malloc(sizeof(cpx) * COLBLK * (size_t)n);
+    if (!line || !work || !buf) {
+        k->err = 1;
+        free(line); free(work); free(buf);
+        return;
+    }
+    long lo, hi;
+    if (k->pass == 0) {
+        long npair = ((long)n * n + 1) / 2;
+        orc_range(npair, t, nt, &lo, &hi);
+        if (k->q) fft_x_r2c(k, lo, hi, line, work);
+        else fft_x_c2r(k, lo, hi, line, work);
+    } else {
+        orc_range(n, t, nt, &lo, &hi);
+        for (long i = lo; i < hi; ++i) {
+            if (k->pass == 1) fft_columns(n, k->fq + (size_t)i * n * nh, nh, nh, k->sign, buf, work);
+            else fft_columns(n, k->fq + (size_t)i * nh, (size_t)n * nh, nh, k->sign, buf, work);
+        }
+    }
     free(line); free(work); free(buf);
+}
+
+static int fft_pass(fft_task *k, int pass, int sign) {
+    k->pass = pass;
+    k->sign = sign;
+    int nt = orc_threads();
+    if (nt > k->n) nt = k->n;
+    orc_par_run(fft_task_run, k, nt);
+    return k->err ? -1 : 0;
+}
+
+int orc_fft_r2c_3d(int n, const double *q, double *fqd) {
+    (void)get_twiddles(n);   /* fill the table cache before any thread reads it */
+    fft_task k = {n, -1, 0, q, NULL, (cpx *)fqd, 0};
+    /* x: real -> half spectrum, two real lines per complex transform
+       (A + iB; X_A = (Z_k + conj Z_{n-k})/2, X_B = (Z_k - conj Z_{n-k})/2i);
+       then y and z: columns of the half spectrum */
+    if (fft_pass(&k, 0, -1) || fft_pass(&k, 1, -1) || fft_pass(&k, 2, -1)) return -1;
     return 0;
 }
 
@@ -175,36 +247,15 @@ int orc_fft_c2r_3d(int n, const double *fqd, double *q) {
     int nh = n / 2 + 1;
     size_t nc = (size_t)nh * n * n;
     cpx *fq = malloc(sizeof(cpx) * nc);
-    cpx *line = malloc(sizeof(cpx) * n), *work = malloc(sizeof(cpx) * 2 * n);
-    cpx *buf = malloc(sizeof(cpx) * COLBLK * (size_t)n);
-    if (!fq || !line || !work || !buf) { free(fq); free(line); free(work); free(buf); return -1; }
+    if (!fq) return -1;
     memcpy(fq, fqd, sizeof(cpx) * nc);
-    /* z, then y: complex backward */
-    for (int y = 0; y < n; ++y) fft_columns(n, fq + (size_t)y * nh, (size_t)n * nh, nh, +1, buf, work);
-    for (int z = 0; z < n; ++z) fft_columns(n, fq + (size_t)z * n * nh, nh, nh, +1, buf, work);
-    /* x: two Hermitian lines per complex transform, Z = X_A + i X_B over the
-       completed spectra; the imaginary parts of the k = 0 and k = n/2 terms
-       are dropped, as a Hermitian-input c2r does */
-    size_t nl = (size_t)n * n;
-    for (size_t l = 0; l < nl; l += 2) {
-        const cpx *ha = fq + l * nh, *hb = (l + 1 < nl) ? fq + (l + 1) * nh : NULL;
-        for (int k = 0; k < n; ++k) {
-            cpx xa, xb = {0.0, 0.0};
-            int kk = k < nh ? k : n - k;
-            double sg = k < nh ? 1.0 : -1.0;
-            xa.re = ha[kk].re; xa.im = sg * ha[kk].im;
-            if (hb) { xb.re = hb[kk].re; xb.im = sg * hb[kk].im; }
-            if (kk == 0 || 2 * kk == n) { xa.im = 0.0; xb.im = 0.0; }
-            line[k].re = xa.re - xb.im;
-            line[k].im = xa.im + xb.re;
-        }
-        dft_line(n, line, +1, work);
-        double *qa = q + l * n, *qb = hb ? q + (l + 1) * n : NULL;
-        for (int x = 0; x < n; ++x) {
-            qa[x] = line[x].re;
-            if (qb) qb[x] = line[x].im;
-        }
-    }
-    free(fq); free(line); free(work); free(buf);
-    return 0;
+    (void)get_twiddles(n);
+    fft_task k = {n, +1, 0, NULL, q, fq, 0};
+    /* z, then y: complex backward; then x: two Hermitian lines per complex
+       transform, Z = X_A + i X_B over the completed spectra; the imaginary
+       parts of the k = 0 and k = n/2 terms are dropped, as a Hermitian-input
+       c2r does */
+    int st = (fft_pass(&k, 2, +1) || fft_pass(&k, 1, +1) || fft_pass(&k, 0, +1)) ? -1 : 0;
+    free(fq);
+    return st;
 }
