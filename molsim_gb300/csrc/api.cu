@@ -125,6 +125,8 @@ static void free_all(mg_handle *h) {
     }
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->ev_sr) cudaEventDestroy(h->ev_sr);
+    if (h->ev_rec) cudaEventDestroy(h->ev_rec);
     if (h->st2) cudaStreamDestroy(h->st2);
     if (h->st) cudaStreamDestroy(h->st);
 }
@@ -214,6 +216,8 @@ static int create_impl(const mg_params *p, mg_handle *h) {
     MG_CUDA(h, cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
     MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_sr, cudaEventDisableTiming));
+    MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_rec, cudaEventDisableTiming));
     MG_CUDA(h, cudaMalloc(&h->d_ro, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMemset(h->d_ro, 0, sizeof(double) * 3 * np));
     MG_TRY(upload(h, &h->d_az, p->az, np));

@@ -798,6 +798,9 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
     return MG_OK;
 }
 
+static int utotal_reduce(mg_handle *h, bool mixed, bool par);
+static int utotal_epilogue(mg_handle *h, bool mixed, bool par);
+
 // Queue one UTotal on the handle's stream.
 int mg_utotal_launch(mg_handle *h) {
     int np = h->np;
@@ -924,6 +927,7 @@ int mg_utotal_launch(mg_handle *h) {
                                                              h->d_part + h->part_bond);
         h->launches++;
     }
+    if (par) MG_CUDA(h, cudaEventRecord(h->ev_sr, ss));   // the short-range forces are in d_ffx2 / d_force2
     h->chk_queued = false;
     h->cand_queued = false;
     if (par && h->cand_side) {   // the next BD step's candidates (after this step's move)
@@ -942,29 +946,64 @@ int mg_utotal_launch(mg_handle *h) {
         MG_TRY(cst);
         h->chk_queued = true;
     }
-    if (par) MG_CUDA(h, cudaEventRecord(h->ev_join, ss));
     h->launches += 2;
     MG_TRY(mg_phase_end(h, "pair"));
 
+    // forked: the mesh path waits for ev_sr (the short-range forces) before
+    // its gather, which then writes forceo itself when there is no surface
+    // term; it records ev_rec once the reciprocal energy partials are summed,
+    // for the reduction on the second stream
+    bool fused = par && !(h->ewald != MG_EWALD_NONE && h->lsurf);
     h->par_forces = par;
+    h->par_final = fused;
     int spst = MG_OK;
     if (h->ewald == MG_EWALD_SPM) spst = mg_spme_launch(h);
     else if (h->ewald == MG_EWALD_STD) spst = mg_ewald_std_launch(h);
     h->par_forces = false;
-    if (par) MG_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_join, 0));   // join before any return
+    h->par_final = false;
+    if (par && spst == MG_OK) {
+        cudaError_t ce = cudaStreamWaitEvent(ss, h->ev_rec, 0);
+        if (ce == cudaSuccess) {
+            cudaStream_t keep = h->st;
+            h->st = ss;
+            spst = utotal_reduce(h, mixed, par);
+            h->st = keep;
+        } else {
+            spst = mg_fail(h, MG_ERR_CUDA, "stream wait: %s", cudaGetErrorString(ce));
+        }
+    }
+    if (par) {   // join before any return
+        MG_CUDA(h, cudaEventRecord(h->ev_join, ss));
+        MG_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_join, 0));
+    }
     MG_TRY(spst);
+    if (!par) MG_TRY(utotal_reduce(h, mixed, par));
+    else if (!fused) MG_TRY(utotal_epilogue(h, mixed, par));
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
 
+// bonds (unforked), surface sums and the energy reduction, queued on h->st;
+// unforked also the force epilogue
+static int utotal_reduce(mg_handle *h, bool mixed, bool par) {
+    int np = h->np;
+    mg_box box;
+    for (int m = 0; m < 3; ++m) {
+        box.len[m] = h->boxlen[m];
+        box.half[m] = h->boxlen2[m];
+        box.inv[m] = h->boxleni[m];
+    }
     MG_TRY(mg_phase_begin(h, "bond+reduce"));
     if (h->nbond > 0 && !par) {
         if (mixed)
             k_bond<true><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
                                                                h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                               h->d_bond_p, a.box, h->d_force, h->d_ffx,
+                                                               h->d_bond_p, box, h->d_force, h->d_ffx,
                                                                h->d_part + h->part_bond);
         else
             k_bond<false><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
                                                                 h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                                h->d_bond_p, a.box, h->d_force, h->d_ffx,
+                                                                h->d_bond_p, box, h->d_force, h->d_ffx,
                                                                 h->d_part + h->part_bond);
         h->launches++;
     }
@@ -1001,7 +1040,17 @@ int mg_utotal_launch(mg_handle *h) {
     r.rows = h->d_part + h->part_red;
     r.ticket = reinterpret_cast<unsigned *>(h->d_part + 2 * (size_t)h->part_red);
     mg_launch_pdl(k_reduce, r.blk0[4], kRedThreads, 0, h->st, r);
-    double surf_k = h->EpsiFourPi * (2.0 * r.surf_fac);
+    h->launches++;
+    MG_TRY(mg_phase_end(h, "bond+reduce"));
+    if (!par) MG_TRY(utotal_epilogue(h, mixed, par));
+    return MG_OK;
+}
+
+// forceo from the force accumulators (and the surface force), on h->st
+static int utotal_epilogue(mg_handle *h, bool mixed, bool par) {
+    int np = h->np;
+    double surf_fac = 2.0 * 3.1415926535897932 / (3.0 * h->vol);
+    double surf_k = h->EpsiFourPi * (2.0 * surf_fac);
     int lsurf = (h->ewald != MG_EWALD_NONE && h->lsurf) ? 1 : 0;
     if (mixed)
         mg_launch_pdl(k_epilogue<true>, (np + kThreads - 1) / kThreads, kThreads, 0, h->st, (const double *)h->d_force,
@@ -1012,8 +1061,7 @@ int mg_utotal_launch(mg_handle *h) {
         k_epilogue<false><<<(np + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
             h->d_force, par ? h->d_force2 : nullptr, h->d_ffx, nullptr, h->d_az, h->d_uout, h->nptpt + 1, np,
             lsurf, surf_k, h->force_fac, h->d_forceo);
-    h->launches += 2;
-    MG_TRY(mg_phase_end(h, "bond+reduce"));
+    h->launches++;
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }

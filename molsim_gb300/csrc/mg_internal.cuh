@@ -39,6 +39,8 @@ struct mg_handle {
     // form, d_force2 in the FP64 form)
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_sr = nullptr, ev_rec = nullptr;   // short-range forces done; reciprocal partials done
+    bool par_final = false;         // the gather writes forceo (forked, no surface term)
     long long *d_ffx2 = nullptr;
     double *d_force2 = nullptr;
     bool par_forces = false;        // set while a forked UTotal queues its mesh path

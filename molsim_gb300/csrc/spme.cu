@@ -334,6 +334,13 @@ struct SplineArgs {
     int lB, lnb;
     int *count, *rank, *brick;
     int assign;            // gather: the first writer of the force accumulator
+    // gather, forked UTotal without a surface term: forceo = (mesh force +
+    // the short-range accumulator) * fac, as the epilogue would write it
+    int final_;
+    const long long *ffx2;
+    const double *force2;
+    double *forceo;
+    double fac;
 };
 
 // Spline data of every particle, once per call (the only FP64 of the mesh
@@ -698,7 +705,14 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     if (MIXED) {
         long long f0 = mg_f2fx((float)(qk * kx * e0)), f1 = mg_f2fx((float)(qk * ky * e1)),
                   f2 = mg_f2fx((float)(qk * kz * e2));
-        if (a.assign) {   // the short-range forces went to their own accumulator
+        if (a.final_) {   // the epilogue's arithmetic (k_epilogue)
+            double g0 = (double)(f0 + a.ffx2[3 * p + 0]) * MG_FX_INV;
+            double g1 = (double)(f1 + a.ffx2[3 * p + 1]) * MG_FX_INV;
+            double g2 = (double)(f2 + a.ffx2[3 * p + 2]) * MG_FX_INV;
+            a.forceo[3 * p + 0] = g0 * a.fac;
+            a.forceo[3 * p + 1] = g1 * a.fac;
+            a.forceo[3 * p + 2] = g2 * a.fac;
+        } else if (a.assign) {   // the short-range forces went to their own accumulator
             ffx[3 * p + 0] = f0;
             ffx[3 * p + 1] = f1;
             ffx[3 * p + 2] = f2;
@@ -710,7 +724,11 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     } else {
         double f0 = (double)qk * (double)e0 * (double)kx, f1 = (double)qk * (double)e1 * (double)ky,
                f2 = (double)qk * (double)e2 * (double)kz;
-        if (a.assign) {
+        if (a.final_) {   // the epilogue's arithmetic (k_epilogue)
+            a.forceo[3 * p + 0] = __dadd_rn(f0, a.force2[3 * p + 0]) * a.fac;
+            a.forceo[3 * p + 1] = __dadd_rn(f1, a.force2[3 * p + 1]) * a.fac;
+            a.forceo[3 * p + 2] = __dadd_rn(f2, a.force2[3 * p + 2]) * a.fac;
+        } else if (a.assign) {
             force[3 * p + 0] = f0;
             force[3 * p + 1] = f1;
             force[3 * p + 2] = f2;
@@ -1175,6 +1193,7 @@ static int plane_passes(mg_handle *h, float *Q, float2 *F, const float2 *tw, Con
     MG_TRY(mg_phase_end(h, "fft_xy_fwd"));
     MG_TRY(mg_phase_begin(h, "fft_z_conv"));
     mg_launch_pdl(k_slab_conv<float, P>, n, thr, slab_smem<P>(), h->st, F, tw, cv, fnh);
+    if (h->par_forces) MG_CUDA(h, cudaEventRecord(h->ev_rec, h->st));   // reciprocal partials complete
     MG_TRY(mg_phase_end(h, "fft_z_conv"));
     MG_TRY(mg_phase_begin(h, "fft_yx_inv"));
     mg_launch_pdl(k_plane_inv<float, P>, n, thr, plane_smem<P>(h->fft_warps), h->st, (const float2 *)F, Q, tw, fnh);
@@ -1226,6 +1245,7 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_
     MG_TRY(mg_phase_end(h, "fft_y_fwd"));
     MG_TRY(mg_phase_begin(h, "fft_z_conv"));
     k_fft_col<T, true><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, zstride, zother, -1, tw, cv, ftx);
+    if (h->par_forces) MG_CUDA(h, cudaEventRecord(h->ev_rec, h->st));   // reciprocal partials complete
     MG_TRY(mg_phase_end(h, "fft_z_conv"));
     MG_TRY(mg_phase_begin(h, "fft_y_inv"));
     k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, +1, tw, cv, ftx);
@@ -1460,6 +1480,11 @@ static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
     sa.rank = h->d_brick_rank;
     sa.brick = h->d_brick_of;
     sa.assign = h->par_forces ? 1 : 0;
+    sa.final_ = h->par_final ? 1 : 0;
+    sa.ffx2 = h->d_ffx2;
+    sa.force2 = h->d_force2;
+    sa.forceo = h->d_forceo;
+    sa.fac = h->force_fac;
     bk.n = n;
     bk.B = h->brick;
     bk.nb = h->nbrick_edge;
@@ -1605,6 +1630,7 @@ int mg_spme_launch(mg_handle *h) {
         h->launches++;
     }
     MG_TRY(mg_spme_potential(h));
+    if (h->par_forces) MG_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_sr, 0));   // the short-range forces
     MG_TRY(mg_phase_begin(h, "gather"));
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 2, sa, bk)));
     else MG_TRY((mesh_kernel<double, long long>(h, 2, sa, bk)));
