@@ -31,6 +31,11 @@ int mg_check_device_error(mg_handle *h) {
     MG_CUDA(h, cudaStreamSynchronize(h->st));
     int e[4];
     MG_CUDA(h, cudaMemcpy(e, h->d_err, sizeof(e), cudaMemcpyDeviceToHost));
+    return mg_device_error_status(h, e);
+}
+
+// the status of a device error word read to the host (and the word cleared)
+int mg_device_error_status(mg_handle *h, const int *e) {
     mg_phase_collect(h);
     if (e[0] == 0) return MG_OK;
     int zero[4] = {0, 0, 0, 0};
@@ -117,6 +122,7 @@ static void free_all(mg_handle *h) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
+    if (h->h_stage) cudaFreeHost(h->h_stage);
     if (h->g_bd) cudaGraphExecDestroy(h->g_bd);
     if (h->g_md) cudaGraphExecDestroy(h->g_md);
     for (auto &p : h->phases) {
@@ -214,6 +220,7 @@ static int create_impl(const mg_params *p, mg_handle *h) {
 
     MG_CUDA(h, cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     MG_CUDA(h, cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
+    MG_CUDA(h, cudaMallocHost(&h->h_stage, sizeof(double) * kStageDoubles));
     MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     MG_CUDA(h, cudaEventCreateWithFlags(&h->ev_sr, cudaEventDisableTiming));

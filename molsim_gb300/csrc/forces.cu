@@ -1066,14 +1066,20 @@ static int utotal_epilogue(mg_handle *h, bool mixed, bool par) {
     return MG_OK;
 }
 
+// energies and forces to the host: the copies and the device error word are
+// queued together behind the step, and the host waits once
 int mg_utotal_fetch(mg_handle *h, double *forceo, double *u_twob, double *uout) {
     int n = h->nptpt + 1 + 4;
-    std::vector<double> u(n);
-    MG_CUDA(h, cudaMemcpyAsync(u.data(), h->d_uout, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    double *u = h->h_stage;
+    int *err = reinterpret_cast<int *>(h->h_stage + n);
+    MG_CUDA(h, cudaMemcpyAsync(u, h->d_uout, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
     if (forceo)
         MG_CUDA(h, cudaMemcpyAsync(forceo, h->d_forceo, sizeof(double) * 3 * h->np,
                                    cudaMemcpyDeviceToHost, h->st));
-    MG_TRY(mg_check_device_error(h));
+    MG_CUDA(h, cudaMemcpyAsync(err, h->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->st));
+    MG_CUDA(h, cudaStreamSynchronize(h->st));
+    int e[4] = {err[0], err[1], err[2], err[3]};
+    MG_TRY(mg_device_error_status(h, e));
     if (u_twob)
         for (int k = 0; k <= h->nptpt; ++k) u_twob[k] = u[k];
     if (uout)

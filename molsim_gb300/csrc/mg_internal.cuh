@@ -101,6 +101,7 @@ struct mg_handle {
     double *d_uout = nullptr;      // [nptpt+1] u_twob, then u_tot,u_rec,u_bond,virial, then surf sums (3)
     int *d_err = nullptr;          // [4] code, info1, info2, info3
     double *h_pinned = nullptr;    // pinned staging for outputs
+    double *h_stage = nullptr;     // pinned: the energies of a fetch, then the device error word
     size_t h_pinned_bytes = 0;
 
     // ---- bonds -----------------------------------------------------------
@@ -367,6 +368,8 @@ int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, cons
                           const double *rodd);
 
 int mg_check_device_error(mg_handle *h);               // sync + read the device error word
+int mg_device_error_status(mg_handle *h, const int *e);  // status of an error word already read
+constexpr int kStageDoubles = MG_MAX_NPTPT + 1 + 8 + 2;  // energies (nptpt + 1 + 4) and the error word
 
 // host set-up (host_setup.cu)
 int mg_host_table(const mg_pot_params *pp, double *ubuf, int32_t nbuf_cap, int32_t *nbuf_used,
