@@ -124,6 +124,8 @@ static void free_all(mg_handle *h) {
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
     if (h->h_stage) cudaFreeHost(h->h_stage);
     if (h->g_bd) cudaGraphExecDestroy(h->g_bd);
+    if (h->g_bd_io) cudaGraphExecDestroy(h->g_bd_io);
+    if (h->d_hostio) cudaFree(h->d_hostio);
     if (h->g_md) cudaGraphExecDestroy(h->g_md);
     for (auto &p : h->phases) {
         cudaEventDestroy(p.e0);
@@ -485,19 +487,21 @@ static int count_kernels(cudaGraph_t graph) {
     return nk;
 }
 
-static int capture_step(mg_handle *h, bool bd) {
-    cudaGraphExec_t &g = bd ? h->g_bd : h->g_md;
+static int capture_step(mg_handle *h, bool bd, bool io = false) {
+    cudaGraphExec_t &g = io ? h->g_bd_io : bd ? h->g_bd : h->g_md;
     if (g) return MG_OK;
     cudaGraph_t graph = nullptr;
     MG_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    h->hostio = io;
     int st = capture_step_body(h, bd);
+    h->hostio = false;
     cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
     if (st != MG_OK || ce != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         if (st != MG_OK) return st;
         return mg_fail(h, MG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
     }
-    (bd ? h->kernels_bd : h->kernels_md) = count_kernels(graph);
+    if (!io) (bd ? h->kernels_bd : h->kernels_md) = count_kernels(graph);
     ce = cudaGraphInstantiate(&g, graph, 0);
     cudaGraphDestroy(graph);
     if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
@@ -551,9 +555,37 @@ int mg_bd_run(mg_handle *h, int32_t nstep, double *forceo, double *uout) {
     return mg_utotal_fetch(h, forceo, nullptr, uout);
 }
 
+// true when the device can read and write p in place (pinned host memory
+// mapped into the device address space, the pointer valid on the device)
+static bool device_mapped_host(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost && at.devicePointer == p;
+}
+
 int mg_bd_step_host(mg_handle *h, double *ro_io, double *forceo, double *uout) {
     if (!h || !ro_io) return MG_ERR_ARG;
     if (!h->bd_ready || !h->list_valid) return mg_fail(h, MG_ERR_STATE, "BD not set up");
+    // pinned, mapped buffers: the step's kernels read and write them in place
+    // (positions in the move kernel, forces in the step's last kernel)
+    bool cached = h->hostio_last.ro == ro_io && h->hostio_last.forceo == forceo;   // checked before
+    if (!h->timing && h->have_force && forceo &&
+        (cached || (device_mapped_host(ro_io) && device_mapped_host(forceo) && device_mapped_host(h->h_stage)))) {
+        if (!h->d_hostio) MG_CUDA(h, cudaMalloc(&h->d_hostio, sizeof(mg_hostio)));
+        if (h->hostio_last.ro != ro_io || h->hostio_last.forceo != forceo) {
+            mg_hostio io = {ro_io, forceo, h->h_stage, h->d_uout, h->d_err, h->nptpt + 1 + 4};
+            MG_CUDA(h, cudaMemcpy(h->d_hostio, &io, sizeof(io), cudaMemcpyHostToDevice));
+            h->hostio_last = io;
+        }
+        MG_TRY(capture_step(h, true, true));
+        MG_TRY(mg_integrate_bd_prime(h));
+        MG_CUDA(h, cudaGraphLaunch(h->g_bd_io, h->st));
+        MG_CUDA(h, cudaStreamSynchronize(h->st));
+        return mg_utotal_staged(h, nullptr, uout);
+    }
     MG_CUDA(h, cudaMemcpyAsync(h->d_ro, ro_io, sizeof(double) * 3 * h->np, cudaMemcpyHostToDevice, h->st));
     if (!h->have_force) {
         MG_TRY(mg_utotal_launch(h));

@@ -1078,6 +1078,14 @@ int mg_utotal_fetch(mg_handle *h, double *forceo, double *u_twob, double *uout) 
                                    cudaMemcpyDeviceToHost, h->st));
     MG_CUDA(h, cudaMemcpyAsync(err, h->d_err, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->st));
     MG_CUDA(h, cudaStreamSynchronize(h->st));
+    return mg_utotal_staged(h, u_twob, uout);
+}
+
+// the energies and the device error word already in h_stage
+int mg_utotal_staged(mg_handle *h, double *u_twob, double *uout) {
+    int n = h->nptpt + 1 + 4;
+    const double *u = h->h_stage;
+    const int *err = reinterpret_cast<const int *>(h->h_stage + n);
     int e[4] = {err[0], err[1], err[2], err[3]};
     MG_TRY(mg_device_error_status(h, e));
     if (u_twob)

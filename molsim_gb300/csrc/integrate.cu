@@ -106,6 +106,7 @@ struct BdArgs {
     mg_box box;
     int *err;
     mg_chk_args chk;        // the list check's first pass runs here
+    const mg_hostio *io;    // host positions in and out (nullptr: device only)
 };
 
 // prefix of the per-block accepted counts in shared memory (inclusive): all
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(kChkThreads) k_bd_move(BdArgs a) {
     int off = (a.rng[1] == 0) ? 1 : 0;   // a saved deviate is pending
     bool reset = (*a.chk.flag != 0);
     double dd[3] = {0.0, 0.0, 0.0};
+    double *hro = a.io ? a.io->ro : nullptr;   // host positions, read then written
     if (p < a.np) {
         int t = a.type[p];
         double f1 = a.fac1[t], f2 = a.fac2[t];
@@ -190,8 +192,10 @@ __global__ void __launch_bounds__(kChkThreads) k_bd_move(BdArgs a) {
             double d = __dadd_rn(__dmul_rn(f1, a.forceo[3 * p + m]), __dmul_rn(f2, dev));
             a.drostep[3 * p + m] = d;
             dd[m] = d;
-            double r = __dadd_rn(a.ro[3 * p + m], d);
-            a.ro[3 * p + m] = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
+            double r = __dadd_rn(hro ? hro[3 * p + m] : a.ro[3 * p + m], d);
+            r = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
+            a.ro[3 * p + m] = r;
+            if (hro) hro[3 * p + m] = r;
         }
     }
     mg_chk_accum(p, a.np, dd[0], dd[1], dd[2], reset, a.chk.drosum, a.chk.r2out, a.chk.blkmax);
@@ -216,6 +220,17 @@ __global__ void __launch_bounds__(kChkThreads) k_bd_move(BdArgs a) {
         a.rng[1] = 0;
     } else {
         a.rng[1] = 1;
+    }
+}
+
+// the step's results to the host buffers of a host-I/O step: forceo
+// (coalesced writes), the energies and the device error word
+__global__ void k_forces_to_host(const double *__restrict__ forceo, const mg_hostio *io, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) io->forceo[i] = forceo[i];
+    if (blockIdx.x == 0) {
+        if (threadIdx.x < io->nu) io->stage[threadIdx.x] = io->uout[threadIdx.x];
+        if (threadIdx.x < 4) reinterpret_cast<int *>(io->stage + io->nu)[threadIdx.x] = io->err[threadIdx.x];
     }
 }
 
@@ -362,6 +377,7 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     a.box = box_of(h);
     a.err = h->d_err;
     a.chk = mg_lists_chk_args(h);
+    a.io = h->hostio ? h->d_hostio : nullptr;
     size_t sm = sizeof(int) * nblk;
     if (!prefetch) {
         MG_TRY(mg_phase_begin(h, "bd_rng"));
@@ -381,6 +397,10 @@ int mg_integrate_bd_step_launch(mg_handle *h) {
     if (prefetch && !h->cand_queued) MG_TRY(mg_integrate_bd_cand(h));   // UTotal did not fork
     h->cand_queued = false;
     if (!prefetch) h->cand_ready = false;   // consumed, none drawn ahead
+    if (h->hostio) {   // the forces straight into the host buffer
+        k_forces_to_host<<<(3 * np + 255) / 256, 256, 0, h->st>>>(h->d_forceo, h->d_hostio, 3 * np);
+        h->launches++;
+    }
     MG_TRY(list_step(h, true));
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;

@@ -31,6 +31,17 @@ struct mg_phase {
     bool pending = false;
 };
 
+// host buffers that a step reads and writes directly (pinned, mapped into
+// the device address space): positions in and out, forces out
+struct mg_hostio {
+    double *ro;      // 3 np: read before the move, written after it
+    double *forceo;  // 3 np: written at the end of the step
+    double *stage;   // the energies (nu values) and then the device error word
+    const double *uout;
+    const int *err;
+    int nu;
+};
+
 struct mg_handle {
     int dev = 0;
     cudaStream_t st = nullptr;
@@ -187,6 +198,13 @@ struct mg_handle {
 
     // ---- graphs and timing -----------------------------------------------------
     cudaGraphExec_t g_bd = nullptr, g_md = nullptr;
+    // mg_bd_step_host with pinned (device-mapped) host buffers: a second BD
+    // graph whose move kernel reads and writes the host positions and whose
+    // last kernel writes the host forces; the pointers live in d_hostio
+    cudaGraphExec_t g_bd_io = nullptr;
+    mg_hostio *d_hostio = nullptr;
+    mg_hostio hostio_last = {nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    bool hostio = false;            // set while the host-I/O graph is captured
     // while a step is captured, the list check sets a graph condition that
     // runs the (otherwise skipped) rebuild body
     bool use_cond = false;
@@ -369,6 +387,7 @@ int mg_integrate_md_setup(mg_handle *h, double tstep, const double *massip, cons
 
 int mg_check_device_error(mg_handle *h);               // sync + read the device error word
 int mg_device_error_status(mg_handle *h, const int *e);  // status of an error word already read
+int mg_utotal_staged(mg_handle *h, double *u_twob, double *uout);   // energies and status from h_stage (after a sync)
 constexpr int kStageDoubles = MG_MAX_NPTPT + 1 + 8 + 2;  // energies (nptpt + 1 + 4) and the error word
 
 // host set-up (host_setup.cu)

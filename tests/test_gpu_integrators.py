@@ -5,6 +5,8 @@ GauRandom stream (mollib.F90:2739-2766) in parallel, so after n steps the
 LCG seed must be identical and positions equal to rounding.  MD (VelVer,
 md.F90:252-420): positions, velocities and energies after n steps.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -86,3 +88,47 @@ def test_md_rebuilds_match(orc, gpu_lib):
     nr, lr = ref.VList()
     ng, lg = gpu.VList()
     assert [sorted(x.tolist()) for x in lr] == [sorted(x.tolist()) for x in lg]
+
+
+@pytest.mark.parametrize("form", [abi.MG_MIXED, abi.MG_FP64])
+def test_bd_step_host_pinned_buffers_match_copies(form, orc, gpu_lib):
+    """mg_bd_step_host with pinned host buffers runs the step graph whose
+    kernels read and write those buffers in place; with pageable buffers it
+    copies.  Both give the same positions, forces and energies, bit for bit,
+    as steps of mg_bd_run."""
+    torch = pytest.importorskip("torch")
+    s = prepared(configs.small_system(seed=54, n=400, L=40.0, mode=abi.MG_BD, chains=2, nseg=10), orc)
+    lib = abi.load_library()
+    n3 = 3 * s.np_
+    runs = []
+    for kind in ("pinned", "pageable", "run"):
+        e = Engine(s, form=form)
+        e.SetPositions(s.ro_flat())
+        e.NList("write")
+        e.BDSetup(0.01, 2468)
+        e.BDRun(0)   # initial forces
+        if kind == "run":
+            out = e.BDRun(4)
+            runs.append((e.GetPositions().reshape(-1), out["forceo"].reshape(-1), out["u_tot"]))
+            e.close()
+            continue
+        if kind == "pinned":
+            ro = torch.from_numpy(e.GetPositions().reshape(-1).copy()).pin_memory()
+            f = torch.zeros(n3, dtype=torch.float64).pin_memory()
+            p_ro, p_f = C.cast(ro.data_ptr(), abi.PF64), C.cast(f.data_ptr(), abi.PF64)
+        else:
+            ro_np = e.GetPositions().reshape(-1).copy()
+            f_np = np.zeros(n3)
+            p_ro, p_f = abi.f64(ro_np), abi.f64(f_np)
+        u = np.zeros(4)
+        for _ in range(4):
+            assert lib.mg_bd_step_host(e.h, p_ro, p_f, abi.f64(u)) == 0
+        if kind == "pinned":
+            runs.append((ro.numpy().copy(), f.numpy().copy(), u[0]))
+        else:
+            runs.append((ro_np.copy(), f_np.copy(), u[0]))
+        e.close()
+    (r0, f0, u0), (r1, f1, u1), (r2, f2, u2) = runs
+    assert np.array_equal(r0, r1) and np.array_equal(r0, r2)
+    assert np.array_equal(f0, f1) and np.array_equal(f0, f2)
+    assert u0 == u1 == u2
