@@ -860,9 +860,18 @@ __device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >
 
 // in-place P-point DFT in registers (natural order in and out): iterative
 // radix-2 with the bit reversal as compile-time register renaming
+// times -i (forward quarter turn) or +i (backward)
+template <typename T, bool INV> __device__ __forceinline__ V2<T> quarter(V2<T> t) {
+    V2<T> r;
+    if (INV) { r.x = -t.y; r.y = t.x; }
+    else { r.x = t.y; r.y = -t.x; }
+    return r;
+}
+
 template <typename T, int P, bool INV>
-__device__ __forceinline__ void reg_dft(V2<T> *v, const V2<T> *tw, int n) {
+__device__ __forceinline__ void reg_dft(V2<T> *v, const V2<T> *tw, int) {
     typedef V2<T> V;
+    constexpr int n = 32 * P;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
         int r = 0;
@@ -878,7 +887,9 @@ __device__ __forceinline__ void reg_dft(V2<T> *v, const V2<T> *tw, int n) {
 #pragma unroll
             for (int e = 0; e < half; ++e) {
                 V u = v[i + e], t = v[i + e + half];
-                if (e) {
+                if (e && 4 * e == len) {   // w_n^(n/4): a quarter turn
+                    t = quarter<T, INV>(t);
+                } else if (e) {
                     V w = tw[e * (n / len)];
                     t = cmul(t, INV ? conj_c<T>(w) : w);
                 }
@@ -915,15 +926,26 @@ __device__ __forceinline__ void warp_fft_fwd(V2<T> *v, const V2<T> *tw, const V2
     for (int k1 = 1; k1 < P; ++k1) v[k1] = cmul(v[k1], tk[32 * (k1 - 1) + lane]);
 #pragma unroll
     for (int h = 16; h > 0; h >>= 1) {
-        V2<T> w = tl[h - 1 + (lane & (h - 1))];
         const T s = (lane & h) ? (T)-1 : (T)1;   // lower lane: a + b, upper lane: (a - b) w
-        if (!(lane & h)) { w.x = (T)1; w.y = (T)0; }
+        if (h >= 4) {
+            V2<T> w = tl[h - 1 + (lane & (h - 1))];
+            if (!(lane & h)) { w.x = (T)1; w.y = (T)0; }
 #pragma unroll
-        for (int k1 = 0; k1 < P; ++k1) {
-            V2<T> p = shfl_xor_c<T>(v[k1], h), t;
-            t.x = p.x + s * v[k1].x;
-            t.y = p.y + s * v[k1].y;
-            v[k1] = cmul(t, w);
+            for (int k1 = 0; k1 < P; ++k1) {
+                V2<T> p = shfl_xor_c<T>(v[k1], h), t;
+                t.x = p.x + s * v[k1].x;
+                t.y = p.y + s * v[k1].y;
+                v[k1] = cmul(t, w);
+            }
+        } else {   // h = 2: w = 1 or -i (upper lanes with e = 1); h = 1: w = 1
+            const bool rot = (h == 2) && (lane & 3) == 3;
+#pragma unroll
+            for (int k1 = 0; k1 < P; ++k1) {
+                V2<T> p = shfl_xor_c<T>(v[k1], h), t;
+                t.x = p.x + s * v[k1].x;
+                t.y = p.y + s * v[k1].y;
+                v[k1] = rot ? quarter<T, false>(t) : t;
+            }
         }
     }
 }
@@ -934,13 +956,20 @@ __device__ __forceinline__ void warp_fft_inv(V2<T> *v, const V2<T> *tw, const V2
     constexpr int n = 32 * P;
 #pragma unroll
     for (int h = 1; h <= 16; h <<= 1) {
-        const V2<T> w = conj_c<T>(tl[h - 1 + (lane & (h - 1))]);
         const bool up = lane & h;   // lower lane: a + w b, upper lane: a - w b
+        const T s = up ? (T)-1 : (T)1;
+        // h = 1: w = 1; h = 2: w = 1 or +i (e = 1)
+        const bool rot = (h == 2) && (lane & 1);
+        V2<T> w;
+        if (h >= 4) w = conj_c<T>(tl[h - 1 + (lane & (h - 1))]);
 #pragma unroll
         for (int k1 = 0; k1 < P; ++k1) {
             V2<T> p = shfl_xor_c<T>(v[k1], h);
-            V2<T> b = cmul(up ? v[k1] : p, w), a = up ? p : v[k1];
-            v[k1] = up ? csub(a, b) : cadd(a, b);
+            V2<T> a = up ? p : v[k1], b = up ? v[k1] : p;
+            if (h >= 4) b = cmul(b, w);
+            else if (h == 2) b = rot ? quarter<T, true>(b) : b;
+            v[k1].x = a.x + s * b.x;
+            v[k1].y = a.y + s * b.y;
         }
     }
 #pragma unroll
