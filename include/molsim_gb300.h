@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define MG_ABI_VERSION 1
+#define MG_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 #define MG_OK                   0
@@ -101,6 +101,17 @@ typedef struct mg_params {
     const double  *bond_k;    /* [nbond]                                        */
     const double  *bond_eq;   /* [nbond]                                        */
     const int32_t *bond_p;    /* [nbond] integer power                          */
+
+    /* chain angles (UAngle, energy.F90:5409): u = k*(theta-eq)**p per angle
+       jm-ip-jp, theta the angle at ip; in the reference's order (chains,
+       then segments 2..npct-1).  No contribution to the virial. */
+    int32_t nangle;
+    const int32_t *angle_jm;  /* [nangle] previous segment, 1-based             */
+    const int32_t *angle_ip;  /* [nangle] vertex, 1-based                       */
+    const int32_t *angle_jp;  /* [nangle] next segment, 1-based                 */
+    const double  *angle_k;   /* [nangle]                                       */
+    const double  *angle_eq;  /* [nangle] radians                               */
+    const int32_t *angle_p;   /* [nangle] integer power                         */
 } mg_params;
 
 /* Parameters of the (1,6,12) potential table (Pot_1_6_12, potential.F90:1349). */
@@ -182,11 +193,16 @@ int mg_celllist_get(mg_handle *h, int32_t *ncell, int32_t *cellip);
 
 /* UTotal (energy.F90:280-430) for a charged monoatomic system: two-body
  * (UTwoBodyA / UTwoBodyACellList), Ewald (UEwaldRecStd or UEwaldRecSPM,
- * UEwaldSelf, UEwaldSurf), UBond and the force epilogue.
+ * UEwaldSelf, UEwaldSurf), UBond, UAngle and the force epilogue.
  *   forceo  [3*np]  forces scaled by force_fac (may be NULL)
  *   u_twob  [nptpt+1] u%twob(0:nptpt)            (may be NULL)
  *   uout    [4]  u%tot, u%rec, u%bond, virial    (may be NULL)          */
 int mg_utotal(mg_handle *h, double *forceo, double *u_twob, double *uout);
+
+/* The energy terms of the last UTotal (or step) of this handle:
+ *   terms [6]  u%tot, u%twob(0), u%rec, u%bond, u%angle, virial
+ * (UTotal's sums, energy.F90:280-337; u%angle from UAngle, energy.F90:5409). */
+int mg_energy_terms(mg_handle *h, double *terms);
 
 /* ---- Monte Carlo trial moves (A13, A14) ------------------------------------ */
 

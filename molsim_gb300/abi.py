@@ -8,7 +8,7 @@ import os
 
 import numpy as np
 
-MG_ABI_VERSION = 1
+MG_ABI_VERSION = 2
 
 MG_OK = 0
 STATUS = {
@@ -38,6 +38,8 @@ class MgParams(C.Structure):
         ("lsurf", C.c_int32), ("epsi_four_pi", C.c_double), ("force_fac", C.c_double),
         ("nbond", C.c_int32), ("bond_ip", PI32), ("bond_jp", PI32), ("bond_k", PF64),
         ("bond_eq", PF64), ("bond_p", PI32),
+        ("nangle", C.c_int32), ("angle_jm", PI32), ("angle_ip", PI32), ("angle_jp", PI32),
+        ("angle_k", PF64), ("angle_eq", PF64), ("angle_p", PI32),
     ]
 
 
@@ -63,6 +65,7 @@ SIGNATURES = [
     ("nlist_get", C.c_int, [H, PI32, PI32, C.c_int32]),
     ("celllist_get", C.c_int, [H, PI32, PI32]),
     ("utotal", C.c_int, [H, PF64, PF64, PF64]),
+    ("energy_terms", C.c_int, [H, PF64]),
     ("dutotal", C.c_int, [H, C.c_int32, PI32, PF64, PF64, PF64, PF64, PI32]),
     ("accept", C.c_int, [H]),
     ("md_setup", C.c_int, [H, C.c_double, PF64, PF64, PF64]),

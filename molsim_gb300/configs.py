@@ -209,8 +209,10 @@ def polyelectrolyte(seed=3, nchain=64, nseg=200, nsalt=20000, L=700.0, nmesh=128
 
 def small_system(seed=7, n=400, L=40.0, ewald=abi.MG_EWALD_SPM, nmesh=16, order=6, ncut=6,
                  rcut=9.0, drnlist=1.5, txintlist=abi.MG_VLIST, mode=abi.MG_MD, lsurf=0,
-                 chains=0, nseg=10, eps_kt=0.1, rmin=3.0, lljcut=0):
-    """A small charged LJ system (three species) for parity tests."""
+                 chains=0, nseg=10, eps_kt=0.1, rmin=3.0, lljcut=0, angle_kt=0.0, angle_eq=2.5, angle_p=2):
+    """A small charged LJ system (three species) for parity tests; chains of
+    nseg beads with harmonic bonds and, when angle_kt > 0, angle potentials
+    k*(theta - angle_eq)**angle_p at every interior bead (UAngle's order)."""
     T = 298.0
     kt = units.kT(T)
     sp = [Species("A", +1.0, 3.5, eps_kt * kt, mass=23.0),
@@ -218,7 +220,7 @@ def small_system(seed=7, n=400, L=40.0, ewald=abi.MG_EWALD_SPM, nmesh=16, order=
           Species("C", +2.0, 4.5, 2 * eps_kt * kt, mass=40.0)]
     rng = np.random.Generator(np.random.PCG64(seed))
     grid = _Grid([L, L, L], rmin)
-    pos, types, bip, bjp = [], [], [], []
+    pos, types, bip, bjp, ajm = [], [], [], [], []
     for _c in range(chains):
         chain = place_chain(rng, grid, nseg, 4.5)
         base = len(pos)
@@ -226,6 +228,7 @@ def small_system(seed=7, n=400, L=40.0, ewald=abi.MG_EWALD_SPM, nmesh=16, order=
         types += [2] * nseg
         bip += [base + i + 1 for i in range(nseg - 1)]
         bjp += [base + i + 2 for i in range(nseg - 1)]
+        ajm += [base + i + 1 for i in range(nseg - 2)]   # angle (i+1, i+2, i+3), 1-based
     nrest = n - len(pos)
     nC = nrest // 10
     nB_ions = (nrest - nC) // 2
@@ -245,6 +248,11 @@ def small_system(seed=7, n=400, L=40.0, ewald=abi.MG_EWALD_SPM, nmesh=16, order=
         kw = dict(bond_ip=np.array(bip, dtype=np.int32), bond_jp=np.array(bjp, dtype=np.int32),
                   bond_k=np.full(nb, 0.3 * kt), bond_eq=np.full(nb, 4.5),
                   bond_p=np.full(nb, 2, dtype=np.int32))
+    if angle_kt > 0 and ajm:
+        jm = np.array(ajm, dtype=np.int32)
+        na = len(jm)
+        kw.update(angle_jm=jm, angle_ip=jm + 1, angle_jp=jm + 2, angle_k=np.full(na, angle_kt * kt),
+                  angle_eq=np.full(na, angle_eq), angle_p=np.full(na, angle_p, dtype=np.int32))
     return System(species=sp, iptpn=types, ro=ro, boxlen=np.array([L, L, L]), temp=T,
                   relpermitt=units.relpermitt_from_bjerrum(7.1, T), rcut=rcut, drnlist=drnlist,
                   txintlist=txintlist, mode=mode, ewald=ewald, ualpha=alpha_for_erfc(1e-5, rcut),

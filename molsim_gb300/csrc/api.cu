@@ -110,7 +110,8 @@ static void free_all(mg_handle *h) {
                     h->d_pos_s, h->d_iphead, h->d_npart, h->d_ipnext, h->d_ipprev, h->d_neighcells,
                     h->d_nneighcell, h->d_force, h->d_forceo, h->d_ffx, h->d_part, h->d_uout, h->d_err,
                     h->d_bond_ij, h->d_bond_p, h->d_bond_k, h->d_bond_eq, h->d_bond_off,
-                    h->d_bond_list, h->d_kvec, h->d_kfac, h->d_eik, h->d_S, h->d_Stm, h->d_Q, h->d_F,
+                    h->d_bond_list, h->d_angle_ijk, h->d_angle_p, h->d_angle_off, h->d_angle_list, h->d_angle_k,
+                    h->d_angle_eq, h->d_kvec, h->d_kfac, h->d_eik, h->d_S, h->d_Stm, h->d_Q, h->d_F,
                     h->d_Qfx, h->d_mf, h->d_ew, h->d_vw, h->d_mf_f, h->d_ew_f, h->d_vw_f, h->d_tw,
                     h->d_Qref, h->d_phi, h->d_gker, h->d_ipnptm, h->d_rotm, h->d_du, h->d_drostep,
                     h->d_drosum, h->d_blkmax, h->d_rebuild, h->d_massip, h->d_rod, h->d_rodd,
@@ -269,6 +270,35 @@ static int create_impl(const mg_params *p, mg_handle *h) {
         MG_TRY(upload(h, &h->d_bond_list, list.data(), list.size()));
     }
 
+    // angles: triples (0-based) and per-particle CSR of (angle, role)
+    h->nangle = p->nangle;
+    if (p->nangle > 0) {
+        if (!p->angle_jm || !p->angle_ip || !p->angle_jp || !p->angle_k || !p->angle_eq || !p->angle_p)
+            return mg_fail(h, MG_ERR_ARG, "missing angle arrays");
+        int na = p->nangle;
+        std::vector<int> ijk(3 * na), deg(np + 1, 0), off(np + 1, 0), list(3 * na);
+        for (int a = 0; a < na; ++a) {
+            int t[3] = {p->angle_jm[a] - 1, p->angle_ip[a] - 1, p->angle_jp[a] - 1};
+            for (int r = 0; r < 3; ++r) {
+                if (t[r] < 0 || t[r] >= np) return mg_fail(h, MG_ERR_ARG, "angle %d", a + 1);
+                ijk[3 * a + r] = t[r];
+                deg[t[r]]++;
+            }
+            if (t[0] == t[1] || t[1] == t[2] || t[0] == t[2]) return mg_fail(h, MG_ERR_ARG, "angle %d", a + 1);
+            if (p->angle_p[a] < 1) return mg_fail(h, MG_ERR_ARG, "angle power %d", p->angle_p[a]);
+        }
+        for (int i = 0; i < np; ++i) off[i + 1] = off[i] + deg[i];
+        std::vector<int> fill(off.begin(), off.end() - 1);
+        for (int a = 0; a < na; ++a)
+            for (int r = 0; r < 3; ++r) list[fill[ijk[3 * a + r]]++] = 4 * a + r;
+        MG_TRY(upload(h, &h->d_angle_ijk, ijk.data(), ijk.size()));
+        MG_TRY(upload(h, &h->d_angle_p, p->angle_p, na));
+        MG_TRY(upload(h, &h->d_angle_k, p->angle_k, na));
+        MG_TRY(upload(h, &h->d_angle_eq, p->angle_eq, na));
+        MG_TRY(upload(h, &h->d_angle_off, off.data(), off.size()));
+        MG_TRY(upload(h, &h->d_angle_list, list.data(), list.size()));
+    }
+
     if (h->ewald == MG_EWALD_SPM) MG_TRY(mg_spme_init(h));
     else if (h->ewald == MG_EWALD_STD) MG_TRY(mg_ewald_std_init(h));
     else if (h->ewald != MG_EWALD_NONE) return mg_fail(h, MG_ERR_ARG, "ewald = %d", h->ewald);
@@ -383,6 +413,22 @@ int mg_nlist_get(mg_handle *h, int32_t *nneighpn, int32_t *jpnlist, int32_t maxn
 int mg_celllist_get(mg_handle *h, int32_t *ncell, int32_t *cellip) {
     if (!h || !ncell || !cellip) return MG_ERR_ARG;
     return mg_cells_export(h, ncell, cellip);
+}
+
+int mg_energy_terms(mg_handle *h, double *terms) {
+    if (!h || !terms) return MG_ERR_ARG;
+    int n = h->nptpt + 1 + 8;
+    std::vector<double> u(n);
+    MG_CUDA(h, cudaStreamSynchronize(h->st));
+    MG_CUDA(h, cudaMemcpy(u.data(), h->d_uout, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    int o = h->nptpt + 1;
+    terms[0] = u[o + 0];   // u%tot
+    terms[1] = u[0];       // u%twob(0)
+    terms[2] = u[o + 1];   // u%rec
+    terms[3] = u[o + 2];   // u%bond
+    terms[4] = u[o + 7];   // u%angle
+    terms[5] = u[o + 3];   // virial
+    return MG_OK;
 }
 
 int mg_utotal(mg_handle *h, double *forceo, double *u_twob, double *uout) {

@@ -432,54 +432,156 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_f32(PairArgsF a) {
 
 // UBond: every particle adds the forces of its (at most a few) bonds; the
 // bond's first particle counts its energy and virial.
+struct BondArgs {
+    const double *ro;
+    int np;
+    // bonds: per-particle CSR (bond*2 + role), pairs, parameters
+    const int *off, *list, *ij;
+    const double *bk, *beq;
+    const int *bp;
+    // angles: per-particle CSR (angle*4 + role: 0 jm, 1 ip, 2 jp), triples, parameters
+    const int *aoff, *alist, *aijk;
+    const double *ak, *aeq;
+    const int *ap;
+    int nangle;
+    mg_box box;
+    double *force;
+    long long *ffx;
+    double *part;   // per block: u%bond, bond virial, u%angle
+};
+
+// x**n as the oracle's powi (gfortran's expansion of an integer power)
+__device__ __forceinline__ double powi_d(double x, int n) {
+    switch (n) {
+    case 0: return 1.0;
+    case 1: return x;
+    case 2: return __dmul_rn(x, x);
+    case 3: return __dmul_rn(__dmul_rn(x, x), x);
+    case 4: { double x2 = __dmul_rn(x, x); return __dmul_rn(x2, x2); }
+    default: { double r = 1.0; for (int i = 0; i < n; ++i) r = __dmul_rn(r, x); return r; }
+    }
+}
+
+// PBC (molaux.F90:104-146, box): d - L*anint(d/L) when |d| > L/2
+__device__ __forceinline__ double pbc_anint(double d, double half, double len, double inv) {
+    if (fabs(d) > half) d = __dsub_rn(d, __dmul_rn(len, round(__dmul_rn(d, inv))));
+    return d;
+}
+
+// UBond (energy.F90:5335-5400) and UAngle (energy.F90:5409-5506), one
+// thread per particle: the force of every bond and angle the particle takes
+// part in (its role in it), summed in a fixed order; each bond's energy and
+// virial counted by its first particle, each angle's energy by its vertex.
 template <bool MIXED>
-__global__ void __launch_bounds__(kBondThreads) k_bond(const double *__restrict__ ro, int np,
-                                                   const int *__restrict__ off,
-                                                   const int *__restrict__ list,
-                                                   const int *__restrict__ ij,
-                                                   const double *__restrict__ bk,
-                                                   const double *__restrict__ beq,
-                                                   const int *__restrict__ bp, mg_box box,
-                                                   double *__restrict__ force,
-                                                   long long *__restrict__ ffx,
-                                                   double *__restrict__ part) {
-    __shared__ double sh[2 * (kBondThreads / 32)];
-    double acc[2] = {0.0, 0.0};
+__global__ void __launch_bounds__(kBondThreads) k_bond(BondArgs a) {
+    __shared__ double sh[3 * (kBondThreads / 32)];
+    double acc[3] = {0.0, 0.0, 0.0};
+    const double *ro = a.ro;
+    const mg_box &box = a.box;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < np) {
+    if (p < a.np) {
         double f[3] = {0.0, 0.0, 0.0};
-        for (int e = off[p]; e < off[p + 1]; ++e) {
-            int b = list[e] >> 1, role = list[e] & 1;
-            int ip = ij[2 * b], jp = ij[2 * b + 1];
-            double dx = mg_pbc1(__dsub_rn(ro[3 * ip], ro[3 * jp]), box.half[0], box.len[0]);
-            double dy = mg_pbc1(__dsub_rn(ro[3 * ip + 1], ro[3 * jp + 1]), box.half[1], box.len[1]);
-            double dz = mg_pbc1(__dsub_rn(ro[3 * ip + 2], ro[3 * jp + 2]), box.half[2], box.len[2]);
-            double r2 = dx * dx + dy * dy + dz * dz;
-            double r1 = sqrt(r2);
-            double term = r1 - beq[b];
-            double pw = 1.0;
-            for (int k = 0; k < bp[b] - 1; ++k) pw *= term;
-            double fac = bk[b] * pw;
-            double u = fac * term;
-            fac = -bp[b] * fac / r1;
-            double sgn = role ? -1.0 : 1.0;
-            f[0] += sgn * (fac * dx);
-            f[1] += sgn * (fac * dy);
-            f[2] += sgn * (fac * dz);
-            if (!role) {
-                acc[0] += u;
-                acc[1] -= fac * r2;
+        bool any = false;
+        if (a.off) {
+            for (int e = a.off[p]; e < a.off[p + 1]; ++e) {
+                int b = a.list[e] >> 1, role = a.list[e] & 1;
+                int ip = a.ij[2 * b], jp = a.ij[2 * b + 1];
+                double dx = mg_pbc1(__dsub_rn(ro[3 * ip], ro[3 * jp]), box.half[0], box.len[0]);
+                double dy = mg_pbc1(__dsub_rn(ro[3 * ip + 1], ro[3 * jp + 1]), box.half[1], box.len[1]);
+                double dz = mg_pbc1(__dsub_rn(ro[3 * ip + 2], ro[3 * jp + 2]), box.half[2], box.len[2]);
+                double r2 = dx * dx + dy * dy + dz * dz;
+                double r1 = sqrt(r2);
+                double term = r1 - a.beq[b];
+                double pw = 1.0;
+                for (int k = 0; k < a.bp[b] - 1; ++k) pw *= term;
+                double fac = a.bk[b] * pw;
+                double u = fac * term;
+                fac = -a.bp[b] * fac / r1;
+                double sgn = role ? -1.0 : 1.0;
+                f[0] += sgn * (fac * dx);
+                f[1] += sgn * (fac * dy);
+                f[2] += sgn * (fac * dz);
+                if (!role) {
+                    acc[0] += u;
+                    acc[1] -= fac * r2;
+                }
+                any = true;
             }
         }
-        if (off[p + 1] > off[p]) {
+        if (a.aoff) {
+            for (int e = a.aoff[p]; e < a.aoff[p + 1]; ++e) {
+                int an = a.alist[e] >> 2, role = a.alist[e] & 3;
+                int jm = a.aijk[3 * an], ip = a.aijk[3 * an + 1], jp = a.aijk[3 * an + 2];
+                double dm[3], dq[3];
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    dm[m] = pbc_anint(__dsub_rn(ro[3 * ip + m], ro[3 * jm + m]), box.half[m], box.len[m], box.inv[m]);
+                    dq[m] = pbc_anint(__dsub_rn(ro[3 * ip + m], ro[3 * jp + m]), box.half[m], box.len[m], box.inv[m]);
+                }
+                double dmi = 1.0 / sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dm[0], dm[0]), __dmul_rn(dm[1], dm[1])),
+                                                  __dmul_rn(dm[2], dm[2])));
+                double dpi = 1.0 / sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dq[0], dq[0]), __dmul_rn(dq[1], dq[1])),
+                                                  __dmul_rn(dq[2], dq[2])));
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    dm[m] = __dmul_rn(dm[m], dmi);
+                    dq[m] = __dmul_rn(dq[m], dpi);
+                }
+                double cosine = __dadd_rn(__dadd_rn(__dmul_rn(dm[0], dq[0]), __dmul_rn(dm[1], dq[1])),
+                                          __dmul_rn(dm[2], dq[2]));
+                double theta = acos(fmax(-1.0, fmin(cosine, 1.0)));
+                double term = __dsub_rn(theta, a.aeq[an]);
+                double fac = __dmul_rn(a.ak[an], powi_d(term, a.ap[an] - 1));
+                if (role == 1) acc[2] += __dmul_rn(fac, term);
+                fac = __dmul_rn((double)(-a.ap[an]), fac) / sin(theta);
+                double fm = __dmul_rn(fac, dmi), fp = __dmul_rn(fac, dpi);
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    double gm = __dmul_rn(fm, __dsub_rn(dq[m], __dmul_rn(cosine, dm[m])));   // on jm
+                    double gp = __dmul_rn(fp, __dsub_rn(dm[m], __dmul_rn(cosine, dq[m])));   // on jp
+                    f[m] += role == 0 ? gm : role == 2 ? gp : -__dadd_rn(gm, gp);
+                }
+                any = true;
+            }
+        }
+        if (any) {
             if (MIXED) {
-                for (int m = 0; m < 3; ++m) ffx[3 * p + m] += __double2ll_rn(f[m] * MG_FX_SCALE);
+                for (int m = 0; m < 3; ++m) a.ffx[3 * p + m] += __double2ll_rn(f[m] * MG_FX_SCALE);
             } else {
-                for (int m = 0; m < 3; ++m) force[3 * p + m] += f[m];
+                for (int m = 0; m < 3; ++m) a.force[3 * p + m] += f[m];
             }
         }
     }
-    block_sum<kBondThreads>(acc, 2, part + (size_t)blockIdx.x * 2, sh);
+    block_sum<kBondThreads>(acc, 3, a.part + (size_t)blockIdx.x * 3, sh);
+}
+
+// the bond/angle kernel's arguments for the handle, forces into force / ffx
+static BondArgs bond_args(mg_handle *h, double *force, long long *ffx) {
+    BondArgs b;
+    b.ro = h->d_ro;
+    b.np = h->np;
+    b.off = h->nbond > 0 ? h->d_bond_off : nullptr;
+    b.list = h->d_bond_list;
+    b.ij = h->d_bond_ij;
+    b.bk = h->d_bond_k;
+    b.beq = h->d_bond_eq;
+    b.bp = h->d_bond_p;
+    b.aoff = h->nangle > 0 ? h->d_angle_off : nullptr;
+    b.alist = h->d_angle_list;
+    b.aijk = h->d_angle_ijk;
+    b.ak = h->d_angle_k;
+    b.aeq = h->d_angle_eq;
+    b.ap = h->d_angle_p;
+    b.nangle = h->nangle;
+    for (int m = 0; m < 3; ++m) {
+        b.box.len[m] = h->boxlen[m];
+        b.box.half[m] = h->boxlen2[m];
+        b.box.inv[m] = h->boxleni[m];
+    }
+    b.force = force;
+    b.ffx = ffx;
+    b.part = h->d_part + h->part_bond;
+    return b;
 }
 
 // sum of az*r per block (UEwaldSurf, energy.F90:1352-1355)
@@ -523,7 +625,7 @@ struct ReduceArgs {
 constexpr int kRedThreads = 256;
 
 __host__ __device__ __forceinline__ int red_stride(int g, int nv_pair) {
-    return g == 0 ? nv_pair : g == 3 ? 3 : 2;
+    return g == 0 ? nv_pair : g == 1 ? 2 : 3;   // pair, reciprocal, bond (+ angle), surface
 }
 
 // sum of component comp over the per-thread sums tsum[t0 + i], i < S
@@ -537,7 +639,7 @@ __device__ __forceinline__ double red_comp(const double *tsum, int t0, int S, in
 __global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
     mg_pdl_begin();
     __shared__ double tsum[kRedThreads];
-    __shared__ double vals[MG_MAX_NPTPT + 1 + 2 + 2 + 3];
+    __shared__ double vals[MG_MAX_NPTPT + 1 + 2 + 3 + 3];
     __shared__ int is_last;
     int t = threadIdx.x, lane = t & 31, w = t >> 5;
     constexpr int nwarp = kRedThreads / 32;
@@ -580,10 +682,10 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
     }
     tsum[t] = s0 + s1;
     __syncthreads();
-    int nv = nv_pair + 2 + 2 + 3;
+    int nv = nv_pair + 2 + 3 + 3;
     for (int v = w; v < nv; v += nwarp) {
-        int gv = v < nv_pair ? 0 : v < nv_pair + 2 ? 1 : v < nv_pair + 4 ? 2 : 3;
-        int comp = gv == 0 ? v : gv == 1 ? v - nv_pair : gv == 2 ? v - nv_pair - 2 : v - nv_pair - 4;
+        int gv = v < nv_pair ? 0 : v < nv_pair + 2 ? 1 : v < nv_pair + 5 ? 2 : 3;
+        int comp = gv == 0 ? v : gv == 1 ? v - nv_pair : gv == 2 ? v - nv_pair - 2 : v - nv_pair - 5;
         int sg = red_stride(gv, nv_pair);
         double sv = red_comp(tsum, t0s[gv], sg * (nts[gv] / sg), sg, comp, lane);
         if (lane == 0) vals[v] = sv;
@@ -606,24 +708,25 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce(ReduceArgs a) {
         virrec = vals[nv_pair + 1];
         urec = urec + a.u_self;
         if (a.lsurf) {
-            sx = vals[nv_pair + 4];
-            sy = vals[nv_pair + 5];
-            sz = vals[nv_pair + 6];
+            sx = vals[nv_pair + 5];
+            sy = vals[nv_pair + 6];
+            sz = vals[nv_pair + 7];
             double term = a.surf_fac * (sx * sx + sy * sy + sz * sz);
             urec = urec + term;
             virrec = virrec - term;
         }
         urec = a.EpsiFourPi * urec;
     }
-    double ubond = vals[nv_pair + 2], virbond = vals[nv_pair + 3];
+    double ubond = vals[nv_pair + 2], virbond = vals[nv_pair + 3], uangle = vals[nv_pair + 4];
     int o = a.nptpt + 1;
-    u[o + 0] = twob0 + urec + ubond;                          // u%tot
+    u[o + 0] = twob0 + urec + ubond + uangle;                 // u%tot
     u[o + 1] = urec;                                          // u%rec
     u[o + 2] = ubond;                                         // u%bond
-    u[o + 3] = virtwob + a.EpsiFourPi * virrec + virbond;     // virial
+    u[o + 3] = virtwob + a.EpsiFourPi * virrec + virbond;     // virial (angles contribute none)
     u[o + 4] = sx;
     u[o + 5] = sy;
     u[o + 6] = sz;
+    u[o + 7] = uangle;                                        // u%angle
 }
 
 // force -> forceo with the surface force and the unit factor (energy.F90:405-424)
@@ -775,7 +878,7 @@ int mg_forces_init(mg_handle *h, const double *ubuf, const int *start, const int
     h->part_pair = 0;
     h->part_rec = h->part_pair + h->nblk_pair * (h->nptpt + 1);
     h->part_bond = h->part_rec + 2 * (h->nblk_rec > 0 ? h->nblk_rec : 1);
-    h->part_surf = h->part_bond + 2 * h->nblk_bond;
+    h->part_surf = h->part_bond + 3 * h->nblk_bond;
     // k_reduce: its stage-1 rows (at most one per partial row) and its ticket
     h->part_red = h->part_surf + 3 * h->nblk_surf;
     size_t npart = 2 * (size_t)h->part_red + 1;
@@ -914,17 +1017,10 @@ int mg_utotal_launch(mg_handle *h) {
         if (h->pair_warp) k_pair<false, true><<<nb, kPairThreads, sm, ss>>>(a);
         else k_pair<false, false><<<nb, kPairThreads, sm, ss>>>(a);
     }
-    if (par && h->nbond > 0) {   // bonds follow the pairs on the second stream
-        if (mixed)
-            k_bond<true><<<h->nblk_bond, kBondThreads, 0, ss>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
-                                                            h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                            h->d_bond_p, a.box, force_sr, ffx_sr,
-                                                            h->d_part + h->part_bond);
-        else
-            k_bond<false><<<h->nblk_bond, kBondThreads, 0, ss>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
-                                                             h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                             h->d_bond_p, a.box, force_sr, ffx_sr,
-                                                             h->d_part + h->part_bond);
+    if (par && (h->nbond > 0 || h->nangle > 0)) {   // bonds and angles follow the pairs on the second stream
+        BondArgs ba = bond_args(h, force_sr, ffx_sr);
+        if (mixed) k_bond<true><<<h->nblk_bond, kBondThreads, 0, ss>>>(ba);
+        else k_bond<false><<<h->nblk_bond, kBondThreads, 0, ss>>>(ba);
         h->launches++;
     }
     if (par) MG_CUDA(h, cudaEventRecord(h->ev_sr, ss));   // the short-range forces are in d_ffx2 / d_force2
@@ -994,17 +1090,10 @@ static int utotal_reduce(mg_handle *h, bool mixed, bool par) {
         box.inv[m] = h->boxleni[m];
     }
     MG_TRY(mg_phase_begin(h, "bond+reduce"));
-    if (h->nbond > 0 && !par) {
-        if (mixed)
-            k_bond<true><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
-                                                               h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                               h->d_bond_p, box, h->d_force, h->d_ffx,
-                                                               h->d_part + h->part_bond);
-        else
-            k_bond<false><<<h->nblk_bond, kBondThreads, 0, h->st>>>(h->d_ro, np, h->d_bond_off, h->d_bond_list,
-                                                                h->d_bond_ij, h->d_bond_k, h->d_bond_eq,
-                                                                h->d_bond_p, box, h->d_force, h->d_ffx,
-                                                                h->d_part + h->part_bond);
+    if ((h->nbond > 0 || h->nangle > 0) && !par) {
+        BondArgs ba = bond_args(h, h->d_force, h->d_ffx);
+        if (mixed) k_bond<true><<<h->nblk_bond, kBondThreads, 0, h->st>>>(ba);
+        else k_bond<false><<<h->nblk_bond, kBondThreads, 0, h->st>>>(ba);
         h->launches++;
     }
     if (h->ewald != MG_EWALD_NONE && h->lsurf) {
@@ -1019,7 +1108,7 @@ static int utotal_reduce(mg_handle *h, bool mixed, bool par) {
     r.off[1] = h->part_rec;
     r.nblk[1] = (h->ewald != MG_EWALD_NONE) ? h->nblk_rec : 0;
     r.off[2] = h->part_bond;
-    r.nblk[2] = (h->nbond > 0) ? h->nblk_bond : 0;
+    r.nblk[2] = (h->nbond > 0 || h->nangle > 0) ? h->nblk_bond : 0;
     r.off[3] = h->part_surf;
     r.nblk[3] = (h->ewald != MG_EWALD_NONE && h->lsurf) ? h->nblk_surf : 0;
     r.blk0[0] = 0;

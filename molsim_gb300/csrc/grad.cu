@@ -102,12 +102,45 @@ __global__ void __launch_bounds__(kGradThreads) k_grad_pairs(GradArgs a) {
     }
 }
 
-// bonds: dU/dL_a = sum du/dr dx_a^2 / r (divided by L_a at the end)
+// bonds: dU/dL_a = sum du/dr dx_a^2 / r (divided by L_a at the end);
+// angles (UAngle): sum over the two arms d = r_ip - r_j of F_j,a d_a, F_j the
+// force on the arm's end (dU/dd = F_j since d depends on r_j with sign -1)
 __global__ void k_grad_bonds(const double *__restrict__ ro, const int *__restrict__ ij,
                              const double *__restrict__ bk, const double *__restrict__ beq,
-                             const int *__restrict__ bp, int nbond, mg_box box, double *__restrict__ part) {
+                             const int *__restrict__ bp, int nbond, const int *__restrict__ aijk,
+                             const double *__restrict__ ak, const double *__restrict__ aeq,
+                             const int *__restrict__ ap, int nangle, mg_box box, double *__restrict__ part) {
     __shared__ double red[3][8];
     double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+    for (int an = blockIdx.x * blockDim.x + threadIdx.x; an < nangle; an += gridDim.x * blockDim.x) {
+        int jm = aijk[3 * an], ip = aijk[3 * an + 1], jp = aijk[3 * an + 2];
+        double dm[3], dq[3], um[3], uq[3];
+        for (int m = 0; m < 3; ++m) {
+            double x = ro[3 * (size_t)ip + m] - ro[3 * (size_t)jm + m];
+            double y = ro[3 * (size_t)ip + m] - ro[3 * (size_t)jp + m];
+            if (fabs(x) > box.half[m]) x -= box.len[m] * round(x * box.inv[m]);
+            if (fabs(y) > box.half[m]) y -= box.len[m] * round(y * box.inv[m]);
+            dm[m] = x;
+            dq[m] = y;
+        }
+        double dmi = 1.0 / sqrt(dm[0] * dm[0] + dm[1] * dm[1] + dm[2] * dm[2]);
+        double dpi = 1.0 / sqrt(dq[0] * dq[0] + dq[1] * dq[1] + dq[2] * dq[2]);
+        for (int m = 0; m < 3; ++m) {
+            um[m] = dm[m] * dmi;
+            uq[m] = dq[m] * dpi;
+        }
+        double c = um[0] * uq[0] + um[1] * uq[1] + um[2] * uq[2];
+        double theta = acos(fmax(-1.0, fmin(c, 1.0)));
+        double term = theta - aeq[an];
+        int pw = ap[an];
+        double fac = -pw * ak[an] * pow(term, pw - 1) / sin(theta);
+        double g[3];
+        for (int m = 0; m < 3; ++m)
+            g[m] = (fac * dmi) * (uq[m] - c * um[m]) * dm[m] + (fac * dpi) * (um[m] - c * uq[m]) * dq[m];
+        w0 += g[0];
+        w1 += g[1];
+        w2 += g[2];
+    }
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbond; b += gridDim.x * blockDim.x) {
         int i = ij[2 * b], j = ij[2 * b + 1];
         double dx = mg_pbc1(ro[3 * (size_t)i] - ro[3 * (size_t)j], box.half[0], box.len[0]);
@@ -316,7 +349,8 @@ extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, doubl
     }
     MG_TRY(mg_utotal_launch(h));   // energies, structure factors / potential mesh, surface sums
     int nblk_pair = (np + kGradThreads - 1) / kGradThreads, nv = 2 * nptpt + 3;
-    int nblk_bond = h->nbond > 0 ? std::min(304, (h->nbond + 255) / 256) : 0;
+    int nbonded = std::max(h->nbond, h->nangle);
+    int nblk_bond = nbonded > 0 ? std::min(304, (nbonded + 255) / 256) : 0;
     size_t need = (size_t)np + 3 * nptpt + (size_t)nblk_pair * nv + 3 * (size_t)std::max(nblk_bond, 1) + 3 +
                   3 * 304 + (size_t)nv;
     if (need > h->grad_cap) {
@@ -394,7 +428,8 @@ extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, doubl
     if (nblk_bond > 0) {
         mg_box box = a.box;
         k_grad_bonds<<<nblk_bond, 256, 0, h->st>>>(h->d_ro, h->d_bond_ij, h->d_bond_k, h->d_bond_eq, h->d_bond_p,
-                                                    h->nbond, box, d_bp);
+                                                    h->nbond, h->d_angle_ijk, h->d_angle_k, h->d_angle_eq,
+                                                    h->d_angle_p, h->nangle, box, d_bp);
         h->launches++;
     }
     const double *rec3 = nullptr;

@@ -119,6 +119,11 @@ struct mg_handle {
     int *d_bond_ij = nullptr, *d_bond_p = nullptr;   // [2*nbond] (0-based), [nbond]
     double *d_bond_k = nullptr, *d_bond_eq = nullptr;
     int *d_bond_off = nullptr, *d_bond_list = nullptr;  // CSR per particle: entries b*2 + (0 first, 1 second)
+    // angles jm-ip-jp (UAngle): 0-based triples, parameters, and a CSR per
+    // particle of entries a*4 + role (0 jm, 1 ip, 2 jp)
+    int nangle = 0;
+    int *d_angle_ijk = nullptr, *d_angle_p = nullptr, *d_angle_off = nullptr, *d_angle_list = nullptr;
+    double *d_angle_k = nullptr, *d_angle_eq = nullptr;
 
     // ---- standard Ewald ----------------------------------------------------
     int nkvec = 0;

@@ -179,6 +179,13 @@ class Engine:
         f1, f2 = self.system.bd_factors(tstep)
         self._check(self._fn("bd_setup")(self.h, abi.f64(f1), abi.f64(f2), int(iseed)), "bd_setup")
 
+    def EnergyTerms(self):
+        """u%tot, u%twob(0), u%rec, u%bond, u%angle and the virial of the last
+        UTotal or step."""
+        t = np.zeros(6)
+        self._check(self._fn("energy_terms")(self.h, abi.f64(t)), "energy_terms")
+        return dict(u_tot=t[0], u_twob0=t[1], u_rec=t[2], u_bond=t[3], u_angle=t[4], virial=t[5])
+
     def BDRun(self, nstep):
         forceo = np.zeros(3 * self.np)
         uo = np.zeros(4)

@@ -74,6 +74,13 @@ class System:
     bond_k: Optional[np.ndarray] = None
     bond_eq: Optional[np.ndarray] = None
     bond_p: Optional[np.ndarray] = None
+    # chain angles jm-ip-jp (1-based), u = k*(theta-eq)**p (UAngle)
+    angle_jm: Optional[np.ndarray] = None
+    angle_ip: Optional[np.ndarray] = None
+    angle_jp: Optional[np.ndarray] = None
+    angle_k: Optional[np.ndarray] = None
+    angle_eq: Optional[np.ndarray] = None
+    angle_p: Optional[np.ndarray] = None
     name: str = "system"
     # table (filled by build_table)
     ubuf: Optional[np.ndarray] = None
@@ -178,6 +185,11 @@ class System:
             keep.update(bond_ip=abi.as_i32(self.bond_ip), bond_jp=abi.as_i32(self.bond_jp),
                         bond_k=abi.as_f64(self.bond_k), bond_eq=abi.as_f64(self.bond_eq),
                         bond_p=abi.as_i32(self.bond_p))
+        na = 0 if self.angle_ip is None else int(len(self.angle_ip))
+        if na:
+            keep.update(angle_jm=abi.as_i32(self.angle_jm), angle_ip=abi.as_i32(self.angle_ip),
+                        angle_jp=abi.as_i32(self.angle_jp), angle_k=abi.as_f64(self.angle_k),
+                        angle_eq=abi.as_f64(self.angle_eq), angle_p=abi.as_i32(self.angle_p))
         p = abi.MgParams()
         p.abi_version = abi.MG_ABI_VERSION
         p.np = self.np_
@@ -215,6 +227,12 @@ class System:
             p.bond_k = abi.f64(keep["bond_k"])
             p.bond_eq = abi.f64(keep["bond_eq"])
             p.bond_p = abi.i32(keep["bond_p"])
+        p.nangle = na
+        if na:
+            for f in ("angle_jm", "angle_ip", "angle_jp", "angle_p"):
+                setattr(p, f, abi.i32(keep[f]))
+            p.angle_k = abi.f64(keep["angle_k"])
+            p.angle_eq = abi.f64(keep["angle_eq"])
         return p, keep
 
     # ---- integrator inputs --------------------------------------------------

@@ -459,6 +459,11 @@ struct orc_sys {
     int nbond;
     int *bond_ip, *bond_jp, *bond_p;
     double *bond_k, *bond_eq;
+    /* angles */
+    int nangle;
+    int *angle_jm, *angle_ip, *angle_jp, *angle_p;
+    double *angle_k, *angle_eq;
+    double u_angle;
     /* state */
     double *ro, *force, *forceo, *u_twob, *utwobnew, *utwobold;
     double u_tot, u_rec, u_bond, virial;
@@ -687,6 +692,16 @@ int orc_create(const mg_params *p, orc_sys **out) {
         s->bond_k = xcalloc(s->nbond, sizeof(double)); memcpy(s->bond_k, p->bond_k, sizeof(double) * s->nbond);
         s->bond_eq = xcalloc(s->nbond, sizeof(double)); memcpy(s->bond_eq, p->bond_eq, sizeof(double) * s->nbond);
     }
+    s->nangle = p->nangle;
+    if (s->nangle > 0) {
+        size_t na = (size_t)s->nangle;
+        s->angle_jm = xcalloc(na, sizeof(int)); memcpy(s->angle_jm, p->angle_jm, sizeof(int) * na);
+        s->angle_ip = xcalloc(na, sizeof(int)); memcpy(s->angle_ip, p->angle_ip, sizeof(int) * na);
+        s->angle_jp = xcalloc(na, sizeof(int)); memcpy(s->angle_jp, p->angle_jp, sizeof(int) * na);
+        s->angle_p = xcalloc(na, sizeof(int)); memcpy(s->angle_p, p->angle_p, sizeof(int) * na);
+        s->angle_k = xcalloc(na, sizeof(double)); memcpy(s->angle_k, p->angle_k, sizeof(double) * na);
+        s->angle_eq = xcalloc(na, sizeof(double)); memcpy(s->angle_eq, p->angle_eq, sizeof(double) * na);
+    }
     s->ro = xcalloc((size_t)3 * np, sizeof(double));
     s->force = xcalloc((size_t)3 * np, sizeof(double));
     s->forceo = xcalloc((size_t)3 * np, sizeof(double));
@@ -712,6 +727,7 @@ void orc_destroy(orc_sys *s) {
     if (!s) return;
     void *ptrs[] = {s->iptpn, s->iptpt, s->az, s->ubuf, s->r2umin, s->r2atat, s->iubuflow,
                     s->bond_ip, s->bond_jp, s->bond_p, s->bond_k, s->bond_eq,
+                    s->angle_jm, s->angle_ip, s->angle_jp, s->angle_p, s->angle_k, s->angle_eq,
                     s->ro, s->force, s->forceo, s->u_twob, s->utwobnew, s->utwobold,
                     s->nneighpn, s->jpnlist, s->drosum, s->ipnext, s->ipprev, s->cellip,
                     s->kfac, s->eikx, s->eiky, s->eikz, s->eikyzm, s->eikyzp, s->eikr, s->sumeikr,
@@ -1530,6 +1546,68 @@ static void ubond(orc_sys *s) {
     s->virial = s->virial + virbond;
 }
 
+/* UAngle, energy.F90:5409-5506: u = k*(theta - eq)**p at each interior
+   segment, theta the angle at ip between ip-jm and ip-jp; forces on jm, jp
+   and ip; no contribution to the virial.  The reference carries the unit
+   vector of the previous segment into the next angle (dxm = -dxp); the
+   angles here are listed in its order and the vector recomputed, which
+   gives the same bits (PBC and the norm are symmetric in the sign). */
+static void uangle(orc_sys *s) {
+    s->u_angle = Zero;
+    int any = 0;
+    for (int a = 0; a < s->nangle; ++a) any |= s->angle_k[a] != Zero;
+    if (!any) return;
+    for (int a = 0; a < s->nangle; ++a) {
+        int jm = s->angle_jm[a], ip = s->angle_ip[a], jp = s->angle_jp[a];
+        double dxm = RO(1, ip) - RO(1, jm), dym = RO(2, ip) - RO(2, jm), dzm = RO(3, ip) - RO(3, jm);
+        pbc(s, &dxm, &dym, &dzm);
+        double dmi = One / sqrt(pow2(dxm) + pow2(dym) + pow2(dzm));
+        dxm = dxm * dmi;
+        dym = dym * dmi;
+        dzm = dzm * dmi;
+        double dxp = RO(1, ip) - RO(1, jp), dyp = RO(2, ip) - RO(2, jp), dzp = RO(3, ip) - RO(3, jp);
+        pbc(s, &dxp, &dyp, &dzp);
+        double dpi = One / sqrt(pow2(dxp) + pow2(dyp) + pow2(dzp));
+        dxp = dxp * dpi;
+        dyp = dyp * dpi;
+        dzp = dzp * dpi;
+        double cosine = dxm * dxp + dym * dyp + dzm * dzp;
+        double theta = acos(fmax(-One, fmin(cosine, One)));
+        double term = theta - s->angle_eq[a];
+        double fac = s->angle_k[a] * powi(term, s->angle_p[a] - 1);
+        s->u_angle = s->u_angle + fac * term;
+        fac = -s->angle_p[a] * fac / sin(theta);
+        double fxm = (fac * dmi) * (dxp - cosine * dxm);
+        double fym = (fac * dmi) * (dyp - cosine * dym);
+        double fzm = (fac * dmi) * (dzp - cosine * dzm);
+        double fxp = (fac * dpi) * (dxm - cosine * dxp);
+        double fyp = (fac * dpi) * (dym - cosine * dyp);
+        double fzp = (fac * dpi) * (dzm - cosine * dzp);
+        FORCE(1, jm) = FORCE(1, jm) + fxm;
+        FORCE(2, jm) = FORCE(2, jm) + fym;
+        FORCE(3, jm) = FORCE(3, jm) + fzm;
+        FORCE(1, jp) = FORCE(1, jp) + fxp;
+        FORCE(2, jp) = FORCE(2, jp) + fyp;
+        FORCE(3, jp) = FORCE(3, jp) + fzp;
+        FORCE(1, ip) = FORCE(1, ip) - (fxm + fxp);
+        FORCE(2, ip) = FORCE(2, ip) - (fym + fyp);
+        FORCE(3, ip) = FORCE(3, ip) - (fzm + fzp);
+    }
+    s->u_tot = s->u_tot + s->u_angle;
+}
+
+/* the energy terms of the last UTotal: u%tot, u%twob(0), u%rec, u%bond,
+   u%angle, virial */
+int orc_energy_terms(orc_sys *s, double *terms) {
+    terms[0] = s->u_tot;
+    terms[1] = s->u_twob[0];
+    terms[2] = s->u_rec;
+    terms[3] = s->u_bond;
+    terms[4] = s->u_angle;
+    terms[5] = s->virial;
+    return 0;
+}
+
 /* UTotal, energy.F90:280-430 (charged monoatomic branch) */
 static int utotal_core(orc_sys *s) {
     int st = 0;
@@ -1548,6 +1626,7 @@ static int utotal_core(orc_sys *s) {
     if (st) return st;
     if (s->ewald != MG_EWALD_NONE) { st = uewald(s); if (st) return st; }
     if (s->nbond > 0) ubond(s);
+    if (s->nangle > 0) uangle(s);
     double fac = s->force_fac;
     for (int ia = 1; ia <= s->np; ++ia) {
         /* monoatomic: r == ro, so the molecular virial term is zero */

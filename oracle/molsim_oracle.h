@@ -60,6 +60,7 @@ int  orc_nlist_get(orc_sys *s, int32_t *nneighpn, int32_t *jpnlist, int32_t maxn
 int  orc_celllist_get(orc_sys *s, int32_t *ncell, int32_t *cellip);
 int  orc_celllist_test(orc_sys *s);   /* TestCellList: brute-force completeness */
 int  orc_utotal(orc_sys *s, double *forceo, double *u_twob, double *uout);
+int  orc_energy_terms(orc_sys *s, double *terms);
 int  orc_dutotal(orc_sys *s, int32_t nptm, const int32_t *ipnptm, const double *rotm,
                  double *du_twob, double *du_rec, double *du_tot, int32_t *lhsoverlap);
 int  orc_accept(orc_sys *s);

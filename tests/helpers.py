@@ -63,6 +63,7 @@ def small_cases():
         ("spme_order10_n128", lambda: configs.small_system(seed=22, nmesh=128, order=10, n=500, L=45.0)),
         ("spme_order4_n128", lambda: configs.small_system(seed=23, nmesh=128, order=4, n=600, L=50.0)),
         ("spme_order6_n256", lambda: configs.small_system(seed=24, nmesh=256, order=6, n=500, L=45.0)),
+        ("spme_bonds_angles", lambda: configs.small_system(seed=25, chains=4, nseg=12, angle_kt=1.0)),
     ]
 
 

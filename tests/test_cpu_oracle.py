@@ -233,3 +233,34 @@ def test_dutotal_accumulates_to_utotal(orc, kw):
     e2.NList("write")
     u1 = e2.UTotal()["u_tot"]
     assert abs((u0 + acc) - u1) < 1e-9 * abs(u1)
+
+
+def test_angle_forces_are_minus_energy_gradient(orc):
+    """UAngle (energy.F90:5409-5506): forces on the three beads of every angle
+    against central differences of the oracle's energy; u%angle in the total."""
+    s = configs.small_system(seed=41, ewald=abi.MG_EWALD_NONE, chains=3, nseg=8, angle_kt=0.8, eps_kt=0.0)
+    s.utoltab, s.ftoltab = 1e-8, 1e-7
+    s.build_table(orc.orc_pot_twobody_tab)
+    e = Engine(s, lib=orc, prefix="orc_")
+    ro = s.ro_flat().copy()
+    e.SetPositions(ro)
+    e.NList("write")
+    r = e.UTotal()
+    t = e.EnergyTerms()
+    assert t["u_angle"] > 0
+    assert abs(t["u_tot"] - (t["u_twob0"] + t["u_rec"] + t["u_bond"] + t["u_angle"])) <= 1e-12 * abs(t["u_tot"])
+    f = r["forceo"].reshape(-1)
+    h = 1e-5
+    for k in (0, 5, 3 * 3 + 1, 3 * 7 + 2, 3 * 12):   # chain beads (ends and interior)
+        up, dn = ro.copy(), ro.copy()
+        up[k] += h
+        dn[k] -= h
+        e.SetPositions(up)
+        e.NList("write")
+        uu = e.UTotal()["u_tot"]
+        e.SetPositions(dn)
+        e.NList("write")
+        ud = e.UTotal()["u_tot"]
+        fd = -units.FORCE_FAC * (uu - ud) / (2 * h)
+        assert abs(fd - f[k]) < 1e-6 * np.abs(f).max(), (k, fd, f[k])
+    e.close()

@@ -54,6 +54,7 @@ SYSTEMS = {
     "std_cell": lambda: configs.small_system(seed=83, ewald=abi.MG_EWALD_STD, ncut=5,
                                              txintlist=abi.MG_CELLLIST),
     "no_ewald_wca": lambda: configs.small_system(seed=84, ewald=abi.MG_EWALD_NONE, lljcut=1),
+    "spme_angles": lambda: configs.small_system(seed=89, chains=3, nseg=8, angle_kt=0.8),
 }
 
 

@@ -6,7 +6,7 @@ surface, bonds, force epilogue).
 import numpy as np
 import pytest
 
-from molsim_gb300 import abi, configs
+from molsim_gb300 import Engine, abi, configs
 from tests.helpers import (TOL_FP64, TOL_MIXED_RMS, force_err, force_rms_err, prepared, rel,
                            run_pair, small_cases, utotal_errors)
 
@@ -45,3 +45,27 @@ def test_electrolyte_std_config(orc, gpu_lib):
     e = utotal_errors(g, r, s.nptpt)
     bad = {k: v for k, v in e.items() if not v <= TOL_FP64}
     assert not bad, (bad, e)
+
+
+@pytest.mark.parametrize("form", [abi.MG_FP64, abi.MG_MIXED])
+def test_angle_energy_matches_oracle(form, orc, gpu_lib):
+    """u%angle (UAngle) and the total through mg_energy_terms against the
+    oracle: the bonded terms to 1e-10 in both forms (the mixed form computes
+    them in FP64 too); the total and the virial to 1e-10 in FP64 and to 1e-5
+    in the mixed form (its pair and mesh terms are FP32)."""
+    s = prepared(configs.small_system(seed=26, chains=4, nseg=12, angle_kt=1.0, angle_eq=2.2, angle_p=3), orc)
+    ref = Engine(s, lib=orc, prefix="orc_")
+    gpu = Engine(s, form=form)
+    out = []
+    for e in (ref, gpu):
+        e.SetPositions(s.ro_flat())
+        e.NList("write")
+        e.UTotal()
+        out.append(e.EnergyTerms())
+    r, g = out
+    tol = 1e-10 if form == abi.MG_FP64 else 1e-5
+    assert abs(g["u_angle"] - r["u_angle"]) <= 1e-10 * abs(r["u_angle"])
+    # the chains are placed at the bond length, so u%bond is ~0: absolute bar
+    assert abs(g["u_bond"] - r["u_bond"]) <= 1e-10 * abs(r["u_tot"])
+    assert abs(g["u_tot"] - r["u_tot"]) <= tol * abs(r["u_tot"])
+    assert abs(g["virial"] - r["virial"]) <= tol * abs(r["virial"])
