@@ -208,7 +208,11 @@ int mg_energy_terms(mg_handle *h, double *terms);
 
 /* DUTotal (denergy.F90:98-215) for nptm moving particles ipnptm(1:nptm)
  * at trial positions rotm(3,nptm).  Returns du%twob(0:nptpt) in du_twob,
- * du%rec in *du_rec, du%tot in *du_tot and the hard-core flag. */
+ * du%rec in *du_rec, du%tot in *du_tot and the hard-core flag.  With bonds,
+ * du%tot includes du%bond and du%angle of the moving chain segments (DUBond,
+ * DUAngle: denergy.F90:2893-3077; a moved neighbour's trial position is the
+ * previous or next entry of ipnptm, as there, so a multi-particle move lists
+ * the segments of one string in chain order). */
 int mg_dutotal(mg_handle *h, int32_t nptm, const int32_t *ipnptm,
                const double *rotm, double *du_twob, double *du_rec,
                double *du_tot, int32_t *lhsoverlap);

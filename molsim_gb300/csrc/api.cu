@@ -111,7 +111,7 @@ static void free_all(mg_handle *h) {
                     h->d_nneighcell, h->d_force, h->d_forceo, h->d_ffx, h->d_part, h->d_uout, h->d_err,
                     h->d_bond_ij, h->d_bond_p, h->d_bond_k, h->d_bond_eq, h->d_bond_off,
                     h->d_bond_list, h->d_angle_ijk, h->d_angle_p, h->d_angle_off, h->d_angle_list, h->d_angle_k,
-                    h->d_angle_eq, h->d_kvec, h->d_kfac, h->d_eik, h->d_S, h->d_Stm, h->d_Q, h->d_F,
+                    h->d_angle_eq, h->d_chain, h->d_kvec, h->d_kfac, h->d_eik, h->d_S, h->d_Stm, h->d_Q, h->d_F,
                     h->d_Qfx, h->d_mf, h->d_ew, h->d_vw, h->d_mf_f, h->d_ew_f, h->d_vw_f, h->d_tw,
                     h->d_Qref, h->d_phi, h->d_gker, h->d_ipnptm, h->d_rotm, h->d_du, h->d_drostep,
                     h->d_drosum, h->d_blkmax, h->d_rebuild, h->d_massip, h->d_rod, h->d_rodd,
@@ -297,6 +297,23 @@ static int create_impl(const mg_params *p, mg_handle *h) {
         MG_TRY(upload(h, &h->d_angle_eq, p->angle_eq, na));
         MG_TRY(upload(h, &h->d_angle_off, off.data(), off.size()));
         MG_TRY(upload(h, &h->d_angle_list, list.data(), list.size()));
+    }
+    if (p->nbond > 0) {
+        std::vector<int> chain(5 * (size_t)np, 0);
+        for (int i = 0; i < np; ++i) chain[5 * i + 2] = chain[5 * i + 3] = chain[5 * i + 4] = -1;
+        for (int b = 0; b < p->nbond; ++b) {
+            int i = p->bond_ip[b] - 1, j = p->bond_jp[b] - 1;
+            chain[5 * i + 1] = j + 1;
+            chain[5 * i + 3] = b;
+            chain[5 * j + 0] = i + 1;
+            chain[5 * j + 2] = b;
+        }
+        h->chain_angles = 0;
+        for (int a = 0; a < p->nangle; ++a) {
+            chain[5 * (p->angle_ip[a] - 1) + 4] = a;
+            if (p->angle_k[a] != 0.0) h->chain_angles = 1;
+        }
+        MG_TRY(upload(h, &h->d_chain, chain.data(), chain.size()));
     }
 
     if (h->ewald == MG_EWALD_SPM) MG_TRY(mg_spme_init(h));

@@ -30,7 +30,9 @@
 //                     dE = d.phi + d.G.d,
 //                the same number the reference gets by spreading QmeshTM and
 //                transforming it (denergy.F90:1413-1495), up to rounding.
-//   k_mc_final   du%rec = EpsiFourPi (dE_rec + dE_surf), du%tot, overlap
+//   k_mc_final   du%rec = EpsiFourPi (dE_rec + dE_surf), du%bond and
+//                du%angle of the moving chain segments (DUBond, DUAngle:
+//                denergy.F90:2893-3077), du%tot, overlap
 //
 // On accept the moving particles take their trial positions, the mesh
 // charges Q += d, the potential phi is recomputed from Q by one FFT round
@@ -400,6 +402,121 @@ __global__ void k_mc_spm_accept(McArgs a, SpmArgs s, double *__restrict__ Q) {
     }
 }
 
+// ---- bonds and angles of the moving chain segments ---------------------------------
+struct ChainArgs {
+    const int *nn;           // [5 np]: lower, upper neighbour (1-based, 0 none), bond to
+                             // each (-1 none), angle at the particle as vertex (-1 none);
+                             // null: no chains
+    const double *bk, *beq, *ak, *aeq;
+    const int *bp, *ap;
+    int angles;              // some angle has k != 0
+};
+
+// x**n with the integer power expanded as products (gfortran's **)
+__device__ __forceinline__ double mc_powi(double x, int n) {
+    if (n == 2) return __dmul_rn(x, x);
+    double r = x;
+    for (int i = 1; i < n; ++i) r = __dmul_rn(r, x);
+    return n == 0 ? 1.0 : r;
+}
+
+// PBC with anint (molaux.F90:104-146)
+__device__ __forceinline__ double mc_pbc_anint(const McArgs &a, double d, int m) {
+    if (fabs(d) > a.box.half[m]) d = __dsub_rn(d, __dmul_rn(a.box.len[m], round(__dmul_rn(d, a.box.inv[m]))));
+    return d;
+}
+
+// angle_rad(-(r0 - rm), r+ - r0) (molaux.F90:836-846) with PBC on both arms
+__device__ double mc_angle(const McArgs &a, const double *rm, const double *r0, const double *rp) {
+    double x1[3], x2[3];
+    for (int m = 0; m < 3; ++m) {
+        x1[m] = -mc_pbc_anint(a, __dsub_rn(r0[m], rm[m]), m);
+        x2[m] = mc_pbc_anint(a, __dsub_rn(rp[m], r0[m]), m);
+    }
+    double t1 = __dadd_rn(__dadd_rn(__dmul_rn(x1[0], x2[0]), __dmul_rn(x1[1], x2[1])), __dmul_rn(x1[2], x2[2]));
+    double t2 = mg_r2_exact(x1[0], x1[1], x1[2]);
+    double t3 = mg_r2_exact(x2[0], x2[1], x2[2]);
+    double t = __ddiv_rn(t1, sqrt(__dmul_rn(t2, t3)));
+    return acos(fmax(-1.0, fmin(t, 1.0)));
+}
+
+// DUBond and DUAngle of trial t: the moving list in order, a moved
+// neighbour's new position from the previous / next list entry inside the
+// list and from its own entry at the ends (the reference's routines assume
+// that the moving segments form one string)
+__device__ void mc_bonded(const McArgs &a, const ChainArgs &c, int t, double *dub, double *dua) {
+    const int *ipl = a.ip + (size_t)t * a.nptm;
+    const double *rtl = a.rt + 3 * (size_t)t * a.nptm;
+    auto rtm = [&](int k) { return rtl + 3 * k; };
+    auto rold = [&](int jp) { return a.ro + 3 * (size_t)(jp - 1); };
+    auto loc = [&](int jp) {
+        for (int k = 0; k < a.nptm; ++k)
+            if (ipl[k] == jp) return k;
+        return 0;
+    };
+    int last = a.nptm - 1;
+    double ub = 0.0;
+    for (int k = 0; k < a.nptm; ++k) {
+        int ip = ipl[k];
+        const int *e = c.nn + 5 * (size_t)(ip - 1);
+        int jm = e[0], jp = e[1];
+        for (int side = 0; side < 2; ++side) {
+            int jn = side ? jp : jm;
+            if (jn == 0) continue;
+            const double *rn;
+            if (!is_moving(a, t, jn)) rn = rold(jn);
+            else if (side) continue;   // the upper bond is counted by the upper segment
+            else rn = k > 0 ? rtm(k - 1) : rtm(loc(jm));
+            int b = e[2 + side];
+            double r2n = mc_r2(a, rtm(k), rn), r2o = mc_r2(a, rold(ip), rold(jn));
+            ub = __dadd_rn(ub, __dmul_rn(c.bk[b], __dsub_rn(mc_powi(__dsub_rn(sqrt(r2n), c.beq[b]), c.bp[b]),
+                                                             mc_powi(__dsub_rn(sqrt(r2o), c.beq[b]), c.bp[b]))));
+        }
+    }
+    *dub = ub;
+    double ua = 0.0;
+    if (c.angles) {
+        auto term = [&](int an, const double *nm, const double *n0, const double *np_, const double *om,
+                        const double *o0, const double *op) {
+            double tn = mc_angle(a, nm, n0, np_), to = mc_angle(a, om, o0, op);
+            ua = __dadd_rn(ua, __dmul_rn(c.ak[an], __dsub_rn(mc_powi(__dsub_rn(tn, c.aeq[an]), c.ap[an]),
+                                                             mc_powi(__dsub_rn(to, c.aeq[an]), c.ap[an]))));
+        };
+        for (int k = 0; k < a.nptm; ++k) {
+            int ip = ipl[k];
+            const int *e = c.nn + 5 * (size_t)(ip - 1);
+            int jm = e[0], jp = e[1];
+            if (jm != 0 && jp != 0 && e[4] >= 0) {
+                bool mm = is_moving(a, t, jm), mp = is_moving(a, t, jp);
+                const double *nm, *np_;
+                if (mm && mp) {
+                    bool inner = k > 0 && k < last;
+                    nm = inner ? rtm(k - 1) : rtm(loc(jm));
+                    np_ = inner ? rtm(k + 1) : rtm(loc(jp));
+                } else if (mm) {
+                    nm = k > 0 ? rtm(k - 1) : rtm(loc(jm));
+                    np_ = rold(jp);
+                } else {
+                    nm = rold(jm);
+                    np_ = mp ? (k < last ? rtm(k + 1) : rtm(loc(jp))) : rold(jp);
+                }
+                term(e[4], nm, rtm(k), np_, rold(jm), rold(ip), rold(jp));
+            }
+            if (jm != 0) {
+                const int *em = c.nn + 5 * (size_t)(jm - 1);
+                if (em[0] != 0 && !is_moving(a, t, jm) && em[4] >= 0)
+                    term(em[4], rold(em[0]), rold(jm), rtm(k), rold(em[0]), rold(jm), rold(ip));
+            }
+            if (jp != 0) {
+                const int *ep = c.nn + 5 * (size_t)(jp - 1);
+                if (ep[1] != 0 && !is_moving(a, t, jp) && ep[4] >= 0)
+                    term(ep[4], rtm(k), rold(jp), rold(ep[1]), rold(ip), rold(jp), rold(ep[1]));
+            }
+        }
+    }
+    *dua = ua;
+}
+
 // ---- combine --------------------------------------------------------------------
 struct FinalArgs {
     int ntrial, nptpt, ewald, lsurf, nblk;
@@ -409,13 +526,15 @@ struct FinalArgs {
     const double *rec_std;   // [ntrial] or null
     const double *spm_part;  // [ntrial][nblk][2] or null
     const double *dip;       // [3] sum q r of the accepted state
-    double *out;             // [ntrial][nptpt + 4]: du_twob(0:nptpt), du_rec, du_tot, overlap
+    ChainArgs chain;
+    double *out;             // [ntrial][nptpt + 6]: du_twob(0:nptpt), du_rec, du_tot, overlap,
+                             // du_bond, du_angle
 };
 
 __global__ void k_mc_final(McArgs a, FinalArgs f) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= f.ntrial) return;
-    double *o = f.out + (size_t)t * (f.nptpt + 4);
+    double *o = f.out + (size_t)t * (f.nptpt + 6);
     int ovl = f.flag[t];
     const double *un = f.tw + (size_t)t * 2 * f.nptpt, *uo = un + f.nptpt;
     double tn = 0.0, to = 0.0;
@@ -454,9 +573,17 @@ __global__ void k_mc_final(McArgs a, FinalArgs f) {
             du_tot = du_tot + du_rec;
         }
     }
+    double du_bond = 0.0, du_angle = 0.0;
+    if (!ovl && f.chain.nn) {
+        mc_bonded(a, f.chain, t, &du_bond, &du_angle);
+        du_tot = __dadd_rn(du_tot, du_bond);
+        if (f.chain.angles) du_tot = __dadd_rn(du_tot, du_angle);
+    }
     o[f.nptpt + 1] = du_rec;
     o[f.nptpt + 2] = du_tot;
     o[f.nptpt + 3] = ovl;
+    o[f.nptpt + 4] = du_bond;
+    o[f.nptpt + 5] = du_angle;
 }
 
 __global__ void k_mc_flags(const int *__restrict__ ip, int n, unsigned char *__restrict__ lptm, unsigned char v) {
@@ -512,12 +639,12 @@ static int mc_reserve(mg_handle *h, int ntrial, int nptm) {
         m->d_spm = nullptr;
         MG_CUDA(h, cudaMalloc(&m->d_tw, sizeof(double) * 2 * MG_MAX_NPTPT * (size_t)ct));
         MG_CUDA(h, cudaMalloc(&m->d_rec, sizeof(double) * (size_t)ct));
-        MG_CUDA(h, cudaMalloc(&m->d_out, sizeof(double) * (MG_MAX_NPTPT + 5) * (size_t)ct));
+        MG_CUDA(h, cudaMalloc(&m->d_out, sizeof(double) * (MG_MAX_NPTPT + 7) * (size_t)ct));
         MG_CUDA(h, cudaMalloc(&m->d_flag, sizeof(int) * (size_t)ct));
         if (h->ewald == MG_EWALD_SPM)
             MG_CUDA(h, cudaMalloc(&m->d_spm, sizeof(double) * 2 * kMcMaxSpmBlocks * (size_t)ct));
         m->cap_trial = ct;
-        m->h_out.resize((size_t)(MG_MAX_NPTPT + 5) * ct);
+        m->h_out.resize((size_t)(MG_MAX_NPTPT + 7) * ct);
     }
     if (tm > m->cap_tm) {
         size_t c = std::max(tm, 2 * m->cap_tm);
@@ -665,6 +792,14 @@ static int mc_launch(mg_handle *h, int ntrial, int nptm, bool flags, bool store_
     f.dip = m->d_dip;
     f.out = m->d_out;
     f.nblk = 1;
+    f.chain.nn = h->d_chain;
+    f.chain.bk = h->d_bond_k;
+    f.chain.beq = h->d_bond_eq;
+    f.chain.bp = h->d_bond_p;
+    f.chain.ak = h->d_angle_k;
+    f.chain.aeq = h->d_angle_eq;
+    f.chain.ap = h->d_angle_p;
+    f.chain.angles = h->chain_angles;
     int nl = 2;
     if (h->ewald == MG_EWALD_STD) {
         StdArgs s;
@@ -712,7 +847,7 @@ int mg_mc_dutotal(mg_handle *h, int nptm, const int32_t *ipnptm, const double *r
     if (flags) k_mc_flags<<<(nptm + 255) / 256, 256, 0, h->st>>>(m->d_ip, nptm, m->d_lptm, 1);
     MG_TRY(mc_launch(h, 1, nptm, flags, true));
     if (flags) k_mc_flags<<<(nptm + 255) / 256, 256, 0, h->st>>>(m->d_ip, nptm, m->d_lptm, 0);
-    int nv = h->nptpt + 4;
+    int nv = h->nptpt + 6;
     MG_CUDA(h, cudaMemcpyAsync(m->h_out.data(), m->d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, h->st));
     MG_TRY(mg_check_device_error(h));
     const double *o = m->h_out.data();
@@ -770,7 +905,7 @@ int mg_mc_batch(mg_handle *h, int ntrial, const int32_t *ip, const double *rt, d
     MG_CUDA(h, cudaMemcpyAsync(m->d_ip, ip, sizeof(int) * ntrial, cudaMemcpyHostToDevice, h->st));
     MG_CUDA(h, cudaMemcpyAsync(m->d_rt, rt, sizeof(double) * 3 * ntrial, cudaMemcpyHostToDevice, h->st));
     MG_TRY(mc_launch(h, ntrial, 1, false, false));
-    int nv = h->nptpt + 4;
+    int nv = h->nptpt + 6;
     MG_CUDA(h, cudaMemcpyAsync(m->h_out.data(), m->d_out, sizeof(double) * nv * (size_t)ntrial,
                                cudaMemcpyDeviceToHost, h->st));
     MG_TRY(mg_check_device_error(h));

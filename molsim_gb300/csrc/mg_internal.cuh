@@ -124,6 +124,12 @@ struct mg_handle {
     int nangle = 0;
     int *d_angle_ijk = nullptr, *d_angle_p = nullptr, *d_angle_off = nullptr, *d_angle_list = nullptr;
     double *d_angle_k = nullptr, *d_angle_eq = nullptr;
+    // chain table for MC trial moves (DUBond/DUAngle), 5 ints per particle:
+    // lower and upper neighbour (1-based, 0 none; bond b joins lower bond_ip
+    // and upper bond_jp), the bond to each (-1 none), the angle with the
+    // particle as vertex (-1 none); chain_angles: some angle has k != 0
+    int *d_chain = nullptr;
+    int chain_angles = 0;
 
     // ---- standard Ewald ----------------------------------------------------
     int nkvec = 0;

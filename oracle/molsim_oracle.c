@@ -464,6 +464,11 @@ struct orc_sys {
     int *angle_jm, *angle_ip, *angle_jp, *angle_p;
     double *angle_k, *angle_eq;
     double u_angle;
+    /* chain neighbours for DUBond/DUAngle (bondnn of the reference, from the
+       bond list: bond b joins lower bond_ip and upper bond_jp), the bond to
+       each neighbour, the angle with each particle as vertex (0-based, -1 none) */
+    int *nn_lo, *nn_up, *bond_lo, *bond_up, *angle_at;
+    double du_bond, du_angle;
     /* state */
     double *ro, *force, *forceo, *u_twob, *utwobnew, *utwobold;
     double u_tot, u_rec, u_bond, virial;
@@ -692,6 +697,20 @@ int orc_create(const mg_params *p, orc_sys **out) {
         s->bond_k = xcalloc(s->nbond, sizeof(double)); memcpy(s->bond_k, p->bond_k, sizeof(double) * s->nbond);
         s->bond_eq = xcalloc(s->nbond, sizeof(double)); memcpy(s->bond_eq, p->bond_eq, sizeof(double) * s->nbond);
     }
+    s->nn_lo = xcalloc(s->np, sizeof(int));
+    s->nn_up = xcalloc(s->np, sizeof(int));
+    s->bond_lo = xcalloc(s->np, sizeof(int));
+    s->bond_up = xcalloc(s->np, sizeof(int));
+    s->angle_at = xcalloc(s->np, sizeof(int));
+    for (int i = 0; i < s->np; ++i) s->bond_lo[i] = s->bond_up[i] = s->angle_at[i] = -1;
+    for (int b = 0; b < s->nbond; ++b) {
+        int i = p->bond_ip[b], j = p->bond_jp[b];   /* 1-based */
+        s->nn_up[i - 1] = j;
+        s->bond_up[i - 1] = b;
+        s->nn_lo[j - 1] = i;
+        s->bond_lo[j - 1] = b;
+    }
+    for (int a = 0; a < p->nangle; ++a) s->angle_at[p->angle_ip[a] - 1] = a;
     s->nangle = p->nangle;
     if (s->nangle > 0) {
         size_t na = (size_t)s->nangle;
@@ -728,6 +747,7 @@ void orc_destroy(orc_sys *s) {
     void *ptrs[] = {s->iptpn, s->iptpt, s->az, s->ubuf, s->r2umin, s->r2atat, s->iubuflow,
                     s->bond_ip, s->bond_jp, s->bond_p, s->bond_k, s->bond_eq,
                     s->angle_jm, s->angle_ip, s->angle_jp, s->angle_p, s->angle_k, s->angle_eq,
+                    s->nn_lo, s->nn_up, s->bond_lo, s->bond_up, s->angle_at,
                     s->ro, s->force, s->forceo, s->u_twob, s->utwobnew, s->utwobold,
                     s->nneighpn, s->jpnlist, s->drosum, s->ipnext, s->ipprev, s->cellip,
                     s->kfac, s->eikx, s->eiky, s->eikz, s->eikyzm, s->eikyzp, s->eikr, s->sumeikr,
@@ -1916,8 +1936,113 @@ static void du_ewald_surf(orc_sys *s) {
     s->du_rec = s->du_rec + term;
 }
 
-/* DUTotal, denergy.F90:98-215 with DUTwoBody (:246-286) and DUTwoBodyEwald
-   (:1240-1270), charged monoatomic branch. */
+/* position of particle jp (1-based) in the moving list, 0-based (iptmpn) */
+static int iptmpn(const orc_sys *s, int jp) {
+    for (int i = 0; i < s->nptm; ++i)
+        if (s->ipnptm[i] == jp) return i;
+    return -1;
+}
+
+#define ROTM(i) (&s->rotm[3 * (i)])
+#define ROP(ip) (&s->ro[3 * ((ip) - 1)])
+
+/* DUBondSub: bond between moving particle iploc (old ro(ip)) and a
+   neighbour at ronew (new) / roold (old), parameters of bond b */
+static void du_bond_sub(orc_sys *s, int iploc, int ip, int b, const double *ronew, const double *roold) {
+    double dx = ROTM(iploc)[0] - ronew[0], dy = ROTM(iploc)[1] - ronew[1], dz = ROTM(iploc)[2] - ronew[2], r2new;
+    pbcr2(s, &dx, &dy, &dz, &r2new);
+    dx = ROP(ip)[0] - roold[0];
+    dy = ROP(ip)[1] - roold[1];
+    dz = ROP(ip)[2] - roold[2];
+    double r2old;
+    pbcr2(s, &dx, &dy, &dz, &r2old);
+    s->du_bond = s->du_bond + s->bond_k[b] * (powi(sqrt(r2new) - s->bond_eq[b], s->bond_p[b]) -
+                                              powi(sqrt(r2old) - s->bond_eq[b], s->bond_p[b]));
+}
+
+/* angle_rad, molaux.F90:836-846 */
+static double angle_rad(double x1, double y1, double z1, double x2, double y2, double z2) {
+    double term1 = x1 * x2 + y1 * y2 + z1 * z2;
+    double term2 = pow2(x1) + pow2(y1) + pow2(z1);
+    double term3 = pow2(x2) + pow2(y2) + pow2(z2);
+    double term = term1 / sqrt(term2 * term3);
+    return acos(fmax(-One, fmin(term, One)));
+}
+
+/* DUAngleSub: angle a (vertex 0) from old to new positions */
+static void du_angle_sub(orc_sys *s, int a, const double *nm, const double *n0, const double *np_,
+                         const double *om, const double *o0, const double *op) {
+    double dxm = n0[0] - nm[0], dym = n0[1] - nm[1], dzm = n0[2] - nm[2];
+    pbc(s, &dxm, &dym, &dzm);
+    double dxp = np_[0] - n0[0], dyp = np_[1] - n0[1], dzp = np_[2] - n0[2];
+    pbc(s, &dxp, &dyp, &dzp);
+    double thetanew = angle_rad(-dxm, -dym, -dzm, dxp, dyp, dzp);
+    dxm = o0[0] - om[0]; dym = o0[1] - om[1]; dzm = o0[2] - om[2];
+    pbc(s, &dxm, &dym, &dzm);
+    dxp = op[0] - o0[0]; dyp = op[1] - o0[1]; dzp = op[2] - o0[2];
+    pbc(s, &dxp, &dyp, &dzp);
+    double thetaold = angle_rad(-dxm, -dym, -dzm, dxp, dyp, dzp);
+    s->du_angle = s->du_angle + s->angle_k[a] * (powi(thetanew - s->angle_eq[a], s->angle_p[a]) -
+                                                 powi(thetaold - s->angle_eq[a], s->angle_p[a]));
+}
+
+/* DUBond (denergy.F90:2893-2955) and DUAngle (:2962-3040): the bonds and
+   angles of the moving chain segments.  A moving neighbour's new position is
+   taken from the previous / next entry of the moving list inside the list
+   and from its own entry at the ends, as the reference does (its routines
+   assume the moving segments form one string). */
+static void du_bonded(orc_sys *s) {
+    s->du_bond = Zero;
+    s->du_angle = Zero;
+    int nptm = s->nptm;
+    for (int iploc = 0; iploc < nptm; ++iploc) {
+        int ip = s->ipnptm[iploc];
+        int jm = s->nn_lo[ip - 1], jp = s->nn_up[ip - 1];
+        if (jm == 0 && jp == 0) continue;   /* not a chain segment */
+        if (jm != 0) {
+            int b = s->bond_lo[ip - 1];
+            if (!s->lptm[jm - 1]) du_bond_sub(s, iploc, ip, b, ROP(jm), ROP(jm));
+            else du_bond_sub(s, iploc, ip, b, iploc > 0 ? ROTM(iploc - 1) : ROTM(iptmpn(s, jm)), ROP(jm));
+        }
+        if (jp != 0 && !s->lptm[jp - 1]) du_bond_sub(s, iploc, ip, s->bond_up[ip - 1], ROP(jp), ROP(jp));
+    }
+    s->du_tot = s->du_tot + s->du_bond;
+    int any = 0;
+    for (int a = 0; a < s->nangle; ++a) any |= s->angle_k[a] != Zero;
+    if (!any) return;
+    for (int iploc = 0; iploc < nptm; ++iploc) {
+        int ip = s->ipnptm[iploc];
+        int jm = s->nn_lo[ip - 1], jp = s->nn_up[ip - 1];
+        if (jm == 0 && jp == 0) continue;
+        int jmm = jm ? s->nn_lo[jm - 1] : 0, jpp = jp ? s->nn_up[jp - 1] : 0;
+        if (jm != 0 && jp != 0 && s->angle_at[ip - 1] >= 0) {
+            int a = s->angle_at[ip - 1];
+            const double *nm, *np_;
+            if (s->lptm[jm - 1]) {
+                if (s->lptm[jp - 1]) {
+                    int inner = iploc > 0 && iploc < nptm - 1;
+                    nm = inner ? ROTM(iploc - 1) : ROTM(iptmpn(s, jm));
+                    np_ = inner ? ROTM(iploc + 1) : ROTM(iptmpn(s, jp));
+                } else {
+                    nm = iploc > 0 ? ROTM(iploc - 1) : ROTM(iptmpn(s, jm));
+                    np_ = ROP(jp);
+                }
+            } else {
+                nm = ROP(jm);
+                np_ = s->lptm[jp - 1] ? (iploc < nptm - 1 ? ROTM(iploc + 1) : ROTM(iptmpn(s, jp))) : ROP(jp);
+            }
+            du_angle_sub(s, a, nm, ROTM(iploc), np_, ROP(jm), ROP(ip), ROP(jp));
+        }
+        if (jm != 0 && jmm != 0 && !s->lptm[jm - 1] && s->angle_at[jm - 1] >= 0)
+            du_angle_sub(s, s->angle_at[jm - 1], ROP(jmm), ROP(jm), ROTM(iploc), ROP(jmm), ROP(jm), ROP(ip));
+        if (jp != 0 && jpp != 0 && !s->lptm[jp - 1] && s->angle_at[jp - 1] >= 0)
+            du_angle_sub(s, s->angle_at[jp - 1], ROTM(iploc), ROP(jp), ROP(jpp), ROP(ip), ROP(jp), ROP(jpp));
+    }
+    s->du_tot = s->du_tot + s->du_angle;
+}
+
+/* DUTotal, denergy.F90:98-215 with DUTwoBody (:246-286), DUTwoBodyEwald
+   (:1240-1270), DUBond and DUAngle; charged monoatomic branch. */
 int orc_dutotal(orc_sys *s, int32_t nptm, const int32_t *ipnptm, const double *rotm,
                 double *du_twob, double *du_rec, double *du_tot, int32_t *lhsoverlap) {
     if (nptm < 1 || nptm > s->np) return MG_ERR_ARG;
@@ -1933,6 +2058,8 @@ int orc_dutotal(orc_sys *s, int32_t nptm, const int32_t *ipnptm, const double *r
     }
     s->du_tot = Zero;
     s->du_rec = Zero;
+    s->du_bond = Zero;
+    s->du_angle = Zero;
     double du_tw[64];
     int ntw = s->nptpt + 1;
     for (int k = 0; k < ntw && k < 64; ++k) du_tw[k] = Zero;
@@ -1954,6 +2081,7 @@ int orc_dutotal(orc_sys *s, int32_t nptm, const int32_t *ipnptm, const double *r
             s->du_rec = s->EpsiFourPi * s->du_rec;
             s->du_tot = s->du_tot + s->du_rec;
         }
+        if (s->nbond > 0) du_bonded(s);
         s->trial_ok = 1;
     }
     if (du_twob) for (int k = 0; k < ntw; ++k) du_twob[k] = overlap ? Zero : du_tw[k];
@@ -1999,6 +2127,8 @@ int orc_accept(orc_sys *s) {
         }
     }
     s->u_tot = s->u_tot + s->du_tot;
+    s->u_bond = s->u_bond + s->du_bond;
+    s->u_angle = s->u_angle + s->du_angle;
     s->trial_ok = 0;
     return 0;
 }

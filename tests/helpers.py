@@ -80,3 +80,17 @@ def utotal_errors(g, r, nptpt):
     e["force_max"] = force_err(g["forceo"], r["forceo"])
     e["force_rms"] = force_rms_err(g["forceo"], r["forceo"])
     return e
+
+
+def chain_trial(rng, s, ro, chains, nseg, step=1.0):
+    """A trial on the chain beads (particles 1 .. chains*nseg, nseg per
+    chain): one bead, or a string of 2-4 consecutive beads of one chain in
+    chain order, each displaced by up to step."""
+    c = int(rng.integers(chains))
+    n = 1 if rng.random() < 0.4 else int(rng.integers(2, 5))
+    i0 = int(rng.integers(nseg - n + 1))
+    ips = c * nseg + i0 + np.arange(n)
+    L = s.boxlen[0]
+    new = ro[ips] + rng.uniform(-step, step, (n, 3))
+    new -= L * np.round(new / L)
+    return ips + 1, new

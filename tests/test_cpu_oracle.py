@@ -14,6 +14,7 @@ import pytest
 
 from molsim_gb300 import Engine, abi, configs, units
 from molsim_gb300.system import Species, System, iptpt_matrix
+from tests.helpers import chain_trial
 
 MADELUNG_NACL = 1.747564594633182
 
@@ -202,6 +203,7 @@ def test_forces_are_minus_energy_gradient(orc, ewald):
     dict(ewald=abi.MG_EWALD_SPM),
     dict(ewald=abi.MG_EWALD_STD, ncut=5, lsurf=1),
     dict(ewald=abi.MG_EWALD_SPM, txintlist=abi.MG_CELLLIST),
+    dict(ewald=abi.MG_EWALD_SPM, chains=4, nseg=8, angle_kt=0.5),
 ])
 def test_dutotal_accumulates_to_utotal(orc, kw):
     """u%tot after n accepted moves equals u%tot before plus the sum of the
@@ -233,6 +235,58 @@ def test_dutotal_accumulates_to_utotal(orc, kw):
     e2.NList("write")
     u1 = e2.UTotal()["u_tot"]
     assert abs((u0 + acc) - u1) < 1e-9 * abs(u1)
+
+
+def test_dutotal_bonded_terms_match_fresh_energies(orc):
+    """DUBond and DUAngle (denergy.F90:2893-3077): for single beads and
+    strings of beads of a chain, du%tot - du%twob(0) - du%rec equals the
+    change of u%bond + u%angle evaluated from scratch (UBond, UAngle), and
+    the accepted du%tot add up to the final UTotal (ucheck)."""
+    chains, nseg = 4, 8
+    # the linked cells stay exact however far the beads wander (a Verlet
+    # list would need its displacement check)
+    s = configs.small_system(seed=14, mode=abi.MG_MC, chains=chains, nseg=nseg, angle_kt=0.7,
+                             txintlist=abi.MG_CELLLIST)
+    s.build_table(orc.orc_pot_twobody_tab)
+
+    def fresh(ro):
+        e = Engine(s, lib=orc, prefix="orc_")
+        e.SetPositions(ro.reshape(-1))
+        e.NList("write")
+        e.UTotal()
+        return e.EnergyTerms()
+
+    e = Engine(s, lib=orc, prefix="orc_")
+    e.SetPositions(s.ro_flat())
+    e.NList("write")
+    u0 = e.UTotal()["u_tot"]
+    t_old = fresh(s.ro)
+    rng = np.random.default_rng(14)
+    ro = s.ro.copy()
+    acc, nacc, nstr = 0.0, 0, 0
+    for it in range(40):
+        ips, new = chain_trial(rng, s, ro, chains, nseg)
+        du, ovl = e.DUTotal(ips, new)
+        if ovl:
+            continue
+        ro_new = ro.copy()
+        ro_new[ips - 1] = new
+        t_new = fresh(ro_new)
+        dub = du["du_tot"] - du["du_twob"][0] - du["du_rec"]
+        ref = (t_new["u_bond"] + t_new["u_angle"]) - (t_old["u_bond"] + t_old["u_angle"])
+        scale = abs(t_old["u_bond"]) + abs(t_old["u_angle"]) + abs(t_old["u_tot"])
+        assert abs(dub - ref) <= 1e-10 * scale, (it, dub, ref)
+        if rng.random() < 0.7:
+            e.MCUpdate()
+            ro, t_old = ro_new, t_new
+            acc += du["du_tot"]
+            nacc += 1
+            nstr += len(ips) > 1
+    assert nacc >= 15 and nstr >= 5
+    u1 = fresh(ro)["u_tot"]
+    assert abs((u0 + acc) - u1) < 1e-9 * abs(u1)
+    t = e.EnergyTerms()
+    assert abs(t["u_bond"] - fresh(ro)["u_bond"]) < 1e-9 * abs(u1)
 
 
 def test_angle_forces_are_minus_energy_gradient(orc):

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from molsim_gb300 import Engine, abi, configs
-from tests.helpers import prepared, rel
+from tests.helpers import chain_trial, prepared, rel
 
 pytestmark = pytest.mark.gpu
 
@@ -28,6 +28,7 @@ CASES = [
     ("std_cell", dict(seed=65, ewald=abi.MG_EWALD_STD, ncut=5, txintlist=abi.MG_CELLLIST)),
     ("no_ewald_cell", dict(seed=66, ewald=abi.MG_EWALD_NONE, txintlist=abi.MG_CELLLIST)),
     ("spme_bonds_vlist", dict(seed=67, chains=3, nseg=8)),
+    ("spme_angles_cell", dict(seed=68, chains=4, nseg=8, angle_kt=0.6, txintlist=abi.MG_CELLLIST)),
 ]
 
 
@@ -140,3 +141,55 @@ def test_mixed_form_trials_near_fp64(orc, gpu_lib):
     ok = ~o64
     err = np.abs(dmx[ok] - d64[ok])
     assert np.sqrt((err ** 2).mean()) <= 1e-5 * np.sqrt((d64[ok] ** 2).mean())
+
+
+@pytest.mark.parametrize("txintlist", [abi.MG_CELLLIST, abi.MG_VLIST], ids=["cell", "vlist"])
+def test_chain_string_trials_match_oracle(txintlist, orc, gpu_lib):
+    """DUBond and DUAngle (denergy.F90:2893-3077) on the GPU: single chain
+    beads and strings of 2-4 consecutive beads of one chain, against the
+    oracle trial by trial (du%tot within 1e-10 of the energy scale), then
+    the same moves accepted on both and the GPU's ucheck."""
+    chains, nseg = 4, 8
+    s = prepared(configs.small_system(seed=69, mode=MC, chains=chains, nseg=nseg, angle_kt=0.6,
+                                      txintlist=txintlist), orc)
+    ref, gpu, u_ref, u_gpu = _pair(s, orc)
+    t0 = ref.EnergyTerms()
+    scale = abs(t0["u_twob0"]) + abs(t0["u_rec"]) + abs(t0["u_bond"]) + abs(t0["u_angle"]) + 1.0
+    rng = np.random.default_rng(69)
+    ro = s.ro.copy()
+    acc, nacc, nstr = 0.0, 0, 0
+    step = 1.0 if txintlist == abi.MG_CELLLIST else 0.15   # Verlet list: stay inside drnlist
+    for it in range(30):
+        ips, new = chain_trial(rng, s, ro, chains, nseg, step)
+        r, ovl_r = ref.DUTotal(ips, new)
+        g, ovl_g = gpu.DUTotal(ips, new)
+        assert ovl_g == ovl_r, it
+        if ovl_r:
+            continue
+        assert abs(g["du_tot"] - r["du_tot"]) <= 1e-10 * scale, (it, g["du_tot"], r["du_tot"])
+        bonded_g = g["du_tot"] - g["du_twob"][0] - g["du_rec"]
+        bonded_r = r["du_tot"] - r["du_twob"][0] - r["du_rec"]
+        assert abs(bonded_g - bonded_r) <= 1e-10 * scale, it
+        if it < 8 or rng.random() < 0.5:
+            ref.MCUpdate()
+            gpu.MCUpdate()
+            ro[ips - 1] = new
+            acc += g["du_tot"]
+            nacc += 1
+            nstr += len(ips) > 1
+    assert nacc >= 8 and nstr >= 3
+    assert np.array_equal(gpu.GetPositions(), ref.GetPositions())
+    u1 = gpu.UTotal()
+    assert abs((u_gpu["u_tot"] + acc) - u1["u_tot"]) <= 1e-9 * scale
+    # batched single-bead trials on the chain beads
+    n = 48
+    ips = rng.integers(chains * nseg, size=n) + 1
+    L = s.boxlen[0]
+    new = ro[ips - 1] + rng.uniform(-step, step, (n, 3))
+    new -= L * np.round(new / L)
+    du, ovl = gpu.DUTotalBatch(ips, new)
+    for t in range(n):
+        r, o = ref.DUTotal([ips[t]], new[t:t + 1])
+        assert bool(ovl[t]) == o, t
+        if not o:
+            assert abs(du[t] - r["du_tot"]) <= 1e-10 * scale, t
