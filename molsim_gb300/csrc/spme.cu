@@ -370,7 +370,13 @@ __global__ void k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__re
     }
     int id = ((((c[2] >> a.lB) << a.lnb) + (c[1] >> a.lB)) << a.lnb) + (c[0] >> a.lB);
     a.brick[p] = id;
-    a.rank[p] = atomicAdd(&a.count[id], 1);
+    // rank among the brick's particles: one atomic per brick and warp (chain
+    // beads, numbered along the chain, share bricks within a warp)
+    unsigned peers = __match_any_sync(__activemask(), id);
+    int lane = threadIdx.x & 31, leader = __ffs(peers) - 1, base = 0;
+    if (lane == leader) base = atomicAdd(&a.count[id], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    a.rank[p] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // ---- brick-sorted spread -------------------------------------------------------
