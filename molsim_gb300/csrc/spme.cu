@@ -343,37 +343,101 @@ struct SplineArgs {
     double fac;
 };
 
+// The spline record of a particle: the B-spline values along x, y, z, then
+// their derivatives (order values each), padded to a multiple of four values
+// so that records start on 16-byte boundaries.  One record per particle:
+// the spread and the gather read a particle's weights from one or a few
+// sectors instead of one sector per weight.
+__host__ __device__ constexpr int spl_rec(int order) { return (6 * order + 3) & ~3; }
+
+template <typename T, int N> __device__ __forceinline__ void store_rec(T *__restrict__ dst, const T (&r)[N]) {
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int k = 0; k < N / 4; ++k)
+            reinterpret_cast<float4 *>(dst)[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N / 2; ++k) reinterpret_cast<double2 *>(dst)[k] = make_double2(r[2 * k], r[2 * k + 1]);
+    }
+}
+
+// the first N values of a record (16-byte aligned)
+template <typename T, int N> __device__ __forceinline__ void load_rec(const T *__restrict__ src, T (&r)[N]) {
+    constexpr int VW = 16 / sizeof(T), NV = N / VW;
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            float4 v = reinterpret_cast<const float4 *>(src)[k];
+            r[4 * k] = v.x;
+            r[4 * k + 1] = v.y;
+            r[4 * k + 2] = v.z;
+            r[4 * k + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double2 v = reinterpret_cast<const double2 *>(src)[k];
+            r[2 * k] = v.x;
+            r[2 * k + 1] = v.y;
+        }
+    }
+#pragma unroll
+    for (int k = NV * VW; k < N; ++k) r[k] = src[k];
+}
+
 // Spline data of every particle, once per call (the only FP64 of the mesh
 // path: position -> mesh coordinate).  Layout: corner[m*np + p] (stamp
-// upper corner, meshmax of the reference), w and dw[(m*ORDER + i)*np + p].
+// upper corner, meshmax of the reference); the record of particle p at
+// w[p * spl_rec(ORDER)].
 template <typename T, int ORDER>
-__global__ void k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__restrict__ w,
-                                 T *__restrict__ dw) {
+__global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__restrict__ w) {
     mg_pdl_begin();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.np) return;
+    bool valid = p < a.np;
+    if (!valid) p = a.np - 1;   // a tail lane recomputes the last particle and stores nothing
     int c[3];
+    constexpr int S = spl_rec(ORDER);
+    T r[S];
+#pragma unroll
+    for (int k = 6 * ORDER; k < S; ++k) r[k] = (T)0;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         double pos = a.dkdr[m] * a.ro[3 * p + m];
         double fl = floor(pos);
         int mm = (int)fl % a.n;
         c[m] = mm < 0 ? mm + a.n : mm;
-        corner[m * a.np + p] = c[m];
+        if (valid) corner[m * a.np + p] = c[m];
         T v[ORDER], d[ORDER];
         bspline_o<T, ORDER>((T)(pos - fl), v, d);
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            w[(size_t)(m * ORDER + i) * a.np + p] = v[i];
-            dw[(size_t)(m * ORDER + i) * a.np + p] = d[i];
+            r[m * ORDER + i] = v[i];
+            r[3 * ORDER + m * ORDER + i] = d[i];
         }
     }
+    int lane = threadIdx.x & 31;
+    if constexpr (sizeof(T) == 4 && S <= 48) {
+        // the warp's 32 records are contiguous in memory: staged in shared
+        // memory (at most 48 KB per block), then written as coalesced
+        // 16-byte stores
+        __shared__ float4 st[8][32 * S / 4];
+        float4 *sw = st[threadIdx.x >> 5];
+        store_rec<T, S>(reinterpret_cast<T *>(sw) + lane * S, r);
+        __syncwarp();
+        int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31), nv = min(32, a.np - p0);   // p is clamped in the tail
+        float4 *dst = reinterpret_cast<float4 *>(w + (size_t)p0 * S);
+        for (int k = lane; k < nv * S / 4; k += 32) dst[k] = sw[k];
+    } else if (valid) {
+        store_rec<T, S>(w + (size_t)p * S, r);
+    }
     int id = ((((c[2] >> a.lB) << a.lnb) + (c[1] >> a.lB)) << a.lnb) + (c[0] >> a.lB);
+    unsigned vm = __ballot_sync(0xffffffffu, valid);
+    if (!valid) return;
     a.brick[p] = id;
     // rank among the brick's particles: one atomic per brick and warp (chain
     // beads, numbered along the chain, share bricks within a warp)
-    unsigned peers = __match_any_sync(__activemask(), id);
-    int lane = threadIdx.x & 31, leader = __ffs(peers) - 1, base = 0;
+    unsigned peers = __match_any_sync(vm, id);
+    int leader = __ffs(peers) - 1, base = 0;
     if (lane == leader) base = atomicAdd(&a.count[id], __popc(peers));
     base = __shfl_sync(peers, base, leader);
     a.rank[p] = base + __popc(peers & ((1u << lane) - 1u));
@@ -518,11 +582,13 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
             stg->off[lane] = cx | (cy << 8) | (cz << 16);
             T qp = (T)az[p];
             T *rec = stg->w[lane];
+            T r[3 * ORDER];
+            load_rec<T, 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
 #pragma unroll
             for (int i = 0; i < ORDER; ++i) {
-                rec[i] = qp * w[(size_t)i * np + p];
-                rec[ORDER + i] = w[(size_t)(ORDER + i) * np + p];
-                rec[2 * ORDER + i] = w[(size_t)(2 * ORDER + i) * np + p];
+                rec[i] = qp * r[i];
+                rec[ORDER + i] = r[ORDER + i];
+                rec[2 * ORDER + i] = r[2 * ORDER + i];
             }
         }
         __syncwarp();
@@ -607,11 +673,13 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, 
         int cx = corner[p] - ox, cy = corner[np + p] - oy, cz = corner[2 * np + p] - oz;
         base = (cz * t + cy) * t + cx;
         float qs = (float)az[p] * b.fx_scale;
+        float r[3 * ORDER];
+        load_rec<float, 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            wx[i] = qs * w[(size_t)i * np + p];
-            wy[i] = w[(size_t)(ORDER + i) * np + p];
-            wz[i] = w[(size_t)(2 * ORDER + i) * np + p];
+            wx[i] = qs * r[i];
+            wy[i] = r[ORDER + i];
+            wz[i] = r[2 * ORDER + i];
         }
     }
     __syncwarp();
@@ -658,7 +726,7 @@ template <int ORDER> void spread_lane_attr() {
 template <typename T, bool MIXED, int ORDER>
 __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
                                                     const int *__restrict__ corner, const T *__restrict__ w,
-                                                    const T *__restrict__ dw, const T *__restrict__ Q,
+                                                    const T *__restrict__ Q,
                                                     T kx, T ky, T kz, double *__restrict__ force,
                                                     long long *__restrict__ ffx) {
     mg_pdl_begin();
@@ -671,19 +739,20 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     int np = a.np, n = a.n, mn = n - 1;
     T e0 = 0, e1 = 0, e2 = 0;
     if (act) {
+        const T *rec = w + (size_t)p * spl_rec(ORDER);   // values x, y, z, then derivatives x, y, z
         T vy[ORDER], dy[ORDER];
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            vy[i] = w[(size_t)(ORDER + i) * np + p];
-            dy[i] = dw[(size_t)(ORDER + i) * np + p];
+            vy[i] = rec[ORDER + i];
+            dy[i] = rec[4 * ORDER + i];
         }
-        T vx = w[(size_t)j * np + p], dx = dw[(size_t)j * np + p];
+        T vx = rec[j], dx = rec[3 * ORDER + j];
         int c0 = corner[p], c1 = corner[np + p], c2 = corner[2 * np + p];
         const T *col = Q + ((c0 - j) & mn);
         T A = 0, B = 0, C = 0;
 #pragma unroll
         for (int iz = 0; iz < ORDER; ++iz) {
-            T vz = w[(size_t)(2 * ORDER + iz) * np + p], dz = dw[(size_t)(2 * ORDER + iz) * np + p];
+            T vz = rec[2 * ORDER + iz], dz = rec[5 * ORDER + iz];
             const T *pl = col + ((size_t)((c2 - iz) & mn) << (2 * a.n_log));
             T r0 = 0, r1 = 0;
 #pragma unroll
@@ -768,9 +837,9 @@ template <typename T, typename ACC, int ORDER>
 void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const BrickArgs &bk) {
     int np = h->np;
     int *corner = h->d_corner;
-    T *w = (T *)h->d_spl_w, *dw = (T *)h->d_spl_dw;
+    T *w = (T *)h->d_spl_w;
     if (which == 0) {
-        mg_launch_pdl(k_spline_prepare<T, ORDER>, (np + 255) / 256, 256, 0, h->st, sa, corner, w, dw);
+        mg_launch_pdl(k_spline_prepare<T, ORDER>, (np + 255) / 256, 256, 0, h->st, sa, corner, w);
     } else if (which == 1 && sizeof(T) == 4) {   // mixed form
         int wpb = h->spread_wpb_lane;
         int grid = (h->max_items + wpb - 1) / wpb;
@@ -796,7 +865,7 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
           kz = (T)(h->dkdr[2] * h->EpsiFourPi);
         constexpr int G = ORDER <= 8 ? 8 : 16;
         mg_launch_pdl(k_gather_grp<T, sizeof(T) == 4, ORDER>, (unsigned)(((long)np * G + 255) / 256), 256, 0,
-                      h->st, sa, h->d_perm, corner, w, (const T *)h->d_spl_dw, (const T *)h->d_Q, kx, ky, kz,
+                      h->st, sa, h->d_perm, corner, w, (const T *)h->d_Q, kx, ky, kz,
                       h->d_force, h->d_ffx);
     }
 }
@@ -1382,8 +1451,7 @@ int mg_spme_init(mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_Qfx, sizeof(long long) * (size_t)n * n * n));
     MG_CUDA(h, cudaMemset(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n));
     MG_CUDA(h, cudaMalloc(&h->d_corner, sizeof(int) * 3 * (size_t)h->np));
-    MG_CUDA(h, cudaMalloc(&h->d_spl_w, tsz * 3 * h->order * (size_t)h->np));
-    MG_CUDA(h, cudaMalloc(&h->d_spl_dw, tsz * 3 * h->order * (size_t)h->np));
+    MG_CUDA(h, cudaMalloc(&h->d_spl_w, tsz * spl_rec(h->order) * (size_t)h->np));   // spline records
     spread_attrs<float, int>();
     spread_attrs<double, long long>();
     spread_lane_attr<4>(); spread_lane_attr<5>(); spread_lane_attr<6>(); spread_lane_attr<7>(); spread_lane_attr<8>();
