@@ -162,7 +162,6 @@ struct mg_handle {
     int *d_brick_istart = nullptr, *d_item_brick = nullptr;   // spread work items per brick
     int spread_m = 32, max_items = 0;
     void *d_tiles = nullptr;        // per-brick spread tiles (mesh type)
-    int *d_corner = nullptr;        // [3][np] stamp corner per particle and dimension
     void *d_spl_w = nullptr;   // per particle: B-spline values x, y, z, derivatives x, y, z (padded to 4)
     double *d_Qref = nullptr;       // MC: charge mesh of the accepted state (FP64)
     double *d_phi = nullptr;        // MC: potential mesh of the accepted state

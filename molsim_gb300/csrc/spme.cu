@@ -343,12 +343,22 @@ struct SplineArgs {
     double fac;
 };
 
-// The spline record of a particle: the B-spline values along x, y, z, then
-// their derivatives (order values each), padded to a multiple of four values
-// so that records start on 16-byte boundaries.  One record per particle:
-// the spread and the gather read a particle's weights from one or a few
-// sectors instead of one sector per weight.
-__host__ __device__ constexpr int spl_rec(int order) { return (6 * order + 3) & ~3; }
+// The spline record of a particle: a head of four values (the stamp's
+// upper corner, 10 bits per axis, stored in the bits of the first value;
+// the charge; two unused), the B-spline values along x, y, z, then their
+// derivatives (order values each), padded to a multiple of four values so
+// that records start on 16-byte boundaries.  The spread and the gather read
+// a particle's corner, charge and weights from a few consecutive sectors.
+constexpr int kRecHead = 4;
+__host__ __device__ constexpr int spl_rec(int order) { return (kRecHead + 6 * order + 3) & ~3; }
+
+template <typename T> __device__ __forceinline__ T rec_put_corner(int c);
+template <> __device__ __forceinline__ float rec_put_corner<float>(int c) { return __int_as_float(c); }
+template <> __device__ __forceinline__ double rec_put_corner<double>(int c) {
+    return __longlong_as_double((long long)c);
+}
+__device__ __forceinline__ int rec_corner(float v) { return __float_as_int(v); }
+__device__ __forceinline__ int rec_corner(double v) { return (int)__double_as_longlong(v); }
 
 template <typename T, int N> __device__ __forceinline__ void store_rec(T *__restrict__ dst, const T (&r)[N]) {
     if constexpr (sizeof(T) == 4) {
@@ -386,11 +396,10 @@ template <typename T, int N> __device__ __forceinline__ void load_rec(const T *_
 }
 
 // Spline data of every particle, once per call (the only FP64 of the mesh
-// path: position -> mesh coordinate).  Layout: corner[m*np + p] (stamp
-// upper corner, meshmax of the reference); the record of particle p at
-// w[p * spl_rec(ORDER)].
+// path: position -> mesh coordinate): the record of particle p at
+// w[p * spl_rec(ORDER)], its corner the meshmax of the reference.
 template <typename T, int ORDER>
-__global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, int *__restrict__ corner, T *__restrict__ w) {
+__global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restrict__ w) {
     mg_pdl_begin();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = p < a.np;
@@ -399,22 +408,24 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, int *__res
     constexpr int S = spl_rec(ORDER);
     T r[S];
 #pragma unroll
-    for (int k = 6 * ORDER; k < S; ++k) r[k] = (T)0;
+    for (int k = kRecHead + 6 * ORDER; k < S; ++k) r[k] = (T)0;
+    r[2] = r[3] = (T)0;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         double pos = a.dkdr[m] * a.ro[3 * p + m];
         double fl = floor(pos);
         int mm = (int)fl % a.n;
         c[m] = mm < 0 ? mm + a.n : mm;
-        if (valid) corner[m * a.np + p] = c[m];
         T v[ORDER], d[ORDER];
         bspline_o<T, ORDER>((T)(pos - fl), v, d);
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            r[m * ORDER + i] = v[i];
-            r[3 * ORDER + m * ORDER + i] = d[i];
+            r[kRecHead + m * ORDER + i] = v[i];
+            r[kRecHead + 3 * ORDER + m * ORDER + i] = d[i];
         }
     }
+    r[0] = rec_put_corner<T>(c[0] | (c[1] << 10) | (c[2] << 20));
+    r[1] = (T)a.az[p];
     int lane = threadIdx.x & 31;
     if constexpr (sizeof(T) == 4 && S <= 48) {
         // the warp's 32 records are contiguous in memory: staged in shared
@@ -536,9 +547,7 @@ constexpr int kSpreadItem = 32;   // most particles per spread work item
 // exact, so the mesh does not depend on how particles fall into items or on
 // the order in which items run.
 template <typename T, typename ACC, int ORDER, int B>
-__global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, const int *__restrict__ corner,
-                                                                   const T *__restrict__ w,
-                                                                   const double *__restrict__ az, int np,
+__global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, const T *__restrict__ w,
                                                                    long long *__restrict__ Qfx) {
     constexpr int t = B + ORDER - 1, t3 = t * t * t, O3 = ORDER * ORDER * ORDER;
     constexpr int NPASS = (O3 + 31) / 32;
@@ -578,17 +587,18 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
         __syncwarp();
         if (lane < cnt) {   // stage one particle per lane
             int p = b.perm[q0 + lane];
-            int cx = corner[p] - ox, cy = corner[np + p] - oy, cz = corner[2 * np + p] - oz;
+            T r[kRecHead + 3 * ORDER];
+            load_rec<T, kRecHead + 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
+            int c = rec_corner(r[0]);
+            int cx = (c & 1023) - ox, cy = ((c >> 10) & 1023) - oy, cz = (c >> 20) - oz;
             stg->off[lane] = cx | (cy << 8) | (cz << 16);
-            T qp = (T)az[p];
+            T qp = r[1];
             T *rec = stg->w[lane];
-            T r[3 * ORDER];
-            load_rec<T, 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
 #pragma unroll
             for (int i = 0; i < ORDER; ++i) {
-                rec[i] = qp * r[i];
-                rec[ORDER + i] = r[ORDER + i];
-                rec[2 * ORDER + i] = r[2 * ORDER + i];
+                rec[i] = qp * r[kRecHead + i];
+                rec[ORDER + i] = r[kRecHead + ORDER + i];
+                rec[2 * ORDER + i] = r[kRecHead + 2 * ORDER + i];
             }
         }
         __syncwarp();
@@ -646,9 +656,7 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
 // added into the 64-bit fixed-point mesh with integer atomics, as in
 // k_spread_warp.
 template <int ORDER, int B>
-__global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, const int *__restrict__ corner,
-                                                                   const float *__restrict__ w,
-                                                                   const double *__restrict__ az, int np,
+__global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, const float *__restrict__ w,
                                                                    long long *__restrict__ Qfx) {
     mg_pdl_begin();
     constexpr int t = B + ORDER - 1, t3 = t * t * t;
@@ -670,16 +678,17 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, 
     int base = 0;
     if (act) {
         int p = b.perm[q];
-        int cx = corner[p] - ox, cy = corner[np + p] - oy, cz = corner[2 * np + p] - oz;
+        float r[kRecHead + 3 * ORDER];
+        load_rec<float, kRecHead + 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
+        int c = rec_corner(r[0]);
+        int cx = (c & 1023) - ox, cy = ((c >> 10) & 1023) - oy, cz = (c >> 20) - oz;
         base = (cz * t + cy) * t + cx;
-        float qs = (float)az[p] * b.fx_scale;
-        float r[3 * ORDER];
-        load_rec<float, 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
+        float qs = r[1] * b.fx_scale;
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            wx[i] = qs * r[i];
-            wy[i] = r[ORDER + i];
-            wz[i] = r[2 * ORDER + i];
+            wx[i] = qs * r[kRecHead + i];
+            wy[i] = r[kRecHead + ORDER + i];
+            wz[i] = r[kRecHead + 2 * ORDER + i];
         }
     }
     __syncwarp();
@@ -725,8 +734,7 @@ template <int ORDER> void spread_lane_attr() {
 // dM*M*M*phi (energy.F90:1255-1285); force -= q*E*dkdr*EpsiFourPi.
 template <typename T, bool MIXED, int ORDER>
 __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
-                                                    const int *__restrict__ corner, const T *__restrict__ w,
-                                                    const T *__restrict__ Q,
+                                                    const T *__restrict__ w, const T *__restrict__ Q,
                                                     T kx, T ky, T kz, double *__restrict__ force,
                                                     long long *__restrict__ ffx) {
     mg_pdl_begin();
@@ -736,23 +744,25 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     bool valid = g < a.np;
     bool act = valid && j < ORDER;
     int p = valid ? perm[g] : 0;
-    int np = a.np, n = a.n, mn = n - 1;
+    int n = a.n, mn = n - 1;
     T e0 = 0, e1 = 0, e2 = 0;
+    const T *rec = w + (size_t)p * spl_rec(ORDER);   // head, values x, y, z, derivatives x, y, z
+    const T *rv = rec + kRecHead, *rd = rv + 3 * ORDER;
     if (act) {
-        const T *rec = w + (size_t)p * spl_rec(ORDER);   // values x, y, z, then derivatives x, y, z
         T vy[ORDER], dy[ORDER];
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            vy[i] = rec[ORDER + i];
-            dy[i] = rec[4 * ORDER + i];
+            vy[i] = rv[ORDER + i];
+            dy[i] = rd[ORDER + i];
         }
-        T vx = rec[j], dx = rec[3 * ORDER + j];
-        int c0 = corner[p], c1 = corner[np + p], c2 = corner[2 * np + p];
+        T vx = rv[j], dx = rd[j];
+        int c = rec_corner(rec[0]);
+        int c0 = c & 1023, c1 = (c >> 10) & 1023, c2 = c >> 20;
         const T *col = Q + ((c0 - j) & mn);
         T A = 0, B = 0, C = 0;
 #pragma unroll
         for (int iz = 0; iz < ORDER; ++iz) {
-            T vz = rec[2 * ORDER + iz], dz = rec[5 * ORDER + iz];
+            T vz = rv[2 * ORDER + iz], dz = rd[2 * ORDER + iz];
             const T *pl = col + ((size_t)((c2 - iz) & mn) << (2 * a.n_log));
             T r0 = 0, r1 = 0;
 #pragma unroll
@@ -776,7 +786,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
         e2 += __shfl_xor_sync(0xffffffffu, e2, o, G);
     }
     if (j != 0 || !valid) return;
-    T qk = -(T)a.az[p];   // kx, ky, kz = dkdr * EpsiFourPi
+    T qk = -rec[1];   // the charge; kx, ky, kz = dkdr * EpsiFourPi
     if (MIXED) {
         long long f0 = mg_f2fx((float)(qk * kx * e0)), f1 = mg_f2fx((float)(qk * ky * e1)),
                   f2 = mg_f2fx((float)(qk * kz * e2));
@@ -836,36 +846,35 @@ __global__ void k_mesh_to_f64(const T *__restrict__ Q, double *__restrict__ out,
 template <typename T, typename ACC, int ORDER>
 void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const BrickArgs &bk) {
     int np = h->np;
-    int *corner = h->d_corner;
     T *w = (T *)h->d_spl_w;
     if (which == 0) {
-        mg_launch_pdl(k_spline_prepare<T, ORDER>, (np + 255) / 256, 256, 0, h->st, sa, corner, w);
+        mg_launch_pdl(k_spline_prepare<T, ORDER>, (np + 255) / 256, 256, 0, h->st, sa, w);
     } else if (which == 1 && sizeof(T) == 4) {   // mixed form
         int wpb = h->spread_wpb_lane;
         int grid = (h->max_items + wpb - 1) / wpb;
         const float *wf = (const float *)w;
         if (h->brick == 8)
-            mg_launch_pdl(k_spread_lane<ORDER, 8>, grid, 32 * wpb, h->spread_smem_lane, h->st, bk, corner, wf,
-                          h->d_az, np, (long long *)h->d_Qfx);
+            mg_launch_pdl(k_spread_lane<ORDER, 8>, grid, 32 * wpb, h->spread_smem_lane, h->st, bk, wf,
+                          (long long *)h->d_Qfx);
         else
-            mg_launch_pdl(k_spread_lane<ORDER, 16>, grid, 32 * wpb, h->spread_smem_lane, h->st, bk, corner, wf,
-                          h->d_az, np, (long long *)h->d_Qfx);
+            mg_launch_pdl(k_spread_lane<ORDER, 16>, grid, 32 * wpb, h->spread_smem_lane, h->st, bk, wf,
+                          (long long *)h->d_Qfx);
     } else if (which == 1) {
         int wpb = h->spread_wpb;
         int grid = (h->max_items + wpb - 1) / wpb;
         if (h->brick == 8)
             k_spread_warp<T, ACC, ORDER, 8><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
-                bk, corner, w, h->d_az, np, (long long *)h->d_Qfx);
+                bk, w, (long long *)h->d_Qfx);
         else
             k_spread_warp<T, ACC, ORDER, 16><<<grid, 32 * wpb, h->spread_smem, h->st>>>(
-                bk, corner, w, h->d_az, np, (long long *)h->d_Qfx);
+                bk, w, (long long *)h->d_Qfx);
     } else {
         // force factors dkdr * EpsiFourPi per direction
         T kx = (T)(h->dkdr[0] * h->EpsiFourPi), ky = (T)(h->dkdr[1] * h->EpsiFourPi),
           kz = (T)(h->dkdr[2] * h->EpsiFourPi);
         constexpr int G = ORDER <= 8 ? 8 : 16;
         mg_launch_pdl(k_gather_grp<T, sizeof(T) == 4, ORDER>, (unsigned)(((long)np * G + 255) / 256), 256, 0,
-                      h->st, sa, h->d_perm, corner, w, (const T *)h->d_Q, kx, ky, kz,
+                      h->st, sa, h->d_perm, w, (const T *)h->d_Q, kx, ky, kz,
                       h->d_force, h->d_ffx);
     }
 }
@@ -1413,7 +1422,6 @@ int mg_spme_init(mg_handle *h) {
     // warps (work items) per block: the count that keeps the most warps
     // resident per SM (228 KB of shared memory, 1 KB reserved per block)
     size_t stage = 32 * sizeof(int) + 32 * (3 * (size_t)h->order + 1) * tsz;   // per-warp particle staging
-    size_t per_warp = acc * t3 + stage;
     int best = 0;
     h->spread_wpb = 0;
     for (int wpb = 1; wpb <= kSpreadWarps; ++wpb) {
@@ -1425,7 +1433,6 @@ int mg_spme_init(mg_handle *h) {
     if (h->spread_wpb < 1)
         return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME spread tile does not fit in shared memory");
     h->spread_smem = ((h->spread_wpb * acc * t3 + 15) & ~(size_t)15) + h->spread_wpb * stage;
-    (void)per_warp;
     // lane-per-particle spread (mixed form): a 32-bit tile per warp, no staging
     {
         int bestl = 0;
@@ -1450,7 +1457,6 @@ int mg_spme_init(mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_item_brick, sizeof(int) * h->max_items));
     MG_CUDA(h, cudaMalloc(&h->d_Qfx, sizeof(long long) * (size_t)n * n * n));
     MG_CUDA(h, cudaMemset(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n));
-    MG_CUDA(h, cudaMalloc(&h->d_corner, sizeof(int) * 3 * (size_t)h->np));
     MG_CUDA(h, cudaMalloc(&h->d_spl_w, tsz * spl_rec(h->order) * (size_t)h->np));   // spline records
     spread_attrs<float, int>();
     spread_attrs<double, long long>();
