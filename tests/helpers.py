@@ -1,4 +1,6 @@
 """Shared helpers for parity tests: systems, comparisons, tolerances."""
+import dataclasses
+
 import numpy as np
 
 from molsim_gb300 import Engine, abi, configs
@@ -94,3 +96,15 @@ def chain_trial(rng, s, ro, chains, nseg, step=1.0):
     new = ro[ips] + rng.uniform(-step, step, (n, 3))
     new -= L * np.round(new / L)
     return ips + 1, new
+
+
+def chain_system(seed=71, chains=4, nseg=10, **kw):
+    """small_system with the chain beads as a fourth particle type (a copy
+    of their ion type), as the reference gives chain particles their own
+    types."""
+    s = configs.small_system(seed=seed, mode=abi.MG_MC, chains=chains, nseg=nseg, angle_kt=0.5, **kw)
+    t = int(s.iptpn[0]) - 1
+    s.species = list(s.species) + [dataclasses.replace(s.species[t], name="bead")]
+    s.iptpn = s.iptpn.copy()
+    s.iptpn[:chains * nseg] = len(s.species)
+    return s

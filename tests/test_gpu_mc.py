@@ -193,3 +193,33 @@ def test_chain_string_trials_match_oracle(txintlist, orc, gpu_lib):
         assert bool(ovl[t]) == o, t
         if not o:
             assert abs(du[t] - r["du_tot"]) <= 1e-10 * scale, t
+
+
+@pytest.mark.parametrize("mode", [1, 3])
+def test_mc_passes_match_oracle(mode, orc, gpu_lib):
+    """MC passes of single-particle, pivot and chain moves (molsim_gb300.mc,
+    restating mc.F90's SPartMove, PivotMove and ChainMove) driven by the same
+    Random stream through the oracle and through the GPU: the same trials
+    are accepted, the positions agree bit for bit, and the accepted du%tot
+    add up to the GPU's UTotal."""
+    from molsim_gb300.mc import MCPass, MoveParams
+    from tests.helpers import chain_system
+    s = prepared(chain_system(seed=72, txintlist=abi.MG_CELLLIST), orc)
+    ref, gpu, u_ref, u_gpu = _pair(s, orc)
+    chain_p = MoveParams(pspart=0.3, dtran=1.0, ppivot=0.4, ipivotrotmode=mode, drotpivot=60.0,
+                         pchain=0.3, dtranchain=1.0)
+    ion_p = MoveParams(pspart=1.0, dtran=2.0)
+    params = [ion_p, ion_p, ion_p, chain_p]
+    runs = [MCPass(e, s, iseed=11, params=params, record=True) for e in (ref, gpu)]
+    for mc in runs:
+        for _ in range(2):
+            mc.run_pass()
+    a, b = runs
+    assert a.stats.events == b.stats.events
+    assert b.stats.accepted["pivot"] > 3 and b.stats.accepted["chain"] > 0
+    assert np.array_equal(a.ro, b.ro)
+    assert np.array_equal(gpu.GetPositions(), b.ro)
+    scale = abs(u_ref["u_tot"]) + abs(u_ref["u_rec"]) + 1.0
+    assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
+    u1 = gpu.UTotal()
+    assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
