@@ -55,12 +55,31 @@ def build(verbose=False, force=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     if os.path.exists(LIB) and not force and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
+        build_harness()
         return LIB
     cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
+    build_harness()
     return LIB
+
+
+def build_harness():
+    """mg_replay: the compiled C++ caller of the ABI, linked against the
+    library next to it (rpath $ORIGIN)."""
+    src = os.path.join(HERE, "harness", "mg_replay.cpp")
+    exe = os.path.join(HERE, "mg_replay")
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        return exe
+    # no contraction: the harness restates the reference's arithmetic
+    # (PBC, Metropolis) and must round as the Python and Fortran callers do
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I", os.path.join(HERE, "..", "include"), src,
+           "-L", HERE, "-lmolsim_gb300", "-Wl,-rpath,$ORIGIN", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness build failed:\n{r.stderr}")
+    return exe
 
 
 if __name__ == "__main__":

@@ -193,7 +193,8 @@ class MCPass:
             x = r[..., m]
             big = np.abs(x) > self.half[m]
             t = x * self.Li[m]
-            a = np.sign(t) * np.floor(np.abs(t) + 0.5)   # anint: half away from zero
+            a = np.trunc(t)                                # anint: half away from zero, exactly
+            a = a + np.sign(t) * (np.abs(t - a) >= 0.5)
             r[..., m] = np.where(big, x - self.L[m] * a, x)
         return r
 
