@@ -13,6 +13,7 @@ __all__ = ["abi", "configs", "units", "Engine", "MolsimError", "Species", "Syste
 
 
 def build(verbose=False, force=False):
-    """Compile the native library in place (nvcc, sm_103a)."""
-    from .build import build as _b
+    """Compile the native library in place (nvcc, sm_103a) and the compiled
+    ABI caller next to it (native_build.py)."""
+    from .native_build import build as _b
     return _b(verbose=verbose, force=force)
