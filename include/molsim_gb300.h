@@ -311,6 +311,51 @@ int mg_bench_steps(mg_handle *h, int32_t kind, int32_t nstep, int64_t flush_byte
  * mg_md_run / mg_bd_run / mg_bench_steps). */
 int mg_step_kernels(mg_handle *h, int32_t kind, int32_t *nkernels);
 
+/* ---- polyatomic particles (UTwoBodyP) ------------------------------------------ */
+
+/* Particles made of atoms (rigid molecules): the two-body energy is the sum
+ * over the atom pairs of every particle pair whose centres are within rcut
+ * (UTwoBodyP, energy.F90:786-896).  The atom positions come from the caller
+ * (the reference's r(3,na), built from the particle positions and
+ * orientations), the particle neighbour list too (jpnlist of NList). */
+typedef struct mg_poly_params {
+    int32_t abi_version;      /* must be MG_ABI_VERSION                          */
+    int32_t np, npt, nptpt;   /* particles, particle types, type pairs          */
+    const int32_t *iptpn;     /* [np] particle type, 1..npt                     */
+    const int32_t *iptpt;     /* [npt*npt] column-major, 1..nptpt               */
+    const int32_t *napt;      /* [npt] atoms per particle of each type          */
+    int32_t na;               /* atoms in all                                   */
+    const int32_t *ianpn;     /* [np] first atom of each particle, 1-based      */
+    const int32_t *iatan;     /* [na] atom type, 1..nat                         */
+    int32_t nat, natat;       /* atom types, atom-type pairs                    */
+    const int32_t *iatat;     /* [nat*nat] column-major, 1..natat               */
+    /* the two-body table over atom-type pairs (PotTwoBodyTab1 with the atom
+       types as its types; mg_pot_twobody_tab builds it) */
+    int32_t nbuf;
+    const double  *ubuf;      /* [nbuf]                                         */
+    const int32_t *iubuflow;  /* [natat] 1-based                                */
+    const double  *r2umin;    /* [natat]                                        */
+    double  boxlen[3];        /* box edges; box centred at the origin           */
+    double  rcut;             /* cutoff on the particle-centre distance         */
+    int32_t lmc;              /* 1: jpnlist is the full (MC) list: a pair is
+                                 taken from its lower-numbered particle         */
+} mg_poly_params;
+
+typedef struct mg_poly mg_poly;
+/* A context on the current device for systems of these parameters; its
+ * neighbour list holds up to maxnneigh entries per particle. */
+int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_poly **c);
+/* UTwoBodyP for particle centres ro[3*np], atom positions r[3*na] and the
+ * neighbour list nneighpn[np], jpnlist[maxnneigh*np] (column-major, 1-based,
+ * as NList stores it).  Writes the atom forces force[3*na] (not scaled by
+ * force_fac, as force(3,na) in the reference), u%twob(0:nptpt) into
+ * u_twob[nptpt+1] and the two-body virial into *virial.  An atom pair
+ * closer than its table (r2 < r2umin) returns MG_ERR_TABLE_UNDERRUN. */
+int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
+                     const int32_t *jpnlist, double *force, double *u_twob, double *virial);
+int mg_poly_last_error(const mg_poly *c, char *buf, size_t n);
+int mg_poly_destroy(mg_poly *c);
+
 /* ---- allocation-free entry point ----------------------------------------------- */
 
 /* Largest ncut that mg_ewald_rec_std_noalloc accepts. */

@@ -53,6 +53,16 @@ class MgPotParams(C.Structure):
     ]
 
 
+class MgPolyParams(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32), ("np", C.c_int32), ("npt", C.c_int32), ("nptpt", C.c_int32),
+        ("iptpn", PI32), ("iptpt", PI32), ("napt", PI32), ("na", C.c_int32), ("ianpn", PI32),
+        ("iatan", PI32), ("nat", C.c_int32), ("natat", C.c_int32), ("iatat", PI32),
+        ("nbuf", C.c_int32), ("ubuf", PF64), ("iubuflow", PI32), ("r2umin", PF64),
+        ("boxlen", C.c_double * 3), ("rcut", C.c_double), ("lmc", C.c_int32),
+    ]
+
+
 # (name without prefix, restype, argtypes) shared by the library (mg_) and the
 # oracle (orc_), whose entry points take the same arguments.
 H = C.c_void_p
@@ -94,6 +104,10 @@ LIB_ONLY = [
     ("ensemble_kernels", C.c_int, [H, C.c_int32, PI32]),
     ("ensemble_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
     ("ensemble_destroy", C.c_int, [H]),
+    ("poly_create", C.c_int, [C.POINTER(MgPolyParams), C.c_int32, C.POINTER(C.c_void_p)]),
+    ("poly_utwobody", C.c_int, [H, PF64, PF64, PI32, PI32, PF64, PF64, PF64]),
+    ("poly_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
+    ("poly_destroy", C.c_int, [H]),
     ("ewald_rec_std_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, PF64, C.c_double, C.c_int32,
                                         C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_char_p, C.c_size_t]),

@@ -291,3 +291,33 @@ def replica_set(seed=5, nrep=256, nmin=500, nmax=8000, cmin=0.01, cmax=1.0, rcut
                           ualpha=alpha_for_erfc(1e-5, rcut), order=order, nmesh=k, lsurf=0, lljcut=0,
                           name=f"replica{r}_N{n}_c{c:.3f}"))
     return out
+
+
+def water_ions(seed=9, nwater=300, nsalt=20, L=24.0, rcut=9.0, rmin=3.0):
+    """A polyatomic system for the UTwoBodyP path: rigid three-site waters
+    (O and two H, SPC/E-like charges and geometry) and NaCl ion pairs as
+    one-atom particles, centres on a jittered grid at least rmin apart,
+    random orientations; Coulomb without Ewald plus (1,6,12) LJ between
+    atoms (H without LJ)."""
+    from .poly import AtomType, ParticleType, PolySystem
+    rng = np.random.Generator(np.random.PCG64(seed))
+    atom_types = [AtomType("O", -0.8476, 3.166, 0.650), AtomType("H", 0.4238, 0.0, 0.0),
+                  AtomType("Na", 1.0, 2.35, 0.544), AtomType("Cl", -1.0, 4.40, 0.419)]
+    hx, hz = 0.8165, 0.5773
+    ptypes = [ParticleType("water", [(0, (0.0, 0.0, -0.0656)), (1, (hx, 0.0, hz - 0.0656)),
+                                     (1, (-hx, 0.0, hz - 0.0656))]),
+              ParticleType("Na", [(2, (0.0, 0.0, 0.0))]), ParticleType("Cl", [(3, (0.0, 0.0, 0.0))])]
+    n = nwater + 2 * nsalt
+    grid = _Grid([L, L, L], rmin)
+    ro = place_uniform(rng, grid, n)
+    types = np.array([1] * nwater + [2] * nsalt + [3] * nsalt, dtype=np.int32)
+    ori = np.empty((n, 3, 3))
+    for i in range(n):
+        q, r = np.linalg.qr(rng.standard_normal((3, 3)))
+        q = q * np.sign(np.diag(r))
+        if np.linalg.det(q) < 0:
+            q[:, 0] = -q[:, 0]
+        ori[i] = q
+    return PolySystem(atom_types=atom_types, particle_types=ptypes, iptpn=types,
+                      ro=np.ascontiguousarray(np.asarray(ro, dtype=np.float64)), ori=ori,
+                      boxlen=np.array([L, L, L]), rcut=rcut)

@@ -1,0 +1,310 @@
+// poly.cu — the two-body energy of polyatomic particles (UTwoBodyP,
+// energy.F90:786-896).
+//
+// For every particle pair of the neighbour list whose centres lie within
+// rcut (minimum image by PBC2, molaux.F90:193-248: the shift of the centre
+// separation is applied to every atom pair of the two particles), every atom
+// pair adds the tabulated energy (the linear interval search from iubuflow
+// of its atom-type pair and the quintic in d = r^2 - z_low) to u%twob of the
+// particle-type pair, fsum*dr to the first atom's force and -fsum*dr to the
+// second's, and -fsum*r^2 to the virial.  FP64 throughout.
+//
+// One thread per particle walks its list row; the atom forces are added
+// with FP64 atomics (the order of the additions is not fixed, so forces
+// agree with the reference's sequential sums to rounding), the energies and
+// the virial are summed per block and the blocks in order on the host.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "mg_internal.cuh"
+
+namespace {
+
+constexpr int kPolyThreads = 128;
+
+struct PolyArgs {
+    int np, nptpt, maxnneigh, lmc, nbuf;
+    const int *iptpn, *iptpt, *napt, *ianpn, *iatan, *iatat, *iubuflow;
+    int npt, nat;
+    const double *ubuf, *r2umin;
+    const double *ro, *r;
+    const int *nneighpn, *jpnlist;
+    double len[3], half[3], rcut2;
+    double *force;
+    double *part;   // [nblk][nptpt + 2]: u%twob(1:nptpt), virial
+    int *err;
+};
+
+__global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
+    extern __shared__ double red[];   // [nptpt + 1][kPolyThreads]
+    const int nv = a.nptpt + 1;
+    double acc[MG_MAX_NPTPT], vir = 0.0;   // u%twob(1:nptpt) and the virial of this thread
+#pragma unroll
+    for (int k = 0; k < MG_MAX_NPTPT; ++k) acc[k] = 0.0;
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;   // 0-based particle
+    if (ip < a.np) {
+        int ipt = a.iptpn[ip];
+        int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[ipt - 1];
+        int nn = a.nneighpn[ip];
+        for (int jploc = 0; jploc < nn; ++jploc) {
+            int jp = a.jpnlist[(size_t)ip * a.maxnneigh + jploc] - 1;
+            if (a.lmc && jp < ip) continue;
+            int jpt = a.iptpn[jp];
+            int iptjpt = a.iptpt[(jpt - 1) * a.npt + (ipt - 1)];
+            double d[3], sh[3];
+            for (int m = 0; m < 3; ++m) {
+                d[m] = __dsub_rn(a.ro[3 * ip + m], a.ro[3 * jp + m]);
+                sh[m] = fabs(d[m]) > a.half[m] ? copysign(a.len[m], d[m]) : 0.0;   // PBC2
+                d[m] = __dsub_rn(d[m], sh[m]);
+            }
+            double r2 = mg_r2_exact(d[0], d[1], d[2]);
+            if (r2 > a.rcut2) continue;
+            double usum = 0.0;
+            int jalow = a.ianpn[jp] - 1, jaupp = jalow + a.napt[jpt - 1];
+            for (int ia = ialow; ia < iaupp; ++ia) {
+                int iat = a.iatan[ia];
+                for (int ja = jalow; ja < jaupp; ++ja) {
+                    int jat = a.iatan[ja];
+                    int iatjat = a.iatat[(jat - 1) * a.nat + (iat - 1)];
+                    double dx = __dsub_rn(__dsub_rn(a.r[3 * ia], a.r[3 * ja]), sh[0]);
+                    double dy = __dsub_rn(__dsub_rn(a.r[3 * ia + 1], a.r[3 * ja + 1]), sh[1]);
+                    double dz = __dsub_rn(__dsub_rn(a.r[3 * ia + 2], a.r[3 * ja + 2]), sh[2]);
+                    double ar2 = mg_r2_exact(dx, dy, dz);
+                    if (ar2 < a.r2umin[iatjat - 1]) {
+                        mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, ia + 1, ja + 1, iatjat);
+                        continue;
+                    }
+                    int ibuf = a.iubuflow[iatjat - 1] - 1;   // 0-based start of the record
+                    while (!(ar2 >= a.ubuf[ibuf])) {
+                        ibuf += 12;
+                        if (ibuf >= a.nbuf) break;
+                    }
+                    if (ibuf >= a.nbuf) {
+                        mg_dev_error(a.err, MG_ERR_IBUF, iatjat, ia + 1, ja + 1);
+                        continue;
+                    }
+                    const double *c = a.ubuf + ibuf;
+                    double dd = __dsub_rn(ar2, c[0]);
+                    // usum = usum + ubuf(ibuf+1) + d*(...): Fortran adds left to right
+                    usum = __dadd_rn(__dadd_rn(usum, c[1]), __dmul_rn(dd, __dadd_rn(c[2], __dmul_rn(dd, __dadd_rn(c[3],
+                                     __dmul_rn(dd, __dadd_rn(c[4], __dmul_rn(dd, __dadd_rn(c[5], __dmul_rn(dd, c[6]))))))))));
+                    double fsum = __dadd_rn(c[7], __dmul_rn(dd, __dadd_rn(c[8], __dmul_rn(dd, __dadd_rn(c[9],
+                                  __dmul_rn(dd, __dadd_rn(c[10], __dmul_rn(dd, c[11]))))))));
+                    double fx = __dmul_rn(fsum, dx), fy = __dmul_rn(fsum, dy), fz = __dmul_rn(fsum, dz);
+                    atomicAdd(&a.force[3 * ia], fx);
+                    atomicAdd(&a.force[3 * ia + 1], fy);
+                    atomicAdd(&a.force[3 * ia + 2], fz);
+                    atomicAdd(&a.force[3 * ja], -fx);
+                    atomicAdd(&a.force[3 * ja + 1], -fy);
+                    atomicAdd(&a.force[3 * ja + 2], -fz);
+                    vir = __dsub_rn(vir, __dmul_rn(fsum, ar2));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < MG_MAX_NPTPT; ++k)   // static indices keep acc in registers
+                if (k == iptjpt - 1) acc[k] = __dadd_rn(acc[k], usum);
+        }
+    }
+    // block sums in a fixed order (thread 0 adds the block's values in turn)
+#pragma unroll
+    for (int k = 0; k <= MG_MAX_NPTPT; ++k)
+        if (k < nv) red[k * blockDim.x + threadIdx.x] = (k == a.nptpt) ? vir : acc[k < MG_MAX_NPTPT ? k : 0];
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double s = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) s = __dadd_rn(s, red[threadIdx.x * blockDim.x + t]);
+        a.part[(size_t)blockIdx.x * nv + threadIdx.x] = s;
+    }
+}
+
+}  // namespace
+
+struct mg_poly {
+    mg_poly_params p{};
+    int maxnneigh = 0, nblk = 0;
+    std::string err;
+    int *d_iptpn = nullptr, *d_iptpt = nullptr, *d_napt = nullptr, *d_ianpn = nullptr, *d_iatan = nullptr,
+        *d_iatat = nullptr, *d_iubuflow = nullptr, *d_nneigh = nullptr, *d_jpnlist = nullptr, *d_err = nullptr;
+    double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
+           *d_part = nullptr;
+    std::vector<double> h_part;
+};
+
+static int poly_fail(mg_poly *c, int code, const char *fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+#define POLY_CUDA(c, call)                                                                                \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return poly_fail((c), MG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T> static int poly_upload(mg_poly *c, T **d, const T *h, size_t n) {
+    POLY_CUDA(c, cudaMalloc(d, sizeof(T) * std::max<size_t>(n, 1)));
+    if (n) POLY_CUDA(c, cudaMemcpy(*d, h, sizeof(T) * n, cudaMemcpyHostToDevice));
+    return MG_OK;
+}
+
+extern "C" int mg_poly_destroy(mg_poly *c) {
+    if (!c) return MG_OK;
+    void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
+                    c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
+                    c->d_force, c->d_part};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    delete c;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_last_error(const mg_poly *c, char *buf, size_t n) {
+    if (!buf || !n) return MG_ERR_ARG;
+    std::snprintf(buf, n, "%s", c ? c->err.c_str() : "");
+    return MG_OK;
+}
+
+static int poly_check_params(const mg_poly_params *p, int maxnneigh) {
+    if (p->abi_version != MG_ABI_VERSION || p->np < 1 || p->npt < 1 || p->nptpt != p->npt * (p->npt + 1) / 2 ||
+        p->nptpt > MG_MAX_NPTPT || p->na < 1 || p->nat < 1 || p->natat < 1 || p->nbuf < 12 || maxnneigh < 1)
+        return MG_ERR_ARG;
+    if (!p->iptpn || !p->iptpt || !p->napt || !p->ianpn || !p->iatan || !p->iatat || !p->ubuf || !p->iubuflow ||
+        !p->r2umin)
+        return MG_ERR_ARG;
+    for (int i = 0; i < p->np; ++i) {
+        int t = p->iptpn[i];
+        if (t < 1 || t > p->npt) return MG_ERR_ARG;
+        int a0 = p->ianpn[i], na = p->napt[t - 1];
+        if (a0 < 1 || na < 1 || a0 - 1 + na > p->na) return MG_ERR_ARG;
+    }
+    for (int a = 0; a < p->na; ++a)
+        if (p->iatan[a] < 1 || p->iatan[a] > p->nat) return MG_ERR_ARG;
+    for (int k = 0; k < p->nat * p->nat; ++k)
+        if (p->iatat[k] < 1 || p->iatat[k] > p->natat) return MG_ERR_ARG;
+    for (int k = 0; k < p->npt * p->npt; ++k)
+        if (p->iptpt[k] < 1 || p->iptpt[k] > p->nptpt) return MG_ERR_ARG;
+    for (int k = 0; k < p->natat; ++k)
+        if (p->iubuflow[k] < 1 || p->iubuflow[k] + 11 > p->nbuf) return MG_ERR_ARG;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_poly **out) {
+    if (!p || !out) return MG_ERR_ARG;
+    *out = nullptr;
+    int st = poly_check_params(p, maxnneigh);
+    if (st) return st;
+    mg_poly *c = new (std::nothrow) mg_poly();
+    if (!c) return MG_ERR_ALLOC;
+    c->p = *p;
+    c->maxnneigh = maxnneigh;
+    c->nblk = (p->np + kPolyThreads - 1) / kPolyThreads;
+    int np = p->np, na = p->na;
+    if ((st = poly_upload(c, &c->d_iptpn, p->iptpn, np)) || (st = poly_upload(c, &c->d_iptpt, p->iptpt, (size_t)p->npt * p->npt)) ||
+        (st = poly_upload(c, &c->d_napt, p->napt, p->npt)) || (st = poly_upload(c, &c->d_ianpn, p->ianpn, np)) ||
+        (st = poly_upload(c, &c->d_iatan, p->iatan, na)) ||
+        (st = poly_upload(c, &c->d_iatat, p->iatat, (size_t)p->nat * p->nat)) ||
+        (st = poly_upload(c, &c->d_iubuflow, p->iubuflow, p->natat)) ||
+        (st = poly_upload(c, &c->d_ubuf, p->ubuf, p->nbuf)) || (st = poly_upload(c, &c->d_r2umin, p->r2umin, p->natat))) {
+        mg_poly_destroy(c);
+        return st;
+    }
+    cudaError_t e = cudaMalloc(&c->d_ro, sizeof(double) * 3 * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_r, sizeof(double) * 3 * na);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_force, sizeof(double) * 3 * na);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_nneigh, sizeof(int) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_jpnlist, sizeof(int) * (size_t)maxnneigh * np);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->nblk * (p->nptpt + 1));
+    if (e != cudaSuccess) {
+        mg_poly_destroy(c);
+        return MG_ERR_CUDA;
+    }
+    c->h_part.resize((size_t)c->nblk * (p->nptpt + 1));
+    *out = c;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
+                                const int32_t *jpnlist, double *force, double *u_twob, double *virial) {
+    if (!c || !ro || !r || !nneighpn || !jpnlist || !force || !u_twob || !virial) return MG_ERR_ARG;
+    const mg_poly_params &p = c->p;
+    int np = p.np, na = p.na;
+    for (int i = 0; i < np; ++i) {
+        if (nneighpn[i] < 0 || nneighpn[i] > c->maxnneigh)
+            return poly_fail(c, MG_ERR_NEIGH_OVERFLOW, "nneighpn(%d) = %d > maxnneigh %d", i + 1, nneighpn[i],
+                             c->maxnneigh);
+        for (int k = 0; k < nneighpn[i]; ++k) {
+            int j = jpnlist[(size_t)i * c->maxnneigh + k];
+            if (j < 1 || j > np || j == i + 1) return poly_fail(c, MG_ERR_ARG, "jpnlist(%d,%d) = %d", k + 1, i + 1, j);
+        }
+    }
+    POLY_CUDA(c, cudaMemcpy(c->d_ro, ro, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_nneigh, nneighpn, sizeof(int) * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_jpnlist, jpnlist, sizeof(int) * (size_t)c->maxnneigh * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemset(c->d_force, 0, sizeof(double) * 3 * na));
+    POLY_CUDA(c, cudaMemset(c->d_err, 0, sizeof(int) * 4));
+    PolyArgs a;
+    a.np = np;
+    a.nptpt = p.nptpt;
+    a.maxnneigh = c->maxnneigh;
+    a.lmc = p.lmc;
+    a.nbuf = p.nbuf;
+    a.iptpn = c->d_iptpn;
+    a.iptpt = c->d_iptpt;
+    a.napt = c->d_napt;
+    a.ianpn = c->d_ianpn;
+    a.iatan = c->d_iatan;
+    a.iatat = c->d_iatat;
+    a.iubuflow = c->d_iubuflow;
+    a.npt = p.npt;
+    a.nat = p.nat;
+    a.ubuf = c->d_ubuf;
+    a.r2umin = c->d_r2umin;
+    a.ro = c->d_ro;
+    a.r = c->d_r;
+    a.nneighpn = c->d_nneigh;
+    a.jpnlist = c->d_jpnlist;
+    for (int m = 0; m < 3; ++m) {
+        a.len[m] = p.boxlen[m];
+        a.half[m] = 0.5 * p.boxlen[m];
+    }
+    a.rcut2 = p.rcut * p.rcut;
+    a.force = c->d_force;
+    a.part = c->d_part;
+    a.err = c->d_err;
+    size_t sm = sizeof(double) * (p.nptpt + 1) * kPolyThreads;
+    k_twobody_p<<<c->nblk, kPolyThreads, sm>>>(a);
+    POLY_CUDA(c, cudaGetLastError());
+    int herr[4];
+    POLY_CUDA(c, cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr[0] == MG_ERR_TABLE_UNDERRUN)
+        return poly_fail(c, herr[0], "r2 < r2umin for atoms %d and %d (atom-type pair %d)", herr[1], herr[2], herr[3]);
+    if (herr[0]) return poly_fail(c, herr[0], "ibuf > nbuf for atom-type pair %d", herr[1]);
+    POLY_CUDA(c, cudaMemcpy(force, c->d_force, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->h_part.size(), cudaMemcpyDeviceToHost));
+    int nv = p.nptpt + 1;
+    double tot = 0.0, vir = 0.0;
+    for (int k = 0; k < p.nptpt; ++k) {
+        double s = 0.0;
+        for (int b = 0; b < c->nblk; ++b) s += c->h_part[(size_t)b * nv + k];
+        u_twob[k + 1] = s;
+    }
+    for (int k = 1; k <= p.nptpt; ++k) tot += u_twob[k];   // u%twob(0) = sum(u%twob(1:nptpt))
+    u_twob[0] = tot;
+    for (int b = 0; b < c->nblk; ++b) vir += c->h_part[(size_t)b * nv + p.nptpt];
+    *virial = vir;
+    return MG_OK;
+}

@@ -1,0 +1,182 @@
+"""Polyatomic particles: the two-body energy over atom pairs (UTwoBodyP,
+energy.F90:786-896) through the library's mg_poly_* entry points.
+
+A `PolySystem` holds atom types (charge, LJ sigma and epsilon), particle
+types as rigid sets of atoms (local positions), the particles (type,
+centre) and their orientations; `atom_positions` places the atoms as the
+reference does (r = ro + ori . local, the local frame rotated by the
+particle's orientation matrix).  The pair table runs over atom-type pairs:
+PotTwoBodyTab1 (potential.F90:868) with the atom types as its types.
+`PolyEngine.UTwoBodyP` evaluates u%twob, the atom forces and the virial for
+a particle neighbour list (NList's nneighpn, jpnlist).
+"""
+from dataclasses import dataclass, field
+from typing import List, Optional, Tuple
+
+import ctypes as C
+import numpy as np
+
+from . import abi, units
+from .engine import MolsimError
+from .system import iptpt_matrix
+
+__all__ = ["AtomType", "ParticleType", "PolySystem", "PolyEngine"]
+
+
+@dataclass
+class AtomType:
+    name: str
+    charge: float
+    sigma: float
+    eps: float
+
+
+@dataclass
+class ParticleType:
+    name: str
+    atoms: List[Tuple[int, Tuple[float, float, float]]]   # (atom type, 0-based; local position)
+
+
+@dataclass
+class PolySystem:
+    atom_types: List[AtomType]
+    particle_types: List[ParticleType]
+    iptpn: np.ndarray                 # (np,) 1-based particle type
+    ro: np.ndarray                    # (np, 3) centres
+    ori: np.ndarray                   # (np, 3, 3) orientation matrices
+    boxlen: np.ndarray
+    rcut: float = 10.0
+    relpermitt: float = 1.0
+    lmc: int = 0
+    r2uminin: float = 0.1
+    ubuf: Optional[np.ndarray] = None
+    iubuflow: Optional[np.ndarray] = None
+    r2umin: Optional[np.ndarray] = None
+    keep: dict = field(default_factory=dict)
+
+    @property
+    def np_(self):
+        return int(len(self.iptpn))
+
+    @property
+    def npt(self):
+        return len(self.particle_types)
+
+    @property
+    def nat(self):
+        return len(self.atom_types)
+
+    def napt(self):
+        return np.array([len(t.atoms) for t in self.particle_types], dtype=np.int32)
+
+    def ianpn(self):
+        """First atom (1-based) of each particle: atoms numbered particle by
+        particle, as the reference's ianpn."""
+        n = self.napt()[self.iptpn - 1]
+        return (np.concatenate([[0], np.cumsum(n)[:-1]]) + 1).astype(np.int32)
+
+    def iatan(self):
+        return np.concatenate([[a for a, _ in self.particle_types[t - 1].atoms] for t in self.iptpn]).astype(np.int32) + 1
+
+    def atom_positions(self):
+        out = []
+        for ip, t in enumerate(self.iptpn):
+            loc = np.array([x for _, x in self.particle_types[t - 1].atoms], dtype=np.float64)
+            out.append(self.ro[ip] + loc @ self.ori[ip].T)
+        return np.ascontiguousarray(np.concatenate(out))
+
+    def build_table(self, tabfn):
+        """PotTwoBodyTab1 over the atom types (Coulomb without Ewald, plus
+        (1,6,12) Lennard-Jones)."""
+        nat = self.nat
+        keep = {"iptpt": iptpt_matrix(nat),
+                "zat": abi.as_f64([a.charge for a in self.atom_types]),
+                "sigat": abi.as_f64([a.sigma for a in self.atom_types]),
+                "epsat": abi.as_f64([a.eps for a in self.atom_types])}
+        pp = abi.MgPotParams(npt=nat, iptpt=abi.i32(keep["iptpt"]), zat=abi.f64(keep["zat"]),
+                             sigat=abi.f64(keep["sigat"]), epsat=abi.f64(keep["epsat"]), rcut=self.rcut,
+                             ualpha=0.0, epsi_four_pi=units.Epsi0FourPi / self.relpermitt, lcharge_ewald=0,
+                             lljcut=0, ljrcut=units.ljrcut_default(), ljushift=1.0, r2uminin=self.r2uminin,
+                             utoltab=units.tol_default(), ftoltab=units.tol_default(), umaxtab=20000.0,
+                             fmaxtab=20000.0)
+        natat = nat * (nat + 1) // 2
+        cap = 4000
+        while True:
+            ubuf = np.zeros(cap)
+            used = np.zeros(1, dtype=np.int32)
+            iub = np.zeros(natat, dtype=np.int32)
+            r2 = np.zeros(natat)
+            nug = np.zeros(natat, dtype=np.int32)
+            st = tabfn(C.byref(pp), abi.f64(ubuf), cap, abi.i32(used), abi.i32(iub), abi.f64(r2), abi.i32(nug))
+            if st == 0:
+                break
+            if used[0] > cap and cap < 10_000_000:
+                cap = max(3 * cap, int(used[0]))
+                continue
+            raise RuntimeError(f"atom-pair table construction failed: {abi.STATUS.get(st, st)}")
+        self.ubuf, self.iubuflow, self.r2umin = np.ascontiguousarray(ubuf[: used[0]]), iub, r2
+        return self
+
+    def params(self):
+        if self.ubuf is None:
+            raise RuntimeError("build_table() must run before params()")
+        k = {"iptpn": abi.as_i32(self.iptpn), "iptpt": iptpt_matrix(self.npt), "napt": self.napt(),
+             "ianpn": self.ianpn(), "iatan": self.iatan(), "iatat": iptpt_matrix(self.nat),
+             "ubuf": abi.as_f64(self.ubuf), "iubuflow": abi.as_i32(self.iubuflow), "r2umin": abi.as_f64(self.r2umin)}
+        p = abi.MgPolyParams()
+        p.abi_version = abi.MG_ABI_VERSION
+        p.np, p.npt, p.nptpt = self.np_, self.npt, self.npt * (self.npt + 1) // 2
+        p.iptpn, p.iptpt, p.napt = abi.i32(k["iptpn"]), abi.i32(k["iptpt"]), abi.i32(k["napt"])
+        p.na = int(len(k["iatan"]))
+        p.ianpn, p.iatan = abi.i32(k["ianpn"]), abi.i32(k["iatan"])
+        p.nat, p.natat = self.nat, self.nat * (self.nat + 1) // 2
+        p.iatat = abi.i32(k["iatat"])
+        p.nbuf = int(len(self.ubuf))
+        p.ubuf, p.iubuflow, p.r2umin = abi.f64(k["ubuf"]), abi.i32(k["iubuflow"]), abi.f64(k["r2umin"])
+        for m in range(3):
+            p.boxlen[m] = float(self.boxlen[m])
+        p.rcut = self.rcut
+        p.lmc = self.lmc
+        self.keep = k
+        return p
+
+
+class PolyEngine:
+    """mg_poly_* for one PolySystem; maxnneigh is the list's leading size."""
+
+    def __init__(self, system, maxnneigh, lib=None):
+        self.s = system
+        self.lib = lib or abi.load_library()
+        self.p = system.params()
+        self.maxnneigh = int(maxnneigh)
+        self.h = C.c_void_p()
+        st = self.lib.mg_poly_create(C.byref(self.p), self.maxnneigh, C.byref(self.h))
+        if st != 0:
+            raise MolsimError(st, "poly_create")
+
+    def UTwoBodyP(self, nneighpn, jpnlist, r=None):
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        force = np.zeros(3 * len(r))
+        ut = np.zeros(self.p.nptpt + 1)
+        vir = np.zeros(1)
+        nn = abi.as_i32(nneighpn)
+        jl = abi.as_i32(np.asarray(jpnlist).reshape(-1))
+        st = self.lib.mg_poly_utwobody(self.h, abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)),
+                                       abi.i32(nn), abi.i32(jl), abi.f64(force), abi.f64(ut), abi.f64(vir))
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.lib.mg_poly_last_error(self.h, buf, 512)
+            raise MolsimError(st, f"poly_utwobody: {buf.value.decode(errors='replace')}")
+        return dict(force=force.reshape(-1, 3), u_twob=ut, virial=float(vir[0]))
+
+    def close(self):
+        if self.h:
+            self.lib.mg_poly_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

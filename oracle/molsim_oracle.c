@@ -1616,6 +1616,77 @@ static void uangle(orc_sys *s) {
     s->u_tot = s->u_tot + s->u_angle;
 }
 
+/* UTwoBodyP, energy.F90:786-896: particles iploc in order, their list
+   neighbours (in MC only jp > ip), the centre separation folded by PBC2
+   (molaux.F90:193-248) and that shift applied to every atom pair; the
+   table search of UTwoBodyA per atom-type pair; u%twob(0) the sum of the
+   type-pair energies.  Atom forces are not scaled (force(3,na)). */
+int orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                      const int32_t *nneighpn, const int32_t *jpnlist, double *force, double *u_twob,
+                      double *virial) {
+    int npt = p->npt, nat = p->nat, nptpt = p->nptpt;
+    double half[3], rcut2 = p->rcut * p->rcut, virtwob = Zero;
+    for (int m = 0; m < 3; ++m) half[m] = p->boxlen[m] / Two;
+    for (int k = 0; k <= nptpt; ++k) u_twob[k] = Zero;
+    for (int k = 0; k < 3 * p->na; ++k) force[k] = Zero;
+    for (int ip = 1; ip <= p->np; ++ip) {
+        int ipt = p->iptpn[ip - 1];
+        int ialow = p->ianpn[ip - 1], iaupp = ialow + p->napt[ipt - 1] - 1;
+        for (int jploc = 1; jploc <= nneighpn[ip - 1]; ++jploc) {
+            int jp = jpnlist[(size_t)(ip - 1) * maxnneigh + jploc - 1];
+            if (p->lmc && jp < ip) continue;
+            int jpt = p->iptpn[jp - 1];
+            int iptjpt = p->iptpt[(jpt - 1) * npt + ipt - 1];
+            double d[3], sh[3];
+            for (int m = 0; m < 3; ++m) {
+                d[m] = ro[3 * (ip - 1) + m] - ro[3 * (jp - 1) + m];
+                sh[m] = Zero;
+                if (fabs(d[m]) > half[m]) sh[m] = fsign(p->boxlen[m], d[m]);
+                d[m] = d[m] - sh[m];
+            }
+            double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (r2 > rcut2) continue;
+            double usum = Zero;
+            int jalow = p->ianpn[jp - 1], jaupp = jalow + p->napt[jpt - 1] - 1;
+            for (int ia = ialow; ia <= iaupp; ++ia) {
+                int iat = p->iatan[ia - 1];
+                for (int ja = jalow; ja <= jaupp; ++ja) {
+                    int jat = p->iatan[ja - 1];
+                    int iatjat = p->iatat[(jat - 1) * nat + iat - 1];
+                    double dx = r[3 * (ia - 1)] - r[3 * (ja - 1)] - sh[0];
+                    double dy = r[3 * (ia - 1) + 1] - r[3 * (ja - 1) + 1] - sh[1];
+                    double dz = r[3 * (ia - 1) + 2] - r[3 * (ja - 1) + 2] - sh[2];
+                    double ar2 = dx * dx + dy * dy + dz * dz;
+                    if (ar2 < p->r2umin[iatjat - 1]) return MG_ERR_TABLE_UNDERRUN;
+                    int ibuf = p->iubuflow[iatjat - 1];
+                    for (;;) {
+                        if (ar2 >= p->ubuf[ibuf - 1]) break;
+                        ibuf = ibuf + 12;
+                        if (ibuf > p->nbuf) return MG_ERR_IBUF;
+                    }
+                    const double *u = &p->ubuf[ibuf - 1];
+                    double dd = ar2 - u[0];
+                    usum = usum + u[1] + dd * (u[2] + dd * (u[3] + dd * (u[4] + dd * (u[5] + dd * u[6]))));
+                    double fsum = u[7] + dd * (u[8] + dd * (u[9] + dd * (u[10] + dd * u[11])));
+                    force[3 * (ia - 1)] = force[3 * (ia - 1)] + (fsum * dx);
+                    force[3 * (ia - 1) + 1] = force[3 * (ia - 1) + 1] + (fsum * dy);
+                    force[3 * (ia - 1) + 2] = force[3 * (ia - 1) + 2] + (fsum * dz);
+                    force[3 * (ja - 1)] = force[3 * (ja - 1)] - (fsum * dx);
+                    force[3 * (ja - 1) + 1] = force[3 * (ja - 1) + 1] - (fsum * dy);
+                    force[3 * (ja - 1) + 2] = force[3 * (ja - 1) + 2] - (fsum * dz);
+                    virtwob = virtwob - (fsum * ar2);
+                }
+            }
+            u_twob[iptjpt] = u_twob[iptjpt] + usum;
+        }
+    }
+    double s = Zero;
+    for (int k = 1; k <= nptpt; ++k) s = s + u_twob[k];
+    u_twob[0] = s;
+    *virial = virtwob;
+    return 0;
+}
+
 /* the energy terms of the last UTotal: u%tot, u%twob(0), u%rec, u%bond,
    u%angle, virial */
 int orc_energy_terms(orc_sys *s, double *terms) {

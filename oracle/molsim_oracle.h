@@ -71,6 +71,11 @@ int  orc_md_run(orc_sys *s, int32_t nstep, double *forceo, double *uout, double 
 int  orc_bd_setup(orc_sys *s, const double *fac1, const double *fac2, int32_t iseed);
 int  orc_bd_run(orc_sys *s, int32_t nstep, double *forceo, double *uout);
 int  orc_bd_get_seed(orc_sys *s, int32_t *iseed);
+/* UTwoBodyP (energy.F90:786-896) for polyatomic particles: no state; the
+   arguments as mg_poly_utwobody's, with maxnneigh the list's leading size */
+int  orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                       const int32_t *nneighpn, const int32_t *jpnlist, double *force, double *u_twob,
+                       double *virial);
 /* the SPME charge mesh after the last spread (before the FFT), n^3 doubles */
 int  orc_get_qmesh(orc_sys *s, double *q);
 

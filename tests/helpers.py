@@ -108,3 +108,25 @@ def chain_system(seed=71, chains=4, nseg=10, **kw):
     s.iptpn = s.iptpn.copy()
     s.iptpn[:chains * nseg] = len(s.species)
     return s
+
+
+def centre_lists(ro, L, rlist, full=False):
+    """A Verlet list of particle centres (nneighpn, jpnlist as NList stores
+    it: 1-based, maxnneigh entries per particle): every pair within rlist
+    (minimum image) once, on its lower-numbered particle, or (full, the MC
+    list) on both."""
+    ro = np.asarray(ro)
+    d = ro[:, None, :] - ro[None, :, :]
+    d -= L * np.round(d / L)
+    r2 = (d * d).sum(-1)
+    n = len(ro)
+    near = (r2 <= rlist * rlist) & ~np.eye(n, dtype=bool)
+    if not full:
+        near &= np.triu(np.ones((n, n), dtype=bool), 1)
+    nn = near.sum(1).astype(np.int32)
+    maxn = max(1, int(nn.max()))
+    jl = np.zeros((n, maxn), dtype=np.int32)
+    for i in range(n):
+        js = np.flatnonzero(near[i]) + 1
+        jl[i, :len(js)] = js
+    return nn, jl, maxn

@@ -60,6 +60,7 @@ int main(void) {
 @FIELDS@
     printf("mg_params sizeof %zu\n", sizeof(mg_params));
     printf("mg_pot_params sizeof %zu\n", sizeof(mg_pot_params));
+    printf("mg_poly_params sizeof %zu\n", sizeof(mg_poly_params));
     return 0;
 }
 """
@@ -67,7 +68,8 @@ int main(void) {
 
 def test_struct_layouts_match_the_header(tmp_path):
     lines = []
-    for T, cls in (("mg_params", abi.MgParams), ("mg_pot_params", abi.MgPotParams)):
+    for T, cls in (("mg_params", abi.MgParams), ("mg_pot_params", abi.MgPotParams),
+                   ("mg_poly_params", abi.MgPolyParams)):
         for name, _ in cls._fields_:
             lines.append(f"    F({T}, {name})")
     src = tmp_path / "layout.c"
@@ -81,7 +83,8 @@ def test_struct_layouts_match_the_header(tmp_path):
         if line:
             T, m, v = line.split()
             got[(T, m)] = int(v)
-    for T, cls in (("mg_params", abi.MgParams), ("mg_pot_params", abi.MgPotParams)):
+    for T, cls in (("mg_params", abi.MgParams), ("mg_pot_params", abi.MgPotParams),
+                   ("mg_poly_params", abi.MgPolyParams)):
         for name, _ in cls._fields_:
             assert getattr(cls, name).offset == got[(T, name)], (T, name)
         assert C.sizeof(cls) == got[(T, "sizeof")], T

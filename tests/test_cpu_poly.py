@@ -1,0 +1,76 @@
+"""UTwoBodyP (energy.F90:786-896) in the oracle: atom forces are minus the
+gradient of its energy, the MC full list gives the half list's sums, and
+the atom-pair table is the library's (bit for bit)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from molsim_gb300 import abi, configs
+from tests.helpers import centre_lists
+
+
+def oracle_poly(orc, s, nn, jl, maxn, r=None, lmc=0):
+    s.lmc = lmc
+    p = s.params()
+    r = s.atom_positions() if r is None else r
+    force = np.zeros(r.size)
+    ut = np.zeros(p.nptpt + 1)
+    vir = np.zeros(1)
+    st = orc.orc_poly_utwobody(C.byref(p), maxn, abi.f64(abi.as_f64(s.ro.reshape(-1))),
+                               abi.f64(np.ascontiguousarray(r.reshape(-1))), abi.i32(abi.as_i32(nn)),
+                               abi.i32(abi.as_i32(jl.reshape(-1))), abi.f64(force), abi.f64(ut), abi.f64(vir))
+    assert st == 0, abi.STATUS.get(st, st)
+    return dict(force=force.reshape(-1, 3), u_twob=ut, virial=vir[0])
+
+
+@pytest.fixture(scope="module")
+def lib():
+    """The library's host-side table builder (no GPU needed)."""
+    import molsim_gb300
+    molsim_gb300.build()
+    return abi.load_library()
+
+
+@pytest.fixture(scope="module")
+def water(orc):
+    s = configs.water_ions(seed=9, nwater=120, nsalt=10, L=18.0)
+    s.build_table(orc.orc_pot_twobody_tab)
+    return s
+
+
+def test_atom_forces_are_minus_the_energy_gradient(water, orc):
+    s = water
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0)
+    r = s.atom_positions()
+    out = oracle_poly(orc, s, nn, jl, maxn, r)
+    f = out["force"]
+    rng = np.random.default_rng(1)
+    h = 1e-5
+    for ia in rng.choice(len(r), 12, replace=False):
+        for m in range(3):
+            up, dn = r.copy(), r.copy()
+            up[ia, m] += h
+            dn[ia, m] -= h
+            uu = oracle_poly(orc, s, nn, jl, maxn, up)["u_twob"][0]
+            ud = oracle_poly(orc, s, nn, jl, maxn, dn)["u_twob"][0]
+            fd = -(uu - ud) / (2 * h)
+            assert abs(fd - f[ia, m]) < 2e-4 * np.abs(f).max(), (ia, m, fd, f[ia, m])
+
+
+def test_full_list_with_lmc_gives_the_half_list_sums(water, orc):
+    s = water
+    a = oracle_poly(orc, s, *centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0), lmc=0)
+    b = oracle_poly(orc, s, *centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0, full=True), lmc=1)
+    assert np.allclose(a["u_twob"], b["u_twob"], rtol=1e-12, atol=0)
+    assert np.allclose(a["force"], b["force"], rtol=0, atol=1e-10 * np.abs(a["force"]).max())
+    assert abs(a["virial"] - b["virial"]) <= 1e-12 * abs(a["virial"])
+    # u%twob(0) is the sum of the type-pair energies; water-water dominates
+    assert abs(a["u_twob"][0] - a["u_twob"][1:].sum()) <= 1e-12 * abs(a["u_twob"][0])
+
+
+def test_atom_table_is_the_library_table(water, lib, orc):
+    from molsim_gb300.configs import water_ions
+    t = water_ions(seed=9, nwater=120, nsalt=10, L=18.0)
+    t.build_table(lib.mg_pot_twobody_tab)
+    assert np.array_equal(t.ubuf, water.ubuf) and np.array_equal(t.iubuflow, water.iubuflow)

@@ -1,0 +1,51 @@
+"""UTwoBodyP on the GPU (mg_poly_utwobody) against the oracle.
+
+Rigid three-site waters and one-atom ions: u%twob per particle-type pair and
+the virial within 1e-10 relative, atom forces within 1e-10 of the largest
+(the GPU adds atom forces with atomics, so only the order of the additions
+differs), for the MD half list and the MC full list; an atom pair below its
+table reports MG_ERR_TABLE_UNDERRUN as the reference's Stop does.
+"""
+import numpy as np
+import pytest
+
+from molsim_gb300 import abi, configs
+from molsim_gb300.engine import MolsimError
+from molsim_gb300.poly import PolyEngine
+from tests.helpers import centre_lists
+from tests.test_cpu_poly import oracle_poly
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("full", [False, True], ids=["half", "mc_full"])
+@pytest.mark.parametrize("seed,nw,ns,L", [(9, 120, 10, 18.0), (10, 400, 30, 30.0)])
+def test_poly_utwobody_matches_oracle(seed, nw, ns, L, full, orc, gpu_lib):
+    s = configs.water_ions(seed=seed, nwater=nw, nsalt=ns, L=L)
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0, full=full)
+    s.lmc = 1 if full else 0
+    ref = oracle_poly(orc, s, nn, jl, maxn, lmc=s.lmc)
+    e = PolyEngine(s, maxn)
+    g = e.UTwoBodyP(nn, jl)
+    for k in range(len(ref["u_twob"])):
+        assert abs(g["u_twob"][k] - ref["u_twob"][k]) <= 1e-10 * abs(ref["u_twob"][0]), k
+    assert abs(g["virial"] - ref["virial"]) <= 1e-10 * abs(ref["virial"])
+    assert np.abs(g["force"] - ref["force"]).max() <= 1e-10 * np.abs(ref["force"]).max()
+    e.close()
+
+
+def test_poly_underrun_is_reported(orc, gpu_lib):
+    s = configs.water_ions(seed=11, nwater=60, nsalt=4, L=14.0)
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0)
+    r = s.atom_positions()
+    # put an atom of particle 2 onto an atom of particle 1 (r2 below every table)
+    j = int(jl[0, 0])   # a neighbour of particle 1
+    ia, ja = 0, int(s.ianpn()[j - 1]) - 1
+    r[ja] = r[ia] + 1e-3
+    e = PolyEngine(s, maxn)
+    with pytest.raises(MolsimError) as ex:
+        e.UTwoBodyP(nn, jl, r=r)
+    assert abi.STATUS[ex.value.status] == "MG_ERR_TABLE_UNDERRUN"
+    e.close()
