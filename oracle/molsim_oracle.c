@@ -161,7 +161,8 @@ double orc_random(int32_t *idum) {
     const int32_t ia = 16807, im = 2147483647, iq = 127773, ir = 2836;
     int32_t k;
     if (*idum <= 0 || rnd_iy < 0) {
-        rnd_am = (double)nextafterf(1.0f, -1.0f) / im;
+        /* nearest(1.0,-1.0)/im: default (single-precision) real, im converted to it */
+        rnd_am = (double)(nextafterf(1.0f, -1.0f) / (float)im);
         rnd_iy = ((888889999 ^ abs(*idum)) | 1);
         rnd_ix = 777755555 ^ abs(*idum);
         *idum = abs(*idum) + 1;
