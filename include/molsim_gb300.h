@@ -339,6 +339,11 @@ typedef struct mg_poly_params {
     double  rcut;             /* cutoff on the particle-centre distance         */
     int32_t lmc;              /* 1: jpnlist is the full (MC) list: a pair is
                                  taken from its lower-numbered particle         */
+    /* Ewald: the atom charges and the damping, for the intramolecular part
+       of UEwaldSelf (mg_poly_ewald_intra); aza may be NULL without Ewald */
+    const double *aza;        /* [na] atom charges (units of e)                 */
+    double  ualpha;
+    double  epsi_four_pi;
 } mg_poly_params;
 
 typedef struct mg_poly mg_poly;
@@ -353,6 +358,14 @@ int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_poly **c);
  * closer than its table (r2 < r2umin) returns MG_ERR_TABLE_UNDERRUN. */
 int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
                      const int32_t *jpnlist, double *force, double *u_twob, double *virial);
+/* The molecular part of UEwaldSelf (energy.F90:1301-1345): within every
+ * particle, each atom pair removes q_i q_j erf(alpha r)/r (the reciprocal
+ * sum counts it, the real-space table does not).  Writes its contribution to
+ * u%rec (EpsiFourPi applied) into *u_rec and to the atom forces into
+ * force[3*na] (unscaled, as force(3,na)).  The atomic self term and the
+ * reciprocal sum over the atoms come from a handle whose particles are the
+ * atoms (mg_utotal). */
+int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, double *u_rec);
 int mg_poly_last_error(const mg_poly *c, char *buf, size_t n);
 int mg_poly_destroy(mg_poly *c);
 

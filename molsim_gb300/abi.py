@@ -60,6 +60,7 @@ class MgPolyParams(C.Structure):
         ("iatan", PI32), ("nat", C.c_int32), ("natat", C.c_int32), ("iatat", PI32),
         ("nbuf", C.c_int32), ("ubuf", PF64), ("iubuflow", PI32), ("r2umin", PF64),
         ("boxlen", C.c_double * 3), ("rcut", C.c_double), ("lmc", C.c_int32),
+        ("aza", PF64), ("ualpha", C.c_double), ("epsi_four_pi", C.c_double),
     ]
 
 
@@ -106,6 +107,7 @@ LIB_ONLY = [
     ("ensemble_destroy", C.c_int, [H]),
     ("poly_create", C.c_int, [C.POINTER(MgPolyParams), C.c_int32, C.POINTER(C.c_void_p)]),
     ("poly_utwobody", C.c_int, [H, PF64, PF64, PI32, PI32, PF64, PF64, PF64]),
+    ("poly_ewald_intra", C.c_int, [H, PF64, PF64, PF64]),
     ("poly_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
     ("poly_destroy", C.c_int, [H]),
     ("ewald_rec_std_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, PF64, C.c_double, C.c_int32,

@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "mg_erf.cuh"
 #include "mg_internal.cuh"
 
 namespace {
@@ -122,6 +123,51 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
     }
 }
 
+// the molecular part of UEwaldSelf: one thread per particle, its atom pairs
+// ia < ja in order; the thread owns its atoms' forces
+__global__ void __launch_bounds__(kPolyThreads) k_ewald_intra(PolyArgs a, const double *__restrict__ aza,
+                                                              double ualpha, double ualpha2, double ewaldfac1,
+                                                              double efp) {
+    __shared__ double red[kPolyThreads];
+    double u = 0.0;
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip < a.np) {
+        int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[a.iptpn[ip] - 1];
+        for (int ia = ialow; ia < iaupp; ++ia)
+            for (int k = 0; k < 3; ++k) a.force[3 * ia + k] = 0.0;
+        for (int ia = ialow; ia < iaupp; ++ia) {
+            for (int ja = ia + 1; ja < iaupp; ++ja) {
+                double dx = __dsub_rn(a.r[3 * ia], a.r[3 * ja]);
+                double dy = __dsub_rn(a.r[3 * ia + 1], a.r[3 * ja + 1]);
+                double dz = __dsub_rn(a.r[3 * ia + 2], a.r[3 * ja + 2]);
+                double r2 = mg_r2_exact(dx, dy, dz);
+                double r1 = sqrt(r2);
+                double r1i = 1.0 / r1;
+                double r2i = __dmul_rn(r1i, r1i);
+                double ex = exp(-__dmul_rn(ualpha2, r2));
+                r1i = __dmul_rn(r1i, mg_erf2(__dmul_rn(ualpha, r1)));
+                double r3i = __dmul_rn(r2i, __dsub_rn(r1i, __dmul_rn(ewaldfac1, ex)));
+                u = __dsub_rn(u, __dmul_rn(__dmul_rn(aza[ia], aza[ja]), r1i));
+                double fac = __dmul_rn(__dmul_rn(__dmul_rn(efp, aza[ia]), aza[ja]), r3i);
+                double fx = __dmul_rn(fac, dx), fy = __dmul_rn(fac, dy), fz = __dmul_rn(fac, dz);
+                a.force[3 * ia] = __dsub_rn(a.force[3 * ia], fx);
+                a.force[3 * ia + 1] = __dsub_rn(a.force[3 * ia + 1], fy);
+                a.force[3 * ia + 2] = __dsub_rn(a.force[3 * ia + 2], fz);
+                a.force[3 * ja] = __dadd_rn(a.force[3 * ja], fx);
+                a.force[3 * ja + 1] = __dadd_rn(a.force[3 * ja + 1], fy);
+                a.force[3 * ja + 2] = __dadd_rn(a.force[3 * ja + 2], fz);
+            }
+        }
+    }
+    red[threadIdx.x] = u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) s = __dadd_rn(s, red[t]);
+        a.part[blockIdx.x] = s;
+    }
+}
+
 }  // namespace
 
 struct mg_poly {
@@ -131,7 +177,7 @@ struct mg_poly {
     int *d_iptpn = nullptr, *d_iptpt = nullptr, *d_napt = nullptr, *d_ianpn = nullptr, *d_iatan = nullptr,
         *d_iatat = nullptr, *d_iubuflow = nullptr, *d_nneigh = nullptr, *d_jpnlist = nullptr, *d_err = nullptr;
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
-           *d_part = nullptr;
+           *d_part = nullptr, *d_aza = nullptr;
     std::vector<double> h_part;
 };
 
@@ -163,7 +209,7 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
     if (!c) return MG_OK;
     void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
-                    c->d_force, c->d_part};
+                    c->d_force, c->d_part, c->d_aza};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -216,7 +262,8 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
         (st = poly_upload(c, &c->d_iatan, p->iatan, na)) ||
         (st = poly_upload(c, &c->d_iatat, p->iatat, (size_t)p->nat * p->nat)) ||
         (st = poly_upload(c, &c->d_iubuflow, p->iubuflow, p->natat)) ||
-        (st = poly_upload(c, &c->d_ubuf, p->ubuf, p->nbuf)) || (st = poly_upload(c, &c->d_r2umin, p->r2umin, p->natat))) {
+        (st = poly_upload(c, &c->d_ubuf, p->ubuf, p->nbuf)) || (st = poly_upload(c, &c->d_r2umin, p->r2umin, p->natat)) ||
+        (p->aza && (st = poly_upload(c, &c->d_aza, p->aza, na)))) {
         mg_poly_destroy(c);
         return st;
     }
@@ -306,5 +353,32 @@ extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, c
     u_twob[0] = tot;
     for (int b = 0; b < c->nblk; ++b) vir += c->h_part[(size_t)b * nv + p.nptpt];
     *virial = vir;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, double *u_rec) {
+    if (!c || !r || !force || !u_rec) return MG_ERR_ARG;
+    if (!c->d_aza) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.aza (atom charges) was not given");
+    const mg_poly_params &p = c->p;
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    PolyArgs a = {};
+    a.np = p.np;
+    a.iptpn = c->d_iptpn;
+    a.napt = c->d_napt;
+    a.ianpn = c->d_ianpn;
+    a.r = c->d_r;
+    a.force = c->d_force;
+    a.part = c->d_part;
+    // UEwaldSelf's constants (EwaldSetup, energy.F90:7040-7042)
+    double ualpha2 = p.ualpha * p.ualpha;
+    double fac = 1.0 / (std::sqrt(3.1415926535897932) * p.ualpha);
+    double ewaldfac1 = fac * 2.0 * ualpha2;
+    k_ewald_intra<<<c->nblk, kPolyThreads>>>(a, c->d_aza, p.ualpha, ualpha2, ewaldfac1, p.epsi_four_pi);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(force, c->d_force, sizeof(double) * 3 * p.na, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->nblk, cudaMemcpyDeviceToHost));
+    double u = 0.0;
+    for (int b = 0; b < c->nblk; ++b) u += c->h_part[b];
+    *u_rec = p.epsi_four_pi * u;   // u%rec = EpsiFourPi*u%rec (UEwald, energy.F90:950)
     return MG_OK;
 }

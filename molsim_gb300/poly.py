@@ -49,6 +49,12 @@ class PolySystem:
     relpermitt: float = 1.0
     lmc: int = 0
     r2uminin: float = 0.1
+    # Ewald over the atom charges (none, standard or SPME, as mg_params)
+    ewald: int = abi.MG_EWALD_NONE
+    ualpha: float = 0.0
+    ncut: int = 0
+    order: int = 0
+    nmesh: int = 0
     ubuf: Optional[np.ndarray] = None
     iubuflow: Optional[np.ndarray] = None
     r2umin: Optional[np.ndarray] = None
@@ -85,9 +91,31 @@ class PolySystem:
             out.append(self.ro[ip] + loc @ self.ori[ip].T)
         return np.ascontiguousarray(np.concatenate(out))
 
+    def aza(self):
+        return np.array([self.atom_types[t - 1].charge for t in self.iatan()], dtype=np.float64)
+
+    @property
+    def epsi_four_pi(self):
+        return units.Epsi0FourPi / self.relpermitt
+
+    def atoms_in_box(self, r=None):
+        """Atom positions folded into the box (PBC, molaux.F90:104-146) for
+        the Ewald sums, which are periodic in each atom position: an atom of
+        a particle near a face may lie just outside the box."""
+        r = self.atom_positions() if r is None else np.array(r, dtype=np.float64).reshape(-1, 3)
+        L = np.asarray(self.boxlen, dtype=np.float64)
+        out = r.copy()
+        for m in range(3):
+            big = np.abs(out[:, m]) > 0.5 * L[m]
+            t = out[:, m] * (1.0 / L[m])
+            a = np.trunc(t)
+            a = a + np.sign(t) * (np.abs(t - a) >= 0.5)
+            out[:, m] = np.where(big, out[:, m] - L[m] * a, out[:, m])
+        return np.ascontiguousarray(out)
+
     def build_table(self, tabfn):
-        """PotTwoBodyTab1 over the atom types (Coulomb without Ewald, plus
-        (1,6,12) Lennard-Jones)."""
+        """PotTwoBodyTab1 over the atom types: (1,6,12) Lennard-Jones plus
+        Coulomb, the real-space Ewald part (CalcEwaldUfac) when Ewald is on."""
         nat = self.nat
         keep = {"iptpt": iptpt_matrix(nat),
                 "zat": abi.as_f64([a.charge for a in self.atom_types]),
@@ -95,7 +123,8 @@ class PolySystem:
                 "epsat": abi.as_f64([a.eps for a in self.atom_types])}
         pp = abi.MgPotParams(npt=nat, iptpt=abi.i32(keep["iptpt"]), zat=abi.f64(keep["zat"]),
                              sigat=abi.f64(keep["sigat"]), epsat=abi.f64(keep["epsat"]), rcut=self.rcut,
-                             ualpha=0.0, epsi_four_pi=units.Epsi0FourPi / self.relpermitt, lcharge_ewald=0,
+                             ualpha=self.ualpha, epsi_four_pi=self.epsi_four_pi,
+                             lcharge_ewald=int(self.ewald != abi.MG_EWALD_NONE),
                              lljcut=0, ljrcut=units.ljrcut_default(), ljushift=1.0, r2uminin=self.r2uminin,
                              utoltab=units.tol_default(), ftoltab=units.tol_default(), umaxtab=20000.0,
                              fmaxtab=20000.0)
@@ -122,7 +151,8 @@ class PolySystem:
             raise RuntimeError("build_table() must run before params()")
         k = {"iptpn": abi.as_i32(self.iptpn), "iptpt": iptpt_matrix(self.npt), "napt": self.napt(),
              "ianpn": self.ianpn(), "iatan": self.iatan(), "iatat": iptpt_matrix(self.nat),
-             "ubuf": abi.as_f64(self.ubuf), "iubuflow": abi.as_i32(self.iubuflow), "r2umin": abi.as_f64(self.r2umin)}
+             "ubuf": abi.as_f64(self.ubuf), "iubuflow": abi.as_i32(self.iubuflow), "r2umin": abi.as_f64(self.r2umin),
+             "aza": self.aza()}
         p = abi.MgPolyParams()
         p.abi_version = abi.MG_ABI_VERSION
         p.np, p.npt, p.nptpt = self.np_, self.npt, self.npt * (self.npt + 1) // 2
@@ -137,8 +167,32 @@ class PolySystem:
             p.boxlen[m] = float(self.boxlen[m])
         p.rcut = self.rcut
         p.lmc = self.lmc
+        p.aza = abi.f64(k["aza"])
+        p.ualpha = self.ualpha
+        p.epsi_four_pi = self.epsi_four_pi
+        p._keep = k        # the arrays live as long as the structure that points at them
         self.keep = k
         return p
+
+    def atom_system(self, rlist=3.0, skin=0.5):
+        """The atoms as a monoatomic System for the reciprocal Ewald sum (and
+        the atomic self term) through a handle: the atom types as species,
+        a two-body table that is zero everywhere (the atom pairs' real-space
+        terms belong to UTwoBodyP), a short list cutoff."""
+        from .system import Species, System
+        sp = [Species(a.name, a.charge, 1.0, 0.0) for a in self.atom_types]
+        nat = self.nat
+        natat = nat * (nat + 1) // 2
+        ubuf = np.zeros(12 * natat)
+        ubuf[0::12] = 1e-4                       # one zero record from r^2 = 1e-4 up
+        s = System(species=sp, iptpn=self.iatan(), ro=self.atoms_in_box(), boxlen=np.asarray(self.boxlen),
+                   relpermitt=self.relpermitt, rcut=rlist, drnlist=skin, ewald=self.ewald, ualpha=self.ualpha,
+                   ncut=self.ncut, order=self.order, nmesh=self.nmesh, lsurf=0, name="atoms")
+        s.ubuf = ubuf
+        s.iubuflow = (np.arange(natat, dtype=np.int32) * 12 + 1)
+        s.r2umin = np.full(natat, 1e-4)
+        s.nugrid = np.ones(natat, dtype=np.int32)
+        return s
 
 
 class PolyEngine:
@@ -169,6 +223,39 @@ class PolyEngine:
             self.lib.mg_poly_last_error(self.h, buf, 512)
             raise MolsimError(st, f"poly_utwobody: {buf.value.decode(errors='replace')}")
         return dict(force=force.reshape(-1, 3), u_twob=ut, virial=float(vir[0]))
+
+    def EwaldIntra(self, r=None):
+        """The molecular part of UEwaldSelf: its u%rec share and atom forces."""
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        force = np.zeros(3 * len(r))
+        u = np.zeros(1)
+        st = self.lib.mg_poly_ewald_intra(self.h, abi.f64(r.reshape(-1)), abi.f64(force), abi.f64(u))
+        if st != 0:
+            raise MolsimError(st, "poly_ewald_intra")
+        return dict(force=force.reshape(-1, 3), u_rec=float(u[0]))
+
+    def UTotal(self, nneighpn, jpnlist, engine_factory=None):
+        """u%tot and the atom forces of a polyatomic system with Ewald: the
+        atom pairs (UTwoBodyP, with the real-space Ewald table), the
+        reciprocal sum and atomic self term over the atoms (a handle of the
+        atoms), and the molecular self term.  Forces in force(3,na) units."""
+        from .engine import Engine
+        s = self.s
+        r = s.atom_positions()
+        tw = self.UTwoBodyP(nneighpn, jpnlist, r)
+        out = dict(u_twob=tw["u_twob"], virial=tw["virial"], force=tw["force"].copy(), u_rec=0.0)
+        if s.ewald != abi.MG_EWALD_NONE:
+            a = s.atom_system()
+            e = engine_factory(a) if engine_factory else Engine(a)
+            e.SetPositions(s.atoms_in_box(r).reshape(-1))
+            e.NList("write")
+            rec = e.UTotal()
+            intra = self.EwaldIntra(r)
+            out["u_rec"] = rec["u_rec"] + intra["u_rec"]
+            out["force"] += rec["forceo"] / units.FORCE_FAC + intra["force"]
+        out["u_tot"] = out["u_twob"][0] + out["u_rec"]
+        return out
 
     def close(self):
         if self.h:

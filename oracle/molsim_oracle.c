@@ -1688,6 +1688,46 @@ int orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double *
     return 0;
 }
 
+/* UEwaldSelf, molecular contribution (energy.F90:1313-1341), with the
+   constants of EwaldSetup (energy.F90:7040-7042) and ErfLocal = Erf2; the
+   result scaled by EpsiFourPi as UEwald does at its end (energy.F90:950) */
+int orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force, double *u_rec) {
+    double ualpha = p->ualpha, ualpha2 = ualpha * ualpha;
+    double fac0 = One / (sqrt(Pi) * ualpha);
+    double ewaldfac1 = fac0 * Two * ualpha2;
+    double u = Zero;
+    for (int k = 0; k < 3 * p->na; ++k) force[k] = Zero;
+    for (int ip = 1; ip <= p->np; ++ip) {
+        int ipt = p->iptpn[ip - 1];
+        int ialow = p->ianpn[ip - 1], iaupp = p->ianpn[ip - 1] + p->napt[ipt - 1] - 1;
+        for (int ia = ialow; ia <= iaupp; ++ia) {
+            for (int ja = ia + 1; ja <= iaupp; ++ja) {
+                double dx = r[3 * (ia - 1)] - r[3 * (ja - 1)];
+                double dy = r[3 * (ia - 1) + 1] - r[3 * (ja - 1) + 1];
+                double dz = r[3 * (ia - 1) + 2] - r[3 * (ja - 1) + 2];
+                double r2 = dx * dx + dy * dy + dz * dz;
+                double r1 = sqrt(r2);
+                double r1i = One / r1;
+                double r2i = r1i * r1i;
+                double ex = exp(-ualpha2 * r2);
+                r1i = r1i * orc_erf2(ualpha * r1);
+                double r3i = r2i * (r1i - ewaldfac1 * ex);
+                double qa = p->aza[ia - 1], qb = p->aza[ja - 1];
+                u = u - (qa * qb * r1i);
+                double fac = p->epsi_four_pi * qa * qb * r3i;
+                force[3 * (ia - 1)] = force[3 * (ia - 1)] - (fac * dx);
+                force[3 * (ia - 1) + 1] = force[3 * (ia - 1) + 1] - (fac * dy);
+                force[3 * (ia - 1) + 2] = force[3 * (ia - 1) + 2] - (fac * dz);
+                force[3 * (ja - 1)] = force[3 * (ja - 1)] + (fac * dx);
+                force[3 * (ja - 1) + 1] = force[3 * (ja - 1) + 1] + (fac * dy);
+                force[3 * (ja - 1) + 2] = force[3 * (ja - 1) + 2] + (fac * dz);
+            }
+        }
+    }
+    *u_rec = p->epsi_four_pi * u;
+    return 0;
+}
+
 /* the energy terms of the last UTotal: u%tot, u%twob(0), u%rec, u%bond,
    u%angle, virial */
 int orc_energy_terms(orc_sys *s, double *terms) {

@@ -76,6 +76,9 @@ int  orc_bd_get_seed(orc_sys *s, int32_t *iseed);
 int  orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
                        const int32_t *nneighpn, const int32_t *jpnlist, double *force, double *u_twob,
                        double *virial);
+/* the molecular part of UEwaldSelf (energy.F90:1301-1345), arguments as
+   mg_poly_ewald_intra's */
+int  orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force, double *u_rec);
 /* the SPME charge mesh after the last spread (before the FFT), n^3 doubles */
 int  orc_get_qmesh(orc_sys *s, double *q);
 

@@ -74,3 +74,43 @@ def test_atom_table_is_the_library_table(water, lib, orc):
     t = water_ions(seed=9, nwater=120, nsalt=10, L=18.0)
     t.build_table(lib.mg_pot_twobody_tab)
     assert np.array_equal(t.ubuf, water.ubuf) and np.array_equal(t.iubuflow, water.iubuflow)
+
+
+def oracle_poly_utotal(orc, s, nn, jl, maxn):
+    """The polyatomic UTotal with Ewald on the oracle: UTwoBodyP with the
+    real-space table, the atoms' reciprocal sum and self term (a handle of
+    the atoms with a zero pair table), the molecular self term."""
+    from molsim_gb300 import Engine, units
+    p = s.params()
+    r = s.atom_positions()
+    tw = oracle_poly(orc, s, nn, jl, maxn, r, lmc=s.lmc)
+    a = s.atom_system()
+    e = Engine(a, lib=orc, prefix="orc_")
+    e.SetPositions(s.atoms_in_box(r).reshape(-1))
+    e.NList("write")
+    rec = e.UTotal()
+    fi = np.zeros(r.size)
+    ui = np.zeros(1)
+    assert orc.orc_poly_ewald_intra(C.byref(p), abi.f64(np.ascontiguousarray(r.reshape(-1))), abi.f64(fi),
+                                    abi.f64(ui)) == 0
+    force = tw["force"] + rec["forceo"] / units.FORCE_FAC + fi.reshape(-1, 3)
+    u_rec = rec["u_rec"] + ui[0]
+    return dict(u_twob=tw["u_twob"], u_rec=u_rec, u_tot=tw["u_twob"][0] + u_rec, force=force,
+                parts=(tw["u_twob"][0], rec["u_rec"], ui[0]))
+
+
+def test_ewald_splitting_does_not_change_the_energy(orc):
+    """With the molecular self term, the total energy does not depend on the
+    Ewald split: alpha 0.45 and 0.55 agree to the table tolerance while the
+    reciprocal and molecular terms each change by about a hundred kJ/mol."""
+    tot, parts = [], []
+    for alpha, ncut in ((0.45, 14), (0.55, 18)):
+        s = configs.water_ions(seed=9, nwater=120, nsalt=10, L=18.0)
+        s.ewald, s.ualpha, s.ncut, s.relpermitt = abi.MG_EWALD_STD, alpha, ncut, 78.0
+        s.build_table(orc.orc_pot_twobody_tab)
+        out = oracle_poly_utotal(orc, s, *centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0))
+        tot.append(out["u_tot"])
+        parts.append(out["parts"])
+    scale = abs(parts[0][1]) + abs(parts[0][2])
+    assert abs(parts[0][2] - parts[1][2]) > 50.0        # the split moves energy between the terms
+    assert abs(tot[0] - tot[1]) <= 1e-4 * scale, (tot, parts)

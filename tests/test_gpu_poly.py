@@ -49,3 +49,28 @@ def test_poly_underrun_is_reported(orc, gpu_lib):
         e.UTwoBodyP(nn, jl, r=r)
     assert abi.STATUS[ex.value.status] == "MG_ERR_TABLE_UNDERRUN"
     e.close()
+
+
+@pytest.mark.parametrize("ewald", ["spm", "std"])
+def test_poly_utotal_with_ewald_matches_oracle(ewald, orc, gpu_lib):
+    """UTwoBodyP with the real-space Ewald table, the reciprocal sum and self
+    term over the atoms, and the molecular self term: the GPU against the
+    oracle, u%tot and u%rec within 1e-10, atom forces within 1e-10 of the
+    largest."""
+    from tests.test_cpu_poly import oracle_poly_utotal
+    s = configs.water_ions(seed=12, nwater=150, nsalt=10, L=20.0)
+    s.relpermitt = 78.0
+    if ewald == "spm":
+        s.ewald, s.ualpha, s.order, s.nmesh = abi.MG_EWALD_SPM, 0.4, 6, 32
+    else:
+        s.ewald, s.ualpha, s.ncut = abi.MG_EWALD_STD, 0.4, 10
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0)
+    ref = oracle_poly_utotal(orc, s, nn, jl, maxn)
+    e = PolyEngine(s, maxn)
+    g = e.UTotal(nn, jl)
+    scale = abs(ref["parts"][0]) + abs(ref["parts"][1]) + abs(ref["parts"][2])
+    assert abs(g["u_tot"] - ref["u_tot"]) <= 1e-10 * scale
+    assert abs(g["u_rec"] - ref["u_rec"]) <= 1e-10 * scale
+    assert np.abs(g["force"] - ref["force"]).max() <= 1e-10 * np.abs(ref["force"]).max()
+    e.close()
