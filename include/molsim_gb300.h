@@ -335,6 +335,7 @@ typedef struct mg_poly_params {
     const double  *ubuf;      /* [nbuf]                                         */
     const int32_t *iubuflow;  /* [natat] 1-based                                */
     const double  *r2umin;    /* [natat]                                        */
+    const double  *r2atat;    /* [natat] hard-core distance squared (MC trials) */
     double  boxlen[3];        /* box edges; box centred at the origin           */
     double  rcut;             /* cutoff on the particle-centre distance         */
     int32_t lmc;              /* 1: jpnlist is the full (MC) list: a pair is
@@ -366,6 +367,17 @@ int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, const int32_
  * reciprocal sum over the atoms come from a handle whose particles are the
  * atoms (mg_utotal). */
 int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, double *u_rec);
+/* Single-particle MC trials of polyatomic particles (DUTwoBody with
+ * UTwoBodyPNew/UTwoBodyPOld, denergy.F90:937-1231, for nptm = 1): trial t
+ * moves particle ip[t] (1-based) to centre rotm[3*t] with its atoms at
+ * rtm (the atoms of all trials one after another, napt of each particle's
+ * type).  Every trial is against the same current state (ro, r and the
+ * full MC list nneighpn, jpnlist).  Writes du_twob[t] = u%twob(0) new minus
+ * old and lhsoverlap[t] (an atom pair of the trial below r2atat or r2umin:
+ * the reference's hard-core rejection); the trials run in parallel. */
+int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
+                            const int32_t *jpnlist, int32_t ntrial, const int32_t *ip, const double *rotm,
+                            const double *rtm, double *du_twob, int32_t *lhsoverlap);
 int mg_poly_last_error(const mg_poly *c, char *buf, size_t n);
 int mg_poly_destroy(mg_poly *c);
 

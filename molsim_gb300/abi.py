@@ -58,7 +58,7 @@ class MgPolyParams(C.Structure):
         ("abi_version", C.c_int32), ("np", C.c_int32), ("npt", C.c_int32), ("nptpt", C.c_int32),
         ("iptpn", PI32), ("iptpt", PI32), ("napt", PI32), ("na", C.c_int32), ("ianpn", PI32),
         ("iatan", PI32), ("nat", C.c_int32), ("natat", C.c_int32), ("iatat", PI32),
-        ("nbuf", C.c_int32), ("ubuf", PF64), ("iubuflow", PI32), ("r2umin", PF64),
+        ("nbuf", C.c_int32), ("ubuf", PF64), ("iubuflow", PI32), ("r2umin", PF64), ("r2atat", PF64),
         ("boxlen", C.c_double * 3), ("rcut", C.c_double), ("lmc", C.c_int32),
         ("aza", PF64), ("ualpha", C.c_double), ("epsi_four_pi", C.c_double),
     ]
@@ -108,6 +108,7 @@ LIB_ONLY = [
     ("poly_create", C.c_int, [C.POINTER(MgPolyParams), C.c_int32, C.POINTER(C.c_void_p)]),
     ("poly_utwobody", C.c_int, [H, PF64, PF64, PI32, PI32, PF64, PF64, PF64]),
     ("poly_ewald_intra", C.c_int, [H, PF64, PF64, PF64]),
+    ("poly_dutwobody_batch", C.c_int, [H, PF64, PF64, PI32, PI32, C.c_int32, PI32, PF64, PF64, PF64, PI32]),
     ("poly_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
     ("poly_destroy", C.c_int, [H]),
     ("ewald_rec_std_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, PF64, C.c_double, C.c_int32,

@@ -32,7 +32,7 @@ struct PolyArgs {
     int np, nptpt, maxnneigh, lmc, nbuf;
     const int *iptpn, *iptpt, *napt, *ianpn, *iatan, *iatat, *iubuflow;
     int npt, nat;
-    const double *ubuf, *r2umin;
+    const double *ubuf, *r2umin, *r2atat;
     const double *ro, *r;
     const int *nneighpn, *jpnlist;
     double len[3], half[3], rcut2;
@@ -168,6 +168,100 @@ __global__ void __launch_bounds__(kPolyThreads) k_ewald_intra(PolyArgs a, const 
     }
 }
 
+// the tabulated energy of one atom pair (UTwoBodyA's search and Horner
+// sums); 0: ok, MG_ERR_IBUF past the table
+__device__ __forceinline__ int poly_pair_u(const PolyArgs &a, int iatjat, double r2, double *u) {
+    int ibuf = a.iubuflow[iatjat - 1] - 1;
+    while (!(r2 >= a.ubuf[ibuf])) {
+        ibuf += 12;
+        if (ibuf >= a.nbuf) return MG_ERR_IBUF;
+    }
+    const double *c = a.ubuf + ibuf;
+    double d = __dsub_rn(r2, c[0]);
+    *u = __dadd_rn(c[1], __dmul_rn(d, __dadd_rn(c[2], __dmul_rn(d, __dadd_rn(c[3], __dmul_rn(d,
+         __dadd_rn(c[4], __dmul_rn(d, __dadd_rn(c[5], __dmul_rn(d, c[6]))))))))));
+    return 0;
+}
+
+// Single-particle trials (UTwoBodyPNew minus UTwoBodyPOld, nptm = 1): one
+// warp per trial, lanes over the moving particle's list row; the energy of
+// each neighbour with the trial centre and atoms (a hard core or a pair
+// below its table rejects the trial, lhsoverlap) minus that with the
+// current ones.
+__global__ void k_poly_dutwobody(PolyArgs a, int ntrial, const int *__restrict__ tip,
+                                 const double *__restrict__ trotm, const double *__restrict__ trtm,
+                                 const int *__restrict__ tatom0, double *__restrict__ du,
+                                 int *__restrict__ ovl) {
+    int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (t >= ntrial) return;
+    int ip = tip[t] - 1, ipt = a.iptpn[ip];
+    int ialow = a.ianpn[ip] - 1, nai = a.napt[ipt - 1];
+    const double *rn = trotm + 3 * t, *rt = trtm + 3 * (size_t)tatom0[t];
+    double dnew = 0.0, dold = 0.0;
+    int bad = 0;
+    int nn = a.nneighpn[ip];
+    for (int jploc = lane; jploc < nn; jploc += 32) {
+        int jp = a.jpnlist[(size_t)ip * a.maxnneigh + jploc] - 1;
+        if (jp == ip) continue;
+        int jpt = a.iptpn[jp];
+        int jalow = a.ianpn[jp] - 1, naj = a.napt[jpt - 1];
+        for (int pass = 0; pass < 2; ++pass) {   // 0: trial (new), 1: current (old)
+            const double *ci = pass ? a.ro + 3 * ip : rn;
+            double sh[3], r2 = 0.0;
+            {
+                double d[3];
+                for (int m = 0; m < 3; ++m) {
+                    d[m] = __dsub_rn(ci[m], a.ro[3 * jp + m]);
+                    sh[m] = fabs(d[m]) > a.half[m] ? copysign(a.len[m], d[m]) : 0.0;
+                    d[m] = __dsub_rn(d[m], sh[m]);
+                }
+                r2 = mg_r2_exact(d[0], d[1], d[2]);
+            }
+            if (r2 > a.rcut2) continue;
+            double usum = 0.0;
+            for (int k = 0; k < nai; ++k) {
+                const double *ra = pass ? a.r + 3 * (size_t)(ialow + k) : rt + 3 * k;
+                int iat = a.iatan[ialow + k];
+                for (int l = 0; l < naj; ++l) {
+                    int ja = jalow + l, jat = a.iatan[ja];
+                    int iatjat = a.iatat[(jat - 1) * a.nat + (iat - 1)];
+                    double dx = __dsub_rn(__dsub_rn(ra[0], a.r[3 * ja]), sh[0]);
+                    double dy = __dsub_rn(__dsub_rn(ra[1], a.r[3 * ja + 1]), sh[1]);
+                    double dz = __dsub_rn(__dsub_rn(ra[2], a.r[3 * ja + 2]), sh[2]);
+                    double ar2 = mg_r2_exact(dx, dy, dz);
+                    if (pass == 0 && (ar2 < a.r2atat[iatjat - 1] || ar2 < a.r2umin[iatjat - 1])) {
+                        bad = 1;
+                        continue;
+                    }
+                    if (pass == 1 && ar2 < a.r2umin[iatjat - 1]) {
+                        mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, ialow + k + 1, ja + 1, iatjat);
+                        continue;
+                    }
+                    double u;
+                    int st = poly_pair_u(a, iatjat, ar2, &u);
+                    if (st) {
+                        mg_dev_error(a.err, st, iatjat, ialow + k + 1, ja + 1);
+                        continue;
+                    }
+                    usum = __dadd_rn(usum, u);
+                }
+            }
+            if (pass == 0) dnew = __dadd_rn(dnew, usum);
+            else dold = __dadd_rn(dold, usum);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dnew += __shfl_xor_sync(0xffffffffu, dnew, o);
+        dold += __shfl_xor_sync(0xffffffffu, dold, o);
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) {
+        ovl[t] = bad;
+        du[t] = bad ? 0.0 : __dsub_rn(dnew, dold);
+    }
+}
+
 }  // namespace
 
 struct mg_poly {
@@ -175,7 +269,10 @@ struct mg_poly {
     int maxnneigh = 0, nblk = 0;
     std::string err;
     int *d_iptpn = nullptr, *d_iptpt = nullptr, *d_napt = nullptr, *d_ianpn = nullptr, *d_iatan = nullptr,
-        *d_iatat = nullptr, *d_iubuflow = nullptr, *d_nneigh = nullptr, *d_jpnlist = nullptr, *d_err = nullptr;
+        *d_iatat = nullptr, *d_iubuflow = nullptr, *d_nneigh = nullptr, *d_jpnlist = nullptr, *d_err = nullptr,
+        *d_tip = nullptr, *d_tatom0 = nullptr, *d_tovl = nullptr;
+    double *d_r2atat = nullptr, *d_trotm = nullptr, *d_trtm = nullptr, *d_tdu = nullptr;
+    int tcap = 0, tacap = 0;
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
            *d_part = nullptr, *d_aza = nullptr;
     std::vector<double> h_part;
@@ -209,7 +306,8 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
     if (!c) return MG_OK;
     void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
-                    c->d_force, c->d_part, c->d_aza};
+                    c->d_force, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
+                    c->d_trotm, c->d_trtm, c->d_tdu};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -263,7 +361,8 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
         (st = poly_upload(c, &c->d_iatat, p->iatat, (size_t)p->nat * p->nat)) ||
         (st = poly_upload(c, &c->d_iubuflow, p->iubuflow, p->natat)) ||
         (st = poly_upload(c, &c->d_ubuf, p->ubuf, p->nbuf)) || (st = poly_upload(c, &c->d_r2umin, p->r2umin, p->natat)) ||
-        (p->aza && (st = poly_upload(c, &c->d_aza, p->aza, na)))) {
+        (p->aza && (st = poly_upload(c, &c->d_aza, p->aza, na))) ||
+        (p->r2atat && (st = poly_upload(c, &c->d_r2atat, p->r2atat, p->natat)))) {
         mg_poly_destroy(c);
         return st;
     }
@@ -380,5 +479,105 @@ extern "C" int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, d
     double u = 0.0;
     for (int b = 0; b < c->nblk; ++b) u += c->h_part[b];
     *u_rec = p.epsi_four_pi * u;   // u%rec = EpsiFourPi*u%rec (UEwald, energy.F90:950)
+    return MG_OK;
+}
+
+static PolyArgs poly_args(mg_poly *c) {
+    const mg_poly_params &p = c->p;
+    PolyArgs a = {};
+    a.np = p.np;
+    a.nptpt = p.nptpt;
+    a.maxnneigh = c->maxnneigh;
+    a.lmc = p.lmc;
+    a.nbuf = p.nbuf;
+    a.iptpn = c->d_iptpn;
+    a.iptpt = c->d_iptpt;
+    a.napt = c->d_napt;
+    a.ianpn = c->d_ianpn;
+    a.iatan = c->d_iatan;
+    a.iatat = c->d_iatat;
+    a.iubuflow = c->d_iubuflow;
+    a.npt = p.npt;
+    a.nat = p.nat;
+    a.ubuf = c->d_ubuf;
+    a.r2umin = c->d_r2umin;
+    a.r2atat = c->d_r2atat;
+    a.ro = c->d_ro;
+    a.r = c->d_r;
+    a.nneighpn = c->d_nneigh;
+    a.jpnlist = c->d_jpnlist;
+    for (int m = 0; m < 3; ++m) {
+        a.len[m] = p.boxlen[m];
+        a.half[m] = 0.5 * p.boxlen[m];
+    }
+    a.rcut2 = p.rcut * p.rcut;
+    a.force = c->d_force;
+    a.part = c->d_part;
+    a.err = c->d_err;
+    return a;
+}
+
+extern "C" int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
+                                       const int32_t *jpnlist, int32_t ntrial, const int32_t *ip,
+                                       const double *rotm, const double *rtm, double *du_twob,
+                                       int32_t *lhsoverlap) {
+    if (!c || !ro || !r || !nneighpn || !jpnlist || ntrial < 0 || (ntrial && (!ip || !rotm || !rtm || !du_twob ||
+                                                                               !lhsoverlap)))
+        return MG_ERR_ARG;
+    if (ntrial == 0) return MG_OK;
+    if (!c->d_r2atat) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.r2atat was not given");
+    const mg_poly_params &p = c->p;
+    int np = p.np;
+    std::vector<int> atom0(ntrial);
+    int tot = 0;
+    for (int t = 0; t < ntrial; ++t) {
+        if (ip[t] < 1 || ip[t] > np) return poly_fail(c, MG_ERR_ARG, "ip(%d) = %d", t + 1, ip[t]);
+        atom0[t] = tot;
+        tot += p.napt[p.iptpn[ip[t] - 1] - 1];
+    }
+    for (int i = 0; i < np; ++i)
+        if (nneighpn[i] < 0 || nneighpn[i] > c->maxnneigh)
+            return poly_fail(c, MG_ERR_NEIGH_OVERFLOW, "nneighpn(%d) = %d > maxnneigh %d", i + 1, nneighpn[i],
+                             c->maxnneigh);
+    if (ntrial > c->tcap) {
+        void *q[] = {c->d_tip, c->d_tatom0, c->d_tovl, c->d_trotm, c->d_tdu};
+        for (void *x : q)
+            if (x) cudaFree(x);
+        c->d_tip = c->d_tatom0 = c->d_tovl = nullptr;
+        c->d_trotm = c->d_tdu = nullptr;
+        POLY_CUDA(c, cudaMalloc(&c->d_tip, sizeof(int) * ntrial));
+        POLY_CUDA(c, cudaMalloc(&c->d_tatom0, sizeof(int) * ntrial));
+        POLY_CUDA(c, cudaMalloc(&c->d_tovl, sizeof(int) * ntrial));
+        POLY_CUDA(c, cudaMalloc(&c->d_trotm, sizeof(double) * 3 * ntrial));
+        POLY_CUDA(c, cudaMalloc(&c->d_tdu, sizeof(double) * ntrial));
+        c->tcap = ntrial;
+    }
+    if (tot > c->tacap) {
+        if (c->d_trtm) cudaFree(c->d_trtm);
+        c->d_trtm = nullptr;
+        POLY_CUDA(c, cudaMalloc(&c->d_trtm, sizeof(double) * 3 * tot));
+        c->tacap = tot;
+    }
+    POLY_CUDA(c, cudaMemcpy(c->d_ro, ro, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_nneigh, nneighpn, sizeof(int) * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_jpnlist, jpnlist, sizeof(int) * (size_t)c->maxnneigh * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_tip, ip, sizeof(int) * ntrial, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_tatom0, atom0.data(), sizeof(int) * ntrial, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_trotm, rotm, sizeof(double) * 3 * ntrial, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_trtm, rtm, sizeof(double) * 3 * tot, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemset(c->d_err, 0, sizeof(int) * 4));
+    PolyArgs a = poly_args(c);
+    int threads = 128, blocks = (int)(((long)ntrial * 32 + threads - 1) / threads);
+    k_poly_dutwobody<<<blocks, threads>>>(a, ntrial, c->d_tip, c->d_trotm, c->d_trtm, c->d_tatom0, c->d_tdu,
+                                          c->d_tovl);
+    POLY_CUDA(c, cudaGetLastError());
+    int herr[4];
+    POLY_CUDA(c, cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr[0] == MG_ERR_TABLE_UNDERRUN)
+        return poly_fail(c, herr[0], "current state: r2 < r2umin for atoms %d and %d", herr[1], herr[2]);
+    if (herr[0]) return poly_fail(c, herr[0], "ibuf > nbuf for atom-type pair %d", herr[1]);
+    POLY_CUDA(c, cudaMemcpy(du_twob, c->d_tdu, sizeof(double) * ntrial, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(lhsoverlap, c->d_tovl, sizeof(int) * ntrial, cudaMemcpyDeviceToHost));
     return MG_OK;
 }

@@ -152,7 +152,7 @@ class PolySystem:
         k = {"iptpn": abi.as_i32(self.iptpn), "iptpt": iptpt_matrix(self.npt), "napt": self.napt(),
              "ianpn": self.ianpn(), "iatan": self.iatan(), "iatat": iptpt_matrix(self.nat),
              "ubuf": abi.as_f64(self.ubuf), "iubuflow": abi.as_i32(self.iubuflow), "r2umin": abi.as_f64(self.r2umin),
-             "aza": self.aza()}
+             "aza": self.aza(), "r2atat": np.zeros(self.nat * (self.nat + 1) // 2)}
         p = abi.MgPolyParams()
         p.abi_version = abi.MG_ABI_VERSION
         p.np, p.npt, p.nptpt = self.np_, self.npt, self.npt * (self.npt + 1) // 2
@@ -163,6 +163,7 @@ class PolySystem:
         p.iatat = abi.i32(k["iatat"])
         p.nbuf = int(len(self.ubuf))
         p.ubuf, p.iubuflow, p.r2umin = abi.f64(k["ubuf"]), abi.i32(k["iubuflow"]), abi.f64(k["r2umin"])
+        p.r2atat = abi.f64(k["r2atat"])   # atoms without a hard core
         for m in range(3):
             p.boxlen[m] = float(self.boxlen[m])
         p.rcut = self.rcut
@@ -223,6 +224,28 @@ class PolyEngine:
             self.lib.mg_poly_last_error(self.h, buf, 512)
             raise MolsimError(st, f"poly_utwobody: {buf.value.decode(errors='replace')}")
         return dict(force=force.reshape(-1, 3), u_twob=ut, virial=float(vir[0]))
+
+    def DUTwoBodyBatch(self, nneighpn, jpnlist, ips, rotm, rtm, r=None):
+        """Independent single-particle trials against the current state:
+        particle ips[t] to centre rotm[t] with atoms rtm (the trials' atoms
+        one after another).  Returns du_twob (u%twob(0) new minus old) and
+        the hard-core overlap flags."""
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        ips = abi.as_i32(np.atleast_1d(ips))
+        n = len(ips)
+        du = np.zeros(n)
+        ovl = np.zeros(n, dtype=np.int32)
+        st = self.lib.mg_poly_dutwobody_batch(
+            self.h, abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)), abi.i32(abi.as_i32(nneighpn)),
+            abi.i32(abi.as_i32(np.asarray(jpnlist).reshape(-1))), n, abi.i32(ips),
+            abi.f64(abi.as_f64(np.asarray(rotm).reshape(-1))), abi.f64(abi.as_f64(np.asarray(rtm).reshape(-1))),
+            abi.f64(du), abi.i32(ovl))
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.lib.mg_poly_last_error(self.h, buf, 512)
+            raise MolsimError(st, f"poly_dutwobody_batch: {buf.value.decode(errors='replace')}")
+        return du, ovl.astype(bool)
 
     def EwaldIntra(self, r=None):
         """The molecular part of UEwaldSelf: its u%rec share and atom forces."""

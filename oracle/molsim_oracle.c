@@ -1688,6 +1688,88 @@ int orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double *
     return 0;
 }
 
+/* the atom-pair sum of one particle pair for UTwoBodyPNew/Old: centre ci
+   and atoms ra (napt of ip's type) against particle jp; returns 1 on a
+   hard-core or table underrun (only checked with lnew), -1 past the table */
+static int poly_pair_sum(const mg_poly_params *p, int ipt, int ialow, const double *ci, const double *ra,
+                         const double *ro, const double *r, int jp, int lnew, double *usum_out, int *inrange) {
+    double d[3], sh[3];
+    *inrange = 0;
+    for (int m = 0; m < 3; ++m) {
+        d[m] = ci[m] - ro[3 * (jp - 1) + m];
+        sh[m] = Zero;
+        if (fabs(d[m]) > p->boxlen[m] / Two) sh[m] = fsign(p->boxlen[m], d[m]);
+        d[m] = d[m] - sh[m];
+    }
+    double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (r2 > p->rcut * p->rcut) return 0;
+    *inrange = 1;
+    int jpt = p->iptpn[jp - 1];
+    int jalow = p->ianpn[jp - 1], jaupp = jalow + p->napt[jpt - 1] - 1;
+    double usum = Zero;
+    for (int k = 0; k < p->napt[ipt - 1]; ++k) {
+        int iat = p->iatan[ialow - 1 + k];
+        for (int ja = jalow; ja <= jaupp; ++ja) {
+            int jat = p->iatan[ja - 1];
+            int iatjat = p->iatat[(jat - 1) * p->nat + iat - 1];
+            double dx = ra[3 * k] - r[3 * (ja - 1)] - sh[0];
+            double dy = ra[3 * k + 1] - r[3 * (ja - 1) + 1] - sh[1];
+            double dz = ra[3 * k + 2] - r[3 * (ja - 1) + 2] - sh[2];
+            double ar2 = dx * dx + dy * dy + dz * dz;
+            if (lnew && ar2 < p->r2atat[iatjat - 1]) return 1;
+            if (ar2 < p->r2umin[iatjat - 1]) return 1;
+            int ibuf = p->iubuflow[iatjat - 1];
+            for (;;) {
+                if (ar2 >= p->ubuf[ibuf - 1]) break;
+                ibuf = ibuf + 12;
+                if (ibuf > p->nbuf) return -1;
+            }
+            const double *u = &p->ubuf[ibuf - 1];
+            double dd = ar2 - u[0];
+            usum = usum + u[1] + dd * (u[2] + dd * (u[3] + dd * (u[4] + dd * (u[5] + dd * u[6]))));
+        }
+    }
+    *usum_out = usum;
+    return 0;
+}
+
+int orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                       const int32_t *nneighpn, const int32_t *jpnlist, int32_t ip, const double *rotm,
+                       const double *rtm, double *du_twob, int32_t *lhsoverlap) {
+    int nptpt = p->nptpt, ipt = p->iptpn[ip - 1], ialow = p->ianpn[ip - 1];
+    double unew[64], uold[64];   /* nptpt + 1 entries */
+    if (nptpt + 1 > 64) return MG_ERR_ARG;
+    for (int k = 0; k <= nptpt; ++k) unew[k] = uold[k] = du_twob[k] = Zero;
+    *lhsoverlap = 1;
+    for (int pass = 0; pass < 2; ++pass) {   /* UTwoBodyPNew, then UTwoBodyPOld */
+        const double *ci = pass ? &ro[3 * (ip - 1)] : rotm;
+        const double *ra = pass ? &r[3 * (ialow - 1)] : rtm;
+        double *acc = pass ? uold : unew;
+        for (int jploc = 1; jploc <= nneighpn[ip - 1]; ++jploc) {
+            int jp = jpnlist[(size_t)(ip - 1) * maxnneigh + jploc - 1];
+            if (jp == ip) continue;   /* lptm(jp) */
+            double usum;
+            int inr, st = poly_pair_sum(p, ipt, ialow, ci, ra, ro, r, jp, pass == 0, &usum, &inr);
+            if (st < 0) return MG_ERR_IBUF;
+            if (st > 0) {
+                if (pass == 0) return 0;          /* hard-core overlap: the trial is rejected */
+                return MG_ERR_TABLE_UNDERRUN;
+            }
+            if (!inr) continue;
+            int iptjpt = p->iptpt[(p->iptpn[jp - 1] - 1) * p->npt + ipt - 1];
+            acc[iptjpt] = acc[iptjpt] + usum;
+        }
+    }
+    *lhsoverlap = 0;
+    double s = Zero;
+    for (int k = 1; k <= nptpt; ++k) {
+        du_twob[k] = unew[k] - uold[k];
+        s = s + du_twob[k];
+    }
+    du_twob[0] = s;
+    return 0;
+}
+
 /* UEwaldSelf, molecular contribution (energy.F90:1313-1341), with the
    constants of EwaldSetup (energy.F90:7040-7042) and ErfLocal = Erf2; the
    result scaled by EpsiFourPi as UEwald does at its end (energy.F90:950) */

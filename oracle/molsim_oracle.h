@@ -76,6 +76,11 @@ int  orc_bd_get_seed(orc_sys *s, int32_t *iseed);
 int  orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
                        const int32_t *nneighpn, const int32_t *jpnlist, double *force, double *u_twob,
                        double *virial);
+/* one single-particle polyatomic trial (UTwoBodyPNew/UTwoBodyPOld,
+   denergy.F90:937-1231, nptm = 1): du_twob[nptpt+1] and the overlap flag */
+int  orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                        const int32_t *nneighpn, const int32_t *jpnlist, int32_t ip, const double *rotm,
+                        const double *rtm, double *du_twob, int32_t *lhsoverlap);
 /* the molecular part of UEwaldSelf (energy.F90:1301-1345), arguments as
    mg_poly_ewald_intra's */
 int  orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force, double *u_rec);

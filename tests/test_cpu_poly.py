@@ -114,3 +114,65 @@ def test_ewald_splitting_does_not_change_the_energy(orc):
     scale = abs(parts[0][1]) + abs(parts[0][2])
     assert abs(parts[0][2] - parts[1][2]) > 50.0        # the split moves energy between the terms
     assert abs(tot[0] - tot[1]) <= 1e-4 * scale, (tot, parts)
+
+
+def poly_trials(s, rng, n, step=0.8, angle=0.4):
+    """n single-particle trials: a random particle displaced by up to step
+    and turned by up to angle radians about a random axis; returns ips
+    (1-based), trial centres, the trials' atoms, and per trial its atoms."""
+    from molsim_gb300.mc import axis_angle_matrix
+    L = s.boxlen[0]
+    ips = rng.integers(s.np_, size=n) + 1
+    rotm = np.empty((n, 3))
+    atoms = []
+    for t, ip in enumerate(ips):
+        c = s.ro[ip - 1] + rng.uniform(-step, step, 3)
+        c -= L * np.round(c / L)
+        rotm[t] = c
+        R = axis_angle_matrix(rng.normal(size=3), rng.uniform(-angle, angle)) @ s.ori[ip - 1]
+        loc = np.array([x for _, x in s.particle_types[s.iptpn[ip - 1] - 1].atoms])
+        atoms.append(c + loc @ R.T)
+    return ips, rotm, atoms
+
+
+def oracle_trial(orc, s, nn, jl, maxn, ip, c, atoms):
+    p = s.params()
+    du = np.zeros(p.nptpt + 1)
+    ovl = np.zeros(1, dtype=np.int32)
+    st = orc.orc_poly_dutwobody(C.byref(p), maxn, abi.f64(abi.as_f64(s.ro.reshape(-1))),
+                                abi.f64(np.ascontiguousarray(s.atom_positions().reshape(-1))),
+                                abi.i32(abi.as_i32(nn)), abi.i32(abi.as_i32(jl.reshape(-1))), int(ip),
+                                abi.f64(abi.as_f64(c)), abi.f64(np.ascontiguousarray(atoms.reshape(-1))),
+                                abi.f64(du), abi.i32(ovl))
+    assert st == 0, abi.STATUS.get(st, st)
+    return du, bool(ovl[0])
+
+
+def test_trial_differences_match_full_energies(water, orc):
+    """du%twob of a trial (UTwoBodyPNew minus UTwoBodyPOld) equals UTwoBodyP
+    of the moved configuration minus that of the current one."""
+    s = water
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0, full=True)
+    hn, hl, hmax = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0)
+    u0 = oracle_poly(orc, s, hn, hl, hmax)["u_twob"][0]
+    rng = np.random.default_rng(4)
+    ips, rotm, atoms = poly_trials(s, rng, 12)
+    nchecked = 0
+    for ip, c, a in zip(ips, rotm, atoms):
+        du, ovl = oracle_trial(orc, s, nn, jl, maxn, ip, c, a)
+        if ovl:
+            continue
+        r = s.atom_positions()
+        a0 = int(s.ianpn()[ip - 1]) - 1
+        r[a0:a0 + len(a)] = a
+        ro = s.ro.copy()
+        ro[ip - 1] = c
+        keep = s.ro
+        s.ro = ro
+        try:
+            u1 = oracle_poly(orc, s, hn, hl, hmax, r)["u_twob"][0]
+        finally:
+            s.ro = keep
+        assert abs(du[0] - (u1 - u0)) <= 1e-9 * abs(u0), (ip, du[0], u1 - u0)
+        nchecked += 1
+    assert nchecked >= 8

@@ -74,3 +74,28 @@ def test_poly_utotal_with_ewald_matches_oracle(ewald, orc, gpu_lib):
     assert abs(g["u_rec"] - ref["u_rec"]) <= 1e-10 * scale
     assert np.abs(g["force"] - ref["force"]).max() <= 1e-10 * np.abs(ref["force"]).max()
     e.close()
+
+
+def test_poly_trial_batch_matches_oracle(orc, gpu_lib):
+    """Independent single-particle trials of rigid waters and ions in one
+    launch: the same overlap flags as the oracle's UTwoBodyPNew/Old, and
+    du%twob within 1e-10 of the two-body energy."""
+    from tests.test_cpu_poly import oracle_trial, poly_trials
+    s = configs.water_ions(seed=13, nwater=200, nsalt=12, L=22.0)
+    s.lmc = 1
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0, full=True)
+    ref_u0 = oracle_poly(orc, s, nn, jl, maxn, lmc=1)["u_twob"][0]
+    rng = np.random.default_rng(5)
+    ips, rotm, atoms = poly_trials(s, rng, 96, step=1.2, angle=0.8)
+    e = PolyEngine(s, maxn)
+    du, ovl = e.DUTwoBodyBatch(nn, jl, ips, rotm, np.concatenate(atoms))
+    n_ok = 0
+    for t in range(len(ips)):
+        r_du, r_ovl = oracle_trial(orc, s, nn, jl, maxn, ips[t], rotm[t], atoms[t])
+        assert bool(ovl[t]) == r_ovl, t
+        if not r_ovl:
+            assert abs(du[t] - r_du[0]) <= 1e-10 * abs(ref_u0), (t, du[t], r_du[0])
+            n_ok += 1
+    assert n_ok > 60
+    e.close()
