@@ -378,6 +378,13 @@ int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, double *u_re
 int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
                             const int32_t *jpnlist, int32_t ntrial, const int32_t *ip, const double *rotm,
                             const double *rtm, double *du_twob, int32_t *lhsoverlap);
+/* The end of UTotal for polyatomic particles (energy.F90:405-427): from
+ * the total atom forces force[3*na] (unscaled) and the atom and particle
+ * positions, the particle forces forceo[3*np] and torques torqueo[3*np]
+ * (both scaled by force_fac, atoms summed in order per particle) and the
+ * molecular virial sum (r_a - ro_p) . f_a into *virmolecule. */
+int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force, double force_fac,
+                     double *forceo, double *torqueo, double *virmolecule);
 int mg_poly_last_error(const mg_poly *c, char *buf, size_t n);
 int mg_poly_destroy(mg_poly *c);
 

@@ -262,6 +262,43 @@ __global__ void k_poly_dutwobody(PolyArgs a, int ntrial, const int *__restrict__
     }
 }
 
+// the end of UTotal: one thread per particle over its atoms in order
+__global__ void __launch_bounds__(kPolyThreads) k_poly_epilogue(PolyArgs a, double fac, double *__restrict__ fo,
+                                                                double *__restrict__ to) {
+    __shared__ double red[kPolyThreads];
+    double vir = 0.0;
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip < a.np) {
+        int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[a.iptpn[ip] - 1];
+        double f[3] = {0.0, 0.0, 0.0}, tq[3] = {0.0, 0.0, 0.0};
+        for (int ia = ialow; ia < iaupp; ++ia) {
+            double dx = __dsub_rn(a.r[3 * ia], a.ro[3 * ip]);
+            double dy = __dsub_rn(a.r[3 * ia + 1], a.ro[3 * ip + 1]);
+            double dz = __dsub_rn(a.r[3 * ia + 2], a.ro[3 * ip + 2]);
+            const double *fa = a.force + 3 * ia;
+            vir = __dadd_rn(__dadd_rn(__dadd_rn(vir, __dmul_rn(dx, fa[0])), __dmul_rn(dy, fa[1])), __dmul_rn(dz, fa[2]));
+            double gx = __dmul_rn(fa[0], fac), gy = __dmul_rn(fa[1], fac), gz = __dmul_rn(fa[2], fac);
+            f[0] = __dadd_rn(f[0], gx);
+            f[1] = __dadd_rn(f[1], gy);
+            f[2] = __dadd_rn(f[2], gz);
+            tq[0] = __dadd_rn(tq[0], __dsub_rn(__dmul_rn(dy, gz), __dmul_rn(dz, gy)));
+            tq[1] = __dadd_rn(tq[1], __dsub_rn(__dmul_rn(dz, gx), __dmul_rn(dx, gz)));
+            tq[2] = __dadd_rn(tq[2], __dsub_rn(__dmul_rn(dx, gy), __dmul_rn(dy, gx)));
+        }
+        for (int m = 0; m < 3; ++m) {
+            fo[3 * ip + m] = f[m];
+            to[3 * ip + m] = tq[m];
+        }
+    }
+    red[threadIdx.x] = vir;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) sum = __dadd_rn(sum, red[t]);
+        a.part[blockIdx.x] = sum;
+    }
+}
+
 }  // namespace
 
 struct mg_poly {
@@ -273,6 +310,7 @@ struct mg_poly {
         *d_tip = nullptr, *d_tatom0 = nullptr, *d_tovl = nullptr;
     double *d_r2atat = nullptr, *d_trotm = nullptr, *d_trtm = nullptr, *d_tdu = nullptr;
     int tcap = 0, tacap = 0;
+    double *d_fo = nullptr, *d_to = nullptr;
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
            *d_part = nullptr, *d_aza = nullptr;
     std::vector<double> h_part;
@@ -307,7 +345,7 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
     void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
                     c->d_force, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
-                    c->d_trotm, c->d_trtm, c->d_tdu};
+                    c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -579,5 +617,28 @@ extern "C" int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const doubl
     if (herr[0]) return poly_fail(c, herr[0], "ibuf > nbuf for atom-type pair %d", herr[1]);
     POLY_CUDA(c, cudaMemcpy(du_twob, c->d_tdu, sizeof(double) * ntrial, cudaMemcpyDeviceToHost));
     POLY_CUDA(c, cudaMemcpy(lhsoverlap, c->d_tovl, sizeof(int) * ntrial, cudaMemcpyDeviceToHost));
+    return MG_OK;
+}
+
+extern "C" int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force, double force_fac,
+                                double *forceo, double *torqueo, double *virmolecule) {
+    if (!c || !ro || !r || !force || !forceo || !torqueo || !virmolecule) return MG_ERR_ARG;
+    const mg_poly_params &p = c->p;
+    if (!c->d_fo) {
+        POLY_CUDA(c, cudaMalloc(&c->d_fo, sizeof(double) * 3 * p.np));
+        POLY_CUDA(c, cudaMalloc(&c->d_to, sizeof(double) * 3 * p.np));
+    }
+    POLY_CUDA(c, cudaMemcpy(c->d_ro, ro, sizeof(double) * 3 * p.np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_force, force, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    PolyArgs a = poly_args(c);
+    k_poly_epilogue<<<c->nblk, kPolyThreads>>>(a, force_fac, c->d_fo, c->d_to);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(forceo, c->d_fo, sizeof(double) * 3 * p.np, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(torqueo, c->d_to, sizeof(double) * 3 * p.np, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->nblk, cudaMemcpyDeviceToHost));
+    double v = 0.0;
+    for (int b = 0; b < c->nblk; ++b) v += c->h_part[b];
+    *virmolecule = v;
     return MG_OK;
 }

@@ -247,6 +247,21 @@ class PolyEngine:
             raise MolsimError(st, f"poly_dutwobody_batch: {buf.value.decode(errors='replace')}")
         return du, ovl.astype(bool)
 
+    def Epilogue(self, force, r=None):
+        """UTotal's end (energy.F90:405-427): particle forces and torques
+        (scaled by force_fac) from the atom forces, and the molecular virial."""
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        fo = np.zeros(3 * s.np_)
+        to = np.zeros(3 * s.np_)
+        vm = np.zeros(1)
+        st = self.lib.mg_poly_epilogue(self.h, abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)),
+                                       abi.f64(abi.as_f64(np.asarray(force).reshape(-1))), units.FORCE_FAC,
+                                       abi.f64(fo), abi.f64(to), abi.f64(vm))
+        if st != 0:
+            raise MolsimError(st, "poly_epilogue")
+        return dict(forceo=fo.reshape(-1, 3), torqueo=to.reshape(-1, 3), virmolecule=float(vm[0]))
+
     def EwaldIntra(self, r=None):
         """The molecular part of UEwaldSelf: its u%rec share and atom forces."""
         s = self.s
@@ -259,10 +274,11 @@ class PolyEngine:
         return dict(force=force.reshape(-1, 3), u_rec=float(u[0]))
 
     def UTotal(self, nneighpn, jpnlist, engine_factory=None):
-        """u%tot and the atom forces of a polyatomic system with Ewald: the
-        atom pairs (UTwoBodyP, with the real-space Ewald table), the
-        reciprocal sum and atomic self term over the atoms (a handle of the
-        atoms), and the molecular self term.  Forces in force(3,na) units."""
+        """UTotal of a polyatomic system: the atom pairs (UTwoBodyP, with the
+        real-space Ewald table when Ewald is on), the reciprocal sum and
+        atomic self term over the atoms (a handle of the atoms), the
+        molecular self term, then UTotal's end: atom forces (force(3,na)
+        units), particle forces and torques (forceo, torqueo), the virial."""
         from .engine import Engine
         s = self.s
         r = s.atom_positions()
@@ -277,7 +293,11 @@ class PolyEngine:
             intra = self.EwaldIntra(r)
             out["u_rec"] = rec["u_rec"] + intra["u_rec"]
             out["force"] += rec["forceo"] / units.FORCE_FAC + intra["force"]
+            out["virial"] += rec["virial"]
         out["u_tot"] = out["u_twob"][0] + out["u_rec"]
+        ep = self.Epilogue(out["force"], r)
+        out.update(forceo=ep["forceo"], torqueo=ep["torqueo"])
+        out["virial"] += ep["virmolecule"]
         return out
 
     def close(self):

@@ -39,6 +39,9 @@ def oracle():
         lib.orc_poly_dutwobody.restype = C.c_int
         lib.orc_poly_dutwobody.argtypes = [C.POINTER(abi.MgPolyParams), C.c_int32, abi.PF64, abi.PF64, abi.PI32,
                                            abi.PI32, C.c_int32, abi.PF64, abi.PF64, abi.PF64, abi.PI32]
+        lib.orc_poly_epilogue.restype = C.c_int
+        lib.orc_poly_epilogue.argtypes = [C.POINTER(abi.MgPolyParams), abi.PF64, abi.PF64, abi.PF64, C.c_double,
+                                          abi.PF64, abi.PF64, abi.PF64]
         lib.orc_poly_ewald_intra.restype = C.c_int
         lib.orc_poly_ewald_intra.argtypes = [C.POINTER(abi.MgPolyParams), abi.PF64, abi.PF64, abi.PF64]
         lib.orc_poly_utwobody.restype = C.c_int

@@ -1770,6 +1770,35 @@ int orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double 
     return 0;
 }
 
+/* UTotal, energy.F90:405-427: atoms in order, each adding to its particle
+   (ipnan) the scaled force, the torque of the scaled force about the
+   particle centre, and (r_a - ro_p) . f_a (unscaled) to virmolecule */
+int orc_poly_epilogue(const mg_poly_params *p, const double *ro, const double *r, const double *force,
+                      double force_fac, double *forceo, double *torqueo, double *virmolecule) {
+    double virmol = Zero;
+    for (int k = 0; k < 3 * p->np; ++k) forceo[k] = torqueo[k] = Zero;
+    for (int ip = 1; ip <= p->np; ++ip) {
+        int ialow = p->ianpn[ip - 1], iaupp = ialow + p->napt[p->iptpn[ip - 1] - 1] - 1;
+        for (int ia = ialow; ia <= iaupp; ++ia) {
+            const double *fa = &force[3 * (ia - 1)];
+            double dx = r[3 * (ia - 1)] - ro[3 * (ip - 1)];
+            double dy = r[3 * (ia - 1) + 1] - ro[3 * (ip - 1) + 1];
+            double dz = r[3 * (ia - 1) + 2] - ro[3 * (ip - 1) + 2];
+            virmol = virmol + dx * fa[0] + dy * fa[1] + dz * fa[2];
+            double gx = fa[0] * force_fac, gy = fa[1] * force_fac, gz = fa[2] * force_fac;
+            double *fo = &forceo[3 * (ip - 1)], *to = &torqueo[3 * (ip - 1)];
+            fo[0] = fo[0] + gx;
+            fo[1] = fo[1] + gy;
+            fo[2] = fo[2] + gz;
+            to[0] = to[0] + (dy * gz - dz * gy);
+            to[1] = to[1] + (dz * gx - dx * gz);
+            to[2] = to[2] + (dx * gy - dy * gx);
+        }
+    }
+    *virmolecule = virmol;
+    return 0;
+}
+
 /* UEwaldSelf, molecular contribution (energy.F90:1313-1341), with the
    constants of EwaldSetup (energy.F90:7040-7042) and ErfLocal = Erf2; the
    result scaled by EpsiFourPi as UEwald does at its end (energy.F90:950) */

@@ -81,6 +81,10 @@ int  orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double 
 int  orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
                         const int32_t *nneighpn, const int32_t *jpnlist, int32_t ip, const double *rotm,
                         const double *rtm, double *du_twob, int32_t *lhsoverlap);
+/* the end of UTotal for polyatomic particles (energy.F90:405-427),
+   arguments as mg_poly_epilogue's */
+int  orc_poly_epilogue(const mg_poly_params *p, const double *ro, const double *r, const double *force,
+                       double force_fac, double *forceo, double *torqueo, double *virmolecule);
 /* the molecular part of UEwaldSelf (energy.F90:1301-1345), arguments as
    mg_poly_ewald_intra's */
 int  orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force, double *u_rec);

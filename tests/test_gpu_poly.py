@@ -99,3 +99,29 @@ def test_poly_trial_batch_matches_oracle(orc, gpu_lib):
             n_ok += 1
     assert n_ok > 60
     e.close()
+
+
+def test_poly_epilogue_matches_oracle(orc, gpu_lib):
+    """UTotal's end for polyatomic particles: particle forces and torques
+    from the atom forces, summed atom by atom in order per particle as the
+    reference does (the same bits), and the molecular virial."""
+    import ctypes as C
+    from molsim_gb300 import units
+    s = configs.water_ions(seed=14, nwater=150, nsalt=10, L=20.0)
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0)
+    e = PolyEngine(s, maxn)
+    g = e.UTotal(nn, jl)
+    p = s.params()
+    r = s.atom_positions()
+    fo, to, vm = np.zeros(3 * s.np_), np.zeros(3 * s.np_), np.zeros(1)
+    assert orc.orc_poly_epilogue(C.byref(p), abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)),
+                                 abi.f64(np.ascontiguousarray(g["force"].reshape(-1))), units.FORCE_FAC,
+                                 abi.f64(fo), abi.f64(to), abi.f64(vm)) == 0
+    assert np.array_equal(g["forceo"].reshape(-1), fo)
+    assert np.array_equal(g["torqueo"].reshape(-1), to)
+    assert abs((g["virial"] - e.UTwoBodyP(nn, jl)["virial"]) - vm[0]) <= 1e-10 * abs(vm[0])
+    # the particle forces add up to the atom forces
+    assert np.allclose(g["forceo"].sum(0), g["force"].sum(0) * units.FORCE_FAC, rtol=0,
+                       atol=1e-9 * np.abs(g["forceo"]).max())
+    e.close()
