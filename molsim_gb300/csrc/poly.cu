@@ -27,6 +27,7 @@
 namespace {
 
 constexpr int kPolyThreads = 128;
+constexpr int kPolyMaxAtoms = 16;   // atoms per particle that the pair loop accepts
 
 struct PolyArgs {
     int np, nptpt, maxnneigh, lmc, nbuf;
@@ -52,6 +53,8 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
         int ipt = a.iptpn[ip];
         int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[ipt - 1];
         int nn = a.nneighpn[ip];
+        double fi[3 * kPolyMaxAtoms];   // forces on ip's atoms from its list row
+        for (int k = 0; k < 3 * (iaupp - ialow); ++k) fi[k] = 0.0;
         for (int jploc = 0; jploc < nn; ++jploc) {
             int jp = a.jpnlist[(size_t)ip * a.maxnneigh + jploc] - 1;
             if (a.lmc && jp < ip) continue;
@@ -67,10 +70,13 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
             if (r2 > a.rcut2) continue;
             double usum = 0.0;
             int jalow = a.ianpn[jp] - 1, jaupp = jalow + a.napt[jpt - 1];
-            for (int ia = ialow; ia < iaupp; ++ia) {
-                int iat = a.iatan[ia];
-                for (int ja = jalow; ja < jaupp; ++ja) {
-                    int jat = a.iatan[ja];
+            // the atoms of jp outer, so that each of its forces takes one
+            // atomic add per particle pair; ip's atom forces stay in fi
+            for (int ja = jalow; ja < jaupp; ++ja) {
+                int jat = a.iatan[ja];
+                double fj0 = 0.0, fj1 = 0.0, fj2 = 0.0;
+                for (int ia = ialow; ia < iaupp; ++ia) {
+                    int iat = a.iatan[ia];
                     int iatjat = a.iatat[(jat - 1) * a.nat + (iat - 1)];
                     double dx = __dsub_rn(__dsub_rn(a.r[3 * ia], a.r[3 * ja]), sh[0]);
                     double dy = __dsub_rn(__dsub_rn(a.r[3 * ia + 1], a.r[3 * ja + 1]), sh[1]);
@@ -97,19 +103,24 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
                     double fsum = __dadd_rn(c[7], __dmul_rn(dd, __dadd_rn(c[8], __dmul_rn(dd, __dadd_rn(c[9],
                                   __dmul_rn(dd, __dadd_rn(c[10], __dmul_rn(dd, c[11]))))))));
                     double fx = __dmul_rn(fsum, dx), fy = __dmul_rn(fsum, dy), fz = __dmul_rn(fsum, dz);
-                    atomicAdd(&a.force[3 * ia], fx);
-                    atomicAdd(&a.force[3 * ia + 1], fy);
-                    atomicAdd(&a.force[3 * ia + 2], fz);
-                    atomicAdd(&a.force[3 * ja], -fx);
-                    atomicAdd(&a.force[3 * ja + 1], -fy);
-                    atomicAdd(&a.force[3 * ja + 2], -fz);
+                    int k = ia - ialow;
+                    fi[3 * k] = __dadd_rn(fi[3 * k], fx);
+                    fi[3 * k + 1] = __dadd_rn(fi[3 * k + 1], fy);
+                    fi[3 * k + 2] = __dadd_rn(fi[3 * k + 2], fz);
+                    fj0 = __dsub_rn(fj0, fx);
+                    fj1 = __dsub_rn(fj1, fy);
+                    fj2 = __dsub_rn(fj2, fz);
                     vir = __dsub_rn(vir, __dmul_rn(fsum, ar2));
                 }
+                atomicAdd(&a.force[3 * ja], fj0);
+                atomicAdd(&a.force[3 * ja + 1], fj1);
+                atomicAdd(&a.force[3 * ja + 2], fj2);
             }
 #pragma unroll
             for (int k = 0; k < MG_MAX_NPTPT; ++k)   // static indices keep acc in registers
                 if (k == iptjpt - 1) acc[k] = __dadd_rn(acc[k], usum);
         }
+        for (int k = 0; k < 3 * (iaupp - ialow); ++k) atomicAdd(&a.force[3 * ialow + k], fi[k]);
     }
     // block sums in a fixed order (thread 0 adds the block's values in turn)
 #pragma unroll
@@ -369,7 +380,7 @@ static int poly_check_params(const mg_poly_params *p, int maxnneigh) {
         int t = p->iptpn[i];
         if (t < 1 || t > p->npt) return MG_ERR_ARG;
         int a0 = p->ianpn[i], na = p->napt[t - 1];
-        if (a0 < 1 || na < 1 || a0 - 1 + na > p->na) return MG_ERR_ARG;
+        if (a0 < 1 || na < 1 || na > kPolyMaxAtoms || a0 - 1 + na > p->na) return MG_ERR_ARG;
     }
     for (int a = 0; a < p->na; ++a)
         if (p->iatan[a] < 1 || p->iatan[a] > p->nat) return MG_ERR_ARG;

@@ -85,11 +85,18 @@ class PolySystem:
         return np.concatenate([[a for a, _ in self.particle_types[t - 1].atoms] for t in self.iptpn]).astype(np.int32) + 1
 
     def atom_positions(self):
-        out = []
-        for ip, t in enumerate(self.iptpn):
-            loc = np.array([x for _, x in self.particle_types[t - 1].atoms], dtype=np.float64)
-            out.append(self.ro[ip] + loc @ self.ori[ip].T)
-        return np.ascontiguousarray(np.concatenate(out))
+        """r = ro + ori . local for every atom, particle by particle."""
+        na = self.napt()[self.iptpn - 1]
+        first = self.ianpn() - 1
+        out = np.empty((int(na.sum()), 3))
+        for t, pt in enumerate(self.particle_types, start=1):
+            idx = np.flatnonzero(self.iptpn == t)
+            if idx.size == 0:
+                continue
+            loc = np.array([x for _, x in pt.atoms], dtype=np.float64)          # (a, 3)
+            pos = self.ro[idx][:, None, :] + np.einsum("nij,aj->nai", self.ori[idx], loc)
+            out[(first[idx][:, None] + np.arange(len(loc))[None, :]).reshape(-1)] = pos.reshape(-1, 3)
+        return np.ascontiguousarray(out)
 
     def aza(self):
         return np.array([self.atom_types[t - 1].charge for t in self.iatan()], dtype=np.float64)
@@ -285,8 +292,12 @@ class PolyEngine:
         tw = self.UTwoBodyP(nneighpn, jpnlist, r)
         out = dict(u_twob=tw["u_twob"], virial=tw["virial"], force=tw["force"].copy(), u_rec=0.0)
         if s.ewald != abi.MG_EWALD_NONE:
-            a = s.atom_system()
-            e = engine_factory(a) if engine_factory else Engine(a)
+            if engine_factory is not None:
+                e = engine_factory(s.atom_system())
+            else:   # one handle of the atoms, kept for the following calls
+                if getattr(self, "_atoms", None) is None:
+                    self._atoms = Engine(s.atom_system())
+                e = self._atoms
             e.SetPositions(s.atoms_in_box(r).reshape(-1))
             e.NList("write")
             rec = e.UTotal()
@@ -301,6 +312,9 @@ class PolyEngine:
         return out
 
     def close(self):
+        if getattr(self, "_atoms", None) is not None:
+            self._atoms.close()
+            self._atoms = None
         if self.h:
             self.lib.mg_poly_destroy(self.h)
             self.h = C.c_void_p()
