@@ -367,6 +367,14 @@ int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, const int32_
  * reciprocal sum over the atoms come from a handle whose particles are the
  * atoms (mg_utotal). */
 int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, double *u_rec);
+/* mg_poly_utwobody with the particle list kept on the device: the centres
+ * and their neighbour list are those of the handle `centres` (a handle whose
+ * particles are the polyatomic particles' centres, after mg_set_positions
+ * and mg_nlist_set or mg_nlist_update); only the atom positions r[3*na]
+ * travel.  Same outputs; every thread adds the forces of its own particle's
+ * atoms only, so the atom forces need no atomics and are reproducible. */
+int mg_poly_utwobody_list(mg_poly *c, mg_handle *centres, const double *r, double *force, double *u_twob,
+                          double *virial);
 /* Single-particle MC trials of polyatomic particles (DUTwoBody with
  * UTwoBodyPNew/UTwoBodyPOld, denergy.F90:937-1231, for nptm = 1): trial t
  * moves particle ip[t] (1-based) to centre rotm[3*t] with its atoms at

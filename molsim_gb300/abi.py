@@ -108,6 +108,7 @@ LIB_ONLY = [
     ("poly_create", C.c_int, [C.POINTER(MgPolyParams), C.c_int32, C.POINTER(C.c_void_p)]),
     ("poly_utwobody", C.c_int, [H, PF64, PF64, PI32, PI32, PF64, PF64, PF64]),
     ("poly_ewald_intra", C.c_int, [H, PF64, PF64, PF64]),
+    ("poly_utwobody_list", C.c_int, [H, H, PF64, PF64, PF64, PF64]),
     ("poly_epilogue", C.c_int, [H, PF64, PF64, PF64, C.c_double, PF64, PF64, PF64]),
     ("poly_dutwobody_batch", C.c_int, [H, PF64, PF64, PI32, PI32, C.c_int32, PI32, PF64, PF64, PF64, PI32]),
     ("poly_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),

@@ -28,12 +28,20 @@ namespace {
 
 constexpr int kPolyThreads = 128;
 constexpr int kPolyMaxAtoms = 16;   // atoms per particle that the pair loop accepts
+constexpr int kPolyBins = 1024;     // table-search start bins per atom-type pair
+
 
 struct PolyArgs {
     int np, nptpt, maxnneigh, lmc, nbuf;
     const int *iptpn, *iptpt, *napt, *ianpn, *iatan, *iatat, *iubuflow;
     int npt, nat;
     const double *ubuf, *r2umin, *r2atat;
+    // where the table search of each atom-type pair starts: r2 in bin b
+    // (bin_z0 + b/bin_inv) starts at record bin_k[pair*kPolyBins + b], the
+    // first record below the bin's upper edge, so the linear search of the
+    // reference finds the same record in a few steps
+    const double *bin_z0, *bin_inv;
+    const int *bin_k;
     const double *ro, *r;
     const int *nneighpn, *jpnlist;
     double len[3], half[3], rcut2;
@@ -42,20 +50,28 @@ struct PolyArgs {
     int *err;
 };
 
+// the record (0-based index into ubuf) where the search for r2 starts
+__device__ __forceinline__ int poly_search_start(const PolyArgs &a, int iatjat, double r2) {
+    double x = (r2 - a.bin_z0[iatjat - 1]) * a.bin_inv[iatjat - 1];
+    int b = x < 0.0 ? 0 : (x >= (double)(kPolyBins - 1) ? kPolyBins - 1 : (int)x);
+    return a.bin_k[(size_t)(iatjat - 1) * kPolyBins + b];
+}
+
 __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
     extern __shared__ double red[];   // [nptpt + 1][kPolyThreads]
     const int nv = a.nptpt + 1;
     double acc[MG_MAX_NPTPT], vir = 0.0;   // u%twob(1:nptpt) and the virial of this thread
 #pragma unroll
     for (int k = 0; k < MG_MAX_NPTPT; ++k) acc[k] = 0.0;
-    int ip = blockIdx.x * blockDim.x + threadIdx.x;   // 0-based particle
+    // one warp per particle, its lanes over the list row
+    int ip = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (ip < a.np) {
         int ipt = a.iptpn[ip];
         int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[ipt - 1];
         int nn = a.nneighpn[ip];
-        double fi[3 * kPolyMaxAtoms];   // forces on ip's atoms from its list row
+        double fi[3 * kPolyMaxAtoms];   // forces on ip's atoms from this lane's neighbours
         for (int k = 0; k < 3 * (iaupp - ialow); ++k) fi[k] = 0.0;
-        for (int jploc = 0; jploc < nn; ++jploc) {
+        for (int jploc = lane; jploc < nn; jploc += 32) {
             int jp = a.jpnlist[(size_t)ip * a.maxnneigh + jploc] - 1;
             if (a.lmc && jp < ip) continue;
             int jpt = a.iptpn[jp];
@@ -86,7 +102,7 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
                         mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, ia + 1, ja + 1, iatjat);
                         continue;
                     }
-                    int ibuf = a.iubuflow[iatjat - 1] - 1;   // 0-based start of the record
+                    int ibuf = poly_search_start(a, iatjat, ar2);   // 0-based start of the search
                     while (!(ar2 >= a.ubuf[ibuf])) {
                         ibuf += 12;
                         if (ibuf >= a.nbuf) break;
@@ -120,7 +136,11 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
             for (int k = 0; k < MG_MAX_NPTPT; ++k)   // static indices keep acc in registers
                 if (k == iptjpt - 1) acc[k] = __dadd_rn(acc[k], usum);
         }
-        for (int k = 0; k < 3 * (iaupp - ialow); ++k) atomicAdd(&a.force[3 * ialow + k], fi[k]);
+        for (int k = 0; k < 3 * (iaupp - ialow); ++k) {
+            double v = fi[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) atomicAdd(&a.force[3 * ialow + k], v);
+        }
     }
     // block sums in a fixed order (thread 0 adds the block's values in turn)
 #pragma unroll
@@ -182,7 +202,7 @@ __global__ void __launch_bounds__(kPolyThreads) k_ewald_intra(PolyArgs a, const 
 // the tabulated energy of one atom pair (UTwoBodyA's search and Horner
 // sums); 0: ok, MG_ERR_IBUF past the table
 __device__ __forceinline__ int poly_pair_u(const PolyArgs &a, int iatjat, double r2, double *u) {
-    int ibuf = a.iubuflow[iatjat - 1] - 1;
+    int ibuf = poly_search_start(a, iatjat, r2);
     while (!(r2 >= a.ubuf[ibuf])) {
         ibuf += 12;
         if (ibuf >= a.nbuf) return MG_ERR_IBUF;
@@ -310,11 +330,111 @@ __global__ void __launch_bounds__(kPolyThreads) k_poly_epilogue(PolyArgs a, doub
     }
 }
 
+// the atom-pair loop over the handle's full list (slot space: nbr[k*np +
+// slot] holds neighbour slots, perm maps a slot to its particle): every
+// thread computes its particle's atom forces from both members of each
+// pair; the energy and virial of a pair are taken once, from the particle
+// with the lower number
+__global__ void __launch_bounds__(kPolyThreads) k_twobody_p_list(PolyArgs a, const int *__restrict__ perm,
+                                                                 const int *__restrict__ nnb,
+                                                                 const int *__restrict__ nbr) {
+    extern __shared__ double red[];   // [nptpt + 1][kPolyThreads]
+    const int nv = a.nptpt + 1;
+    double acc[MG_MAX_NPTPT], vir = 0.0;
+#pragma unroll
+    for (int k = 0; k < MG_MAX_NPTPT; ++k) acc[k] = 0.0;
+    // one warp per particle (slot), its lanes over the list row
+    int slot = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (slot < a.np) {
+        int ip = perm[slot];
+        int ipt = a.iptpn[ip];
+        int ialow = a.ianpn[ip] - 1, nai = a.napt[ipt - 1];
+        double fi[3 * kPolyMaxAtoms];
+        for (int k = 0; k < 3 * nai; ++k) fi[k] = 0.0;
+        int nn = nnb[slot];
+        for (int kk = lane; kk < nn; kk += 32) {
+            int jp = perm[nbr[(size_t)kk * a.np + slot]];
+            int jpt = a.iptpn[jp];
+            int iptjpt = a.iptpt[(jpt - 1) * a.npt + (ipt - 1)];
+            double sh[3], r2;
+            {
+                double d[3];
+                for (int m = 0; m < 3; ++m) {
+                    d[m] = __dsub_rn(a.ro[3 * ip + m], a.ro[3 * jp + m]);
+                    sh[m] = fabs(d[m]) > a.half[m] ? copysign(a.len[m], d[m]) : 0.0;   // PBC2
+                    d[m] = __dsub_rn(d[m], sh[m]);
+                }
+                r2 = mg_r2_exact(d[0], d[1], d[2]);
+            }
+            if (r2 > a.rcut2) continue;
+            bool own = ip < jp;   // the pair's energy is counted from its lower-numbered particle
+            double usum = 0.0;
+            int jalow = a.ianpn[jp] - 1, naj = a.napt[jpt - 1];
+            for (int k = 0; k < nai; ++k) {
+                int ia = ialow + k, iat = a.iatan[ia];
+                for (int l = 0; l < naj; ++l) {
+                    int ja = jalow + l, jat = a.iatan[ja];
+                    int iatjat = a.iatat[(jat - 1) * a.nat + (iat - 1)];
+                    double dx = __dsub_rn(__dsub_rn(a.r[3 * ia], a.r[3 * ja]), sh[0]);
+                    double dy = __dsub_rn(__dsub_rn(a.r[3 * ia + 1], a.r[3 * ja + 1]), sh[1]);
+                    double dz = __dsub_rn(__dsub_rn(a.r[3 * ia + 2], a.r[3 * ja + 2]), sh[2]);
+                    double ar2 = mg_r2_exact(dx, dy, dz);
+                    if (ar2 < a.r2umin[iatjat - 1]) {
+                        mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, ia + 1, ja + 1, iatjat);
+                        continue;
+                    }
+                    int ibuf = poly_search_start(a, iatjat, ar2);
+                    while (!(ar2 >= a.ubuf[ibuf])) {
+                        ibuf += 12;
+                        if (ibuf >= a.nbuf) break;
+                    }
+                    if (ibuf >= a.nbuf) {
+                        mg_dev_error(a.err, MG_ERR_IBUF, iatjat, ia + 1, ja + 1);
+                        continue;
+                    }
+                    const double *c = a.ubuf + ibuf;
+                    double dd = __dsub_rn(ar2, c[0]);
+                    double fsum = __dadd_rn(c[7], __dmul_rn(dd, __dadd_rn(c[8], __dmul_rn(dd, __dadd_rn(c[9],
+                                  __dmul_rn(dd, __dadd_rn(c[10], __dmul_rn(dd, c[11]))))))));
+                    fi[3 * k] = __dadd_rn(fi[3 * k], __dmul_rn(fsum, dx));
+                    fi[3 * k + 1] = __dadd_rn(fi[3 * k + 1], __dmul_rn(fsum, dy));
+                    fi[3 * k + 2] = __dadd_rn(fi[3 * k + 2], __dmul_rn(fsum, dz));
+                    if (own) {
+                        usum = __dadd_rn(__dadd_rn(usum, c[1]), __dmul_rn(dd, __dadd_rn(c[2], __dmul_rn(dd,
+                               __dadd_rn(c[3], __dmul_rn(dd, __dadd_rn(c[4], __dmul_rn(dd, __dadd_rn(c[5],
+                               __dmul_rn(dd, c[6]))))))))));
+                        vir = __dsub_rn(vir, __dmul_rn(fsum, ar2));
+                    }
+                }
+            }
+            if (own) {
+#pragma unroll
+                for (int k = 0; k < MG_MAX_NPTPT; ++k)
+                    if (k == iptjpt - 1) acc[k] = __dadd_rn(acc[k], usum);
+            }
+        }
+        for (int k = 0; k < 3 * nai; ++k) {
+            double v = fi[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) a.force[3 * ialow + k] = v;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k <= MG_MAX_NPTPT; ++k)
+        if (k < nv) red[k * blockDim.x + threadIdx.x] = (k == a.nptpt) ? vir : acc[k < MG_MAX_NPTPT ? k : 0];
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double sum = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) sum = __dadd_rn(sum, red[threadIdx.x * blockDim.x + t]);
+        a.part[(size_t)blockIdx.x * nv + threadIdx.x] = sum;
+    }
+}
+
 }  // namespace
 
 struct mg_poly {
     mg_poly_params p{};
-    int maxnneigh = 0, nblk = 0;
+    int maxnneigh = 0, nblk = 0, nblk_w = 0;   // blocks of the thread- and warp-per-particle kernels
     std::string err;
     int *d_iptpn = nullptr, *d_iptpt = nullptr, *d_napt = nullptr, *d_ianpn = nullptr, *d_iatan = nullptr,
         *d_iatat = nullptr, *d_iubuflow = nullptr, *d_nneigh = nullptr, *d_jpnlist = nullptr, *d_err = nullptr,
@@ -322,6 +442,8 @@ struct mg_poly {
     double *d_r2atat = nullptr, *d_trotm = nullptr, *d_trtm = nullptr, *d_tdu = nullptr;
     int tcap = 0, tacap = 0;
     double *d_fo = nullptr, *d_to = nullptr;
+    double *d_bin_z0 = nullptr, *d_bin_inv = nullptr;
+    int *d_bin_k = nullptr;
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
            *d_part = nullptr, *d_aza = nullptr;
     std::vector<double> h_part;
@@ -356,7 +478,7 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
     void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
                     c->d_force, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
-                    c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to};
+                    c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to, c->d_bin_z0, c->d_bin_inv, c->d_bin_k};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -403,6 +525,7 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
     c->p = *p;
     c->maxnneigh = maxnneigh;
     c->nblk = (p->np + kPolyThreads - 1) / kPolyThreads;
+    c->nblk_w = (int)(((long)p->np * 32 + kPolyThreads - 1) / kPolyThreads);
     int np = p->np, na = p->na;
     if ((st = poly_upload(c, &c->d_iptpn, p->iptpn, np)) || (st = poly_upload(c, &c->d_iptpt, p->iptpt, (size_t)p->npt * p->npt)) ||
         (st = poly_upload(c, &c->d_napt, p->napt, p->npt)) || (st = poly_upload(c, &c->d_ianpn, p->ianpn, np)) ||
@@ -421,12 +544,38 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
     if (e == cudaSuccess) e = cudaMalloc(&c->d_nneigh, sizeof(int) * np);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_jpnlist, sizeof(int) * (size_t)maxnneigh * np);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int) * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->nblk * (p->nptpt + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_part, sizeof(double) * (size_t)c->nblk_w * (p->nptpt + 1));
     if (e != cudaSuccess) {
         mg_poly_destroy(c);
         return MG_ERR_CUDA;
     }
-    c->h_part.resize((size_t)c->nblk * (p->nptpt + 1));
+    c->h_part.resize((size_t)c->nblk_w * (p->nptpt + 1));
+    // search-start bins per atom-type pair over [r2umin, z_low of the first
+    // record]: bin b starts at the first record whose z_low is at or below
+    // the bin's upper edge (records run from large to small z_low)
+    {
+        std::vector<double> z0(p->natat), inv(p->natat);
+        std::vector<int> kk((size_t)p->natat * kPolyBins);
+        for (int q = 0; q < p->natat; ++q) {
+            int r0 = p->iubuflow[q] - 1;
+            double lo = p->r2umin[q], hi = p->ubuf[r0];
+            if (!(hi > lo)) hi = lo + 1.0;
+            z0[q] = lo;
+            inv[q] = kPolyBins / (hi - lo);
+            for (int b = 0; b < kPolyBins; ++b) {
+                double upper = lo + (b + 1) / inv[q];
+                int rr = r0;
+                while (rr + 12 < p->nbuf && p->ubuf[rr] > upper) rr += 12;
+                kk[(size_t)q * kPolyBins + b] = b == kPolyBins - 1 ? r0 : rr;
+            }
+        }
+        if ((st = poly_upload(c, &c->d_bin_z0, z0.data(), z0.size())) ||
+            (st = poly_upload(c, &c->d_bin_inv, inv.data(), inv.size())) ||
+            (st = poly_upload(c, &c->d_bin_k, kk.data(), kk.size()))) {
+            mg_poly_destroy(c);
+            return st;
+        }
+    }
     *out = c;
     return MG_OK;
 }
@@ -468,6 +617,10 @@ extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, c
     a.nat = p.nat;
     a.ubuf = c->d_ubuf;
     a.r2umin = c->d_r2umin;
+    a.r2atat = c->d_r2atat;
+    a.bin_z0 = c->d_bin_z0;
+    a.bin_inv = c->d_bin_inv;
+    a.bin_k = c->d_bin_k;
     a.ro = c->d_ro;
     a.r = c->d_r;
     a.nneighpn = c->d_nneigh;
@@ -481,7 +634,7 @@ extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, c
     a.part = c->d_part;
     a.err = c->d_err;
     size_t sm = sizeof(double) * (p.nptpt + 1) * kPolyThreads;
-    k_twobody_p<<<c->nblk, kPolyThreads, sm>>>(a);
+    k_twobody_p<<<c->nblk_w, kPolyThreads, sm>>>(a);
     POLY_CUDA(c, cudaGetLastError());
     int herr[4];
     POLY_CUDA(c, cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
@@ -494,12 +647,12 @@ extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, c
     double tot = 0.0, vir = 0.0;
     for (int k = 0; k < p.nptpt; ++k) {
         double s = 0.0;
-        for (int b = 0; b < c->nblk; ++b) s += c->h_part[(size_t)b * nv + k];
+        for (int b = 0; b < c->nblk_w; ++b) s += c->h_part[(size_t)b * nv + k];
         u_twob[k + 1] = s;
     }
     for (int k = 1; k <= p.nptpt; ++k) tot += u_twob[k];   // u%twob(0) = sum(u%twob(1:nptpt))
     u_twob[0] = tot;
-    for (int b = 0; b < c->nblk; ++b) vir += c->h_part[(size_t)b * nv + p.nptpt];
+    for (int b = 0; b < c->nblk_w; ++b) vir += c->h_part[(size_t)b * nv + p.nptpt];
     *virial = vir;
     return MG_OK;
 }
@@ -551,6 +704,9 @@ static PolyArgs poly_args(mg_poly *c) {
     a.ubuf = c->d_ubuf;
     a.r2umin = c->d_r2umin;
     a.r2atat = c->d_r2atat;
+    a.bin_z0 = c->d_bin_z0;
+    a.bin_inv = c->d_bin_inv;
+    a.bin_k = c->d_bin_k;
     a.ro = c->d_ro;
     a.r = c->d_r;
     a.nneighpn = c->d_nneigh;
@@ -651,5 +807,43 @@ extern "C" int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, c
     double v = 0.0;
     for (int b = 0; b < c->nblk; ++b) v += c->h_part[b];
     *virmolecule = v;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_utwobody_list(mg_poly *c, mg_handle *h, const double *r, double *force, double *u_twob,
+                                     double *virial) {
+    if (!c || !h || !r || !force || !u_twob || !virial) return MG_ERR_ARG;
+    const mg_poly_params &p = c->p;
+    if (h->np != p.np) return poly_fail(c, MG_ERR_ARG, "the centres handle holds %d particles, not %d", h->np, p.np);
+    if (!h->list_valid) return poly_fail(c, MG_ERR_STATE, "the centres handle has no list (mg_nlist_set)");
+    if (!(h->rcut + h->drnlist >= p.rcut)) return poly_fail(c, MG_ERR_ARG, "the centres list is shorter than rcut");
+    for (int m = 0; m < 3; ++m)
+        if (h->boxlen[m] != p.boxlen[m]) return poly_fail(c, MG_ERR_ARG, "the centres handle has another box");
+    POLY_CUDA(c, cudaStreamSynchronize(h->st));
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemset(c->d_err, 0, sizeof(int) * 4));
+    PolyArgs a = poly_args(c);
+    a.ro = h->d_ro;
+    size_t sm = sizeof(double) * (p.nptpt + 1) * kPolyThreads;
+    k_twobody_p_list<<<c->nblk_w, kPolyThreads, sm>>>(a, h->d_perm, h->d_nnb, h->d_nbr);
+    POLY_CUDA(c, cudaGetLastError());
+    int herr[4];
+    POLY_CUDA(c, cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr[0] == MG_ERR_TABLE_UNDERRUN)
+        return poly_fail(c, herr[0], "r2 < r2umin for atoms %d and %d (atom-type pair %d)", herr[1], herr[2], herr[3]);
+    if (herr[0]) return poly_fail(c, herr[0], "ibuf > nbuf for atom-type pair %d", herr[1]);
+    POLY_CUDA(c, cudaMemcpy(force, c->d_force, sizeof(double) * 3 * p.na, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->h_part.size(), cudaMemcpyDeviceToHost));
+    int nv = p.nptpt + 1;
+    double tot = 0.0, vir = 0.0;
+    for (int k = 0; k < p.nptpt; ++k) {
+        double sum = 0.0;
+        for (int b = 0; b < c->nblk_w; ++b) sum += c->h_part[(size_t)b * nv + k];
+        u_twob[k + 1] = sum;
+    }
+    for (int k = 1; k <= p.nptpt; ++k) tot += u_twob[k];
+    u_twob[0] = tot;
+    for (int b = 0; b < c->nblk_w; ++b) vir += c->h_part[(size_t)b * nv + p.nptpt];
+    *virial = vir;
     return MG_OK;
 }

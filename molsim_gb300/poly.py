@@ -182,6 +182,25 @@ class PolySystem:
         self.keep = k
         return p
 
+    def centre_system(self, skin=1.0):
+        """The particle centres as a monoatomic System whose handle keeps the
+        particle list on the device (mg_poly_utwobody_list): one species per
+        particle type, no charges, no Ewald, a two-body table that is zero."""
+        from .system import Species, System
+        sp = [Species(t.name, 0.0, 1.0, 0.0) for t in self.particle_types]
+        npt = self.npt
+        nptpt = npt * (npt + 1) // 2
+        ubuf = np.zeros(12 * nptpt)
+        ubuf[0::12] = 1e-4
+        c = System(species=sp, iptpn=np.asarray(self.iptpn, dtype=np.int32), ro=np.asarray(self.ro),
+                   boxlen=np.asarray(self.boxlen), rcut=self.rcut, drnlist=skin, txintlist=abi.MG_VLIST,
+                   mode=abi.MG_MD, ewald=abi.MG_EWALD_NONE, name="centres")
+        c.ubuf = ubuf
+        c.iubuflow = (np.arange(nptpt, dtype=np.int32) * 12 + 1)
+        c.r2umin = np.full(nptpt, 1e-4)
+        c.nugrid = np.ones(nptpt, dtype=np.int32)
+        return c
+
     def atom_system(self, rlist=3.0, skin=0.5):
         """The atoms as a monoatomic System for the reciprocal Ewald sum (and
         the atomic self term) through a handle: the atom types as species,
@@ -232,6 +251,29 @@ class PolyEngine:
             raise MolsimError(st, f"poly_utwobody: {buf.value.decode(errors='replace')}")
         return dict(force=force.reshape(-1, 3), u_twob=ut, virial=float(vir[0]))
 
+    def UTwoBodyPList(self, r=None):
+        """UTwoBodyP with the particle list on the device: a handle of the
+        centres (kept between calls) rebuilds its list from the current
+        centres, and only the atom positions are copied."""
+        from .engine import Engine
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        if getattr(self, "_centres", None) is None:
+            self._centres = Engine(s.centre_system())
+        e = self._centres
+        e.SetPositions(abi.as_f64(s.ro.reshape(-1)))
+        e.NList("write")
+        force = np.zeros(3 * len(r))
+        ut = np.zeros(self.p.nptpt + 1)
+        vir = np.zeros(1)
+        st = self.lib.mg_poly_utwobody_list(self.h, e.h, abi.f64(r.reshape(-1)), abi.f64(force), abi.f64(ut),
+                                            abi.f64(vir))
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.lib.mg_poly_last_error(self.h, buf, 512)
+            raise MolsimError(st, f"poly_utwobody_list: {buf.value.decode(errors='replace')}")
+        return dict(force=force.reshape(-1, 3), u_twob=ut, virial=float(vir[0]))
+
     def DUTwoBodyBatch(self, nneighpn, jpnlist, ips, rotm, rtm, r=None):
         """Independent single-particle trials against the current state:
         particle ips[t] to centre rotm[t] with atoms rtm (the trials' atoms
@@ -280,7 +322,7 @@ class PolyEngine:
             raise MolsimError(st, "poly_ewald_intra")
         return dict(force=force.reshape(-1, 3), u_rec=float(u[0]))
 
-    def UTotal(self, nneighpn, jpnlist, engine_factory=None):
+    def UTotal(self, nneighpn=None, jpnlist=None, engine_factory=None):
         """UTotal of a polyatomic system: the atom pairs (UTwoBodyP, with the
         real-space Ewald table when Ewald is on), the reciprocal sum and
         atomic self term over the atoms (a handle of the atoms), the
@@ -289,7 +331,8 @@ class PolyEngine:
         from .engine import Engine
         s = self.s
         r = s.atom_positions()
-        tw = self.UTwoBodyP(nneighpn, jpnlist, r)
+        # no list given: the device-resident list of a centres handle
+        tw = self.UTwoBodyPList(r) if nneighpn is None else self.UTwoBodyP(nneighpn, jpnlist, r)
         out = dict(u_twob=tw["u_twob"], virial=tw["virial"], force=tw["force"].copy(), u_rec=0.0)
         if s.ewald != abi.MG_EWALD_NONE:
             if engine_factory is not None:
@@ -312,9 +355,10 @@ class PolyEngine:
         return out
 
     def close(self):
-        if getattr(self, "_atoms", None) is not None:
-            self._atoms.close()
-            self._atoms = None
+        for k in ("_atoms", "_centres"):
+            if getattr(self, k, None) is not None:
+                getattr(self, k).close()
+                setattr(self, k, None)
         if self.h:
             self.lib.mg_poly_destroy(self.h)
             self.h = C.c_void_p()

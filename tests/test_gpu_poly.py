@@ -125,3 +125,29 @@ def test_poly_epilogue_matches_oracle(orc, gpu_lib):
     assert np.allclose(g["forceo"].sum(0), g["force"].sum(0) * units.FORCE_FAC, rtol=0,
                        atol=1e-9 * np.abs(g["forceo"]).max())
     e.close()
+
+
+@pytest.mark.parametrize("ewald", [False, True])
+def test_poly_device_list_matches_host_list(ewald, orc, gpu_lib):
+    """The atom-pair loop over the device-resident list of a centres handle
+    (full list, every thread its own atoms' forces) against the oracle with
+    the host list: energies and virial within 1e-10, atom forces within 1e-10
+    of the largest."""
+    s = configs.water_ions(seed=15, nwater=200, nsalt=12, L=22.0)
+    if ewald:
+        s.relpermitt = 78.0
+        s.ewald, s.ualpha, s.order, s.nmesh = abi.MG_EWALD_SPM, 0.4, 6, 32
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 1.0)
+    ref = oracle_poly(orc, s, nn, jl, maxn)
+    e = PolyEngine(s, maxn)
+    g = e.UTwoBodyPList()
+    for k in range(len(ref["u_twob"])):
+        assert abs(g["u_twob"][k] - ref["u_twob"][k]) <= 1e-10 * abs(ref["u_twob"][0]), k
+    assert abs(g["virial"] - ref["virial"]) <= 1e-10 * abs(ref["virial"])
+    assert np.abs(g["force"] - ref["force"]).max() <= 1e-10 * np.abs(ref["force"]).max()
+    g2 = e.UTwoBodyPList()                     # reproducible: no atomics
+    assert np.array_equal(g["force"], g2["force"])
+    a, b = e.UTotal(nn, jl), e.UTotal()
+    assert abs(a["u_tot"] - b["u_tot"]) <= 1e-10 * abs(a["u_tot"])
+    e.close()
