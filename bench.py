@@ -18,8 +18,13 @@ buffers (positions in, positions and forces out every step).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 With --impl reference the CPU oracle (the C restatement of the reference's
-Fortran, one thread, as the reference's serial build) runs BD steps of the
-same workload; each step is timed on the host.
+Fortran) runs BD steps of the same workload on every host core, its threads
+standing in for the reference's MPI ranks (replicated data, particle ranges
+per rank); each step is timed on the host.  The default run also reports the
+oracle on one thread, the reference's serial build (molsim_ser).
+
+Accuracy: the oracle's FP64 UTotal of the same configuration is the
+reference for the force and energy errors of both GPU forms.
 """
 import argparse
 import ctypes as C
@@ -127,6 +132,9 @@ class ClockSampler:
         self.gpu = gpu_index
 
     def __enter__(self):
+        import threading
+        self.lines = []
+        self.first = threading.Event()
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
@@ -134,17 +142,28 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+            return self
+
+        def reader():
+            for line in self.proc.stdout:
+                self.lines.append(line)
+                self.first.set()
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+        # the timed region starts once the sampler runs (nvidia-smi takes
+        # about a second to start)
+        self.first.wait(timeout=10.0)
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
         if self.proc is not None:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                self.out, _ = self.proc.communicate()
+            self.thread.join(timeout=5)
+        self.out = "".join(self.lines)
         return False
 
     def summary(self):
@@ -168,22 +187,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def traffic_from_profiles(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/*.md lines 'traffic_bytes_per_launch <kernel>: <bytes>')."""
-    d = os.path.join(ROOT, "profiles")
-    if not os.path.isdir(d):
-        return None
-    for f in sorted(os.listdir(d)):
-        if not f.endswith(".md"):
-            continue
-        for line in open(os.path.join(d, f)):
-            if line.startswith("traffic_bytes_per_launch ") and line.split()[1].rstrip(":") == kernel:
-                try:
-                    return float(line.split(":")[1].split()[0])
-                except (IndexError, ValueError):
-                    return None
-    return None
+def utotal_errors(g, r):
+    """Errors of a GPU UTotal against the oracle's: RMS and largest
+    per-particle force error over the RMS force, energy and virial relative
+    errors."""
+    d = np.asarray(g["forceo"]).reshape(-1, 3) - np.asarray(r["forceo"]).reshape(-1, 3)
+    fr = np.asarray(r["forceo"]).reshape(-1, 3)
+    frms = float(np.sqrt((fr * fr).sum(1).mean()))
+    dn = np.sqrt((d * d).sum(1))
+    return {"force_rms": float(np.sqrt((dn * dn).mean()) / frms), "force_max": float(dn.max() / frms),
+            "energy_rel": abs(g["u_tot"] - r["u_tot"]) / abs(r["u_tot"]),
+            "u_rec_rel": abs(g["u_rec"] - r["u_rec"]) / abs(r["u_rec"]),
+            "virial_rel": abs(g["virial"] - r["virial"]) / abs(r["virial"])}
 
 
 def cpu_threads():
@@ -195,11 +210,14 @@ def cpu_threads():
     return max(1, min(64, n))
 
 
-def cpu_baseline(seed, budget_s=20.0, max_steps=12, warmup=1, threads=1):
+def cpu_baseline(seed, budget_s=20.0, max_steps=12, warmup=1, threads=1, initial=None):
     """The oracle on BD steps of the same workload, with `threads` threads
     standing in for the reference's MPI ranks (replicated data, particle
     ranges per rank, partial sums combined in rank order); cell-list mode so
-    that set-up is O(N) (the Verlet-list build is O(N^2))."""
+    that set-up is O(N) (the Verlet-list build is O(N^2)).  Returns the host
+    time of each step; with `initial` (a dict), also the oracle's FP64 UTotal
+    of the initial configuration (forces, energies, virial) in it, the
+    reference for the GPU forms' errors."""
     from molsim_gb300 import Engine, abi
     from oracle.loader import oracle
     orc = oracle()
@@ -213,7 +231,9 @@ def cpu_baseline(seed, budget_s=20.0, max_steps=12, warmup=1, threads=1):
         e.SetPositions(s.ro_flat())
         e.NList("write")
         e.BDSetup(BD_DT, BD_SEED)
-        e.BDRun(0)  # initial forces, untimed
+        r0 = e.BDRun(0)  # initial forces, untimed
+        if initial is not None:
+            initial.update(r0)
         for _ in range(warmup):
             e.BDRun(1)
         times = []
@@ -276,18 +296,18 @@ def run_ours(args):
         e.BDSetup(BD_DT, BD_SEED)
         return e
 
-    # accuracy of the mixed form on this workload (same configuration)
+    # UTotal of the initial configuration in both forms; their errors against
+    # the oracle's FP64 UTotal of the same configuration come with the CPU
+    # baseline below
     e64, emx = engine(abi.MG_FP64), engine(abi.MG_MIXED)
     r64, rmx = e64.UTotal(), emx.UTotal()
-    d = rmx["forceo"] - r64["forceo"]
-    force_rms = float(np.sqrt((d * d).sum() / (r64["forceo"] ** 2).sum()))
-    energy_rel = abs(rmx["u_tot"] - r64["u_tot"]) / abs(r64["u_tot"])
 
     results = {}
     clocks = None
     for name, e in (("fp64", e64), ("mixed", emx)):
         e.BenchSteps(1, W, FLUSH_BYTES)
         barrier(world)
+        calls0 = e.NListCalls()
         if name == "mixed":
             with ClockSampler(dev_index) as cs:
                 ms = e.BenchSteps(1, K, FLUSH_BYTES)
@@ -296,7 +316,8 @@ def run_ours(args):
             ms = e.BenchSteps(1, K, FLUSH_BYTES)
         barrier(world)
         ms = max_over_ranks(ms, world)
-        results[name] = {"ms_per_step": ms / K, "steps_per_s": world * K / (ms * 1e-3)}
+        results[name] = {"ms_per_step": ms / K, "steps_per_s": world * K / (ms * 1e-3),
+                         "list_rebuilds": e.NListCalls() - calls0}
     kernels_per_step = emx.StepKernels(1)
 
     # per-kernel device times (uncaptured launches, same flush regime)
@@ -322,7 +343,6 @@ def run_ours(args):
         peak, peak_src = 6800.0, "fallback"
     ab = algorithmic_bytes(dom, s.np_, s.nmesh, pairs, nbond, s.order)
     achieved = ab / (phases[dom] * 1e-3) / 1e9 if ab else None
-    traffic = traffic_from_profiles(dom)
 
     # end to end through the C ABI with host buffers
     lib = abi.load_library()
@@ -351,13 +371,23 @@ def run_ours(args):
     tsum = max_over_ranks(tsum, world)
     e2e = world * ke / tsum
 
-    cpu = None
+    cpu = cpu1 = None
+    accuracy = {"reference": "none (--no-cpu)"}
     if rank == 0 and not args.no_cpu:
         nt = cpu_threads()
-        times = cpu_baseline(args.seed, threads=nt)
+        ref0 = {}
+        times = cpu_baseline(args.seed, threads=nt, initial=ref0)
         cpu = {"value": len(times) / sum(times), "unit": "steps/s", "cores": nt, "kind": "port",
                "sample": f"{len(times)} BD steps of the full N=65600 workload on {nt} host threads "
                          "(oracle, cell-list mode, threads as the reference's MPI ranks), wall clock per step"}
+        times1 = cpu_baseline(args.seed, budget_s=10.0, max_steps=5, warmup=0, threads=1)
+        cpu1 = {"value": len(times1) / sum(times1), "unit": "steps/s", "cores": 1, "kind": "port",
+                "sample": f"{len(times1)} BD steps of the full N=65600 workload on one host thread "
+                          "(oracle, cell-list mode: the reference's serial build), wall clock per step"}
+        accuracy = {"reference": "oracle FP64 UTotal of the same configuration (CPU restatement of the "
+                                 "reference), forces per particle",
+                    "mixed": utotal_errors(rmx, ref0), "fp64": utotal_errors(r64, ref0),
+                    "bar": {"force_rms": 1e-5}}
 
     if rank == 0:
         out = {
@@ -371,14 +401,17 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "fp64": results["fp64"],
             "mixed_over_fp64": results["mixed"]["steps_per_s"] / results["fp64"]["steps_per_s"],
-            "accuracy": {"force_rms_mixed_vs_fp64": force_rms, "energy_rel_mixed_vs_fp64": energy_rel},
+            "list_rebuilds": {"mixed": results["mixed"]["list_rebuilds"],
+                              "fp64": results["fp64"]["list_rebuilds"], "steps": K},
+            "accuracy": accuracy,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_source": peak_src, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "frac": (achieved / peak) if achieved else None, "traffic": None,
                          "algorithmic_bytes": ab, "kernel_ms": phases[dom]},
             "phases_ms": phases,
             "phases_ms_fp64": phases64,
             "cpu_baseline": cpu,
+            "cpu_baseline_1thread": cpu1,
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 24 * s.np_,
                     "d2h_bytes_per_step": 48 * s.np_ + 32},
             "clocks": clocks,

@@ -167,6 +167,19 @@ int mg_destroy(mg_handle *h);
 int mg_set_positions(mg_handle *h, const double *ro);
 int mg_get_positions(mg_handle *h, double *ro);
 
+/* The device 3D FFT alone, to check it against another FFT library.  It
+ * replaces the FFTW r2c/c2r pair of SPMFFTRec (energy.F90:6525-6587) around
+ * the influence-function multiply of UEwaldRecSPM.  q: an nmesh^3 mesh
+ * (x fastest, then y, then z), loaded in the handle's form as the spread
+ * would leave it; mult, ew: octant tables [fz][fy][kx] of (nmesh/2+1)^3
+ * values, used at fz = min(kz, nmesh-kz), fy = min(ky, nmesh-ky).  Returns
+ * phi = c2r(mult * r2c(q)) (unnormalised, nmesh^3) and *esum = the sum of
+ * ew |r2c(q)|^2 over the half spectrum (kx <= nmesh/2, all ky, kz).  The
+ * handle (an SPME handle) keeps no result: its next UTotal recomputes the
+ * meshes. */
+int mg_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew,
+                 double *phi, double *esum);
+
 /* ---- neighbour lists (A1-A4) --------------------------------------------- */
 
 /* NList(iWriteInput) (nlist.F90:553-596): builds the Verlet list
@@ -178,6 +191,12 @@ int mg_nlist_set(mg_handle *h);
  * rebuilds the Verlet list when sqrt(r2max1)+sqrt(r2max2) > drnlist.
  * drostep may be NULL to use the displacements of the last device step. */
 int mg_nlist_update(mg_handle *h, const double *drostep, int32_t *rebuilt);
+
+/* The number of Verlet-list builds since mg_nlist_set, counting that one:
+ * VListAver's ncall (nlist.F90:953-986), "no of neighbour list calls".
+ * Rebuilds inside device steps (mg_md_run, mg_bd_run, mg_bench_steps) are
+ * counted on the device. */
+int mg_nlist_calls(mg_handle *h, int32_t *ncall);
 
 /* Verlet list in the reference's layout: nneighpn(np) and
  * jpnlist(maxnneigh,np), column-major, 1-based.  MD/BD: half list with the
@@ -372,7 +391,11 @@ int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, double *u_re
  * particles are the polyatomic particles' centres, after mg_set_positions
  * and mg_nlist_set or mg_nlist_update); only the atom positions r[3*na]
  * travel.  Same outputs; every thread adds the forces of its own particle's
- * atoms only, so the atom forces need no atomics and are reproducible. */
+ * atoms only, so the atom forces need no atomics and are reproducible.  The
+ * handle's rcut must be at least the pair cutoff p.rcut (its list holds every
+ * pair within its rcut, and pairs between rcut and rcut + drnlist only right
+ * after a build), else MG_ERR_ARG; a handle whose last list build failed
+ * (MG_ERR_NEIGH_OVERFLOW, MG_ERR_CELL) has no list, MG_ERR_STATE. */
 int mg_poly_utwobody_list(mg_poly *c, mg_handle *centres, const double *r, double *force, double *u_twob,
                           double *virial);
 /* Single-particle MC trials of polyatomic particles (DUTwoBody with
@@ -418,8 +441,11 @@ int mg_poly_destroy(mg_poly *c);
  * ncut above MG_NOALLOC_MAX_NCUT is rejected (MG_ERR_ARG).  All calls share
  * that array, so calls that overlap on the GPU (other streams, other threads)
  * race.  The first call on a device looks up the array's device address; make
- * that first call before any stream capture begins.  On error a message is
- * written to err (if non-NULL). */
+ * that first call before any stream capture begins.  Every later call made
+ * outside stream capture looks the address up again, so a cudaDeviceReset
+ * between calls is harmless; a call made during capture uses the address
+ * found by the last call outside it.  On error a message is written to err
+ * (if non-NULL). */
 int mg_ewald_rec_std_noalloc(int32_t np, const double *d_ro, const double *d_az,
                              const double boxlen[3], double ualpha, int32_t ncut,
                              int32_t ncutregion_cube, double epsi_four_pi, double *d_force,

@@ -94,6 +94,8 @@ LIB_ONLY = [
     ("last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
     ("destroy", C.c_int, [H]),
     ("dutotal_batch", C.c_int, [H, C.c_int32, PI32, PF64, PF64, PI32]),
+    ("nlist_calls", C.c_int, [H, PI32]),
+    ("fft_check", C.c_int, [H, PF64, PF64, PF64, PF64, PF64]),
     ("bd_step_host", C.c_int, [H, PF64, PF64, PF64]),
     ("phase_times", C.c_int, [H, PF64, C.c_int32, PI32, C.c_char_p, C.c_size_t]),
     ("phase_reset", C.c_int, [H, C.c_int32]),

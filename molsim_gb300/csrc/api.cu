@@ -119,7 +119,7 @@ static void free_all(mg_handle *h) {
                     h->d_scan_tmp, h->d_zlow, h->d_coef, h->d_coef_f, h->d_bin_z0, h->d_bin_inv,
                     h->d_bin_kstart, h->d_brick_count, h->d_brick_perm, h->d_brick_rank,
                     h->d_brick_of, h->d_brick_start, h->d_brick_istart, h->d_item_brick, h->d_tiles, h->d_grad, h->d_f32_tabs, h->d_pos_f,
-                    h->d_cell_s, h->d_spl_w, h->d_ffx2, h->d_force2};
+                    h->d_cell_s, h->d_spl_w, h->d_ffx2, h->d_force2, h->d_ro_slot, h->d_ro_slot_f, h->d_scan_tiles};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -403,7 +403,10 @@ int mg_nlist_set(mg_handle *h) {
     if (h->mode == MG_MC && h->txintlist == MG_CELLLIST) MG_TRY(mg_mc_cells_set(h));
     MG_CUDA(h, cudaMemsetAsync(h->d_drosum, 0, sizeof(double) * 3 * h->np, h->st));
     MG_CUDA(h, cudaMemsetAsync(h->d_rebuild, 0, sizeof(int) * 2, h->st));
-    return mg_check_device_error(h);
+    MG_TRY(mg_lists_reset_calls(h));
+    int st = mg_check_device_error(h);
+    if (st != MG_OK) h->list_valid = false;   // an overflowed or failed build is no list
+    return st;
 }
 
 int mg_nlist_update(mg_handle *h, const double *drostep, int32_t *rebuilt) {
@@ -417,8 +420,33 @@ int mg_nlist_update(mg_handle *h, const double *drostep, int32_t *rebuilt) {
     MG_TRY(mg_lists_build(h, true));
     int flag = 0;
     MG_CUDA(h, cudaMemcpyAsync(&flag, h->d_rebuild, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    MG_TRY(mg_check_device_error(h));
+    int st = mg_check_device_error(h);
+    if (st != MG_OK) {
+        h->list_valid = false;   // an overflowed or failed rebuild is no list
+        return st;
+    }
     *rebuilt = flag;
+    return MG_OK;
+}
+
+int mg_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew, double *phi,
+                 double *esum) {
+    if (!h || !q || !mult || !ew || !phi || !esum) return MG_ERR_ARG;
+    if (h->ewald != MG_EWALD_SPM) return mg_fail(h, MG_ERR_STATE, "the handle has no SPME mesh");
+    MG_CUDA(h, cudaStreamSynchronize(h->st));
+    MG_TRY(mg_spme_fft_check(h, q, mult, ew, phi, esum));
+    h->have_force = false;
+    h->have_rec = false;
+    return MG_OK;
+}
+
+int mg_nlist_calls(mg_handle *h, int32_t *ncall) {
+    if (!h || !ncall) return MG_ERR_ARG;
+    if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_nlist_set has not been called");
+    int v[3];
+    MG_CUDA(h, cudaMemcpyAsync(v, h->d_rebuild, sizeof(int) * 3, cudaMemcpyDeviceToHost, h->st));
+    MG_CUDA(h, cudaStreamSynchronize(h->st));
+    *ncall = v[2];
     return MG_OK;
 }
 

@@ -43,18 +43,12 @@ __global__ void k_cell_assign(const double *__restrict__ ro, int np, double3 hal
     atomicAdd(&count[c], 1);
 }
 
-// single-block exclusive scan: out[i] = sum(in[0..i)), out[n] = total
-__global__ void k_scan1(const int *__restrict__ in, int *__restrict__ out, int n,
-                        const int *__restrict__ gate) {
-    if (gate && *gate == 0) return;
-    __shared__ int warp_sums[32];
-    int t = threadIdx.x, nt = blockDim.x;
-    int chunk = (n + nt - 1) / nt;
-    int b = t * chunk, e = min(n, b + chunk);
-    int s = 0;
-    for (int i = b; i < e; ++i) s += in[i];
-    // block exclusive scan of s
-    int lane = t & 31, w = t >> 5;
+// Exclusive scan of the cell counts in two passes over tiles of kScanTile
+// cells: k_scan_tiles scans each tile (coalesced loads, a block per tile) and
+// records the tile total; k_scan_fix adds the sum of the earlier tiles' totals
+// and writes out[n] = total.  out[i] = sum(in[0..i)).
+__device__ __forceinline__ int block_excl_scan(int s, int *warp_sums, int *total) {
+    int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
     int v = s;
     for (int o = 1; o < 32; o <<= 1) {
         int y = __shfl_up_sync(0xffffffffu, v, o);
@@ -63,7 +57,6 @@ __global__ void k_scan1(const int *__restrict__ in, int *__restrict__ out, int n
     if (lane == 31) warp_sums[w] = v;
     __syncthreads();
     if (w == 0) {
-        int nw = nt >> 5;
         int x = (lane < nw) ? warp_sums[lane] : 0;
         for (int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -72,12 +65,51 @@ __global__ void k_scan1(const int *__restrict__ in, int *__restrict__ out, int n
         if (lane < nw) warp_sums[lane] = x;
     }
     __syncthreads();
-    int excl = v - s + (w > 0 ? warp_sums[w - 1] : 0);
-    for (int i = b; i < e; ++i) {
-        out[i] = excl;
-        excl += in[i];
+    if (total) *total = warp_sums[nw - 1];
+    return v - s + (w > 0 ? warp_sums[w - 1] : 0);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int *__restrict__ in, int *__restrict__ out,
+                                                             int n, int *__restrict__ tilesum,
+                                                             const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    __shared__ int warp_sums[32];
+    constexpr int per = kScanTile / kScanThreads;
+    int base = blockIdx.x * kScanTile + threadIdx.x * per;
+    int v[per], s = 0;
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        s += v[k];
     }
-    if (t == nt - 1) out[n] = excl;
+    int tot;
+    int excl = block_excl_scan(s, warp_sums, &tot);
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+        if (base + k < n) out[base + k] = excl;
+        excl += v[k];
+    }
+    if (threadIdx.x == 0) tilesum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_fix(int *__restrict__ out, int n,
+                                                           const int *__restrict__ tilesum, int ntile,
+                                                           const int *__restrict__ gate) {
+    if (gate && *gate == 0) return;
+    __shared__ int warp_sums[32];
+    __shared__ int off;
+    int b = blockIdx.x;
+    int s = 0;
+    for (int k = threadIdx.x; k < b; k += blockDim.x) s += tilesum[k];
+    int tot;
+    block_excl_scan(s, warp_sums, &tot);
+    if (threadIdx.x == 0) off = tot;
+    __syncthreads();
+    int o = off;
+    if (o != 0) {
+        for (int i = b * kScanTile + threadIdx.x; i < min(n, (b + 1) * kScanTile); i += blockDim.x) out[i] += o;
+    }
+    if (b == ntile - 1 && threadIdx.x == 0) out[n] = o + tilesum[b];
 }
 
 __global__ void k_cell_scatter(const int *__restrict__ cellof, int np, const int *__restrict__ start,
@@ -108,11 +140,20 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start, int *__res
     }
 }
 
-__global__ void k_slot_of(const int *__restrict__ perm, int np, int *__restrict__ slot,
+// slot of each particle, and the positions in slot order with the cell
+// index in .w (exact: cell indices are far below 2^53)
+__global__ void k_slot_of(const int *__restrict__ perm, const double *__restrict__ ro,
+                          const int *__restrict__ cellof, int np, int *__restrict__ slot,
+                          double4 *__restrict__ ro_slot, float4 *__restrict__ ro_f,
                           const int *__restrict__ gate) {
     if (gate && *gate == 0) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < np) slot[perm[s]] = s;
+    if (s >= np) return;
+    int p = perm[s];
+    slot[p] = s;
+    double x = ro[3 * p], y = ro[3 * p + 1], z = ro[3 * p + 2];
+    ro_slot[s] = make_double4(x, y, z, (double)cellof[p]);
+    ro_f[s] = make_float4((float)x, (float)y, (float)z, 0.0f);
 }
 
 struct StencilArgs {
@@ -123,48 +164,106 @@ struct StencilArgs {
 // Verlet list of slot i: all slots j != i in the neighbour cells with
 // r^2 < rs2cut (SetVListMD/MC membership; the half-list ownership rule is
 // applied only when the list is exported in the reference layout).
-__global__ void k_vlist(const double *__restrict__ ro, const int *__restrict__ perm,
-                        const int *__restrict__ cellof, const int *__restrict__ start, int np,
-                        StencilArgs sa, mg_box box, double rs2cut, int maxnb,
-                        int *__restrict__ nnb, int *__restrict__ nbr, int *__restrict__ err,
-                        const int *__restrict__ gate) {
+// Positions are read in slot order (ro_slot), so the candidates of a cell
+// are consecutive.  The three cells x-1, x, x+1 of a stencil row are
+// consecutive cells too, so a row that does not wrap around the box is one
+// slot range; the nine rows' ranges are loaded before the distance loop.
+// Neighbours are listed by cell (dz, dy, dx order) and by slot within a
+// cell, as cell-by-cell scanning would list them.
+// Membership is decided by the reference's FP64 arithmetic, but GB300 issues
+// FP64 at 1/64 of the FP32 rate, so every candidate first gets an FP32
+// distance from FP32 copies of the positions (ro_f).  Its error is far below
+// `band` (see vlist_band); only candidates within `band` of the cutoff are
+// decided in FP64, which gives the same set as testing every candidate so.
+__device__ __forceinline__ float pbc1f(float d, float half, float len) {
+    return (fabsf(d) > half) ? d - copysignf(len, d) : d;
+}
+__device__ __forceinline__ int wrap_cell(int x, int n) {
+    x += (x < 0) ? n : 0;
+    return x - ((x >= n) ? n : 0);
+}
+
+struct VlistBand {
+    float lo, hi;        // FP32 r^2 below lo: inside; at or above hi: outside
+    float half[3], len[3];
+};
+
+__global__ void __launch_bounds__(128) k_vlist(const double4 *__restrict__ ro_slot,
+                                               const float4 *__restrict__ ro_f,
+                                               const int *__restrict__ start, int np, StencilArgs sa,
+                                               mg_box box, VlistBand band, double rs2cut, int maxnb,
+                                               int *__restrict__ nnb, int *__restrict__ nbr,
+                                               const int *__restrict__ perm, int *__restrict__ err,
+                                               const int *__restrict__ gate) {
     if (gate && *gate == 0) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    int p = perm[i];
-    double xi = ro[3 * p], yi = ro[3 * p + 1], zi = ro[3 * p + 2];
-    int c = cellof[p];
+    double4 me = ro_slot[i];
+    float4 mf = ro_f[i];
+    int c = (int)me.w;
     int cx = c % sa.nc.x, cy = (c / sa.nc.x) % sa.nc.y, cz = c / (sa.nc.x * sa.nc.y);
+    // a row is one range when it spans three distinct cells without wrapping
+    // (or is a collapsed dimension's single cell)
+    bool one = (sa.lo[0] == sa.hi[0]) || (cx >= 1 && cx + 1 < sa.nc.x);
+    // the nine rows (dz, dy in -1..1; the offsets a collapsed dimension does
+    // not have are empty), their slot ranges loaded up front
+    int rb[9], re[9];
+    unsigned rows = 0;   // bit r: row r exists
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        int dz = r / 3 - 1, dy = r % 3 - 1;
+        rb[r] = 0;
+        re[r] = 0;
+        if (dz < sa.lo[2] || dz > sa.hi[2] || dy < sa.lo[1] || dy > sa.hi[1]) continue;
+        rows |= 1u << r;
+        int z = wrap_cell(cz + dz, sa.nc.z);
+        int y = wrap_cell(cy + dy, sa.nc.y);
+        int row = (y + z * sa.nc.y) * sa.nc.x;
+        if (one) {
+            rb[r] = start[row + cx + sa.lo[0]];
+            re[r] = start[row + cx + sa.hi[0] + 1];
+        } else {
+            rb[r] = row;   // a wrapping row: its three cells are visited one by one below
+            re[r] = -1;
+        }
+    }
     int cnt = 0;
-    for (int dz = sa.lo[2]; dz <= sa.hi[2]; ++dz) {
-        int z = cz + dz;
-        z += (z < 0) ? sa.nc.z : 0;
-        z -= (z >= sa.nc.z) ? sa.nc.z : 0;
-        for (int dy = sa.lo[1]; dy <= sa.hi[1]; ++dy) {
-            int y = cy + dy;
-            y += (y < 0) ? sa.nc.y : 0;
-            y -= (y >= sa.nc.y) ? sa.nc.y : 0;
-            for (int dx = sa.lo[0]; dx <= sa.hi[0]; ++dx) {
-                int x = cx + dx;
-                x += (x < 0) ? sa.nc.x : 0;
-                x -= (x >= sa.nc.x) ? sa.nc.x : 0;
-                int cc = x + y * sa.nc.x + z * sa.nc.x * sa.nc.y;
-                int b = start[cc], e = start[cc + 1];
-                for (int j = b; j < e; ++j) {
-                    if (j == i) continue;
-                    int q = perm[j];
-                    double ddx = mg_pbc1(__dsub_rn(xi, ro[3 * q]), box.half[0], box.len[0]);
-                    double ddy = mg_pbc1(__dsub_rn(yi, ro[3 * q + 1]), box.half[1], box.len[1]);
-                    double ddz = mg_pbc1(__dsub_rn(zi, ro[3 * q + 2]), box.half[2], box.len[2]);
-                    double r2 = mg_r2_exact(ddx, ddy, ddz);
-                    if (r2 < rs2cut) {
-                        if (cnt < maxnb) nbr[(size_t)cnt * np + i] = j;
-                        ++cnt;
-                    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        if (!(rows >> r & 1u)) continue;   // an offset of a collapsed dimension
+        for (int d = 0; d < (one ? 1 : 3); ++d) {
+            int b, e;
+            if (one) {
+                b = rb[r];
+                e = re[r];
+            } else {
+                int cc = rb[r] + wrap_cell(cx + d - 1, sa.nc.x);
+                b = start[cc];
+                e = start[cc + 1];
+            }
+            for (int j = b; j < e; ++j) {
+                if (j == i) continue;
+                float4 qf = ro_f[j];
+                float fx = pbc1f(mf.x - qf.x, band.half[0], band.len[0]);
+                float fy = pbc1f(mf.y - qf.y, band.half[1], band.len[1]);
+                float fz = pbc1f(mf.z - qf.z, band.half[2], band.len[2]);
+                float r2f = fx * fx + fy * fy + fz * fz;
+                bool in = r2f < band.lo;
+                if (!in && r2f < band.hi) {   // near the cutoff: the reference's FP64 test
+                    double4 q = ro_slot[j];
+                    double ddx = mg_pbc1(__dsub_rn(me.x, q.x), box.half[0], box.len[0]);
+                    double ddy = mg_pbc1(__dsub_rn(me.y, q.y), box.half[1], box.len[1]);
+                    double ddz = mg_pbc1(__dsub_rn(me.z, q.z), box.half[2], box.len[2]);
+                    in = mg_r2_exact(ddx, ddy, ddz) < rs2cut;
+                }
+                if (in) {
+                    if (cnt < maxnb) nbr[(size_t)cnt * np + i] = j;
+                    ++cnt;
                 }
             }
         }
     }
+    int p = perm[i];
     if (cnt > maxnb) {
         mg_dev_error(err, MG_ERR_NEIGH_OVERFLOW, p + 1, cnt, maxnb);
         cnt = maxnb;
@@ -268,6 +367,7 @@ __global__ void __launch_bounds__(kChkThreads) k_chk_second(const double *__rest
     if (lane == 0) {
         int f = (sqrt(__longlong_as_double(m1)) + sqrt(__longlong_as_double(m2)) > drnlist) ? 1 : 0;
         flag[0] = f;
+        flag[2] += f;   // list builds (the rebuild follows this check)
         *counter = 0;
         if (use_cond) cudaGraphSetConditional(cond, (unsigned)f);
     }
@@ -366,6 +466,30 @@ StencilArgs make_stencil(const mg_handle *h) {
     return sa;
 }
 
+// The FP32 filter's band around the cutoff.  With |x| <= L/2 + rcell, the
+// FP32 copy of a coordinate is off by at most ulp(L)/2, the difference and the
+// periodic shift round once each, so a component is off by at most
+// e = 2 ulp(Lmax) (ulp(v) = v 2^-23); r^2 <= rs2cut + band then is off by at
+// most about 6 e sqrt(rs2cut) plus its own rounding, 4 ulp(rs2cut).  The band
+// takes ten times that and 1e-4 rs2cut more.  (Where |dx| is near L/2 the
+// FP32 and FP64 forms may shift differently, but the two shifted values have
+// the same magnitude, so r^2 does not jump.)
+VlistBand make_band(const mg_handle *h) {
+    VlistBand b;
+    double lmax = 0;
+    for (int m = 0; m < 3; ++m) {
+        b.half[m] = (float)h->boxlen2[m];
+        b.len[m] = (float)h->boxlen[m];
+        lmax = fmax(lmax, h->boxlen[m]);
+    }
+    double ulp = ldexp(1.0, -23);
+    double e = 2.0 * (lmax + h->rcut + h->drnlist) * ulp;
+    double band = 10.0 * (6.0 * e * sqrt(h->rs2cut) + 4.0 * h->rs2cut * ulp) + 1e-4 * h->rs2cut;
+    b.lo = (float)(h->rs2cut - band);
+    b.hi = (float)(h->rs2cut + band);
+    return b;
+}
+
 mg_box make_box(const mg_handle *h) {
     mg_box b;
     for (int m = 0; m < 3; ++m) {
@@ -379,8 +503,10 @@ mg_box make_box(const mg_handle *h) {
 }  // namespace
 
 void mg_scan_exclusive(mg_handle *h, const int *in, int *out, int n, const int *gate) {
-    k_scan1<<<1, 1024, 0, h->st>>>(in, out, n, gate);
-    h->launches++;
+    int ntile = (n + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<ntile, kScanThreads, 0, h->st>>>(in, out, n, h->d_scan_tiles, gate);
+    k_scan_fix<<<ntile, kScanThreads, 0, h->st>>>(out, n, h->d_scan_tiles, ntile, gate);
+    h->launches += 2;
 }
 
 // InitCellList(rcut + drnlist) (celllist.F90:76-152): grid and stencil range
@@ -425,14 +551,17 @@ int mg_lists_init(mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_nnb, sizeof(int) * np));
     MG_CUDA(h, cudaMalloc(&h->d_nbr, sizeof(int) * (size_t)h->maxnb * np));
     MG_CUDA(h, cudaMalloc(&h->d_pos_s, sizeof(double4) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_ro_slot, sizeof(double4) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_ro_slot_f, sizeof(float4) * np));
+    MG_CUDA(h, cudaMalloc(&h->d_scan_tiles, sizeof(int) * ((nc + kScanTile - 1) / kScanTile)));
     h->nblk_chk = (np + kChkThreads - 1) / kChkThreads;
     MG_CUDA(h, cudaMalloc(&h->d_drostep, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMalloc(&h->d_drosum, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMalloc(&h->d_blkmax, sizeof(double) * (2 * h->nblk_chk + np)));
-    MG_CUDA(h, cudaMalloc(&h->d_rebuild, sizeof(int) * 2));
+    MG_CUDA(h, cudaMalloc(&h->d_rebuild, sizeof(int) * 3));
     MG_CUDA(h, cudaMemsetAsync(h->d_drosum, 0, sizeof(double) * 3 * np, h->st));
     MG_CUDA(h, cudaMemsetAsync(h->d_drostep, 0, sizeof(double) * 3 * np, h->st));
-    MG_CUDA(h, cudaMemsetAsync(h->d_rebuild, 0, sizeof(int) * 2, h->st));
+    MG_CUDA(h, cudaMemsetAsync(h->d_rebuild, 0, sizeof(int) * 3, h->st));
     if (h->mode == MG_MC && h->txintlist == MG_CELLLIST) {
         MG_CUDA(h, cudaMalloc(&h->d_iphead, sizeof(int) * nc));
         MG_CUDA(h, cudaMalloc(&h->d_npart, sizeof(int) * nc));
@@ -460,13 +589,23 @@ int mg_lists_build(mg_handle *h, bool conditional) {
                                          gate);
     k_cell_sort<<<(h->ncelltot + tb - 1) / tb, tb, 0, h->st>>>(h->ncelltot, h->d_cellstart,
                                                                h->d_perm, gate);
-    k_slot_of<<<gb, tb, 0, h->st>>>(h->d_perm, np, h->d_slot, gate);
-    k_vlist<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_ro, h->d_perm, h->d_cellof, h->d_cellstart, np,
-                                   make_stencil(h), make_box(h), h->rs2cut, h->maxnb, h->d_nnb,
-                                   h->d_nbr, h->d_err, gate);
-    h->launches += 6;
+    k_slot_of<<<gb, tb, 0, h->st>>>(h->d_perm, h->d_ro, h->d_cellof, np, h->d_slot, h->d_ro_slot,
+                                    h->d_ro_slot_f, gate);
+    k_vlist<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_ro_slot, h->d_ro_slot_f, h->d_cellstart, np,
+                                                 make_stencil(h), make_box(h), make_band(h), h->rs2cut,
+                                                 h->maxnb, h->d_nnb, h->d_nbr, h->d_perm, h->d_err, gate);
+    h->launches += 5;
     MG_CUDA(h, cudaGetLastError());
     h->list_valid = true;
+    return MG_OK;
+}
+
+// the list-build count of VListAver (nlist.F90:953-986): 1 after the
+// initial build, then one more per rebuild (counted by k_chk_second)
+int mg_lists_reset_calls(mg_handle *h) {
+    k_set_int<<<1, 1, 0, h->st>>>(h->d_rebuild + 2, 1);
+    h->launches++;
+    MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }
 

@@ -95,6 +95,9 @@ struct mg_handle {
     int *d_perm = nullptr, *d_slot = nullptr;
     int *d_nnb = nullptr, *d_nbr = nullptr;
     double4 *d_pos_s = nullptr;
+    double4 *d_ro_slot = nullptr;   // list build: positions in slot order, cell index in .w
+    float4 *d_ro_slot_f = nullptr;  // list build: their FP32 copies (the distance filter)
+    int *d_scan_tiles = nullptr;    // list build: per-tile totals of the cell-count scan
     bool list_valid = false;
     bool list_stale = false;        // MC + cell list: particles moved since the last build
     // MC cell list (doubly linked lists, reference layout; 1-based, 0 = none)
@@ -185,7 +188,9 @@ struct mg_handle {
 
     // ---- list check ---------------------------------------------------------
     double *d_drostep = nullptr, *d_drosum = nullptr, *d_blkmax = nullptr;
-    int *d_rebuild = nullptr;       // [2]: current flag, flag of the previous step
+    // [3]: current flag, the list check's block counter, number of list
+    // builds since mg_nlist_set (counting that one: VListAver's ncall)
+    int *d_rebuild = nullptr;
     int nblk_chk = 0;
 
     // ---- MD / BD ----------------------------------------------------------------
@@ -284,6 +289,9 @@ inline cudaError_t mg_launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, 
 // order as their 64-bit patterns, so the maximum runs on integers.  Every
 // thread of the block calls it (it holds a barrier).
 constexpr int kChkThreads = 256;
+// cell-count scan: tiles of kScanTile cells, a block of kScanThreads per tile
+constexpr int kScanThreads = 512;
+constexpr int kScanTile = 4096;
 __device__ __forceinline__ void mg_chk_accum(int p, int np, double d0, double d1, double d2, bool reset,
                                              double *__restrict__ drosum, double *__restrict__ r2out,
                                              double *__restrict__ blkmax) {
@@ -380,6 +388,8 @@ double mg_spme_fx_scale(const mg_handle *h);
 int mg_spme_potential(mg_handle *h);
 int mg_spme_load_mesh(mg_handle *h, const double *q);
 int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul);
+int mg_spme_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew, double *phi,
+                      double *esum);
 int mg_mc_init(mg_handle *h);
 void mg_mc_free(mg_handle *h);
 int mg_mc_dutotal(mg_handle *h, int nptm, const int32_t *ipnptm, const double *rotm,
@@ -414,6 +424,7 @@ int mg_host_bspline(int order, double pos, int *kmax, double *values, double *de
 
 // kernels shared between modules
 void mg_scan_exclusive(mg_handle *h, const int *in, int *out, int n, const int *gate);
+int mg_lists_reset_calls(mg_handle *h);
 
 template <typename T> struct mg_cplx;
 template <> struct mg_cplx<double> { typedef double2 type; };

@@ -199,9 +199,12 @@ int na_fail(char *err, size_t err_len, int code, const char *fmt, ...) {
     return code;
 }
 
-// Device address of the scratch array on the current device, looked up once
-// per device and kept.
-int scratch_address(double2 **out, char *err, size_t err_len) {
+// Device address of the scratch array on the current device.  A call made
+// outside stream capture looks it up again (cheap), so that a device reset
+// between calls, after which the library's module and its array are loaded
+// anew, cannot leave a stale address behind; a call made while `s` is being
+// captured uses the address kept by the last call outside capture.
+int scratch_address(cudaStream_t s, double2 **out, char *err, size_t err_len) {
     int dev = -1;
     cudaError_t ce = cudaGetDevice(&dev);
     if (ce != cudaSuccess)
@@ -209,8 +212,13 @@ int scratch_address(double2 **out, char *err, size_t err_len) {
     if (dev < 0 || dev >= kNaMaxDevices)
         return na_fail(err, err_len, MG_ERR_UNSUPPORTED, "device ordinal %d is beyond the %d supported",
                        dev, kNaMaxDevices);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+        cudaGetLastError();   // cannot tell: treat the call as one under capture
+        cs = cudaStreamCaptureStatusActive;
+    }
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_addr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone || !g_na_addr[dev]) {
         void *p = nullptr;
         ce = cudaGetSymbolAddress(&p, g_na_scratch);
         if (ce != cudaSuccess || !p)
@@ -239,8 +247,9 @@ extern "C" int mg_ewald_rec_std_noalloc(int32_t np, const double *d_ro, const do
         return na_fail(err, err_len, MG_ERR_ARG,
                        "ncut = %d exceeds the %d that the fixed scratch array of %zu bytes holds",
                        ncut, kNaMaxNcut, sizeof(g_na_scratch));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     double2 *scratch = nullptr;
-    int st = scratch_address(&scratch, err, err_len);
+    int st = scratch_address(s, &scratch, err, err_len);
     if (st != MG_OK) return st;
 
     const double tp = 2.0 * 3.1415926535897932;
@@ -252,7 +261,6 @@ extern "C" int mg_ewald_rec_std_noalloc(int32_t np, const double *d_ro, const do
     a.tpbi = make_double3(tp / boxlen[0], tp / boxlen[1], tp / boxlen[2]);
     a.fac0 = tp / (boxlen[0] * boxlen[1] * boxlen[2]);
     a.ualpha2 = ualpha * ualpha;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     int nslot = a.nside * a.nside * a.nside;
     k_na_sk<<<nslot, 256, 0, s>>>(a, d_ro, d_az, scratch);
     k_na_force<<<(np + 127) / 128, 128, 0, s>>>(a, d_ro, d_az, epsi_four_pi, scratch, d_force);

@@ -552,7 +552,11 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
     c->h_part.resize((size_t)c->nblk_w * (p->nptpt + 1));
     // search-start bins per atom-type pair over [r2umin, z_low of the first
     // record]: bin b starts at the first record whose z_low is at or below
-    // the bin's upper edge (records run from large to small z_low)
+    // the upper edge of bin b+1 (records run from large to small z_low).
+    // The device rounds the bin of an r2 independently of this edge, so an
+    // r2 a few ulps past bin b's own upper edge can land in bin b; the
+    // margin of one bin keeps such an r2 below the edge used here, and the
+    // search never starts past the reference's record.
     {
         std::vector<double> z0(p->natat), inv(p->natat);
         std::vector<int> kk((size_t)p->natat * kPolyBins);
@@ -563,7 +567,7 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
             z0[q] = lo;
             inv[q] = kPolyBins / (hi - lo);
             for (int b = 0; b < kPolyBins; ++b) {
-                double upper = lo + (b + 1) / inv[q];
+                double upper = lo + (b + 2) / inv[q];
                 int rr = r0;
                 while (rr + 12 < p->nbuf && p->ubuf[rr] > upper) rr += 12;
                 kk[(size_t)q * kPolyBins + b] = b == kPolyBins - 1 ? r0 : rr;
@@ -816,7 +820,14 @@ extern "C" int mg_poly_utwobody_list(mg_poly *c, mg_handle *h, const double *r, 
     const mg_poly_params &p = c->p;
     if (h->np != p.np) return poly_fail(c, MG_ERR_ARG, "the centres handle holds %d particles, not %d", h->np, p.np);
     if (!h->list_valid) return poly_fail(c, MG_ERR_STATE, "the centres handle has no list (mg_nlist_set)");
-    if (!(h->rcut + h->drnlist >= p.rcut)) return poly_fail(c, MG_ERR_ARG, "the centres list is shorter than rcut");
+    // after mg_nlist_update the list holds every pair within the handle's
+    // rcut (pairs beyond it may have moved in unnoticed within the skin)
+    if (!(h->rcut >= p.rcut))
+        return poly_fail(c, MG_ERR_ARG, "the centres handle's rcut %g is below the pair cutoff %g", h->rcut, p.rcut);
+    // a pending device error of the handle (mg_nlist_set and mg_nlist_update
+    // drop a list whose build failed, so an overflowed list never gets here)
+    if (mg_check_device_error(h) != MG_OK)
+        return poly_fail(c, MG_ERR_STATE, "the centres handle reports an error: %s", h->err.c_str());
     for (int m = 0; m < 3; ++m)
         if (h->boxlen[m] != p.boxlen[m]) return poly_fail(c, MG_ERR_ARG, "the centres handle has another box");
     POLY_CUDA(c, cudaStreamSynchronize(h->st));

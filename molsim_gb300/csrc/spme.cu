@@ -1554,6 +1554,70 @@ int mg_spme_potential(mg_handle *h) {
                               1.0 / mg_spme_fx_scale(h));
 }
 
+// The device FFT on a given mesh, for checking it against another FFT: the
+// FP64 mesh q (n^3, x fastest) is loaded as the spread would leave it, the
+// form's forward transform, the multiplier `mult` (the place of meshfac) and
+// the inverse transform run as in UTotal, and phi = c2r(mult * r2c(q))
+// (unnormalised, FFTW's conventions) and esum = sum of ew |r2c(q)|^2 over the
+// half spectrum come back.  mult and ew are octant tables [fz][fy][kx] of
+// (n/2+1)^3 values, looked up at fz = min(kz, n-kz), fy = min(ky, n-ky).
+// The handle's meshes are overwritten (the next UTotal rebuilds them).
+int mg_spme_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew, double *phi,
+                      double *esum) {
+    const int n = h->nmesh, nh = h->nh;
+    const size_t n3 = (size_t)n * n * n, o3 = (size_t)nh * nh * nh;
+    const bool mixed = h->form == MG_MIXED;
+    const size_t esz = mixed ? sizeof(float) : sizeof(double);
+    double *d_q = nullptr;
+    void *d_tab = nullptr;
+    std::vector<unsigned char> tab(3 * o3 * esz, 0);   // mult, ew, vw = 0
+    for (size_t i = 0; i < o3; ++i) {
+        if (mixed) {
+            ((float *)tab.data())[i] = (float)mult[i];
+            ((float *)tab.data())[o3 + i] = (float)ew[i];
+        } else {
+            ((double *)tab.data())[i] = mult[i];
+            ((double *)tab.data())[o3 + i] = ew[i];
+        }
+    }
+    int st = MG_OK;
+    std::vector<double> part(2 * (size_t)h->nblk_rec);
+    cudaError_t ce = cudaMalloc(&d_q, sizeof(double) * n3);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_tab, tab.size());
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_q, q, sizeof(double) * n3, cudaMemcpyHostToDevice, h->st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, h->st);
+    if (ce == cudaSuccess) {
+        st = mg_spme_load_mesh(h, d_q);
+        ConvArgs cv;
+        cv.part = h->d_part + h->part_rec;
+        cv.mf = d_tab;
+        cv.ew = (const unsigned char *)d_tab + o3 * esz;
+        cv.vw = (const unsigned char *)d_tab + 2 * o3 * esz;
+        if (st == MG_OK) {
+            st = mixed ? fft_launch<float>(h, (float *)h->d_Q, (float2 *)h->d_F, (const float2 *)h->d_tw, cv,
+                                           (float)(1.0 / mg_spme_fx_scale(h)))
+                       : fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw,
+                                            cv, 1.0 / mg_spme_fx_scale(h));
+        }
+        if (st == MG_OK) st = mg_spme_mesh_to_f64(h, d_q, 1.0);
+        if (st == MG_OK) {
+            ce = cudaMemcpyAsync(phi, d_q, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->st);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(part.data(), h->d_part + h->part_rec, sizeof(double) * part.size(),
+                                     cudaMemcpyDeviceToHost, h->st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);
+        }
+    }
+    if (d_q) cudaFree(d_q);
+    if (d_tab) cudaFree(d_tab);
+    if (st != MG_OK) return st;
+    if (ce != cudaSuccess) return mg_fail(h, MG_ERR_CUDA, "fft check: %s", cudaGetErrorString(ce));
+    double e = 0.0;
+    for (int b = 0; b < h->nblk_rec; ++b) e += part[2 * b];
+    *esum = e;
+    return MG_OK;
+}
+
 // FP64 charge mesh -> the fixed-point mesh the FFT reads
 int mg_spme_load_mesh(mg_handle *h, const double *q) {
     size_t n3 = (size_t)h->nmesh * h->nmesh * h->nmesh;

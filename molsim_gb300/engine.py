@@ -97,6 +97,13 @@ class Engine:
         self._check(self._fn("nlist_update")(self.h, abi.f64(d), abi.i32(reb)), "nlist_update")
         return bool(reb[0])
 
+    def NListCalls(self):
+        """Verlet-list builds since NList('write'), counting it (VListAver's
+        ncall, nlist.F90:953-986)."""
+        n = np.zeros(1, dtype=np.int32)
+        self._check(self.lib.mg_nlist_calls(self.h, abi.i32(n)), "nlist_calls")
+        return int(n[0])
+
     def VList(self, maxnneigh=None):
         """nneighpn(np), jpnlist as a list of neighbour arrays (1-based)."""
         maxn = maxnneigh or self.np

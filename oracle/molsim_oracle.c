@@ -963,10 +963,12 @@ int orc_celllist_test(orc_sys *s) {
  * nlist.F90
  * ====================================================================== */
 
-/* SetVListMD, nlist.F90:724-765 (serial: ipmyid = 1..np) */
-static int set_vlist_md(orc_sys *s) {
+/* SetVListMD, nlist.F90:724-765: the rows of particles ip in [lo, hi)
+   (the reference's rank loop over ipmyid; every row depends on the
+   positions only, so a split of the rows gives the serial lists) */
+static int set_vlist_md_rows(orc_sys *s, int lo, int hi) {
     double rs2cut = pow2(s->rcut + s->drnlist);
-    for (int ip = 1; ip <= s->np; ++ip) {
+    for (int ip = lo + 1; ip <= hi; ++ip) {
         int *nn = &s->nneighpn[ip - 1];
         *nn = 0;
         for (int jp = 1; jp <= s->np; ++jp) {
@@ -983,6 +985,29 @@ static int set_vlist_md(orc_sys *s) {
             }
         }
     }
+    return 0;
+}
+
+typedef struct {
+    orc_sys *s;
+    int st[ORC_MAX_THREADS];
+} vlist_job;
+
+static void vlist_job_run(void *ctx, int t, int nt) {
+    vlist_job *j = (vlist_job *)ctx;
+    long lo, hi;
+    orc_range(j->s->np, t, nt, &lo, &hi);
+    j->st[t] = set_vlist_md_rows(j->s, (int)lo, (int)hi);
+}
+
+static int set_vlist_md(orc_sys *s) {
+    int nt = orc_threads();
+    if (nt <= 1) return set_vlist_md_rows(s, 0, s->np);
+    vlist_job j;
+    j.s = s;
+    orc_par_run(vlist_job_run, &j, nt);
+    for (int t = 0; t < nt; ++t)
+        if (j.st[t]) return j.st[t];
     return 0;
 }
 

@@ -52,6 +52,7 @@ def test_rebuild_rule_sequence(orc, gpu_lib):
         e.NList("write")
     rng = np.random.default_rng(5)
     ro = s.ro_flat().copy()
+    nreb = 0
     for step in range(25):
         d = rng.normal(0, 0.08, ro.shape)
         ro = ro + d
@@ -63,3 +64,26 @@ def test_rebuild_rule_sequence(orc, gpu_lib):
             rb.append(e.NList("step", d))
         assert rb[0] == rb[1], step
         assert _lists(gpu) == _lists(ref)
+        nreb += rb[0]
+    assert nreb >= 2
+    # VListAver's ncall: the initial build and every rebuild
+    assert gpu.NListCalls() == 1 + nreb
+
+
+def test_rebuild_count_in_device_steps(orc, gpu_lib):
+    """Rebuilds inside captured MD steps (the graph's conditional node) are
+    counted on the device: the same count as the same steps launched one
+    kernel at a time, where the host reads the rebuild flag."""
+    s = prepared(configs.small_system(seed=44, n=300, L=36.0, drnlist=0.3), orc)
+    v = s.maxwell_velocities(seed=3)
+    counts = []
+    for uncaptured in (True, False):
+        gpu = Engine(s)
+        gpu.SetPositions(s.ro_flat())
+        gpu.NList("write")
+        gpu.MDSetup(0.002, v)
+        gpu.PhaseReset(uncaptured)
+        gpu.VelVer(40)
+        counts.append(gpu.NListCalls())
+        gpu.close()
+    assert counts[0] == counts[1] and counts[0] >= 3, counts

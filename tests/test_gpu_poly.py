@@ -151,3 +151,37 @@ def test_poly_device_list_matches_host_list(ewald, orc, gpu_lib):
     a, b = e.UTotal(nn, jl), e.UTotal()
     assert abs(a["u_tot"] - b["u_tot"]) <= 1e-10 * abs(a["u_tot"])
     e.close()
+
+
+def test_poly_device_list_needs_the_pair_cutoff(orc, gpu_lib):
+    """A centres handle whose rcut is below the pair cutoff is refused even
+    when rcut + drnlist reaches it: after mg_nlist_update its list holds only
+    the pairs within its rcut.  A handle whose list build failed has no list."""
+    from molsim_gb300 import Engine
+    s = configs.water_ions(seed=16, nwater=120, nsalt=8, L=20.0)
+    s.build_table(orc.orc_pot_twobody_tab)
+    e = PolyEngine(s, 64)
+    c = s.centre_system(skin=2.0)
+    c.rcut = s.rcut - 1.0                     # rcut + skin > pair cutoff > rcut
+    short = Engine(c)
+    short.SetPositions(abi.as_f64(s.ro.reshape(-1)))
+    short.NList("write")
+    r = s.atom_positions()
+    force = np.zeros(3 * len(r))
+    ut = np.zeros(e.p.nptpt + 1)
+    vir = np.zeros(1)
+    st = gpu_lib.mg_poly_utwobody_list(e.h, short.h, abi.f64(r.reshape(-1)), abi.f64(force), abi.f64(ut),
+                                       abi.f64(vir))
+    assert abi.STATUS[st] == "MG_ERR_ARG"
+    # a list that overflows its capacity is dropped, and the poly call refuses it
+    c2 = s.centre_system(skin=1.0)
+    c2.maxnneigh = 1
+    tiny = Engine(c2)
+    tiny.SetPositions(abi.as_f64(s.ro.reshape(-1)))
+    with pytest.raises(MolsimError):
+        tiny.NList("write")
+    st = gpu_lib.mg_poly_utwobody_list(e.h, tiny.h, abi.f64(r.reshape(-1)), abi.f64(force), abi.f64(ut),
+                                       abi.f64(vir))
+    assert abi.STATUS[st] == "MG_ERR_STATE"
+    for x in (short, tiny, e):
+        x.close()

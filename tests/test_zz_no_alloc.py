@@ -23,6 +23,7 @@ from molsim_gb300 import Engine, abi, configs, units
 pytestmark = pytest.mark.gpu
 
 MG_ERR_ARG = {name: code for code, name in abi.STATUS.items()}["MG_ERR_ARG"]
+MAX_NCUT = 24   # MG_NOALLOC_MAX_NCUT
 
 
 class _EwaldOff:
@@ -42,8 +43,9 @@ class _EwaldOff:
         return getattr(self._s, name)
 
 
-def _system():
-    s = configs.small_system(seed=16, ewald=abi.MG_EWALD_STD, ncut=6)
+def _system(ncut=6, cube=0):
+    s = configs.small_system(seed=16, ewald=abi.MG_EWALD_STD, ncut=ncut)
+    s.ncutregion_cube = cube
     s.build_table()
     return s
 
@@ -70,9 +72,12 @@ def _call(lib, s, d_ro, d_az, d_force, d_uout, ncut=None):
     return st, err.value.decode()
 
 
-def test_noalloc_matches_utotal_twice(gpu_lib):
+# (ncut, ncutregion_cube): the spherical region; the largest ncut, which
+# uses every slot of the fixed array; the cube region (|n|^2 <= 3 ncut^2)
+@pytest.mark.parametrize("ncut,cube", [(6, 0), (MAX_NCUT, 0), (4, 1)], ids=["sphere6", "sphere_max", "cube4"])
+def test_noalloc_matches_utotal_twice(ncut, cube, gpu_lib):
     torch = pytest.importorskip("torch")
-    s = _system()
+    s = _system(ncut, cube)
     on = _utotal(s)
     off = _utotal(_EwaldOff(s))
     f_rec = (on["forceo"] - off["forceo"]).reshape(-1) / units.FORCE_FAC
@@ -109,7 +114,7 @@ def test_noalloc_rejects_ncut_beyond_scratch(gpu_lib):
     d_az = torch.from_numpy(np.ascontiguousarray(s.az)).to(dev)
     d_force = torch.zeros(3 * s.np_, dtype=torch.float64, device=dev)
     d_uout = torch.zeros(2, dtype=torch.float64, device=dev)
-    st, msg = _call(gpu_lib, s, d_ro, d_az, d_force, d_uout, ncut=25)
+    st, msg = _call(gpu_lib, s, d_ro, d_az, d_force, d_uout, ncut=MAX_NCUT + 1)
     assert st == MG_ERR_ARG
-    assert "ncut = 25" in msg and "scratch" in msg
+    assert f"ncut = {MAX_NCUT + 1}" in msg and "scratch" in msg
     assert not d_force.any().item()
