@@ -41,7 +41,9 @@ def lj_shift_at(rc_over_sigma):
 
 
 class _Grid:
-    """Cell grid for overlap rejection during placement."""
+    """Cell grid for overlap rejection during placement: no two particles
+    closer than rmin, or, for particles added with a radius, than the sum of
+    their radii (rmin is then the largest such sum)."""
 
     def __init__(self, boxlen, rmin):
         self.L = np.asarray(boxlen, dtype=np.float64)
@@ -50,11 +52,12 @@ class _Grid:
         self.rmin2 = rmin * rmin
         self.cells = {}
         self.pos = []
+        self.rad = []
 
     def _cell(self, r):
         return tuple((np.floor((r + self.L / 2) / self.h).astype(int)) % self.n)
 
-    def ok(self, r, skip=-1):
+    def ok(self, r, skip=-1, rad=None):
         c = self._cell(r)
         rng = [range(-1, 2) if self.n[m] >= 3 else range(0, self.n[m]) for m in range(3)]
         for dx in rng[0]:
@@ -70,13 +73,15 @@ class _Grid:
                             continue
                         d = r - self.pos[j]
                         d -= self.L * np.round(d / self.L)
-                        if d @ d < self.rmin2:
+                        lim2 = self.rmin2 if rad is None or self.rad[j] is None else (rad + self.rad[j]) ** 2
+                        if d @ d < lim2:
                             return False
         return True
 
-    def add(self, r):
+    def add(self, r, rad=None):
         self.cells.setdefault(self._cell(r), []).append(len(self.pos))
         self.pos.append(r)
+        self.rad.append(rad)
 
 
 def _wrap(r, L):

@@ -11,7 +11,8 @@ and meaning:
   natpt (1: monoatomic), zat, sigat, epsat, radat, massat; chains nct, txct,
   ncct, npptct, txcopolymer ('block' or 'regular').
 - &nmlPotential (potential.F90:307-330, defaults :332-380): rcut,
-  relpermitt, txpot ('default' or '(1,6,12)' for every pair), lewald,
+  relpermitt, txpot ('(1,6,12)' for every pair, or 'default' for every pair
+  with only its Coulomb term: npot, ipot, ucoff are refused), lewald,
   txewaldrec ('std', 'spm'), iewaldopt (0: ualpha = ualphared/rcut; 1:
   the same, with ncut from the error estimate (std); 3: alpha from
   uewaldtol, RcutToAlpha, and ncut as for 1 (std)), ncut, ncutregion, lsurf,
@@ -147,13 +148,28 @@ def system_from_input(inp, cnf=None, seed=1, text=False):
     npart = int(nppt.sum())
 
     # potential
-    txpot = array(pot, "txpot", npt * (npt + 1) // 2, "default", dtype=object)
+    txpot = [_lower(t) for t in array(pot, "txpot", npt * (npt + 1) // 2, "default", dtype=object)]
     for t in txpot:
-        if _lower(t) not in ("default", "(1,6,12)"):
-            raise NotImplementedError(f"txpot = {t!r} (the path tabulates '(1,6,12)')")
+        if t not in ("default", "(1,6,12)"):
+            raise NotImplementedError(f"txpot = {t!r} (the path tabulates '(1,6,12)' and the Coulomb term)")
+    # txpot 'default' is PotDefault (potential.F90:1290-1330): the sum of
+    # ucoff(m)/r**ipot(m), whose 1/r term is the Coulomb term EpsiFourPi z z
+    # (potential.F90:533-571) -- no Lennard-Jones term.  Only the Coulomb
+    # term is read here: further terms are refused.
+    for name in ("npot", "ipot", "ucoff"):
+        v = pot.get(name)
+        if v is not None and any(x not in (0, 0.0) for x in list(v.values or []) +
+                                 [y for vv in v.items.values() for y in vv]):
+            raise NotImplementedError(f"{name} (terms of txpot = 'default' beyond the Coulomb term)")
+    if "default" in txpot and "(1,6,12)" in txpot:
+        raise NotImplementedError("txpot = 'default' for some pairs and '(1,6,12)' for others")
+    if txpot and txpot[0] == "default":
+        epsat = np.zeros(npt)   # Coulomb only
+        species = [Species(sp.name, sp.charge, sp.sigma, 0.0, mass=sp.mass, dcoeff=sp.dcoeff, radat=sp.radat)
+                   for sp in species]
     rcut = float(scalar(pot, "rcut", 0.0))
-    if rcut <= 0:
-        raise ValueError("rcut must be positive")
+    if rcut <= 0:   # potential.F90:418-422: half the box diagonal ('xyz')
+        rcut = float(np.sqrt(((0.5 * boxlen) ** 2).sum()))
     relpermitt = float(scalar(pot, "relpermitt", 1.0))
     lewald = bool(scalar(pot, "lewald", False))
     ewald = abi.MG_EWALD_NONE
@@ -252,7 +268,8 @@ def system_from_input(inp, cnf=None, seed=1, text=False):
         ro = c["ro"]
         boxlen = c["boxlen"] if (c["boxlen"] > 0).all() else boxlen
     else:
-        ro = _generate(boxlen, npart, chains, kw, radat, iptpn, seed)
+        ro, placed = _lattices(g("nmlSetConfiguration"), boxlen, nppt)
+        ro = _generate(boxlen, npart, chains, kw, radat, iptpn, seed, ro, placed)
 
     md = g("nmlMD")
     tstep = scalar(bd, "tstep") if mode == abi.MG_BD else scalar(md, "tstep") if mode == abi.MG_MD else None
@@ -300,23 +317,109 @@ def alpha_to_ncut(tol, q2sum, l, alpha, unit):
     return int(xnew + 1.0)
 
 
-def _generate(boxlen, npart, chains, kw, radat, iptpn, seed):
-    from .configs import _Grid, place_chain, place_uniform
-    rng = np.random.Generator(np.random.PCG64(seed))
-    rmin = max(2.0, 2.0 * float(radat.max()) if len(radat) else 2.0)
-    grid = _Grid(boxlen, rmin)
+# unit-cell lattice points of SetPC, SetBCC and SetFCC (coordinate.F90:905-976)
+_LATTICE_POINTS = {
+    "pclattice": [(0.0, 0.0, 0.0)],
+    "bcclattice": [(0.0, 0.0, 0.0), (0.5, 0.5, 0.5)],
+    "fcclattice": [(0.0, 0.0, 0.0), (0.0, 0.5, 0.5), (0.5, 0.0, 0.5), (0.5, 0.5, 0.0)],
+}
+
+
+def _pbc_position(x, boxlen):
+    """PBC for a position in a box (molaux.F90:104-118): one shift by
+    boxlen*anint(x/boxlen) where |x| > boxlen/2 (anint rounds half away from
+    zero)."""
+    for m in range(3):
+        if abs(x[m]) > 0.5 * boxlen[m]:
+            t = x[m] * (1.0 / boxlen[m])
+            x[m] = x[m] - boxlen[m] * float(np.copysign(np.floor(abs(t) + 0.5), t))
+    return x
+
+
+def _lattices(setconf, boxlen, nppt):
+    """Particle types placed on a lattice by SetLattice
+    (coordinate.F90:713-832) with the &nmlSetConfiguration variables
+    txsetconf, nucell, rclow, rcupp, roshift (defaults coordinate.F90:449-510:
+    the whole box, no shift).  Returns positions (rows of the other types
+    zero) and a mask of the placed particles."""
+    npt = len(nppt)
+    npart = int(nppt.sum())
     ro = np.zeros((npart, 3))
-    done = np.zeros(npart, dtype=bool)
+    placed = np.zeros(npart, dtype=bool)
+    if not setconf:
+        return ro, placed
+    half = 0.5 * boxlen
+    txsetconf = array(setconf, "txsetconf", npt, "", dtype=object)
+    nucell = array(setconf, "nucell", (3, npt), 0, dtype=int)
+    # unassigned elements keep the box defaults (lbcbox)
+    rclow = array(setconf, "rclow", (3, npt), np.nan)
+    rcupp = array(setconf, "rcupp", (3, npt), np.nan)
+    for m in range(3):
+        rclow[m, np.isnan(rclow[m])] = -half[m]
+        rcupp[m, np.isnan(rcupp[m])] = +half[m]
+    roshift = array(setconf, "roshift", (3, npt), 0.0)
+    ddelta = 1.0e-10
+    for ipt in range(npt):
+        kind = _lower(txsetconf[ipt])
+        if kind not in _LATTICE_POINTS:
+            continue
+        ipnpt = int(nppt[:ipt].sum())
+        rlen = (rcupp[:, ipt] - rclow[:, ipt]) / nucell[:, ipt]
+        rorigin = 0.5 * (rclow[:, ipt] + rcupp[:, ipt])
+        nset = 0
+        for rol in _LATTICE_POINTS[kind]:
+            for iz in range(int(nucell[2, ipt])):
+                for iy in range(int(nucell[1, ipt])):
+                    for ix in range(int(nucell[0, ipt])):
+                        if nset == nppt[ipt]:
+                            break
+                        idx = (ix, iy, iz)
+                        x = np.empty(3)
+                        for m in range(3):
+                            u = (float(idx[m]) - 0.5 * float(nucell[m, ipt])) + (rol[m] + roshift[m, ipt])
+                            x[m] = (rorigin[m] + ddelta) + u * rlen[m]
+                        ro[ipnpt + nset] = _pbc_position(x, boxlen)
+                        placed[ipnpt + nset] = True
+                        nset += 1
+        if nset < nppt[ipt]:   # SetLattice: 'lattice set failed'
+            raise ValueError(f"{kind} of particle type {ipt + 1} holds {nset} of {nppt[ipt]} particles")
+    return ro, placed
+
+
+def _generate(boxlen, npart, chains, kw, radat, iptpn, seed, ro=None, placed=None):
+    """Positions of the particles not placed on a lattice: chains as random
+    walks at the bond length, then the other particles uniform, no two
+    closer than the sum of their radii radat (at least 1 A each, so that no
+    pair comes near r2umin)."""
+    from .configs import _Grid, place_chain
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rad = np.maximum(np.asarray(radat, dtype=float), 1.0)[iptpn - 1]
+    grid = _Grid(boxlen, 2.0 * float(rad.max()))
+    ro = np.zeros((npart, 3)) if ro is None else ro
+    done = np.zeros(npart, dtype=bool) if placed is None else placed.copy()
+    for i in np.nonzero(done)[0]:
+        grid.add(ro[i], rad[i])
     bond_eq = {}
     if "bond_ip" in kw:
         for i, e in zip(kw["bond_ip"], kw["bond_eq"]):
             bond_eq[int(i)] = float(e)
     for _ict, segs in chains:
-        b = bond_eq.get(segs[0], 0.0) or max(rmin, 1.0) * 1.2
-        for s, r in zip(segs, place_chain(rng, grid, len(segs), max(b, rmin * 1.01))):
+        rmin = 2.0 * float(rad[np.asarray(segs) - 1].max())
+        b = bond_eq.get(segs[0], 0.0) or rmin * 1.2
+        sub = _Grid(boxlen, rmin)
+        for i in np.nonzero(done)[0]:
+            sub.add(ro[i])
+        for s, r in zip(segs, place_chain(rng, sub, len(segs), max(b, rmin * 1.01))):
             ro[s - 1] = r
             done[s - 1] = True
-    rest = np.nonzero(~done)[0]
-    for i, r in zip(rest, place_uniform(rng, grid, len(rest))):
-        ro[i] = r
+            grid.add(r, rad[s - 1])
+    for i in np.nonzero(~done)[0]:
+        for _t in range(100000):
+            r = (rng.random(3) - 0.5) * grid.L
+            if grid.ok(r, rad=rad[i]):
+                grid.add(r, rad[i])
+                ro[i] = r
+                break
+        else:
+            raise RuntimeError("could not place particle without overlap")
     return ro

@@ -88,6 +88,40 @@ class System:
     r2umin: Optional[np.ndarray] = None
     nugrid: Optional[np.ndarray] = None
 
+    # ---- plain-data form (JSON) ------------------------------------------
+    _TABLE_FIELDS = ("ubuf", "iubuflow", "r2umin", "nugrid")
+
+    def to_dict(self):
+        """The system as plain data (lists, numbers, strings) for JSON; the
+        two-body table is left out (build_table makes it again)."""
+        import dataclasses
+        out = {}
+        for f in dataclasses.fields(self):
+            if f.name in self._TABLE_FIELDS:
+                continue
+            v = getattr(self, f.name)
+            if f.name == "species":
+                out[f.name] = [dataclasses.asdict(sp) for sp in v]
+            elif isinstance(v, np.ndarray):
+                out[f.name] = {"dtype": str(v.dtype), "shape": list(v.shape), "data": v.reshape(-1).tolist()}
+            elif isinstance(v, (np.integer, np.floating)):
+                out[f.name] = v.item()
+            else:
+                out[f.name] = v
+        return out
+
+    @classmethod
+    def from_dict(cls, d):
+        kw = {}
+        for k, v in d.items():
+            if k == "species":
+                kw[k] = [Species(**sp) for sp in v]
+            elif isinstance(v, dict) and "dtype" in v:
+                kw[k] = np.asarray(v["data"], dtype=v["dtype"]).reshape(v["shape"])
+            else:
+                kw[k] = v
+        return cls(**kw)
+
     # ---- derived quantities -------------------------------------------
     @property
     def np_(self):

@@ -3,8 +3,11 @@ configuration file (<project>.cnf, IOCnf's unformatted records), read into a
 System that the oracle and the GPU library run.
 
 The inputs below are written for these tests in the reference's format
-(&nmlSystem ... / groups with its variable names and defaults).
+(&nmlSystem ... / groups with its variable names and defaults); the last
+test checks the fixture made from the reference's own Testin inputs.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -172,3 +175,19 @@ def test_ewald_parameter_options():
     run3 = system_from_input(_input(ewald="std").replace("iewaldopt = 0", "iewaldopt = 3, uewaldtol = 1e-4"),
                              text=True)
     assert 0.1 < run3.system.ualpha * 12.0 < 10.0 and run3.system.ncut > 0
+
+
+def test_reference_input_fixture_is_current():
+    """The committed fixture tests/golden/reference_inputs.json is what the
+    reference's own input files give today (skipped where the files are
+    not present)."""
+    import json
+    from tests.golden import make_reference_inputs as mk
+    if not os.path.isdir(mk.TESTIN):
+        pytest.skip("the reference's Testin inputs are not present")
+    with open(mk.OUT) as fh:
+        stored = json.load(fh)
+    fresh = json.loads(json.dumps(mk.make()))
+    assert [e["input"] for e in stored] == [e["input"] for e in fresh]
+    for a, b in zip(stored, fresh):
+        assert a == b, a["input"]
