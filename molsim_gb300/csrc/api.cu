@@ -119,7 +119,8 @@ static void free_all(mg_handle *h) {
                     h->d_scan_tmp, h->d_zlow, h->d_coef, h->d_coef_f, h->d_bin_z0, h->d_bin_inv,
                     h->d_bin_kstart, h->d_brick_count, h->d_brick_perm, h->d_brick_rank,
                     h->d_brick_of, h->d_brick_start, h->d_brick_istart, h->d_item_brick, h->d_tiles, h->d_grad, h->d_f32_tabs, h->d_pos_f,
-                    h->d_cell_s, h->d_spl_w, h->d_ffx2, h->d_force2, h->d_ro_slot, h->d_ro_slot_f, h->d_scan_tiles};
+                    h->d_cell_s, h->d_spl_w, h->d_ffx2, h->d_force2, h->d_ro_slot, h->d_ro_slot_f, h->d_scan_tiles,
+                    h->d_spl_plane};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);

@@ -153,6 +153,12 @@ struct mg_handle {
     void *d_tw = nullptr;           // twiddles exp(-2 pi i m/n), m < n
     int fft_tx = 0, fft_tiles = 0;
     int fft_plane = 0, fft_warps = 0;   // mixed form, 32 <= nmesh <= 128: three plane/slab passes
+    // mixed form with plane passes, MD/BD: the spread runs inside the forward
+    // plane pass (particles sorted by the z plane of their stamp corner), so
+    // the charge mesh never leaves shared memory
+    int plane_fused = 0;
+    int plane_shift = 30;           // fused spread: stamp values to integers (2^plane_shift)
+    float *d_spl_plane = nullptr;   // fused spread: the spread records in plane order
     int brick = 0, nbrick_edge = 0, nbricks = 0;
     size_t spread_smem = 0, gather_smem = 0;
     int fx_shift = 30, fx_shift64 = 48;

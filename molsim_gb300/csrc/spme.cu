@@ -332,6 +332,7 @@ struct SplineArgs {
     // brick sort, first pass: brick of each particle and its rank among the
     // brick's particles (log2 of the brick edge and of the bricks per edge)
     int lB, lnb;
+    int plane;             // sort by the z plane of the stamp corner instead of by brick
     int *count, *rank, *brick;
     int assign;            // gather: the first writer of the force accumulator
     // gather, forked UTotal without a surface term: forceo = (mesh force +
@@ -345,12 +346,18 @@ struct SplineArgs {
 
 // The spline record of a particle: a head of four values (the stamp's
 // upper corner, 10 bits per axis, stored in the bits of the first value;
-// the charge; two unused), the B-spline values along x, y, z, then their
-// derivatives (order values each), padded to a multiple of four values so
-// that records start on 16-byte boundaries.  The spread and the gather read
-// a particle's corner, charge and weights from a few consecutive sectors.
+// the charge; two unused), then order values each of the B-spline values
+// along x and y, their derivatives along x and y, the values along z and
+// the derivatives along z, padded to a multiple of four values so that
+// records start on 16-byte boundaries.  The spreads read the head and the x
+// and y values as one block (plus the z values), the gather the head, the
+// x and y values and derivatives (plus the z pair of each plane).
 constexpr int kRecHead = 4;
 __host__ __device__ constexpr int spl_rec(int order) { return (kRecHead + 6 * order + 3) & ~3; }
+template <int ORDER> struct RecIx {
+    static constexpr int VX = kRecHead, VY = kRecHead + ORDER, DX = kRecHead + 2 * ORDER,
+                         DY = kRecHead + 3 * ORDER, VZ = kRecHead + 4 * ORDER, DZ = kRecHead + 5 * ORDER;
+};
 
 template <typename T> __device__ __forceinline__ T rec_put_corner(int c);
 template <> __device__ __forceinline__ float rec_put_corner<float>(int c) { return __int_as_float(c); }
@@ -420,8 +427,8 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
         bspline_o<T, ORDER>((T)(pos - fl), v, d);
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            r[kRecHead + m * ORDER + i] = v[i];
-            r[kRecHead + 3 * ORDER + m * ORDER + i] = d[i];
+            r[(m < 2 ? kRecHead + m * ORDER : RecIx<ORDER>::VZ) + i] = v[i];
+            r[(m < 2 ? RecIx<ORDER>::DX + m * ORDER : RecIx<ORDER>::DZ) + i] = d[i];
         }
     }
     r[0] = rec_put_corner<T>(c[0] | (c[1] << 10) | (c[2] << 20));
@@ -440,6 +447,23 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
         for (int k = lane; k < nv * S / 4; k += 32) dst[k] = sw[k];
     } else if (valid) {
         store_rec<T, S>(w + (size_t)p * S, r);
+    }
+    if (a.plane) {
+        // sort by the corner's z plane (at most 128 planes): the block's
+        // counts in shared memory, one global atomic per plane and block
+        __shared__ int hcnt[128], hbase[128];
+        for (int k = threadIdx.x; k < a.n; k += blockDim.x) hcnt[k] = 0;
+        __syncthreads();
+        int lr = valid ? atomicAdd(&hcnt[c[2]], 1) : 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < a.n; k += blockDim.x)
+            if (hcnt[k]) hbase[k] = atomicAdd(&a.count[k], hcnt[k]);
+        __syncthreads();
+        if (valid) {
+            a.brick[p] = c[2];
+            a.rank[p] = hbase[c[2]] + lr;
+        }
+        return;
     }
     int id = ((((c[2] >> a.lB) << a.lnb) + (c[1] >> a.lB)) << a.lnb) + (c[0] >> a.lB);
     unsigned vm = __ballot_sync(0xffffffffu, valid);
@@ -533,6 +557,32 @@ __global__ void k_brick_scatter(int np, BrickArgs b) {
     if (p < np) b.perm[b.start[b.brick[p]] + b.rank[p]] = p;
 }
 
+// The spread record of a particle in plane order: the head (corner,
+// charge), then the x, y and z B-spline values, padded to a multiple of four
+template <int ORDER> __host__ __device__ constexpr int spread_rec() { return (kRecHead + 3 * ORDER + 3) & ~3; }
+
+// plane sort, second pass: each particle's spread record to its place in
+// the plane order
+template <int ORDER>
+__global__ void k_plane_scatter(int np, BrickArgs b, const float *__restrict__ w, float *__restrict__ ws) {
+    mg_pdl_begin();
+    typedef RecIx<ORDER> RI;
+    constexpr int SR = spread_rec<ORDER>();
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int dst = b.start[b.brick[p]] + b.rank[p];
+    const float *src = w + (size_t)p * spl_rec(ORDER);
+    float hv[kRecHead + 2 * ORDER], r[SR];
+    load_rec<float, kRecHead + 2 * ORDER>(src, hv);   // head, x and y values
+#pragma unroll
+    for (int i = 0; i < kRecHead + 2 * ORDER; ++i) r[i] = hv[i];
+#pragma unroll
+    for (int i = 0; i < ORDER; ++i) r[kRecHead + 2 * ORDER + i] = src[RI::VZ + i];
+#pragma unroll
+    for (int i = kRecHead + 3 * ORDER; i < SR; ++i) r[i] = 0.f;
+    store_rec<float, SR>(ws + (size_t)dst * SR, r);
+}
+
 constexpr int kSpreadWarps = 8;   // most work items (warps) per block
 constexpr int kSpreadItem = 32;   // most particles per spread work item
 
@@ -587,8 +637,9 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
         __syncwarp();
         if (lane < cnt) {   // stage one particle per lane
             int p = b.perm[q0 + lane];
-            T r[kRecHead + 3 * ORDER];
-            load_rec<T, kRecHead + 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
+            const T *src = w + (size_t)p * spl_rec(ORDER);
+            T r[kRecHead + 2 * ORDER];
+            load_rec<T, kRecHead + 2 * ORDER>(src, r);
             int c = rec_corner(r[0]);
             int cx = (c & 1023) - ox, cy = ((c >> 10) & 1023) - oy, cz = (c >> 20) - oz;
             stg->off[lane] = cx | (cy << 8) | (cz << 16);
@@ -596,9 +647,9 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
             T *rec = stg->w[lane];
 #pragma unroll
             for (int i = 0; i < ORDER; ++i) {
-                rec[i] = qp * r[kRecHead + i];
-                rec[ORDER + i] = r[kRecHead + ORDER + i];
-                rec[2 * ORDER + i] = r[kRecHead + 2 * ORDER + i];
+                rec[i] = qp * r[RecIx<ORDER>::VX + i];
+                rec[ORDER + i] = r[RecIx<ORDER>::VY + i];
+                rec[2 * ORDER + i] = src[RecIx<ORDER>::VZ + i];
             }
         }
         __syncwarp();
@@ -678,17 +729,18 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, 
     int base = 0;
     if (act) {
         int p = b.perm[q];
-        float r[kRecHead + 3 * ORDER];
-        load_rec<float, kRecHead + 3 * ORDER>(w + (size_t)p * spl_rec(ORDER), r);
+        const float *src = w + (size_t)p * spl_rec(ORDER);
+        float r[kRecHead + 2 * ORDER];
+        load_rec<float, kRecHead + 2 * ORDER>(src, r);
         int c = rec_corner(r[0]);
         int cx = (c & 1023) - ox, cy = ((c >> 10) & 1023) - oy, cz = (c >> 20) - oz;
         base = (cz * t + cy) * t + cx;
         float qs = r[1] * b.fx_scale;
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            wx[i] = qs * r[kRecHead + i];
-            wy[i] = r[kRecHead + ORDER + i];
-            wz[i] = r[kRecHead + 2 * ORDER + i];
+            wx[i] = qs * r[RecIx<ORDER>::VX + i];
+            wy[i] = r[RecIx<ORDER>::VY + i];
+            wz[i] = src[RecIx<ORDER>::VZ + i];
         }
     }
     __syncwarp();
@@ -746,23 +798,23 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     int p = valid ? perm[g] : 0;
     int n = a.n, mn = n - 1;
     T e0 = 0, e1 = 0, e2 = 0;
-    const T *rec = w + (size_t)p * spl_rec(ORDER);   // head, values x, y, z, derivatives x, y, z
-    const T *rv = rec + kRecHead, *rd = rv + 3 * ORDER;
+    const T *rec = w + (size_t)p * spl_rec(ORDER);
+    typedef RecIx<ORDER> RI;
     if (act) {
         T vy[ORDER], dy[ORDER];
 #pragma unroll
         for (int i = 0; i < ORDER; ++i) {
-            vy[i] = rv[ORDER + i];
-            dy[i] = rd[ORDER + i];
+            vy[i] = rec[RI::VY + i];
+            dy[i] = rec[RI::DY + i];
         }
-        T vx = rv[j], dx = rd[j];
+        T vx = rec[RI::VX + j], dx = rec[RI::DX + j];
         int c = rec_corner(rec[0]);
         int c0 = c & 1023, c1 = (c >> 10) & 1023, c2 = c >> 20;
         const T *col = Q + ((c0 - j) & mn);
         T A = 0, B = 0, C = 0;
 #pragma unroll
         for (int iz = 0; iz < ORDER; ++iz) {
-            T vz = rv[2 * ORDER + iz], dz = rd[2 * ORDER + iz];
+            T vz = rec[RI::VZ + iz], dz = rec[RI::DZ + iz];
             const T *pl = col + ((size_t)((c2 - iz) & mn) << (2 * a.n_log));
             T r0 = 0, r1 = 0;
 #pragma unroll
@@ -1288,6 +1340,175 @@ __global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F,
     }
 }
 
+// ---- fused spread and forward plane pass ---------------------------------------
+// Particles are counting-sorted by the z plane c2 of their stamp corner
+// (start[c2] .. start[c2+1]), their spread records copied into that order.
+// Stamp point iz of a particle lies on plane (c2 - iz) mod n, so the
+// particles reaching plane z are those with c2 = z + iz (mod n), iz < ORDER:
+// ORDER ranges of the plane order, the plane's window.  One CTA per plane
+// spreads its window's (particle, plane) items into the plane in shared
+// memory and transforms it: the charge mesh never goes to global memory.
+struct PlaneArgs {
+    const int *start;
+    const float *srec;         // spread records in plane order (spread_rec values each)
+    float scale;               // stamp values to integers: 2^plane_shift
+    float inv_hi, inv_lo;      // 2^(15 - plane_shift), 2^-plane_shift
+    int *err;
+};
+
+// the window of plane z in shared memory: ws[iz] = items before range iz,
+// wb[iz] = its first index into the plane order; ws[ORDER] = the item count
+template <int ORDER>
+__device__ __forceinline__ void plane_window(const PlaneArgs &a, int z, int n, int *wb, int *ws) {
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int iz = 0; iz < ORDER; ++iz) {
+            int c2 = (z + iz) & (n - 1);
+            wb[iz] = a.start[c2];
+            ws[iz] = acc;
+            acc += a.start[c2 + 1] - a.start[c2];
+        }
+        ws[ORDER] = acc;
+    }
+}
+
+template <int ORDER> __device__ __forceinline__ int window_iz(const int *ws, int t) {
+    int iz = 0;
+#pragma unroll
+    for (int k = 1; k < ORDER; ++k) iz += (t >= ws[k]) ? 1 : 0;
+    return iz;
+}
+
+// Spread of the plane's window into the plane, then x r2c + forward y FFT
+// as k_plane_fwd.  One lane per item; rows are padded to n + 1 points so
+// that the lanes' stamp rows spread over the banks.  Stamp values
+// v = round(q Mx My Mz 2^s), |v| < 2^30, are added as two 32-bit integer
+// parts, hi = v >> 15 (signed) and lo = v & (2^15 - 1) (unsigned), each with
+// a shared-memory atomic: both sums stay exact for up to 2^16 items per
+// point, and a window of more items is reported (MG_ERR_UNSUPPORTED).
+// Integer sums do not depend on the order of the adds, so the plane is
+// bit-reproducible.  The two integer planes share memory with the FFT's
+// plane and line buffers, which are used only after every line has been
+// read into registers.
+template <int P, int ORDER>
+__global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *__restrict__ F,
+                                                           const float2 *__restrict__ tw, FastDiv fnh) {
+    mg_pdl_begin();
+    typedef float2 V;
+    typedef float T;
+    constexpr int n = 32 * P, nh = n / 2 + 1, RS = n + 1, n2 = n * RS;
+    constexpr int SR = spread_rec<ORDER>();
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ int wb[ORDER], ws[ORDER + 1];
+    V *s_tw = reinterpret_cast<V *>(smem_raw), *s_tl = s_tw + n, *s_tk = s_tl + 32;
+    V *S = s_tw + plane_tw_entries<P>();
+    int *thi = reinterpret_cast<int *>(S);
+    unsigned *tlo = reinterpret_cast<unsigned *>(thi + n2);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    V *Zs = S + n * nh + w * (n + n / 16);
+    load_tw<T>(s_tw, tw, n);
+    load_lane_tw<T, P>(s_tl, s_tk, tw);
+    for (int k = threadIdx.x; k < n2; k += blockDim.x) {
+        thi[k] = 0;
+        tlo[k] = 0u;
+    }
+    const int z = blockIdx.x;
+    plane_window<ORDER>(a, z, n, wb, ws);
+    __syncthreads();
+    const int total = ws[ORDER];
+    if (total >= 65536) {   // the integer parts could overflow: report, spread nothing
+        if (threadIdx.x == 0) mg_dev_error(a.err, MG_ERR_UNSUPPORTED, z, total, 65535);
+    } else {
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            int iz = window_iz<ORDER>(ws, t);
+            const float *rec = a.srec + (size_t)(wb[iz] + t - ws[iz]) * SR;
+            float r[kRecHead + 2 * ORDER];
+            load_rec<float, kRecHead + 2 * ORDER>(rec, r);
+            float qz = r[1] * rec[kRecHead + 2 * ORDER + iz] * a.scale;
+            int c = rec_corner(r[0]);
+            int c0 = c & 1023, c1 = (c >> 10) & 1023;
+#pragma unroll
+            for (int iy = 0; iy < ORDER; ++iy) {
+                float wyz = r[kRecHead + ORDER + iy] * qz;
+                int row = ((c1 - iy) & (n - 1)) * RS;
+#pragma unroll
+                for (int ix = 0; ix < ORDER; ++ix) {
+                    int v = __float2int_rn(r[kRecHead + ix] * wyz);
+                    int k = row + ((c0 - ix) & (n - 1));
+                    atomicAdd(&thi[k], v >> 15);
+                    atomicAdd(&tlo[k], (unsigned)(v & 0x7fff));
+                }
+            }
+        }
+    }
+    __syncthreads();
+    constexpr int MP = (P + 1) / 2;   // line pairs per warp at 32 warps
+    T val[MP][2 * P];
+#pragma unroll
+    for (int r = 0; r < MP; ++r) {
+        int pr = w + 32 * r;
+        if (pr < n / 2) {
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                int ka = (2 * pr) * RS + lane + 32 * j, kb = ka + RS;
+                val[r][2 * j] = (float)thi[ka] * a.inv_hi + (float)tlo[ka] * a.inv_lo;
+                val[r][2 * j + 1] = (float)thi[kb] * a.inv_hi + (float)tlo[kb] * a.inv_lo;
+            }
+        }
+    }
+    __syncthreads();   // the integer planes are dead: S and Zs take their place
+    const int bl = brev5(lane);
+#pragma unroll
+    for (int r = 0; r < MP; ++r) {
+        int pr = w + 32 * r;
+        if (pr >= n / 2) break;
+        V v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            v[j].x = val[r][2 * j];
+            v[j].y = val[r][2 * j + 1];
+        }
+        warp_fft_fwd<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) Zs[zsk(k1 + P * bl)] = v[k1];
+        __syncwarp();
+        V *Sa = S + (2 * pr) * nh, *Sb = Sa + nh;
+        for (int k = lane; k < nh; k += 32) {
+            V zk = Zs[zsk(k)], zc = Zs[zsk((n - k) & (n - 1))];
+            V aa, bb;
+            aa.x = (T)0.5 * (zk.x + zc.x);
+            aa.y = (T)0.5 * (zk.y - zc.y);
+            bb.x = (T)0.5 * (zk.y + zc.y);
+            bb.y = (T)-0.5 * (zk.x - zc.x);
+            Sa[k] = aa;
+            Sb[k] = bb;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int c = w; c < nh; c += nw) {   // forward y FFT of column kx = c
+        V v[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) v[j] = S[(lane + 32 * j) * nh + c];
+        warp_fft_fwd<T, P>(v, s_tw, s_tl, s_tk, lane);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) S[(32 * k1 + lane) * nh + c] = v[k1];
+    }
+    __syncthreads();
+    V *Fp = F + (size_t)z * n * nh;
+    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
+        int ky = (int)fdiv((unsigned)e, fnh), kx = e - ky * nh;
+        Fp[e] = S[perm_row<P>(ky) * nh + kx];
+    }
+}
+
+template <int P> static size_t fused_fwd_smem() {
+    const int n = 32 * P, nh = n / 2 + 1;
+    size_t fft = sizeof(float2) * ((size_t)n * nh + (size_t)32 * (n + n / 16));
+    size_t tiles = 2 * sizeof(int) * (size_t)n * (n + 1);
+    return sizeof(float2) * (size_t)plane_tw_entries<P>() + std::max(fft, tiles);
+}
+
 template <int P> static size_t plane_smem(int warps) {
     const int n = 32 * P, nh = n / 2 + 1;
     return sizeof(float2) * ((size_t)plane_tw_entries<P>() + (size_t)n * nh + (size_t)warps * (n + n / 16));
@@ -1325,10 +1546,55 @@ static int plane_dispatch(mg_handle *h, float *Q, float2 *F, const float2 *tw, C
     }
 }
 
+// the plane passes with the spread fused into the forward one: spread +
+// x/y forward per plane, the z pass with the influence function per ky
+// slab, y/x inverse per plane (the potential mesh, for the gather)
+template <int P, int ORDER> static int fused_passes_o(mg_handle *h, const PlaneArgs &pa) {
+    const int n = 32 * P, thr = 32 * h->fft_warps;
+    float2 *F = (float2 *)h->d_F;
+    const float2 *tw = (const float2 *)h->d_tw;
+    FastDiv fnh = make_fastdiv((unsigned)h->nh);
+    ConvArgs cv;
+    cv.part = h->d_part + h->part_rec;
+    cv.mf = h->d_mf_f;
+    cv.ew = h->d_ew_f;
+    cv.vw = h->d_vw_f;
+    MG_TRY(mg_phase_begin(h, "spread+fft_xy"));
+    mg_launch_pdl(k_plane_spread_fwd<P, ORDER>, n, thr, fused_fwd_smem<P>(), h->st, pa, F, tw, fnh);
+    MG_TRY(mg_phase_end(h, "spread+fft_xy"));
+    MG_TRY(mg_phase_begin(h, "fft_z_conv"));
+    mg_launch_pdl(k_slab_conv<float, P>, n, thr, slab_smem<P>(), h->st, F, tw, cv, fnh);
+    if (h->par_forces) MG_CUDA(h, cudaEventRecord(h->ev_rec, h->st));   // reciprocal partials complete
+    MG_TRY(mg_phase_end(h, "fft_z_conv"));
+    MG_TRY(mg_phase_begin(h, "fft_yx_inv"));
+    mg_launch_pdl(k_plane_inv<float, P>, n, thr, plane_smem<P>(h->fft_warps), h->st, (const float2 *)F,
+                  (float *)h->d_Q, tw, fnh);
+    MG_TRY(mg_phase_end(h, "fft_yx_inv"));
+    h->launches += 3;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
+template <int P> static int fused_passes(mg_handle *h, const PlaneArgs &pa) {
+    switch (h->order) {
+    case 4: return fused_passes_o<P, 4>(h, pa);
+    case 5: return fused_passes_o<P, 5>(h, pa);
+    case 6: return fused_passes_o<P, 6>(h, pa);
+    case 7: return fused_passes_o<P, 7>(h, pa);
+    case 8: return fused_passes_o<P, 8>(h, pa);
+    default: return mg_fail(h, MG_ERR_UNSUPPORTED, "fused plane passes for order %d", h->order);
+    }
+}
+
 template <int P> static void set_plane_limits() {
     cudaFuncSetAttribute(k_plane_fwd<float, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_slab_conv<float, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_plane_inv<float, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_plane_spread_fwd<P, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_plane_spread_fwd<P, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_plane_spread_fwd<P, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_plane_spread_fwd<P, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_plane_spread_fwd<P, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 template <typename T>
@@ -1406,6 +1672,9 @@ int mg_spme_init(mg_handle *h) {
         h->fft_warps = 32;
         h->nblk_rec = n;
     }
+    // the spread fused into the forward plane pass: MD and BD (MC keeps the
+    // charge mesh of the accepted state), orders up to 8
+    h->plane_fused = (h->fft_plane && h->mode != MG_MC && h->order >= 4 && h->order <= 8) ? 1 : 0;
     // bricks of 8^3 points (16^3 for orders above 9, whose halo would
     // otherwise reach beyond the next brick)
     if (h->order < 4) return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d (supported: 4..12)", h->order);
@@ -1458,6 +1727,8 @@ int mg_spme_init(mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_Qfx, sizeof(long long) * (size_t)n * n * n));
     MG_CUDA(h, cudaMemset(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n));
     MG_CUDA(h, cudaMalloc(&h->d_spl_w, tsz * spl_rec(h->order) * (size_t)h->np));   // spline records
+    if (h->plane_fused)   // spread records in plane order (at most order 8)
+        MG_CUDA(h, cudaMalloc(&h->d_spl_plane, sizeof(float) * spread_rec<8>() * (size_t)h->np));
     spread_attrs<float, int>();
     spread_attrs<double, long long>();
     spread_lane_attr<4>(); spread_lane_attr<5>(); spread_lane_attr<6>(); spread_lane_attr<7>(); spread_lane_attr<8>();
@@ -1481,6 +1752,12 @@ int mg_spme_init(mg_handle *h) {
     int k = 30;
     while (k > 4 && std::ldexp(bound, k) >= 2147483648.0 * 0.99) --k;
     h->fx_shift = k;
+    // fused spread: one stamp value, at most max|q| (max B-spline value)^3,
+    // stays below 2^30
+    double bound1 = qmax * mmax * mmax * mmax * 1.01;
+    int kp = 30;
+    while (kp > 4 && std::ldexp(bound1, kp) >= 1073741824.0 * 0.99) --kp;
+    h->plane_shift = kp;
     // FP64 form: the whole mesh sums in 64 bits; no point can hold more than
     // np * max|q| * (max B-spline value)^3
     double bound64 = (double)h->np * qmax * mmax * mmax * mmax * 1.01;
@@ -1649,6 +1926,7 @@ static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
     for (int m = 0; m < 3; ++m) sa.dkdr[m] = h->dkdr[m];
     sa.lB = ilog2(h->brick);
     sa.lnb = ilog2(h->nbrick_edge);
+    sa.plane = 0;
     sa.count = h->d_brick_count;
     sa.rank = h->d_brick_rank;
     sa.brick = h->d_brick_of;
@@ -1789,12 +2067,59 @@ int mg_spme_box_grad(mg_handle *h, double *out3, double *scratch) {
     return box_grad_t<double>(h, out3, scratch, 304);
 }
 
+// UTotal's mesh part with the spread fused into the forward plane pass:
+// splines and the plane sort, spread + forward, z + influence function,
+// inverse, gather.
+static int spme_fused(mg_handle *h, SplineArgs sa, BrickArgs bk) {
+    int np = h->np, n = h->nmesh, tb = 256, gb = (np + tb - 1) / tb;
+    sa.plane = 1;
+    bk.nbricks = n;          // one bucket per z plane
+    bk.M = 1 << 30;          // one (unused) work item per bucket
+    MG_TRY(mg_phase_begin(h, "splines"));
+    MG_TRY((mesh_kernel<float, int>(h, 0, sa, bk)));
+    MG_TRY(mg_phase_end(h, "splines"));
+    MG_TRY(mg_phase_begin(h, "plane_sort"));
+    mg_launch_pdl(k_brick_prefix, 1, 1024, 0, h->st, bk);
+    const float *w = (const float *)h->d_spl_w;
+    switch (h->order) {
+    case 4: mg_launch_pdl(k_plane_scatter<4>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
+    case 5: mg_launch_pdl(k_plane_scatter<5>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
+    case 6: mg_launch_pdl(k_plane_scatter<6>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
+    case 7: mg_launch_pdl(k_plane_scatter<7>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
+    default: mg_launch_pdl(k_plane_scatter<8>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
+    }
+    h->launches += 2;
+    MG_TRY(mg_phase_end(h, "plane_sort"));
+    PlaneArgs pa;
+    pa.start = h->d_brick_start;
+    pa.srec = h->d_spl_plane;
+    pa.scale = std::ldexp(1.0f, h->plane_shift);
+    pa.inv_hi = std::ldexp(1.0f, 15 - h->plane_shift);
+    pa.inv_lo = std::ldexp(1.0f, -h->plane_shift);
+    pa.err = h->d_err;
+    int st;
+    switch (n) {
+    case 32: st = fused_passes<1>(h, pa); break;
+    case 64: st = fused_passes<2>(h, pa); break;
+    case 128: st = fused_passes<4>(h, pa); break;
+    default: st = mg_fail(h, MG_ERR_UNSUPPORTED, "fused plane passes for nmesh = %d", n);
+    }
+    MG_TRY(st);
+    if (h->par_forces) MG_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_sr, 0));   // the short-range forces
+    MG_TRY(mg_phase_begin(h, "gather"));
+    MG_TRY((mesh_kernel<float, int>(h, 2, sa, bk)));
+    MG_TRY(mg_phase_end(h, "gather"));
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
 int mg_spme_launch(mg_handle *h) {
     int n = h->nmesh;
     size_t n3 = (size_t)n * n * n;
     SplineArgs sa;
     BrickArgs bk;
     spme_args(h, sa, bk);
+    if (h->plane_fused && !h->d_Qref) return spme_fused(h, sa, bk);
     bool mixed = h->form == MG_MIXED;
     MG_TRY(spme_spread(h, sa, bk));
     if (h->d_Qref) {   // MC: keep the charge mesh of the accepted state in FP64

@@ -28,6 +28,12 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+def _report(what):
+    """Each compile or link step that runs is reported on stderr, so that a
+    build log shows whether the library was compiled or found up to date."""
+    sys.stderr.write(f"[molsim_gb300 build] {what}\n")
+
+
 def _compile(src, verbose):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
@@ -38,6 +44,7 @@ def _compile(src, verbose):
            "-Xcompiler", "-ffp-contract=off", "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
+    _report(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
@@ -55,9 +62,11 @@ def build(verbose=False, force=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     if os.path.exists(LIB) and not force and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
+        _report(f"{LIB} up to date (objects newer than their sources)")
         build_harness()
         return LIB
     cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    _report(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
@@ -76,6 +85,7 @@ def build_harness():
     # (PBC, Metropolis) and must round as the Python and Fortran callers do
     cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I", os.path.join(HERE, "..", "include"), src,
            "-L", HERE, "-lmolsim_gb300", "-Wl,-rpath,$ORIGIN", "-o", exe]
+    _report(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"harness build failed:\n{r.stderr}")

@@ -5,6 +5,7 @@ baseline x86-64 gfortran -O2 build of the reference.
 """
 import os
 import subprocess
+import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle_molsim.so")
@@ -17,6 +18,7 @@ def build(force=False):
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-Wall", "-o", LIB, *SRCS, "-lm"]
+    sys.stderr.write("[oracle build] " + " ".join(cmd) + "\n")
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stderr)

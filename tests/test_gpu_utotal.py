@@ -38,6 +38,22 @@ def test_mixed_is_bit_reproducible(orc, gpu_lib):
     assert g1["u_tot"] == g2["u_tot"]
 
 
+@pytest.mark.parametrize("nmesh,order", [(32, 4), (64, 6), (128, 8)])
+def test_mixed_fused_planes_reproducible(nmesh, order, orc, gpu_lib):
+    """The mixed form's spread inside the forward plane FFT (particles sorted
+    by the z plane of their stamp corner, integer shared-memory atomics)
+    gives the same bits on every call, in MD and BD handles, and agrees with
+    the oracle."""
+    for mode in (abi.MG_MD, abi.MG_BD):
+        s = prepared(configs.small_system(seed=32, n=900, L=60.0, nmesh=nmesh, order=order, mode=mode,
+                                          chains=6, nseg=20), orc)
+        r, g1, _, gpu = run_pair(s, orc, form=abi.MG_MIXED)
+        g2 = gpu.UTotal()
+        assert np.array_equal(g1["forceo"], g2["forceo"]) and g1["u_tot"] == g2["u_tot"]
+        e = utotal_errors(g1, r, s.nptpt)
+        assert e["force_rms"] <= TOL_MIXED_RMS and e["u_tot"] <= 1e-5 and e["virial"] <= 1e-5, e
+
+
 def test_electrolyte_std_config(orc, gpu_lib):
     """The N=1000 standard-Ewald electrolyte (r_c = 30 A, |n| <= 8)."""
     s = prepared(configs.electrolyte_std(), orc)
