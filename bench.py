@@ -520,6 +520,126 @@ def run_water(args):
     return 0
 
 
+def run_replicas(args):
+    """The batched configuration (not the headline workload): nrep
+    independent electrolyte boxes, N log-uniform in [500, 8000], salt
+    uniform in [0.01, 1.0] M, charges +-1 e, LJ sigma = 4 A, eps = 0.1 kT;
+    SPME order 6 with the real-space cutoff and mesh chosen per box for a
+    force RMS error of 1e-5 (autotune.choose_spme).  Timed: K MD steps of
+    all boxes (mixed form, one CUDA graph launch per step over every box),
+    then 10^4 single-ion displacement trials (dtran = 2 A) per box through
+    the denergy path (mg_dutotal_batch, FP64).  Reported: aggregate box-steps
+    per second, trials per second, every box's mixed-form force RMS error
+    against its FP64 form, and the SPME error against a converged FP64
+    reference measured on a sample of boxes.  One JSON line, rank 0."""
+    import dataclasses
+
+    import torch
+
+    import molsim_gb300
+    from molsim_gb300 import Engine, abi, autotune, configs
+    from molsim_gb300.ensemble import Ensemble
+    torch.cuda.set_device(0)
+    molsim_gb300.build()
+    nrep = args.replicas
+    t = time.time()
+    rs = configs.replica_set(seed=args.seed, nrep=nrep, mode=abi.MG_MD)
+    conc, choice = [], []
+    for s in rs:
+        c = (s.np_ / 2) / (float(np.prod(s.boxlen)) * 1e-27 * configs.AVOGADRO)
+        ch = autotune.choose_spme(s, c, ns_per_point=args.mesh_ns)
+        s.rcut, s.ualpha, s.order, s.nmesh = ch["rcut"], ch["ualpha"], ch["order"], ch["nmesh"]
+        s.build_table()
+        conc.append(c)
+        choice.append(ch)
+    log(f"[bench] {nrep} replicas generated and tabulated in {time.time() - t:.1f}s "
+        f"({sum(s.np_ for s in rs)} ions)")
+
+    def engine(s, form, mode=abi.MG_MD):
+        e = Engine(dataclasses.replace(s, mode=mode), form=form)
+        e.SetPositions(s.ro_flat())
+        e.NList("write")
+        return e
+
+    # per box: the mixed form against the FP64 form of the same settings
+    err_mixed = []
+    for s in rs:
+        e64, emx = engine(s, abi.MG_FP64), engine(s, abi.MG_MIXED)
+        f64, fmx = e64.UTotal()["forceo"], emx.UTotal()["forceo"]
+        e64.close()
+        emx.close()
+        err_mixed.append(float(np.sqrt(((fmx - f64) ** 2).mean() / (f64 ** 2).mean())))
+    # the SPME setting against a converged FP64 reference (order 10, twice
+    # the mesh up to 256) on boxes spread over the concentrations
+    order_c = np.argsort(conc)
+    sample = sorted(set(int(order_c[int(i)]) for i in np.linspace(0, nrep - 1, min(8, nrep))))
+    err_spme = []
+    for i in sample:
+        s = rs[i]
+        ref = dataclasses.replace(s, order=10, nmesh=min(256, 2 * s.nmesh))
+        er, e0 = engine(ref, abi.MG_FP64), engine(s, abi.MG_FP64)
+        fr, f0 = er.UTotal()["forceo"], e0.UTotal()["forceo"]
+        er.close()
+        e0.close()
+        err_spme.append({"box": i, "N": s.np_, "c_M": round(conc[i], 4), "rcut": s.rcut, "nmesh": s.nmesh,
+                         "ref_nmesh": ref.nmesh,
+                         "force_rms": float(np.sqrt(((f0 - fr) ** 2).mean() / (fr ** 2).mean()))})
+
+    # MD: all boxes, one graph launch per step
+    engines = []
+    for i, s in enumerate(rs):
+        e = engine(s, abi.MG_MIXED)
+        e.MDSetup(0.002, s.maxwell_velocities(seed=1000 + i))
+        engines.append(e)
+    ens = Ensemble(engines)
+    K, W = args.steps, args.warmup
+    ens.run(0, W)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as cs:
+        ms = ens.run(0, K)
+    clocks = cs.summary()
+    kernels = ens.kernels(0)
+    ens.close()
+    for e in engines:
+        e.close()
+
+    # MC: 10^4 single-ion trials per box, FP64 denergy path
+    ntrial = args.trials
+    rng = np.random.Generator(np.random.PCG64(args.seed))
+    t_mc = 0.0
+    for s in (rs if ntrial > 0 else []):
+        e = engine(s, abi.MG_FP64, abi.MG_MC)
+        e.UTotal()
+        ip = rng.integers(1, s.np_ + 1, ntrial).astype(np.int32)
+        ro = s.ro[ip - 1] + 2.0 * (rng.random((ntrial, 3)) - 0.5)
+        ro -= s.boxlen * np.round(ro / s.boxlen)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        du, ovl = e.DUTotalBatch(ip, ro)
+        t_mc += time.perf_counter() - t0
+        e.close()
+    box_steps = nrep * K / (ms * 1e-3)
+    print(json.dumps({
+        "metric": "batched replicas: box MD steps/s (mixed) and MC trial dU/s (FP64)",
+        "value": box_steps, "unit": "box-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "dtype": "f32+i64",
+        "data": "synthetic (seeded replica set)",
+        "config": {"workload": f"{nrep} electrolyte boxes, N log-uniform in [500, 8000], c uniform in [0.01, 1.0] M, "
+                               "SPME order 6, r_c and mesh per box for force RMS 1e-5",
+                   "ions": int(sum(s.np_ for s in rs)),
+                   "settings": {f"rc{int(k[0])}_K{k[1]}": v for k, v in sorted(
+                       __import__("collections").Counter((s.rcut, s.nmesh) for s in rs).items())},
+                   "l2": "not flushed: the boxes' meshes and particles together exceed the 129 MB L2"},
+        "ensemble_steps_per_s": K / (ms * 1e-3),
+        "mc": {"trials_per_box": ntrial, "trials_per_s": nrep * ntrial / t_mc if t_mc > 0 else None,
+               "note": "host wall clock of mg_dutotal_batch per box (copies in and out included)"},
+        "accuracy": {"mixed_vs_fp64_force_rms": {"max": max(err_mixed), "median": float(np.median(err_mixed))},
+                     "spme_vs_converged_sample": err_spme},
+        "kernels_per_step": kernels, "clocks": clocks,
+    }), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,13 +650,19 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--profile", choices=["mixed", "fp64"],
                     help="profiling run for ncu: only W + K BD steps of one form, nothing else")
-    ap.add_argument("--workload", choices=["polyelectrolyte", "water"], default="polyelectrolyte",
-                    help="water: the polyatomic path on its own (not the headline metric)")
+    ap.add_argument("--workload", choices=["polyelectrolyte", "water", "replicas"], default="polyelectrolyte",
+                    help="water: the polyatomic path on its own; replicas: the batched boxes (not the headline metric)")
+    ap.add_argument("--replicas", type=int, default=256, help="boxes of the replicas workload")
+    ap.add_argument("--trials", type=int, default=10000, help="MC trials per box of the replicas workload")
+    ap.add_argument("--mesh-ns", type=float, default=0.01,
+                    help="replicas workload: modelled ns per mesh point when choosing r_c and the mesh")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
     if args.workload == "water":
         return run_water(args)
+    if args.workload == "replicas":
+        return run_replicas(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

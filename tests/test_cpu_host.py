@@ -74,3 +74,20 @@ def test_maxwell_velocities_remove_momentum():
     v = s.maxwell_velocities(seed=1).reshape(-1, 3)
     m = np.array([sp.mass for sp in s.species])[s.iptpn - 1]
     assert np.abs((m[:, None] * v).sum(0)).max() < 1e-9
+
+
+def test_choose_spme_meets_its_spacing_rule():
+    """The replicas' SPME chooser: every box gets order 6, r_c <= L/2, a
+    power-of-two mesh of at most 256 whose spacing keeps alpha*h within the
+    error model's bound, and alpha from erfc(alpha r_c) = 1e-5."""
+    import math
+
+    from molsim_gb300 import autotune, configs
+    for s in configs.replica_set(seed=5, nrep=64):
+        c = (s.np_ / 2) / (float(np.prod(s.boxlen)) * 1e-27 * configs.AVOGADRO)
+        ch = autotune.choose_spme(s, c)
+        L = float(s.boxlen.min())
+        assert ch["order"] == 6 and ch["rcut"] <= L / 2
+        assert ch["nmesh"] <= 256 and ch["nmesh"] & (ch["nmesh"] - 1) == 0
+        assert ch["ualpha"] * L / ch["nmesh"] <= autotune.alpha_h_max(1e-5, c) * (1 + 1e-12)
+        assert abs(math.erfc(ch["ualpha"] * ch["rcut"]) - 1e-5) < 1e-9

@@ -88,3 +88,22 @@ def test_autotuner_meets_its_target(gpu_lib):
     assert res["ms"] == min(c["ms"] for c in ok)
     # coarser settings that miss the target were measured and rejected
     assert any(c["err"] > target for c in res["candidates"]), res["candidates"]
+
+
+@pytest.mark.parametrize("conc", [0.01, 0.1, 1.0])
+def test_replica_chooser_meets_target(conc, gpu_lib):
+    """The batched boxes' SPME chooser (order 6, cutoff and mesh per box):
+    the mixed form's forces against a converged FP64 reference (order 10,
+    twice the mesh up to 256) stay within the 1e-5 RMS target."""
+    import dataclasses
+
+    from molsim_gb300 import autotune
+    s = configs.replica_set(seed=11, nrep=1, nmin=2000, nmax=2000, cmin=conc, cmax=conc)[0]
+    ch = autotune.choose_spme(s, conc)
+    s.rcut, s.ualpha, s.order, s.nmesh = ch["rcut"], ch["ualpha"], ch["order"], ch["nmesh"]
+    s.build_table()
+    ref = dataclasses.replace(s, order=10, nmesh=min(256, 2 * s.nmesh))
+    fr = _engine(ref, abi.MG_FP64).UTotal()["forceo"]
+    f = _engine(s, abi.MG_MIXED).UTotal()["forceo"]
+    err = np.sqrt(((f - fr) ** 2).mean() / (fr ** 2).mean())
+    assert err <= 1e-5, (ch, err)
