@@ -262,6 +262,15 @@ int mg_dutotal_batch(mg_handle *h, int32_t ntrial, const int32_t *ip,
 int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps,
             double *du_dsig, double *du_dbox);
 
+/* UTotal at the current positions and its derivative by an affine strain of
+ * the box and the positions, r -> (1 + eps) r: w[9] (row-major, symmetric)
+ * = dU/deps_ab, the virial tensor (pairs and bonds r_a f_b, angles through
+ * their arms, the reciprocal sum through k -> (1 - eps^T) k and V, the
+ * surface term through M and V).  Its trace is the reference's scalar
+ * virial (UTotal's `virial`, energy.F90:405-430, of which the reference
+ * keeps only the trace); w[0], w[4], w[8] are L_a du_dbox[a] of mg_grad. */
+int mg_virial_tensor(mg_handle *h, double *w);
+
 /* ---- integrators ------------------------------------------------------------ */
 
 /* Velocity-Verlet (VelVer, md.F90:252-420 + GetLinAcc md.F90:601-625) for a

@@ -13,11 +13,14 @@
 //                (Pot_1_6_12, potential.F90:1349-1434: sig_ab = (sig_a +
 //                sig_b)/2, eps_ab = sqrt(eps_a eps_b), with lljcut's cut and
 //                shift) from the analytic Lennard-Jones form
-//   dU/dL_a    for an affine stretch of the box along a (positions scaled
-//                with it): pairs and bonds through their radial derivative,
-//                the reciprocal sum through the L-dependence of meshfac /
-//                kfac, the surface term through its volume and dipole;
-//                sum_a L_a dU/dL_a is the reference's scalar virial.
+//   dU/deps_ab for an affine strain of the box and the positions,
+//                r -> (1 + eps) r (components xx, yy, zz, xy, xz, yz; the
+//                tensor is symmetric): pairs and bonds through their radial
+//                derivative, angles through their arms, the reciprocal sum
+//                through the k-dependence of meshfac / kfac (k -> (1 -
+//                eps^T) k, V -> (1 + tr eps) V), the surface term through
+//                its volume and dipole.  Its trace is the reference's scalar
+//                virial; dU/dL_a = dU/deps_aa / L_a.
 // All arithmetic is FP64 in both forms (the mixed form reads its FP32
 // potential mesh).
 #include <cmath>
@@ -41,13 +44,23 @@ struct GradArgs {
     int lljcut;
     double ljushift;
     double *phi;                      // [np]
-    double *part;                     // per block: deps[nptpt], dsig[nptpt], dL[3]
+    double *part;                     // per block: deps[nptpt], dsig[nptpt], strain[6]
 };
 
+// strain components: xx, yy, zz, xy, xz, yz
+__device__ __forceinline__ void strain_add(double *w, double f, double dx, double dy, double dz) {
+    w[0] += f * dx * dx;
+    w[1] += f * dy * dy;
+    w[2] += f * dz * dz;
+    w[3] += f * dx * dy;
+    w[4] += f * dx * dz;
+    w[5] += f * dy * dz;
+}
+
 __global__ void __launch_bounds__(kGradThreads) k_grad_pairs(GradArgs a) {
-    __shared__ double red[2 * MG_MAX_NPTPT + 3][kGradThreads / 32];
+    __shared__ double red[2 * MG_MAX_NPTPT + 6][kGradThreads / 32];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double de[MG_MAX_NPTPT], ds[MG_MAX_NPTPT], w0 = 0.0, w1 = 0.0, w2 = 0.0;
+    double de[MG_MAX_NPTPT], ds[MG_MAX_NPTPT], wv[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int k = 0; k < a.nptpt; ++k) { de[k] = 0.0; ds[k] = 0.0; }
     if (i < a.np) {
         int p = a.perm[i], ti = a.type[p];
@@ -70,27 +83,25 @@ __global__ void __launch_bounds__(kGradThreads) k_grad_pairs(GradArgs a) {
             // Lennard-Jones parameter derivatives (each pair is met twice)
             double sg = a.sig[pair], x = sg * sg / r2;
             x = x * x * x;
-            bool lj = !a.lljcut || r < a.ljrc[pair];
+            bool lj = a.sig && (!a.lljcut || r < a.ljrc[pair]);
             if (lj) {
                 de[pair] += 0.5 * (4.0 * (x * x - x) + (a.lljcut ? a.ljushift : 0.0));
                 ds[pair] += 0.5 * (24.0 * a.eps[pair] / sg) * (2.0 * x * x - x);
             }
-            // table force: dU/dL_a = -sum fsum dx_a^2 / L_a
+            // table force: dU/deps_ab = -sum fsum dx_a dx_b
             int rr = a.tab_start[pair], nr = a.tab_n[pair], kk = 0;
             while (kk + 1 < nr && r2 < a.ubuf[12 * (size_t)(rr + kk)]) ++kk;
             const double *c = a.ubuf + 12 * (size_t)(rr + kk);
             double d = r2 - c[0];
             double fsum = c[7] + d * (c[8] + d * (c[9] + d * (c[10] + d * c[11])));
-            w0 -= 0.5 * fsum * dx * dx;
-            w1 -= 0.5 * fsum * dy * dy;
-            w2 -= 0.5 * fsum * dz * dz;
+            strain_add(wv, -0.5 * fsum, dx, dy, dz);
         }
         a.phi[p] = site;
     }
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int nv = 2 * a.nptpt + 3;
+    int nv = 2 * a.nptpt + 6;
     for (int v = 0; v < nv; ++v) {
-        double x = v < a.nptpt ? de[v] : v < 2 * a.nptpt ? ds[v - a.nptpt] : (v == 2 * a.nptpt ? w0 : v == 2 * a.nptpt + 1 ? w1 : w2);
+        double x = v < a.nptpt ? de[v] : v < 2 * a.nptpt ? ds[v - a.nptpt] : wv[v - 2 * a.nptpt];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (lane == 0) red[v][w] = x;
     }
@@ -102,16 +113,15 @@ __global__ void __launch_bounds__(kGradThreads) k_grad_pairs(GradArgs a) {
     }
 }
 
-// bonds: dU/dL_a = sum du/dr dx_a^2 / r (divided by L_a at the end);
-// angles (UAngle): sum over the two arms d = r_ip - r_j of F_j,a d_a, F_j the
-// force on the arm's end (dU/dd = F_j since d depends on r_j with sign -1)
+// bonds: dU/deps_ab = sum du/dr dx_a dx_b / r; angles (UAngle): sum over
+// the two arms d = r_ip - r_j of (dU/dd)_a d_b
 __global__ void k_grad_bonds(const double *__restrict__ ro, const int *__restrict__ ij,
                              const double *__restrict__ bk, const double *__restrict__ beq,
                              const int *__restrict__ bp, int nbond, const int *__restrict__ aijk,
                              const double *__restrict__ ak, const double *__restrict__ aeq,
                              const int *__restrict__ ap, int nangle, mg_box box, double *__restrict__ part) {
-    __shared__ double red[3][8];
-    double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+    __shared__ double red[6][8];
+    double wv[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int an = blockIdx.x * blockDim.x + threadIdx.x; an < nangle; an += gridDim.x * blockDim.x) {
         int jm = aijk[3 * an], ip = aijk[3 * an + 1], jp = aijk[3 * an + 2];
         double dm[3], dq[3], um[3], uq[3];
@@ -134,12 +144,13 @@ __global__ void k_grad_bonds(const double *__restrict__ ro, const int *__restric
         double term = theta - aeq[an];
         int pw = ap[an];
         double fac = -pw * ak[an] * pow(term, pw - 1) / sin(theta);
-        double g[3];
-        for (int m = 0; m < 3; ++m)
-            g[m] = (fac * dmi) * (uq[m] - c * um[m]) * dm[m] + (fac * dpi) * (um[m] - c * uq[m]) * dq[m];
-        w0 += g[0];
-        w1 += g[1];
-        w2 += g[2];
+        double gm[3], gq[3];   // dU/d(arm) for the two arms
+        for (int m = 0; m < 3; ++m) {
+            gm[m] = (fac * dmi) * (uq[m] - c * um[m]);
+            gq[m] = (fac * dpi) * (um[m] - c * uq[m]);
+        }
+        const int ca[6] = {0, 1, 2, 0, 0, 1}, cb[6] = {0, 1, 2, 1, 2, 2};
+        for (int v = 0; v < 6; ++v) wv[v] += gm[ca[v]] * dm[cb[v]] + gq[ca[v]] * dq[cb[v]];
     }
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbond; b += gridDim.x * blockDim.x) {
         int i = ij[2 * b], j = ij[2 * b + 1];
@@ -149,22 +160,19 @@ __global__ void k_grad_bonds(const double *__restrict__ ro, const int *__restric
         double r = sqrt(dx * dx + dy * dy + dz * dz);
         int pw = bp[b];
         double du = bk[b] * pw * pow(r - beq[b], pw - 1) / r;
-        w0 += du * dx * dx;
-        w1 += du * dy * dy;
-        w2 += du * dz * dz;
+        strain_add(wv, du, dx, dy, dz);
     }
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) {
-        w0 += __shfl_down_sync(0xffffffffu, w0, o);
-        w1 += __shfl_down_sync(0xffffffffu, w1, o);
-        w2 += __shfl_down_sync(0xffffffffu, w2, o);
+    for (int v = 0; v < 6; ++v) {
+        double x = wv[v];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[v][w] = x;
     }
-    if (lane == 0) { red[0][w] = w0; red[1][w] = w1; red[2][w] = w2; }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 6) {
         double x = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x += red[threadIdx.x][k];
-        part[3 * blockIdx.x + threadIdx.x] = x;
+        part[6 * blockIdx.x + threadIdx.x] = x;
     }
 }
 
@@ -257,66 +265,69 @@ __global__ void k_grad_site(SiteArgs a) {
     a.phi[p] += a.efp * v;
 }
 
-// standard Ewald: dE/dL_a = sum_k kfac g_a(k) sum_c |S_c|^2
+// standard Ewald: dE/deps_ab = sum_k kfac sum_c |S_c|^2 (-delta_ab + 2 k_a
+// k_b (1/(4 alpha^2) + 1/k^2)), the sign combination c = (sx, sy) giving
+// k = (sx kx, sy ky, kz)
 __global__ void k_grad_box_std(const int4 *__restrict__ kv, const double *__restrict__ kfac,
-                               const double2 *__restrict__ S, int nk, double3 tpbi, double3 li, double ia2,
-                               double *__restrict__ out3) {
-    __shared__ double red[3][8];
-    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+                               const double2 *__restrict__ S, int nk, double3 tpbi, double ia2,
+                               double *__restrict__ out6) {
+    __shared__ double red[6][8];
+    double g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int k = threadIdx.x; k < nk; k += blockDim.x) {
         int4 n = kv[k];
-        double s2 = 0.0;
-        for (int c = 0; c < 4; ++c) s2 += S[4 * k + c].x * S[4 * k + c].x + S[4 * k + c].y * S[4 * k + c].y;
         double mx = n.x * tpbi.x, my = n.y * tpbi.y, mz = n.z * tpbi.z;
-        mx *= mx;
-        my *= my;
-        mz *= mz;
-        double c = ia2 + 1.0 / (mx + my + mz), e = kfac[k] * s2;
-        g0 += e * (-1.0 + 2.0 * mx * c) * li.x;
-        g1 += e * (-1.0 + 2.0 * my * c) * li.y;
-        g2 += e * (-1.0 + 2.0 * mz * c) * li.z;
+        double c = ia2 + 1.0 / (mx * mx + my * my + mz * mz);
+        for (int cmb = 0; cmb < 4; ++cmb) {
+            double sx = (cmb & 2) ? 1.0 : -1.0, sy = (cmb & 1) ? 1.0 : -1.0;
+            double e = kfac[k] * (S[4 * k + cmb].x * S[4 * k + cmb].x + S[4 * k + cmb].y * S[4 * k + cmb].y);
+            double kx = sx * mx, ky = sy * my, kz = mz;
+            g[0] += e * (-1.0 + 2.0 * kx * kx * c);
+            g[1] += e * (-1.0 + 2.0 * ky * ky * c);
+            g[2] += e * (-1.0 + 2.0 * kz * kz * c);
+            g[3] += e * (2.0 * kx * ky * c);
+            g[4] += e * (2.0 * kx * kz * c);
+            g[5] += e * (2.0 * ky * kz * c);
+        }
     }
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) {
-        g0 += __shfl_down_sync(0xffffffffu, g0, o);
-        g1 += __shfl_down_sync(0xffffffffu, g1, o);
-        g2 += __shfl_down_sync(0xffffffffu, g2, o);
+    for (int v = 0; v < 6; ++v) {
+        double x = g[v];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[v][w] = x;
     }
-    if (lane == 0) { red[0][w] = g0; red[1][w] = g1; red[2][w] = g2; }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 6) {
         double x = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x += red[threadIdx.x][k];
-        out3[threadIdx.x] = x;
+        out6[threadIdx.x] = x;
     }
 }
 
-// fixed-order totals: out = [deps(nptpt), dsig(nptpt), dL(3)]
+// fixed-order totals: out = [deps(nptpt), dsig(nptpt), strain(6)]
 struct FinalGrad {
     const double *pair_part;
     int nblk_pair, nptpt;
     const double *bond_part;
     int nblk_bond;
-    const double *rec3;      // dE_rec/dL (before EpsiFourPi) or null
+    const double *rec6;      // dE_rec/deps (before EpsiFourPi) or null
     const double *dip;       // surface sums or null
     double efp, surf_fac;
-    double L[3];
     double *out;
 };
 
 __global__ void k_grad_final(FinalGrad f) {
-    int v = threadIdx.x, nv = 2 * f.nptpt + 3;
+    int v = threadIdx.x, nv = 2 * f.nptpt + 6;
     if (v >= nv) return;
     double s = 0.0;
     for (int b = 0; b < f.nblk_pair; ++b) s += f.pair_part[(size_t)b * nv + v];
     if (v >= 2 * f.nptpt) {
+        const int ca[6] = {0, 1, 2, 0, 0, 1}, cb[6] = {0, 1, 2, 1, 2, 2};
         int d = v - 2 * f.nptpt;
-        for (int b = 0; b < f.nblk_bond; ++b) s += f.bond_part[3 * b + d];
-        s /= f.L[d];                       // pair and bond sums are L_a dU/dL_a
-        double r = f.rec3 ? f.rec3[d] : 0.0;
-        if (f.dip) {
+        for (int b = 0; b < f.nblk_bond; ++b) s += f.bond_part[6 * b + d];
+        double r = f.rec6 ? f.rec6[d] : 0.0;
+        if (f.dip) {   // E_surf = surf_fac |M|^2, M -> (1 + eps) M, V -> (1 + tr eps) V
             double m2 = f.dip[0] * f.dip[0] + f.dip[1] * f.dip[1] + f.dip[2] * f.dip[2];
-            r += f.surf_fac * (2.0 * f.dip[d] * f.dip[d] - m2) / f.L[d];
+            r += f.surf_fac * (2.0 * f.dip[ca[d]] * f.dip[cb[d]] - (d < 3 ? m2 : 0.0));
         }
         s += f.efp * r;
     }
@@ -325,34 +336,39 @@ __global__ void k_grad_final(FinalGrad f) {
 
 }  // namespace
 
-int mg_spme_box_grad(mg_handle *h, double *out3, double *scratch);
+int mg_spme_box_grad(mg_handle *h, double *out6, double *scratch);
 
-extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps, double *du_dsig,
-                       double *du_dbox) {
-    if (!h || !pp || !pp->sigat || !pp->epsat) return MG_ERR_ARG;
-    if (pp->npt != h->npt) return mg_fail(h, MG_ERR_ARG, "pot params npt %d != %d", pp->npt, h->npt);
+namespace {
+
+// UTotal at the current positions and its gradients: phi (dU/dq_i) into
+// phi (if non-null), and out = [deps(nptpt), dsig(nptpt), strain(6)]; with
+// pp null the Lennard-Jones parameter derivatives are zero
+int grad_run(mg_handle *h, const mg_pot_params *pp, double *phi, std::vector<double> &out) {
+    if (pp && (!pp->sigat || !pp->epsat)) return MG_ERR_ARG;
+    if (pp && pp->npt != h->npt) return mg_fail(h, MG_ERR_ARG, "pot params npt %d != %d", pp->npt, h->npt);
     if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_nlist_set has not been called");
     int np = h->np, nptpt = h->nptpt, npt = h->npt;
     // per pair type: Lorentz-Berthelot sigma_ab, eps_ab and the LJ cut
     std::vector<double> ab(3 * (size_t)nptpt, 0.0);
-    for (int a = 0; a < npt; ++a)
-        for (int b = 0; b < npt; ++b) {
-            int pair = h->h_pairidx[b * npt + a] - 1;
-            double sg = 0.5 * (pp->sigat[a] + pp->sigat[b]);
-            ab[pair] = sg;
-            ab[nptpt + pair] = std::sqrt(pp->epsat[a] * pp->epsat[b]);
-            ab[2 * nptpt + pair] = pp->ljrcut * sg;
-        }
+    if (pp)
+        for (int a = 0; a < npt; ++a)
+            for (int b = 0; b < npt; ++b) {
+                int pair = h->h_pairidx[b * npt + a] - 1;
+                double sg = 0.5 * (pp->sigat[a] + pp->sigat[b]);
+                ab[pair] = sg;
+                ab[nptpt + pair] = std::sqrt(pp->epsat[a] * pp->epsat[b]);
+                ab[2 * nptpt + pair] = pp->ljrcut * sg;
+            }
     if (h->list_stale) {
         MG_TRY(mg_lists_build(h, false));
         h->list_stale = false;
     }
     MG_TRY(mg_utotal_launch(h));   // energies, structure factors / potential mesh, surface sums
-    int nblk_pair = (np + kGradThreads - 1) / kGradThreads, nv = 2 * nptpt + 3;
+    int nblk_pair = (np + kGradThreads - 1) / kGradThreads, nv = 2 * nptpt + 6;
     int nbonded = std::max(h->nbond, h->nangle);
     int nblk_bond = nbonded > 0 ? std::min(304, (nbonded + 255) / 256) : 0;
-    size_t need = (size_t)np + 3 * nptpt + (size_t)nblk_pair * nv + 3 * (size_t)std::max(nblk_bond, 1) + 3 +
-                  3 * 304 + (size_t)nv;
+    size_t need = (size_t)np + 3 * nptpt + (size_t)nblk_pair * nv + 6 * (size_t)std::max(nblk_bond, 1) + 6 +
+                  6 * 304 + (size_t)nv;
     if (need > h->grad_cap) {
         if (h->d_grad) cudaFree(h->d_grad);
         h->d_grad = nullptr;
@@ -360,8 +376,8 @@ extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, doubl
         h->grad_cap = need;
     }
     double *d_phi = h->d_grad, *d_ab = d_phi + np, *d_pp = d_ab + 3 * nptpt;
-    double *d_bp = d_pp + (size_t)nblk_pair * nv, *d_rec3 = d_bp + 3 * (size_t)std::max(nblk_bond, 1);
-    double *d_scr = d_rec3 + 3, *d_out = d_scr + 3 * 304;
+    double *d_bp = d_pp + (size_t)nblk_pair * nv, *d_rec6 = d_bp + 6 * (size_t)std::max(nblk_bond, 1);
+    double *d_scr = d_rec6 + 6, *d_out = d_scr + 6 * 304;
     MG_CUDA(h, cudaMemcpyAsync(d_ab, ab.data(), sizeof(double) * 3 * nptpt, cudaMemcpyHostToDevice, h->st));
     GradArgs a;
     a.ro = h->d_ro;
@@ -389,11 +405,11 @@ extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, doubl
     a.rcut2 = h->rcut2;
     a.efp = h->EpsiFourPi;
     a.alpha = h->ualpha;
-    a.sig = d_ab;
+    a.sig = pp ? d_ab : nullptr;
     a.eps = d_ab + nptpt;
     a.ljrc = d_ab + 2 * nptpt;
-    a.lljcut = pp->lljcut;
-    a.ljushift = pp->ljushift;
+    a.lljcut = pp ? pp->lljcut : 0;
+    a.ljushift = pp ? pp->ljushift : 0.0;
     a.phi = d_phi;
     a.part = d_pp;
     k_grad_pairs<<<nblk_pair, kGradThreads, 0, h->st>>>(a);
@@ -432,17 +448,16 @@ extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, doubl
                                                     h->d_angle_p, h->nangle, box, d_bp);
         h->launches++;
     }
-    const double *rec3 = nullptr;
-    double3 li = make_double3(1.0 / h->boxlen[0], 1.0 / h->boxlen[1], 1.0 / h->boxlen[2]);
+    const double *rec6 = nullptr;
     if (h->ewald == MG_EWALD_STD) {
         k_grad_box_std<<<1, 256, 0, h->st>>>(h->d_kvec, h->d_kfac, h->d_S, h->nkvec,
-                                             make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]), li,
-                                             1.0 / (4.0 * h->ualpha * h->ualpha), d_rec3);
+                                             make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]),
+                                             1.0 / (4.0 * h->ualpha * h->ualpha), d_rec6);
         h->launches++;
-        rec3 = d_rec3;
+        rec6 = d_rec6;
     } else if (h->ewald == MG_EWALD_SPM) {
-        MG_TRY(mg_spme_box_grad(h, d_rec3, d_scr));
-        rec3 = d_rec3;
+        MG_TRY(mg_spme_box_grad(h, d_rec6, d_scr));
+        rec6 = d_rec6;
     }
     FinalGrad f;
     f.pair_part = d_pp;
@@ -450,24 +465,43 @@ extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, doubl
     f.nptpt = nptpt;
     f.bond_part = d_bp;
     f.nblk_bond = nblk_bond;
-    f.rec3 = rec3;
+    f.rec6 = rec6;
     f.dip = d_dip;
     f.efp = h->EpsiFourPi;
     f.surf_fac = 2.0 * 3.1415926535897932 / (3.0 * h->vol);
-    for (int d = 0; d < 3; ++d) f.L[d] = h->boxlen[d];
     f.out = d_out;
     k_grad_final<<<1, 32, 0, h->st>>>(f);
     h->launches++;
     MG_CUDA(h, cudaGetLastError());
-    std::vector<double> out(nv);
+    out.assign(nv, 0.0);
     if (phi) MG_CUDA(h, cudaMemcpyAsync(phi, d_phi, sizeof(double) * np, cudaMemcpyDeviceToHost, h->st));
     MG_CUDA(h, cudaMemcpyAsync(out.data(), d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, h->st));
-    MG_TRY(mg_check_device_error(h));
+    return mg_check_device_error(h);
+}
+
+}  // namespace
+
+extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps, double *du_dsig,
+                       double *du_dbox) {
+    if (!h || !pp || !pp->sigat || !pp->epsat) return MG_ERR_ARG;
+    std::vector<double> out;
+    MG_TRY(grad_run(h, pp, phi, out));
+    int nptpt = h->nptpt;
     if (du_deps)
         for (int k = 0; k < nptpt; ++k) du_deps[k] = out[k];
     if (du_dsig)
         for (int k = 0; k < nptpt; ++k) du_dsig[k] = out[nptpt + k];
     if (du_dbox)
-        for (int d = 0; d < 3; ++d) du_dbox[d] = out[2 * nptpt + d];
+        for (int d = 0; d < 3; ++d) du_dbox[d] = out[2 * nptpt + d] / h->boxlen[d];
+    return MG_OK;
+}
+
+extern "C" int mg_virial_tensor(mg_handle *h, double *w) {
+    if (!h || !w) return MG_ERR_ARG;
+    std::vector<double> out;
+    MG_TRY(grad_run(h, nullptr, nullptr, out));
+    const double *e = out.data() + 2 * h->nptpt;   // xx, yy, zz, xy, xz, yz
+    const int ix[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};
+    for (int k = 0; k < 9; ++k) w[k] = e[ix[k]];
     return MG_OK;
 }

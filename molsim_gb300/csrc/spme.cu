@@ -1977,17 +1977,20 @@ static int spme_spread(mg_handle *h, const SplineArgs &sa, const BrickArgs &bk) 
     return MG_OK;
 }
 
-// d(E_rec)/dL_a for an affine stretch of the box along a (positions scaled
-// with it, so the mesh charges do not change): sum over the half spectrum of
-// |F|^2 ew(k) g_a(k), g_a = (1/L_a) (-1 + 2 m_a^2 (1/(4 alpha^2) + 1/m^2)),
-// the derivative of meshfac = 4 pi/V exp(-m^2/4alpha^2)/m^2 b2 by L_a.
+// d(E_rec)/deps_ab for an affine strain of the box (positions strained with
+// it, so the mesh charges do not change): sum over the half spectrum of
+// |F|^2 ew(k) (-delta_ab + 2 m_a m_b (1/(4 alpha^2) + 1/m^2)), the
+// derivative of meshfac = 4 pi/V exp(-m^2/4alpha^2)/m^2 b2 by the strain
+// (m -> (1 - eps^T) m, V -> (1 + tr eps) V), with the signed wave vector m
+// of the spectrum entry (ky, kz above n/2 are negative); components xx, yy,
+// zz, xy, xz, yz.
 template <typename T>
 __global__ void __launch_bounds__(256) k_box_grad(const V2<T> *__restrict__ F, const T *__restrict__ ew, int n,
-                                                  double3 tpbi, double3 li, double ia2, double *__restrict__ part) {
-    __shared__ double red[3][8];
+                                                  double3 tpbi, double ia2, double *__restrict__ part) {
+    __shared__ double red[6][8];
     int nh = n / 2 + 1;
     size_t total = (size_t)nh * n * n;
-    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    double g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         int kx = (int)(e % nh), ky = (int)((e / nh) % n), kz = (int)(e / ((size_t)nh * n));
         int fy = min(ky, n - ky), fz = min(kz, n - kz);
@@ -1996,38 +1999,37 @@ __global__ void __launch_bounds__(256) k_box_grad(const V2<T> *__restrict__ F, c
         if (w == 0.0) continue;
         V2<T> f = F[e];
         double p2 = (double)f.x * f.x + (double)f.y * f.y;
-        double mx = kx * tpbi.x, my = fy * tpbi.y, mz = fz * tpbi.z;
-        mx *= mx;
-        my *= my;
-        mz *= mz;
-        double c = ia2 + 1.0 / (mx + my + mz), pw = p2 * w;
-        g0 += pw * (-1.0 + 2.0 * mx * c) * li.x;
-        g1 += pw * (-1.0 + 2.0 * my * c) * li.y;
-        g2 += pw * (-1.0 + 2.0 * mz * c) * li.z;
+        double mx = kx * tpbi.x, my = (ky <= n / 2 ? ky : ky - n) * tpbi.y, mz = (kz <= n / 2 ? kz : kz - n) * tpbi.z;
+        double c = ia2 + 1.0 / (mx * mx + my * my + mz * mz), pw = p2 * w;
+        g[0] += pw * (-1.0 + 2.0 * mx * mx * c);
+        g[1] += pw * (-1.0 + 2.0 * my * my * c);
+        g[2] += pw * (-1.0 + 2.0 * mz * mz * c);
+        g[3] += pw * (2.0 * mx * my * c);
+        g[4] += pw * (2.0 * mx * mz * c);
+        g[5] += pw * (2.0 * my * mz * c);
     }
     int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) {
-        g0 += __shfl_down_sync(0xffffffffu, g0, o);
-        g1 += __shfl_down_sync(0xffffffffu, g1, o);
-        g2 += __shfl_down_sync(0xffffffffu, g2, o);
+    for (int v = 0; v < 6; ++v) {
+        double x = g[v];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[v][wp] = x;
     }
-    if (lane == 0) { red[0][wp] = g0; red[1][wp] = g1; red[2][wp] = g2; }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 6) {
         double x = 0.0;
         for (int k = 0; k < 8; ++k) x += red[threadIdx.x][k];
-        part[3 * blockIdx.x + threadIdx.x] = x;
+        part[6 * blockIdx.x + threadIdx.x] = x;
     }
 }
 
-__global__ void k_sum3(const double *__restrict__ part, int nblk, double *__restrict__ out) {
-    if (threadIdx.x >= 3) return;
+__global__ void k_sum6(const double *__restrict__ part, int nblk, double *__restrict__ out) {
+    if (threadIdx.x >= 6) return;
     double x = 0.0;
-    for (int b = 0; b < nblk; ++b) x += part[3 * b + threadIdx.x];
+    for (int b = 0; b < nblk; ++b) x += part[6 * b + threadIdx.x];
     out[threadIdx.x] = x;
 }
 
-template <typename T> static int box_grad_t(mg_handle *h, double *out3, double *scratch, int nblk) {
+template <typename T> static int box_grad_t(mg_handle *h, double *out6, double *scratch, int nblk) {
     int n = h->nmesh, logn = ilog2(n), nh = h->nh;
     int lp = 4;
     size_t vsz = sizeof(V2<T>);
@@ -2048,23 +2050,22 @@ template <typename T> static int box_grad_t(mg_handle *h, double *out3, double *
     k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, (size_t)n * nh, nh, -1, tw, cv, ftx);
     const T *ew = (const T *)(h->form == MG_MIXED ? (const void *)h->d_ew_f : (const void *)h->d_ew);
     double3 tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
-    double3 li = make_double3(1.0 / h->boxlen[0], 1.0 / h->boxlen[1], 1.0 / h->boxlen[2]);
-    k_box_grad<T><<<nblk, 256, 0, h->st>>>(F, ew, n, tpbi, li, 1.0 / (4.0 * h->ualpha * h->ualpha), scratch);
-    k_sum3<<<1, 32, 0, h->st>>>(scratch, nblk, out3);
+    k_box_grad<T><<<nblk, 256, 0, h->st>>>(F, ew, n, tpbi, 1.0 / (4.0 * h->ualpha * h->ualpha), scratch);
+    k_sum6<<<1, 32, 0, h->st>>>(scratch, nblk, out6);
     h->launches += 6;
     MG_CUDA(h, cudaGetLastError());
     return MG_OK;
 }
 
-// d(E_rec)/dL (before EpsiFourPi) into the device array out3; scratch holds
-// 3 * 304 doubles
-int mg_spme_box_grad(mg_handle *h, double *out3, double *scratch) {
+// d(E_rec)/deps (before EpsiFourPi; xx, yy, zz, xy, xz, yz) into the device
+// array out6; scratch holds 6 * 304 doubles
+int mg_spme_box_grad(mg_handle *h, double *out6, double *scratch) {
     SplineArgs sa;
     BrickArgs bk;
     spme_args(h, sa, bk);
     MG_TRY(spme_spread(h, sa, bk));
-    if (h->form == MG_MIXED) return box_grad_t<float>(h, out3, scratch, 304);
-    return box_grad_t<double>(h, out3, scratch, 304);
+    if (h->form == MG_MIXED) return box_grad_t<float>(h, out6, scratch, 304);
+    return box_grad_t<double>(h, out6, scratch, 304);
 }
 
 // UTotal's mesh part with the spread fused into the forward plane pass:

@@ -164,6 +164,13 @@ class Engine:
                     "grad")
         return dict(phi=phi, du_deps=de, du_dsig=ds, du_dbox=db)
 
+    def VirialTensor(self):
+        """dU/deps_ab (3x3) for an affine strain of the box and positions;
+        its trace is UTotal's virial."""
+        w = np.zeros(9)
+        self._check(self.lib.mg_virial_tensor(self.h, abi.f64(w)), "virial_tensor")
+        return w.reshape(3, 3)
+
     # ---- integrators ------------------------------------------------------------
     def MDSetup(self, tstep, rod, rodd=None):
         massip = self.system.massip()
