@@ -12,6 +12,14 @@ with its own DUTotal and MCUpdate.  Restated from mc.F90:
   (mc.F90:4527-4580): the same random displacement in a cube of edge dtran
   (or a sphere of diameter |dtran| for dtran < 0) for every moving particle.
 - ChainMove (mc.F90:2541-2629): a whole chain, displaced by dtranchain.
+- SPartCl2Move (mc.F90:1818-1945): the cluster of the chosen particle (its
+  connected component among the particles of its type, or all particles
+  with txmembcl2 = 'all', two particles joined when closer than radcl2:
+  CalcPartPairListIpt/All molaux.F90:1863-1984, MakeCluster and
+  CalcClusterMember mollib.F90:1805-1935), displaced together by one
+  GetRandomTrialPos of dtrancl2; after DUTotal the move is rejected without
+  a Metropolis draw when a cluster member would come within radcl2 of a
+  particle of the type outside the cluster (the cluster would change).
 - PivotMove (mc.F90:1967-2172): the part of a chain on one side of a pivot
   bead ('short', 'lower' or 'upper'), unwrapped by UndoPBCChain
   (molaux.F90:1266-1325), rotated by alpha = drotpivot (Random - 1/2) about
@@ -25,8 +33,9 @@ with its own DUTotal and MCUpdate.  Restated from mc.F90:
 - Random (mollib.F90:2689-2709): Marsaglia's xorshift combined with
   Park-Miller, the generator every move draws from.
 
-Cluster moves, the pivot's crosslinked generations and the non-energetic
-weights (umbrella, MC weights) are not part of this path.
+The cluster moves' second shell (radcl1 > 0), the pivot's crosslinked
+generations and the non-energetic weights (umbrella, MC weights) are not
+part of this path.
 """
 from dataclasses import dataclass, field
 from typing import Dict, List
@@ -35,7 +44,7 @@ import numpy as np
 
 from . import units
 
-__all__ = ["RefRandom", "MoveParams", "MCPass", "chains_from_bonds", "axis_angle_matrix"]
+__all__ = ["RefRandom", "MoveParams", "MCPass", "chains_from_bonds", "axis_angle_matrix", "clusters"]
 
 _M32 = 0xFFFFFFFF
 
@@ -124,6 +133,24 @@ def chains_from_bonds(np_, bond_ip, bond_jp):
     return chains, chain_of, seg_of
 
 
+def clusters(n, pairs):
+    """Connected components of n objects (0-based) joined by pairs, as a
+    label per object (MakeCluster, mollib.F90:1805-1904: the labels differ,
+    the membership is the same)."""
+    parent = list(range(n))
+
+    def top(i):
+        while parent[i] != i:
+            parent[i] = parent[parent[i]]
+            i = parent[i]
+        return i
+    for i, j in pairs:
+        a, b = top(int(i)), top(int(j))
+        if a != b:
+            parent[b] = a
+    return np.array([top(i) for i in range(n)])
+
+
 @dataclass
 class MoveParams:
     """nmlMC variables of one particle type (mc.F90:959-983 defaults; the
@@ -136,12 +163,16 @@ class MoveParams:
     ipivotrotmode: int = 1
     pchain: float = 0.0
     dtranchain: float = 0.0
+    pspartcl2: float = 0.0
+    txmembcl2: str = "ipt"
+    radcl2: float = 0.0
+    dtrancl2: float = 0.0
 
 
 @dataclass
 class MCStats:
-    trials: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "pivot": 0, "chain": 0})
-    accepted: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "pivot": 0, "chain": 0})
+    trials: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0})
+    accepted: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0})
     events: List[str] = field(default_factory=list)
 
 
@@ -162,14 +193,16 @@ class MCPass:
         if len(plist) != npt:
             raise ValueError(f"{len(plist)} move parameter sets for {npt} particle types")
         self.p = plist
-        # cumulative probabilities (IOMC): pspart, then ppivot, then pchain
+        # cumulative probabilities (IOMC, CallMove's order): pspart, then
+        # pspartcl2, ppivot and pchain
         self.cum = []
         for mp in plist:
-            tot = max(mp.pspart + mp.ppivot + mp.pchain, 1e-15)
+            tot = max(mp.pspart + mp.pspartcl2 + mp.ppivot + mp.pchain, 1e-15)
             a = mp.pspart / tot
-            b = a + mp.ppivot / tot
+            a2 = a + mp.pspartcl2 / tot
+            b = a2 + mp.ppivot / tot
             c = b + mp.pchain / tot
-            self.cum.append((a, b, c, tot > 1e-15))
+            self.cum.append((a, a2, b, c, tot > 1e-15))
         self.L = np.asarray(system.boxlen, dtype=np.float64)
         self.half = 0.5 * self.L
         self.Li = 1.0 / self.L
@@ -197,6 +230,15 @@ class MCPass:
             a = a + np.sign(t) * (np.abs(t - a) >= 0.5)
             r[..., m] = np.where(big, x - self.L[m] * a, x)
         return r
+
+    def _pbcr2(self, d):
+        """PBCr2 (molaux.F90:149-184): one shift by L where |d| > L/2, then
+        r^2 = dx^2 + dy^2 + dz^2 (rows of d)."""
+        d = np.array(d, dtype=np.float64)
+        for m in range(3):
+            x = d[..., m]
+            d[..., m] = np.where(np.abs(x) > self.half[m], x - np.copysign(self.L[m], x), x)
+        return d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1] + d[..., 2] * d[..., 2]
 
     def _trial_translation(self, dtran):
         """GetRandomTrialPos: one displacement for all moving particles."""
@@ -244,6 +286,45 @@ class MCPass:
         d = self._trial_translation(mp.dtran)
         rotm = self._pbc(self.ro[ipmove - 1] + d).reshape(1, 3)
         return self._try("spart", [ipmove], rotm, d.reshape(1, 3))
+
+    def spartcl2(self, ipmove, mp):
+        """SPartCl2Move (radcl1 = 0)."""
+        ipt = int(self.s.iptpn[ipmove - 1])
+        of_type = np.flatnonzero(self.s.iptpn == ipt) + 1          # iplow .. ipupp
+        objs = of_type if mp.txmembcl2 == "ipt" else np.arange(1, self.s.np_ + 1)
+        rc2 = mp.radcl2 ** 2
+        pos = self.ro[objs - 1]
+        pairs = []
+        for a in range(len(objs) - 1):
+            r2 = self._pbcr2(pos[a] - pos[a + 1:])
+            for b in np.flatnonzero(r2 < rc2):
+                pairs.append((a, a + 1 + b))
+        lab = clusters(len(objs), pairs)
+        me = int(np.flatnonzero(objs == ipmove)[0])
+        ips = objs[lab == lab[me]]                                  # members in object order
+        d = self._trial_translation(mp.dtrancl2)
+        rotm = self._pbc(self.ro[ips - 1] + d)
+        self.stats.trials["cl2"] += 1
+        du, ovl = self.e.DUTotal(ips, rotm)
+        if not ovl:
+            # a particle of the type outside the cluster within radcl2 of a
+            # moved member: the cluster would change, rejected outright
+            outside = of_type[~np.isin(of_type, ips)]
+            for k in range(len(ips)):
+                if outside.size and (self._pbcr2(self.ro[outside - 1] - rotm[k]) < rc2).any():
+                    if self.record:
+                        self.stats.events.append("cl2:x")
+                    return False
+        acc = self._metropolis(ovl, du["du_tot"])
+        if acc:
+            self.e.MCUpdate()
+            self.ro[ips - 1] = rotm
+            self.drostep[ips - 1] += d
+            self.du_acc += du["du_tot"]
+            self.stats.accepted["cl2"] += 1
+        if self.record:
+            self.stats.events.append(f"cl2:{'a' if acc else ('o' if ovl else 'r')}{len(ips)}")
+        return acc
 
     def chain(self, ipmove, mp):
         ic = int(self.chain_of[ipmove])
@@ -319,7 +400,7 @@ class MCPass:
             ipmove = ipass if self.isamp == 0 else 1 + int(np_ * self.rng())
             ipmove = max(1, min(ipmove, np_))
             ipt = int(self.s.iptpn[ipmove - 1]) - 1
-            a, b, c, moving = self.cum[ipt]
+            a, a2, b, c, moving = self.cum[ipt]
             if not moving:
                 continue
             mp = self.p[ipt]
@@ -329,6 +410,8 @@ class MCPass:
             pr = self.rng()
             if pr < a:
                 self.spart(ipmove, mp)
+            elif pr < a2:
+                self.spartcl2(ipmove, mp)
             elif pr < b:
                 self.pivot(ipmove, mp)
             else:

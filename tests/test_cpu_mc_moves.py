@@ -122,3 +122,34 @@ def test_pivot_about_a_bond_keeps_bond_lengths(orc):
     mc.run_pass()
     assert mc.stats.accepted["pivot"] > 3
     assert np.abs(bonds(mc.ro) - b0).max() < 1e-9
+
+
+def test_clusters_are_connected_components():
+    from molsim_gb300.mc import clusters
+    lab = clusters(7, [(0, 3), (3, 5), (1, 2), (6, 6)])
+    groups = {}
+    for i, l in enumerate(lab):
+        groups.setdefault(l, []).append(i)
+    assert sorted(groups.values()) == [[0, 3, 5], [1, 2], [4], [6]]
+
+
+@pytest.mark.parametrize("memb", ["ipt", "all"])
+def test_cluster_moves_ucheck(memb, orc):
+    """SPartCl2Move (mc.F90:1818-1945) beside single-particle moves: clusters
+    of several ions move, moves that would change a cluster are rejected,
+    and the accepted du%tot add up to the change of UTotal."""
+    s, e = _setup(orc)
+    u0 = e.UTotal()["u_tot"]
+    ion_p = MoveParams(pspart=0.5, dtran=2.0, pspartcl2=0.5, txmembcl2=memb, radcl2=6.0, dtrancl2=3.0)
+    chain_p = MoveParams(pspart=1.0, dtran=1.0)
+    mc = MCPass(e, s, iseed=17, params=[ion_p, ion_p, ion_p, chain_p], record=True)
+    for _ in range(2):
+        mc.run_pass()
+    st = mc.stats
+    sizes = [int(ev[5:]) for ev in st.events if ev.startswith("cl2:") and ev[4] in "aro"]
+    assert st.trials["cl2"] > 50 and st.accepted["cl2"] > 5
+    assert max(sizes) >= 3
+    assert any(ev == "cl2:x" for ev in st.events)
+    u1 = _fresh(s, orc, mc.ro)
+    assert abs((u0 + mc.du_acc) - u1) < 1e-9 * abs(u1)
+    assert np.array_equal(e.GetPositions(), mc.ro)

@@ -223,3 +223,32 @@ def test_mc_passes_match_oracle(mode, orc, gpu_lib):
     assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
     u1 = gpu.UTotal()
     assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
+
+
+@pytest.mark.parametrize("memb", ["ipt", "all"])
+def test_cluster_passes_match_oracle(memb, orc, gpu_lib):
+    """MC passes with the cluster move SPartCl2Move (mc.F90:1818-1945) beside
+    single-particle moves, through the oracle and through the GPU with the
+    same Random stream: the same clusters are tried and accepted or
+    rejected, positions agree bit for bit, and the accepted du%tot add up to
+    the GPU's UTotal."""
+    from molsim_gb300.mc import MCPass, MoveParams
+    from tests.helpers import chain_system
+    s = prepared(chain_system(seed=73, txintlist=abi.MG_CELLLIST), orc)
+    ref, gpu, u_ref, u_gpu = _pair(s, orc)
+    ion_p = MoveParams(pspart=0.5, dtran=2.0, pspartcl2=0.5, txmembcl2=memb, radcl2=6.0, dtrancl2=3.0)
+    chain_p = MoveParams(pspart=1.0, dtran=1.0)
+    params = [ion_p, ion_p, ion_p, chain_p]
+    runs = [MCPass(e, s, iseed=19, params=params, record=True) for e in (ref, gpu)]
+    for mc in runs:
+        for _ in range(2):
+            mc.run_pass()
+    a, b = runs
+    assert a.stats.events == b.stats.events
+    assert b.stats.accepted["cl2"] > 5
+    assert np.array_equal(a.ro, b.ro)
+    assert np.array_equal(gpu.GetPositions(), b.ro)
+    scale = abs(u_ref["u_tot"]) + abs(u_ref["u_rec"]) + 1.0
+    assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
+    u1 = gpu.UTotal()
+    assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
