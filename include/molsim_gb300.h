@@ -425,6 +425,35 @@ int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const double *r, const
  * molecular virial sum (r_a - ro_p) . f_a into *virmolecule. */
 int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force, double force_fac,
                      double *forceo, double *torqueo, double *virmolecule);
+/* Rigid-body velocity Verlet of the polyatomic particles (VelVer with
+ * lpolyatom, md.F90:252-420): the state lives on the device.  Set-up takes
+ * the inverse masses massip[np], the principal moments momp[3*np], the
+ * centres ro[3*np], the quaternions qua[4*np] (qua(0:3,np)), the linear
+ * velocities rod[3*np], the angular velocities angvelo[3*np] (principal
+ * frame; the quaternion velocities follow by AngVelToQuaVel,
+ * mollib.F90:2621-2642), the linear and quaternion accelerations rodd[3*np]
+ * and quadd[4*np] (zero at the start of a simulation, as MDDriver sets
+ * them, md.F90:131-146), and tvvite, nvvite of the quaternion velocity
+ * iteration.  _move advances centres
+ * (with PBC) and quaternions (normalised) and writes ro[3*np], the
+ * orientation matrices ori[9*np] (ori(3,3,np), column-major, from QuaToOri
+ * mollib.F90:2221-2255) and drostep[3*np]; the caller then places the atoms
+ * and evaluates UTotal; _kick takes its forceo and torqueo, updates the
+ * linear velocities (GetLinAcc md.F90:601-617) and the quaternion
+ * velocities (nvvite iterations of GetAngAcc md.F90:628-663) and writes rod
+ * and angvelo (that of the last iteration's trial quaternion velocities,
+ * as the reference leaves it). */
+int mg_poly_rigid_setup(mg_poly *c, double tstep, double tvvite, int32_t nvvite, const double *massip,
+                        const double *momp, const double *ro, const double *qua, const double *rod,
+                        const double *angvelo, const double *rodd, const double *quadd);
+int mg_poly_rigid_move(mg_poly *c, double *ro, double *ori, double *drostep);
+int mg_poly_rigid_kick(mg_poly *c, const double *forceo, const double *torqueo, double *rod, double *angvelo);
+/* the accelerations of the current state from forceo and torqueo (a kick
+ * of zero length: GetLinAcc, GetAngAcc), for a run that starts from
+ * evaluated forces instead of the reference's zero accelerations */
+int mg_poly_rigid_prime(mg_poly *c, const double *forceo, const double *torqueo);
+/* the quaternions qua[4*np] and quaternion velocities quad[4*np] */
+int mg_poly_rigid_get(mg_poly *c, double *qua, double *quad);
 int mg_poly_last_error(const mg_poly *c, char *buf, size_t n);
 int mg_poly_destroy(mg_poly *c);
 

@@ -306,8 +306,8 @@ def water_ions(seed=9, nwater=300, nsalt=20, L=24.0, rcut=9.0, rmin=3.0):
     atoms (H without LJ)."""
     from .poly import AtomType, ParticleType, PolySystem
     rng = np.random.Generator(np.random.PCG64(seed))
-    atom_types = [AtomType("O", -0.8476, 3.166, 0.650), AtomType("H", 0.4238, 0.0, 0.0),
-                  AtomType("Na", 1.0, 2.35, 0.544), AtomType("Cl", -1.0, 4.40, 0.419)]
+    atom_types = [AtomType("O", -0.8476, 3.166, 0.650, 15.9994), AtomType("H", 0.4238, 0.0, 0.0, 1.008),
+                  AtomType("Na", 1.0, 2.35, 0.544, 22.99), AtomType("Cl", -1.0, 4.40, 0.419, 35.45)]
     hx, hz = 0.8165, 0.5773
     ptypes = [ParticleType("water", [(0, (0.0, 0.0, -0.0656)), (1, (hx, 0.0, hz - 0.0656)),
                                      (1, (-hx, 0.0, hz - 0.0656))]),

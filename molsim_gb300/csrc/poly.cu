@@ -447,6 +447,13 @@ struct mg_poly {
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
            *d_part = nullptr, *d_aza = nullptr;
     std::vector<double> h_part;
+    // rigid-body velocity Verlet (mg_poly_rigid_*): per particle
+    // [0,3) ro, [3,7) qua, [7,10) rod, [10,13) rodd, [13,17) quad,
+    // [17,21) quadd, [21,24) massip (repeated), [24,27) momp, [27,30) momip
+    double *d_rig = nullptr;
+    double rig_tstep = 0.0, rig_tvvite = 0.0;
+    int rig_nvvite = 0;
+    double *d_rig_io = nullptr;   // staging: ro, ori, drostep out; forceo, torqueo in; rod, angvelo out
 };
 
 static int poly_fail(mg_poly *c, int code, const char *fmt, ...) {
@@ -478,7 +485,8 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
     void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
                     c->d_force, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
-                    c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to, c->d_bin_z0, c->d_bin_inv, c->d_bin_k};
+                    c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to, c->d_bin_z0, c->d_bin_inv, c->d_bin_k,
+                    c->d_rig, c->d_rig_io};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -856,5 +864,228 @@ extern "C" int mg_poly_utwobody_list(mg_poly *c, mg_handle *h, const double *r, 
     u_twob[0] = tot;
     for (int b = 0; b < c->nblk_w; ++b) vir += c->h_part[(size_t)b * nv + p.nptpt];
     *virial = vir;
+    return MG_OK;
+}
+
+// ---- rigid-body velocity Verlet (VelVer, md.F90:252-420, lpolyatom) -------------
+// Positions and quaternions advance from the velocities and accelerations
+// of the last step; after UTotal the linear velocities take the new forces
+// (GetLinAcc, md.F90:601-617) and the quaternion velocities are iterated
+// nvvite times from a trial tvvite * tstep * the old acceleration
+// (QuaVelToAngVel mollib.F90:2651-2669, GetAngAcc md.F90:628-663).  The
+// arithmetic follows the reference's expressions.
+namespace {
+
+// rigid-body state per particle: [0,3) ro, [3,7) qua, [7,10) rod, [10,13) rodd,
+// [13,17) quad, [17,21) quadd, [21,24) massip, [24,27) momp, [27,30) momip,
+// [30,33) angvelo
+constexpr int kRig = 33;
+
+__device__ void rig_qua_to_ori(const double *q, double *ori) {   // QuaToOri, ori(3,3) column-major
+    double q00 = q[0] * q[0], q11 = q[1] * q[1], q22 = q[2] * q[2], q33 = q[3] * q[3];
+    double q01 = q[0] * q[1], q02 = q[0] * q[2], q03 = q[0] * q[3];
+    double q12 = q[1] * q[2], q13 = q[1] * q[3], q23 = q[2] * q[3];
+    ori[0] = -q22 + q11 - q33 + q00;
+    ori[1] = 2.0 * (q03 - q12);
+    ori[2] = 2.0 * (q13 + q02);
+    ori[3] = -2.0 * (q12 + q03);
+    ori[4] = q22 - q11 - q33 + q00;
+    ori[5] = 2.0 * (q01 - q23);
+    ori[6] = 2.0 * (q13 - q02);
+    ori[7] = -2.0 * (q23 + q01);
+    ori[8] = -q22 - q11 + q33 + q00;
+}
+
+// GetAngAcc for one particle: quaternion acceleration from the torque
+// (lab frame) and the angular velocity (principal frame)
+__device__ void rig_ang_acc(const double *q, const double *qd, const double *tq, const double *w,
+                            const double *momp, const double *momip, double *qdd) {
+    double ori[9];
+    rig_qua_to_ori(q, ori);
+    double t1 = tq[0] * ori[0] + tq[1] * ori[1] + tq[2] * ori[2];
+    double t2 = tq[0] * ori[3] + tq[1] * ori[4] + tq[2] * ori[5];
+    double t3 = tq[0] * ori[6] + tq[1] * ori[7] + tq[2] * ori[8];
+    double a1 = (t1 + w[1] * w[2] * (momp[1] - momp[2])) * momip[0];
+    double a2 = (t2 + w[2] * w[0] * (momp[2] - momp[0])) * momip[1];
+    double a3 = (t3 + w[0] * w[1] * (momp[0] - momp[1])) * momip[2];
+    double fac = -2.0 * (qd[2] * qd[2] + qd[1] * qd[1] + qd[3] * qd[3] + qd[0] * qd[0]);
+    qdd[0] = 0.5 * (-q[1] * a1 + q[2] * a2 - q[3] * a3 + q[0] * fac);
+    qdd[1] = 0.5 * (+q[0] * a1 - q[3] * a2 - q[2] * a3 + q[1] * fac);
+    qdd[2] = 0.5 * (-q[3] * a1 - q[0] * a2 + q[1] * a3 + q[2] * fac);
+    qdd[3] = 0.5 * (+q[2] * a1 + q[1] * a2 + q[0] * a3 + q[3] * fac);
+}
+
+__device__ void rig_angvel(const double *q, const double *qd, double *w) {   // QuaVelToAngVel
+    w[0] = 2.0 * (-q[3] * qd[2] + q[0] * qd[1] + q[2] * qd[3] - q[1] * qd[0]);
+    w[1] = 2.0 * (-q[0] * qd[2] - q[3] * qd[1] + q[1] * qd[3] + q[2] * qd[0]);
+    w[2] = 2.0 * (+q[1] * qd[2] - q[2] * qd[1] + q[0] * qd[3] - q[3] * qd[0]);
+}
+
+// set-up: quaternion velocities from the angular velocities
+// (AngVelToQuaVel mollib.F90:2621-2642)
+__global__ void k_rigid_setup(int np, double *__restrict__ rig) {
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= np) return;
+    double *g = rig + (size_t)kRig * ip;
+    const double *q = g + 3, *w = g + 30;
+    double *qd = g + 13;
+    qd[0] = 0.5 * (-q[1] * w[0] + q[2] * w[1] - q[3] * w[2]);
+    qd[1] = 0.5 * (+q[0] * w[0] - q[3] * w[1] - q[2] * w[2]);
+    qd[2] = 0.5 * (-q[3] * w[0] - q[0] * w[1] + q[1] * w[2]);
+    qd[3] = 0.5 * (+q[2] * w[0] + q[1] * w[1] + q[0] * w[2]);
+}
+
+// VelVer's first part: new positions (PBC) and quaternions (QuaNorm), the
+// orientation matrices (QuaToOri) and drostep
+__global__ void k_rigid_move(int np, double tstep, mg_box box, double *__restrict__ rig, double *__restrict__ ro,
+                             double *__restrict__ ori, double *__restrict__ drostep) {
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= np) return;
+    double *g = rig + (size_t)kRig * ip;
+    double fac = 0.5 * (tstep * tstep);
+    for (int m = 0; m < 3; ++m) {
+        double d = tstep * g[7 + m] + fac * g[10 + m];
+        double x = g[m] + d;
+        if (fabs(x) > box.half[m]) x = x - box.len[m] * round(x * box.inv[m]);   // PBC (anint)
+        g[m] = x;
+        ro[3 * ip + m] = x;
+        drostep[3 * ip + m] = d;
+    }
+    double *q = g + 3;
+    for (int k = 0; k < 4; ++k) q[k] = q[k] + tstep * g[13 + k] + fac * g[17 + k];
+    double norm = 1.0 / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    for (int k = 0; k < 4; ++k) q[k] = q[k] * norm;
+    rig_qua_to_ori(q, ori + 9 * (size_t)ip);
+}
+
+// VelVer's second part, after UTotal
+__global__ void k_rigid_kick(int np, double tstep, double tvvite, int nvvite, double *__restrict__ rig,
+                             const double *__restrict__ forceo, const double *__restrict__ torqueo,
+                             double *__restrict__ rod, double *__restrict__ angvelo) {
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= np) return;
+    double *g = rig + (size_t)kRig * ip;
+    for (int m = 0; m < 3; ++m) {
+        double roddo = g[10 + m];
+        g[10 + m] = g[21] * forceo[3 * ip + m];
+        g[7 + m] = g[7 + m] + (0.5 * tstep) * (g[10 + m] + roddo);
+        rod[3 * ip + m] = g[7 + m];
+    }
+    double *q = g + 3, *qd = g + 13, *qdd = g + 17, *w = g + 30;
+    double qddo[4], qdo[4];
+    for (int k = 0; k < 4; ++k) {
+        qddo[k] = qdd[k];
+        qdo[k] = qd[k];
+        qd[k] = qdo[k] + (tvvite * tstep) * qddo[k];
+    }
+    // angvelo is that of the last iteration's trial quad, as in the
+    // reference (QuaVelToAngVel precedes each GetAngAcc)
+    for (int it = 0; it < nvvite; ++it) {
+        rig_angvel(q, qd, w);
+        rig_ang_acc(q, qd, torqueo + 3 * ip, w, g + 24, g + 27, qdd);
+        for (int k = 0; k < 4; ++k) qd[k] = qdo[k] + (0.5 * tstep) * (qdd[k] + qddo[k]);
+    }
+    for (int m = 0; m < 3; ++m) angvelo[3 * ip + m] = w[m];
+}
+
+}  // namespace
+
+extern "C" int mg_poly_rigid_setup(mg_poly *c, double tstep, double tvvite, int32_t nvvite, const double *massip,
+                                   const double *momp, const double *ro, const double *qua, const double *rod,
+                                   const double *angvelo, const double *rodd, const double *quadd) {
+    if (!c || !massip || !momp || !ro || !qua || !rod || !angvelo || !rodd || !quadd) return MG_ERR_ARG;
+    if (!(tstep > 0.0) || nvvite < 0) return poly_fail(c, MG_ERR_ARG, "tstep must be > 0 and nvvite >= 0");
+    int np = c->p.np;
+    std::vector<double> h((size_t)kRig * np, 0.0);
+    for (int ip = 0; ip < np; ++ip) {
+        double *g = h.data() + (size_t)kRig * ip;
+        for (int m = 0; m < 3; ++m) {
+            g[m] = ro[3 * ip + m];
+            g[7 + m] = rod[3 * ip + m];
+            g[10 + m] = rodd[3 * ip + m];
+            g[21 + m] = massip[ip];
+            g[24 + m] = momp[3 * ip + m];
+            g[27 + m] = momp[3 * ip + m] > 0.0 ? 1.0 / momp[3 * ip + m] : 0.0;   // InvFlt
+            g[30 + m] = angvelo[3 * ip + m];
+        }
+        for (int k = 0; k < 4; ++k) {
+            g[3 + k] = qua[4 * ip + k];
+            g[17 + k] = quadd[4 * ip + k];
+        }
+    }
+    if (!c->d_rig) POLY_CUDA(c, cudaMalloc(&c->d_rig, sizeof(double) * h.size()));
+    if (!c->d_rig_io) POLY_CUDA(c, cudaMalloc(&c->d_rig_io, sizeof(double) * 15 * (size_t)np));
+    POLY_CUDA(c, cudaMemcpy(c->d_rig, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    k_rigid_setup<<<(np + 127) / 128, 128>>>(np, c->d_rig);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaDeviceSynchronize());
+    c->rig_tstep = tstep;
+    c->rig_tvvite = tvvite;
+    c->rig_nvvite = nvvite;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_rigid_move(mg_poly *c, double *ro, double *ori, double *drostep) {
+    if (!c || !ro || !ori || !drostep) return MG_ERR_ARG;
+    if (!c->d_rig) return poly_fail(c, MG_ERR_STATE, "mg_poly_rigid_setup has not been called");
+    int np = c->p.np;
+    mg_box box;
+    for (int m = 0; m < 3; ++m) {
+        box.len[m] = c->p.boxlen[m];
+        box.half[m] = 0.5 * c->p.boxlen[m];
+        box.inv[m] = 1.0 / c->p.boxlen[m];
+    }
+    double *io = c->d_rig_io;   // ro, ori, drostep
+    k_rigid_move<<<(np + 127) / 128, 128>>>(np, c->rig_tstep, box, c->d_rig, io, io + 3 * np, io + 12 * np);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(ro, io, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(ori, io + 3 * np, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(drostep, io + 12 * np, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
+    return MG_OK;
+}
+
+extern "C" int mg_poly_rigid_kick(mg_poly *c, const double *forceo, const double *torqueo, double *rod,
+                                  double *angvelo) {
+    if (!c || !forceo || !torqueo || !rod || !angvelo) return MG_ERR_ARG;
+    if (!c->d_rig) return poly_fail(c, MG_ERR_STATE, "mg_poly_rigid_setup has not been called");
+    int np = c->p.np;
+    double *io = c->d_rig_io;   // forceo, torqueo, rod, angvelo
+    POLY_CUDA(c, cudaMemcpy(io, forceo, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(io + 3 * np, torqueo, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+    k_rigid_kick<<<(np + 127) / 128, 128>>>(np, c->rig_tstep, c->rig_tvvite, c->rig_nvvite, c->d_rig, io,
+                                           io + 3 * np, io + 6 * np, io + 9 * np);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(rod, io + 6 * np, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(angvelo, io + 9 * np, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
+    return MG_OK;
+}
+
+extern "C" int mg_poly_rigid_prime(mg_poly *c, const double *forceo, const double *torqueo) {
+    if (!c || !forceo || !torqueo) return MG_ERR_ARG;
+    if (!c->d_rig) return poly_fail(c, MG_ERR_STATE, "mg_poly_rigid_setup has not been called");
+    int np = c->p.np;
+    double *io = c->d_rig_io;   // forceo, torqueo; rod, angvelo are written and not read back
+    POLY_CUDA(c, cudaMemcpy(io, forceo, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(io + 3 * np, torqueo, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+    // a kick of zero length: rod and quad stay, rodd and quadd are those of
+    // the current state
+    k_rigid_kick<<<(np + 127) / 128, 128>>>(np, 0.0, 0.0, c->rig_nvvite > 0 ? c->rig_nvvite : 1, c->d_rig, io,
+                                           io + 3 * np, io + 6 * np, io + 9 * np);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaDeviceSynchronize());
+    return MG_OK;
+}
+
+extern "C" int mg_poly_rigid_get(mg_poly *c, double *qua, double *quad) {
+    if (!c || !qua || !quad) return MG_ERR_ARG;
+    if (!c->d_rig) return poly_fail(c, MG_ERR_STATE, "mg_poly_rigid_setup has not been called");
+    int np = c->p.np;
+    std::vector<double> h((size_t)kRig * np);
+    POLY_CUDA(c, cudaMemcpy(h.data(), c->d_rig, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+    for (int ip = 0; ip < np; ++ip)
+        for (int k = 0; k < 4; ++k) {
+            qua[4 * ip + k] = h[(size_t)kRig * ip + 3 + k];
+            quad[4 * ip + k] = h[(size_t)kRig * ip + 13 + k];
+        }
     return MG_OK;
 }

@@ -9,6 +9,13 @@ particle's orientation matrix).  The pair table runs over atom-type pairs:
 PotTwoBodyTab1 (potential.F90:868) with the atom types as its types.
 `PolyEngine.UTwoBodyP` evaluates u%twob, the atom forces and the virial for
 a particle neighbour list (NList's nneighpn, jpnlist).
+
+Rigid-body molecular dynamics (VelVer with lpolyatom, md.F90:252-420):
+`PolySystem.principal_axes` re-expresses each particle type in its
+principal axes (PAxesSystem, particle.F90:2350-2420) with the particles'
+centres at their centres of mass, `PolyEngine.RigidSetup` puts the
+integrator state on the device and `PolyEngine.VelVer` advances it, one
+UTotal per step.
 """
 from dataclasses import dataclass, field
 from typing import List, Optional, Tuple
@@ -20,7 +27,7 @@ from . import abi, units
 from .engine import MolsimError
 from .system import iptpt_matrix
 
-__all__ = ["AtomType", "ParticleType", "PolySystem", "PolyEngine"]
+__all__ = ["AtomType", "ParticleType", "PolySystem", "PolyEngine", "qua_to_ori", "ori_to_qua"]
 
 
 @dataclass
@@ -29,6 +36,51 @@ class AtomType:
     charge: float
     sigma: float
     eps: float
+    mass: float = 1.0     # g/mol (massat)
+
+
+def qua_to_ori(qua):
+    """QuaToOri (mollib.F90:2221-2255) for qua (n, 4): ori (n, 3, 3) with
+    atom position = ro + ori @ local."""
+    q = np.asarray(qua, dtype=np.float64).reshape(-1, 4)
+    q0, q1, q2, q3 = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    o = np.empty((len(q), 3, 3))
+    o[:, 0, 0] = -q2 * q2 + q1 * q1 - q3 * q3 + q0 * q0
+    o[:, 1, 0] = 2.0 * (q0 * q3 - q1 * q2)
+    o[:, 2, 0] = 2.0 * (q1 * q3 + q0 * q2)
+    o[:, 0, 1] = -2.0 * (q1 * q2 + q0 * q3)
+    o[:, 1, 1] = q2 * q2 - q1 * q1 - q3 * q3 + q0 * q0
+    o[:, 2, 1] = 2.0 * (q0 * q1 - q2 * q3)
+    o[:, 0, 2] = 2.0 * (q1 * q3 - q0 * q2)
+    o[:, 1, 2] = -2.0 * (q2 * q3 + q0 * q1)
+    o[:, 2, 2] = -q2 * q2 - q1 * q1 + q3 * q3 + q0 * q0
+    return o
+
+
+def ori_to_qua(ori):
+    """OriToQua (mollib.F90:2166-2212): the quaternion of each orientation
+    matrix from its largest diagonal combination, then normalised."""
+    o = np.asarray(ori, dtype=np.float64).reshape(-1, 3, 3)
+    out = np.empty((len(o), 4))
+    for i, a in enumerate(o):
+        tr = a[0, 0] + a[1, 1] + a[2, 2]
+        d = [0.25 * (1.0 + tr), 0.25 * (1.0 + 2.0 * a[0, 0] - tr), 0.25 * (1.0 + 2.0 * a[1, 1] - tr),
+             0.25 * (1.0 + 2.0 * a[2, 2] - tr)]
+        q = np.empty(4)
+        if d[0] >= d[1] and d[0] >= d[2] and d[0] >= d[3]:
+            q[0] = np.sqrt(d[0]); f = 0.25 / q[0]
+            q[1], q[2], q[3] = f * (a[2, 1] - a[1, 2]), f * (a[2, 0] - a[0, 2]), f * (a[1, 0] - a[0, 1])
+        elif d[1] >= d[2] and d[1] >= d[3] and d[1] >= d[0]:
+            q[1] = np.sqrt(d[1]); f = 0.25 / q[1]
+            q[2], q[3], q[0] = f * (-a[1, 0] - a[0, 1]), f * (a[2, 0] + a[0, 2]), f * (a[2, 1] - a[1, 2])
+        elif d[2] >= d[3] and d[2] >= d[0] and d[2] >= d[1]:
+            q[2] = np.sqrt(d[2]); f = 0.25 / q[2]
+            q[3], q[0], q[1] = f * (-a[2, 1] - a[1, 2]), f * (a[2, 0] - a[0, 2]), f * (-a[1, 0] - a[0, 1])
+        else:
+            q[3] = np.sqrt(d[3]); f = 0.25 / q[3]
+            q[0], q[1], q[2] = f * (a[1, 0] - a[0, 1]), f * (a[2, 0] + a[0, 2]), f * (-a[2, 1] - a[1, 2])
+        out[i] = q / np.sqrt((q * q).sum())
+    return out
 
 
 @dataclass
@@ -100,6 +152,71 @@ class PolySystem:
 
     def aza(self):
         return np.array([self.atom_types[t - 1].charge for t in self.iatan()], dtype=np.float64)
+
+    def type_inertia(self, t):
+        """Mass, centre of mass and inertia tensor of particle type t
+        (0-based) in its local frame (PAxesSystem, particle.F90:2360-2395,
+        with entries below 1e-10 set to zero)."""
+        pt = self.particle_types[t]
+        m = np.array([self.atom_types[a].mass for a, _ in pt.atoms], dtype=np.float64)
+        x = np.array([p for _, p in pt.atoms], dtype=np.float64)
+        mass = float(m.sum())
+        com = (m[:, None] * x).sum(0) / mass
+        d = x - com
+        tpi = np.zeros((3, 3))
+        for k in range(len(m)):
+            tpi += m[k] * (np.dot(d[k], d[k]) * np.eye(3) - np.outer(d[k], d[k]))
+        tpi[np.abs(tpi) < 1e-10] = 0.0
+        return mass, com, tpi
+
+    def principal_axes(self):
+        """The same particles with each type's atoms in its principal axes
+        about its centre of mass (ra, particle.F90:2409-2420), the centres
+        moved to the centres of mass and the orientations composed with the
+        axes, so that every atom stays where it was."""
+        from dataclasses import replace
+        types, com, axes = [], [], []
+        for t, pt in enumerate(self.particle_types):
+            _, c, tpi = self.type_inertia(t)
+            _, e = np.linalg.eigh(tpi)
+            if np.linalg.det(e) < 0.0:
+                e[:, 2] = -e[:, 2]
+            loc = np.array([p for _, p in pt.atoms], dtype=np.float64)
+            ra = (loc - c) @ e
+            types.append(ParticleType(pt.name, [(a, tuple(ra[k])) for k, (a, _) in enumerate(pt.atoms)]))
+            com.append(c)
+            axes.append(e)
+        ti = np.asarray(self.iptpn) - 1
+        com, axes = np.array(com), np.array(axes)
+        ro = self.ro + np.einsum("nij,nj->ni", self.ori, com[ti])
+        ori = np.einsum("nij,njk->nik", self.ori, axes[ti])
+        return replace(self, particle_types=types, ro=np.ascontiguousarray(ro), ori=np.ascontiguousarray(ori),
+                       ubuf=self.ubuf, iubuflow=self.iubuflow, r2umin=self.r2umin, keep={})
+
+    def rigid_props(self, tol=1e-8):
+        """Per particle: inverse mass (massip) and principal moments (momp),
+        for particle types already in their principal axes."""
+        mass, momp = [], []
+        for t in range(self.npt):
+            m, c, tpi = self.type_inertia(t)
+            off = tpi - np.diag(np.diag(tpi))
+            scale = max(1.0, float(np.abs(tpi).max()))
+            if np.abs(c).max() > tol * max(1.0, float(np.abs(c).max()) + 1.0) or np.abs(off).max() > tol * scale:
+                raise ValueError(f"particle type {self.particle_types[t].name!r} is not in its principal axes: "
+                                 "use PolySystem.principal_axes()")
+            mass.append(m)
+            momp.append(np.diag(tpi).copy())
+        ti = np.asarray(self.iptpn) - 1
+        return (np.ascontiguousarray(1.0 / np.array(mass)[ti]), np.ascontiguousarray(np.array(momp)[ti]))
+
+    def kinetic_energy(self, rod, angvelo):
+        """Translational and rotational kinetic energy in kJ/mol for
+        velocities in A/ps and angular velocities (principal frame) in
+        rad/ps: 0.005 * (sum m v^2 + sum I w^2)."""
+        massip, momp = self.rigid_props()
+        rod = np.asarray(rod).reshape(-1, 3)
+        w = np.asarray(angvelo).reshape(-1, 3)
+        return 0.005 * float(((rod * rod).sum(1) / massip).sum()), 0.005 * float((momp * w * w).sum())
 
     @property
     def epsi_four_pi(self):
@@ -353,6 +470,75 @@ class PolyEngine:
         out.update(forceo=ep["forceo"], torqueo=ep["torqueo"])
         out["virial"] += ep["virmolecule"]
         return out
+
+    # ---- rigid-body velocity Verlet ---------------------------------------------
+    def RigidSetup(self, tstep, rod, angvelo, tvvite=0.0, nvvite=2, rodd=None, quadd=None, prime=False):
+        """The integrator state on the device: centres, quaternions
+        (OriToQua of the orientations), velocities (A/ps), angular
+        velocities (principal frame, rad/ps), accelerations (zero unless
+        given, as at the start of a simulation; prime=True takes them from
+        a UTotal of the initial state) and tstep (ps), tvvite, nvvite
+        (nmlMD)."""
+        s = self.s
+        massip, momp = s.rigid_props()
+        qua = ori_to_qua(s.ori)
+        n = s.np_
+        rodd = np.zeros(3 * n) if rodd is None else abi.as_f64(np.asarray(rodd).reshape(-1))
+        quadd = np.zeros(4 * n) if quadd is None else abi.as_f64(np.asarray(quadd).reshape(-1))
+        st = self.lib.mg_poly_rigid_setup(
+            self.h, float(tstep), float(tvvite), int(nvvite), abi.f64(massip), abi.f64(abi.as_f64(momp.reshape(-1))),
+            abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(abi.as_f64(qua.reshape(-1))),
+            abi.f64(abi.as_f64(np.asarray(rod).reshape(-1))), abi.f64(abi.as_f64(np.asarray(angvelo).reshape(-1))),
+            abi.f64(rodd), abi.f64(quadd))
+        self._fail(st, "poly_rigid_setup")
+        if prime:
+            u = self.UTotal()
+            self._fail(self.lib.mg_poly_rigid_prime(self.h, abi.f64(abi.as_f64(u["forceo"].reshape(-1))),
+                                                    abi.f64(abi.as_f64(u["torqueo"].reshape(-1)))),
+                       "poly_rigid_prime")
+        self.rod = np.asarray(rod, dtype=np.float64).reshape(n, 3).copy()
+        self.angvelo = np.asarray(angvelo, dtype=np.float64).reshape(n, 3).copy()
+
+    def VelVer(self, nstep=1, nneighpn=None, jpnlist=None):
+        """nstep steps of VelVer: new centres and orientations on the
+        device, UTotal (the list of a centres handle unless one is given),
+        then the velocity updates.  The system's ro and ori follow.  Returns
+        the last step's UTotal with rod and angvelo."""
+        s = self.s
+        n = s.np_
+        ro = np.zeros(3 * n)
+        ori = np.zeros(9 * n)
+        dro = np.zeros(3 * n)
+        rod = np.zeros(3 * n)
+        w = np.zeros(3 * n)
+        out = None
+        for _ in range(nstep):
+            self._fail(self.lib.mg_poly_rigid_move(self.h, abi.f64(ro), abi.f64(ori), abi.f64(dro)),
+                       "poly_rigid_move")
+            s.ro = ro.reshape(n, 3).copy()
+            s.ori = np.ascontiguousarray(ori.reshape(n, 3, 3).transpose(0, 2, 1))   # ori(3,3,np) column-major
+            out = self.UTotal(nneighpn, jpnlist)
+            self._fail(self.lib.mg_poly_rigid_kick(self.h, abi.f64(abi.as_f64(out["forceo"].reshape(-1))),
+                                                   abi.f64(abi.as_f64(out["torqueo"].reshape(-1))), abi.f64(rod),
+                                                   abi.f64(w)), "poly_rigid_kick")
+        self.rod = rod.reshape(n, 3).copy()
+        self.angvelo = w.reshape(n, 3).copy()
+        out.update(rod=self.rod, angvelo=self.angvelo, drostep=dro.reshape(n, 3).copy())
+        return out
+
+    def RigidState(self):
+        """The device's quaternions and quaternion velocities, (np, 4) each."""
+        n = self.s.np_
+        q = np.zeros(4 * n)
+        qd = np.zeros(4 * n)
+        self._fail(self.lib.mg_poly_rigid_get(self.h, abi.f64(q), abi.f64(qd)), "poly_rigid_get")
+        return q.reshape(n, 4), qd.reshape(n, 4)
+
+    def _fail(self, st, what):
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.lib.mg_poly_last_error(self.h, buf, 512)
+            raise MolsimError(st, f"{what}: {buf.value.decode(errors='replace')}")
 
     def close(self):
         for k in ("_atoms", "_centres"):

@@ -47,5 +47,13 @@ def oracle():
         lib.orc_poly_utwobody.restype = C.c_int
         lib.orc_poly_utwobody.argtypes = [C.POINTER(abi.MgPolyParams), C.c_int32, abi.PF64, abi.PF64, abi.PI32,
                                           abi.PI32, abi.PF64, abi.PF64, abi.PF64]
+        lib.orc_angvel_to_quavel.restype = C.c_int
+        lib.orc_angvel_to_quavel.argtypes = [C.c_int32, abi.PF64, abi.PF64, abi.PF64]
+        lib.orc_rigid_move.restype = C.c_int
+        lib.orc_rigid_move.argtypes = [C.c_int32, C.c_double, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64,
+                                       abi.PF64, abi.PF64, abi.PF64, abi.PF64]
+        lib.orc_rigid_kick.restype = C.c_int
+        lib.orc_rigid_kick.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_int32, abi.PF64, abi.PF64, abi.PF64,
+                                       abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64]
         _lib = lib
     return _lib

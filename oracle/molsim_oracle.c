@@ -1864,6 +1864,122 @@ int orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force
     return 0;
 }
 
+/* ---- rigid-body velocity Verlet (VelVer, md.F90:252-420, lpolyatom) ----
+   Stateless: the caller holds ro(3,np), qua(0:3,np), rod, rodd, quad, quadd,
+   angvelo; each routine updates them in place, loop by loop as VelVer
+   does. */
+
+/* QuaToOri, mollib.F90:2221-2255: ori(3,3,np), column-major */
+static void rigid_qua_to_ori(const double *q, double *ori) {
+    double qua00 = q[0] * q[0], qua11 = q[1] * q[1], qua22 = q[2] * q[2], qua33 = q[3] * q[3];
+    double qua01 = q[0] * q[1], qua02 = q[0] * q[2], qua03 = q[0] * q[3];
+    double qua12 = q[1] * q[2], qua13 = q[1] * q[3], qua23 = q[2] * q[3];
+    ori[0] = -qua22 + qua11 - qua33 + qua00;      /* ori(1,1) */
+    ori[1] = Two * (qua03 - qua12);               /* ori(2,1) */
+    ori[2] = Two * (qua13 + qua02);               /* ori(3,1) */
+    ori[3] = -Two * (qua12 + qua03);              /* ori(1,2) */
+    ori[4] = qua22 - qua11 - qua33 + qua00;       /* ori(2,2) */
+    ori[5] = Two * (qua01 - qua23);               /* ori(3,2) */
+    ori[6] = Two * (qua13 - qua02);               /* ori(1,3) */
+    ori[7] = -Two * (qua23 + qua01);              /* ori(2,3) */
+    ori[8] = -qua22 - qua11 + qua33 + qua00;      /* ori(3,3) */
+}
+
+/* AngVelToQuaVel, mollib.F90:2621-2642 */
+int orc_angvel_to_quavel(int32_t np, const double *qua, const double *angvelo, double *quad) {
+    for (int ip = 0; ip < np; ++ip) {
+        const double *q = &qua[4 * ip], *w = &angvelo[3 * ip];
+        double *d = &quad[4 * ip];
+        d[0] = Half * (-q[1] * w[0] + q[2] * w[1] - q[3] * w[2]);
+        d[1] = Half * (+q[0] * w[0] - q[3] * w[1] - q[2] * w[2]);
+        d[2] = Half * (-q[3] * w[0] - q[0] * w[1] + q[1] * w[2]);
+        d[3] = Half * (+q[2] * w[0] + q[1] * w[1] + q[0] * w[2]);
+    }
+    return 0;
+}
+
+/* VelVer's first part (md.F90:288-306): drostep, ro with PBC (box-like
+   cell, molaux.F90:104-118), qua, QuaNorm (mollib.F90:2594-2612),
+   QuaToOri */
+int orc_rigid_move(int32_t np, double tstep, const double *boxlen, double *ro, double *qua, const double *rod,
+                   const double *rodd, const double *quad, const double *quadd, double *drostep, double *ori) {
+    double fac = Half * (tstep * tstep);
+    for (int ip = 0; ip < np; ++ip) {
+        for (int m = 0; m < 3; ++m) {
+            drostep[3 * ip + m] = tstep * rod[3 * ip + m] + fac * rodd[3 * ip + m];
+            ro[3 * ip + m] = ro[3 * ip + m] + drostep[3 * ip + m];
+            double x = ro[3 * ip + m];
+            if (fabs(x) > Half * boxlen[m]) x = x - boxlen[m] * round(x * (One / boxlen[m]));
+            ro[3 * ip + m] = x;
+        }
+    }
+    for (int ip = 0; ip < np; ++ip)
+        for (int k = 0; k < 4; ++k)
+            qua[4 * ip + k] = qua[4 * ip + k] + tstep * quad[4 * ip + k] + fac * quadd[4 * ip + k];
+    for (int ip = 0; ip < np; ++ip) {
+        double *q = &qua[4 * ip];
+        double norm = One / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+        for (int k = 0; k < 4; ++k) q[k] = q[k] * norm;
+        rigid_qua_to_ori(q, &ori[9 * ip]);
+    }
+    return 0;
+}
+
+/* VelVer's second part (md.F90:347-402): GetLinAcc (md.F90:601-617), rod;
+   quaddo, quado, the trial quad, nvvite times QuaVelToAngVel
+   (mollib.F90:2651-2669), GetAngAcc (md.F90:628-663) and quad.  momp are
+   the principal moments; momip = InvFlt(momp) (mollib.F90:2814-2819). */
+int orc_rigid_kick(int32_t np, double tstep, double tvvite, int32_t nvvite, const double *massip,
+                   const double *momp, const double *qua, const double *forceo, const double *torqueo, double *rod,
+                   double *rodd, double *quad, double *quadd, double *angvelo) {
+    for (int ip = 0; ip < np; ++ip)
+        for (int m = 0; m < 3; ++m) {
+            double roddo = rodd[3 * ip + m];
+            rodd[3 * ip + m] = massip[ip] * forceo[3 * ip + m];
+            rod[3 * ip + m] = rod[3 * ip + m] + Half * tstep * (rodd[3 * ip + m] + roddo);
+        }
+    double *quaddo = (double *)malloc(sizeof(double) * 4 * (size_t)(np > 0 ? np : 1));
+    double *quado = (double *)malloc(sizeof(double) * 4 * (size_t)(np > 0 ? np : 1));
+    if (!quaddo || !quado) { free(quaddo); free(quado); return MG_ERR_ALLOC; }
+    for (int k = 0; k < 4 * np; ++k) quaddo[k] = quadd[k];
+    for (int k = 0; k < 4 * np; ++k) {
+        quado[k] = quad[k];
+        quad[k] = quado[k] + (tvvite * tstep) * quaddo[k];
+    }
+    for (int it = 1; it <= nvvite; ++it) {
+        for (int ip = 0; ip < np; ++ip) {   /* QuaVelToAngVel */
+            const double *q = &qua[4 * ip], *d = &quad[4 * ip];
+            double *w = &angvelo[3 * ip];
+            w[0] = Two * (-q[3] * d[2] + q[0] * d[1] + q[2] * d[3] - q[1] * d[0]);
+            w[1] = Two * (-q[0] * d[2] - q[3] * d[1] + q[1] * d[3] + q[2] * d[0]);
+            w[2] = Two * (+q[1] * d[2] - q[2] * d[1] + q[0] * d[3] - q[3] * d[0]);
+        }
+        for (int ip = 0; ip < np; ++ip) {   /* GetAngAcc */
+            const double *q = &qua[4 * ip], *d = &quad[4 * ip], *tq = &torqueo[3 * ip], *w = &angvelo[3 * ip];
+            const double *mp = &momp[3 * ip];
+            double ori[9], mi[3];
+            for (int m = 0; m < 3; ++m) mi[m] = mp[m] > Zero ? One / mp[m] : Zero;
+            rigid_qua_to_ori(q, ori);
+            double tor1 = tq[0] * ori[0] + tq[1] * ori[1] + tq[2] * ori[2];
+            double tor2 = tq[0] * ori[3] + tq[1] * ori[4] + tq[2] * ori[5];
+            double tor3 = tq[0] * ori[6] + tq[1] * ori[7] + tq[2] * ori[8];
+            double a1 = (tor1 + w[1] * w[2] * (mp[1] - mp[2])) * mi[0];
+            double a2 = (tor2 + w[2] * w[0] * (mp[2] - mp[0])) * mi[1];
+            double a3 = (tor3 + w[0] * w[1] * (mp[0] - mp[1])) * mi[2];
+            double fac = -Two * (d[2] * d[2] + d[1] * d[1] + d[3] * d[3] + d[0] * d[0]);
+            double *dd = &quadd[4 * ip];
+            dd[0] = Half * (-q[1] * a1 + q[2] * a2 - q[3] * a3 + q[0] * fac);
+            dd[1] = Half * (+q[0] * a1 - q[3] * a2 - q[2] * a3 + q[1] * fac);
+            dd[2] = Half * (-q[3] * a1 - q[0] * a2 + q[1] * a3 + q[2] * fac);
+            dd[3] = Half * (+q[2] * a1 + q[1] * a2 + q[0] * a3 + q[3] * fac);
+        }
+        for (int k = 0; k < 4 * np; ++k) quad[k] = quado[k] + (Half * tstep) * (quadd[k] + quaddo[k]);
+    }
+    free(quaddo);
+    free(quado);
+    return 0;
+}
+
 /* the energy terms of the last UTotal: u%tot, u%twob(0), u%rec, u%bond,
    u%angle, virial */
 int orc_energy_terms(orc_sys *s, double *terms) {
