@@ -180,6 +180,20 @@ int mg_get_positions(mg_handle *h, double *ro);
 int mg_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew,
                  double *phi, double *esum);
 
+/* The reciprocal part of UDipoleEwald (energy.F90:1807-1830) for charges
+ * and point dipoles, on an FP64 handle with Ewald whose particles are the
+ * atoms (positions from mg_set_positions, charges az): UDipoleEwaldRecStd
+ * (energy.F90:1830-2040: structure factors of q + i k.dip, then per atom
+ * the potential, field and field gradient of each k-vector) or
+ * UDipoleEwaldRecSPM (:2046-2170: the generalized charge mesh through the
+ * B-spline derivatives, SPMFFTRec, then the potential, field and field
+ * gradient through the first and second derivatives), followed by the
+ * atomic part of UDipoleEwaldSelf (:2183-2191).  dip[3*np] in the lab
+ * frame; potstat[np], estat[3*np], efg[6*np] and *virelec are added to, as
+ * the reference adds to the real-space part (mg_poly_udipole_real). */
+int mg_dipole_ewald(mg_handle *h, const double *dip, double *potstat, double *estat, double *efg,
+                    double *virelec);
+
 /* ---- neighbour lists (A1-A4) --------------------------------------------- */
 
 /* NList(iWriteInput) (nlist.F90:553-596): builds the Verlet list
@@ -419,12 +433,46 @@ int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const double *r, const
                             const int32_t *jpnlist, int32_t ntrial, const int32_t *ip, const double *rotm,
                             const double *rtm, double *du_twob, int32_t *lhsoverlap);
 /* The end of UTotal for polyatomic particles (energy.F90:405-427): from
- * the total atom forces force[3*na] (unscaled) and the atom and particle
- * positions, the particle forces forceo[3*np] and torques torqueo[3*np]
- * (both scaled by force_fac, atoms summed in order per particle) and the
- * molecular virial sum (r_a - ro_p) . f_a into *virmolecule. */
-int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force, double force_fac,
-                     double *forceo, double *torqueo, double *virmolecule);
+ * the total atom forces force[3*na] (unscaled), the atom torques
+ * torque[3*na] of the dipole electrostatics (NULL when there are none) and
+ * the atom and particle positions, the particle forces forceo[3*np] and
+ * torques torqueo[3*np] (both scaled by force_fac, atoms summed in order
+ * per particle) and the molecular virial sum (r_a - ro_p) . f_a into
+ * *virmolecule. */
+int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force, const double *torque,
+                     double force_fac, double *forceo, double *torqueo, double *virmolecule);
+/* Charges and point dipoles of the atoms (UDipole, energy.F90:1476-1579),
+ * in the reference's order of calls:
+ *   mg_poly_udipole_real    UDipoleP (energy.F90:1588-1798): the atom pairs
+ *                           of the particle pairs in the list (NList's
+ *                           nneighpn, jpnlist; PBC2 shift of the centres),
+ *                           erfc-screened with Ewald (ualpha > 0), bare
+ *                           otherwise; sets potstat[na], estat[3*na],
+ *                           efg[6*na] (xx, yy, zz, xy, xz, yz) and
+ *                           *virelec; *u_real = EpsiFourPi/2 sum (q pot -
+ *                           dip . e) of this part (UDipole's ureal)
+ *   mg_dipole_ewald         UDipoleEwaldRecStd / UDipoleEwaldRecSPM and the
+ *                           atomic part of UDipoleEwaldSelf, on a handle
+ *                           of the atoms (below)
+ *   mg_poly_udipole_self    the molecular part of UDipoleEwaldSelf
+ *                           (energy.F90:2196-2268) and, with lsurf,
+ *                           UDipoleEwaldSurf (:2272-2295, the atom
+ *                           positions r as they are)
+ *   mg_poly_udipole_finish  UDipole's loop (:1510-1545): *u_stat, the atom
+ *                           forces added to force[3*na] (EpsiFourPi (q e +
+ *                           dip . efg)) and torques added to torque[3*na]
+ *                           (EpsiFourPi dip x e)
+ * dip[3*na] are the atoms' dipoles in the lab frame (e A); the atom charges
+ * are mg_poly_params.aza.  The arrays are read and written on the host at
+ * every call.  The pair table of a dipole system holds no Coulomb term
+ * (PotTwoBodyTab with ldipole, potential.F90:1380). */
+int mg_poly_udipole_real(mg_poly *c, const double *ro, const double *r, const double *dip, const int32_t *nneighpn,
+                         const int32_t *jpnlist, double *potstat, double *estat, double *efg, double *virelec,
+                         double *u_real);
+int mg_poly_udipole_self(mg_poly *c, const double *r, const double *dip, int32_t lsurf, double *potstat,
+                         double *estat, double *efg, double *virelec);
+int mg_poly_udipole_finish(mg_poly *c, const double *dip, const double *potstat, const double *estat,
+                           const double *efg, double *force, double *torque, double *u_stat);
 /* Rigid-body velocity Verlet of the polyatomic particles (VelVer with
  * lpolyatom, md.F90:252-420): the state lives on the device.  Set-up takes
  * the inverse masses massip[np], the principal moments momp[3*np], the

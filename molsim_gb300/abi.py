@@ -96,6 +96,7 @@ LIB_ONLY = [
     ("dutotal_batch", C.c_int, [H, C.c_int32, PI32, PF64, PF64, PI32]),
     ("nlist_calls", C.c_int, [H, PI32]),
     ("fft_check", C.c_int, [H, PF64, PF64, PF64, PF64, PF64]),
+    ("dipole_ewald", C.c_int, [H, PF64, PF64, PF64, PF64, PF64]),
     ("bd_step_host", C.c_int, [H, PF64, PF64, PF64]),
     ("phase_times", C.c_int, [H, PF64, C.c_int32, PI32, C.c_char_p, C.c_size_t]),
     ("phase_reset", C.c_int, [H, C.c_int32]),
@@ -112,7 +113,10 @@ LIB_ONLY = [
     ("poly_utwobody", C.c_int, [H, PF64, PF64, PI32, PI32, PF64, PF64, PF64]),
     ("poly_ewald_intra", C.c_int, [H, PF64, PF64, PF64]),
     ("poly_utwobody_list", C.c_int, [H, H, PF64, PF64, PF64, PF64]),
-    ("poly_epilogue", C.c_int, [H, PF64, PF64, PF64, C.c_double, PF64, PF64, PF64]),
+    ("poly_epilogue", C.c_int, [H, PF64, PF64, PF64, PF64, C.c_double, PF64, PF64, PF64]),
+    ("poly_udipole_real", C.c_int, [H, PF64, PF64, PF64, PI32, PI32, PF64, PF64, PF64, PF64, PF64]),
+    ("poly_udipole_self", C.c_int, [H, PF64, PF64, C.c_int32, PF64, PF64, PF64, PF64]),
+    ("poly_udipole_finish", C.c_int, [H, PF64, PF64, PF64, PF64, PF64, PF64, PF64]),
     ("poly_dutwobody_batch", C.c_int, [H, PF64, PF64, PI32, PI32, C.c_int32, PI32, PF64, PF64, PF64, PI32]),
     ("poly_rigid_setup", C.c_int, [H, C.c_double, C.c_double, C.c_int32, PF64, PF64, PF64, PF64, PF64, PF64,
                                    PF64, PF64]),

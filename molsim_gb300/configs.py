@@ -298,6 +298,24 @@ def replica_set(seed=5, nrep=256, nmin=500, nmax=8000, cmin=0.01, cmax=1.0, rcut
     return out
 
 
+def dipolar_waters(seed=9, nwater=200, nsalt=10, L=22.0, rcut=9.0, rmin=3.0, ewald=abi.MG_EWALD_SPM,
+                   ualpha=0.35, order=6, nmesh=32, ncut=8):
+    """Rigid three-site waters whose atoms carry charges and point dipoles
+    (txelec = 'dip': UDipole takes the electrostatics, the pair table only
+    the LJ term), with NaCl ion pairs as one-atom particles; relative
+    permittivity 1, Ewald over the atoms.  The dipoles lie in the molecular
+    plane: on O along the symmetry axis, on the H atoms along their bonds."""
+    s = water_ions(seed=seed, nwater=nwater, nsalt=nsalt, L=L, rcut=rcut, rmin=rmin)
+    s.atom_types[0].charge, s.atom_types[1].charge = -0.66, 0.33
+    w = s.particle_types[0]
+    ho = np.array(w.atoms[1][1]) - np.array(w.atoms[0][1])
+    ho2 = np.array(w.atoms[2][1]) - np.array(w.atoms[0][1])
+    w.dipoles = [(0.0, 0.0, -0.11), tuple(0.06 * ho / np.linalg.norm(ho)), tuple(0.06 * ho2 / np.linalg.norm(ho2))]
+    s.txelec = "dip"
+    s.ewald, s.ualpha, s.order, s.nmesh, s.ncut = ewald, ualpha, order, nmesh, ncut
+    return s
+
+
 def water_ions(seed=9, nwater=300, nsalt=20, L=24.0, rcut=9.0, rmin=3.0):
     """A polyatomic system for the UTwoBodyP path: rigid three-site waters
     (O and two H, SPC/E-like charges and geometry) and NaCl ion pairs as

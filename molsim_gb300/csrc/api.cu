@@ -6,6 +6,7 @@
 // A handle owns one CUDA stream; every call queues its kernels on it and
 // returns after a synchronisation that also reads the device error word.  The
 // multi-step MD/BD entry points capture one step as a CUDA graph and replay it.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -120,7 +121,7 @@ static void free_all(mg_handle *h) {
                     h->d_bin_kstart, h->d_brick_count, h->d_brick_perm, h->d_brick_rank,
                     h->d_brick_of, h->d_brick_start, h->d_brick_istart, h->d_item_brick, h->d_tiles, h->d_grad, h->d_f32_tabs, h->d_pos_f,
                     h->d_cell_s, h->d_spl_w, h->d_ffx2, h->d_force2, h->d_ro_slot, h->d_ro_slot_f, h->d_scan_tiles,
-                    h->d_spl_plane};
+                    h->d_spl_plane, h->d_dip_scr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -232,6 +233,7 @@ static int create_impl(const mg_params *p, mg_handle *h) {
     MG_CUDA(h, cudaMalloc(&h->d_ro, sizeof(double) * 3 * np));
     MG_CUDA(h, cudaMemset(h->d_ro, 0, sizeof(double) * 3 * np));
     MG_TRY(upload(h, &h->d_az, p->az, np));
+    for (int i = 0; i < np; ++i) h->az_absmax = std::max(h->az_absmax, std::fabs(p->az[i]));
     MG_TRY(upload(h, &h->d_type, h->h_type.data(), np));
     MG_TRY(upload(h, &h->d_pairidx, h->h_pairidx.data(), h->h_pairidx.size()));
     MG_TRY(upload(h, &h->d_ubuf, p->ubuf, p->nbuf));

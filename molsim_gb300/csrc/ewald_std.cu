@@ -150,7 +150,138 @@ __global__ void __launch_bounds__(128) k_fk(const double2 *__restrict__ eik,
     }
 }
 
+// UDipoleEwaldRecStd (energy.F90:1830-2040, serial branch :1960-2036), one
+// block per k-vector: the structure factors of charges and dipoles, S with
+// (q + i k.dip) and Sd with i k.dip in the four sign combinations, and the
+// k-vector's virial term -kfac (2 sum(Re Sd Re S + Im Sd Im S) + |S|^2 (1 -
+// k^2 / (2 alpha^2)))
+__global__ void __launch_bounds__(256) k_dip_sk(const double2 *__restrict__ eik, const double *__restrict__ az,
+                                                const double *__restrict__ dip, int np, int ncut,
+                                                const int4 *__restrict__ kv, const double *__restrict__ kfac,
+                                                double3 tpbi, double ualpha2, double2 *__restrict__ S,
+                                                double *__restrict__ vir) {
+    __shared__ double sh[16][8];
+    int k = blockIdx.x;
+    int4 n = kv[k];
+    double kx = n.x * tpbi.x, ky = n.y * tpbi.y, kz = n.z * tpbi.z;
+    double acc[16];
+#pragma unroll
+    for (int v = 0; v < 16; ++v) acc[v] = 0.0;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+        double2 er[4];
+        eikr4(eik, np, ncut, p, n.x, n.y, n.z, 1.0, er);
+        double tx = kx * dip[3 * p], ty = ky * dip[3 * p + 1], tz = kz * dip[3 * p + 2];
+        double fac[4] = {-tx - ty + tz, -tx + ty + tz, +tx - ty + tz, +tx + ty + tz};
+        double q = az[p];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            // (q + i f) e and (i f) e
+            acc[2 * c] += q * er[c].x - fac[c] * er[c].y;
+            acc[2 * c + 1] += q * er[c].y + fac[c] * er[c].x;
+            acc[8 + 2 * c] += -fac[c] * er[c].y;
+            acc[8 + 2 * c + 1] += fac[c] * er[c].x;
+        }
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int v = 0; v < 16; ++v) {
+        double x = acc[v];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[v][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int nw = blockDim.x >> 5;
+        double t[16];
+        for (int v = 0; v < 16; ++v) {
+            double x = 0.0;
+            for (int q = 0; q < nw; ++q) x += sh[v][q];
+            t[v] = x;
+        }
+        double termx = 0.0, termy = 0.0;
+        for (int c = 0; c < 4; ++c) {
+            S[4 * k + c] = make_double2(t[2 * c], t[2 * c + 1]);
+            termx = termx + (t[8 + 2 * c] * t[2 * c] + t[8 + 2 * c + 1] * t[2 * c + 1]);
+            termy = termy + (t[2 * c] * t[2 * c] + t[2 * c + 1] * t[2 * c + 1]);
+        }
+        double termz = 1.0 - (kx * kx + ky * ky + kz * kz) / (2.0 * ualpha2);
+        vir[k] = -(kfac[k] * (2.0 * termx + termy * termz));
+    }
+}
+
+// the potential, field and field gradient of every k-vector at each atom
+// (one thread per atom, the k-vectors in order, S staged in shared memory);
+// added to pot[np], est[3 np], efg[6 np]
+__global__ void __launch_bounds__(128) k_dip_fk(const double2 *__restrict__ eik, int np, int ncut,
+                                                const int4 *__restrict__ kv, const double *__restrict__ kfac,
+                                                const double2 *__restrict__ S, int nk, double3 tpbi,
+                                                double *__restrict__ pot, double *__restrict__ est,
+                                                double *__restrict__ efg) {
+    constexpr int CH = 128;
+    __shared__ double2 sS[CH][4];
+    __shared__ int4 sK[CH];
+    __shared__ double sF[CH];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double ps = 0.0, e0 = 0.0, e1 = 0.0, e2 = 0.0, g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k0 = 0; k0 < nk; k0 += CH) {
+        int cnt = min(CH, nk - k0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            sK[e] = kv[k0 + e];
+            sF[e] = kfac[k0 + e];
+            for (int c = 0; c < 4; ++c) sS[e][c] = S[4 * (k0 + e) + c];
+        }
+        __syncthreads();
+        if (p < np) {
+            for (int e = 0; e < cnt; ++e) {
+                int4 n = sK[e];
+                double2 er[4];
+                eikr4(eik, np, ncut, p, n.x, n.y, n.z, 1.0, er);
+                // c = e_c conj(S_c)
+                double2 cc[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) cc[c] = zmul(er[c], zconj(sS[e][c]));
+                double kfac2 = 2.0 * sF[e];
+                double kx = n.x * tpbi.x, ky = n.y * tpbi.y, kz = n.z * tpbi.z;
+                double rsum = cc[0].x + cc[1].x + cc[2].x + cc[3].x;
+                ps += kfac2 * rsum;
+                e0 += kfac2 * kx * (-cc[0].y - cc[1].y + cc[2].y + cc[3].y);
+                e1 += kfac2 * ky * (-cc[0].y + cc[1].y - cc[2].y + cc[3].y);
+                e2 += kfac2 * kz * (+cc[0].y + cc[1].y + cc[2].y + cc[3].y);
+                g[0] += (kfac2 * kx * kx) * rsum;
+                g[1] += (kfac2 * ky * ky) * rsum;
+                g[2] += (kfac2 * kz * kz) * rsum;
+                g[3] += (kfac2 * kx * ky) * (+cc[0].x - cc[1].x - cc[2].x + cc[3].x);
+                g[4] += (kfac2 * kx * kz) * (-cc[0].x - cc[1].x + cc[2].x + cc[3].x);
+                g[5] += (kfac2 * ky * kz) * (-cc[0].x + cc[1].x - cc[2].x + cc[3].x);
+            }
+        }
+    }
+    if (p >= np) return;
+    pot[p] += ps;
+    est[3 * p] += e0;
+    est[3 * p + 1] += e1;
+    est[3 * p + 2] += e2;
+    for (int m = 0; m < 6; ++m) efg[6 * p + m] += g[m];
+}
+
 }  // namespace
+
+// the reciprocal part of UDipoleEwald, standard Ewald: device arrays dip,
+// pot, est, efg of the handle's particles (added to), vir[nkvec] per
+// k-vector virial terms
+int mg_ewald_std_dipole(mg_handle *h, const double *dip, double *pot, double *est, double *efg, double *vir) {
+    int np = h->np;
+    double3 tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
+    k_eik<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_ro, np, h->ncut, tpbi, h->d_eik);
+    k_dip_sk<<<h->nkvec, 256, 0, h->st>>>(h->d_eik, h->d_az, dip, np, h->ncut, h->d_kvec, h->d_kfac, tpbi,
+                                          h->ualpha * h->ualpha, h->d_S, vir);
+    k_dip_fk<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_eik, np, h->ncut, h->d_kvec, h->d_kfac, h->d_S, h->nkvec,
+                                                  tpbi, pot, est, efg);
+    h->launches += 3;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
 
 int mg_ewald_std_init(mg_handle *h) {
     std::vector<int> kv;

@@ -159,6 +159,10 @@ struct mg_handle {
     int plane_fused = 0;
     int plane_shift = 30;           // fused spread: stamp values to integers (2^plane_shift)
     float *d_spl_plane = nullptr;   // fused spread: the spread records in plane order
+    // dipole electrostatics (mg_dipole_ewald): dip, pot, est, efg, virial terms
+    double *d_dip_scr = nullptr;
+    size_t dip_scr_n = 0;
+    double az_absmax = 0.0;          // max |q| of the particles
     int brick = 0, nbrick_edge = 0, nbricks = 0;
     size_t spread_smem = 0, gather_smem = 0;
     int fx_shift = 30, fx_shift64 = 48;
@@ -392,6 +396,9 @@ int mg_ewald_std_launch(mg_handle *h);
 
 double mg_spme_fx_scale(const mg_handle *h);
 int mg_spme_potential(mg_handle *h);
+int mg_spme_dipole(mg_handle *h, const double *dip, double bound, double *pot, double *est, double *efg,
+                   double *vir);
+int mg_ewald_std_dipole(mg_handle *h, const double *dip, double *pot, double *est, double *efg, double *vir);
 int mg_spme_load_mesh(mg_handle *h, const double *q);
 int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul);
 int mg_spme_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew, double *phi,

@@ -295,7 +295,8 @@ __global__ void k_poly_dutwobody(PolyArgs a, int ntrial, const int *__restrict__
 
 // the end of UTotal: one thread per particle over its atoms in order
 __global__ void __launch_bounds__(kPolyThreads) k_poly_epilogue(PolyArgs a, double fac, double *__restrict__ fo,
-                                                                double *__restrict__ to) {
+                                                                double *__restrict__ to,
+                                                                const double *__restrict__ tqa) {
     __shared__ double red[kPolyThreads];
     double vir = 0.0;
     int ip = blockIdx.x * blockDim.x + threadIdx.x;
@@ -315,6 +316,8 @@ __global__ void __launch_bounds__(kPolyThreads) k_poly_epilogue(PolyArgs a, doub
             tq[0] = __dadd_rn(tq[0], __dsub_rn(__dmul_rn(dy, gz), __dmul_rn(dz, gy)));
             tq[1] = __dadd_rn(tq[1], __dsub_rn(__dmul_rn(dz, gx), __dmul_rn(dx, gz)));
             tq[2] = __dadd_rn(tq[2], __dsub_rn(__dmul_rn(dx, gy), __dmul_rn(dy, gx)));
+            if (tqa)   // the atom's own torque (dipoles), scaled like the forces
+                for (int m = 0; m < 3; ++m) tq[m] = __dadd_rn(tq[m], __dmul_rn(tqa[3 * ia + m], fac));
         }
         for (int m = 0; m < 3; ++m) {
             fo[3 * ip + m] = f[m];
@@ -430,6 +433,240 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p_list(PolyArgs a, con
     }
 }
 
+// ---- charges and point dipoles (UDipoleP energy.F90:1588-1798, UDipoleEwaldSelf
+// :2175-2268, UDipoleEwaldSurf :2272-2295, UDipole's loop :1510-1545) ----------
+// potstat, estat (3), efg (6: xx, yy, zz, xy, xz, yz) per atom, FP64.
+
+struct DipTerms {
+    double p, e[3], g[6];
+};
+
+// the potential, field and field gradient at atom i from atom j (charge qj,
+// dipole dj) and at j from i, for d = r_i - r_j and the radial kernels
+// r1i .. r7i; vv is the pair's virial term (-q_i e_i . d - dip_i . efg_i . d)
+__device__ __forceinline__ void dip_pair_terms(const double d[3], double qi, const double *di, double qj,
+                                               const double *dj, double r1i, double r3i, double r5i, double r7i,
+                                               DipTerms &oi, DipTerms &oj, double &vv) {
+    double threer5i = 3.0 * r5i;
+    double doti = di[0] * d[0] + di[1] * d[1] + di[2] * d[2];
+    double dotj = dj[0] * d[0] + dj[1] * d[1] + dj[2] * d[2];
+    double dotir5i = 3.0 * r5i * doti, dotjr5i = 3.0 * r5i * dotj;
+    double dotir7i = 15.0 * r7i * doti, dotjr7i = 15.0 * r7i * dotj;
+    oi.p = qj * r1i + dotj * r3i;
+    oj.p = qi * r1i - doti * r3i;
+    for (int m = 0; m < 3; ++m) {
+        oi.e[m] = (qj * d[m] - dj[m]) * r3i + dotjr5i * d[m];
+        oj.e[m] = (-qi * d[m] - di[m]) * r3i + dotir5i * d[m];
+    }
+    vv = -qi * (oi.e[0] * d[0] + oi.e[1] * d[1] + oi.e[2] * d[2]);
+    for (int m = 0; m < 3; ++m) {
+        double dm2 = d[m] * d[m];
+        oi.g[m] = qj * r3i + (-qj * dm2 + 2.0 * dj[m] * d[m] + dotj) * threer5i - dotjr7i * dm2;
+        oj.g[m] = qi * r3i + (-qi * dm2 - 2.0 * di[m] * d[m] - doti) * threer5i + dotir7i * dm2;
+    }
+    const int A[3] = {0, 0, 1}, B[3] = {1, 2, 2};
+    for (int k = 0; k < 3; ++k) {
+        int x = A[k], y = B[k];
+        double dxy = d[x] * d[y];
+        oi.g[3 + k] = (-qj * dxy + dj[x] * d[y] + dj[y] * d[x]) * threer5i - dotjr7i * dxy;
+        oj.g[3 + k] = (-qi * dxy - di[x] * d[y] - di[y] * d[x]) * threer5i + dotir7i * dxy;
+    }
+    // dip_i . efg_i . d with efg symmetric (xx yy zz xy xz yz)
+    const double *g = oi.g;
+    double gd0 = g[0] * d[0] + g[3] * d[1] + g[4] * d[2];
+    double gd1 = g[3] * d[0] + g[1] * d[1] + g[5] * d[2];
+    double gd2 = g[4] * d[0] + g[5] * d[1] + g[2] * d[2];
+    vv -= di[0] * gd0 + di[1] * gd1 + di[2] * gd2;
+}
+
+struct DipArgs {
+    const double *az, *dip;
+    double *pot, *est, *efg;
+    double ualpha, ualpha2, f1, f2, f3;
+    int lewald;
+};
+
+__device__ __forceinline__ void dip_add_atomic(const DipArgs &q, int ia, const DipTerms &t) {
+    atomicAdd(&q.pot[ia], t.p);
+    for (int m = 0; m < 3; ++m) atomicAdd(&q.est[3 * ia + m], t.e[m]);
+    for (int m = 0; m < 6; ++m) atomicAdd(&q.efg[6 * ia + m], t.g[m]);
+}
+
+// UDipoleP: one warp per particle, lanes over its list row; for each of the
+// particle's atoms the lanes' sums are combined by shuffles, the partner
+// atoms' terms added with FP64 atomics; the virial per block
+__global__ void __launch_bounds__(kPolyThreads) k_dipole_real(PolyArgs a, DipArgs q) {
+    __shared__ double red[kPolyThreads];
+    double vir = 0.0;
+    int ip = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (ip < a.np) {
+        int ipt = a.iptpn[ip];
+        int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[ipt - 1];
+        int nn = a.nneighpn[ip];
+        for (int ia = ialow; ia < iaupp; ++ia) {
+            DipTerms acc = {};
+            double qi = q.az[ia];
+            const double *di = q.dip + 3 * ia;
+            for (int jploc = lane; jploc < nn; jploc += 32) {
+                int jp = a.jpnlist[(size_t)ip * a.maxnneigh + jploc] - 1;
+                if (a.lmc && jp < ip) continue;
+                int jpt = a.iptpn[jp];
+                double dc[3], sh[3];
+                for (int m = 0; m < 3; ++m) {
+                    dc[m] = a.ro[3 * ip + m] - a.ro[3 * jp + m];
+                    sh[m] = fabs(dc[m]) > a.half[m] ? copysign(a.len[m], dc[m]) : 0.0;   // PBC2
+                    dc[m] = dc[m] - sh[m];
+                }
+                if (dc[0] * dc[0] + dc[1] * dc[1] + dc[2] * dc[2] > a.rcut2) continue;
+                int jalow = a.ianpn[jp] - 1, jaupp = jalow + a.napt[jpt - 1];
+                for (int ja = jalow; ja < jaupp; ++ja) {
+                    double d[3];
+                    for (int m = 0; m < 3; ++m) d[m] = a.r[3 * ia + m] - a.r[3 * ja + m] - sh[m];
+                    double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                    double r1 = sqrt(r2), r1i = 1.0 / r1, r2i = r1i * r1i, r3i, r5i, r7i;
+                    if (q.lewald) {
+                        double ex = exp(-q.ualpha2 * r2);
+                        r1i = r1i * (1.0 - mg_erf2(q.ualpha * r1));
+                        r3i = r2i * (r1i + q.f1 * ex);
+                        r5i = r2i * (r3i + q.f2 * ex);
+                        r7i = r2i * (r5i + q.f3 * ex);
+                    } else {
+                        r3i = r2i * r1i;
+                        r5i = r2i * r3i;
+                        r7i = r2i * r5i;
+                    }
+                    DipTerms oi, oj;
+                    double vv;
+                    dip_pair_terms(d, qi, di, q.az[ja], q.dip + 3 * ja, r1i, r3i, r5i, r7i, oi, oj, vv);
+                    acc.p += oi.p;
+                    for (int m = 0; m < 3; ++m) acc.e[m] += oi.e[m];
+                    for (int m = 0; m < 6; ++m) acc.g[m] += oi.g[m];
+                    vir += vv;
+                    dip_add_atomic(q, ja, oj);
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                acc.p += __shfl_xor_sync(0xffffffffu, acc.p, o);
+                for (int m = 0; m < 3; ++m) acc.e[m] += __shfl_xor_sync(0xffffffffu, acc.e[m], o);
+                for (int m = 0; m < 6; ++m) acc.g[m] += __shfl_xor_sync(0xffffffffu, acc.g[m], o);
+            }
+            if (lane == 0) dip_add_atomic(q, ia, acc);
+        }
+    }
+    red[threadIdx.x] = vir;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) sum += red[t];
+        a.part[blockIdx.x] = sum;
+    }
+}
+
+// the molecular part of UDipoleEwaldSelf: one thread per particle, its atom
+// pairs ia < ja in order with the erf kernels, every term negated; the
+// thread owns its atoms
+__global__ void __launch_bounds__(kPolyThreads) k_dipole_intra(PolyArgs a, DipArgs q) {
+    __shared__ double red[kPolyThreads];
+    double vir = 0.0;
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip < a.np) {
+        int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[a.iptpn[ip] - 1];
+        for (int ia = ialow; ia < iaupp; ++ia) {
+            for (int ja = ia + 1; ja < iaupp; ++ja) {
+                double d[3];
+                for (int m = 0; m < 3; ++m) d[m] = a.r[3 * ia + m] - a.r[3 * ja + m];
+                double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                double r1 = sqrt(r2), r1i = 1.0 / r1, r2i = r1i * r1i;
+                double ex = exp(-q.ualpha2 * r2);
+                r1i = r1i * mg_erf2(q.ualpha * r1);
+                double r3i = r2i * (r1i - q.f1 * ex);
+                double r5i = r2i * (r3i - q.f2 * ex);
+                double r7i = r2i * (r5i - q.f3 * ex);
+                DipTerms oi, oj;
+                double vv;
+                dip_pair_terms(d, q.az[ia], q.dip + 3 * ia, q.az[ja], q.dip + 3 * ja, r1i, r3i, r5i, r7i, oi, oj, vv);
+                q.pot[ia] -= oi.p;
+                q.pot[ja] -= oj.p;
+                for (int m = 0; m < 3; ++m) { q.est[3 * ia + m] -= oi.e[m]; q.est[3 * ja + m] -= oj.e[m]; }
+                for (int m = 0; m < 6; ++m) { q.efg[6 * ia + m] -= oi.g[m]; q.efg[6 * ja + m] -= oj.g[m]; }
+                vir -= vv;
+            }
+        }
+    }
+    red[threadIdx.x] = vir;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) sum += red[t];
+        a.part[blockIdx.x] = sum;
+    }
+}
+
+// UDipoleEwaldSurf's sums (q r and dip over all atoms), one block of 1024
+// threads, strided per-thread sums combined in a fixed order
+__global__ void __launch_bounds__(1024) k_dipole_surf_sums(int na, DipArgs q, const double *__restrict__ r,
+                                                           double *__restrict__ out6) {
+    __shared__ double red[6][32];
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int ia = threadIdx.x; ia < na; ia += blockDim.x) {
+        for (int m = 0; m < 3; ++m) s[m] += q.az[ia] * r[3 * ia + m];
+        for (int m = 0; m < 3; ++m) s[3 + m] += q.dip[3 * ia + m];
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < 6; ++k) {
+        for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+        if (lane == 0) red[k][w] = s[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[threadIdx.x][k];
+        out6[threadIdx.x] = t;
+    }
+}
+
+__global__ void k_dipole_surf_apply(int na, DipArgs q, const double *__restrict__ r, const double *__restrict__ s6,
+                                    double fac) {
+    int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ia >= na) return;
+    double tx = s6[0] + s6[3], ty = s6[1] + s6[4], tz = s6[2] + s6[5];
+    q.pot[ia] += fac * (r[3 * ia] * tx + r[3 * ia + 1] * ty + r[3 * ia + 2] * tz);
+    q.est[3 * ia] -= fac * tx;
+    q.est[3 * ia + 1] -= fac * ty;
+    q.est[3 * ia + 2] -= fac * tz;
+}
+
+// the UDipole loop: force += EpsiFourPi (q e + dip . efg), torque +=
+// EpsiFourPi dip x e, and per block the sum of q pot - dip . e
+__global__ void __launch_bounds__(kPolyThreads) k_dipole_finish(int na, DipArgs q, double efp,
+                                                                double *__restrict__ force,
+                                                                double *__restrict__ torque,
+                                                                double *__restrict__ part) {
+    __shared__ double red[kPolyThreads];
+    double u = 0.0;
+    int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ia < na) {
+        const double *d = q.dip + 3 * ia, *e = q.est + 3 * ia, *g = q.efg + 6 * ia;
+        double qa = q.az[ia];
+        u = qa * q.pot[ia] - (d[0] * e[0] + d[1] * e[1] + d[2] * e[2]);
+        if (force) {
+            force[3 * ia] += efp * (qa * e[0] + (d[0] * g[0] + d[1] * g[3] + d[2] * g[4]));
+            force[3 * ia + 1] += efp * (qa * e[1] + (d[0] * g[3] + d[1] * g[1] + d[2] * g[5]));
+            force[3 * ia + 2] += efp * (qa * e[2] + (d[0] * g[4] + d[1] * g[5] + d[2] * g[2]));
+            torque[3 * ia] += efp * (d[1] * e[2] - d[2] * e[1]);
+            torque[3 * ia + 1] += efp * (d[2] * e[0] - d[0] * e[2]);
+            torque[3 * ia + 2] += efp * (d[0] * e[1] - d[1] * e[0]);
+        }
+    }
+    red[threadIdx.x] = u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) sum += red[t];
+        part[blockIdx.x] = sum;
+    }
+}
+
 }  // namespace
 
 struct mg_poly {
@@ -454,6 +691,9 @@ struct mg_poly {
     double rig_tstep = 0.0, rig_tvvite = 0.0;
     int rig_nvvite = 0;
     double *d_rig_io = nullptr;   // staging: ro, ori, drostep out; forceo, torqueo in; rod, angvelo out
+    // dipole electrostatics (mg_poly_udipole_*): dip, pot, est, efg, force,
+    // torque per atom and the surface sums
+    double *d_dscr = nullptr;
 };
 
 static int poly_fail(mg_poly *c, int code, const char *fmt, ...) {
@@ -486,7 +726,7 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
                     c->d_force, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
                     c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to, c->d_bin_z0, c->d_bin_inv, c->d_bin_k,
-                    c->d_rig, c->d_rig_io};
+                    c->d_rig, c->d_rig_io, c->d_dscr};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -799,8 +1039,13 @@ extern "C" int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const doubl
     return MG_OK;
 }
 
-extern "C" int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force, double force_fac,
-                                double *forceo, double *torqueo, double *virmolecule) {
+namespace {
+int dip_scratch(mg_poly *c);
+}
+
+extern "C" int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, const double *force,
+                                const double *torque, double force_fac, double *forceo, double *torqueo,
+                                double *virmolecule) {
     if (!c || !ro || !r || !force || !forceo || !torqueo || !virmolecule) return MG_ERR_ARG;
     const mg_poly_params &p = c->p;
     if (!c->d_fo) {
@@ -810,8 +1055,14 @@ extern "C" int mg_poly_epilogue(mg_poly *c, const double *ro, const double *r, c
     POLY_CUDA(c, cudaMemcpy(c->d_ro, ro, sizeof(double) * 3 * p.np, cudaMemcpyHostToDevice));
     POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
     POLY_CUDA(c, cudaMemcpy(c->d_force, force, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    double *d_tqa = nullptr;
+    if (torque) {   // the atom torques go through the dipole scratch's torque slot
+        MG_TRY(dip_scratch(c));
+        d_tqa = c->d_dscr + 16 * (size_t)p.na;
+        POLY_CUDA(c, cudaMemcpy(d_tqa, torque, sizeof(double) * 3 * p.na, cudaMemcpyHostToDevice));
+    }
     PolyArgs a = poly_args(c);
-    k_poly_epilogue<<<c->nblk, kPolyThreads>>>(a, force_fac, c->d_fo, c->d_to);
+    k_poly_epilogue<<<c->nblk, kPolyThreads>>>(a, force_fac, c->d_fo, c->d_to, d_tqa);
     POLY_CUDA(c, cudaGetLastError());
     POLY_CUDA(c, cudaMemcpy(forceo, c->d_fo, sizeof(double) * 3 * p.np, cudaMemcpyDeviceToHost));
     POLY_CUDA(c, cudaMemcpy(torqueo, c->d_to, sizeof(double) * 3 * p.np, cudaMemcpyDeviceToHost));
@@ -1087,5 +1338,162 @@ extern "C" int mg_poly_rigid_get(mg_poly *c, double *qua, double *quad) {
             qua[4 * ip + k] = h[(size_t)kRig * ip + 3 + k];
             quad[4 * ip + k] = h[(size_t)kRig * ip + 13 + k];
         }
+    return MG_OK;
+}
+
+// ---- charges and point dipoles ---------------------------------------------------
+// The arrays potstat[na], estat[3 na], efg[6 na] travel with every call, as
+// the reference's module arrays; the device keeps no state between calls.
+namespace {
+
+int dip_scratch(mg_poly *c) {
+    if (c->d_dscr) return MG_OK;
+    POLY_CUDA(c, cudaMalloc(&c->d_dscr, sizeof(double) * (19 * (size_t)c->p.na + 8)));
+    return MG_OK;
+}
+
+DipArgs dip_args(mg_poly *c) {
+    const mg_poly_params &p = c->p;
+    size_t na = (size_t)p.na;
+    DipArgs q = {};
+    q.az = c->d_aza;
+    q.dip = c->d_dscr;
+    q.pot = c->d_dscr + 3 * na;
+    q.est = q.pot + na;
+    q.efg = q.est + 3 * na;
+    q.ualpha = p.ualpha;
+    q.ualpha2 = p.ualpha * p.ualpha;
+    q.lewald = p.ualpha > 0.0;
+    if (q.lewald) {   // EwaldSetup, energy.F90:7040-7044
+        double fac = 1.0 / (std::sqrt(3.1415926535897932) * p.ualpha);
+        q.f1 = fac * 2.0 * q.ualpha2;
+        q.f2 = fac * (2.0 * q.ualpha2) * (2.0 * q.ualpha2) / 3.0;
+        q.f3 = fac * (2.0 * q.ualpha2) * (2.0 * q.ualpha2) * (2.0 * q.ualpha2) / 15.0;
+    }
+    return q;
+}
+
+int dip_copy(mg_poly *c, const DipArgs &q, const double *pot, const double *est, const double *efg,
+             cudaMemcpyKind kind, double *hpot, double *hest, double *hefg) {
+    size_t na = (size_t)c->p.na;
+    if (kind == cudaMemcpyHostToDevice) {
+        POLY_CUDA(c, cudaMemcpy(q.pot, pot, sizeof(double) * na, kind));
+        POLY_CUDA(c, cudaMemcpy(q.est, est, sizeof(double) * 3 * na, kind));
+        POLY_CUDA(c, cudaMemcpy(q.efg, efg, sizeof(double) * 6 * na, kind));
+    } else {
+        POLY_CUDA(c, cudaMemcpy(hpot, q.pot, sizeof(double) * na, kind));
+        POLY_CUDA(c, cudaMemcpy(hest, q.est, sizeof(double) * 3 * na, kind));
+        POLY_CUDA(c, cudaMemcpy(hefg, q.efg, sizeof(double) * 6 * na, kind));
+    }
+    return MG_OK;
+}
+
+// sum of q pot - dip . e over the atoms (block partials in order)
+int dip_usum(mg_poly *c, const DipArgs &q, double *out) {
+    int na = c->p.na, nb = (na + kPolyThreads - 1) / kPolyThreads;
+    k_dipole_finish<<<nb, kPolyThreads>>>(na, q, 0.0, nullptr, nullptr, c->d_part);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * nb, cudaMemcpyDeviceToHost));
+    double u = 0.0;
+    for (int b = 0; b < nb; ++b) u += c->h_part[b];
+    *out = u;
+    return MG_OK;
+}
+
+}  // namespace
+
+extern "C" int mg_poly_udipole_real(mg_poly *c, const double *ro, const double *r, const double *dip,
+                                    const int32_t *nneighpn, const int32_t *jpnlist, double *potstat, double *estat,
+                                    double *efg, double *virelec, double *u_real) {
+    if (!c || !ro || !r || !dip || !nneighpn || !jpnlist || !potstat || !estat || !efg || !virelec || !u_real)
+        return MG_ERR_ARG;
+    if (!c->d_aza) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.aza (atom charges) was not given");
+    const mg_poly_params &p = c->p;
+    for (int i = 0; i < p.np; ++i)
+        if (nneighpn[i] < 0 || nneighpn[i] > c->maxnneigh)
+            return poly_fail(c, MG_ERR_NEIGH_OVERFLOW, "nneighpn(%d) = %d > maxnneigh %d", i + 1, nneighpn[i],
+                             c->maxnneigh);
+    MG_TRY(dip_scratch(c));
+    DipArgs q = dip_args(c);
+    size_t na = (size_t)p.na;
+    POLY_CUDA(c, cudaMemcpy(c->d_ro, ro, sizeof(double) * 3 * p.np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_dscr, dip, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_nneigh, nneighpn, sizeof(int) * p.np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_jpnlist, jpnlist, sizeof(int) * (size_t)c->maxnneigh * p.np, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemset(q.pot, 0, sizeof(double) * 10 * na));   // pot, est, efg
+    PolyArgs a = poly_args(c);
+    k_dipole_real<<<c->nblk_w, kPolyThreads>>>(a, q);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->nblk_w, cudaMemcpyDeviceToHost));
+    double vir = 0.0;
+    for (int b = 0; b < c->nblk_w; ++b) vir += c->h_part[b];
+    double u = 0.0;
+    MG_TRY(dip_usum(c, q, &u));
+    MG_TRY(dip_copy(c, q, nullptr, nullptr, nullptr, cudaMemcpyDeviceToHost, potstat, estat, efg));
+    *virelec = vir;
+    *u_real = p.epsi_four_pi * 0.5 * u;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_udipole_self(mg_poly *c, const double *r, const double *dip, int32_t lsurf, double *potstat,
+                                    double *estat, double *efg, double *virelec) {
+    if (!c || !r || !dip || !potstat || !estat || !efg || !virelec) return MG_ERR_ARG;
+    if (!c->d_aza) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.aza (atom charges) was not given");
+    const mg_poly_params &p = c->p;
+    if (!(p.ualpha > 0.0)) return poly_fail(c, MG_ERR_STATE, "the Ewald self terms need ualpha > 0");
+    MG_TRY(dip_scratch(c));
+    DipArgs q = dip_args(c);
+    size_t na = (size_t)p.na;
+    POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(c->d_dscr, dip, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    MG_TRY(dip_copy(c, q, potstat, estat, efg, cudaMemcpyHostToDevice, nullptr, nullptr, nullptr));
+    PolyArgs a = poly_args(c);
+    k_dipole_intra<<<c->nblk, kPolyThreads>>>(a, q);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->nblk, cudaMemcpyDeviceToHost));
+    double vir = *virelec;
+    for (int b = 0; b < c->nblk; ++b) vir += c->h_part[b];
+    if (lsurf) {
+        double *s6 = c->d_dscr + 19 * na;
+        double vol = p.boxlen[0] * p.boxlen[1] * p.boxlen[2];
+        double fac = (4.0 * 3.1415926535897932 / 3.0) / vol;
+        k_dipole_surf_sums<<<1, 1024>>>(p.na, q, c->d_r, s6);
+        k_dipole_surf_apply<<<(p.na + 127) / 128, 128>>>(p.na, q, c->d_r, s6, fac);
+        POLY_CUDA(c, cudaGetLastError());
+        double h6[6];
+        POLY_CUDA(c, cudaMemcpy(h6, s6, sizeof h6, cudaMemcpyDeviceToHost));
+        double qq = h6[0] * h6[0] + h6[1] * h6[1] + h6[2] * h6[2];
+        double qd = h6[0] * h6[3] + h6[1] * h6[4] + h6[2] * h6[5];
+        double dd = h6[3] * h6[3] + h6[4] * h6[4] + h6[5] * h6[5];
+        vir = vir - 2.0 * 3.1415926535897932 / (3.0 * vol) * (qq + 2.0 * (2.0 * qd) + 3.0 * dd);
+    }
+    MG_TRY(dip_copy(c, q, nullptr, nullptr, nullptr, cudaMemcpyDeviceToHost, potstat, estat, efg));
+    *virelec = vir;
+    return MG_OK;
+}
+
+extern "C" int mg_poly_udipole_finish(mg_poly *c, const double *dip, const double *potstat, const double *estat,
+                                      const double *efg, double *force, double *torque, double *u_stat) {
+    if (!c || !dip || !potstat || !estat || !efg || !force || !torque || !u_stat) return MG_ERR_ARG;
+    if (!c->d_aza) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.aza (atom charges) was not given");
+    const mg_poly_params &p = c->p;
+    MG_TRY(dip_scratch(c));
+    DipArgs q = dip_args(c);
+    size_t na = (size_t)p.na;
+    double *d_f = q.efg + 6 * na, *d_t = d_f + 3 * na;
+    POLY_CUDA(c, cudaMemcpy(c->d_dscr, dip, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    MG_TRY(dip_copy(c, q, potstat, estat, efg, cudaMemcpyHostToDevice, nullptr, nullptr, nullptr));
+    POLY_CUDA(c, cudaMemcpy(d_f, force, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    POLY_CUDA(c, cudaMemcpy(d_t, torque, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
+    int nb = (p.na + kPolyThreads - 1) / kPolyThreads;
+    k_dipole_finish<<<nb, kPolyThreads>>>(p.na, q, p.epsi_four_pi, d_f, d_t, c->d_part);
+    POLY_CUDA(c, cudaGetLastError());
+    POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * nb, cudaMemcpyDeviceToHost));
+    double u = 0.0;
+    for (int b = 0; b < nb; ++b) u += c->h_part[b];
+    POLY_CUDA(c, cudaMemcpy(force, d_f, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost));
+    POLY_CUDA(c, cudaMemcpy(torque, d_t, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost));
+    *u_stat = p.epsi_four_pi * 0.5 * u;
     return MG_OK;
 }

@@ -1636,6 +1636,137 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_
     return MG_OK;
 }
 
+// ---- UDipoleEwaldRecSPM (energy.F90:2046-2170) ---------------------------------
+// CardinalBSpline (mollib.F90:1629-1685) with first and second derivatives,
+// the recursion and divisions as there; the second derivatives come from
+// the values of order-2 (zero for order 3 and below, as there)
+__device__ void dip_bspline(int order, double pos, int &kmax, double *v, double *d, double *d2) {
+    double last[MG_MAX_ORDER], last2[MG_MAX_ORDER];
+    int iv = (int)floor(pos);
+    double x = pos - iv;
+    kmax = iv;
+    for (int i = 0; i < order; ++i) { last[i] = 0.0; last2[i] = 0.0; v[i] = 0.0; }
+    v[0] = x;
+    v[1] = 1.0 - x;
+    for (int n = 3; n <= order; ++n) {
+        for (int i = 0; i < order; ++i) last[i] = v[i];
+        if (n == order - 1)
+            for (int i = 0; i < order; ++i) last2[i] = v[i];
+        v[0] = x * last[0] / (n - 1);
+        for (int i = 1; i <= n - 2; ++i) {
+            double a = i + x;
+            v[i] = (a * last[i] + (n - a) * last[i - 1]) / (n - 1);
+        }
+        v[n - 1] = (1 - x) * last[n - 2] / (n - 1);
+    }
+    d[0] = last[0];
+    for (int i = 1; i <= order - 2; ++i) d[i] = last[i] - last[i - 1];
+    d[order - 1] = -last[order - 2];
+    d2[0] = last2[0];
+    d2[1] = last2[1] - 2 * last2[0];
+    for (int i = 2; i <= order - 3; ++i) d2[i] = last2[i] - 2 * last2[i - 1] + last2[i - 2];
+    if (order > 3) d2[order - 2] = -2 * last2[order - 3] + last2[order - 4];
+    if (order > 2) d2[order - 1] = last2[order - 3];
+}
+
+struct DipMeshArgs {
+    const double *ro, *az, *dip;
+    int np, order, n;
+    double dkdr[3];
+};
+
+// the generalized charge mesh: one thread per particle, q M_x M_y M_z +
+// dkdr . dip (derivative products) at each stamp point, added to the
+// fixed-point mesh with 64-bit integer atomics (scale 2^k)
+__global__ void __launch_bounds__(128) k_dip_spread(DipMeshArgs a, double scale, unsigned long long *__restrict__ Qfx) {
+    int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ia >= a.np) return;
+    const int order = a.order, n = a.n;
+    double sp[3][MG_MAX_ORDER], dr[3][MG_MAX_ORDER], d2[MG_MAX_ORDER];
+    int mm[3];
+    for (int m = 0; m < 3; ++m) {
+        int kmax;
+        dip_bspline(order, a.dkdr[m] * a.ro[3 * ia + m], kmax, sp[m], dr[m], d2);
+        mm[m] = ((kmax % n) + n) % n;
+    }
+    double dx2 = a.dip[3 * ia] * a.dkdr[0], dy2 = a.dip[3 * ia + 1] * a.dkdr[1], dz2 = a.dip[3 * ia + 2] * a.dkdr[2];
+    double q0 = a.az[ia];
+    for (int iz = 0; iz < order; ++iz) {
+        int nz = (n + mm[2] - iz) % n;
+        double splz = sp[2][iz], dsdz = dr[2][iz];
+        for (int iy = 0; iy < order; ++iy) {
+            int ny = (n + mm[1] - iy) % n;
+            double sply = sp[1][iy];
+            double q1 = q0 * sply * splz;
+            double dipx1 = dx2 * sply * splz;
+            double dipy1 = dy2 * dr[1][iy] * splz;
+            double dipz1 = dz2 * sply * dsdz;
+            size_t row = ((size_t)nz * n + ny) * n;
+            for (int ix = 0; ix < order; ++ix) {
+                int nx = (n + mm[0] - ix) % n;
+                double splx = sp[0][ix];
+                double val = q1 * splx + dipx1 * dr[0][ix] + dipy1 * splx + dipz1 * splx;
+                atomicAdd(&Qfx[row + nx], (unsigned long long)__double2ll_rn(val * scale));
+            }
+        }
+    }
+}
+
+// potential, field, field gradient (second derivatives) at each particle
+// from the potential mesh, and the dipole term of the virial: one warp per
+// particle, lanes over the (iy, iz) rows, the sums combined by shuffles in
+// a fixed order
+__global__ void __launch_bounds__(128) k_dip_gather(DipMeshArgs a, const double *__restrict__ Q,
+                                                    double *__restrict__ pot, double *__restrict__ est,
+                                                    double *__restrict__ efg, double *__restrict__ vir) {
+    int ia = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (ia >= a.np) return;
+    const int order = a.order, n = a.n;
+    double sp[3][MG_MAX_ORDER], dr[3][MG_MAX_ORDER], dd[3][MG_MAX_ORDER];
+    int mm[3];
+    for (int m = 0; m < 3; ++m) {
+        int kmax;
+        dip_bspline(order, a.dkdr[m] * a.ro[3 * ia + m], kmax, sp[m], dr[m], dd[m]);
+        mm[m] = ((kmax % n) + n) % n;
+    }
+    double dx2 = a.dip[3 * ia] * a.dkdr[0], dy2 = a.dip[3 * ia + 1] * a.dkdr[1], dz2 = a.dip[3 * ia + 2] * a.dkdr[2];
+    double acc[11];
+    for (int k = 0; k < 11; ++k) acc[k] = 0.0;
+    for (int t = lane; t < order * order; t += 32) {
+        int iz = t / order, iy = t - iz * order;
+        int nz = (n + mm[2] - iz) % n, ny = (n + mm[1] - iy) % n;
+        double splz = sp[2][iz], dsdz = dr[2][iz], d2sdz = dd[2][iz];
+        double sply = sp[1][iy], dsdy = dr[1][iy], d2sdy = dd[1][iy];
+        const double *row = Q + ((size_t)nz * n + ny) * n;
+        for (int ix = 0; ix < order; ++ix) {
+            int nx = (n + mm[0] - ix) % n;
+            double splx = sp[0][ix], dsdx = dr[0][ix], d2sdx = dd[0][ix];
+            double qv = row[nx];
+            acc[0] += splx * sply * splz * qv;
+            acc[1] += dsdx * sply * splz * qv;
+            acc[2] += splx * dsdy * splz * qv;
+            acc[3] += splx * sply * dsdz * qv;
+            acc[4] += d2sdx * sply * splz * qv;
+            acc[5] += splx * d2sdy * splz * qv;
+            acc[6] += splx * sply * d2sdz * qv;
+            acc[7] += dsdx * dsdy * splz * qv;
+            acc[8] += dsdx * sply * dsdz * qv;
+            acc[9] += splx * dsdy * dsdz * qv;
+            double qdip = dx2 * dsdx * sply * splz + dy2 * splx * dsdy * splz + dz2 * splx * sply * dsdz;
+            acc[10] -= qdip * qv;
+        }
+    }
+    for (int k = 0; k < 11; ++k)
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    if (lane != 0) return;
+    const double *dk = a.dkdr;
+    double d2k[6] = {dk[0] * dk[0], dk[1] * dk[1], dk[2] * dk[2], dk[0] * dk[1], dk[0] * dk[2], dk[1] * dk[2]};
+    pot[ia] += acc[0];
+    for (int m = 0; m < 3; ++m) est[3 * ia + m] -= acc[1 + m] * dk[m];   // E = -dU/dr
+    for (int m = 0; m < 6; ++m) efg[6 * ia + m] -= acc[4 + m] * d2k[m];
+    vir[ia] = acc[10];
+}
+
 template <typename T> void set_smem_limits() {
     cudaFuncSetAttribute(k_fft_x_r2c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_fft_x_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -1829,6 +1960,45 @@ int mg_spme_potential(mg_handle *h) {
     cv.vw = h->d_vw;
     return fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv,
                               1.0 / mg_spme_fx_scale(h));
+}
+
+// the reciprocal part of UDipoleEwald, SPME (FP64 form): device arrays dip,
+// pot, est, efg of the handle's particles (added to); vir[np] the per-particle
+// dipole terms of the virial, then the FFT blocks' (energy, virial) partial
+// pairs, vir[np + 2 b + 1] summing to SPMFFTRec's virloc (nblk_rec blocks).  The fixed-point scale is
+// chosen for the generalized charges: no mesh point can exceed np (max|q| +
+// 3 max|dkdr . dip|) with B-spline values and derivatives at most 1.
+int mg_spme_dipole(mg_handle *h, const double *dip, double bound, double *pot, double *est, double *efg,
+                   double *vir) {
+    if (h->form != MG_FP64) return mg_fail(h, MG_ERR_UNSUPPORTED, "dipole electrostatics need the FP64 form");
+    int k = 52;
+    while (k > 8 && std::ldexp(bound, k) >= 9.2e18 * 0.5) --k;
+    double scale = std::ldexp(1.0, k);
+    DipMeshArgs a;
+    a.ro = h->d_ro;
+    a.az = h->d_az;
+    a.dip = dip;
+    a.np = h->np;
+    a.order = h->order;
+    a.n = h->nmesh;
+    for (int m = 0; m < 3; ++m) a.dkdr[m] = h->dkdr[m];
+    // the FFT pass that read the last mesh cleared it; clear again in case
+    // a spread was left unconsumed
+    MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)a.n * a.n * a.n, h->st));
+    k_dip_spread<<<(a.np + 127) / 128, 128, 0, h->st>>>(a, scale, (unsigned long long *)h->d_Qfx);
+    ConvArgs cv;
+    cv.part = h->d_part + h->part_rec;
+    cv.mf = h->d_mf;
+    cv.ew = h->d_ew;
+    cv.vw = h->d_vw;
+    MG_TRY(fft_launch<double>(h, (double *)h->d_Q, (double2 *)h->d_F, (const double2 *)h->d_tw, cv, 1.0 / scale));
+    k_dip_gather<<<(a.np * 32 + 127) / 128, 128, 0, h->st>>>(a, (const double *)h->d_Q, pot, est, efg, vir);
+    // the FFT blocks' (energy, virial) partial pairs after the per-particle terms
+    MG_CUDA(h, cudaMemcpyAsync(vir + a.np, h->d_part + h->part_rec, sizeof(double) * 2 * h->nblk_rec,
+                               cudaMemcpyDeviceToDevice, h->st));
+    h->launches += 2;
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
 }
 
 // The device FFT on a given mesh, for checking it against another FFT: the

@@ -87,6 +87,9 @@ def ori_to_qua(ori):
 class ParticleType:
     name: str
     atoms: List[Tuple[int, Tuple[float, float, float]]]   # (atom type, 0-based; local position)
+    # point dipoles of the atoms in the local frame (e A; dipain), for
+    # txelec = 'dip'; None: no dipoles
+    dipoles: Optional[List[Tuple[float, float, float]]] = None
 
 
 @dataclass
@@ -107,6 +110,10 @@ class PolySystem:
     ncut: int = 0
     order: int = 0
     nmesh: int = 0
+    # 'charge': atom charges through the pair table and Ewald; 'dip':
+    # charges and point dipoles through UDipole, the table without Coulomb
+    txelec: str = "charge"
+    lsurf: int = 0
     ubuf: Optional[np.ndarray] = None
     iubuflow: Optional[np.ndarray] = None
     r2umin: Optional[np.ndarray] = None
@@ -153,6 +160,24 @@ class PolySystem:
     def aza(self):
         return np.array([self.atom_types[t - 1].charge for t in self.iatan()], dtype=np.float64)
 
+    def atom_dipoles(self):
+        """dip(3, na): each atom's local dipole rotated by its particle's
+        orientation (SetAtomProp), particle by particle; zero where a type
+        has none."""
+        na = self.napt()[self.iptpn - 1]
+        first = self.ianpn() - 1
+        out = np.zeros((int(na.sum()), 3))
+        for t, pt in enumerate(self.particle_types, start=1):
+            if not pt.dipoles:
+                continue
+            idx = np.flatnonzero(self.iptpn == t)
+            if idx.size == 0:
+                continue
+            loc = np.array(pt.dipoles, dtype=np.float64)
+            d = np.einsum("nij,aj->nai", self.ori[idx], loc)
+            out[(first[idx][:, None] + np.arange(len(loc))[None, :]).reshape(-1)] = d.reshape(-1, 3)
+        return np.ascontiguousarray(out)
+
     def type_inertia(self, t):
         """Mass, centre of mass and inertia tensor of particle type t
         (0-based) in its local frame (PAxesSystem, particle.F90:2360-2395,
@@ -183,7 +208,8 @@ class PolySystem:
                 e[:, 2] = -e[:, 2]
             loc = np.array([p for _, p in pt.atoms], dtype=np.float64)
             ra = (loc - c) @ e
-            types.append(ParticleType(pt.name, [(a, tuple(ra[k])) for k, (a, _) in enumerate(pt.atoms)]))
+            dips = None if pt.dipoles is None else [tuple(v) for v in np.array(pt.dipoles, dtype=np.float64) @ e]
+            types.append(ParticleType(pt.name, [(a, tuple(ra[k])) for k, (a, _) in enumerate(pt.atoms)], dips))
             com.append(c)
             axes.append(e)
         ti = np.asarray(self.iptpn) - 1
@@ -241,14 +267,17 @@ class PolySystem:
         """PotTwoBodyTab1 over the atom types: (1,6,12) Lennard-Jones plus
         Coulomb, the real-space Ewald part (CalcEwaldUfac) when Ewald is on."""
         nat = self.nat
+        # a dipole system's table holds no Coulomb term (qq = 0 with
+        # ldipole, potential.F90:1380): UDipole takes all electrostatics
+        dip = self.txelec == "dip"
         keep = {"iptpt": iptpt_matrix(nat),
-                "zat": abi.as_f64([a.charge for a in self.atom_types]),
+                "zat": abi.as_f64([0.0 if dip else a.charge for a in self.atom_types]),
                 "sigat": abi.as_f64([a.sigma for a in self.atom_types]),
                 "epsat": abi.as_f64([a.eps for a in self.atom_types])}
         pp = abi.MgPotParams(npt=nat, iptpt=abi.i32(keep["iptpt"]), zat=abi.f64(keep["zat"]),
                              sigat=abi.f64(keep["sigat"]), epsat=abi.f64(keep["epsat"]), rcut=self.rcut,
                              ualpha=self.ualpha, epsi_four_pi=self.epsi_four_pi,
-                             lcharge_ewald=int(self.ewald != abi.MG_EWALD_NONE),
+                             lcharge_ewald=int(self.ewald != abi.MG_EWALD_NONE and not dip),
                              lljcut=0, ljrcut=units.ljrcut_default(), ljushift=1.0, r2uminin=self.r2uminin,
                              utoltab=units.tol_default(), ftoltab=units.tol_default(), umaxtab=20000.0,
                              fmaxtab=20000.0)
@@ -413,16 +442,18 @@ class PolyEngine:
             raise MolsimError(st, f"poly_dutwobody_batch: {buf.value.decode(errors='replace')}")
         return du, ovl.astype(bool)
 
-    def Epilogue(self, force, r=None):
+    def Epilogue(self, force, r=None, torque=None):
         """UTotal's end (energy.F90:405-427): particle forces and torques
-        (scaled by force_fac) from the atom forces, and the molecular virial."""
+        (scaled by force_fac) from the atom forces and, with dipoles, the
+        atom torques, and the molecular virial."""
         s = self.s
         r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
         fo = np.zeros(3 * s.np_)
         to = np.zeros(3 * s.np_)
         vm = np.zeros(1)
+        tq = None if torque is None else abi.f64(abi.as_f64(np.asarray(torque).reshape(-1)))
         st = self.lib.mg_poly_epilogue(self.h, abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)),
-                                       abi.f64(abi.as_f64(np.asarray(force).reshape(-1))), units.FORCE_FAC,
+                                       abi.f64(abi.as_f64(np.asarray(force).reshape(-1))), tq, units.FORCE_FAC,
                                        abi.f64(fo), abi.f64(to), abi.f64(vm))
         if st != 0:
             raise MolsimError(st, "poly_epilogue")
@@ -439,25 +470,94 @@ class PolyEngine:
             raise MolsimError(st, "poly_ewald_intra")
         return dict(force=force.reshape(-1, 3), u_rec=float(u[0]))
 
+    def _list(self, nneighpn, jpnlist):
+        """The particle list (nneighpn, jpnlist) given, or NList's list of
+        the kept handle of the centres."""
+        if nneighpn is not None:
+            return abi.as_i32(nneighpn), abi.as_i32(np.asarray(jpnlist).reshape(-1))
+        from .engine import Engine
+        s = self.s
+        if getattr(self, "_centres", None) is None:
+            self._centres = Engine(s.centre_system())
+        e = self._centres
+        e.SetPositions(abi.as_f64(s.ro.reshape(-1)))
+        e.NList("write")
+        nn = np.zeros(s.np_, dtype=np.int32)
+        jl = np.zeros(s.np_ * self.maxnneigh, dtype=np.int32)
+        e._check(e._fn("nlist_get")(e.h, abi.i32(nn), abi.i32(jl), self.maxnneigh), "nlist_get")
+        return nn, jl
+
+    def _atoms_handle(self, engine_factory=None):
+        from .engine import Engine
+        s = self.s
+        if engine_factory is not None:
+            return engine_factory(s.atom_system())
+        if getattr(self, "_atoms", None) is None:
+            self._atoms = Engine(s.atom_system())
+        return self._atoms
+
+    def UDipole(self, nneighpn=None, jpnlist=None, dip=None, r=None, engine_factory=None):
+        """UDipole (energy.F90:1476-1579) for charges and point dipoles:
+        UDipoleP over the particle list, with Ewald the reciprocal part on
+        the handle of the atoms, both parts of UDipoleEwaldSelf and (lsurf)
+        UDipoleEwaldSurf, then u%stat, atom forces (force(3,na) units) and
+        atom torques.  Returns potstat, estat, efg, u_stat, u_rec (u_stat
+        minus the real-space part), virial (EpsiFourPi virelec)."""
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        dip = s.atom_dipoles() if dip is None else np.ascontiguousarray(dip, dtype=np.float64).reshape(-1, 3)
+        nn, jl = self._list(nneighpn, jpnlist)
+        na = len(r)
+        pot, est, efg = np.zeros(na), np.zeros(3 * na), np.zeros(6 * na)
+        vir, ureal = np.zeros(1), np.zeros(1)
+        self._fail(self.lib.mg_poly_udipole_real(self.h, abi.f64(abi.as_f64(s.ro.reshape(-1))),
+                                                 abi.f64(r.reshape(-1)), abi.f64(dip.reshape(-1)), abi.i32(nn),
+                                                 abi.i32(jl), abi.f64(pot), abi.f64(est), abi.f64(efg),
+                                                 abi.f64(vir), abi.f64(ureal)), "poly_udipole_real")
+        if s.ewald != abi.MG_EWALD_NONE:
+            e = self._atoms_handle(engine_factory)
+            e.SetPositions(s.atoms_in_box(r).reshape(-1))
+            e._check(e._fn("dipole_ewald")(e.h, abi.f64(dip.reshape(-1)), abi.f64(pot), abi.f64(est),
+                                           abi.f64(efg), abi.f64(vir)), "dipole_ewald")
+            if engine_factory is not None:
+                e.close()
+            self._fail(self.lib.mg_poly_udipole_self(self.h, abi.f64(r.reshape(-1)), abi.f64(dip.reshape(-1)),
+                                                     int(s.lsurf), abi.f64(pot), abi.f64(est), abi.f64(efg),
+                                                     abi.f64(vir)), "poly_udipole_self")
+        force = np.zeros(3 * na)
+        torque = np.zeros(3 * na)
+        ustat = np.zeros(1)
+        self._fail(self.lib.mg_poly_udipole_finish(self.h, abi.f64(dip.reshape(-1)), abi.f64(pot), abi.f64(est),
+                                                   abi.f64(efg), abi.f64(force), abi.f64(torque), abi.f64(ustat)),
+                   "poly_udipole_finish")
+        return dict(potstat=pot, estat=est.reshape(-1, 3), efg=efg.reshape(-1, 6), force=force.reshape(-1, 3),
+                    torque=torque.reshape(-1, 3), u_stat=float(ustat[0]), u_rec=float(ustat[0] - ureal[0]),
+                    virial=s.epsi_four_pi * float(vir[0]))
+
     def UTotal(self, nneighpn=None, jpnlist=None, engine_factory=None):
         """UTotal of a polyatomic system: the atom pairs (UTwoBodyP, with the
         real-space Ewald table when Ewald is on), the reciprocal sum and
         atomic self term over the atoms (a handle of the atoms), the
         molecular self term, then UTotal's end: atom forces (force(3,na)
         units), particle forces and torques (forceo, torqueo), the virial."""
-        from .engine import Engine
         s = self.s
         r = s.atom_positions()
         # no list given: the device-resident list of a centres handle
         tw = self.UTwoBodyPList(r) if nneighpn is None else self.UTwoBodyP(nneighpn, jpnlist, r)
         out = dict(u_twob=tw["u_twob"], virial=tw["virial"], force=tw["force"].copy(), u_rec=0.0)
+        if s.txelec == "dip":   # UTwoBodyP then UDipole (energy.F90:366-369)
+            d = self.UDipole(nneighpn, jpnlist, r=r, engine_factory=engine_factory)
+            out["force"] += d["force"]
+            out["virial"] += d["virial"]
+            out["u_rec"] = d["u_rec"]
+            out["u_stat"] = d["u_stat"]
+            out["u_tot"] = out["u_twob"][0] + d["u_stat"]
+            ep = self.Epilogue(out["force"], r, torque=d["torque"])
+            out.update(forceo=ep["forceo"], torqueo=ep["torqueo"])
+            out["virial"] += ep["virmolecule"]
+            return out
         if s.ewald != abi.MG_EWALD_NONE:
-            if engine_factory is not None:
-                e = engine_factory(s.atom_system())
-            else:   # one handle of the atoms, kept for the following calls
-                if getattr(self, "_atoms", None) is None:
-                    self._atoms = Engine(s.atom_system())
-                e = self._atoms
+            e = self._atoms_handle(engine_factory)   # one handle of the atoms, kept for the following calls
             e.SetPositions(s.atoms_in_box(r).reshape(-1))
             e.NList("write")
             rec = e.UTotal()

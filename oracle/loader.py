@@ -40,7 +40,8 @@ def oracle():
         lib.orc_poly_dutwobody.argtypes = [C.POINTER(abi.MgPolyParams), C.c_int32, abi.PF64, abi.PF64, abi.PI32,
                                            abi.PI32, C.c_int32, abi.PF64, abi.PF64, abi.PF64, abi.PI32]
         lib.orc_poly_epilogue.restype = C.c_int
-        lib.orc_poly_epilogue.argtypes = [C.POINTER(abi.MgPolyParams), abi.PF64, abi.PF64, abi.PF64, C.c_double,
+        lib.orc_poly_epilogue.argtypes = [C.POINTER(abi.MgPolyParams), abi.PF64, abi.PF64, abi.PF64, abi.PF64,
+                                          C.c_double,
                                           abi.PF64, abi.PF64, abi.PF64]
         lib.orc_poly_ewald_intra.restype = C.c_int
         lib.orc_poly_ewald_intra.argtypes = [C.POINTER(abi.MgPolyParams), abi.PF64, abi.PF64, abi.PF64]
@@ -55,5 +56,17 @@ def oracle():
         lib.orc_rigid_kick.restype = C.c_int
         lib.orc_rigid_kick.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_int32, abi.PF64, abi.PF64, abi.PF64,
                                        abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64]
+        P = C.POINTER(abi.MgPolyParams)
+        lib.orc_poly_udipole_real.restype = C.c_int
+        lib.orc_poly_udipole_real.argtypes = [P, C.c_int32, abi.PF64, abi.PF64, abi.PF64, abi.PI32, abi.PI32,
+                                              abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64]
+        lib.orc_poly_udipole_self.restype = C.c_int
+        lib.orc_poly_udipole_self.argtypes = [P, abi.PF64, abi.PF64, C.c_int32, abi.PF64, abi.PF64, abi.PF64,
+                                              abi.PF64]
+        lib.orc_poly_udipole_finish.restype = C.c_int
+        lib.orc_poly_udipole_finish.argtypes = [P, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64,
+                                                abi.PF64]
+        lib.orc_dipole_ewald.restype = C.c_int
+        lib.orc_dipole_ewald.argtypes = [C.c_void_p, abi.PF64, abi.PF64, abi.PF64, abi.PF64, abi.PF64]
         _lib = lib
     return _lib

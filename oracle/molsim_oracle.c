@@ -1549,6 +1549,185 @@ static void uewald_surf(orc_sys *s, double *virrec) {
     *virrec = *virrec - term;
 }
 
+static void cardinal_bspline2(int order, double pos, int *kmax, double *values, double *derivs, double *derivs2);
+static void dipole_ewald_facs(double ualpha, double *f1, double *f2, double *f3, double *s1, double *s2);
+
+/* UDipoleEwaldRecStd (energy.F90:1830-2040, serial branch :1960-2036):
+   structure factors of charges and dipoles, sumeikr with (q + i k.dip) and
+   sumeikrd with i k.dip, in the four sign combinations; then per atom the
+   potential, field and field gradient of every k-vector, and the virial */
+static void dipole_rec_std(orc_sys *s, const double *dip, double *potstat, double *estat, double *efg,
+                           double *virelec) {
+    int na = s->np, kn = 0;
+    ewald_set_array(s, 1, na);
+    zc *Sd = (zc *)xcalloc(4, sizeof(zc));
+    zc *er = (zc *)xcalloc((size_t)na * 4, sizeof(zc));
+    for (int nz = 0; nz <= s->ncut; ++nz) {
+        double kz = s->TwoPiBoxi[2] * nz;
+        for (int ny = 0; ny <= s->ncut; ++ny) {
+            double ky = s->TwoPiBoxi[1] * ny;
+            if (ny * ny + nz * nz > s->ncut2) continue;
+            for (int ia = 1; ia <= na; ++ia) {
+                s->eikyzm[ia - 1] = zmul(zconj(EIK(s->eiky, ia, ny)), EIK(s->eikz, ia, nz));
+                s->eikyzp[ia - 1] = zmul(EIK(s->eiky, ia, ny), EIK(s->eikz, ia, nz));
+            }
+            for (int nx = 0; nx <= s->ncut; ++nx) {
+                if (nx * nx + ny * ny + nz * nz > s->ncut2) continue;
+                if (nx == 0 && ny == 0 && nz == 0) continue;
+                kn = kn + 1;
+                double kx = s->TwoPiBoxi[0] * nx;
+                zc S[4];
+                for (int c = 0; c < 4; ++c) { S[c].re = Zero; S[c].im = Zero; Sd[c].re = Zero; Sd[c].im = Zero; }
+                for (int ia = 1; ia <= na; ++ia) {
+                    zc ex = EIK(s->eikx, ia, nx);
+                    zc *e = &er[(size_t)(ia - 1) * 4];
+                    e[0] = zmul(zconj(ex), s->eikyzm[ia - 1]);
+                    e[1] = zmul(zconj(ex), s->eikyzp[ia - 1]);
+                    e[2] = zmul(ex, s->eikyzm[ia - 1]);
+                    e[3] = zmul(ex, s->eikyzp[ia - 1]);
+                    double tx = kx * dip[3 * (ia - 1)], ty = ky * dip[3 * (ia - 1) + 1], tz = kz * dip[3 * (ia - 1) + 2];
+                    double fac[4] = {-tx - ty + tz, -tx + ty + tz, +tx - ty + tz, +tx + ty + tz};
+                    for (int c = 0; c < 4; ++c) {
+                        zc g = {AZ(ia), fac[c]}, h = {Zero, fac[c]};
+                        S[c] = zadd(S[c], zmul(g, e[c]));
+                        Sd[c] = zadd(Sd[c], zmul(h, e[c]));
+                    }
+                }
+                double kfac2 = Two * s->kfac[kn - 1];
+                double kxkx = kfac2 * kx * kx, kyky = kfac2 * ky * ky, kzkz = kfac2 * kz * kz;
+                double kxky = kfac2 * kx * ky, kxkz = kfac2 * kx * kz, kykz = kfac2 * ky * kz;
+                for (int ia = 1; ia <= na; ++ia) {
+                    zc *e = &er[(size_t)(ia - 1) * 4];
+                    zc cmm = zmul(e[0], zconj(S[0])), cmp = zmul(e[1], zconj(S[1]));
+                    zc cpm = zmul(e[2], zconj(S[2])), cpp = zmul(e[3], zconj(S[3]));
+                    double *ei = &estat[3 * (ia - 1)], *gi = &efg[6 * (ia - 1)];
+                    potstat[ia - 1] = potstat[ia - 1] + kfac2 * (+cmm.re + cmp.re + cpm.re + cpp.re);
+                    ei[0] = ei[0] + kfac2 * kx * (-cmm.im - cmp.im + cpm.im + cpp.im);
+                    ei[1] = ei[1] + kfac2 * ky * (-cmm.im + cmp.im - cpm.im + cpp.im);
+                    ei[2] = ei[2] + kfac2 * kz * (+cmm.im + cmp.im + cpm.im + cpp.im);
+                    gi[0] = gi[0] + kxkx * (+cmm.re + cmp.re + cpm.re + cpp.re);
+                    gi[1] = gi[1] + kyky * (+cmm.re + cmp.re + cpm.re + cpp.re);
+                    gi[2] = gi[2] + kzkz * (+cmm.re + cmp.re + cpm.re + cpp.re);
+                    gi[3] = gi[3] + kxky * (+cmm.re - cmp.re - cpm.re + cpp.re);
+                    gi[4] = gi[4] + kxkz * (-cmm.re - cmp.re + cpm.re + cpp.re);
+                    gi[5] = gi[5] + kykz * (-cmm.re + cmp.re - cpm.re + cpp.re);
+                }
+                double termx = Zero, termy = Zero;
+                for (int c = 0; c < 4; ++c) termx = termx + (Sd[c].re * S[c].re + Sd[c].im * S[c].im);
+                for (int c = 0; c < 4; ++c) termy = termy + (S[c].re * S[c].re + S[c].im * S[c].im);
+                double termz = One - (kx * kx + ky * ky + kz * kz) / (Two * s->ualpha2);
+                *virelec = *virelec - s->kfac[kn - 1] * (Two * termx + termy * termz);
+            }
+        }
+    }
+    free(Sd);
+    free(er);
+}
+
+/* UDipoleEwaldRecSPM (energy.F90:2046-2170): the generalized charge mesh
+   (charges and the dipoles through the B-spline derivatives), SPMFFTRec,
+   then per atom the potential, field and field gradient (second
+   derivatives of the B-splines) and the virial's dipole term */
+static int dipole_rec_spm(orc_sys *s, const double *dip, double *potstat, double *estat, double *efg,
+                          double *virelec) {
+    int order = s->order, *S3 = s->s, na = s->np;
+    size_t n3 = (size_t)S3[0] * S3[1] * S3[2];
+    double *spl = (double *)xcalloc((size_t)na * 3 * order, sizeof(double));
+    double *der = (double *)xcalloc((size_t)na * 3 * order, sizeof(double));
+    double *der2 = (double *)xcalloc((size_t)na * 3 * order, sizeof(double));
+    int *mm = (int *)xcalloc((size_t)na * 3, sizeof(int));
+    if (!spl || !der || !der2 || !mm) { free(spl); free(der); free(der2); free(mm); return MG_ERR_ALLOC; }
+#define SP(a, i, m, ia) (a)[((size_t)(ia) * 3 + (m)) * order + (i)]
+    memset(s->Qmesh, 0, sizeof(double) * n3);
+    for (int ia = 0; ia < na; ++ia) {
+        double dipx2 = dip[3 * ia] * s->dkdr[0], dipy2 = dip[3 * ia + 1] * s->dkdr[1], dipz2 = dip[3 * ia + 2] * s->dkdr[2];
+        for (int m = 0; m < 3; ++m) {
+            int kmax;
+            cardinal_bspline2(order, s->dkdr[m] * s->ro[3 * ia + m], &kmax, &SP(spl, 0, m, ia), &SP(der, 0, m, ia),
+                              &SP(der2, 0, m, ia));
+            mm[3 * ia + m] = (kmax + S3[m]) % S3[m];
+        }
+        for (int iz = 0; iz <= order - 1; ++iz) {
+            int nz = (S3[2] + mm[3 * ia + 2] - iz) % S3[2];
+            double splz = SP(spl, iz, 2, ia), dsdz = SP(der, iz, 2, ia);
+            for (int iy = 0; iy <= order - 1; ++iy) {
+                int ny = (S3[1] + mm[3 * ia + 1] - iy) % S3[1];
+                double sply = SP(spl, iy, 1, ia);
+                double q1 = s->az[ia] * sply * splz;
+                double dipx1 = dipx2 * sply * splz;
+                double dipy1 = dipy2 * SP(der, iy, 1, ia) * splz;
+                double dipz1 = dipz2 * sply * dsdz;
+                for (int ix = 0; ix <= order - 1; ++ix) {
+                    int nx = (S3[0] + mm[3 * ia] - ix) % S3[0];
+                    double splx = SP(spl, ix, 0, ia);
+                    double q = q1 * splx, dx = dipx1 * SP(der, ix, 0, ia), dy = dipy1 * splx, dz = dipz1 * splx;
+                    QM(s->Qmesh, nx, ny, nz) = QM(s->Qmesh, nx, ny, nz) + (q + dx + dy + dz);
+                }
+            }
+        }
+    }
+    double uloc;
+    int st = spm_fft_rec(s, 0, &uloc, virelec);
+    if (st) { free(spl); free(der); free(der2); free(mm); return st; }
+    const double *dk = s->dkdr;
+    double d2k[6] = {dk[0] * dk[0], dk[1] * dk[1], dk[2] * dk[2], dk[0] * dk[1], dk[0] * dk[2], dk[1] * dk[2]};
+    for (int ia = 0; ia < na; ++ia) {
+        double dipx2 = dip[3 * ia] * dk[0], dipy2 = dip[3 * ia + 1] * dk[1], dipz2 = dip[3 * ia + 2] * dk[2];
+        double psum = Zero, es[3] = {Zero, Zero, Zero}, gs[6] = {Zero, Zero, Zero, Zero, Zero, Zero};
+        for (int iz = 0; iz <= order - 1; ++iz) {
+            int nz = (S3[2] + mm[3 * ia + 2] - iz) % S3[2];
+            double splz = SP(spl, iz, 2, ia), dsdz = SP(der, iz, 2, ia), d2sdz = SP(der2, iz, 2, ia);
+            for (int iy = 0; iy <= order - 1; ++iy) {
+                int ny = (S3[1] + mm[3 * ia + 1] - iy) % S3[1];
+                double sply = SP(spl, iy, 1, ia), dsdy = SP(der, iy, 1, ia), d2sdy = SP(der2, iy, 1, ia);
+                for (int ix = 0; ix <= order - 1; ++ix) {
+                    int nx = (S3[0] + mm[3 * ia] - ix) % S3[0];
+                    double splx = SP(spl, ix, 0, ia), dsdx = SP(der, ix, 0, ia), d2sdx = SP(der2, ix, 0, ia);
+                    double Qval = QM(s->Qmesh, nx, ny, nz);
+                    psum = psum + splx * sply * splz * Qval;
+                    es[0] = es[0] + dsdx * sply * splz * Qval;
+                    es[1] = es[1] + splx * dsdy * splz * Qval;
+                    es[2] = es[2] + splx * sply * dsdz * Qval;
+                    gs[0] = gs[0] + d2sdx * sply * splz * Qval;
+                    gs[1] = gs[1] + splx * d2sdy * splz * Qval;
+                    gs[2] = gs[2] + splx * sply * d2sdz * Qval;
+                    gs[3] = gs[3] + dsdx * dsdy * splz * Qval;
+                    gs[4] = gs[4] + dsdx * sply * dsdz * Qval;
+                    gs[5] = gs[5] + splx * dsdy * dsdz * Qval;
+                    double Qdip = dipx2 * dsdx * sply * splz + dipy2 * splx * dsdy * splz + dipz2 * splx * sply * dsdz;
+                    *virelec = *virelec - Qdip * Qval;
+                }
+            }
+        }
+        potstat[ia] = potstat[ia] + psum;
+        for (int m = 0; m < 3; ++m) estat[3 * ia + m] = estat[3 * ia + m] - es[m] * dk[m];
+        for (int m = 0; m < 6; ++m) efg[6 * ia + m] = efg[6 * ia + m] - gs[m] * d2k[m];
+    }
+#undef SP
+    free(spl); free(der); free(der2); free(mm);
+    return 0;
+}
+
+/* UDipoleEwald's reciprocal part and the atomic part of UDipoleEwaldSelf
+   (energy.F90:1807-1830, 2183-2191) on a handle whose particles are the
+   atoms (positions, charges az): adds to potstat, estat, efg and virelec.
+   Leaves the handle's mesh and structure factors as scratch. */
+int orc_dipole_ewald(orc_sys *s, const double *dip, double *potstat, double *estat, double *efg, double *virelec) {
+    if (s->ewald == MG_EWALD_STD) dipole_rec_std(s, dip, potstat, estat, efg, virelec);
+    else if (s->ewald == MG_EWALD_SPM) {
+        int st = dipole_rec_spm(s, dip, potstat, estat, efg, virelec);
+        if (st) return st;
+    } else return MG_ERR_STATE;
+    double f1, f2, f3, s1, s2;
+    dipole_ewald_facs(s->ualpha, &f1, &f2, &f3, &s1, &s2);
+    for (int ia = 0; ia < s->np; ++ia) potstat[ia] = potstat[ia] - s1 * s->az[ia];
+    for (int ia = 0; ia < s->np; ++ia)
+        for (int m = 0; m < 3; ++m) estat[3 * ia + m] = estat[3 * ia + m] + s2 * dip[3 * ia + m];
+    for (int ia = 0; ia < s->np; ++ia)
+        for (int m = 0; m < 3; ++m) efg[6 * ia + m] = efg[6 * ia + m] - s2 * s->az[ia];
+    return 0;
+}
+
 /* UEwald, energy.F90:905-960 */
 static int uewald(orc_sys *s) {
     double virrec = Zero;
@@ -1799,7 +1978,8 @@ int orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double 
    (ipnan) the scaled force, the torque of the scaled force about the
    particle centre, and (r_a - ro_p) . f_a (unscaled) to virmolecule */
 int orc_poly_epilogue(const mg_poly_params *p, const double *ro, const double *r, const double *force,
-                      double force_fac, double *forceo, double *torqueo, double *virmolecule) {
+                      const double *torque, double force_fac, double *forceo, double *torqueo,
+                      double *virmolecule) {
     double virmol = Zero;
     for (int k = 0; k < 3 * p->np; ++k) forceo[k] = torqueo[k] = Zero;
     for (int ip = 1; ip <= p->np; ++ip) {
@@ -1818,6 +1998,11 @@ int orc_poly_epilogue(const mg_poly_params *p, const double *ro, const double *r
             to[0] = to[0] + (dy * gz - dz * gy);
             to[1] = to[1] + (dz * gx - dx * gz);
             to[2] = to[2] + (dx * gy - dy * gx);
+            if (torque) {   /* + torque(m,ia)*fac, the atom torques of the dipole electrostatics */
+                to[0] = to[0] + torque[3 * (ia - 1)] * force_fac;
+                to[1] = to[1] + torque[3 * (ia - 1) + 1] * force_fac;
+                to[2] = to[2] + torque[3 * (ia - 1) + 2] * force_fac;
+            }
         }
     }
     *virmolecule = virmol;
@@ -1861,6 +2046,298 @@ int orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force
         }
     }
     *u_rec = p->epsi_four_pi * u;
+    return 0;
+}
+
+/* ---- electrostatics of charges and point dipoles (UDipole, energy.F90:1476-1579) ----
+   potstat(na), estat(3,na), efg(6,na) (xx, yy, zz, xy, xz, yz) and virelec
+   as the reference's module arrays; nothing is scaled by EpsiFourPi until
+   the UDipole loop (orc_poly_udipole_finish). */
+
+/* CardinalBSpline, mollib.F90:1629-1685, with the second derivatives: they
+   come from the values of order-2, saved when the recursion reaches n =
+   order-1 (zero for order 3 and below, as there) */
+static void cardinal_bspline2(int order, double pos, int *kmax, double *values, double *derivs, double *derivs2) {
+    double lastvals[64], lastvals2[64];
+    int v = (int)floor(pos), n, i;
+    double x = pos - v, a;
+    *kmax = v;
+    for (i = 0; i < order; ++i) { lastvals[i] = Zero; lastvals2[i] = Zero; values[i] = Zero; }
+    values[0] = x;
+    if (order > 1) {
+        values[1] = (One - x);
+        for (n = 3; n <= order; ++n) {
+            for (i = 0; i < order; ++i) lastvals[i] = values[i];
+            if (n == order - 1)
+                for (i = 0; i < order; ++i) lastvals2[i] = values[i];
+            values[0] = x * lastvals[0] / (n - 1);
+            for (i = 1; i <= n - 2; ++i) {
+                a = i + x;
+                values[i] = (a * lastvals[i] + (n - a) * lastvals[i - 1]) / (n - 1);
+            }
+            values[n - 1] = (1 - x) * lastvals[n - 2] / (n - 1);
+        }
+        n = order;
+        derivs[0] = lastvals[0];
+        for (i = 1; i <= n - 2; ++i) derivs[i] = lastvals[i] - lastvals[i - 1];
+        derivs[n - 1] = -lastvals[n - 2];
+        derivs2[0] = lastvals2[0];
+        derivs2[1] = lastvals2[1] - 2 * lastvals2[0];
+        for (i = 2; i <= n - 3; ++i) derivs2[i] = lastvals2[i] - 2 * lastvals2[i - 1] + lastvals2[i - 2];
+        if (n > 3) derivs2[n - 2] = -2 * lastvals2[n - 3] + lastvals2[n - 4];
+        if (n > 2) derivs2[n - 1] = lastvals2[n - 3];
+    } else {
+        derivs[0] = Zero;
+        derivs2[0] = Zero;
+    }
+}
+
+/* the Ewald constants of EwaldSetup, energy.F90:7040-7047 */
+static void dipole_ewald_facs(double ualpha, double *f1, double *f2, double *f3, double *s1, double *s2) {
+    double ualpha2 = ualpha * ualpha;
+    double fac = One / (sqrt(Pi) * ualpha);
+    *f1 = fac * Two * ualpha2;
+    *f2 = fac * pow2(Two * ualpha2) / Three;
+    *f3 = fac * pow3(Two * ualpha2) / (Three * 5.0);
+    *s1 = (Two * ualpha) / sqrt(Pi);
+    *s2 = (Four * pow3(ualpha)) / (Three * sqrt(Pi));
+}
+
+/* UDipoleP, energy.F90:1588-1798: the particle pairs of the list (in MC
+   only jp > ip), the centre separation folded by PBC2 and that shift
+   applied to every atom pair; with Ewald (ualpha > 0) the erfc-screened
+   kernels, otherwise bare ones.  Initialises the arrays.  u_real is
+   UDipole's "ureal", EpsiFourPi/2 sum (q pot - dip . e), energy.F90:1494-1498. */
+int orc_poly_udipole_real(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                          const double *dip, const int32_t *nneighpn, const int32_t *jpnlist, double *potstat,
+                          double *estat, double *efg, double *virelec, double *u_real) {
+    const double *az = p->aza;
+    double half[3], rcut2 = p->rcut * p->rcut, vir = Zero;
+    int lewald = p->ualpha > Zero;
+    double ualpha = p->ualpha, ualpha2 = ualpha * ualpha, f1 = Zero, f2 = Zero, f3 = Zero, s1, s2;
+    if (lewald) dipole_ewald_facs(ualpha, &f1, &f2, &f3, &s1, &s2);
+    for (int m = 0; m < 3; ++m) half[m] = p->boxlen[m] / Two;
+    for (int k = 0; k < p->na; ++k) potstat[k] = Zero;
+    for (int k = 0; k < 3 * p->na; ++k) estat[k] = Zero;
+    for (int k = 0; k < 6 * p->na; ++k) efg[k] = Zero;
+    for (int ip = 1; ip <= p->np; ++ip) {
+        int ipt = p->iptpn[ip - 1];
+        int ialow = p->ianpn[ip - 1], iaupp = ialow + p->napt[ipt - 1] - 1;
+        for (int jploc = 1; jploc <= nneighpn[ip - 1]; ++jploc) {
+            int jp = jpnlist[(size_t)(ip - 1) * maxnneigh + jploc - 1];
+            if (p->lmc && jp < ip) continue;
+            int jpt = p->iptpn[jp - 1];
+            double d[3], sh[3];
+            for (int m = 0; m < 3; ++m) {
+                d[m] = ro[3 * (ip - 1) + m] - ro[3 * (jp - 1) + m];
+                sh[m] = Zero;
+                if (fabs(d[m]) > half[m]) sh[m] = fsign(p->boxlen[m], d[m]);
+                d[m] = d[m] - sh[m];
+            }
+            double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (r2 > rcut2) continue;
+            int jalow = p->ianpn[jp - 1], jaupp = jalow + p->napt[jpt - 1] - 1;
+            for (int ia = ialow; ia <= iaupp; ++ia) {
+                for (int ja = jalow; ja <= jaupp; ++ja) {
+                    double dx = r[3 * (ia - 1)] - r[3 * (ja - 1)] - sh[0];
+                    double dy = r[3 * (ia - 1) + 1] - r[3 * (ja - 1) + 1] - sh[1];
+                    double dz = r[3 * (ia - 1) + 2] - r[3 * (ja - 1) + 2] - sh[2];
+                    double ar2 = dx * dx + dy * dy + dz * dz;
+                    double r1 = sqrt(ar2);
+                    double r1i = One / r1;
+                    double r2i = r1i * r1i, r3i, r5i, r7i;
+                    if (lewald) {
+                        double ex = exp(-ualpha2 * ar2);
+                        r1i = r1i * (One - orc_erf2(ualpha * r1));
+                        r3i = r2i * (r1i + f1 * ex);
+                        r5i = r2i * (r3i + f2 * ex);
+                        r7i = r2i * (r5i + f3 * ex);
+                    } else {
+                        r3i = r2i * r1i;
+                        r5i = r2i * r3i;
+                        r7i = r2i * r5i;
+                    }
+                    double threer5i = Three * r5i;
+                    const double *di = &dip[3 * (ia - 1)], *dj = &dip[3 * (ja - 1)];
+                    double qi = az[ia - 1], qj = az[ja - 1];
+                    double doti = di[0] * dx + di[1] * dy + di[2] * dz;
+                    double dotj = dj[0] * dx + dj[1] * dy + dj[2] * dz;
+                    double dotir5i = Three * r5i * doti;
+                    double dotjr5i = Three * r5i * dotj;
+                    double dotir7i = (Three * 5.0 * r7i) * doti;
+                    double dotjr7i = (Three * 5.0 * r7i) * dotj;
+                    potstat[ia - 1] = potstat[ia - 1] + (qj * r1i + dotj * r3i);
+                    potstat[ja - 1] = potstat[ja - 1] + (qi * r1i - doti * r3i);
+                    double fx = (+qj * dx - dj[0]) * r3i + dotjr5i * dx;
+                    double fy = (+qj * dy - dj[1]) * r3i + dotjr5i * dy;
+                    double fz = (+qj * dz - dj[2]) * r3i + dotjr5i * dz;
+                    double *ei = &estat[3 * (ia - 1)], *ej = &estat[3 * (ja - 1)];
+                    ei[0] = ei[0] + fx;
+                    ei[1] = ei[1] + fy;
+                    ei[2] = ei[2] + fz;
+                    vir = vir - qi * (fx * dx + fy * dy + fz * dz);
+                    fx = (-qi * dx - di[0]) * r3i + dotir5i * dx;
+                    fy = (-qi * dy - di[1]) * r3i + dotir5i * dy;
+                    fz = (-qi * dz - di[2]) * r3i + dotir5i * dz;
+                    ej[0] = ej[0] + fx;
+                    ej[1] = ej[1] + fy;
+                    ej[2] = ej[2] + fz;
+                    double xx = qj * r3i + (-qj * dx * dx + Two * dj[0] * dx + dotj) * threer5i - dotjr7i * dx * dx;
+                    double yy = qj * r3i + (-qj * dy * dy + Two * dj[1] * dy + dotj) * threer5i - dotjr7i * dy * dy;
+                    double zz = qj * r3i + (-qj * dz * dz + Two * dj[2] * dz + dotj) * threer5i - dotjr7i * dz * dz;
+                    double xy = (-qj * dx * dy + dj[0] * dy + dj[1] * dx) * threer5i - dotjr7i * dx * dy;
+                    double xz = (-qj * dx * dz + dj[0] * dz + dj[2] * dx) * threer5i - dotjr7i * dx * dz;
+                    double yz = (-qj * dy * dz + dj[1] * dz + dj[2] * dy) * threer5i - dotjr7i * dy * dz;
+                    double *gi = &efg[6 * (ia - 1)], *gj = &efg[6 * (ja - 1)];
+                    gi[0] = gi[0] + xx; gi[1] = gi[1] + yy; gi[2] = gi[2] + zz;
+                    gi[3] = gi[3] + xy; gi[4] = gi[4] + xz; gi[5] = gi[5] + yz;
+                    vir = vir - (di[0] * xx * dx + di[0] * xy * dy + di[0] * xz * dz
+                               + di[1] * xy * dx + di[1] * yy * dy + di[1] * yz * dz
+                               + di[2] * xz * dx + di[2] * yz * dy + di[2] * zz * dz);
+                    xx = qi * r3i + (-qi * dx * dx - Two * di[0] * dx - doti) * threer5i + dotir7i * dx * dx;
+                    yy = qi * r3i + (-qi * dy * dy - Two * di[1] * dy - doti) * threer5i + dotir7i * dy * dy;
+                    zz = qi * r3i + (-qi * dz * dz - Two * di[2] * dz - doti) * threer5i + dotir7i * dz * dz;
+                    xy = (-qi * dx * dy - di[0] * dy - di[1] * dx) * threer5i + dotir7i * dx * dy;
+                    xz = (-qi * dx * dz - di[0] * dz - di[2] * dx) * threer5i + dotir7i * dx * dz;
+                    yz = (-qi * dy * dz - di[1] * dz - di[2] * dy) * threer5i + dotir7i * dy * dz;
+                    gj[0] = gj[0] + xx; gj[1] = gj[1] + yy; gj[2] = gj[2] + zz;
+                    gj[3] = gj[3] + xy; gj[4] = gj[4] + xz; gj[5] = gj[5] + yz;
+                }
+            }
+        }
+    }
+    *virelec = vir;
+    double ur = Zero;
+    for (int ia = 0; ia < p->na; ++ia)
+        ur = ur + az[ia] * potstat[ia] - (dip[3 * ia] * estat[3 * ia] + dip[3 * ia + 1] * estat[3 * ia + 1]
+                                          + dip[3 * ia + 2] * estat[3 * ia + 2]);
+    *u_real = p->epsi_four_pi * Half * ur;
+    return 0;
+}
+
+/* UDipoleEwaldSelf, molecular contribution (energy.F90:2196-2268), and with
+   lsurf UDipoleEwaldSurf (energy.F90:2272-2295; the atom positions r as
+   they are, not folded into the box) */
+int orc_poly_udipole_self(const mg_poly_params *p, const double *r, const double *dip, int32_t lsurf,
+                          double *potstat, double *estat, double *efg, double *virelec) {
+    const double *az = p->aza;
+    double ualpha = p->ualpha, ualpha2 = ualpha * ualpha, f1, f2, f3, s1, s2;
+    dipole_ewald_facs(ualpha, &f1, &f2, &f3, &s1, &s2);
+    double vir = *virelec;
+    for (int ip = 1; ip <= p->np; ++ip) {
+        int ipt = p->iptpn[ip - 1];
+        int ialow = p->ianpn[ip - 1], iaupp = ialow + p->napt[ipt - 1] - 1;
+        for (int ia = ialow; ia <= iaupp; ++ia) {
+            for (int ja = ia + 1; ja <= iaupp; ++ja) {
+                double dx = r[3 * (ia - 1)] - r[3 * (ja - 1)];
+                double dy = r[3 * (ia - 1) + 1] - r[3 * (ja - 1) + 1];
+                double dz = r[3 * (ia - 1) + 2] - r[3 * (ja - 1) + 2];
+                double ar2 = dx * dx + dy * dy + dz * dz;
+                double r1 = sqrt(ar2);
+                double r1i = One / r1;
+                double r2i = r1i * r1i;
+                double ex = exp(-ualpha2 * ar2);
+                r1i = r1i * orc_erf2(ualpha * r1);
+                double r3i = r2i * (r1i - f1 * ex);
+                double r5i = r2i * (r3i - f2 * ex);
+                double r7i = r2i * (r5i - f3 * ex);
+                double threer5i = Three * r5i;
+                const double *di = &dip[3 * (ia - 1)], *dj = &dip[3 * (ja - 1)];
+                double qi = az[ia - 1], qj = az[ja - 1];
+                double doti = di[0] * dx + di[1] * dy + di[2] * dz;
+                double dotj = dj[0] * dx + dj[1] * dy + dj[2] * dz;
+                double dotir5i = Three * r5i * doti;
+                double dotjr5i = Three * r5i * dotj;
+                double dotir7i = (Three * 5.0 * r7i) * doti;
+                double dotjr7i = (Three * 5.0 * r7i) * dotj;
+                potstat[ia - 1] = potstat[ia - 1] - (qj * r1i + dotj * r3i);
+                potstat[ja - 1] = potstat[ja - 1] - (qi * r1i - doti * r3i);
+                double fx = -((qj * dx - dj[0]) * r3i + dotjr5i * dx);
+                double fy = -((qj * dy - dj[1]) * r3i + dotjr5i * dy);
+                double fz = -((qj * dz - dj[2]) * r3i + dotjr5i * dz);
+                double *ei = &estat[3 * (ia - 1)], *ej = &estat[3 * (ja - 1)];
+                ei[0] = ei[0] + fx;
+                ei[1] = ei[1] + fy;
+                ei[2] = ei[2] + fz;
+                vir = vir - (qi * (fx * dx + fy * dy + fz * dz));
+                fx = -((-qi * dx - di[0]) * r3i + dotir5i * dx);
+                fy = -((-qi * dy - di[1]) * r3i + dotir5i * dy);
+                fz = -((-qi * dz - di[2]) * r3i + dotir5i * dz);
+                ej[0] = ej[0] + fx;
+                ej[1] = ej[1] + fy;
+                ej[2] = ej[2] + fz;
+                double xx = -(qj * r3i + (-qj * dx * dx + Two * dj[0] * dx + dotj) * threer5i - dotjr7i * dx * dx);
+                double yy = -(qj * r3i + (-qj * dy * dy + Two * dj[1] * dy + dotj) * threer5i - dotjr7i * dy * dy);
+                double zz = -(qj * r3i + (-qj * dz * dz + Two * dj[2] * dz + dotj) * threer5i - dotjr7i * dz * dz);
+                double xy = -((-qj * dx * dy + dj[0] * dy + dj[1] * dx) * threer5i - dotjr7i * dx * dy);
+                double xz = -((-qj * dx * dz + dj[0] * dz + dj[2] * dx) * threer5i - dotjr7i * dx * dz);
+                double yz = -((-qj * dy * dz + dj[1] * dz + dj[2] * dy) * threer5i - dotjr7i * dy * dz);
+                double *gi = &efg[6 * (ia - 1)], *gj = &efg[6 * (ja - 1)];
+                gi[0] = gi[0] + xx; gi[1] = gi[1] + yy; gi[2] = gi[2] + zz;
+                gi[3] = gi[3] + xy; gi[4] = gi[4] + xz; gi[5] = gi[5] + yz;
+                vir = vir - (di[0] * xx * dx + di[0] * xy * dy + di[0] * xz * dz
+                           + di[1] * xy * dx + di[1] * yy * dy + di[1] * yz * dz
+                           + di[2] * xz * dx + di[2] * yz * dy + di[2] * zz * dz);
+                xx = -(qi * r3i + (-qi * dx * dx - Two * di[0] * dx - doti) * threer5i + dotir7i * dx * dx);
+                yy = -(qi * r3i + (-qi * dy * dy - Two * di[1] * dy - doti) * threer5i + dotir7i * dy * dy);
+                zz = -(qi * r3i + (-qi * dz * dz - Two * di[2] * dz - doti) * threer5i + dotir7i * dz * dz);
+                xy = -((-qi * dx * dy - di[0] * dy - di[1] * dx) * threer5i + dotir7i * dx * dy);
+                xz = -((-qi * dx * dz - di[0] * dz - di[2] * dx) * threer5i + dotir7i * dx * dz);
+                yz = -((-qi * dy * dz - di[1] * dz - di[2] * dy) * threer5i + dotir7i * dy * dz);
+                gj[0] = gj[0] + xx; gj[1] = gj[1] + yy; gj[2] = gj[2] + zz;
+                gj[3] = gj[3] + xy; gj[4] = gj[4] + xz; gj[5] = gj[5] + yz;
+            }
+        }
+    }
+    if (lsurf) {
+        double vol = p->boxlen[0] * p->boxlen[1] * p->boxlen[2];
+        double fac = (Four * Pi / Three) / vol;
+        double sqx = Zero, sqy = Zero, sqz = Zero, sdx = Zero, sdy = Zero, sdz = Zero;
+        for (int ia = 0; ia < p->na; ++ia) sqx = sqx + az[ia] * r[3 * ia];
+        for (int ia = 0; ia < p->na; ++ia) sqy = sqy + az[ia] * r[3 * ia + 1];
+        for (int ia = 0; ia < p->na; ++ia) sqz = sqz + az[ia] * r[3 * ia + 2];
+        for (int ia = 0; ia < p->na; ++ia) sdx = sdx + dip[3 * ia];
+        for (int ia = 0; ia < p->na; ++ia) sdy = sdy + dip[3 * ia + 1];
+        for (int ia = 0; ia < p->na; ++ia) sdz = sdz + dip[3 * ia + 2];
+        for (int ia = 0; ia < p->na; ++ia)
+            potstat[ia] = potstat[ia] + fac * (r[3 * ia] * (sqx + sdx) + r[3 * ia + 1] * (sqy + sdy)
+                                               + r[3 * ia + 2] * (sqz + sdz));
+        for (int ia = 0; ia < p->na; ++ia) {
+            estat[3 * ia] = estat[3 * ia] - fac * (sqx + sdx);
+            estat[3 * ia + 1] = estat[3 * ia + 1] - fac * (sqy + sdy);
+            estat[3 * ia + 2] = estat[3 * ia + 2] - fac * (sqz + sdz);
+        }
+        vir = vir - TwoPi / (Three * vol) * ((sqx * sqx + sqy * sqy + sqz * sqz)
+                                            + Two * (Two * (sqx * sdx + sqy * sdy + sqz * sdz))
+                                            + Three * (sdx * sdx + sdy * sdy + sdz * sdz));
+    }
+    *virelec = vir;
+    return 0;
+}
+
+/* UDipole's loop, energy.F90:1510-1545: u%stat = EpsiFourPi/2 sum (q pot -
+   dip . e); force(ia) += EpsiFourPi (q e + dip . efg) (added to force, as
+   the reference adds to the UTwoBodyP forces); torque(ia) = EpsiFourPi
+   dip x e (added to torque) */
+int orc_poly_udipole_finish(const mg_poly_params *p, const double *dip, const double *potstat, const double *estat,
+                            const double *efg, double *force, double *torque, double *u_stat) {
+    const double *az = p->aza;
+    double efp = p->epsi_four_pi, us = Zero;
+    for (int ia = 0; ia < p->na; ++ia) {
+        const double *d = &dip[3 * ia], *e = &estat[3 * ia], *g = &efg[6 * ia];
+        double q = az[ia];
+        us = us + q * potstat[ia] - (d[0] * e[0] + d[1] * e[1] + d[2] * e[2]);
+        double fx = q * e[0] + (d[0] * g[0] + d[1] * g[3] + d[2] * g[4]);
+        double fy = q * e[1] + (d[0] * g[3] + d[1] * g[1] + d[2] * g[5]);
+        double fz = q * e[2] + (d[0] * g[4] + d[1] * g[5] + d[2] * g[2]);
+        force[3 * ia] = force[3 * ia] + efp * fx;
+        force[3 * ia + 1] = force[3 * ia + 1] + efp * fy;
+        force[3 * ia + 2] = force[3 * ia + 2] + efp * fz;
+        torque[3 * ia] = torque[3 * ia] + efp * (d[1] * e[2] - d[2] * e[1]);
+        torque[3 * ia + 1] = torque[3 * ia + 1] + efp * (d[2] * e[0] - d[0] * e[2]);
+        torque[3 * ia + 2] = torque[3 * ia + 2] + efp * (d[0] * e[1] - d[1] * e[0]);
+    }
+    *u_stat = efp * Half * us;
     return 0;
 }
 

@@ -84,7 +84,27 @@ int  orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double
 /* the end of UTotal for polyatomic particles (energy.F90:405-427),
    arguments as mg_poly_epilogue's */
 int  orc_poly_epilogue(const mg_poly_params *p, const double *ro, const double *r, const double *force,
-                       double force_fac, double *forceo, double *torqueo, double *virmolecule);
+                       const double *torque, double force_fac, double *forceo, double *torqueo,
+                       double *virmolecule);
+/* UDipole with Ewald (energy.F90:1476-2295), arguments as the library's
+   mg_poly_udipole_real/_self/_finish and mg_dipole_ewald (on an atom handle) */
+int  orc_poly_udipole_real(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                           const double *dip, const int32_t *nneighpn, const int32_t *jpnlist, double *potstat,
+                           double *estat, double *efg, double *virelec, double *u_real);
+int  orc_poly_udipole_self(const mg_poly_params *p, const double *r, const double *dip, int32_t lsurf,
+                           double *potstat, double *estat, double *efg, double *virelec);
+int  orc_poly_udipole_finish(const mg_poly_params *p, const double *dip, const double *potstat,
+                             const double *estat, const double *efg, double *force, double *torque,
+                             double *u_stat);
+int  orc_dipole_ewald(orc_sys *s, const double *dip, double *potstat, double *estat, double *efg,
+                      double *virelec);
+/* rigid-body VelVer (md.F90:252-420) in parts, the state held by the caller */
+int  orc_angvel_to_quavel(int32_t np, const double *qua, const double *angvelo, double *quad);
+int  orc_rigid_move(int32_t np, double tstep, const double *boxlen, double *ro, double *qua, const double *rod,
+                    const double *rodd, const double *quad, const double *quadd, double *drostep, double *ori);
+int  orc_rigid_kick(int32_t np, double tstep, double tvvite, int32_t nvvite, const double *massip,
+                    const double *momp, const double *qua, const double *forceo, const double *torqueo,
+                    double *rod, double *rodd, double *quad, double *quadd, double *angvelo);
 /* the molecular part of UEwaldSelf (energy.F90:1301-1345), arguments as
    mg_poly_ewald_intra's */
 int  orc_poly_ewald_intra(const mg_poly_params *p, const double *r, double *force, double *u_rec);

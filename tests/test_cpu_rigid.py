@@ -215,7 +215,7 @@ def oracle_rigid_utotal(orc, s, ro, ori):
     vm = np.zeros(1)
     r = s.atom_positions()
     assert orc.orc_poly_epilogue(C.byref(p), abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)),
-                                 abi.f64(abi.as_f64(out["force"].reshape(-1))), units.FORCE_FAC, abi.f64(fo),
+                                 abi.f64(abi.as_f64(out["force"].reshape(-1))), None, units.FORCE_FAC, abi.f64(fo),
                                  abi.f64(to), abi.f64(vm)) == 0
     return out["u_tot"], fo.reshape(-1, 3), to.reshape(-1, 3)
 

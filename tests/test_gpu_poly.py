@@ -116,7 +116,7 @@ def test_poly_epilogue_matches_oracle(orc, gpu_lib):
     r = s.atom_positions()
     fo, to, vm = np.zeros(3 * s.np_), np.zeros(3 * s.np_), np.zeros(1)
     assert orc.orc_poly_epilogue(C.byref(p), abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)),
-                                 abi.f64(np.ascontiguousarray(g["force"].reshape(-1))), units.FORCE_FAC,
+                                 abi.f64(np.ascontiguousarray(g["force"].reshape(-1))), None, units.FORCE_FAC,
                                  abi.f64(fo), abi.f64(to), abi.f64(vm)) == 0
     assert np.array_equal(g["forceo"].reshape(-1), fo)
     assert np.array_equal(g["torqueo"].reshape(-1), to)
