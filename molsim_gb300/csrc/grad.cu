@@ -226,13 +226,13 @@ __global__ void k_grad_site(SiteArgs a) {
             c[d] = mm < 0 ? mm + a.n : mm;
             grad_bspline(a.order, pos - fl, w[d]);
         }
-        int mn = a.n - 1;
+        int mn = mg_mesh_mask(a.n);
         for (int iz = 0; iz < a.order; ++iz)
             for (int iy = 0; iy < a.order; ++iy) {
-                size_t row = ((size_t)((c[2] - iz) & mn) * a.n + ((c[1] - iy) & mn)) * a.n;
+                size_t row = ((size_t)mg_wrapm(c[2] - iz, a.n, mn) * a.n + mg_wrapm(c[1] - iy, a.n, mn)) * a.n;
                 double wyz = w[2][iz] * w[1][iy], s = 0.0;
                 for (int ix = 0; ix < a.order; ++ix) {
-                    size_t idx = row + ((c[0] - ix) & mn);
+                    size_t idx = row + mg_wrapm(c[0] - ix, a.n, mn);
                     double v = a.mixed ? (double)((const float *)a.mesh)[idx] : ((const double *)a.mesh)[idx];
                     s += w[0][ix] * v;
                 }

@@ -342,7 +342,7 @@ __global__ void k_mc_stamps(McArgs a, SpmArgs s, int ntrial) {
 __global__ void __launch_bounds__(kMcThreads) k_mc_spm(McArgs a, SpmArgs s) {
     __shared__ double red[2][kMcThreads / 32];
     int t = blockIdx.y, nsets = 2 * a.nptm, p = s.order, p3 = p * p * p;
-    int S = nsets * p3, n = s.n, mn = n - 1;
+    int S = nsets * p3, n = s.n, mn = mg_mesh_mask(n);
     const int *cor = s.corner + (size_t)t * nsets * 3;
     const double *wt = s.w + (size_t)t * nsets * 3 * p;
     const double *qs = s.qs + (size_t)t * nsets;
@@ -351,7 +351,8 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_spm(McArgs a, SpmArgs s) {
         int sa = ia / p3, r = ia % p3, ix = r % p, iy = (r / p) % p, iz = r / (p * p);
         const double *wa = wt + (size_t)sa * 3 * p;
         double da = qs[sa] * wa[ix] * wa[p + iy] * wa[2 * p + iz];
-        int xa = (cor[3 * sa] - ix) & mn, ya = (cor[3 * sa + 1] - iy) & mn, za = (cor[3 * sa + 2] - iz) & mn;
+        int xa = mg_wrapm(cor[3 * sa] - ix, n, mn), ya = mg_wrapm(cor[3 * sa + 1] - iy, n, mn),
+            za = mg_wrapm(cor[3 * sa + 2] - iz, n, mn);
         e1 += da * s.phi[((size_t)za * n + ya) * n + xa];
         double inner = 0.0;
         for (int sb = 0; sb < nsets; ++sb) {
@@ -359,13 +360,13 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_spm(McArgs a, SpmArgs s) {
             double qb = qs[sb];
             int cbx = cor[3 * sb], cby = cor[3 * sb + 1], cbz = cor[3 * sb + 2];
             for (int jz = 0; jz < p; ++jz) {
-                int dz = (za - cbz + jz) & mn;   // za - (cbz - jz)
+                int dz = mg_wrapm(za - cbz + jz, n, mn);   // za - (cbz - jz)
                 double wz = qb * wb[2 * p + jz];
                 for (int jy = 0; jy < p; ++jy) {
-                    int dy = (ya - cby + jy) & mn;
+                    int dy = mg_wrapm(ya - cby + jy, n, mn);
                     double wyz = wz * wb[p + jy];
                     const double *grow = s.g + ((size_t)dz * n + dy) * n;
-                    for (int jx = 0; jx < p; ++jx) inner += wyz * wb[jx] * grow[(xa - cbx + jx) & mn];
+                    for (int jx = 0; jx < p; ++jx) inner += wyz * wb[jx] * grow[mg_wrapm(xa - cbx + jx, n, mn)];
                 }
             }
         }
@@ -389,14 +390,15 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_spm(McArgs a, SpmArgs s) {
 // accept: Q += d, one thread in stamp order (deterministic)
 __global__ void k_mc_spm_accept(McArgs a, SpmArgs s, double *__restrict__ Q) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int nsets = 2 * a.nptm, p = s.order, n = s.n, mn = n - 1;
+    int nsets = 2 * a.nptm, p = s.order, n = s.n, mn = mg_mesh_mask(n);
     for (int sa = 0; sa < nsets; ++sa) {
         const int *c = s.corner + 3 * sa;
         const double *wa = s.w + (size_t)sa * 3 * p;
         for (int iz = 0; iz < p; ++iz)
             for (int iy = 0; iy < p; ++iy)
                 for (int ix = 0; ix < p; ++ix) {
-                    size_t idx = ((size_t)((c[2] - iz) & mn) * n + ((c[1] - iy) & mn)) * n + ((c[0] - ix) & mn);
+                    size_t idx = ((size_t)mg_wrapm(c[2] - iz, n, mn) * n + mg_wrapm(c[1] - iy, n, mn)) * n +
+                                 mg_wrapm(c[0] - ix, n, mn);
                     Q[idx] += s.qs[sa] * wa[ix] * wa[p + iy] * wa[2 * p + iz];
                 }
     }

@@ -153,6 +153,7 @@ struct mg_handle {
     void *d_tw = nullptr;           // twiddles exp(-2 pi i m/n), m < n
     int fft_tx = 0, fft_tiles = 0;
     int fft_plane = 0, fft_warps = 0;   // mixed form, 32 <= nmesh <= 128: three plane/slab passes
+    int gen_mesh = 0;                   // nmesh 2^a 3^b 5^c, not a power of two: generic spread and gather
     // mixed form with plane passes, MD/BD: the spread runs inside the forward
     // plane pass (particles sorted by the z plane of their stamp corner), so
     // the charge mesh never leaves shared memory
@@ -249,6 +250,15 @@ int mg_fail(mg_handle *h, int code, const char *fmt, ...);
             return mg_fail((h), MG_ERR_CUDA, "%s failed: %s (%s:%d)", #call,              \
                            cudaGetErrorString(e_), __FILE__, __LINE__);                    \
     } while (0)
+// x mod n in [0, n) for any int x: a mask when n is a power of two
+// (mn = n - 1), the remainder otherwise (mn < 0: meshes 2^a 3^b 5^c)
+__host__ __device__ __forceinline__ int mg_mesh_mask(int n) { return (n & (n - 1)) == 0 ? n - 1 : -1; }
+__host__ __device__ __forceinline__ int mg_wrapm(int x, int n, int mn) {
+    if (mn >= 0) return x & mn;
+    int r = x % n;
+    return r < 0 ? r + n : r;
+}
+
 #define MG_TRY(x)                  \
     do {                           \
         int s_ = (x);              \

@@ -70,14 +70,139 @@ __device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv &f) {
     return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
+// The line length of the FFT passes: a power of two (logn >= 0) or a
+// product 2^a 3^b 5^c (logn < 0), transformed by Stockham passes of the
+// radices r[0..nf) in that order; fn divides by n.
+struct FftPlan {
+    int logn, nf;
+    int r[12];
+    FastDiv fn;
+};
+
+static FftPlan make_plan(int n) {
+    FftPlan p = {};
+    p.fn = make_fastdiv((unsigned)n);
+    if ((n & (n - 1)) == 0) {
+        int l = 0;
+        while ((1 << l) < n) ++l;
+        p.logn = l;
+        return p;
+    }
+    p.logn = -1;
+    int m = n;
+    while (m % 4 == 0 && p.nf < 12) { p.r[p.nf++] = 4; m /= 4; }
+    while (m % 2 == 0 && p.nf < 12) { p.r[p.nf++] = 2; m /= 2; }
+    while (m % 3 == 0 && p.nf < 12) { p.r[p.nf++] = 3; m /= 3; }
+    while (m % 5 == 0 && p.nf < 12) { p.r[p.nf++] = 5; m /= 5; }
+    if (m != 1) p.nf = 0;   // not 2^a 3^b 5^c: rejected by the caller
+    return p;
+}
+
+// radix-R butterflies (R = 2, 3, 4, 5) on v[0..R), in place; sign -1
+// forward (w = exp(-2 pi i / R)), +1 backward
+template <typename T> __device__ __forceinline__ V2<T> mul_i(V2<T> a, T s) {   // s * i * a
+    V2<T> r;
+    r.x = -s * a.y;
+    r.y = s * a.x;
+    return r;
+}
+
+template <typename T> __device__ __forceinline__ void dft_small(V2<T> *v, int R, int sign) {
+    typedef V2<T> V;
+    const T sg = (T)sign;
+    if (R == 2) {
+        V a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else if (R == 4) {
+        V a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]), a2 = cadd(v[1], v[3]), a3 = csub(v[1], v[3]);
+        v[0] = cadd(a0, a2);
+        v[2] = csub(a0, a2);
+        V t = mul_i<T>(a3, sg);   // sign * i * (v1 - v3)
+        v[1] = cadd(a1, t);
+        v[3] = csub(a1, t);
+    } else if (R == 3) {
+        const T h = (T)0.86602540378443864676;   // sqrt(3)/2
+        V t1 = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+        V t2;
+        t2.x = v[0].x - (T)0.5 * t1.x;
+        t2.y = v[0].y - (T)0.5 * t1.y;
+        V t3 = mul_i<T>(d, sg * h);
+        v[0] = cadd(v[0], t1);
+        v[1] = cadd(t2, t3);
+        v[2] = csub(t2, t3);
+    } else {   // R == 5
+        const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;   // cos(2 pi/5), cos(4 pi/5)
+        const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;    // sin(2 pi/5), sin(4 pi/5)
+        V a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]), a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+        V x0 = v[0], r1, r2, i1, i2;
+        r1.x = x0.x + c1 * a1.x + c2 * a2.x;
+        r1.y = x0.y + c1 * a1.y + c2 * a2.y;
+        r2.x = x0.x + c2 * a1.x + c1 * a2.x;
+        r2.y = x0.y + c2 * a1.y + c1 * a2.y;
+        i1.x = s1 * b1.x + s2 * b2.x;
+        i1.y = s1 * b1.y + s2 * b2.y;
+        i2.x = s2 * b1.x - s1 * b2.x;
+        i2.y = s2 * b1.y - s1 * b2.y;
+        V j1 = mul_i<T>(i1, sg), j2 = mul_i<T>(i2, sg);
+        v[0] = cadd(x0, cadd(a1, a2));
+        v[1] = cadd(r1, j1);
+        v[4] = csub(r1, j1);
+        v[2] = cadd(r2, j2);
+        v[3] = csub(r2, j2);
+    }
+}
+
+// Stockham passes for n = 2^a 3^b 5^c (the radices of the plan): pass of
+// radix R at span Ns reads x[j + r n/R], twiddles by w^(r k n/(R Ns)) with
+// k = j mod Ns, and writes y[(j - k) R + k + r Ns]
+template <typename T, bool LINE_MAJOR>
+__device__ V2<T> *smem_fft_gen(V2<T> *A, V2<T> *B, int n, const FftPlan &pl, int nl, int cs, int ts, int sign,
+                               const V2<T> *__restrict__ tw, const FastDiv &fnl) {
+    typedef V2<T> V;
+    V *in = A, *out = B;
+    int tid = threadIdx.x, nthr = blockDim.x;
+    int Ns = 1;
+    for (int f = 0; f < pl.nf; ++f) {
+        int R = pl.r[f], m = n / R, stride = n / (R * Ns);
+        for (int b = tid; b < nl * m; b += nthr) {
+            int c, j;
+            if (LINE_MAJOR) { c = b / m; j = b - c * m; }
+            else { j = (int)fdiv((unsigned)b, fnl); c = b - j * nl; }
+            int k = j % Ns;
+            const V *src = in + c * cs;
+            V v[5];
+            for (int r = 0; r < R; ++r) {
+                v[r] = src[(j + r * m) * ts];
+                if (k && r) {
+                    V t = tw[r * k * stride];
+                    if (sign > 0) t.y = -t.y;
+                    v[r] = cmul(v[r], t);
+                }
+            }
+            dft_small<T>(v, R, sign);
+            int d = (j - k) * R + k;
+            V *dst = out + c * cs;
+            for (int r = 0; r < R; ++r) dst[(d + r * Ns) * ts] = v[r];
+        }
+        __syncthreads();
+        V *t = in; in = out; out = t;
+        Ns *= R;
+    }
+    return in;
+}
+
 // Stockham FFT of nl lines of length n = 2^logn held in shared memory.  Element
 // (line c, index t) is at buf[c*cs + t*ts].  LINE_MAJOR (ts == 1): threads run
 // along t; otherwise (cs == 1) threads run along c.  Returns the buffer that
-// holds the result.  sign = -1 forward, +1 backward (unnormalised).
+// holds the result.  sign = -1 forward, +1 backward (unnormalised).  Other
+// lengths (2^a 3^b 5^c) go to smem_fft_gen.
 template <typename T, bool LINE_MAJOR>
-__device__ V2<T> *smem_fft(V2<T> *A, V2<T> *B, int n, int logn, int nl, int cs, int ts, int sign,
+__device__ V2<T> *smem_fft(V2<T> *A, V2<T> *B, int n, const FftPlan &pl, int nl, int cs, int ts, int sign,
                            const V2<T> *__restrict__ tw, const FastDiv &fnl) {
     typedef V2<T> V;
+    if (pl.logn < 0) return smem_fft_gen<T, LINE_MAJOR>(A, B, n, pl, nl, cs, ts, sign, tw, fnl);
+    const int logn = pl.logn;
     V *in = A, *out = B;
     int tid = threadIdx.x, nthr = blockDim.x;
     int Ns = 1, logNs = 0;
@@ -151,11 +276,16 @@ __device__ __forceinline__ void load_tw(V2<T> *s_tw, const V2<T> *__restrict__ t
 template <typename T> __device__ __forceinline__ T fx_to_real(long long x);
 template <> __device__ __forceinline__ double fx_to_real<double>(long long x) { return (double)x; }
 template <> __device__ __forceinline__ float fx_to_real<float>(long long x) {
-    return (float)(int)(x >> 32) * 4294967296.0f + (float)(unsigned)(x & 0xffffffffll);
+    // x = hi 2^32 + lo with lo the signed low word, so that a small negative
+    // x converts as exactly as a small positive one (an unsigned low word
+    // would cancel 2^32 - |x| against -2^32 in single precision)
+    int lo = (int)(unsigned)(x & 0xffffffffll);
+    int hi = (int)((x - lo) >> 32);
+    return (float)hi * 4294967296.0f + (float)lo;
 }
 
 template <typename T>
-__global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *__restrict__ F, int n, int logn,
+__global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *__restrict__ F, int n, FftPlan pl,
                             int lp, const V2<T> *__restrict__ tw, FastDiv fnh) {
     typedef V2<T> V;
     extern __shared__ unsigned char smem_raw[];
@@ -165,7 +295,7 @@ __global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *
     load_tw<T>(s_tw, tw, n);
     size_t line0 = (size_t)blockIdx.x * 2 * lp;
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
-        int c = e >> logn, t = e & (n - 1);
+        int c = (int)fdiv((unsigned)e, pl.fn), t = e - c * n;
         // the spread's fixed-point mesh (cleared after this pass)
         long long q0 = Qfx[(line0 + 2 * c) * n + t], q1 = Qfx[(line0 + 2 * c + 1) * n + t];
         V v;
@@ -174,10 +304,10 @@ __global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *
         A[c * n + t] = v;
     }
     __syncthreads();
-    V *Z = smem_fft<T, true>(A, B, n, logn, lp, n, 1, -1, s_tw, fnh);
+    V *Z = smem_fft<T, true>(A, B, n, pl, lp, n, 1, -1, s_tw, fnh);
     for (int e = threadIdx.x; e < lp * nh; e += blockDim.x) {
         int c = (int)fdiv((unsigned)e, fnh), k = e - c * nh;
-        V z = Z[c * n + k], zc = Z[c * n + ((n - k) & (n - 1))];
+        V z = Z[c * n + k], zc = Z[c * n + (k ? n - k : 0)];
         V a, b;
         // X_A = (Z_k + conj Z_{n-k})/2,  X_B = (Z_k - conj Z_{n-k})/(2i)
         a.x = (T)0.5 * (z.x + zc.x);
@@ -191,7 +321,7 @@ __global__ void k_fft_x_r2c(const long long *__restrict__ Qfx, T fx_inv, V2<T> *
 
 // ---- x pass: c2r (Hermitian input; imaginary parts of k=0, n/2 dropped) ----
 template <typename T>
-__global__ void k_fft_x_c2r(const V2<T> *__restrict__ F, T *__restrict__ Q, int n, int logn,
+__global__ void k_fft_x_c2r(const V2<T> *__restrict__ F, T *__restrict__ Q, int n, FftPlan pl,
                             int lp, const V2<T> *__restrict__ tw) {
     typedef V2<T> V;
     extern __shared__ unsigned char smem_raw[];
@@ -201,10 +331,10 @@ __global__ void k_fft_x_c2r(const V2<T> *__restrict__ F, T *__restrict__ Q, int 
     load_tw<T>(s_tw, tw, n);
     size_t line0 = (size_t)blockIdx.x * 2 * lp;
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
-        int c = e >> logn, k = e & (n - 1);
+        int c = (int)fdiv((unsigned)e, pl.fn), k = e - c * n;
         int kk = (k < nh) ? k : n - k;
         V a = F[(line0 + 2 * c) * nh + kk], b = F[(line0 + 2 * c + 1) * nh + kk];
-        if (kk == 0 || kk == n / 2) { a.y = (T)0; b.y = (T)0; }
+        if (kk == 0 || 2 * kk == n) { a.y = (T)0; b.y = (T)0; }
         if (k >= nh) { a.y = -a.y; b.y = -b.y; }
         V z;
         z.x = a.x - b.y;
@@ -212,9 +342,9 @@ __global__ void k_fft_x_c2r(const V2<T> *__restrict__ F, T *__restrict__ Q, int 
         A[c * n + k] = z;
     }
     __syncthreads();
-    V *Z = smem_fft<T, true>(A, B, n, logn, lp, n, 1, +1, s_tw, FastDiv{});
+    V *Z = smem_fft<T, true>(A, B, n, pl, lp, n, 1, +1, s_tw, FastDiv{});
     for (int e = threadIdx.x; e < lp * n; e += blockDim.x) {
-        int c = e >> logn, t = e & (n - 1);
+        int c = (int)fdiv((unsigned)e, pl.fn), t = e - c * n;
         V z = Z[c * n + t];
         Q[(line0 + 2 * c) * n + t] = z.x;
         Q[(line0 + 2 * c + 1) * n + t] = z.y;
@@ -229,7 +359,7 @@ struct ConvArgs {
 // ---- column passes (y or z); with CONV the influence function and the
 //      inverse transform follow the forward one -------------------------------
 template <typename T, bool CONV>
-__global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx, size_t tstride,
+__global__ void k_fft_col(V2<T> *__restrict__ F, int n, FftPlan pl, int nh, int tx, size_t tstride,
                           size_t ostride, int sign, const V2<T> *__restrict__ tw, ConvArgs cv, FastDiv ftx) {
     typedef V2<T> V;
     extern __shared__ unsigned char smem_raw[];
@@ -249,12 +379,12 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
         A[t * tx + c] = v;
     }
     __syncthreads();
-    V *R = smem_fft<T, false>(A, B, n, logn, tx, 1, tx, sign, s_tw, ftx);
+    V *R = smem_fft<T, false>(A, B, n, pl, tx, 1, tx, sign, s_tw, ftx);
     if (CONV) {
         const T *mf = (const T *)cv.mf, *ew = (const T *)cv.ew, *vw = (const T *)cv.vw;
         int ky = blockIdx.y;
         int fy = min(ky, n - ky);
-        T e_t = 0, v_t = 0;   // per-thread sums in the mesh type, block sums in FP64
+        double e_t = 0, v_t = 0;   // per-element products in the mesh type, sums in FP64
         for (int e = threadIdx.x; e < tx * n; e += blockDim.x) {
             int t = (int)fdiv((unsigned)e, ftx), c = e - t * tx;
             int kx = kx0 + c;
@@ -263,19 +393,19 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
             size_t id = ((size_t)fz * nh + fy) * nh + kx;
             V f = R[t * tx + c];
             T p2 = f.x * f.x + f.y * f.y;
-            e_t += p2 * ew[id];
-            v_t -= p2 * vw[id];
+            e_t += (double)(p2 * ew[id]);
+            v_t -= (double)(p2 * vw[id]);
             T m = mf[id];
             f.x *= m;
             f.y *= m;
             R[t * tx + c] = f;
         }
         int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-        for (int o = 16; o > 0; o >>= 1) {   // warp sums in the mesh type, FP64 across warps
+        for (int o = 16; o > 0; o >>= 1) {
             e_t += __shfl_down_sync(0xffffffffu, e_t, o);
             v_t += __shfl_down_sync(0xffffffffu, v_t, o);
         }
-        if (lane == 0) { red[w] = (double)e_t; red[32 + w] = (double)v_t; }
+        if (lane == 0) { red[w] = e_t; red[32 + w] = v_t; }
         __syncthreads();
         if (threadIdx.x == 0) {
             double se = 0.0, sv = 0.0;
@@ -285,7 +415,7 @@ __global__ void k_fft_col(V2<T> *__restrict__ F, int n, int logn, int nh, int tx
             cv.part[2 * blk + 1] = sv;
         }
         V *other = (R == A) ? B : A;
-        R = smem_fft<T, false>(R, other, n, logn, tx, 1, tx, +1, s_tw, ftx);
+        R = smem_fft<T, false>(R, other, n, pl, tx, 1, tx, +1, s_tw, ftx);
     }
     for (int e = threadIdx.x; e < tx * n; e += blockDim.x) {
         int t = (int)fdiv((unsigned)e, ftx), c = e - t * tx;
@@ -333,6 +463,7 @@ struct SplineArgs {
     // brick's particles (log2 of the brick edge and of the bricks per edge)
     int lB, lnb;
     int plane;             // sort by the z plane of the stamp corner instead of by brick
+    int nosort;            // records only (meshes that are not powers of two: no bricks)
     int *count, *rank, *brick;
     int assign;            // gather: the first writer of the force accumulator
     // gather, forked UTotal without a surface term: forceo = (mesh force +
@@ -465,6 +596,7 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
         }
         return;
     }
+    if (a.nosort) return;
     int id = ((((c[2] >> a.lB) << a.lnb) + (c[1] >> a.lB)) << a.lnb) + (c[0] >> a.lB);
     unsigned vm = __ballot_sync(0xffffffffu, valid);
     if (!valid) return;
@@ -784,6 +916,10 @@ template <int ORDER> void spread_lane_attr() {
 // M_y*phi and dM_y*phi over the rows, then weights them by M_z and dM_z; the
 // x weight of the lane's column and the group sum follow.  E = sum
 // dM*M*M*phi (energy.F90:1255-1285); force -= q*E*dkdr*EpsiFourPi.
+template <typename T, bool MIXED>
+__device__ __forceinline__ void gather_store(const SplineArgs &a, int p, T qk, T kx, T ky, T kz, T e0, T e1, T e2,
+                                             double *__restrict__ force, long long *__restrict__ ffx);
+
 template <typename T, bool MIXED, int ORDER>
 __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a, const int *__restrict__ perm,
                                                     const T *__restrict__ w, const T *__restrict__ Q,
@@ -838,7 +974,15 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
         e2 += __shfl_xor_sync(0xffffffffu, e2, o, G);
     }
     if (j != 0 || !valid) return;
-    T qk = -rec[1];   // the charge; kx, ky, kz = dkdr * EpsiFourPi
+    gather_store<T, MIXED>(a, p, -rec[1], kx, ky, kz, e0, e1, e2, force, ffx);
+}
+
+// the mesh force of particle p (qk = -charge; kx, ky, kz = dkdr *
+// EpsiFourPi) into the form's accumulator: added, assigned, or with the
+// short-range accumulator straight into forceo (the epilogue's arithmetic)
+template <typename T, bool MIXED>
+__device__ __forceinline__ void gather_store(const SplineArgs &a, int p, T qk, T kx, T ky, T kz, T e0, T e1, T e2,
+                                             double *__restrict__ force, long long *__restrict__ ffx) {
     if (MIXED) {
         long long f0 = mg_f2fx((float)(qk * kx * e0)), f1 = mg_f2fx((float)(qk * ky * e1)),
                   f2 = mg_f2fx((float)(qk * kz * e2));
@@ -877,6 +1021,74 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     }
 }
 
+// ---- meshes 2^a 3^b 5^c that are not powers of two ------------------------------
+// one thread per particle: its record's stamp into the fixed-point mesh
+// (64-bit integer atomics at the form's scale); indices wrap by remainders
+template <typename T, int ORDER>
+__global__ void __launch_bounds__(128) k_spread_gen(int np, int n, const T *__restrict__ w, double scale,
+                                                    unsigned long long *__restrict__ Qfx) {
+    mg_pdl_begin();
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    typedef RecIx<ORDER> RI;
+    const T *rec = w + (size_t)p * spl_rec(ORDER);
+    int c = rec_corner(rec[0]);
+    int c0 = c & 1023, c1 = (c >> 10) & 1023, c2 = c >> 20;
+    T q = rec[1];
+    for (int iz = 0; iz < ORDER; ++iz) {
+        int nz = c2 - iz < 0 ? c2 - iz + n : c2 - iz;   // ORDER <= n: one wrap at most
+        T wz = q * rec[RI::VZ + iz];
+        for (int iy = 0; iy < ORDER; ++iy) {
+            int ny = c1 - iy < 0 ? c1 - iy + n : c1 - iy;
+            T wyz = wz * rec[RI::VY + iy];
+            size_t row = ((size_t)nz * n + ny) * n;
+            for (int ix = 0; ix < ORDER; ++ix) {
+                int nx = c0 - ix < 0 ? c0 - ix + n : c0 - ix;
+                atomicAdd(&Qfx[row + nx], (unsigned long long)__double2ll_rn((double)(wyz * rec[RI::VX + ix]) * scale));
+            }
+        }
+    }
+}
+
+// one warp per particle, lanes over the (iy, iz) rows of its stamp, the
+// three field sums combined by shuffles; the force as k_gather_grp stores it
+template <typename T, bool MIXED, int ORDER>
+__global__ void __launch_bounds__(128) k_gather_gen(SplineArgs a, const T *__restrict__ w, const T *__restrict__ Q,
+                                                    T kx, T ky, T kz, double *__restrict__ force,
+                                                    long long *__restrict__ ffx) {
+    mg_pdl_begin();
+    int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (p >= a.np) return;
+    typedef RecIx<ORDER> RI;
+    const int n = a.n;
+    const T *rec = w + (size_t)p * spl_rec(ORDER);
+    int c = rec_corner(rec[0]);
+    int c0 = c & 1023, c1 = (c >> 10) & 1023, c2 = c >> 20;
+    T e0 = 0, e1 = 0, e2 = 0;
+    for (int t = lane; t < ORDER * ORDER; t += 32) {
+        int iz = t / ORDER, iy = t - iz * ORDER;
+        int nz = c2 - iz < 0 ? c2 - iz + n : c2 - iz, ny = c1 - iy < 0 ? c1 - iy + n : c1 - iy;
+        T vz = rec[RI::VZ + iz], dz = rec[RI::DZ + iz], vy = rec[RI::VY + iy], dy = rec[RI::DY + iy];
+        const T *row = Q + ((size_t)nz * n + ny) * n;
+        T r0 = 0, r1 = 0;
+        for (int ix = 0; ix < ORDER; ++ix) {
+            int nx = c0 - ix < 0 ? c0 - ix + n : c0 - ix;
+            T qv = row[nx];
+            r0 += rec[RI::DX + ix] * qv;
+            r1 += rec[RI::VX + ix] * qv;
+        }
+        e0 += vy * vz * r0;
+        e1 += dy * vz * r1;
+        e2 += vy * dz * r1;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        e0 += __shfl_xor_sync(0xffffffffu, e0, o);
+        e1 += __shfl_xor_sync(0xffffffffu, e1, o);
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    }
+    if (lane == 0) gather_store<T, MIXED>(a, p, -rec[1], kx, ky, kz, e0, e1, e2, force, ffx);
+}
+
 // ---- conversions between the fixed-point, FP64 and mesh-type meshes (MC) ----
 __global__ void k_fx_to_f64(const long long *__restrict__ fx, double *__restrict__ q, size_t n, double inv) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -901,6 +1113,14 @@ void launch_mesh_kernel(mg_handle *h, int which, const SplineArgs &sa, const Bri
     T *w = (T *)h->d_spl_w;
     if (which == 0) {
         mg_launch_pdl(k_spline_prepare<T, ORDER>, (np + 255) / 256, 256, 0, h->st, sa, w);
+    } else if (which == 1 && h->gen_mesh) {
+        mg_launch_pdl(k_spread_gen<T, ORDER>, (np + 127) / 128, 128, 0, h->st, np, h->nmesh, (const T *)w,
+                      mg_spme_fx_scale(h), (unsigned long long *)h->d_Qfx);
+    } else if (which == 2 && h->gen_mesh) {
+        T kx = (T)(h->dkdr[0] * h->EpsiFourPi), ky = (T)(h->dkdr[1] * h->EpsiFourPi),
+          kz = (T)(h->dkdr[2] * h->EpsiFourPi);
+        mg_launch_pdl(k_gather_gen<T, sizeof(T) == 4, ORDER>, (unsigned)(((long)np * 32 + 127) / 128), 128, 0,
+                      h->st, sa, (const T *)w, (const T *)h->d_Q, kx, ky, kz, h->d_force, h->d_ffx);
     } else if (which == 1 && sizeof(T) == 4) {   // mixed form
         int wpb = h->spread_wpb_lane;
         int grid = (h->max_items + wpb - 1) / wpb;
@@ -1602,8 +1822,10 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_
     if constexpr (std::is_same<T, float>::value) {
         if (h->fft_plane) return plane_dispatch(h, Q, F, tw, cv, fx_inv);
     }
-    int n = h->nmesh, logn = ilog2(n), nh = h->nh;
-    int lp = 4;                                  // line pairs per CTA in the x passes
+    int n = h->nmesh, nh = h->nh;
+    FftPlan pl = make_plan(n);
+    // line pairs per CTA in the x passes: the n^2 lines in groups of 2 lp
+    int lp = n % 4 == 0 ? 4 : 1;
     size_t vsz = sizeof(V2<T>);
     size_t smx = vsz * (n + 2 * (size_t)lp * n);
     int thx = max(32, min(1024, lp * n / 4));
@@ -1615,22 +1837,22 @@ int fft_launch(mg_handle *h, T *Q, V2<T> *F, const V2<T> *tw, ConvArgs cv, T fx_
     size_t zstride = (size_t)n * nh, zother = nh;   // z pass: t -> z, other -> y
     MG_TRY(mg_phase_begin(h, "fft_x_r2c"));
     FastDiv fnh = make_fastdiv((unsigned)nh), ftx = make_fastdiv((unsigned)h->fft_tx);
-    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, fx_inv, F, n, logn, lp, tw, fnh);
+    k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, fx_inv, F, n, pl, lp, tw, fnh);
     // the next spread accumulates into a cleared mesh
     MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n, h->st));
     MG_TRY(mg_phase_end(h, "fft_x_r2c"));
     MG_TRY(mg_phase_begin(h, "fft_y_fwd"));
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, -1, tw, cv, ftx);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, pl, nh, h->fft_tx, ystride, yother, -1, tw, cv, ftx);
     MG_TRY(mg_phase_end(h, "fft_y_fwd"));
     MG_TRY(mg_phase_begin(h, "fft_z_conv"));
-    k_fft_col<T, true><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, zstride, zother, -1, tw, cv, ftx);
+    k_fft_col<T, true><<<gc, thc, smc, h->st>>>(F, n, pl, nh, h->fft_tx, zstride, zother, -1, tw, cv, ftx);
     if (h->par_forces) MG_CUDA(h, cudaEventRecord(h->ev_rec, h->st));   // reciprocal partials complete
     MG_TRY(mg_phase_end(h, "fft_z_conv"));
     MG_TRY(mg_phase_begin(h, "fft_y_inv"));
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, ystride, yother, +1, tw, cv, ftx);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, pl, nh, h->fft_tx, ystride, yother, +1, tw, cv, ftx);
     MG_TRY(mg_phase_end(h, "fft_y_inv"));
     MG_TRY(mg_phase_begin(h, "fft_x_c2r"));
-    k_fft_x_c2r<T><<<gx, thx, smx, h->st>>>(F, Q, n, logn, lp, tw);
+    k_fft_x_c2r<T><<<gx, thx, smx, h->st>>>(F, Q, n, pl, lp, tw);
     MG_TRY(mg_phase_end(h, "fft_x_c2r"));
     h->launches += 5;
     return MG_OK;
@@ -1783,9 +2005,11 @@ template <typename T> void set_smem_limits() {
 
 int mg_spme_init(mg_handle *h) {
     int n = h->nmesh;
-    if (n < 8 || (n & (n - 1)) != 0)
-        return mg_fail(h, MG_ERR_UNSUPPORTED, "nmesh = %d: the device FFT supports powers of two >= 8", n);
-    if (n > 512) return mg_fail(h, MG_ERR_UNSUPPORTED, "nmesh = %d > 512", n);
+    bool pow2 = n >= 8 && (n & (n - 1)) == 0;
+    if (n < 8 || n > 512 || n % 2 != 0 || (!pow2 && make_plan(n).nf == 0))
+        return mg_fail(h, MG_ERR_UNSUPPORTED,
+                       "nmesh = %d: the device FFT supports even meshes 2^a 3^b 5^c from 8 to 512", n);
+    h->gen_mesh = pow2 ? 0 : 1;
     if (h->order > n) return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d > nmesh %d", h->order, n);
     if (h->order < 2 || h->order > MG_MAX_ORDER)
         return mg_fail(h, MG_ERR_UNSUPPORTED, "SPME order %d outside 2..%d", h->order, MG_MAX_ORDER);
@@ -1798,7 +2022,7 @@ int mg_spme_init(mg_handle *h) {
     h->nblk_rec = tiles * n;
     // mixed form, 32 <= n <= 128: plane passes, 32 warps per plane, one
     // partial sum per ky slab
-    h->fft_plane = (h->form == MG_MIXED && n >= 32 && n <= 128) ? 1 : 0;
+    h->fft_plane = (h->form == MG_MIXED && pow2 && n >= 32 && n <= 128) ? 1 : 0;
     if (h->fft_plane) {
         h->fft_warps = 32;
         h->nblk_rec = n;
@@ -2097,6 +2321,7 @@ static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
     sa.lB = ilog2(h->brick);
     sa.lnb = ilog2(h->nbrick_edge);
     sa.plane = 0;
+    sa.nosort = h->gen_mesh;
     sa.count = h->d_brick_count;
     sa.rank = h->d_brick_rank;
     sa.brick = h->d_brick_of;
@@ -2135,11 +2360,13 @@ static int spme_spread(mg_handle *h, const SplineArgs &sa, const BrickArgs &bk) 
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 0, sa, bk)));
     else MG_TRY((mesh_kernel<double, long long>(h, 0, sa, bk)));
     MG_TRY(mg_phase_end(h, "splines"));
-    MG_TRY(mg_phase_begin(h, "brick_sort"));
-    mg_launch_pdl(k_brick_prefix, 1, 1024, 0, h->st, bk);   // the counts come from the spline kernel
-    mg_launch_pdl(k_brick_scatter, gb, tb, 0, h->st, np, bk);
-    h->launches += 2;
-    MG_TRY(mg_phase_end(h, "brick_sort"));
+    if (!h->gen_mesh) {
+        MG_TRY(mg_phase_begin(h, "brick_sort"));
+        mg_launch_pdl(k_brick_prefix, 1, 1024, 0, h->st, bk);   // the counts come from the spline kernel
+        mg_launch_pdl(k_brick_scatter, gb, tb, 0, h->st, np, bk);
+        h->launches += 2;
+        MG_TRY(mg_phase_end(h, "brick_sort"));
+    }
     MG_TRY(mg_phase_begin(h, "spread"));
     if (mixed) MG_TRY((mesh_kernel<float, int>(h, 1, sa, bk)));
     else MG_TRY((mesh_kernel<double, long long>(h, 1, sa, bk)));
@@ -2200,8 +2427,9 @@ __global__ void k_sum6(const double *__restrict__ part, int nblk, double *__rest
 }
 
 template <typename T> static int box_grad_t(mg_handle *h, double *out6, double *scratch, int nblk) {
-    int n = h->nmesh, logn = ilog2(n), nh = h->nh;
-    int lp = 4;
+    int n = h->nmesh, nh = h->nh;
+    FftPlan pl = make_plan(n);
+    int lp = n % 4 == 0 ? 4 : 1;
     size_t vsz = sizeof(V2<T>);
     size_t smx = vsz * (n + 2 * (size_t)lp * n);
     int thx = max(32, min(1024, lp * n / 4));
@@ -2214,10 +2442,10 @@ template <typename T> static int box_grad_t(mg_handle *h, double *out6, double *
     const V2<T> *tw = (const V2<T> *)h->d_tw;
     FastDiv fnh = make_fastdiv((unsigned)nh), ftx = make_fastdiv((unsigned)h->fft_tx);
     k_fft_x_r2c<T><<<gx, thx, smx, h->st>>>((const long long *)h->d_Qfx, (T)(1.0 / mg_spme_fx_scale(h)), F, n,
-                                            logn, lp, tw, fnh);
+                                            pl, lp, tw, fnh);
     MG_CUDA(h, cudaMemsetAsync(h->d_Qfx, 0, sizeof(long long) * (size_t)n * n * n, h->st));
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, nh, (size_t)n * nh, -1, tw, cv, ftx);
-    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, logn, nh, h->fft_tx, (size_t)n * nh, nh, -1, tw, cv, ftx);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, pl, nh, h->fft_tx, nh, (size_t)n * nh, -1, tw, cv, ftx);
+    k_fft_col<T, false><<<gc, thc, smc, h->st>>>(F, n, pl, nh, h->fft_tx, (size_t)n * nh, nh, -1, tw, cv, ftx);
     const T *ew = (const T *)(h->form == MG_MIXED ? (const void *)h->d_ew_f : (const void *)h->d_ew);
     double3 tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
     k_box_grad<T><<<nblk, 256, 0, h->st>>>(F, ew, n, tpbi, 1.0 / (4.0 * h->ualpha * h->ualpha), scratch);

@@ -66,6 +66,12 @@ def small_cases():
         ("spme_order4_n128", lambda: configs.small_system(seed=23, nmesh=128, order=4, n=600, L=50.0)),
         ("spme_order6_n256", lambda: configs.small_system(seed=24, nmesh=256, order=6, n=500, L=45.0)),
         ("spme_bonds_angles", lambda: configs.small_system(seed=25, chains=4, nseg=12, angle_kt=1.0)),
+        # meshes 2^a 3^b 5^c that are not powers of two (generic spread, gather, FFT radices 3 and 5)
+        ("spme_n40", lambda: configs.small_system(seed=26, nmesh=40)),
+        ("spme_n24_order4", lambda: configs.small_system(seed=27, nmesh=24, order=4)),
+        ("spme_n60_order8_surf", lambda: configs.small_system(seed=28, nmesh=60, order=8, lsurf=1)),
+        ("spme_n120_cell", lambda: configs.small_system(seed=29, nmesh=120, n=500, L=45.0,
+                                                        txintlist=abi.MG_CELLLIST)),
     ]
 
 

@@ -10,8 +10,9 @@ forward and the inverse transform, and returns sum ew |r2c(q)|^2.  The same
 quantities from torch.fft.rfftn/irfftn (cuFFT) must agree: FP64 within
 1e-12, the mixed (FP32) form within 1e-5, relative to the largest value.
 
-The device FFT supports the power-of-two meshes that UTotal and the SPME
-autotuner use (8 to 512 points per edge).
+The device FFT supports the even meshes 2^a 3^b 5^c from 8 to 512 points
+per edge (Stockham passes of radices 4, 2, 3 and 5; powers of two also
+through the mixed form's plane passes); other sizes are refused.
 """
 import ctypes as C
 
@@ -47,7 +48,7 @@ def _cufft(q, mult, ew):
     return phi.cpu().numpy(), esum
 
 
-@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
+@pytest.mark.parametrize("n", [16, 24, 32, 40, 48, 60, 64, 96, 120, 128, 150, 256])
 @pytest.mark.parametrize("form,tol", [(abi.MG_FP64, 1e-12), (abi.MG_MIXED, 1e-5)], ids=["fp64", "mixed"])
 def test_fft_matches_cufft(n, form, tol, gpu_lib):
     rng = np.random.default_rng(1000 + n)
@@ -67,6 +68,18 @@ def test_fft_matches_cufft(n, form, tol, gpu_lib):
     assert err <= tol, err
     assert abs(esum[0] - e_ref) <= tol * abs(e_ref), (esum[0], e_ref)
     g.close()
+
+
+def test_unsupported_meshes_are_refused(gpu_lib):
+    """Odd meshes and meshes with a prime factor above 5 are refused at
+    creation with MG_ERR_UNSUPPORTED."""
+    from molsim_gb300.engine import MolsimError
+    for n in (42, 45, 14):
+        s = configs.small_system(seed=61, n=120, L=40.0, nmesh=n, order=4)
+        s.build_table()
+        with pytest.raises(MolsimError) as ex:
+            Engine(s)
+        assert abi.STATUS[ex.value.status] == "MG_ERR_UNSUPPORTED"
 
 
 def test_fft_check_then_utotal_unchanged(gpu_lib):

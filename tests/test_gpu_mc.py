@@ -29,6 +29,8 @@ CASES = [
     ("no_ewald_cell", dict(seed=66, ewald=abi.MG_EWALD_NONE, txintlist=abi.MG_CELLLIST)),
     ("spme_bonds_vlist", dict(seed=67, chains=3, nseg=8)),
     ("spme_angles_cell", dict(seed=68, chains=4, nseg=8, angle_kt=0.6, txintlist=abi.MG_CELLLIST)),
+    ("spme_n40_cell", dict(seed=69, nmesh=40, txintlist=abi.MG_CELLLIST)),
+    ("spme_n30_order5", dict(seed=70, nmesh=30, order=5)),
 ]
 
 

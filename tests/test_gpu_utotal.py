@@ -30,6 +30,20 @@ def test_utotal_mixed(name, factory, orc, gpu_lib):
     assert e["force_rms"] <= TOL_MIXED_RMS and e["u_tot"] <= 1e-5 and e["virial"] <= 1e-5, e
 
 
+@pytest.mark.parametrize("nmesh,order", [(40, 6), (96, 6), (60, 8)])
+def test_utotal_mixed_generic_meshes(nmesh, order, orc, gpu_lib):
+    """The mixed form on meshes 2^a 3^b 5^c that are not powers of two
+    (line passes with radices 3 and 5, generic spread and gather): force RMS
+    error against the FP64 oracle within the mixed form's bar, and the same
+    bits on a second call."""
+    s = prepared(configs.small_system(seed=34, nmesh=nmesh, order=order, n=600, L=50.0), orc)
+    r, g, _, gpu = run_pair(s, orc, form=abi.MG_MIXED)
+    e = utotal_errors(g, r, s.nptpt)
+    assert e["force_rms"] <= TOL_MIXED_RMS and e["u_tot"] <= 1e-5 and e["virial"] <= 1e-5, e
+    g2 = gpu.UTotal()
+    assert np.array_equal(g["forceo"], g2["forceo"]) and g["u_tot"] == g2["u_tot"]
+
+
 def test_mixed_is_bit_reproducible(orc, gpu_lib):
     s = prepared(configs.small_system(seed=31), orc)
     _, g1, _, gpu = run_pair(s, orc, form=abi.MG_MIXED)
