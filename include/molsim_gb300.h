@@ -276,6 +276,17 @@ int mg_dutotal_batch(mg_handle *h, int32_t ntrial, const int32_t *ip,
 int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps,
             double *du_dsig, double *du_dbox);
 
+/* The force Jacobian along u: jv[3*np] = d(forceo)/dx . u[3*np] (forceo
+ * units per A, i.e. minus force_fac times the Hessian of u%tot applied to
+ * u) at the handle's positions, from hand-written derivative kernels: the
+ * tabulated pair force (its quartic's derivative in r^2), the bonds, and
+ * the reciprocal and surface Ewald parts as the field of the dipoles q_j
+ * u_j plus the field gradient of the charges along u_i (the dipole kernels
+ * of mg_dipole_ewald).  No reference counterpart (the adjoint of MD
+ * trajectories needs it).  FP64 handles with a Verlet list in MD or BD
+ * mode, without angle terms; runs a UTotal first and leaves the reciprocal
+ * scratch (structure factors, meshes) changed. */
+int mg_force_jvp(mg_handle *h, const double *u, double *jv);
 /* UTotal at the current positions and its derivative by an affine strain of
  * the box and the positions, r -> (1 + eps) r: w[9] (row-major, symmetric)
  * = dU/deps_ab, the virial tensor (pairs and bonds r_a f_b, angles through

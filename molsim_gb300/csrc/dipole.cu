@@ -25,7 +25,108 @@ __global__ void k_dip_self_atomic(int np, const double *__restrict__ az, const d
     for (int m = 0; m < 3; ++m) efg[6 * ia + m] = efg[6 * ia + m] - s2 * q;
 }
 
+// p = q u (the dipoles of the charges displaced along u)
+__global__ void k_jvp_dipoles(int np, const double *__restrict__ az, const double *__restrict__ u,
+                              double *__restrict__ p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * np) return;
+    p[i] = az[i / 3] * u[i];
+}
+
+// jv_i += EpsiFourPi q_i (e_p(r_i) + efg_q(r_i) . u_i): the field of the
+// displaced charges' dipoles and the field gradient of the charges moved
+// along u_i; with the surface term -2 (2 pi / 3V) EpsiFourPi q_i sum_j q_j u_j
+__global__ void k_jvp_rec_combine(int np, const double *__restrict__ az, const double *__restrict__ u,
+                                  const double *__restrict__ est, const double *__restrict__ efg,
+                                  const double *__restrict__ s3, double surf, double efp, double *__restrict__ jv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const double *g = efg + 6 * i, *ui = u + 3 * i;
+    double gu[3] = {g[0] * ui[0] + g[3] * ui[1] + g[4] * ui[2], g[3] * ui[0] + g[1] * ui[1] + g[5] * ui[2],
+                    g[4] * ui[0] + g[5] * ui[1] + g[2] * ui[2]};
+    double q = az[i];
+    for (int m = 0; m < 3; ++m) {
+        double v = est[3 * i + m] + gu[m];
+        if (s3) v -= surf * s3[m];
+        jv[3 * i + m] += efp * q * v;
+    }
+}
+
+// sum_j q_j u_j, one block of 1024 threads, a fixed order
+__global__ void __launch_bounds__(1024) k_jvp_qu_sum(int np, const double *__restrict__ az,
+                                                     const double *__restrict__ u, double *__restrict__ s3) {
+    __shared__ double red[3][32];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+        for (int m = 0; m < 3; ++m) s[m] += az[i] * u[3 * i + m];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int m = 0; m < 3; ++m) {
+        for (int o = 16; o > 0; o >>= 1) s[m] += __shfl_down_sync(0xffffffffu, s[m], o);
+        if (lane == 0) red[m][w] = s[m];
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[threadIdx.x][k];
+        s3[threadIdx.x] = t;
+    }
+}
+
 }  // namespace
+
+// the reciprocal and surface parts of d(force)/dx . u (force units before
+// force_fac, added to jv; device arrays; u scaled to a largest component
+// of 1): moving charge j by u_j adds the
+// dipole q_j u_j, and charge i sees the field gradient of the others along
+// u_i, so d(force_i) = EpsiFourPi q_i (e_p(r_i) + efg_q(r_i) . u_i).  Both
+// come from the dipole kernels (charges off with dipoles p, then dipoles off
+// with the charges) with their atomic self terms, which remove each
+// particle's own contribution.
+int mg_force_jvp_rec(mg_handle *h, const double *u, double *jv) {
+    const int np = h->np;
+    const size_t nvir = std::max((size_t)h->nkvec, (size_t)np + 2 * (size_t)std::max(h->nblk_rec, 1));
+    const size_t need = 26 * (size_t)np + nvir + 3;   // p, zero, (pot, est, efg) twice, vir, sums
+    if (h->dip_scr_n < need) {
+        if (h->d_dip_scr) cudaFree(h->d_dip_scr);
+        h->d_dip_scr = nullptr;
+        h->dip_scr_n = 0;
+        MG_CUDA(h, cudaMalloc(&h->d_dip_scr, sizeof(double) * need));
+        h->dip_scr_n = need;
+    }
+    double *p = h->d_dip_scr, *zero = p + 3 * (size_t)np, *pot = zero + 3 * (size_t)np, *est = pot + np,
+           *efg = est + 3 * (size_t)np, *pot2 = efg + 6 * (size_t)np, *est2 = pot2 + np,
+           *efg2 = est2 + 3 * (size_t)np, *vir = efg2 + 6 * (size_t)np, *s3 = vir + nvir;
+    MG_CUDA(h, cudaMemsetAsync(zero, 0, sizeof(double) * 23 * (size_t)np, h->st));   // zero .. efg2
+    k_jvp_dipoles<<<(3 * np + 255) / 256, 256, 0, h->st>>>(np, h->d_az, u, p);
+    const double ualpha = h->ualpha;
+    const double s2 = (4.0 * ualpha * ualpha * ualpha) / (3.0 * std::sqrt(3.14159265358979323846));
+    // the dipoles' field (charges off) and the charges' field gradient (dipoles off)
+    if (h->ewald == MG_EWALD_STD) {
+        MG_TRY(mg_ewald_std_dipole(h, zero, p, pot, est, efg, vir));
+        MG_TRY(mg_ewald_std_dipole(h, h->d_az, zero, pot2, est2, efg2, vir));
+    } else {
+        // u is scaled to a largest component of 1 by the caller
+        double kmax = std::max(h->dkdr[0], std::max(h->dkdr[1], h->dkdr[2]));
+        double b1 = (double)np * (3.0 * kmax * h->az_absmax) * 1.01 + 1.0;
+        double b2 = (double)np * h->az_absmax * 1.01 + 1.0;
+        MG_TRY(mg_spme_dipole(h, zero, p, b1, pot, est, efg, vir));
+        MG_TRY(mg_spme_dipole(h, h->d_az, zero, b2, pot2, est2, efg2, vir));
+    }
+    k_dip_self_atomic<<<(np + 127) / 128, 128, 0, h->st>>>(np, zero, p, 0.0, s2, pot, est, efg);
+    k_dip_self_atomic<<<(np + 127) / 128, 128, 0, h->st>>>(np, h->d_az, zero, 0.0, s2, pot2, est2, efg2);
+    const double *sums = nullptr;
+    double surf = 0.0;
+    if (h->lsurf) {
+        k_jvp_qu_sum<<<1, 1024, 0, h->st>>>(np, h->d_az, u, s3);
+        sums = s3;
+        surf = 2.0 * (2.0 * 3.14159265358979323846 / (3.0 * h->vol));
+    }
+    k_jvp_rec_combine<<<(np + 127) / 128, 128, 0, h->st>>>(np, h->d_az, u, est, efg2, sums, surf, h->EpsiFourPi,
+                                                           jv);
+    h->launches += 5 + (h->lsurf ? 1 : 0);
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
 
 extern "C" int mg_dipole_ewald(mg_handle *h, const double *dip, double *potstat, double *estat, double *efg,
                                double *virelec) {
@@ -33,6 +134,8 @@ extern "C" int mg_dipole_ewald(mg_handle *h, const double *dip, double *potstat,
     if (h->ewald != MG_EWALD_STD && h->ewald != MG_EWALD_SPM)
         return mg_fail(h, MG_ERR_STATE, "mg_dipole_ewald needs a handle with Ewald summation");
     if (h->form != MG_FP64) return mg_fail(h, MG_ERR_UNSUPPORTED, "dipole electrostatics need the FP64 form");
+    if (h->mode == MG_MC)   // the structure factors and meshes of the accepted MC state stay untouched
+        return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_dipole_ewald needs an MD or BD handle");
     const int np = h->np;
     const size_t nvir = std::max((size_t)h->nkvec, (size_t)np + 2 * (size_t)std::max(h->nblk_rec, 1));
     const size_t need = 13 * (size_t)np + nvir;
@@ -51,13 +154,13 @@ extern "C" int mg_dipole_ewald(mg_handle *h, const double *dip, double *potstat,
     MG_CUDA(h, cudaMemcpyAsync(d_efg, efg, sizeof(double) * 6 * np, cudaMemcpyHostToDevice, h->st));
     std::vector<double> vir;
     if (h->ewald == MG_EWALD_STD) {
-        MG_TRY(mg_ewald_std_dipole(h, d_dip, d_pot, d_est, d_efg, d_vir));
+        MG_TRY(mg_ewald_std_dipole(h, h->d_az, d_dip, d_pot, d_est, d_efg, d_vir));
         vir.resize(h->nkvec);
     } else {
         double dmax = 0.0, kmax = std::max(h->dkdr[0], std::max(h->dkdr[1], h->dkdr[2]));
         for (int i = 0; i < 3 * np; ++i) dmax = std::max(dmax, std::fabs(dip[i]));
         double bound = (double)np * (h->az_absmax + 3.0 * kmax * dmax) * 1.01 + 1.0;
-        MG_TRY(mg_spme_dipole(h, d_dip, bound, d_pot, d_est, d_efg, d_vir));
+        MG_TRY(mg_spme_dipole(h, h->d_az, d_dip, bound, d_pot, d_est, d_efg, d_vir));
         vir.resize((size_t)np + 2 * (size_t)h->nblk_rec);
     }
     const double ualpha = h->ualpha;

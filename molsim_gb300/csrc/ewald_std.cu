@@ -267,14 +267,15 @@ __global__ void __launch_bounds__(128) k_dip_fk(const double2 *__restrict__ eik,
 
 }  // namespace
 
-// the reciprocal part of UDipoleEwald, standard Ewald: device arrays dip,
-// pot, est, efg of the handle's particles (added to), vir[nkvec] per
-// k-vector virial terms
-int mg_ewald_std_dipole(mg_handle *h, const double *dip, double *pot, double *est, double *efg, double *vir) {
+// the reciprocal part of UDipoleEwald, standard Ewald: device arrays az
+// (charges), dip, pot, est, efg of the handle's particles (pot, est, efg
+// added to), vir[nkvec] per k-vector virial terms
+int mg_ewald_std_dipole(mg_handle *h, const double *az, const double *dip, double *pot, double *est, double *efg,
+                        double *vir) {
     int np = h->np;
     double3 tpbi = make_double3(h->TwoPiBoxi[0], h->TwoPiBoxi[1], h->TwoPiBoxi[2]);
     k_eik<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_ro, np, h->ncut, tpbi, h->d_eik);
-    k_dip_sk<<<h->nkvec, 256, 0, h->st>>>(h->d_eik, h->d_az, dip, np, h->ncut, h->d_kvec, h->d_kfac, tpbi,
+    k_dip_sk<<<h->nkvec, 256, 0, h->st>>>(h->d_eik, az, dip, np, h->ncut, h->d_kvec, h->d_kfac, tpbi,
                                           h->ualpha * h->ualpha, h->d_S, vir);
     k_dip_fk<<<(np + 127) / 128, 128, 0, h->st>>>(h->d_eik, np, h->ncut, h->d_kvec, h->d_kfac, h->d_S, h->nkvec,
                                                   tpbi, pot, est, efg);

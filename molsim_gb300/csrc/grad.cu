@@ -23,6 +23,7 @@
 //                virial; dU/dL_a = dU/deps_aa / L_a.
 // All arithmetic is FP64 in both forms (the mixed form reads its FP32
 // potential mesh).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -480,6 +481,180 @@ int grad_run(mg_handle *h, const mg_pot_params *pp, double *phi, std::vector<dou
 }
 
 }  // namespace
+
+// ---- force Jacobian-vector products (Hessian-vector products of U) -------------
+namespace {
+
+struct JvpArgs {
+    const double4 *pos_s;
+    const int *perm, *nnb, *nbr;
+    int np, npt, nbins;
+    const int *pairidx, *tab_start, *tab_n;
+    const double *zlow, *coef, *bin_z0, *bin_inv, *r2umin;
+    const unsigned short *bin_kstart;
+    mg_box box;
+    double rcut2;
+    const double *u;
+    double *jv;
+};
+
+// d(force_i)/dx . u over the full Verlet list (one thread per slot): for
+// the tabulated pair force fsum(r^2) d, the change along w = u_i - u_j is
+// fsum w + 2 fsum'(r^2) (d . w) d, fsum' the derivative of the table's
+// quartic in r^2 - zlow
+__global__ void __launch_bounds__(128) k_jvp_pairs(JvpArgs a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.np) return;
+    double4 pi = a.pos_s[i];
+    int ti = (int)pi.w, p = a.perm[i];
+    double ui[3] = {a.u[3 * p], a.u[3 * p + 1], a.u[3 * p + 2]};
+    double g[3] = {0.0, 0.0, 0.0};
+    int nn = a.nnb[i];
+    for (int k = 0; k < nn; ++k) {
+        int j = a.nbr[(size_t)k * a.np + i];
+        double4 pj = a.pos_s[j];
+        double d[3] = {mg_pbc1(pi.x - pj.x, a.box.half[0], a.box.len[0]),
+                       mg_pbc1(pi.y - pj.y, a.box.half[1], a.box.len[1]),
+                       mg_pbc1(pi.z - pj.z, a.box.half[2], a.box.len[2])};
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2 > a.rcut2) continue;
+        int tj = (int)pj.w;
+        int pair = a.pairidx[tj * a.npt + ti] - 1;
+        if (r2 < a.r2umin[pair]) continue;   // below the table: UTotal reports it
+        int b = (int)((r2 - a.bin_z0[pair]) * a.bin_inv[pair]);
+        b = min(max(b, 0), a.nbins - 1);
+        int kk = a.bin_kstart[pair * a.nbins + b], last = a.tab_n[pair] - 1;
+        const double *z = a.zlow + a.tab_start[pair];
+        while (kk < last && z[kk] > r2) ++kk;
+        int rec = a.tab_start[pair] + kk;
+        const double *c = a.coef + (size_t)rec * 11;
+        double dd = r2 - a.zlow[rec];
+        double fs = c[6] + dd * (c[7] + dd * (c[8] + dd * (c[9] + dd * c[10])));
+        double dfs = c[7] + dd * (2.0 * c[8] + dd * (3.0 * c[9] + dd * 4.0 * c[10]));
+        int q = a.perm[j];
+        double w[3] = {ui[0] - a.u[3 * q], ui[1] - a.u[3 * q + 1], ui[2] - a.u[3 * q + 2]};
+        double dw = 2.0 * dfs * (d[0] * w[0] + d[1] * w[1] + d[2] * w[2]);
+        for (int m = 0; m < 3; ++m) g[m] += fs * w[m] + dw * d[m];
+    }
+    for (int m = 0; m < 3; ++m) a.jv[3 * p + m] += g[m];
+}
+
+// bonds u = k (r - r0)^p: d(force_ip)/dx . u = -k p [(p-1)(r-r0)^(p-2)
+// (dh . w) dh + (r-r0)^(p-1) (w - dh (dh . w)) / r], dh = d/r, w = u_ip - u_jp;
+// force_jp the opposite (FP64 atomics)
+__global__ void k_jvp_bonds(int nbond, const int *__restrict__ ij, const double *__restrict__ bk,
+                            const double *__restrict__ beq, const int *__restrict__ bp, const double *__restrict__ ro,
+                            mg_box box, const double *__restrict__ u, double *__restrict__ jv) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbond) return;
+    int ip = ij[2 * b], jp = ij[2 * b + 1];
+    double d[3], w[3];
+    for (int m = 0; m < 3; ++m) {
+        d[m] = mg_pbc1(ro[3 * ip + m] - ro[3 * jp + m], box.half[m], box.len[m]);
+        w[m] = u[3 * ip + m] - u[3 * jp + m];
+    }
+    double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    double dh[3] = {d[0] / r, d[1] / r, d[2] / r};
+    double t = r - beq[b];
+    int pw = bp[b];
+    double t1 = 1.0, t2 = 1.0;   // t^(p-1), t^(p-2)
+    for (int k = 0; k < pw - 1; ++k) t1 *= t;
+    for (int k = 0; k < pw - 2; ++k) t2 *= t;
+    double a1 = pw >= 2 ? (pw - 1) * t2 : 0.0;
+    double hw = dh[0] * w[0] + dh[1] * w[1] + dh[2] * w[2];
+    for (int m = 0; m < 3; ++m) {
+        double g = -bk[b] * pw * (a1 * hw * dh[m] + t1 * (w[m] - dh[m] * hw) / r);
+        atomicAdd(&jv[3 * ip + m], g);
+        atomicAdd(&jv[3 * jp + m], -g);
+    }
+}
+
+__global__ void k_scale(double *__restrict__ x, size_t n, double f) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= f;
+}
+
+}  // namespace
+
+// d(forceo)/dx . u at the handle's positions (FP64 form, Verlet list, MD
+// or BD, bonds without angles): a UTotal first (the slot positions and the
+// list the pair part reads), then the tabulated pairs (LJ and the
+// real-space Ewald part), the bonds, and the reciprocal and surface parts
+// through the dipole kernels
+extern "C" int mg_force_jvp(mg_handle *h, const double *u, double *jv) {
+    if (!h || !u || !jv) return MG_ERR_ARG;
+    if (h->form != MG_FP64) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp needs the FP64 form");
+    if (h->txintlist != MG_VLIST) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp needs the Verlet list");
+    if (h->nangle > 0) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp: angle terms are not differentiated");
+    if (h->mode == MG_MC) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp needs an MD or BD handle");
+    if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_force_jvp needs a neighbour list (NList)");
+    MG_TRY(mg_utotal_launch(h));
+    const int np = h->np;
+    // the product is linear in u: computed for u / max|u| (a fixed-point
+    // scale for the reciprocal mesh independent of the size of u), then scaled
+    double umax = 0.0;
+    for (int i = 0; i < 3 * np; ++i) umax = std::max(umax, std::fabs(u[i]));
+    if (umax == 0.0) {
+        for (int i = 0; i < 3 * np; ++i) jv[i] = 0.0;
+        return MG_OK;
+    }
+    std::vector<double> us(u, u + 3 * (size_t)np);
+    for (double &x : us) x /= umax;
+    double *d_u = nullptr, *d_jv = nullptr;
+    MG_CUDA(h, cudaMalloc(&d_u, sizeof(double) * 6 * (size_t)np));
+    d_jv = d_u + 3 * (size_t)np;
+    int st = MG_OK;
+    do {
+        if (cudaMemcpyAsync(d_u, us.data(), sizeof(double) * 3 * np, cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+            cudaMemsetAsync(d_jv, 0, sizeof(double) * 3 * np, h->st) != cudaSuccess) {
+            st = mg_fail(h, MG_ERR_CUDA, "mg_force_jvp: copy failed");
+            break;
+        }
+        JvpArgs a;
+        a.pos_s = h->d_pos_s;
+        a.perm = h->d_perm;
+        a.nnb = h->d_nnb;
+        a.nbr = h->d_nbr;
+        a.np = np;
+        a.npt = h->npt;
+        a.nbins = h->nbins;
+        a.pairidx = h->d_pairidx;
+        a.tab_start = h->d_tab_start;
+        a.tab_n = h->d_tab_n;
+        a.zlow = h->d_zlow;
+        a.coef = h->d_coef;
+        a.bin_z0 = h->d_bin_z0;
+        a.bin_inv = h->d_bin_inv;
+        a.r2umin = h->d_r2umin;
+        a.bin_kstart = h->d_bin_kstart;
+        for (int m = 0; m < 3; ++m) {
+            a.box.len[m] = h->boxlen[m];
+            a.box.half[m] = h->boxlen2[m];
+            a.box.inv[m] = h->boxleni[m];
+        }
+        a.rcut2 = h->rcut2;
+        a.u = d_u;
+        a.jv = d_jv;
+        k_jvp_pairs<<<(np + 127) / 128, 128, 0, h->st>>>(a);
+        h->launches++;
+        if (h->nbond > 0) {
+            k_jvp_bonds<<<(h->nbond + 127) / 128, 128, 0, h->st>>>(h->nbond, h->d_bond_ij, h->d_bond_k,
+                                                                  h->d_bond_eq, h->d_bond_p, h->d_ro, a.box, d_u,
+                                                                  d_jv);
+            h->launches++;
+        }
+        if (h->ewald != MG_EWALD_NONE && (st = mg_force_jvp_rec(h, d_u, d_jv)) != MG_OK) break;
+        size_t n3 = 3 * (size_t)np;
+        k_scale<<<(unsigned)((n3 + 255) / 256), 256, 0, h->st>>>(d_jv, n3, h->force_fac * umax);
+        h->launches++;
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(jv, d_jv, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->st) != cudaSuccess ||
+            cudaStreamSynchronize(h->st) != cudaSuccess)
+            st = mg_fail(h, MG_ERR_CUDA, "mg_force_jvp: kernels or copy failed");
+    } while (false);
+    cudaFree(d_u);
+    return st;
+}
 
 extern "C" int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps, double *du_dsig,
                        double *du_dbox) {

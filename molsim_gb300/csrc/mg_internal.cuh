@@ -406,9 +406,11 @@ int mg_ewald_std_launch(mg_handle *h);
 
 double mg_spme_fx_scale(const mg_handle *h);
 int mg_spme_potential(mg_handle *h);
-int mg_spme_dipole(mg_handle *h, const double *dip, double bound, double *pot, double *est, double *efg,
-                   double *vir);
-int mg_ewald_std_dipole(mg_handle *h, const double *dip, double *pot, double *est, double *efg, double *vir);
+int mg_spme_dipole(mg_handle *h, const double *az, const double *dip, double bound, double *pot, double *est,
+                   double *efg, double *vir);
+int mg_ewald_std_dipole(mg_handle *h, const double *az, const double *dip, double *pot, double *est, double *efg,
+                        double *vir);
+int mg_force_jvp_rec(mg_handle *h, const double *u, double *jv);
 int mg_spme_load_mesh(mg_handle *h, const double *q);
 int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul);
 int mg_spme_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew, double *phi,

@@ -2186,21 +2186,22 @@ int mg_spme_potential(mg_handle *h) {
                               1.0 / mg_spme_fx_scale(h));
 }
 
-// the reciprocal part of UDipoleEwald, SPME (FP64 form): device arrays dip,
-// pot, est, efg of the handle's particles (added to); vir[np] the per-particle
+// the reciprocal part of UDipoleEwald, SPME (FP64 form): device arrays az
+// (charges), dip, pot, est, efg of the handle's particles (the last three
+// added to); vir[np] the per-particle
 // dipole terms of the virial, then the FFT blocks' (energy, virial) partial
 // pairs, vir[np + 2 b + 1] summing to SPMFFTRec's virloc (nblk_rec blocks).  The fixed-point scale is
 // chosen for the generalized charges: no mesh point can exceed np (max|q| +
 // 3 max|dkdr . dip|) with B-spline values and derivatives at most 1.
-int mg_spme_dipole(mg_handle *h, const double *dip, double bound, double *pot, double *est, double *efg,
-                   double *vir) {
+int mg_spme_dipole(mg_handle *h, const double *az, const double *dip, double bound, double *pot, double *est,
+                   double *efg, double *vir) {
     if (h->form != MG_FP64) return mg_fail(h, MG_ERR_UNSUPPORTED, "dipole electrostatics need the FP64 form");
     int k = 52;
     while (k > 8 && std::ldexp(bound, k) >= 9.2e18 * 0.5) --k;
     double scale = std::ldexp(1.0, k);
     DipMeshArgs a;
     a.ro = h->d_ro;
-    a.az = h->d_az;
+    a.az = az;
     a.dip = dip;
     a.np = h->np;
     a.order = h->order;

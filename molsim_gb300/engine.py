@@ -164,6 +164,15 @@ class Engine:
                     "grad")
         return dict(phi=phi, du_deps=de, du_dsig=ds, du_dbox=db)
 
+    def ForceJVP(self, u):
+        """d(forceo)/dx . u at the current positions (forceo units per A; the
+        Hessian of UTotal times u, negated and scaled by force_fac), by
+        hand-written derivative kernels (mg_force_jvp)."""
+        u = abi.as_f64(np.asarray(u, dtype=np.float64).reshape(-1))
+        jv = np.zeros(3 * self.np)
+        self._check(self.lib.mg_force_jvp(self.h, abi.f64(u), abi.f64(jv)), "force_jvp")
+        return jv.reshape(self.np, 3)
+
     def VirialTensor(self):
         """dU/deps_ab (3x3) for an affine strain of the box and positions;
         its trace is UTotal's virial."""

@@ -10,7 +10,10 @@ the first.  It needs the forces at every step and Hessian-vector products:
 - The states (x, v, a) are stored every `checkpoint` steps on the forward
   pass. The backward pass recomputes one segment at a time from its
   checkpoint, so memory holds one segment, not the whole trajectory.
-- The Hessian-vector products are central differences of the device forces,
+- The Hessian-vector products come from the device's derivative kernels
+  (mg_force_jvp: the tabulated pair force's derivative, the bonds, the
+  reciprocal part through the dipole kernels), hvp="analytic"; or, with
+  hvp="fd", from central differences of the device forces,
   (forceo(x + eps u) - forceo(x - eps u)) / 2 eps, with eps scaled so that
   the largest displacement is 1e-5 A.
 
@@ -26,11 +29,13 @@ from .engine import Engine
 class Trajectory:
     """Velocity Verlet of a System through the GPU forces (FP64 form)."""
 
-    def __init__(self, system, dt=0.002, nsteps=50, checkpoint=10, hvp_disp=1e-5):
+    def __init__(self, system, dt=0.002, nsteps=50, checkpoint=10, hvp_disp=1e-5, hvp="analytic"):
         if system.ubuf is None:
             system.build_table()
+        if hvp not in ("analytic", "fd"):
+            raise ValueError(f"hvp = {hvp!r}: 'analytic' or 'fd'")
         self.s = system
-        self.dt, self.n, self.ck, self.hvp_disp = dt, nsteps, checkpoint, hvp_disp
+        self.dt, self.n, self.ck, self.hvp_disp, self.hvp = dt, nsteps, checkpoint, hvp_disp, hvp
         self.e = Engine(system, form=abi.MG_FP64)
         self.im = np.repeat(system.massip(), 3)          # inverse masses per coordinate
         self.L = system.boxlen
@@ -73,6 +78,10 @@ class Trajectory:
         nrm = np.abs(u).max()
         if nrm == 0.0:
             return np.zeros_like(lam)
+        if self.hvp == "analytic":
+            self.e.SetPositions(self._wrap(x))
+            self.e.NList("write")
+            return self.e.ForceJVP(u).reshape(-1)
         eps = self.hvp_disp / nrm
         fp, _ = self.forces(x + eps * u)
         fm, _ = self.forces(x - eps * u)

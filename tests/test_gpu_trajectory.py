@@ -6,6 +6,8 @@ compared with central finite differences of the whole trajectory, with
 steps of 1e-4 A for positions and 1e-4 of the RMS speed for velocities, to
 1e-6 of the gradient's largest component.  The table is built to 1e-9 so
 that the tabulated forces are the derivatives of the tabulated energy.
+The Hessian-vector products come from the derivative kernels
+(mg_force_jvp) or from differences of the forces.
 """
 import numpy as np
 import pytest
@@ -24,9 +26,12 @@ def _setup():
     return s, s.ro_flat().copy(), v0
 
 
-def test_trajectory_gradient_matches_finite_differences(gpu_lib):
+@pytest.mark.parametrize("hvp", ["analytic", "fd"])
+def test_trajectory_gradient_matches_finite_differences(hvp, gpu_lib):
+    """The backward pass with the Hessian-vector products of the derivative
+    kernels (mg_force_jvp) or of central differences of the forces."""
     s, x0, v0 = _setup()
-    tr = Trajectory(s, dt=0.002, nsteps=50, checkpoint=10)
+    tr = Trajectory(s, dt=0.002, nsteps=50, checkpoint=10, hvp=hvp)
     L, cks = tr.forward(x0, v0)
     gx, gv = tr.backward(cks)
     rng = np.random.default_rng(5)
