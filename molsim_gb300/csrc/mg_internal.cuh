@@ -158,12 +158,12 @@ struct mg_handle {
     // plane pass (particles sorted by the z plane of their stamp corner), so
     // the charge mesh never leaves shared memory
     int plane_fused = 0;
-    int plane_shift = 30;           // fused spread: stamp values to integers (2^plane_shift)
     float *d_spl_plane = nullptr;   // fused spread: the spread records in plane order
     // dipole electrostatics (mg_dipole_ewald): dip, pot, est, efg, virial terms
     double *d_dip_scr = nullptr;
     size_t dip_scr_n = 0;
     double az_absmax = 0.0;          // max |q| of the particles
+    double spl_mmax = 1.0;           // largest cardinal B-spline value at the SPME order
     int brick = 0, nbrick_edge = 0, nbricks = 0;
     size_t spread_smem = 0, gather_smem = 0;
     int fx_shift = 30, fx_shift64 = 48;

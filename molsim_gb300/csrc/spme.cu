@@ -1571,8 +1571,7 @@ __global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F,
 struct PlaneArgs {
     const int *start;
     const float *srec;         // spread records in plane order (spread_rec values each)
-    float scale;               // stamp values to integers: 2^plane_shift
-    float inv_hi, inv_lo;      // 2^(15 - plane_shift), 2^-plane_shift
+    float mmax2;               // (largest B-spline value)^2
     int *err;
 };
 
@@ -1601,15 +1600,16 @@ template <int ORDER> __device__ __forceinline__ int window_iz(const int *ws, int
 
 // Spread of the plane's window into the plane, then x r2c + forward y FFT
 // as k_plane_fwd.  One lane per item; rows are padded to n + 1 points so
-// that the lanes' stamp rows spread over the banks.  Stamp values
-// v = round(q Mx My Mz 2^s), |v| < 2^30, are added as two 32-bit integer
-// parts, hi = v >> 15 (signed) and lo = v & (2^15 - 1) (unsigned), each with
-// a shared-memory atomic: both sums stay exact for up to 2^16 items per
-// point, and a window of more items is reported (MG_ERR_UNSUPPORTED).
-// Integer sums do not depend on the order of the adds, so the plane is
-// bit-reproducible.  The two integer planes share memory with the FFT's
-// plane and line buffers, which are used only after every line has been
-// read into registers.
+// that the lanes' stamp rows spread over the banks.  Stamp values are added
+// as 32-bit integers v = round(q Mx My Mz 2^s) with one shared-memory
+// atomic each.  The plane's scale 2^s comes from a bound of its largest
+// point sum: an item adds at most |q| Mz(plane) mmax^2 to any point of the
+// ORDER rows its stamp covers, so the largest of the rows' sums of those
+// terms (fixed point, rounded up, integer atomics) bounds every point, and
+// B 2^s < 2^30 keeps the integer sums clear of overflow.  Integer sums do
+// not depend on the order of the adds, so the plane is bit-reproducible.  The integer plane shares memory with the FFT's plane
+// and line buffers, which are used only after every line has been read
+// into registers.
 template <int P, int ORDER>
 __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *__restrict__ F,
                                                            const float2 *__restrict__ tw, FastDiv fnh) {
@@ -1622,42 +1622,57 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
     __shared__ int wb[ORDER], ws[ORDER + 1];
     V *s_tw = reinterpret_cast<V *>(smem_raw), *s_tl = s_tw + n, *s_tk = s_tl + 32;
     V *S = s_tw + plane_tw_entries<P>();
-    int *thi = reinterpret_cast<int *>(S);
-    unsigned *tlo = reinterpret_cast<unsigned *>(thi + n2);
+    int *tacc = reinterpret_cast<int *>(S);
+    __shared__ int rowb[n], bmax[32];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     V *Zs = S + n * nh + w * (n + n / 16);
     load_tw<T>(s_tw, tw, n);
     load_lane_tw<T, P>(s_tl, s_tk, tw);
-    for (int k = threadIdx.x; k < n2; k += blockDim.x) {
-        thi[k] = 0;
-        tlo[k] = 0u;
-    }
+    for (int k = threadIdx.x; k < n2; k += blockDim.x) tacc[k] = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) rowb[k] = 0;
     const int z = blockIdx.x;
     plane_window<ORDER>(a, z, n, wb, ws);
     __syncthreads();
     const int total = ws[ORDER];
-    if (total >= 65536) {   // the integer parts could overflow: report, spread nothing
-        if (threadIdx.x == 0) mg_dev_error(a.err, MG_ERR_UNSUPPORTED, z, total, 65535);
-    } else {
-        for (int t = threadIdx.x; t < total; t += blockDim.x) {
-            int iz = window_iz<ORDER>(ws, t);
-            const float *rec = a.srec + (size_t)(wb[iz] + t - ws[iz]) * SR;
-            float r[kRecHead + 2 * ORDER];
-            load_rec<float, kRecHead + 2 * ORDER>(rec, r);
-            float qz = r[1] * rec[kRecHead + 2 * ORDER + iz] * a.scale;
-            int c = rec_corner(r[0]);
-            int c0 = c & 1023, c1 = (c >> 10) & 1023;
+    // per row of the plane: the sum of |q| Mz mmax^2 over the items whose
+    // stamp covers it, in units of 2^-12, each term rounded up
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int iz = window_iz<ORDER>(ws, t);
+        const float *rec = a.srec + (size_t)(wb[iz] + t - ws[iz]) * SR;
+        int bt = (int)ceilf(fabsf(rec[1]) * rec[kRecHead + 2 * ORDER + iz] * a.mmax2 * 4096.0f) + 1;
+        int c1 = (rec_corner(rec[0]) >> 10) & 1023;
 #pragma unroll
-            for (int iy = 0; iy < ORDER; ++iy) {
-                float wyz = r[kRecHead + ORDER + iy] * qz;
-                int row = ((c1 - iy) & (n - 1)) * RS;
+        for (int iy = 0; iy < ORDER; ++iy) atomicAdd(&rowb[(c1 - iy) & (n - 1)], bt);
+    }
+    __syncthreads();
+    int m = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) m = max(m, rowb[k]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) bmax[w] = m;
+    __syncthreads();
+    int mb = 0;
+    for (int k = 0; k < nw; ++k) mb = max(mb, bmax[k]);
+    // B 2^s < 2^30 with B < 2^e
+    int e;
+    frexpf((float)mb * (1.0f / 4096.0f), &e);
+    const int sh = min(30 - e, 60);
+    const float scale = ldexpf(1.0f, sh), inv = ldexpf(1.0f, -sh);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int iz = window_iz<ORDER>(ws, t);
+        const float *rec = a.srec + (size_t)(wb[iz] + t - ws[iz]) * SR;
+        float r[kRecHead + 2 * ORDER];
+        load_rec<float, kRecHead + 2 * ORDER>(rec, r);
+        float qz = r[1] * rec[kRecHead + 2 * ORDER + iz] * scale;
+        int c = rec_corner(r[0]);
+        int c0 = c & 1023, c1 = (c >> 10) & 1023;
 #pragma unroll
-                for (int ix = 0; ix < ORDER; ++ix) {
-                    int v = __float2int_rn(r[kRecHead + ix] * wyz);
-                    int k = row + ((c0 - ix) & (n - 1));
-                    atomicAdd(&thi[k], v >> 15);
-                    atomicAdd(&tlo[k], (unsigned)(v & 0x7fff));
-                }
+        for (int iy = 0; iy < ORDER; ++iy) {
+            float wyz = r[kRecHead + ORDER + iy] * qz;
+            int row = ((c1 - iy) & (n - 1)) * RS;
+#pragma unroll
+            for (int ix = 0; ix < ORDER; ++ix) {
+                int v = __float2int_rn(r[kRecHead + ix] * wyz);
+                atomicAdd(&tacc[row + ((c0 - ix) & (n - 1))], v);
             }
         }
     }
@@ -1671,8 +1686,8 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
 #pragma unroll
             for (int j = 0; j < P; ++j) {
                 int ka = (2 * pr) * RS + lane + 32 * j, kb = ka + RS;
-                val[r][2 * j] = (float)thi[ka] * a.inv_hi + (float)tlo[ka] * a.inv_lo;
-                val[r][2 * j + 1] = (float)thi[kb] * a.inv_hi + (float)tlo[kb] * a.inv_lo;
+                val[r][2 * j] = (float)tacc[ka] * inv;
+                val[r][2 * j + 1] = (float)tacc[kb] * inv;
             }
         }
     }
@@ -1725,7 +1740,7 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
 template <int P> static size_t fused_fwd_smem() {
     const int n = 32 * P, nh = n / 2 + 1;
     size_t fft = sizeof(float2) * ((size_t)n * nh + (size_t)32 * (n + n / 16));
-    size_t tiles = 2 * sizeof(int) * (size_t)n * (n + 1);
+    size_t tiles = sizeof(int) * (size_t)n * (n + 1);
     return sizeof(float2) * (size_t)plane_tw_entries<P>() + std::max(fft, tiles);
 }
 
@@ -2107,12 +2122,8 @@ int mg_spme_init(mg_handle *h) {
     int k = 30;
     while (k > 4 && std::ldexp(bound, k) >= 2147483648.0 * 0.99) --k;
     h->fx_shift = k;
-    // fused spread: one stamp value, at most max|q| (max B-spline value)^3,
-    // stays below 2^30
-    double bound1 = qmax * mmax * mmax * mmax * 1.01;
-    int kp = 30;
-    while (kp > 4 && std::ldexp(bound1, kp) >= 1073741824.0 * 0.99) --kp;
-    h->plane_shift = kp;
+    // fused spread: its per-plane scale bounds point sums with mmax
+    h->spl_mmax = mmax;
     // FP64 form: the whole mesh sums in 64 bits; no point can hold more than
     // np * max|q| * (max B-spline value)^3
     double bound64 = (double)h->np * qmax * mmax * mmax * mmax * 1.01;
@@ -2493,9 +2504,7 @@ static int spme_fused(mg_handle *h, SplineArgs sa, BrickArgs bk) {
     PlaneArgs pa;
     pa.start = h->d_brick_start;
     pa.srec = h->d_spl_plane;
-    pa.scale = std::ldexp(1.0f, h->plane_shift);
-    pa.inv_hi = std::ldexp(1.0f, 15 - h->plane_shift);
-    pa.inv_lo = std::ldexp(1.0f, -h->plane_shift);
+    pa.mmax2 = (float)(h->spl_mmax * h->spl_mmax);
     pa.err = h->d_err;
     int st;
     switch (n) {
