@@ -287,6 +287,18 @@ int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps,
  * mode, without angle terms; runs a UTotal first and leaves the reciprocal
  * scratch (structure factors, meshes) changed. */
 int mg_force_jvp(mg_handle *h, const double *u, double *jv);
+/* The force's parameter derivatives along u: dq[np] = u . d(forceo)/dq_k
+ * for each particle charge, deps[nptpt] and dsig[nptpt] = u . d(forceo)/d
+ * eps_ab, d sigma_ab for the (1,6,12) pair parameters (Lorentz-Berthelot
+ * from pp's sigat, epsat; lljcut's cut as in mg_grad), at the handle's
+ * positions: the Lennard-Jones force differentiated analytically, the
+ * real-space Coulomb force through erfc, the reciprocal part as the
+ * charges' field along u_k minus the potential of the dipoles q_i u_i (the
+ * dipole kernels), and the surface term.  The adjoint of MD trajectories
+ * needs it for parameter gradients.  Same handles as mg_force_jvp; runs a
+ * UTotal first. */
+int mg_force_pvjp(mg_handle *h, const mg_pot_params *pp, const double *u, double *dq, double *deps,
+                  double *dsig);
 /* UTotal at the current positions and its derivative by an affine strain of
  * the box and the positions, r -> (1 + eps) r: w[9] (row-major, symmetric)
  * = dU/deps_ab, the virial tensor (pairs and bonds r_a f_b, angles through

@@ -105,6 +105,7 @@ LIB_ONLY = [
     ("grad", C.c_int, [H, C.POINTER(MgPotParams), PF64, PF64, PF64, PF64]),
     ("virial_tensor", C.c_int, [H, PF64]),
     ("force_jvp", C.c_int, [H, PF64, PF64]),
+    ("force_pvjp", C.c_int, [H, C.POINTER(MgPotParams), PF64, PF64, PF64, PF64]),
     ("ensemble_create", C.c_int, [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     ("ensemble_run", C.c_int, [H, C.c_int32, C.c_int32, PF64]),
     ("ensemble_kernels", C.c_int, [H, C.c_int32, PI32]),

@@ -128,6 +128,71 @@ int mg_force_jvp_rec(mg_handle *h, const double *u, double *jv) {
     return MG_OK;
 }
 
+// dq_k += EpsiFourPi (u_k . e_q(r_k) - phi_p(r_k)) - 2 (2 pi / 3V) EpsiFourPi
+// (u_k . M + S . r_k): the reciprocal field of the charges at k, minus the
+// reciprocal potential at k of the dipoles q_i u_i, and the surface term's
+// charge derivative (M = sum q r, S = sum q u)
+__global__ void k_pvjp_rec_combine(int np, const double *__restrict__ ro, const double *__restrict__ u,
+                                   const double *__restrict__ est, const double *__restrict__ pot,
+                                   const double *__restrict__ m3, const double *__restrict__ s3, double surf,
+                                   double efp, double *__restrict__ dq) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const double *uk = u + 3 * k, *ek = est + 3 * k, *rk = ro + 3 * k;
+    double v = uk[0] * ek[0] + uk[1] * ek[1] + uk[2] * ek[2] - pot[k];
+    if (m3)
+        v -= surf * (uk[0] * m3[0] + uk[1] * m3[1] + uk[2] * m3[2] + s3[0] * rk[0] + s3[1] * rk[1] + s3[2] * rk[2]);
+    dq[k] += efp * v;
+}
+
+// the reciprocal and surface parts of u . d(force)/dq (force units before
+// force_fac, added to dq; device arrays; u scaled to a largest component
+// of 1; after a UTotal of these positions, whose surface sums it reads):
+// force_i = EpsiFourPi q_i e_i with e_i linear in the charges, so
+// u . d(force)/dq_k = EpsiFourPi (u_k . e_k + sum_i q_i u_i . K(r_i, r_k)),
+// and the sum is minus the potential at r_k of the dipoles q_i u_i.  Each
+// particle's own contributions vanish (its field and its dipole's
+// potential at its own site are zero by symmetry).
+int mg_force_pvjp_rec(mg_handle *h, const double *u, double *dq) {
+    const int np = h->np;
+    const size_t nvir = std::max((size_t)h->nkvec, (size_t)np + 2 * (size_t)std::max(h->nblk_rec, 1));
+    const size_t need = 26 * (size_t)np + nvir + 3;
+    if (h->dip_scr_n < need) {
+        if (h->d_dip_scr) cudaFree(h->d_dip_scr);
+        h->d_dip_scr = nullptr;
+        h->dip_scr_n = 0;
+        MG_CUDA(h, cudaMalloc(&h->d_dip_scr, sizeof(double) * need));
+        h->dip_scr_n = need;
+    }
+    double *p = h->d_dip_scr, *zero = p + 3 * (size_t)np, *pot = zero + 3 * (size_t)np, *est = pot + np,
+           *efg = est + 3 * (size_t)np, *pot2 = efg + 6 * (size_t)np, *est2 = pot2 + np,
+           *efg2 = est2 + 3 * (size_t)np, *vir = efg2 + 6 * (size_t)np, *s3 = vir + nvir;
+    MG_CUDA(h, cudaMemsetAsync(zero, 0, sizeof(double) * 23 * (size_t)np, h->st));   // zero .. efg2
+    k_jvp_dipoles<<<(3 * np + 255) / 256, 256, 0, h->st>>>(np, h->d_az, u, p);
+    if (h->ewald == MG_EWALD_STD) {
+        MG_TRY(mg_ewald_std_dipole(h, h->d_az, zero, pot, est, efg, vir));   // the charges' field
+        MG_TRY(mg_ewald_std_dipole(h, zero, p, pot2, est2, efg2, vir));      // the dipoles' potential
+    } else {
+        double kmax = std::max(h->dkdr[0], std::max(h->dkdr[1], h->dkdr[2]));
+        double b1 = (double)np * h->az_absmax * 1.01 + 1.0;
+        double b2 = (double)np * (3.0 * kmax * h->az_absmax) * 1.01 + 1.0;
+        MG_TRY(mg_spme_dipole(h, h->d_az, zero, b1, pot, est, efg, vir));
+        MG_TRY(mg_spme_dipole(h, zero, p, b2, pot2, est2, efg2, vir));
+    }
+    const double *m3 = nullptr;
+    double surf = 0.0;
+    if (h->lsurf) {
+        k_jvp_qu_sum<<<1, 1024, 0, h->st>>>(np, h->d_az, u, s3);
+        m3 = h->d_uout + h->nptpt + 1 + 4;   // sum q r of the last UTotal
+        surf = 2.0 * (2.0 * 3.14159265358979323846 / (3.0 * h->vol));
+    }
+    k_pvjp_rec_combine<<<(np + 127) / 128, 128, 0, h->st>>>(np, h->d_ro, u, est, pot2, m3, s3, surf, h->EpsiFourPi,
+                                                            dq);
+    h->launches += 3 + (h->lsurf ? 1 : 0);
+    MG_CUDA(h, cudaGetLastError());
+    return MG_OK;
+}
+
 extern "C" int mg_dipole_ewald(mg_handle *h, const double *dip, double *potstat, double *estat, double *efg,
                                double *virelec) {
     if (!h || !dip || !potstat || !estat || !efg || !virelec) return MG_ERR_ARG;

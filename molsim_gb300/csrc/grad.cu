@@ -569,6 +569,77 @@ __global__ void k_jvp_bonds(int nbond, const int *__restrict__ ij, const double 
     }
 }
 
+// u . d(force)/d(parameter) over the full Verlet list (one thread per slot,
+// each unordered pair met twice): the Lennard-Jones force fsum = (24 eps /
+// r^2)(2 x^2 - x), x = (sigma/r)^6, differentiated by eps_ab and sigma_ab
+// (with lljcut only inside the cut), and the real-space Coulomb force
+// EpsiFourPi q_i q_j g(r) d by the particle's own charge, g = (erfc(a r)/r +
+// 2a/sqrt(pi) exp(-a^2 r^2)) / r^2 with Ewald, 1/r^3 without; all along
+// w = u_i - u_j.  dq[p] is the particle's charge derivative, the per-pair
+// parameter sums go to per-block partials [deps(nptpt), dsig(nptpt)].
+struct PvjpArgs {
+    const double *ro, *az;
+    const int *type, *pairidx, *perm, *nnb, *nbr;
+    int np, npt, nptpt, ewald, lljcut;
+    mg_box box;
+    double rcut2, efp, alpha;
+    const double *sig, *eps, *ljrc, *r2atat, *r2umin;
+    const double *u;
+    double *dq, *part;
+};
+
+__global__ void __launch_bounds__(kGradThreads) k_pvjp_pairs(PvjpArgs a) {
+    __shared__ double red[2 * MG_MAX_NPTPT][kGradThreads / 32];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double de[MG_MAX_NPTPT], ds[MG_MAX_NPTPT];
+    for (int k = 0; k < a.nptpt; ++k) { de[k] = 0.0; ds[k] = 0.0; }
+    if (i < a.np) {
+        int p = a.perm[i], ti = a.type[p];
+        const double *ri = a.ro + 3 * (size_t)p;
+        const double *ui = a.u + 3 * (size_t)p;
+        double dq = 0.0;
+        int nn = a.nnb[i];
+        for (int k = 0; k < nn; ++k) {
+            int q = a.perm[a.nbr[(size_t)k * a.np + i]];
+            const double *rj = a.ro + 3 * (size_t)q;
+            double d[3] = {mg_pbc1(ri[0] - rj[0], a.box.half[0], a.box.len[0]),
+                           mg_pbc1(ri[1] - rj[1], a.box.half[1], a.box.len[1]),
+                           mg_pbc1(ri[2] - rj[2], a.box.half[2], a.box.len[2])};
+            double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (r2 > a.rcut2) continue;
+            int pair = a.pairidx[a.type[q] * a.npt + ti] - 1;
+            if (r2 < a.r2atat[pair] || r2 < a.r2umin[pair]) continue;
+            const double *uj = a.u + 3 * (size_t)q;
+            double dw = d[0] * (ui[0] - uj[0]) + d[1] * (ui[1] - uj[1]) + d[2] * (ui[2] - uj[2]);
+            double r = sqrt(r2);
+            double g = a.ewald != MG_EWALD_NONE
+                           ? (erfc(a.alpha * r) / r + 1.1283791670955126 * a.alpha * exp(-a.alpha * a.alpha * r2)) / r2
+                           : 1.0 / (r2 * r);
+            dq += a.efp * a.az[q] * g * dw;
+            if (a.sig && (!a.lljcut || r < a.ljrc[pair])) {
+                double sg = a.sig[pair], x = sg * sg / r2;
+                x = x * x * x;
+                de[pair] += 0.5 * (24.0 / r2) * (2.0 * x * x - x) * dw;
+                ds[pair] += 0.5 * (144.0 * a.eps[pair] * x * (4.0 * x - 1.0) / (sg * r2)) * dw;
+            }
+        }
+        a.dq[p] += dq;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int nv = 2 * a.nptpt;
+    for (int v = 0; v < nv; ++v) {
+        double x = v < a.nptpt ? de[v] : ds[v - a.nptpt];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[v][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double t = 0.0;
+        for (int k = 0; k < kGradThreads / 32; ++k) t += red[threadIdx.x][k];
+        a.part[(size_t)blockIdx.x * nv + threadIdx.x] = t;
+    }
+}
+
 __global__ void k_scale(double *__restrict__ x, size_t n, double f) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] *= f;
@@ -653,6 +724,108 @@ extern "C" int mg_force_jvp(mg_handle *h, const double *u, double *jv) {
             st = mg_fail(h, MG_ERR_CUDA, "mg_force_jvp: kernels or copy failed");
     } while (false);
     cudaFree(d_u);
+    return st;
+}
+
+// u . d(forceo)/d(parameter) at the handle's positions: dq[np] for the
+// particles' charges, deps and dsig[nptpt] for the pair types' LJ epsilon
+// and sigma (Lorentz-Berthelot from pp as in mg_grad); forceo units
+extern "C" int mg_force_pvjp(mg_handle *h, const mg_pot_params *pp, const double *u, double *dq, double *deps,
+                             double *dsig) {
+    if (!h || !pp || !pp->sigat || !pp->epsat || !u || !dq || !deps || !dsig) return MG_ERR_ARG;
+    if (pp->npt != h->npt) return mg_fail(h, MG_ERR_ARG, "pot params npt %d != %d", pp->npt, h->npt);
+    if (h->form != MG_FP64) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_pvjp needs the FP64 form");
+    if (h->txintlist != MG_VLIST) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_pvjp needs the Verlet list");
+    if (h->mode == MG_MC) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_pvjp needs an MD or BD handle");
+    if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_force_pvjp needs a neighbour list (NList)");
+    const int np = h->np, npt = h->npt, nptpt = h->nptpt;
+    double umax = 0.0;
+    for (int i = 0; i < 3 * np; ++i) umax = std::max(umax, std::fabs(u[i]));
+    if (umax == 0.0) {
+        for (int i = 0; i < np; ++i) dq[i] = 0.0;
+        for (int k = 0; k < nptpt; ++k) deps[k] = dsig[k] = 0.0;
+        return MG_OK;
+    }
+    std::vector<double> us(u, u + 3 * (size_t)np);
+    for (double &x : us) x /= umax;
+    std::vector<double> ab(3 * (size_t)nptpt, 0.0);
+    for (int a = 0; a < npt; ++a)
+        for (int b = 0; b < npt; ++b) {
+            int pair = h->h_pairidx[b * npt + a] - 1;
+            double sg = 0.5 * (pp->sigat[a] + pp->sigat[b]);
+            ab[pair] = sg;
+            ab[nptpt + pair] = std::sqrt(pp->epsat[a] * pp->epsat[b]);
+            ab[2 * nptpt + pair] = pp->ljrcut * sg;
+        }
+    MG_TRY(mg_utotal_launch(h));   // the reciprocal state and the surface sums of these positions
+    int nblk = (np + kGradThreads - 1) / kGradThreads, nv = 2 * nptpt;
+    size_t need = 4 * (size_t)np + 3 * nptpt + (size_t)nblk * nv;
+    double *d = nullptr;
+    MG_CUDA(h, cudaMalloc(&d, sizeof(double) * need));
+    double *d_u = d, *d_dq = d_u + 3 * (size_t)np, *d_ab = d_dq + np, *d_part = d_ab + 3 * nptpt;
+    int st = MG_OK;
+    std::vector<double> part((size_t)nblk * nv);
+    do {
+        if (cudaMemcpyAsync(d_u, us.data(), sizeof(double) * 3 * np, cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+            cudaMemcpyAsync(d_ab, ab.data(), sizeof(double) * 3 * nptpt, cudaMemcpyHostToDevice, h->st) !=
+                cudaSuccess ||
+            cudaMemsetAsync(d_dq, 0, sizeof(double) * np, h->st) != cudaSuccess) {
+            st = mg_fail(h, MG_ERR_CUDA, "mg_force_pvjp: copy failed");
+            break;
+        }
+        PvjpArgs a;
+        a.ro = h->d_ro;
+        a.az = h->d_az;
+        a.type = h->d_type;
+        a.pairidx = h->d_pairidx;
+        a.perm = h->d_perm;
+        a.nnb = h->d_nnb;
+        a.nbr = h->d_nbr;
+        a.np = np;
+        a.npt = npt;
+        a.nptpt = nptpt;
+        a.ewald = h->ewald;
+        a.lljcut = pp->lljcut;
+        for (int m = 0; m < 3; ++m) {
+            a.box.len[m] = h->boxlen[m];
+            a.box.half[m] = h->boxlen2[m];
+            a.box.inv[m] = h->boxleni[m];
+        }
+        a.rcut2 = h->rcut2;
+        a.efp = h->EpsiFourPi;
+        a.alpha = h->ualpha;
+        a.sig = d_ab;
+        a.eps = d_ab + nptpt;
+        a.ljrc = d_ab + 2 * nptpt;
+        a.r2atat = h->d_r2atat;
+        a.r2umin = h->d_r2umin;
+        a.u = d_u;
+        a.dq = d_dq;
+        a.part = d_part;
+        k_pvjp_pairs<<<nblk, kGradThreads, 0, h->st>>>(a);
+        h->launches++;
+        if (h->ewald != MG_EWALD_NONE && (st = mg_force_pvjp_rec(h, d_u, d_dq)) != MG_OK) break;
+        k_scale<<<(np + 255) / 256, 256, 0, h->st>>>(d_dq, (size_t)np, h->force_fac * umax);
+        h->launches++;
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(dq, d_dq, sizeof(double) * np, cudaMemcpyDeviceToHost, h->st) != cudaSuccess ||
+            cudaMemcpyAsync(part.data(), d_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(h->st) != cudaSuccess) {
+            st = mg_fail(h, MG_ERR_CUDA, "mg_force_pvjp: kernels or copy failed");
+            break;
+        }
+        for (int k = 0; k < nptpt; ++k) {
+            double e = 0.0, g = 0.0;
+            for (int b = 0; b < nblk; ++b) {
+                e += part[(size_t)b * nv + k];
+                g += part[(size_t)b * nv + nptpt + k];
+            }
+            deps[k] = e * h->force_fac * umax;
+            dsig[k] = g * h->force_fac * umax;
+        }
+    } while (false);
+    cudaFree(d);
     return st;
 }
 

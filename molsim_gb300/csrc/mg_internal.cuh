@@ -411,6 +411,7 @@ int mg_spme_dipole(mg_handle *h, const double *az, const double *dip, double bou
 int mg_ewald_std_dipole(mg_handle *h, const double *az, const double *dip, double *pot, double *est, double *efg,
                         double *vir);
 int mg_force_jvp_rec(mg_handle *h, const double *u, double *jv);
+int mg_force_pvjp_rec(mg_handle *h, const double *u, double *dq);
 int mg_spme_load_mesh(mg_handle *h, const double *q);
 int mg_spme_mesh_to_f64(mg_handle *h, double *out, double mul);
 int mg_spme_fft_check(mg_handle *h, const double *q, const double *mult, const double *ew, double *phi,

@@ -173,6 +173,19 @@ class Engine:
         self._check(self.lib.mg_force_jvp(self.h, abi.f64(u), abi.f64(jv)), "force_jvp")
         return jv.reshape(self.np, 3)
 
+    def ForcePVJP(self, u):
+        """u . d(forceo)/d(parameter) at the current positions: dq per
+        particle charge, deps and dsig per pair type (Lorentz-Berthelot from
+        the species), by hand-written kernels (mg_force_pvjp)."""
+        pp, keep = self.system.pot_params()
+        u = abi.as_f64(np.asarray(u, dtype=np.float64).reshape(-1))
+        dq = np.zeros(self.np)
+        de = np.zeros(self.nptpt)
+        ds = np.zeros(self.nptpt)
+        self._check(self.lib.mg_force_pvjp(self.h, C.byref(pp), abi.f64(u), abi.f64(dq), abi.f64(de),
+                                           abi.f64(ds)), "force_pvjp")
+        return dict(dq=dq, deps=de, dsig=ds)
+
     def VirialTensor(self):
         """dU/deps_ab (3x3) for an affine strain of the box and positions;
         its trace is UTotal's virial."""

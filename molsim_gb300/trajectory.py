@@ -18,7 +18,10 @@ the first.  It needs the forces at every step and Hessian-vector products:
   the largest displacement is 1e-5 A.
 
 `TrajectoryFunction` exposes this to torch.autograd; its gradients are
-dL/dx0 and dL/dv0.
+dL/dx0 and dL/dv0.  `backward(cks, params=True)` also returns the gradients
+with respect to the species' charges, sigma and epsilon: each state's
+dU/dtheta (mg_grad) plus, at each force evaluation, the adjoint of the
+acceleration times d(forceo)/dtheta (mg_force_pvjp).
 """
 import numpy as np
 
@@ -87,9 +90,29 @@ class Trajectory:
         fm, _ = self.forces(x - eps * u)
         return (fp - fm) / (2.0 * eps)
 
-    def backward(self, cks):
-        """dL/dx0 and dL/dv0 by the adjoint of velocity Verlet."""
+    def _param_terms(self, x, w, lam):
+        """At x: w dU/dtheta + (d acc / dtheta)^T lam, as dq (per
+        particle), deps and dsig (per pair type)."""
+        self.e.SetPositions(self._wrap(x))
+        self.e.NList("write")
+        g = self.e.Grad()
+        out = dict(dq=w * g["phi"], deps=w * g["du_deps"], dsig=w * g["du_dsig"])
+        u = self.im * lam
+        if np.abs(u).max() > 0.0:
+            pv = self.e.ForcePVJP(u)
+            for k in out:
+                out[k] = out[k] + pv[k]
+        return out
+
+    def backward(self, cks, params=False):
+        """dL/dx0 and dL/dv0 by the adjoint of velocity Verlet; with params
+        also the gradients with respect to the species' charges (dz),
+        sigma (dsig) and epsilon (deps), and their per-particle and
+        per-pair-type forms."""
         dt, w = self.dt, 1.0 / (self.n + 1)
+        gp = None
+        if params:
+            gp = dict(dq=np.zeros(self.s.np_), deps=np.zeros(self.s.nptpt), dsig=np.zeros(self.s.nptpt))
         gx = np.zeros_like(cks[0][0])   # adjoints of x, v, a after the step being undone
         gv = np.zeros_like(gx)
         ga = np.zeros_like(gx)
@@ -111,6 +134,9 @@ class Trajectory:
                 gx = gx - w * f / units.FORCE_FAC
                 # v' = v + dt/2 a + dt/2 a'
                 ga_tot = ga + 0.5 * dt * gv
+                if params:   # U(x_k) and a' = acc(x_k; theta)
+                    for key, val in self._param_terms(xk, w, ga_tot).items():
+                        gp[key] += val
                 gv_prev = gv.copy()
                 ga_prev = 0.5 * dt * gv
                 # a' = acc(x')
@@ -124,7 +150,14 @@ class Trajectory:
         x0 = cks[0][0]
         f0, _ = self.forces(x0)
         gx = gx - w * f0 / units.FORCE_FAC + self._jtv(x0, ga)
-        return gx, gv
+        if not params:
+            return gx, gv
+        for key, val in self._param_terms(x0, w, ga).items():
+            gp[key] += val
+        from .autograd import _species_grads
+        dz, dsig, deps = _species_grads(self.s, dict(phi=gp["dq"], du_dsig=gp["dsig"], du_deps=gp["deps"]))
+        gp.update(dz=dz, dsig_species=dsig, deps_species=deps)
+        return gx, gv, gp
 
     def close(self):
         self.e.close()

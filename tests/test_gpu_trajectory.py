@@ -66,3 +66,59 @@ def test_trajectory_autograd_and_checkpointing(gpu_lib):
     assert np.allclose(v.grad.numpy(), gv, rtol=0, atol=1e-12 * np.abs(gv).max())
     tr.close()
     full.close()
+
+
+def _with_params(s, dz=None, dsig=None, deps=None):
+    """The system with one species parameter changed and its table rebuilt."""
+    import dataclasses
+    sp = list(s.species)
+    for k, d in ((0, dz), (1, dsig), (2, deps)):
+        if d is not None:
+            a, h = d
+            f = ("charge", "sigma", "eps")[k]
+            sp[a] = dataclasses.replace(sp[a], **{f: getattr(sp[a], f) + h})
+    t = dataclasses.replace(s, species=sp, ubuf=None, iubuflow=None, r2umin=None, nugrid=None)
+    t.utoltab, t.ftoltab = s.utoltab, s.ftoltab
+    t.build_table()
+    return t
+
+
+def test_trajectory_parameter_gradients(gpu_lib):
+    """dL/d(sigma, epsilon) of each species through a 20-step trajectory
+    (dU/dtheta at every state from mg_grad, the acceleration adjoints times
+    d(force)/dtheta from mg_force_pvjp) against central differences of L
+    with the species parameter changed by 1e-4 of itself (tables rebuilt),
+    within 1e-5 of the largest gradient of each kind.  The charges are
+    checked along a direction that keeps the system neutral, all of them
+    scaled by (1 + t): dL/dt = sum_a z_a dL/dz_a."""
+    s, x0, v0 = _setup()
+    tr = Trajectory(s, dt=0.002, nsteps=20, checkpoint=5)
+    L0, cks = tr.forward(x0, v0)
+    _, _, gp = tr.backward(cks, params=True)
+    tr.close()
+
+    def L_of(t):
+        tt = Trajectory(t, dt=0.002, nsteps=20, checkpoint=5)
+        val = tt.forward(x0, v0)[0]
+        tt.close()
+        return val
+
+    for a in range(s.npt):
+        h = 1e-4 * s.species[a].sigma
+        fd = (L_of(_with_params(s, dsig=(a, h))) - L_of(_with_params(s, dsig=(a, -h)))) / (2 * h)
+        assert abs(fd - gp["dsig_species"][a]) <= 1e-5 * np.abs(gp["dsig_species"]).max(), (a, fd, gp["dsig_species"])
+        h = 1e-4 * s.species[a].eps
+        fd = (L_of(_with_params(s, deps=(a, h))) - L_of(_with_params(s, deps=(a, -h)))) / (2 * h)
+        assert abs(fd - gp["deps_species"][a]) <= 1e-5 * np.abs(gp["deps_species"]).max(), (a, fd, gp["deps_species"])
+    # charges: every species scaled by (1 + t), d L / dt = sum_a z_a dL/dz_a
+    def scaled(t):
+        import dataclasses
+        sp = [dataclasses.replace(x, charge=x.charge * (1.0 + t)) for x in s.species]
+        u = dataclasses.replace(s, species=sp, ubuf=None, iubuflow=None, r2umin=None, nugrid=None)
+        u.utoltab, u.ftoltab = s.utoltab, s.ftoltab
+        u.build_table()
+        return u
+    h = 1e-4
+    fd = (L_of(scaled(h)) - L_of(scaled(-h))) / (2 * h)
+    an = sum(s.species[a].charge * gp["dz"][a] for a in range(s.npt))
+    assert abs(fd - an) <= 1e-5 * abs(an), (fd, an)
