@@ -88,7 +88,7 @@ def test_trajectory_parameter_gradients(gpu_lib):
     (dU/dtheta at every state from mg_grad, the acceleration adjoints times
     d(force)/dtheta from mg_force_pvjp) against central differences of L
     with the species parameter changed by 1e-4 of itself (tables rebuilt),
-    within 1e-5 of the largest gradient of each kind.  The charges are
+    within 1e-6 of the largest gradient of each kind.  The charges are
     checked along a direction that keeps the system neutral, all of them
     scaled by (1 + t): dL/dt = sum_a z_a dL/dz_a."""
     s, x0, v0 = _setup()
@@ -106,10 +106,10 @@ def test_trajectory_parameter_gradients(gpu_lib):
     for a in range(s.npt):
         h = 1e-4 * s.species[a].sigma
         fd = (L_of(_with_params(s, dsig=(a, h))) - L_of(_with_params(s, dsig=(a, -h)))) / (2 * h)
-        assert abs(fd - gp["dsig_species"][a]) <= 1e-5 * np.abs(gp["dsig_species"]).max(), (a, fd, gp["dsig_species"])
+        assert abs(fd - gp["dsig_species"][a]) <= 1e-6 * np.abs(gp["dsig_species"]).max(), (a, fd, gp["dsig_species"])
         h = 1e-4 * s.species[a].eps
         fd = (L_of(_with_params(s, deps=(a, h))) - L_of(_with_params(s, deps=(a, -h)))) / (2 * h)
-        assert abs(fd - gp["deps_species"][a]) <= 1e-5 * np.abs(gp["deps_species"]).max(), (a, fd, gp["deps_species"])
+        assert abs(fd - gp["deps_species"][a]) <= 1e-6 * np.abs(gp["deps_species"]).max(), (a, fd, gp["deps_species"])
     # charges: every species scaled by (1 + t), d L / dt = sum_a z_a dL/dz_a
     def scaled(t):
         import dataclasses
@@ -121,4 +121,4 @@ def test_trajectory_parameter_gradients(gpu_lib):
     h = 1e-4
     fd = (L_of(scaled(h)) - L_of(scaled(-h))) / (2 * h)
     an = sum(s.species[a].charge * gp["dz"][a] for a in range(s.npt))
-    assert abs(fd - an) <= 1e-5 * abs(an), (fd, an)
+    assert abs(fd - an) <= 1e-6 * abs(an), (fd, an)
