@@ -519,6 +519,21 @@ int mg_poly_rigid_setup(mg_poly *c, double tstep, double tvvite, int32_t nvvite,
                         const double *angvelo, const double *rodd, const double *quadd);
 int mg_poly_rigid_move(mg_poly *c, double *ro, double *ori, double *drostep);
 int mg_poly_rigid_kick(mg_poly *c, const double *forceo, const double *torqueo, double *rod, double *angvelo);
+/* nstep steps of the rigid-body VelVer on the device, without the host
+ * between the steps: move, atom placement (SetAtomProp, r = ro + ori ra
+ * with ra[3*sum(napt)] the local atom positions of the particle types, type
+ * after type), the centres' Verlet list rebuilt on the centres handle hc
+ * (an MD handle of the np particle centres with rcut >= the pair cutoff,
+ * after mg_set_positions and mg_nlist_set), UTwoBodyP over it, with Ewald
+ * (ualpha > 0) the atoms' reciprocal sum and atomic self term on the FP64
+ * atom handle ha (its particles the atoms, folded into the box) and the
+ * molecular self term, UTotal's end and the kick.  After
+ * mg_poly_rigid_setup (and mg_poly_rigid_prime if wanted).  Returns the
+ * last step's ro[3*np], ori[9*np] (column-major), rod[3*np], angvelo[3*np]
+ * and uout[4] = u%tot, u%twob(0), u%rec, virial.  Charges only (no
+ * dipoles). */
+int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const double *ra, int32_t nstep, double *ro,
+                   double *ori, double *rod, double *angvelo, double *uout);
 /* the accelerations of the current state from forceo and torqueo (a kick
  * of zero length: GetLinAcc, GetAngAcc), for a run that starts from
  * evaluated forces instead of the reference's zero accelerations */

@@ -126,6 +126,7 @@ LIB_ONLY = [
     ("poly_rigid_kick", C.c_int, [H, PF64, PF64, PF64, PF64]),
     ("poly_rigid_prime", C.c_int, [H, PF64, PF64]),
     ("poly_rigid_get", C.c_int, [H, PF64, PF64]),
+    ("poly_md_run", C.c_int, [H, H, H, PF64, C.c_int32, PF64, PF64, PF64, PF64, PF64]),
     ("poly_last_error", C.c_int, [H, C.c_char_p, C.c_size_t]),
     ("poly_destroy", C.c_int, [H]),
     ("ewald_rec_std_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, PF64, C.c_double, C.c_int32,

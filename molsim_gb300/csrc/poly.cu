@@ -158,14 +158,15 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
 // ia < ja in order; the thread owns its atoms' forces
 __global__ void __launch_bounds__(kPolyThreads) k_ewald_intra(PolyArgs a, const double *__restrict__ aza,
                                                               double ualpha, double ualpha2, double ewaldfac1,
-                                                              double efp) {
+                                                              double efp, int accumulate) {
     __shared__ double red[kPolyThreads];
     double u = 0.0;
     int ip = blockIdx.x * blockDim.x + threadIdx.x;
     if (ip < a.np) {
         int ialow = a.ianpn[ip] - 1, iaupp = ialow + a.napt[a.iptpn[ip] - 1];
-        for (int ia = ialow; ia < iaupp; ++ia)
-            for (int k = 0; k < 3; ++k) a.force[3 * ia + k] = 0.0;
+        if (!accumulate)
+            for (int ia = ialow; ia < iaupp; ++ia)
+                for (int k = 0; k < 3; ++k) a.force[3 * ia + k] = 0.0;
         for (int ia = ialow; ia < iaupp; ++ia) {
             for (int ja = ia + 1; ja < iaupp; ++ja) {
                 double dx = __dsub_rn(a.r[3 * ia], a.r[3 * ja]);
@@ -926,7 +927,7 @@ extern "C" int mg_poly_ewald_intra(mg_poly *c, const double *r, double *force, d
     double ualpha2 = p.ualpha * p.ualpha;
     double fac = 1.0 / (std::sqrt(3.1415926535897932) * p.ualpha);
     double ewaldfac1 = fac * 2.0 * ualpha2;
-    k_ewald_intra<<<c->nblk, kPolyThreads>>>(a, c->d_aza, p.ualpha, ualpha2, ewaldfac1, p.epsi_four_pi);
+    k_ewald_intra<<<c->nblk, kPolyThreads>>>(a, c->d_aza, p.ualpha, ualpha2, ewaldfac1, p.epsi_four_pi, 0);
     POLY_CUDA(c, cudaGetLastError());
     POLY_CUDA(c, cudaMemcpy(force, c->d_force, sizeof(double) * 3 * p.na, cudaMemcpyDeviceToHost));
     POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->nblk, cudaMemcpyDeviceToHost));
@@ -1496,4 +1497,185 @@ extern "C" int mg_poly_udipole_finish(mg_poly *c, const double *dip, const doubl
     POLY_CUDA(c, cudaMemcpy(torque, d_t, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost));
     *u_stat = p.epsi_four_pi * 0.5 * u;
     return MG_OK;
+}
+
+// ---- rigid-body MD of polyatomic particles on the device ------------------------
+// VelVer with lpolyatom (md.F90:252-420) step after step without the host:
+// move (centres, quaternions, orientations), atom placement (SetAtomProp:
+// r = ro + ori ra, molaux.F90:540-560), the centres' list rebuilt, the atom
+// pairs over it (UTwoBodyP), with Ewald the atoms' reciprocal sum and
+// atomic self term through the atom handle and the molecular self term,
+// UTotal's end (forces and torques of the particles), kick.
+namespace {
+
+// r = ro + ori ra for every atom (ori(3,3,np) column-major, ra the local
+// positions by particle type, atoms of a type consecutive from ra_off[type])
+__global__ void k_place_atoms(int np, const int *__restrict__ iptpn, const int *__restrict__ ianpn,
+                              const int *__restrict__ napt, const int *__restrict__ ra_off,
+                              const double *__restrict__ ra, const double *__restrict__ ro,
+                              const double *__restrict__ ori, double *__restrict__ r) {
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= np) return;
+    int t = iptpn[ip] - 1, a0 = ianpn[ip] - 1, na = napt[t];
+    const double *o = ori + 9 * (size_t)ip, *c = ro + 3 * (size_t)ip;
+    for (int k = 0; k < na; ++k) {
+        const double *x = ra + 3 * (size_t)(ra_off[t] + k);
+        for (int m = 0; m < 3; ++m)
+            r[3 * (size_t)(a0 + k) + m] = c[m] + o[m] * x[0] + o[m + 3] * x[1] + o[m + 6] * x[2];
+    }
+}
+
+// the atom positions folded into the box for the atom handle (PBC: ANINT)
+__global__ void k_fold_atoms(int na, const double *__restrict__ r, mg_box box, double *__restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * na) return;
+    int m = i % 3;
+    double x = r[i];
+    if (fabs(x) > box.half[m]) x -= box.len[m] * round(x * box.inv[m]);
+    out[i] = x;
+}
+
+__global__ void k_add_scaled(size_t n, const double *__restrict__ x, double f, double *__restrict__ y) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += f * x[i];
+}
+
+}  // namespace
+
+extern "C" int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const double *ra, int32_t nstep,
+                              double *ro, double *ori, double *rod, double *angvelo, double *uout) {
+    if (!c || !hc || !ra || nstep < 1 || !ro || !ori || !rod || !angvelo || !uout) return MG_ERR_ARG;
+    const mg_poly_params &p = c->p;
+    if (!c->d_rig) return poly_fail(c, MG_ERR_STATE, "mg_poly_rigid_setup has not been called");
+    if (hc->np != p.np) return poly_fail(c, MG_ERR_ARG, "the centres handle holds %d particles, not %d", hc->np, p.np);
+    if (!hc->list_valid) return poly_fail(c, MG_ERR_STATE, "the centres handle has no list (mg_nlist_set)");
+    if (!(hc->rcut >= p.rcut))
+        return poly_fail(c, MG_ERR_ARG, "the centres handle's rcut %g is below the pair cutoff %g", hc->rcut, p.rcut);
+    for (int m = 0; m < 3; ++m)
+        if (hc->boxlen[m] != p.boxlen[m]) return poly_fail(c, MG_ERR_ARG, "the centres handle has another box");
+    bool ewald = p.ualpha > 0.0;
+    if (ewald) {
+        if (!ha || ha->np != p.na || ha->form != MG_FP64 || ha->ewald == MG_EWALD_NONE)
+            return poly_fail(c, MG_ERR_ARG, "Ewald needs an FP64 Ewald handle of the %d atoms", p.na);
+        if (!c->d_aza) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.aza (atom charges) was not given");
+    }
+    const int np = p.np, na = p.na;
+    // local positions by type, the type offsets
+    std::vector<int> off(p.npt + 1, 0);
+    for (int t = 0; t < p.npt; ++t) off[t + 1] = off[t] + p.napt[t];
+    // scratch: ori 9np, drostep 3np, ra, offsets, per-block partials (intra, epilogue)
+    size_t nra = 3 * (size_t)off[p.npt];
+    size_t need = 12 * (size_t)np + nra + (size_t)p.npt + 2 * (size_t)c->nblk + 8;
+    double *d = nullptr;
+    POLY_CUDA(c, cudaMalloc(&d, sizeof(double) * need));
+    double *d_ori = d, *d_dro = d_ori + 9 * (size_t)np, *d_ra = d_dro + 3 * (size_t)np;
+    int *d_off = reinterpret_cast<int *>(d_ra + nra);
+    double *d_pi = d_ra + nra + p.npt, *d_pe = d_pi + c->nblk;
+    cudaStream_t S = hc->st;
+    cudaEvent_t e1 = nullptr, e2 = nullptr;
+    int st = MG_OK;
+    auto ok = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == MG_OK) st = poly_fail(c, MG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+        return st == MG_OK;
+    };
+    do {
+        if (!ok(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming), "event") ||
+            !ok(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming), "event") ||
+            !ok(cudaMemcpyAsync(d_ra, ra, sizeof(double) * nra, cudaMemcpyHostToDevice, S), "copy ra") ||
+            !ok(cudaMemcpyAsync(d_off, off.data(), sizeof(int) * p.npt, cudaMemcpyHostToDevice, S), "copy offsets") ||
+            !ok(cudaMemsetAsync(c->d_err, 0, sizeof(int) * 4, S), "clear error"))
+            break;
+        mg_box box;
+        for (int m = 0; m < 3; ++m) {
+            box.len[m] = p.boxlen[m];
+            box.half[m] = 0.5 * p.boxlen[m];
+            box.inv[m] = 1.0 / p.boxlen[m];
+        }
+        PolyArgs a = poly_args(c);
+        a.ro = hc->d_ro;
+        size_t sm = sizeof(double) * (p.nptpt + 1) * kPolyThreads;
+        double ualpha2 = p.ualpha * p.ualpha;
+        double ewaldfac1 = ewald ? (1.0 / (std::sqrt(3.1415926535897932) * p.ualpha)) * 2.0 * ualpha2 : 0.0;
+        for (int step = 0; step < nstep && st == MG_OK; ++step) {
+            k_rigid_move<<<(np + 127) / 128, 128, 0, S>>>(np, c->rig_tstep, box, c->d_rig, hc->d_ro, d_ori, d_dro);
+            k_place_atoms<<<(np + 127) / 128, 128, 0, S>>>(np, c->d_iptpn, c->d_ianpn, c->d_napt, d_off, d_ra,
+                                                         hc->d_ro, d_ori, c->d_r);
+            if (!ok(cudaGetLastError(), "move") || mg_lists_build(hc, false) != MG_OK) {
+                if (st == MG_OK) st = poly_fail(c, MG_ERR_STATE, "centres list: %s", hc->err.c_str());
+                break;
+            }
+            k_twobody_p_list<<<c->nblk_w, kPolyThreads, sm, S>>>(a, hc->d_perm, hc->d_nnb, hc->d_nbr);
+            if (ewald) {
+                k_fold_atoms<<<(3 * na + 255) / 256, 256, 0, S>>>(na, c->d_r, box, ha->d_ro);
+                if (!ok(cudaEventRecord(e1, S), "event") || !ok(cudaStreamWaitEvent(ha->st, e1, 0), "wait"))
+                    break;
+                if (mg_utotal_launch(ha) != MG_OK) {
+                    st = poly_fail(c, MG_ERR_STATE, "atom handle: %s", ha->err.c_str());
+                    break;
+                }
+                if (!ok(cudaEventRecord(e2, ha->st), "event") || !ok(cudaStreamWaitEvent(S, e2, 0), "wait")) break;
+                k_add_scaled<<<(unsigned)((3 * (size_t)na + 255) / 256), 256, 0, S>>>(
+                    3 * (size_t)na, ha->d_forceo, 1.0 / ha->force_fac, c->d_force);
+                PolyArgs ai = a;
+                ai.part = d_pi;
+                k_ewald_intra<<<c->nblk, kPolyThreads, 0, S>>>(ai, c->d_aza, p.ualpha, ualpha2, ewaldfac1,
+                                                              p.epsi_four_pi, 1);
+            }
+            PolyArgs ae = a;
+            ae.part = d_pe;
+            k_poly_epilogue<<<c->nblk, kPolyThreads, 0, S>>>(ae, hc->force_fac, c->d_fo, c->d_to, nullptr);
+            double *io = c->d_rig_io;
+            k_rigid_kick<<<(np + 127) / 128, 128, 0, S>>>(np, c->rig_tstep, c->rig_tvvite, c->rig_nvvite, c->d_rig,
+                                                         c->d_fo, c->d_to, io, io + 3 * np);
+            if (!ok(cudaGetLastError(), "step kernels")) break;
+        }
+        if (st != MG_OK) break;
+        // the last step's state and energies
+        std::vector<double> hp((size_t)c->nblk_w * (p.nptpt + 1)), hi(c->nblk), he(c->nblk),
+            hu(ha ? (size_t)ha->nptpt + 5 : 1);
+        int herr[4];
+        double *io = c->d_rig_io;
+        if (!ok(cudaMemcpyAsync(ro, hc->d_ro, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, S), "ro") ||
+            !ok(cudaMemcpyAsync(ori, d_ori, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost, S), "ori") ||
+            !ok(cudaMemcpyAsync(rod, io, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, S), "rod") ||
+            !ok(cudaMemcpyAsync(angvelo, io + 3 * np, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, S), "angvelo") ||
+            !ok(cudaMemcpyAsync(hp.data(), c->d_part, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, S), "part") ||
+            !ok(cudaMemcpyAsync(hi.data(), d_pi, sizeof(double) * hi.size(), cudaMemcpyDeviceToHost, S), "part") ||
+            !ok(cudaMemcpyAsync(he.data(), d_pe, sizeof(double) * he.size(), cudaMemcpyDeviceToHost, S), "part") ||
+            !ok(cudaMemcpyAsync(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost, S), "error word"))
+            break;
+        if (ewald && !ok(cudaMemcpyAsync(hu.data(), ha->d_uout, sizeof(double) * (ha->nptpt + 5),
+                                         cudaMemcpyDeviceToHost, S), "energies"))
+            break;
+        if (!ok(cudaStreamSynchronize(S), "sync")) break;
+        if (herr[0] == MG_ERR_TABLE_UNDERRUN) {
+            st = poly_fail(c, herr[0], "r2 < r2umin for atoms %d and %d (atom-type pair %d)", herr[1], herr[2], herr[3]);
+            break;
+        }
+        if (herr[0]) {
+            st = poly_fail(c, herr[0], "ibuf > nbuf for atom-type pair %d", herr[1]);
+            break;
+        }
+        int nv = p.nptpt + 1;
+        double utw = 0.0, vir = 0.0, uin = 0.0, vmol = 0.0;
+        for (int k = 0; k < p.nptpt; ++k)
+            for (int b = 0; b < c->nblk_w; ++b) utw += hp[(size_t)b * nv + k];
+        for (int b = 0; b < c->nblk_w; ++b) vir += hp[(size_t)b * nv + p.nptpt];
+        for (int b = 0; b < c->nblk; ++b) vmol += he[b];
+        double urec = 0.0;
+        if (ewald) {
+            for (int b = 0; b < c->nblk; ++b) uin += hi[b];
+            int o = ha->nptpt + 1;   // u_tot, u_rec, u_bond, virial of the atom handle
+            urec = hu[o + 1] + p.epsi_four_pi * uin;
+            vir += hu[o + 3];
+        }
+        uout[0] = utw + urec;     // u%tot
+        uout[1] = utw;            // u%twob(0)
+        uout[2] = urec;           // u%rec (atoms' reciprocal and self terms, molecular self term)
+        uout[3] = vir + vmol;     // virial (with the molecular term)
+    } while (false);
+    if (e1) cudaEventDestroy(e1);
+    if (e2) cudaEventDestroy(e2);
+    cudaFree(d);
+    return st;
 }

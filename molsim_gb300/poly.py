@@ -626,6 +626,40 @@ class PolyEngine:
         out.update(rod=self.rod, angvelo=self.angvelo, drostep=dro.reshape(n, 3).copy())
         return out
 
+    def MDRun(self, nstep=1):
+        """nstep steps of VelVer on the device (mg_poly_md_run): the same
+        steps as VelVer with the centres' list and the atom handle kept on
+        the device and no host arrays between the steps.  The system's ro
+        and ori follow; returns u_tot, u_twob0, u_rec, virial, rod,
+        angvelo of the last step."""
+        from .engine import Engine
+        s = self.s
+        if s.txelec != "charge":
+            raise ValueError("MDRun: charges only (txelec = 'charge')")
+        n = s.np_
+        if getattr(self, "_centres", None) is None:
+            self._centres = Engine(s.centre_system())
+            self._centres.SetPositions(abi.as_f64(s.ro.reshape(-1)))
+            self._centres.NList("write")
+        ha = None
+        if s.ewald != abi.MG_EWALD_NONE:
+            ha = self._atoms_handle()
+            ha.SetPositions(s.atoms_in_box().reshape(-1))
+            ha.NList("write")
+        ra = abi.as_f64(np.concatenate([np.array([x for _, x in t.atoms], dtype=np.float64).reshape(-1)
+                                        for t in s.particle_types]))
+        ro, ori = np.zeros(3 * n), np.zeros(9 * n)
+        rod, w, uo = np.zeros(3 * n), np.zeros(3 * n), np.zeros(4)
+        self._fail(self.lib.mg_poly_md_run(self.h, self._centres.h, ha.h if ha is not None else None, abi.f64(ra),
+                                           int(nstep), abi.f64(ro), abi.f64(ori), abi.f64(rod), abi.f64(w),
+                                           abi.f64(uo)), "poly_md_run")
+        s.ro = ro.reshape(n, 3).copy()
+        s.ori = np.ascontiguousarray(ori.reshape(n, 3, 3).transpose(0, 2, 1))
+        self.rod = rod.reshape(n, 3).copy()
+        self.angvelo = w.reshape(n, 3).copy()
+        return dict(u_tot=float(uo[0]), u_twob0=float(uo[1]), u_rec=float(uo[2]), virial=float(uo[3]),
+                    rod=self.rod, angvelo=self.angvelo)
+
     def RigidState(self):
         """The device's quaternions and quaternion velocities, (np, 4) each."""
         n = self.s.np_
