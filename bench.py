@@ -459,8 +459,10 @@ def run_water(args):
     rigid three-site waters and ions with SPME over the atom charges
     (PolyEngine.UTotal: the atom-pair loop, the atoms' reciprocal sum, the
     molecular self term, particle forces and torques), host arrays in and
-    out every call as the reference's argument-less routines see them; and
-    the atom-pair loop alone.  One JSON line, rank 0."""
+    out every call as the reference's argument-less routines see them; the
+    atom-pair loop alone; and rigid-body MD steps of the same particles,
+    host-driven (PolyEngine.VelVer) and on the device (mg_poly_md_run).  One
+    JSON line, rank 0."""
     import torch
 
     import molsim_gb300
@@ -506,12 +508,37 @@ def run_water(args):
     for _ in range(K):
         e.UTwoBodyPList()
     t_pair_dev = (time.perf_counter() - t0) / K
+    # rigid-body MD (VelVer with quaternions) of the same particles: the
+    # host between the parts of every step, then every step on the device
+    r = s.principal_axes()
+    r.build_table(abi.load_library().mg_pot_twobody_tab)
+    rng = np.random.default_rng(args.seed)
+    massip, momp = r.rigid_props()
+    kt = 8.314472e-3 * 298.0
+    v = rng.standard_normal((r.np_, 3)) * np.sqrt(kt * massip / 0.01)[:, None]
+    w = np.where(momp > 0.0, rng.standard_normal(momp.shape) * np.sqrt(kt / (0.01 * np.maximum(momp, 1e-300))), 0.0)
+    em = PolyEngine(r, maxn)
+    em.RigidSetup(0.0005, v, w, prime=True)
+    Km = max(1, min(args.steps, 50))
+    em.VelVer(2)
+    t0 = time.perf_counter()
+    em.VelVer(Km)
+    t_md_host = (time.perf_counter() - t0) / Km
+    em.MDRun(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    md = em.MDRun(Km)
+    t_md_dev = (time.perf_counter() - t0) / Km
+    em.close()
     print(json.dumps({
         "metric": "polyatomic UTotal calls/s (rigid waters and ions, SPME over atoms), host arrays each call",
         "value": 1.0 / t_tot, "unit": "calls/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
         "ms_per_call": 1e3 * t_tot, "ms_atom_pair_loop": 1e3 * t_pair,
         "device_list": {"ms_per_call": 1e3 * t_tot_dev, "ms_atom_pair_loop": 1e3 * t_pair_dev,
                         "u_tot": out_dev["u_tot"]},
+        "rigid_md": {"steps": Km, "dt_ps": 0.0005, "host_driven_ms_per_step": 1e3 * t_md_host,
+                     "device_ms_per_step": 1e3 * t_md_dev, "device_steps_per_s": 1.0 / t_md_dev,
+                     "u_tot": md["u_tot"]},
         "higher_is_better": True,
         "dtype": "f64", "data": "synthetic (seeded rigid waters and NaCl)",
         "config": {"workload": f"{s.np_} particles, {len(s.iatan())} atoms, L={L} A, r_c={s.rcut} A, "

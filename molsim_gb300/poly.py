@@ -197,8 +197,9 @@ class PolySystem:
     def principal_axes(self):
         """The same particles with each type's atoms in its principal axes
         about its centre of mass (ra, particle.F90:2409-2420), the centres
-        moved to the centres of mass and the orientations composed with the
-        axes, so that every atom stays where it was."""
+        moved to the centres of mass (folded into the box) and the
+        orientations composed with the axes, so that every atom stays where
+        it was, up to a box vector."""
         from dataclasses import replace
         types, com, axes = [], [], []
         for t, pt in enumerate(self.particle_types):
@@ -215,6 +216,12 @@ class PolySystem:
         ti = np.asarray(self.iptpn) - 1
         com, axes = np.array(com), np.array(axes)
         ro = self.ro + np.einsum("nij,nj->ni", self.ori, com[ti])
+        # a centre moved past a face goes back into the box (PBC): its atoms
+        # move by the same box vector
+        L = np.asarray(self.boxlen, dtype=np.float64)
+        t = ro / L
+        a = np.trunc(t) + np.sign(t) * (np.abs(t - np.trunc(t)) >= 0.5)   # ANINT
+        ro = np.where(np.abs(ro) > 0.5 * L, ro - L * a, ro)
         ori = np.einsum("nij,njk->nik", self.ori, axes[ti])
         return replace(self, particle_types=types, ro=np.ascontiguousarray(ro), ori=np.ascontiguousarray(ori),
                        ubuf=self.ubuf, iubuflow=self.iubuflow, r2umin=self.r2umin, keep={})
