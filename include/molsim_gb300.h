@@ -455,6 +455,19 @@ int mg_poly_utwobody_list(mg_poly *c, mg_handle *centres, const double *r, doubl
 int mg_poly_dutwobody_batch(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
                             const int32_t *jpnlist, int32_t ntrial, const int32_t *ip, const double *rotm,
                             const double *rtm, double *du_twob, int32_t *lhsoverlap);
+/* One MC trial that moves nptm polyatomic particles together (DUTwoBody
+ * with UTwoBodyPNew/UTwoBodyPOld, denergy.F90:937-1231, any nptm, with
+ * lptmdutwob for the pairs of moving particles): ipnptm[nptm] the moving
+ * particles (1-based, each once), rotm[3*nptm] their new centres, rtm their
+ * new atoms one particle after another.  Each moving particle pairs with its
+ * list neighbours that stay (nneighpn, jpnlist), and every pair of moving
+ * particles counts once.  Writes du_twob[nptpt+1] (index 0 the total, k the
+ * particle-type pair k; new minus old) and *lhsoverlap (1: an atom pair of
+ * the trial configuration below r2atat or r2umin; du_twob is then zero and
+ * the current configuration is not summed).  One block sums the trial. */
+int mg_poly_dutwobody_multi(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
+                            const int32_t *jpnlist, int32_t nptm, const int32_t *ipnptm, const double *rotm,
+                            const double *rtm, double *du_twob, int32_t *lhsoverlap);
 /* The end of UTotal for polyatomic particles (energy.F90:405-427): from
  * the total atom forces force[3*na] (unscaled), the atom torques
  * torque[3*na] of the dipole electrostatics (NULL when there are none) and

@@ -120,6 +120,7 @@ LIB_ONLY = [
     ("poly_udipole_self", C.c_int, [H, PF64, PF64, C.c_int32, PF64, PF64, PF64, PF64]),
     ("poly_udipole_finish", C.c_int, [H, PF64, PF64, PF64, PF64, PF64, PF64, PF64]),
     ("poly_dutwobody_batch", C.c_int, [H, PF64, PF64, PI32, PI32, C.c_int32, PI32, PF64, PF64, PF64, PI32]),
+    ("poly_dutwobody_multi", C.c_int, [H, PF64, PF64, PI32, PI32, C.c_int32, PI32, PF64, PF64, PF64, PI32]),
     ("poly_rigid_setup", C.c_int, [H, C.c_double, C.c_double, C.c_int32, PF64, PF64, PF64, PF64, PF64, PF64,
                                    PF64, PF64]),
     ("poly_rigid_move", C.c_int, [H, PF64, PF64, PF64]),

@@ -1679,3 +1679,225 @@ extern "C" int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const do
     cudaFree(d);
     return st;
 }
+
+// ---- multi-particle polyatomic trials (UTwoBodyPNew/Old, nptm > 1) ------------
+namespace {
+
+struct MultiArgs {
+    int nptm, nitem_a, npair;
+    const int *ipm;       // moving particles (0-based)
+    const int *atom0;     // first trial atom of each moving particle in rtm
+    const int *item0;     // [nptm + 1] prefix of the moving particles' list lengths
+    const int *moving;    // [np] 1 for a moving particle
+    const double *rotm, *rtm;
+    double *out;          // [2 nptpt + 1]: new sums, old sums (per type pair), the overlap flag
+};
+
+// the atom-pair energy of particles ip (centre ci, atoms ra) and jp (centre
+// cj, atoms rb); 1: a hard core or a pair below its table, -1 past the
+// table; *inr when the centres are within rcut
+__device__ int multi_pair(const PolyArgs &a, int ip, const double *ci, const double *ra, int jp, const double *cj,
+                          const double *rb, double *usum, int *inr) {
+    double sh[3], d[3];
+    for (int m = 0; m < 3; ++m) {
+        d[m] = __dsub_rn(ci[m], cj[m]);
+        sh[m] = fabs(d[m]) > a.half[m] ? copysign(a.len[m], d[m]) : 0.0;
+        d[m] = __dsub_rn(d[m], sh[m]);
+    }
+    *inr = 0;
+    if (mg_r2_exact(d[0], d[1], d[2]) > a.rcut2) return 0;
+    *inr = 1;
+    int ipt = a.iptpn[ip], jpt = a.iptpn[jp];
+    int ialow = a.ianpn[ip] - 1, jalow = a.ianpn[jp] - 1;
+    double s = 0.0;
+    for (int k = 0; k < a.napt[ipt - 1]; ++k) {
+        int iat = a.iatan[ialow + k];
+        for (int l = 0; l < a.napt[jpt - 1]; ++l) {
+            int jat = a.iatan[jalow + l];
+            int iatjat = a.iatat[(jat - 1) * a.nat + (iat - 1)];
+            double dx = __dsub_rn(__dsub_rn(ra[3 * k], rb[3 * l]), sh[0]);
+            double dy = __dsub_rn(__dsub_rn(ra[3 * k + 1], rb[3 * l + 1]), sh[1]);
+            double dz = __dsub_rn(__dsub_rn(ra[3 * k + 2], rb[3 * l + 2]), sh[2]);
+            double ar2 = mg_r2_exact(dx, dy, dz);
+            if (ar2 < a.r2atat[iatjat - 1] || ar2 < a.r2umin[iatjat - 1]) return 1;
+            double u;
+            if (poly_pair_u(a, iatjat, ar2, &u)) return -1;
+            s = __dadd_rn(s, u);
+        }
+    }
+    *usum = s;
+    return 0;
+}
+
+__global__ void __launch_bounds__(256) k_poly_dutwobody_multi(PolyArgs a, MultiArgs m) {
+    __shared__ double red[2 * MG_MAX_NPTPT][8];
+    __shared__ int sbad[8];
+    double an[MG_MAX_NPTPT], ao[MG_MAX_NPTPT];
+#pragma unroll
+    for (int k = 0; k < MG_MAX_NPTPT; ++k) an[k] = ao[k] = 0.0;
+    int bad = 0;
+    const int total = m.nitem_a + m.npair;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int il, jp, jl = -1;
+        if (t < m.nitem_a) {   // a moving particle and a list neighbour that stays
+            il = 0;
+            while (m.item0[il + 1] <= t) ++il;
+            int ip = m.ipm[il];
+            jp = a.jpnlist[(size_t)ip * a.maxnneigh + (t - m.item0[il])] - 1;
+            if (m.moving[jp]) continue;
+        } else {               // two moving particles, il < jl
+            int q = t - m.nitem_a;
+            il = 0;
+            while (q >= m.nptm - 1 - il) { q -= m.nptm - 1 - il; ++il; }
+            jl = il + 1 + q;
+            jp = m.ipm[jl];
+        }
+        int ip = m.ipm[il];
+        int ipt = a.iptpn[ip], jpt = a.iptpn[jp];
+        int iptjpt = a.iptpt[(jpt - 1) * a.npt + (ipt - 1)];
+        for (int pass = 0; pass < 2; ++pass) {   // 0: trial, 1: current
+            const double *ci = pass ? a.ro + 3 * ip : m.rotm + 3 * il;
+            const double *ra = pass ? a.r + 3 * (size_t)(a.ianpn[ip] - 1) : m.rtm + 3 * (size_t)m.atom0[il];
+            const double *cj, *rb;
+            if (jl >= 0 && pass == 0) {
+                cj = m.rotm + 3 * jl;
+                rb = m.rtm + 3 * (size_t)m.atom0[jl];
+            } else {
+                cj = a.ro + 3 * jp;
+                rb = a.r + 3 * (size_t)(a.ianpn[jp] - 1);
+            }
+            double u = 0.0;
+            int inr, st = multi_pair(a, ip, ci, ra, jp, cj, rb, &u, &inr);
+            if (st > 0) {
+                if (pass == 0) bad = 1;
+                else mg_dev_error(a.err, MG_ERR_TABLE_UNDERRUN, ip + 1, jp + 1, iptjpt);
+                continue;
+            }
+            if (st < 0) {
+                mg_dev_error(a.err, MG_ERR_IBUF, iptjpt, ip + 1, jp + 1);
+                continue;
+            }
+            if (!inr) continue;
+#pragma unroll
+            for (int k = 0; k < MG_MAX_NPTPT; ++k)
+                if (k == iptjpt - 1) {
+                    if (pass == 0) an[k] = __dadd_rn(an[k], u);
+                    else ao[k] = __dadd_rn(ao[k], u);
+                }
+        }
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < MG_MAX_NPTPT; ++k) {
+        double x = an[k], y = ao[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, o);
+            y += __shfl_down_sync(0xffffffffu, y, o);
+        }
+        if (lane == 0 && k < a.nptpt) { red[k][w] = x; red[MG_MAX_NPTPT + k][w] = y; }
+    }
+    for (int o = 16; o > 0; o >>= 1) bad |= __shfl_down_sync(0xffffffffu, bad, o);
+    if (lane == 0) sbad[w] = bad;
+    __syncthreads();
+    if (threadIdx.x < a.nptpt) {
+        double x = 0.0, y = 0.0;
+        for (int k = 0; k < nw; ++k) { x += red[threadIdx.x][k]; y += red[MG_MAX_NPTPT + threadIdx.x][k]; }
+        m.out[threadIdx.x] = x;
+        m.out[a.nptpt + threadIdx.x] = y;
+    }
+    if (threadIdx.x == 0) {
+        int b = 0;
+        for (int k = 0; k < nw; ++k) b |= sbad[k];
+        m.out[2 * a.nptpt] = b;
+    }
+}
+
+}  // namespace
+
+extern "C" int mg_poly_dutwobody_multi(mg_poly *c, const double *ro, const double *r, const int32_t *nneighpn,
+                                       const int32_t *jpnlist, int32_t nptm, const int32_t *ipnptm,
+                                       const double *rotm, const double *rtm, double *du_twob, int32_t *lhsoverlap) {
+    if (!c || !ro || !r || !nneighpn || !jpnlist || nptm < 1 || !ipnptm || !rotm || !rtm || !du_twob || !lhsoverlap)
+        return MG_ERR_ARG;
+    if (!c->d_r2atat) return poly_fail(c, MG_ERR_STATE, "mg_poly_params.r2atat was not given");
+    const mg_poly_params &p = c->p;
+    const int np = p.np, nptpt = p.nptpt;
+    if (nptpt > MG_MAX_NPTPT) return poly_fail(c, MG_ERR_UNSUPPORTED, "%d particle-type pairs", nptpt);
+    std::vector<int> ipm(nptm), atom0(nptm), item0(nptm + 1, 0), moving(np, 0);
+    int tot = 0;
+    for (int k = 0; k < nptm; ++k) {
+        int ip = ipnptm[k];
+        if (ip < 1 || ip > np) return poly_fail(c, MG_ERR_ARG, "ipnptm(%d) = %d", k + 1, ip);
+        if (moving[ip - 1]) return poly_fail(c, MG_ERR_ARG, "particle %d moves twice", ip);
+        moving[ip - 1] = 1;
+        ipm[k] = ip - 1;
+        atom0[k] = tot;
+        tot += p.napt[p.iptpn[ip - 1] - 1];
+        if (nneighpn[ip - 1] < 0 || nneighpn[ip - 1] > c->maxnneigh)
+            return poly_fail(c, MG_ERR_NEIGH_OVERFLOW, "nneighpn(%d) = %d > maxnneigh %d", ip, nneighpn[ip - 1],
+                             c->maxnneigh);
+        item0[k + 1] = item0[k] + nneighpn[ip - 1];
+    }
+    // scratch: ints (ipm, atom0, item0, moving), doubles (rotm, rtm, out)
+    size_t ni = 3 * (size_t)nptm + 1 + np, nd = 3 * (size_t)nptm + 3 * (size_t)tot + 2 * (size_t)nptpt + 1;
+    void *d = nullptr;
+    POLY_CUDA(c, cudaMalloc(&d, sizeof(double) * nd + sizeof(int) * ni));
+    double *d_rotm = (double *)d, *d_rtm = d_rotm + 3 * nptm, *d_out = d_rtm + 3 * (size_t)tot;
+    int *d_ipm = (int *)(d_out + 2 * nptpt + 1), *d_atom0 = d_ipm + nptm, *d_item0 = d_atom0 + nptm,
+        *d_moving = d_item0 + nptm + 1;
+    int st = MG_OK;
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        if (st == MG_OK && cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+            st = poly_fail(c, MG_ERR_CUDA, "mg_poly_dutwobody_multi: copy failed");
+    };
+    cp(c->d_ro, ro, sizeof(double) * 3 * np);
+    cp(c->d_r, r, sizeof(double) * 3 * p.na);
+    cp(c->d_nneigh, nneighpn, sizeof(int) * np);
+    cp(c->d_jpnlist, jpnlist, sizeof(int) * (size_t)c->maxnneigh * np);
+    cp(d_rotm, rotm, sizeof(double) * 3 * nptm);
+    cp(d_rtm, rtm, sizeof(double) * 3 * tot);
+    cp(d_ipm, ipm.data(), sizeof(int) * nptm);
+    cp(d_atom0, atom0.data(), sizeof(int) * nptm);
+    cp(d_item0, item0.data(), sizeof(int) * (nptm + 1));
+    cp(d_moving, moving.data(), sizeof(int) * np);
+    std::vector<double> out(2 * (size_t)nptpt + 1);
+    int herr[4] = {0, 0, 0, 0};
+    if (st == MG_OK) {
+        cudaMemset(c->d_err, 0, sizeof(int) * 4);
+        PolyArgs a = poly_args(c);
+        MultiArgs m;
+        m.nptm = nptm;
+        m.nitem_a = item0[nptm];
+        m.npair = nptm * (nptm - 1) / 2;
+        m.ipm = d_ipm;
+        m.atom0 = d_atom0;
+        m.item0 = d_item0;
+        m.moving = d_moving;
+        m.rotm = d_rotm;
+        m.rtm = d_rtm;
+        m.out = d_out;
+        k_poly_dutwobody_multi<<<1, 256>>>(a, m);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(out.data(), d_out, sizeof(double) * out.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = poly_fail(c, MG_ERR_CUDA, "mg_poly_dutwobody_multi: kernel failed");
+    }
+    cudaFree(d);
+    if (st != MG_OK) return st;
+    for (int k = 0; k <= nptpt; ++k) du_twob[k] = 0.0;
+    // a hard core in the trial configuration rejects the move before the
+    // current configuration is summed, as UTwoBodyPNew returns before
+    // UTwoBodyPOld runs
+    *lhsoverlap = out[2 * nptpt] != 0.0 ? 1 : 0;
+    if (*lhsoverlap) return MG_OK;
+    if (herr[0] == MG_ERR_TABLE_UNDERRUN)
+        return poly_fail(c, herr[0], "current state: r2 < r2umin for particles %d and %d", herr[1], herr[2]);
+    if (herr[0]) return poly_fail(c, herr[0], "ibuf > nbuf for particle-type pair %d", herr[1]);
+    double s = 0.0;
+    for (int k = 0; k < nptpt; ++k) {
+        du_twob[k + 1] = out[k] - out[nptpt + k];
+        s += du_twob[k + 1];
+    }
+    du_twob[0] = s;
+    return MG_OK;
+}

@@ -449,6 +449,28 @@ class PolyEngine:
             raise MolsimError(st, f"poly_dutwobody_batch: {buf.value.decode(errors='replace')}")
         return du, ovl.astype(bool)
 
+    def DUTwoBodyMulti(self, nneighpn, jpnlist, ips, rotm, rtm, r=None):
+        """One trial moving the particles ips (1-based) together to centres
+        rotm with atoms rtm (the moving particles' atoms one after another):
+        DUTwoBody's UTwoBodyPNew/UTwoBodyPOld for nptm = len(ips).  Returns
+        du_twob per particle-type pair (index 0 the total; new minus old) and
+        the hard-core overlap flag."""
+        s = self.s
+        r = s.atom_positions() if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
+        ips = abi.as_i32(np.atleast_1d(ips))
+        du = np.zeros(self.p.nptpt + 1)
+        ovl = np.zeros(1, dtype=np.int32)
+        st = self.lib.mg_poly_dutwobody_multi(
+            self.h, abi.f64(abi.as_f64(s.ro.reshape(-1))), abi.f64(r.reshape(-1)), abi.i32(abi.as_i32(nneighpn)),
+            abi.i32(abi.as_i32(np.asarray(jpnlist).reshape(-1))), len(ips), abi.i32(ips),
+            abi.f64(abi.as_f64(np.asarray(rotm).reshape(-1))), abi.f64(abi.as_f64(np.asarray(rtm).reshape(-1))),
+            abi.f64(du), abi.i32(ovl))
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.lib.mg_poly_last_error(self.h, buf, 512)
+            raise MolsimError(st, f"poly_dutwobody_multi: {buf.value.decode(errors='replace')}")
+        return du, bool(ovl[0])
+
     def Epilogue(self, force, r=None, torque=None):
         """UTotal's end (energy.F90:405-427): particle forces and torques
         (scaled by force_fac) from the atom forces and, with dipoles, the

@@ -39,6 +39,10 @@ def oracle():
         lib.orc_poly_dutwobody.restype = C.c_int
         lib.orc_poly_dutwobody.argtypes = [C.POINTER(abi.MgPolyParams), C.c_int32, abi.PF64, abi.PF64, abi.PI32,
                                            abi.PI32, C.c_int32, abi.PF64, abi.PF64, abi.PF64, abi.PI32]
+        lib.orc_poly_dutwobody_multi.restype = C.c_int
+        lib.orc_poly_dutwobody_multi.argtypes = [C.POINTER(abi.MgPolyParams), C.c_int32, abi.PF64, abi.PF64,
+                                                 abi.PI32, abi.PI32, C.c_int32, abi.PI32, abi.PF64, abi.PF64,
+                                                 abi.PF64, abi.PI32]
         lib.orc_poly_epilogue.restype = C.c_int
         lib.orc_poly_epilogue.argtypes = [C.POINTER(abi.MgPolyParams), abi.PF64, abi.PF64, abi.PF64, abi.PF64,
                                           C.c_double,

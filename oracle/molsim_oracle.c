@@ -1974,6 +1974,127 @@ int orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double 
     return 0;
 }
 
+/* the atom-pair energy of two particles: centres ci, cj, atoms ra (of ip's
+   type, first atom ialow) and rb (of jp's type, first atom jalow); returns
+   1 on a hard core or a pair below its table, -1 past the table, and sets
+   *inr when the centres are within rcut */
+static int poly_pair_sum2(const mg_poly_params *p, int ipt, int ialow, const double *ci, const double *ra,
+                          int jpt, int jalow, const double *cj, const double *rb, double *usum_out, int *inr) {
+    double d[3], sh[3];
+    *inr = 0;
+    for (int m = 0; m < 3; ++m) {
+        d[m] = ci[m] - cj[m];
+        sh[m] = Zero;
+        if (fabs(d[m]) > p->boxlen[m] / Two) sh[m] = fsign(p->boxlen[m], d[m]);
+        d[m] = d[m] - sh[m];
+    }
+    double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (r2 > p->rcut * p->rcut) return 0;
+    *inr = 1;
+    double usum = Zero;
+    for (int k = 0; k < p->napt[ipt - 1]; ++k) {
+        int iat = p->iatan[ialow - 1 + k];
+        for (int l = 0; l < p->napt[jpt - 1]; ++l) {
+            int jat = p->iatan[jalow - 1 + l];
+            int iatjat = p->iatat[(jat - 1) * p->nat + iat - 1];
+            double dx = ra[3 * k] - rb[3 * l] - sh[0];
+            double dy = ra[3 * k + 1] - rb[3 * l + 1] - sh[1];
+            double dz = ra[3 * k + 2] - rb[3 * l + 2] - sh[2];
+            double ar2 = dx * dx + dy * dy + dz * dz;
+            if (ar2 < p->r2atat[iatjat - 1]) return 1;
+            if (ar2 < p->r2umin[iatjat - 1]) return 1;
+            int ibuf = p->iubuflow[iatjat - 1];
+            for (;;) {
+                if (ar2 >= p->ubuf[ibuf - 1]) break;
+                ibuf = ibuf + 12;
+                if (ibuf > p->nbuf) return -1;
+            }
+            const double *u = &p->ubuf[ibuf - 1];
+            double dd = ar2 - u[0];
+            usum = usum + u[1] + dd * (u[2] + dd * (u[3] + dd * (u[4] + dd * (u[5] + dd * u[6]))));
+        }
+    }
+    *usum_out = usum;
+    return 0;
+}
+
+/* UTwoBodyPNew and UTwoBodyPOld (denergy.F90:937-1231) for nptm moving
+   particles ipnptm (1-based) with new centres rotm(3,nptm) and new atoms
+   rtm (the moving particles' atoms one after another): each moving
+   particle with its list neighbours that do not move, then (lptmdutwob)
+   every pair of moving particles once, in the order the reference loops.
+   du_twob[nptpt+1] = new - old; *lhsoverlap = 1 on a hard core (or a pair
+   below its table) in the new configuration */
+int orc_poly_dutwobody_multi(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                             const int32_t *nneighpn, const int32_t *jpnlist, int32_t nptm, const int32_t *ipnptm,
+                             const double *rotm, const double *rtm, double *du_twob, int32_t *lhsoverlap) {
+    int nptpt = p->nptpt;
+    double acc[2][64];
+    if (nptpt + 1 > 64 || nptm < 1) return MG_ERR_ARG;
+    char *lptm = (char *)calloc((size_t)p->np + 1, 1);
+    int *atom0 = (int *)malloc(sizeof(int) * (size_t)nptm);
+    if (!lptm || !atom0) { free(lptm); free(atom0); return MG_ERR_ALLOC; }
+    int tot = 0;
+    for (int k = 0; k < nptm; ++k) {
+        lptm[ipnptm[k]] = 1;
+        atom0[k] = tot;
+        tot += p->napt[p->iptpn[ipnptm[k] - 1] - 1];
+    }
+    for (int k = 0; k <= nptpt; ++k) acc[0][k] = acc[1][k] = du_twob[k] = Zero;
+    *lhsoverlap = 1;
+    int st = 0;
+    for (int pass = 0; pass < 2 && st == 0; ++pass) {   /* new, then old */
+        double *a = acc[pass];
+        for (int il = 0; il < nptm && st == 0; ++il) {
+            int ip = ipnptm[il], ipt = p->iptpn[ip - 1], ialow = p->ianpn[ip - 1];
+            const double *ci = pass ? &ro[3 * (ip - 1)] : &rotm[3 * il];
+            const double *ra = pass ? &r[3 * (ialow - 1)] : &rtm[3 * atom0[il]];
+            for (int jploc = 1; jploc <= nneighpn[ip - 1]; ++jploc) {
+                int jp = jpnlist[(size_t)(ip - 1) * maxnneigh + jploc - 1];
+                if (lptm[jp]) continue;
+                int jpt = p->iptpn[jp - 1], jalow = p->ianpn[jp - 1];
+                double usum;
+                int inr, q = poly_pair_sum2(p, ipt, ialow, ci, ra, jpt, jalow, &ro[3 * (jp - 1)],
+                                            &r[3 * (jalow - 1)], &usum, &inr);
+                if (q < 0) { st = MG_ERR_IBUF; break; }
+                if (q > 0) { st = pass == 0 ? 1 : MG_ERR_TABLE_UNDERRUN; break; }
+                if (!inr) continue;
+                int iptjpt = p->iptpt[(jpt - 1) * p->npt + ipt - 1];
+                a[iptjpt] = a[iptjpt] + usum;
+            }
+        }
+        for (int il = 0; il < nptm && st == 0; ++il) {   /* both displaced */
+            int ip = ipnptm[il], ipt = p->iptpn[ip - 1], ialow = p->ianpn[ip - 1];
+            const double *ci = pass ? &ro[3 * (ip - 1)] : &rotm[3 * il];
+            const double *ra = pass ? &r[3 * (ialow - 1)] : &rtm[3 * atom0[il]];
+            for (int jl = il + 1; jl < nptm; ++jl) {
+                int jp = ipnptm[jl], jpt = p->iptpn[jp - 1], jalow = p->ianpn[jp - 1];
+                const double *cj = pass ? &ro[3 * (jp - 1)] : &rotm[3 * jl];
+                const double *rb = pass ? &r[3 * (jalow - 1)] : &rtm[3 * atom0[jl]];
+                double usum;
+                int inr, q = poly_pair_sum2(p, ipt, ialow, ci, ra, jpt, jalow, cj, rb, &usum, &inr);
+                if (q < 0) { st = MG_ERR_IBUF; break; }
+                if (q > 0) { st = pass == 0 ? 1 : MG_ERR_TABLE_UNDERRUN; break; }
+                if (!inr) continue;
+                int iptjpt = p->iptpt[(jpt - 1) * p->npt + ipt - 1];
+                a[iptjpt] = a[iptjpt] + usum;
+            }
+        }
+    }
+    free(lptm);
+    free(atom0);
+    if (st == 1) return 0;   /* hard-core overlap in the new configuration: rejected */
+    if (st) return st;
+    *lhsoverlap = 0;
+    double sum = Zero;
+    for (int k = 1; k <= nptpt; ++k) {
+        du_twob[k] = acc[0][k] - acc[1][k];
+        sum = sum + du_twob[k];
+    }
+    du_twob[0] = sum;
+    return 0;
+}
+
 /* UTotal, energy.F90:405-427: atoms in order, each adding to its particle
    (ipnan) the scaled force, the torque of the scaled force about the
    particle centre, and (r_a - ro_p) . f_a (unscaled) to virmolecule */

@@ -81,6 +81,12 @@ int  orc_poly_utwobody(const mg_poly_params *p, int32_t maxnneigh, const double 
 int  orc_poly_dutwobody(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
                         const int32_t *nneighpn, const int32_t *jpnlist, int32_t ip, const double *rotm,
                         const double *rtm, double *du_twob, int32_t *lhsoverlap);
+/* UTwoBodyPNew/Old for nptm moving particles with the pairs among them
+   (denergy.F90:937-1231), arguments as mg_poly_dutwobody_multi's */
+int  orc_poly_dutwobody_multi(const mg_poly_params *p, int32_t maxnneigh, const double *ro, const double *r,
+                              const int32_t *nneighpn, const int32_t *jpnlist, int32_t nptm,
+                              const int32_t *ipnptm, const double *rotm, const double *rtm, double *du_twob,
+                              int32_t *lhsoverlap);
 /* the end of UTotal for polyatomic particles (energy.F90:405-427),
    arguments as mg_poly_epilogue's */
 int  orc_poly_epilogue(const mg_poly_params *p, const double *ro, const double *r, const double *force,

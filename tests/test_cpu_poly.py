@@ -176,3 +176,90 @@ def test_trial_differences_match_full_energies(water, orc):
         assert abs(du[0] - (u1 - u0)) <= 1e-9 * abs(u0), (ip, du[0], u1 - u0)
         nchecked += 1
     assert nchecked >= 8
+
+
+def multi_trial(s, rng, nn, jl, nptm, step=0.6, angle=0.4):
+    """One trial moving nptm particles together: a random particle and up to
+    nptm - 1 of its list neighbours, each displaced by up to step and turned
+    by up to angle radians.  Returns ips (1-based), centres, atoms."""
+    from molsim_gb300.mc import axis_angle_matrix
+    L = s.boxlen[0]
+    ip = int(rng.integers(s.np_)) + 1
+    neigh = [int(j) for j in jl[ip - 1, :nn[ip - 1]]]
+    rng.shuffle(neigh)
+    ips = np.array([ip] + neigh[:nptm - 1], dtype=np.int32)
+    rotm = np.empty((len(ips), 3))
+    atoms = []
+    for t, jp in enumerate(ips):
+        c = s.ro[jp - 1] + rng.uniform(-step, step, 3)
+        c -= L * np.round(c / L)
+        rotm[t] = c
+        R = axis_angle_matrix(rng.normal(size=3), rng.uniform(-angle, angle)) @ s.ori[jp - 1]
+        loc = np.array([x for _, x in s.particle_types[s.iptpn[jp - 1] - 1].atoms])
+        atoms.append(c + loc @ R.T)
+    return ips, rotm, np.concatenate(atoms)
+
+
+def oracle_multi(orc, s, nn, jl, maxn, ips, rotm, atoms):
+    p = s.params()
+    du = np.zeros(p.nptpt + 1)
+    ovl = np.zeros(1, dtype=np.int32)
+    st = orc.orc_poly_dutwobody_multi(C.byref(p), maxn, abi.f64(abi.as_f64(s.ro.reshape(-1))),
+                                      abi.f64(np.ascontiguousarray(s.atom_positions().reshape(-1))),
+                                      abi.i32(abi.as_i32(nn)), abi.i32(abi.as_i32(jl.reshape(-1))), len(ips),
+                                      abi.i32(abi.as_i32(ips)), abi.f64(abi.as_f64(rotm.reshape(-1))),
+                                      abi.f64(abi.as_f64(atoms.reshape(-1))), abi.f64(du), abi.i32(ovl))
+    assert st == 0, abi.STATUS.get(st, st)
+    return du, bool(ovl[0])
+
+
+def test_multi_trial_of_one_particle_is_the_single_trial(water, orc):
+    s = water
+    s.lmc = 1
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0, full=True)
+    rng = np.random.default_rng(6)
+    ips, rotm, atoms = poly_trials(s, rng, 16)
+    for ip, c, a in zip(ips, rotm, atoms):
+        d1, o1 = oracle_trial(orc, s, nn, jl, maxn, ip, c, a)
+        dm, om = oracle_multi(orc, s, nn, jl, maxn, np.array([ip]), c.reshape(1, 3), a)
+        assert o1 == om
+        if not o1:
+            assert np.abs(dm - d1).max() <= 1e-12 * np.abs(d1).max() + 1e-12
+
+
+@pytest.mark.parametrize("nptm", [2, 3, 5])
+def test_multi_trial_is_the_full_energy_difference(nptm, water, orc):
+    """du%twob per particle-type pair of a trial moving nptm neighbouring
+    particles (the moving pairs counted once, at their new separations) is
+    UTwoBodyP of the moved configuration minus that of the current one."""
+    s = water
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0, full=True)
+    hn, hl, hmax = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0)
+    u0 = oracle_poly(orc, s, hn, hl, hmax)["u_twob"]
+    s.lmc = 1
+    rng = np.random.default_rng(40 + nptm)
+    nchecked = 0
+    for _ in range(10):
+        ips, rotm, atoms = multi_trial(s, rng, nn, jl, nptm)
+        du, ovl = oracle_multi(orc, s, nn, jl, maxn, ips, rotm, atoms)
+        if ovl:
+            continue
+        r = s.atom_positions()
+        ro = s.ro.copy()
+        k = 0
+        for t, ip in enumerate(ips):
+            a0 = int(s.ianpn()[ip - 1]) - 1
+            na = len(s.particle_types[s.iptpn[ip - 1] - 1].atoms)
+            r[a0:a0 + na] = atoms[k:k + na]
+            k += na
+            ro[ip - 1] = rotm[t]
+        keep = s.ro
+        s.ro = ro
+        try:
+            u1 = oracle_poly(orc, s, hn, hl, hmax, r)["u_twob"]
+        finally:
+            s.ro = keep
+        assert np.abs(du - (u1 - u0)).max() <= 1e-9 * abs(u0[0]), (ips, du, u1 - u0)
+        nchecked += 1
+    s.lmc = 0
+    assert nchecked >= 5

@@ -185,3 +185,47 @@ def test_poly_device_list_needs_the_pair_cutoff(orc, gpu_lib):
     assert abi.STATUS[st] == "MG_ERR_STATE"
     for x in (short, tiny, e):
         x.close()
+
+
+@pytest.mark.parametrize("nptm", [1, 2, 3, 6])
+def test_poly_multi_trial_matches_oracle(nptm, orc, gpu_lib):
+    """Trials moving nptm neighbouring waters and ions together (one block
+    per trial): the oracle's overlap flag, and du%twob per particle-type pair
+    within 1e-10 of the two-body energy; nptm = 1 also gives the single-trial
+    kernel's du%twob."""
+    from tests.test_cpu_poly import multi_trial, oracle_multi
+    s = configs.water_ions(seed=16, nwater=200, nsalt=12, L=22.0)
+    s.lmc = 1
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0, full=True)
+    u0 = abs(oracle_poly(orc, s, nn, jl, maxn, lmc=1)["u_twob"][0])
+    rng = np.random.default_rng(70 + nptm)
+    e = PolyEngine(s, maxn)
+    n_ok = 0
+    for _ in range(24):
+        ips, rotm, atoms = multi_trial(s, rng, nn, jl, nptm, step=0.5, angle=0.5)
+        r_du, r_ovl = oracle_multi(orc, s, nn, jl, maxn, ips, rotm, atoms)
+        du, ovl = e.DUTwoBodyMulti(nn, jl, ips, rotm, atoms)
+        assert ovl == r_ovl
+        if r_ovl:
+            continue
+        assert np.abs(du - r_du).max() <= 1e-10 * u0, (ips, du, r_du)
+        if nptm == 1:
+            db, ob = e.DUTwoBodyBatch(nn, jl, ips, rotm, atoms)
+            assert not ob[0] and abs(db[0] - du[0]) <= 1e-10 * u0
+        n_ok += 1
+    assert n_ok >= 12
+    e.close()
+
+
+def test_poly_multi_trial_refuses_a_repeated_particle(orc, gpu_lib):
+    s = configs.water_ions(seed=17, nwater=60, nsalt=4, L=14.0)
+    s.lmc = 1
+    s.build_table(orc.orc_pot_twobody_tab)
+    nn, jl, maxn = centre_lists(s.ro, s.boxlen[0], s.rcut + 2.0, full=True)
+    e = PolyEngine(s, maxn)
+    a = s.atom_positions()[:3]
+    with pytest.raises(MolsimError) as ex:
+        e.DUTwoBodyMulti(nn, jl, [1, 1], np.vstack([s.ro[0], s.ro[0]]), np.vstack([a, a]))
+    assert abi.STATUS[ex.value.status] == "MG_ERR_ARG"
+    e.close()
