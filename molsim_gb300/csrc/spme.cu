@@ -457,6 +457,9 @@ __device__ __forceinline__ void bspline_o(T x, T *v, T *dv) {
 
 struct SplineArgs {
     const double *ro, *az;
+    // records in the cell order of the last list build: record i is the
+    // particle perm[i] (nullptr: record p is particle p)
+    const int *perm;
     int np, order, n, n_log;
     double dkdr[3];
     // brick sort, first pass: brick of each particle and its rank among the
@@ -475,19 +478,19 @@ struct SplineArgs {
     double fac;
 };
 
-// The spline record of a particle: a head of four values (the stamp's
+// The spline record of a particle: a head of two values (the stamp's
 // upper corner, 10 bits per axis, stored in the bits of the first value;
-// the charge; two unused), then order values each of the B-spline values
-// along x and y, their derivatives along x and y, the values along z and
-// the derivatives along z, padded to a multiple of four values so that
-// records start on 16-byte boundaries.  The spreads read the head and the x
-// and y values as one block (plus the z values), the gather the head, the
-// x and y values and derivatives (plus the z pair of each plane).
-constexpr int kRecHead = 4;
+// the charge), then order values each of the B-spline values along z, x
+// and y, and of their derivatives along x, y and z, padded to a multiple of
+// four values so that records start on 16-byte boundaries.  The spreads
+// read the head and the values (the first SB values) as one block, the
+// gather the values and derivatives.
+constexpr int kRecHead = 2;
 __host__ __device__ constexpr int spl_rec(int order) { return (kRecHead + 6 * order + 3) & ~3; }
 template <int ORDER> struct RecIx {
-    static constexpr int VX = kRecHead, VY = kRecHead + ORDER, DX = kRecHead + 2 * ORDER,
-                         DY = kRecHead + 3 * ORDER, VZ = kRecHead + 4 * ORDER, DZ = kRecHead + 5 * ORDER;
+    static constexpr int VZ = kRecHead, VX = kRecHead + ORDER, VY = kRecHead + 2 * ORDER,
+                         DX = kRecHead + 3 * ORDER, DY = kRecHead + 4 * ORDER, DZ = kRecHead + 5 * ORDER,
+                         SB = kRecHead + 3 * ORDER;
 };
 
 template <typename T> __device__ __forceinline__ T rec_put_corner(int c);
@@ -539,15 +542,16 @@ template <typename T, int N> __device__ __forceinline__ void load_rec(const T *_
 template <typename T, int ORDER>
 __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restrict__ w) {
     mg_pdl_begin();
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool valid = p < a.np;
-    if (!valid) p = a.np - 1;   // a tail lane recomputes the last particle and stores nothing
+    int i = blockIdx.x * blockDim.x + threadIdx.x;   // the record
+    bool valid = i < a.np;
+    if (!valid) i = a.np - 1;   // a tail lane recomputes the last record and stores nothing
+    const int p = a.perm ? a.perm[i] : i;
     int c[3];
     constexpr int S = spl_rec(ORDER);
+    typedef RecIx<ORDER> RI;
     T r[S];
 #pragma unroll
     for (int k = kRecHead + 6 * ORDER; k < S; ++k) r[k] = (T)0;
-    r[2] = r[3] = (T)0;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         double pos = a.dkdr[m] * a.ro[3 * p + m];
@@ -556,10 +560,12 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
         c[m] = mm < 0 ? mm + a.n : mm;
         T v[ORDER], d[ORDER];
         bspline_o<T, ORDER>((T)(pos - fl), v, d);
+        const int vo = m == 0 ? RI::VX : m == 1 ? RI::VY : RI::VZ;
+        const int dof = m == 0 ? RI::DX : m == 1 ? RI::DY : RI::DZ;
 #pragma unroll
-        for (int i = 0; i < ORDER; ++i) {
-            r[(m < 2 ? kRecHead + m * ORDER : RecIx<ORDER>::VZ) + i] = v[i];
-            r[(m < 2 ? RecIx<ORDER>::DX + m * ORDER : RecIx<ORDER>::DZ) + i] = d[i];
+        for (int k = 0; k < ORDER; ++k) {
+            r[vo + k] = v[k];
+            r[dof + k] = d[k];
         }
     }
     r[0] = rec_put_corner<T>(c[0] | (c[1] << 10) | (c[2] << 20));
@@ -573,11 +579,11 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
         float4 *sw = st[threadIdx.x >> 5];
         store_rec<T, S>(reinterpret_cast<T *>(sw) + lane * S, r);
         __syncwarp();
-        int p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31), nv = min(32, a.np - p0);   // p is clamped in the tail
-        float4 *dst = reinterpret_cast<float4 *>(w + (size_t)p0 * S);
+        int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31), nv = min(32, a.np - i0);   // i is clamped in the tail
+        float4 *dst = reinterpret_cast<float4 *>(w + (size_t)i0 * S);
         for (int k = lane; k < nv * S / 4; k += 32) dst[k] = sw[k];
     } else if (valid) {
-        store_rec<T, S>(w + (size_t)p * S, r);
+        store_rec<T, S>(w + (size_t)i * S, r);
     }
     if (a.plane) {
         // sort by the corner's z plane (at most 128 planes): the block's
@@ -590,9 +596,9 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
         for (int k = threadIdx.x; k < a.n; k += blockDim.x)
             if (hcnt[k]) hbase[k] = atomicAdd(&a.count[k], hcnt[k]);
         __syncthreads();
-        if (valid) {
-            a.brick[p] = c[2];
-            a.rank[p] = hbase[c[2]] + lr;
+        if (valid) {   // of the record
+            a.brick[i] = c[2];
+            a.rank[i] = hbase[c[2]] + lr;
         }
         return;
     }
@@ -600,14 +606,14 @@ __global__ void __launch_bounds__(256) k_spline_prepare(SplineArgs a, T *__restr
     int id = ((((c[2] >> a.lB) << a.lnb) + (c[1] >> a.lB)) << a.lnb) + (c[0] >> a.lB);
     unsigned vm = __ballot_sync(0xffffffffu, valid);
     if (!valid) return;
-    a.brick[p] = id;
+    a.brick[i] = id;
     // rank among the brick's particles: one atomic per brick and warp (chain
     // beads, numbered along the chain, share bricks within a warp)
     unsigned peers = __match_any_sync(vm, id);
     int leader = __ffs(peers) - 1, base = 0;
     if (lane == leader) base = atomicAdd(&a.count[id], __popc(peers));
     base = __shfl_sync(peers, base, leader);
-    a.rank[p] = base + __popc(peers & ((1u << lane) - 1u));
+    a.rank[i] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // ---- brick-sorted spread -------------------------------------------------------
@@ -689,29 +695,24 @@ __global__ void k_brick_scatter(int np, BrickArgs b) {
     if (p < np) b.perm[b.start[b.brick[p]] + b.rank[p]] = p;
 }
 
-// The spread record of a particle in plane order: the head (corner,
-// charge), then the x, y and z B-spline values, padded to a multiple of four
-template <int ORDER> __host__ __device__ constexpr int spread_rec() { return (kRecHead + 3 * ORDER + 3) & ~3; }
+// The spread record of a particle in plane order: the first SB values of
+// its spline record (head, z, x and y values), padded to a multiple of four
+template <int ORDER> __host__ __device__ constexpr int spread_rec() { return (RecIx<ORDER>::SB + 3) & ~3; }
 
-// plane sort, second pass: each particle's spread record to its place in
-// the plane order
+// plane sort, second pass: each spline record's spread part to its place
+// in the plane order
 template <int ORDER>
 __global__ void k_plane_scatter(int np, BrickArgs b, const float *__restrict__ w, float *__restrict__ ws) {
     mg_pdl_begin();
     typedef RecIx<ORDER> RI;
     constexpr int SR = spread_rec<ORDER>();
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
-    int dst = b.start[b.brick[p]] + b.rank[p];
-    const float *src = w + (size_t)p * spl_rec(ORDER);
-    float hv[kRecHead + 2 * ORDER], r[SR];
-    load_rec<float, kRecHead + 2 * ORDER>(src, hv);   // head, x and y values
+    int i = blockIdx.x * blockDim.x + threadIdx.x;   // the record
+    if (i >= np) return;
+    int dst = b.start[b.brick[i]] + b.rank[i];
+    float v[RI::SB], r[SR];
+    load_rec<float, RI::SB>(w + (size_t)i * spl_rec(ORDER), v);
 #pragma unroll
-    for (int i = 0; i < kRecHead + 2 * ORDER; ++i) r[i] = hv[i];
-#pragma unroll
-    for (int i = 0; i < ORDER; ++i) r[kRecHead + 2 * ORDER + i] = src[RI::VZ + i];
-#pragma unroll
-    for (int i = kRecHead + 3 * ORDER; i < SR; ++i) r[i] = 0.f;
+    for (int k = 0; k < SR; ++k) r[k] = k < RI::SB ? v[k] : 0.f;
     store_rec<float, SR>(ws + (size_t)dst * SR, r);
 }
 
@@ -770,8 +771,8 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
         if (lane < cnt) {   // stage one particle per lane
             int p = b.perm[q0 + lane];
             const T *src = w + (size_t)p * spl_rec(ORDER);
-            T r[kRecHead + 2 * ORDER];
-            load_rec<T, kRecHead + 2 * ORDER>(src, r);
+            T r[RecIx<ORDER>::SB];
+            load_rec<T, RecIx<ORDER>::SB>(src, r);
             int c = rec_corner(r[0]);
             int cx = (c & 1023) - ox, cy = ((c >> 10) & 1023) - oy, cz = (c >> 20) - oz;
             stg->off[lane] = cx | (cy << 8) | (cz << 16);
@@ -781,7 +782,7 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_warp(BrickArgs b, 
             for (int i = 0; i < ORDER; ++i) {
                 rec[i] = qp * r[RecIx<ORDER>::VX + i];
                 rec[ORDER + i] = r[RecIx<ORDER>::VY + i];
-                rec[2 * ORDER + i] = src[RecIx<ORDER>::VZ + i];
+                rec[2 * ORDER + i] = r[RecIx<ORDER>::VZ + i];
             }
         }
         __syncwarp();
@@ -862,8 +863,8 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, 
     if (act) {
         int p = b.perm[q];
         const float *src = w + (size_t)p * spl_rec(ORDER);
-        float r[kRecHead + 2 * ORDER];
-        load_rec<float, kRecHead + 2 * ORDER>(src, r);
+        float r[RecIx<ORDER>::SB];
+        load_rec<float, RecIx<ORDER>::SB>(src, r);
         int c = rec_corner(r[0]);
         int cx = (c & 1023) - ox, cy = ((c >> 10) & 1023) - oy, cz = (c >> 20) - oz;
         base = (cz * t + cy) * t + cx;
@@ -872,7 +873,7 @@ __global__ void __launch_bounds__(32 * kSpreadWarps) k_spread_lane(BrickArgs b, 
         for (int i = 0; i < ORDER; ++i) {
             wx[i] = qs * r[RecIx<ORDER>::VX + i];
             wy[i] = r[RecIx<ORDER>::VY + i];
-            wz[i] = src[RecIx<ORDER>::VZ + i];
+            wz[i] = r[RecIx<ORDER>::VZ + i];
         }
     }
     __syncwarp();
@@ -934,7 +935,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 2) k_gather_grp(SplineArgs a,
     int p = valid ? perm[g] : 0;
     int n = a.n, mn = n - 1;
     T e0 = 0, e1 = 0, e2 = 0;
-    const T *rec = w + (size_t)p * spl_rec(ORDER);
+    const T *rec = w + (size_t)(a.perm ? (valid ? g : 0) : p) * spl_rec(ORDER);
     typedef RecIx<ORDER> RI;
     if (act) {
         T vy[ORDER], dy[ORDER];
@@ -1618,6 +1619,7 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
     typedef float T;
     constexpr int n = 32 * P, nh = n / 2 + 1, RS = n + 1, n2 = n * RS;
     constexpr int SR = spread_rec<ORDER>();
+    typedef RecIx<ORDER> RI;
     extern __shared__ unsigned char smem_raw[];
     __shared__ int wb[ORDER], ws[ORDER + 1];
     V *s_tw = reinterpret_cast<V *>(smem_raw), *s_tl = s_tw + n, *s_tk = s_tl + 32;
@@ -1639,7 +1641,7 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         int iz = window_iz<ORDER>(ws, t);
         const float *rec = a.srec + (size_t)(wb[iz] + t - ws[iz]) * SR;
-        int bt = (int)ceilf(fabsf(rec[1]) * rec[kRecHead + 2 * ORDER + iz] * a.mmax2 * 4096.0f) + 1;
+        int bt = (int)ceilf(fabsf(rec[1]) * rec[RI::VZ + iz] * a.mmax2 * 4096.0f) + 1;
         int c1 = (rec_corner(rec[0]) >> 10) & 1023;
 #pragma unroll
         for (int iy = 0; iy < ORDER; ++iy) atomicAdd(&rowb[(c1 - iy) & (n - 1)], bt);
@@ -1660,18 +1662,22 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         int iz = window_iz<ORDER>(ws, t);
         const float *rec = a.srec + (size_t)(wb[iz] + t - ws[iz]) * SR;
-        float r[kRecHead + 2 * ORDER];
-        load_rec<float, kRecHead + 2 * ORDER>(rec, r);
-        float qz = r[1] * rec[kRecHead + 2 * ORDER + iz] * scale;
+        float r[RI::SB];
+        load_rec<float, RI::SB>(rec, r);   // head, z, x and y values
+        float mz = r[RI::VZ];
+#pragma unroll
+        for (int k = 1; k < ORDER; ++k)
+            if (k == iz) mz = r[RI::VZ + k];
+        float qz = r[1] * mz * scale;
         int c = rec_corner(r[0]);
         int c0 = c & 1023, c1 = (c >> 10) & 1023;
 #pragma unroll
         for (int iy = 0; iy < ORDER; ++iy) {
-            float wyz = r[kRecHead + ORDER + iy] * qz;
+            float wyz = r[RI::VY + iy] * qz;
             int row = ((c1 - iy) & (n - 1)) * RS;
 #pragma unroll
             for (int ix = 0; ix < ORDER; ++ix) {
-                int v = __float2int_rn(r[kRecHead + ix] * wyz);
+                int v = __float2int_rn(r[RI::VX + ix] * wyz);
                 atomicAdd(&tacc[row + ((c0 - ix) & (n - 1))], v);
             }
         }
@@ -2325,6 +2331,7 @@ static void spme_args(mg_handle *h, SplineArgs &sa, BrickArgs &bk) {
     int n = h->nmesh;
     sa.ro = h->d_ro;
     sa.az = h->d_az;
+    sa.perm = nullptr;
     sa.np = h->np;
     sa.order = h->order;
     sa.n = n;
@@ -2484,6 +2491,10 @@ int mg_spme_box_grad(mg_handle *h, double *out6, double *scratch) {
 static int spme_fused(mg_handle *h, SplineArgs sa, BrickArgs bk) {
     int np = h->np, n = h->nmesh, tb = 256, gb = (np + tb - 1) / tb;
     sa.plane = 1;
+    // the records in the cell order of the last list build: the gather walks
+    // the particles in that order for the locality of its mesh reads, and
+    // reads the records in order too
+    sa.perm = h->d_perm;
     bk.nbricks = n;          // one bucket per z plane
     bk.M = 1 << 30;          // one (unused) work item per bucket
     MG_TRY(mg_phase_begin(h, "splines"));
