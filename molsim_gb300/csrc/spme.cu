@@ -700,15 +700,45 @@ __global__ void k_brick_scatter(int np, BrickArgs b) {
 template <int ORDER> __host__ __device__ constexpr int spread_rec() { return (RecIx<ORDER>::SB + 3) & ~3; }
 
 // plane sort, second pass: each spline record's spread part to its place
-// in the plane order
+// in the plane order.  Every block scans the plane counts (at most 128)
+// itself; block 0 also stores the plane starts for the spread, which
+// clears the counts.
 template <int ORDER>
 __global__ void k_plane_scatter(int np, BrickArgs b, const float *__restrict__ w, float *__restrict__ ws) {
     mg_pdl_begin();
     typedef RecIx<ORDER> RI;
     constexpr int SR = spread_rec<ORDER>();
+    __shared__ int s_start[129];
+    const int nb = b.nbricks;   // planes
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        int v[4], tot = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int idx = 4 * lane + k;
+            v[k] = idx < nb ? b.count[idx] : 0;
+            tot += v[k];
+        }
+        int x = tot;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        int run = x - tot;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int idx = 4 * lane + k;
+            if (idx < nb) s_start[idx] = run;
+            run += v[k];
+        }
+        if (lane == 31) s_start[nb] = x;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int k = threadIdx.x; k <= nb; k += blockDim.x) b.start[k] = s_start[k];
     int i = blockIdx.x * blockDim.x + threadIdx.x;   // the record
     if (i >= np) return;
-    int dst = b.start[b.brick[i]] + b.rank[i];
+    int dst = s_start[b.brick[i]] + b.rank[i];
     float v[RI::SB], r[SR];
     load_rec<float, RI::SB>(w + (size_t)i * spl_rec(ORDER), v);
 #pragma unroll
@@ -1436,7 +1466,6 @@ __global__ void __launch_bounds__(1024) k_plane_fwd(unsigned long long *__restri
 template <typename T, int P>
 __global__ void __launch_bounds__(1024) k_slab_conv(V2<T> *__restrict__ F, const V2<T> *__restrict__ tw,
                                                     ConvArgs cv, FastDiv fnh) {
-    mg_pdl_begin();
     typedef V2<T> V;
     constexpr int n = 32 * P, nh = n / 2 + 1;
     extern __shared__ unsigned char smem_raw[];
@@ -1449,16 +1478,17 @@ __global__ void __launch_bounds__(1024) k_slab_conv(V2<T> *__restrict__ F, const
     load_lane_tw<T, P>(s_tl, s_tk, tw);
     const int ky = blockIdx.x, fy = min(ky, n - ky);
     const T *mf = (const T *)cv.mf, *ew = (const T *)cv.ew, *vw = (const T *)cv.vw;
-    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
-        int zz = (int)fdiv((unsigned)e, fnh), kx = e - zz * nh;
-        S[e] = F[((size_t)zz * n + ky) * nh + kx];
-    }
-    for (int e = threadIdx.x; e < nh * nh; e += blockDim.x) {
+    for (int e = threadIdx.x; e < nh * nh; e += blockDim.x) {   // constant tables: before the wait
         int fz = (int)fdiv((unsigned)e, fnh), kx = e - fz * nh;
         size_t id = ((size_t)fz * nh + fy) * nh + kx;
         s_mf[e] = mf[id];
         s_ew[e] = ew[id];
         s_vw[e] = vw[id];
+    }
+    mg_pdl_begin();
+    for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
+        int zz = (int)fdiv((unsigned)e, fnh), kx = e - zz * nh;
+        S[e] = F[((size_t)zz * n + ky) * nh + kx];
     }
     __syncthreads();
     const int bl = brev5(lane);
@@ -1506,7 +1536,6 @@ __global__ void __launch_bounds__(1024) k_slab_conv(V2<T> *__restrict__ F, const
 template <typename T, int P>
 __global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F, T *__restrict__ Q,
                                                     const V2<T> *__restrict__ tw, FastDiv fnh) {
-    mg_pdl_begin();
     typedef V2<T> V;
     constexpr int n = 32 * P, nh = n / 2 + 1;
     extern __shared__ unsigned char smem_raw[];
@@ -1516,6 +1545,7 @@ __global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F,
     V *Zs = S + n * nh + w * (n + n / 16);
     load_tw<T>(s_tw, tw, n);
     load_lane_tw<T, P>(s_tl, s_tk, tw);
+    mg_pdl_begin();   // the twiddles need nothing from before
     const size_t z = blockIdx.x;
     const V *Fp = F + z * n * nh;
     for (int e = threadIdx.x; e < n * nh; e += blockDim.x) {
@@ -1571,6 +1601,7 @@ __global__ void __launch_bounds__(1024) k_plane_inv(const V2<T> *__restrict__ F,
 // memory and transforms it: the charge mesh never goes to global memory.
 struct PlaneArgs {
     const int *start;
+    int *count;                // plane counts of the sort, cleared here for the next call
     const float *srec;         // spread records in plane order (spread_rec values each)
     float mmax2;               // (largest B-spline value)^2
     int *err;
@@ -1614,7 +1645,6 @@ template <int ORDER> __device__ __forceinline__ int window_iz(const int *ws, int
 template <int P, int ORDER>
 __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *__restrict__ F,
                                                            const float2 *__restrict__ tw, FastDiv fnh) {
-    mg_pdl_begin();
     typedef float2 V;
     typedef float T;
     constexpr int n = 32 * P, nh = n / 2 + 1, RS = n + 1, n2 = n * RS;
@@ -1633,7 +1663,9 @@ __global__ void __launch_bounds__(1024) k_plane_spread_fwd(PlaneArgs a, float2 *
     for (int k = threadIdx.x; k < n2; k += blockDim.x) tacc[k] = 0;
     for (int k = threadIdx.x; k < n; k += blockDim.x) rowb[k] = 0;
     const int z = blockIdx.x;
+    mg_pdl_begin();   // the twiddles and the cleared planes above need nothing from before
     plane_window<ORDER>(a, z, n, wb, ws);
+    if (threadIdx.x == 0) a.count[z] = 0;   // read by the scatter, which has finished
     __syncthreads();
     const int total = ws[ORDER];
     // per row of the plane: the sum of |q| Mz mmax^2 over the items whose
@@ -2501,7 +2533,6 @@ static int spme_fused(mg_handle *h, SplineArgs sa, BrickArgs bk) {
     MG_TRY((mesh_kernel<float, int>(h, 0, sa, bk)));
     MG_TRY(mg_phase_end(h, "splines"));
     MG_TRY(mg_phase_begin(h, "plane_sort"));
-    mg_launch_pdl(k_brick_prefix, 1, 1024, 0, h->st, bk);
     const float *w = (const float *)h->d_spl_w;
     switch (h->order) {
     case 4: mg_launch_pdl(k_plane_scatter<4>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
@@ -2510,10 +2541,11 @@ static int spme_fused(mg_handle *h, SplineArgs sa, BrickArgs bk) {
     case 7: mg_launch_pdl(k_plane_scatter<7>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
     default: mg_launch_pdl(k_plane_scatter<8>, gb, tb, 0, h->st, np, bk, w, h->d_spl_plane); break;
     }
-    h->launches += 2;
+    h->launches += 1;
     MG_TRY(mg_phase_end(h, "plane_sort"));
     PlaneArgs pa;
     pa.start = h->d_brick_start;
+    pa.count = h->d_brick_count;
     pa.srec = h->d_spl_plane;
     pa.mmax2 = (float)(h->spl_mmax * h->spl_mmax);
     pa.err = h->d_err;
