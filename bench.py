@@ -107,10 +107,11 @@ def algorithmic_bytes(kernel, n, k, pairs, nbond, order=6):
         "splines": n * 24 + n * (12 + 2 * spl),               # ro in; corner, w, dw out
         "brick_sort": n * (12 + 12),                          # corner in; brick, rank, perm out
         "spread": n * (4 + 12 + spl + 8) + k3 * 4,            # perm, corner, w, q in; mesh out
-        # plane sort: plane and rank in, the spread record (head, x/y/z values) in and out
-        "plane_sort": n * (4 + 4) + 2 * n * (16 + spl),
+        # plane sort: plane and rank in, the spread record (corner, charge,
+        # z/x/y values) in and out
+        "plane_sort": n * (4 + 4) + 2 * n * (8 + spl),
         # spread inside the forward plane pass: spread records in; half spectrum out
-        "spread+fft_xy": n * (16 + spl) + spec * 8,
+        "spread+fft_xy": n * (8 + spl) + spec * 8,
         "mesh_fold": k3 * 4,                                  # mesh out
         "fft_x_r2c": k3 * 4 + spec * 8,
         "fft_y_fwd": 2 * spec * 8,
