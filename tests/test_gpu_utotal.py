@@ -68,6 +68,20 @@ def test_mixed_fused_planes_reproducible(nmesh, order, orc, gpu_lib):
         assert e["force_rms"] <= TOL_MIXED_RMS and e["u_tot"] <= 1e-5 and e["virial"] <= 1e-5, e
 
 
+def test_mixed_fused_planes_crowded_windows(orc, gpu_lib):
+    """Crowded plane windows in the fused spread: 14 000 particles on a 32^3
+    mesh at order 6 put 2 500 to 2 700 (particle, plane) items into every
+    plane's CTA.  Same bits on every call, and the oracle's energies and
+    forces within the mixed form's bar."""
+    s = prepared(configs.small_system(seed=33, n=16000, L=150.0, nmesh=32, order=6, mode=abi.MG_BD,
+                                      chains=20, nseg=50), orc)
+    r, g1, _, gpu = run_pair(s, orc, form=abi.MG_MIXED)
+    g2 = gpu.UTotal()
+    assert np.array_equal(g1["forceo"], g2["forceo"]) and g1["u_tot"] == g2["u_tot"]
+    e = utotal_errors(g1, r, s.nptpt)
+    assert e["force_rms"] <= TOL_MIXED_RMS and e["u_tot"] <= 1e-5 and e["virial"] <= 1e-5, e
+
+
 def test_electrolyte_std_config(orc, gpu_lib):
     """The N=1000 standard-Ewald electrolyte (r_c = 30 A, |n| <= 8)."""
     s = prepared(configs.electrolyte_std(), orc)
