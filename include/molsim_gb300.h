@@ -279,13 +279,14 @@ int mg_grad(mg_handle *h, const mg_pot_params *pp, double *phi, double *du_deps,
 /* The force Jacobian along u: jv[3*np] = d(forceo)/dx . u[3*np] (forceo
  * units per A, i.e. minus force_fac times the Hessian of u%tot applied to
  * u) at the handle's positions, from hand-written derivative kernels: the
- * tabulated pair force (its quartic's derivative in r^2), the bonds, and
- * the reciprocal and surface Ewald parts as the field of the dipoles q_j
- * u_j plus the field gradient of the charges along u_i (the dipole kernels
- * of mg_dipole_ewald).  No reference counterpart (the adjoint of MD
+ * tabulated pair force (its quartic's derivative in r^2), the bonds, the
+ * angles (UAngle's forces in forward-mode dual numbers), and the
+ * reciprocal and surface Ewald parts as the field of the dipoles q_j u_j
+ * plus the field gradient of the charges along u_i (the dipole kernels of
+ * mg_dipole_ewald).  No reference counterpart (the adjoint of MD
  * trajectories needs it).  FP64 handles with a Verlet list in MD or BD
- * mode, without angle terms; runs a UTotal first and leaves the reciprocal
- * scratch (structure factors, meshes) changed. */
+ * mode; runs a UTotal first and leaves the reciprocal scratch (structure
+ * factors, meshes) changed. */
 int mg_force_jvp(mg_handle *h, const double *u, double *jv);
 /* The force's parameter derivatives along u: dq[np] = u . d(forceo)/dq_k
  * for each particle charge, deps[nptpt] and dsig[nptpt] = u . d(forceo)/d

@@ -569,6 +569,64 @@ __global__ void k_jvp_bonds(int nbond, const int *__restrict__ ij, const double 
     }
 }
 
+// forward-mode dual numbers (value, derivative along u) for the angle term
+struct Dd {
+    double v, d;
+};
+__device__ __forceinline__ Dd dd_add(Dd a, Dd b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dd dd_sub(Dd a, Dd b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dd dd_mul(Dd a, Dd b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Dd dd_scale(double s, Dd a) { return {s * a.v, s * a.d}; }
+__device__ __forceinline__ Dd dd_rsqrt(Dd a) {   // a^(-1/2)
+    double r = 1.0 / sqrt(a.v);
+    return {r, -0.5 * r * r * r * a.d};
+}
+
+// angles k (theta - theta0)^p (UAngle, energy.F90:5409-5506): the forces
+// of the angle on its three particles, as the angle kernel writes them,
+// evaluated in dual numbers along u, so that the derivative parts are
+// d(force)/dx . u.  One thread per angle (FP64 atomics).
+__global__ void k_jvp_angles(int nangle, const int *__restrict__ ijk, const double *__restrict__ ak,
+                             const double *__restrict__ aeq, const int *__restrict__ ap,
+                             const double *__restrict__ ro, mg_box box, const double *__restrict__ u,
+                             double *__restrict__ jv) {
+    int an = blockIdx.x * blockDim.x + threadIdx.x;
+    if (an >= nangle) return;
+    int jm = ijk[3 * an], ip = ijk[3 * an + 1], jp = ijk[3 * an + 2];
+    Dd dm[3], dq[3];
+    for (int m = 0; m < 3; ++m) {
+        double x = ro[3 * ip + m] - ro[3 * jm + m], y = ro[3 * ip + m] - ro[3 * jp + m];
+        if (fabs(x) > box.half[m]) x -= box.len[m] * round(x * box.inv[m]);   // PBC, anint
+        if (fabs(y) > box.half[m]) y -= box.len[m] * round(y * box.inv[m]);
+        dm[m] = {x, u[3 * ip + m] - u[3 * jm + m]};
+        dq[m] = {y, u[3 * ip + m] - u[3 * jp + m]};
+    }
+    Dd dmi = dd_rsqrt(dd_add(dd_add(dd_mul(dm[0], dm[0]), dd_mul(dm[1], dm[1])), dd_mul(dm[2], dm[2])));
+    Dd dpi = dd_rsqrt(dd_add(dd_add(dd_mul(dq[0], dq[0]), dd_mul(dq[1], dq[1])), dd_mul(dq[2], dq[2])));
+    for (int m = 0; m < 3; ++m) {
+        dm[m] = dd_mul(dm[m], dmi);
+        dq[m] = dd_mul(dq[m], dpi);
+    }
+    Dd c = dd_add(dd_add(dd_mul(dm[0], dq[0]), dd_mul(dm[1], dq[1])), dd_mul(dm[2], dq[2]));
+    double cv = fmax(-1.0, fmin(c.v, 1.0));
+    double th = acos(cv), sn = sin(th);
+    Dd theta = {th, -c.d / sn};                       // d acos(c) = -dc / sin(theta)
+    Dd term = {th - aeq[an], theta.d};
+    int pw = ap[an];
+    Dd tp = {1.0, 0.0};                               // term^(p-1)
+    for (int k = 0; k < pw - 1; ++k) tp = dd_mul(tp, term);
+    Dd rsin = {1.0 / sn, -cos(th) * theta.d / (sn * sn)};   // 1 / sin(theta)
+    Dd fac = dd_mul(dd_scale(-(double)pw * ak[an], tp), rsin);
+    Dd fm = dd_mul(fac, dmi), fp = dd_mul(fac, dpi);
+    for (int m = 0; m < 3; ++m) {
+        Dd gm = dd_mul(fm, dd_sub(dq[m], dd_mul(c, dm[m])));   // on jm
+        Dd gp = dd_mul(fp, dd_sub(dm[m], dd_mul(c, dq[m])));   // on jp
+        atomicAdd(&jv[3 * jm + m], gm.d);
+        atomicAdd(&jv[3 * jp + m], gp.d);
+        atomicAdd(&jv[3 * ip + m], -(gm.d + gp.d));
+    }
+}
+
 // u . d(force)/d(parameter) over the full Verlet list (one thread per slot,
 // each unordered pair met twice): the Lennard-Jones force fsum = (24 eps /
 // r^2)(2 x^2 - x), x = (sigma/r)^6, differentiated by eps_ab and sigma_ab
@@ -648,15 +706,14 @@ __global__ void k_scale(double *__restrict__ x, size_t n, double f) {
 }  // namespace
 
 // d(forceo)/dx . u at the handle's positions (FP64 form, Verlet list, MD
-// or BD, bonds without angles): a UTotal first (the slot positions and the
-// list the pair part reads), then the tabulated pairs (LJ and the
-// real-space Ewald part), the bonds, and the reciprocal and surface parts
-// through the dipole kernels
+// or BD): a UTotal first (the slot positions and the list the pair part
+// reads), then the tabulated pairs (LJ and the real-space Ewald part), the
+// bonds, the angles, and the reciprocal and surface parts through the
+// dipole kernels
 extern "C" int mg_force_jvp(mg_handle *h, const double *u, double *jv) {
     if (!h || !u || !jv) return MG_ERR_ARG;
     if (h->form != MG_FP64) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp needs the FP64 form");
     if (h->txintlist != MG_VLIST) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp needs the Verlet list");
-    if (h->nangle > 0) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp: angle terms are not differentiated");
     if (h->mode == MG_MC) return mg_fail(h, MG_ERR_UNSUPPORTED, "mg_force_jvp needs an MD or BD handle");
     if (!h->list_valid) return mg_fail(h, MG_ERR_STATE, "mg_force_jvp needs a neighbour list (NList)");
     MG_TRY(mg_utotal_launch(h));
@@ -712,6 +769,12 @@ extern "C" int mg_force_jvp(mg_handle *h, const double *u, double *jv) {
             k_jvp_bonds<<<(h->nbond + 127) / 128, 128, 0, h->st>>>(h->nbond, h->d_bond_ij, h->d_bond_k,
                                                                   h->d_bond_eq, h->d_bond_p, h->d_ro, a.box, d_u,
                                                                   d_jv);
+            h->launches++;
+        }
+        if (h->nangle > 0) {
+            k_jvp_angles<<<(h->nangle + 127) / 128, 128, 0, h->st>>>(h->nangle, h->d_angle_ijk, h->d_angle_k,
+                                                                     h->d_angle_eq, h->d_angle_p, h->d_ro, a.box,
+                                                                     d_u, d_jv);
             h->launches++;
         }
         if (h->ewald != MG_EWALD_NONE && (st = mg_force_jvp_rec(h, d_u, d_jv)) != MG_OK) break;

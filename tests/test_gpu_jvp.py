@@ -2,7 +2,8 @@
 forces.
 
 jv = d(forceo)/dx . u from the derivative kernels (the tabulated pair
-force's derivative, bonds, the reciprocal part through the dipole kernels)
+force's derivative, bonds, angles, the reciprocal part through the dipole
+kernels)
 against fourth-order central differences of the device's FP64 forces and
 of the oracle's forces, (8 (F(+h) - F(-h)) - (F(+2h) - F(-2h))) / 12h along
 u, within 1e-6 of the largest component (particles with a pair within
@@ -25,6 +26,8 @@ CASES = [
     ("std_surf", dict(seed=84, ewald=abi.MG_EWALD_STD, ncut=6, lsurf=1)),
     ("no_ewald", dict(seed=85, ewald=abi.MG_EWALD_NONE)),
     ("bonds", dict(seed=86, chains=4, nseg=10)),
+    ("bonds_angles", dict(seed=86, chains=4, nseg=10, angle_kt=1.0)),
+    ("angles_p3", dict(seed=92, chains=3, nseg=8, angle_kt=0.6, angle_p=3, angle_eq=2.2)),
 ]
 
 
@@ -86,8 +89,7 @@ def test_jvp_matches_force_differences(name, kw, orc, gpu_lib):
 
 
 def test_jvp_refuses_what_it_does_not_differentiate(orc, gpu_lib):
-    cases = [(configs.small_system(seed=87, chains=2, nseg=6, angle_kt=1.0), abi.MG_FP64),
-             (configs.small_system(seed=88, mode=abi.MG_MC), abi.MG_FP64),
+    cases = [(configs.small_system(seed=88, mode=abi.MG_MC), abi.MG_FP64),
              (configs.small_system(seed=89), abi.MG_MIXED),
              (configs.small_system(seed=90, txintlist=abi.MG_CELLLIST), abi.MG_FP64)]
     for s, form in cases:

@@ -18,19 +18,22 @@ from molsim_gb300.trajectory import Trajectory, trajectory_function
 pytestmark = pytest.mark.gpu
 
 
-def _setup():
-    s = configs.small_system(seed=91, n=240, L=32.0, ewald=abi.MG_EWALD_SPM, nmesh=32, order=6)
+def _setup(**kw):
+    s = configs.small_system(seed=91, n=240, L=32.0, ewald=abi.MG_EWALD_SPM, nmesh=32, order=6, **kw)
     s.utoltab, s.ftoltab = 1e-9, 1e-8
     s.build_table()
     v0 = s.maxwell_velocities(seed=3)
     return s, s.ro_flat().copy(), v0
 
 
-@pytest.mark.parametrize("hvp", ["analytic", "fd"])
-def test_trajectory_gradient_matches_finite_differences(hvp, gpu_lib):
+@pytest.mark.parametrize("hvp,kw", [("analytic", {}), ("fd", {}),
+                                    ("analytic", dict(chains=3, nseg=8, angle_kt=0.8))],
+                         ids=["analytic", "fd", "analytic_bonds_angles"])
+def test_trajectory_gradient_matches_finite_differences(hvp, kw, gpu_lib):
     """The backward pass with the Hessian-vector products of the derivative
-    kernels (mg_force_jvp) or of central differences of the forces."""
-    s, x0, v0 = _setup()
+    kernels (mg_force_jvp) or of central differences of the forces; also
+    through chains with bonds and angles."""
+    s, x0, v0 = _setup(**kw)
     tr = Trajectory(s, dt=0.002, nsteps=50, checkpoint=10, hvp=hvp)
     L, cks = tr.forward(x0, v0)
     gx, gv = tr.backward(cks)
