@@ -9,7 +9,9 @@ system.  Inputs are seeded synthetic configurations (no dataset exists).
 
 Timing: W untimed warm-up steps, then K device steps; before every step an
 untimed write of 512 MiB evicts the L2 cache (the system fits in L2, so it is
-flushed rather than outgrown); CUDA events on the library's stream bracket
+flushed rather than outgrown), and an untimed read of the same buffer has
+the write's dirty lines written back before the step starts; CUDA events on
+the library's stream bracket
 each step; the per-step times are summed.  `value` is the mixed form
 (FP32 arithmetic, 64-bit fixed-point accumulation); the plain FP64 form is
 reported beside it.  `e2e` runs the same steps through the C ABI with host
@@ -367,6 +369,7 @@ def run_ours(args):
     barrier(world)
     for i in range(ke):
         flush.fill_(float(i))
+        flush.sum()   # the written lines read back: clean before the step
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         st = lib.mg_bd_step_host(emx.h, p_ro, p_f, p_u)
@@ -402,7 +405,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
             "data": "synthetic (seeded polyelectrolyte configuration)",
             "config": {"workload": WORKLOAD, "form": "mixed (FP32 arithmetic, int64 fixed-point accumulation)",
-                       "l2": "flushed (512 MiB write) before every timed step",
+                       "l2": "flushed before every timed step (512 MiB written, then read back so its dirty lines are written back outside the timed step)",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "fp64": results["fp64"],
             "mixed_over_fp64": results["mixed"]["steps_per_s"] / results["fp64"]["steps_per_s"],

@@ -367,8 +367,10 @@ int mg_phase_reset(mg_handle *h, int32_t enable);
 
 /* Benchmark helper: nstep device steps of the set-up integrator (kind 0 =
  * velocity Verlet, 1 = BD).  Before every step a buffer of flush_bytes is
- * written on the handle's stream (0 = no flush) to evict the L2 cache; CUDA
- * events on the same stream bracket each step (not the flush).  *ms_sum
+ * written on the handle's stream (0 = no flush) to evict the L2 cache, then
+ * read back, so that the lines the write left dirty are written back before
+ * the step rather than during it; CUDA events on the same stream bracket
+ * each step (not the flush).  *ms_sum
  * receives the summed device time of the steps.  With phase timing enabled
  * the steps run uncaptured so every kernel can be timed. */
 int mg_bench_steps(mg_handle *h, int32_t kind, int32_t nstep, int64_t flush_bytes,

@@ -164,15 +164,25 @@ __device__ __forceinline__ long pair_slot(const int *sp, int nblk, int j) {
 __global__ void __launch_bounds__(kChkThreads) k_bd_move(BdArgs a) {
     extern __shared__ int sp[];
     __shared__ bool last;
-    load_block_prefix(a.blkcnt, a.nblk, sp);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int off = (a.rng[1] == 0) ? 1 : 0;   // a saved deviate is pending
     bool reset = (*a.chk.flag != 0);
-    double dd[3] = {0.0, 0.0, 0.0};
     double *hro = a.io ? a.io->ro : nullptr;   // host positions, read then written
+    // the particle's own data first: none of it waits for the block prefix
+    double fo[3] = {0.0, 0.0, 0.0}, r0[3] = {0.0, 0.0, 0.0}, sum0[3] = {0.0, 0.0, 0.0}, f1 = 0.0, f2 = 0.0;
     if (p < a.np) {
         int t = a.type[p];
-        double f1 = a.fac1[t], f2 = a.fac2[t];
+        f1 = a.fac1[t];
+        f2 = a.fac2[t];
+        for (int m = 0; m < 3; ++m) {
+            fo[m] = a.forceo[3 * p + m];
+            r0[m] = hro ? hro[3 * p + m] : a.ro[3 * p + m];
+            if (!reset) sum0[m] = a.chk.drosum[3 * p + m];
+        }
+    }
+    load_block_prefix(a.blkcnt, a.nblk, sp);
+    int off = (a.rng[1] == 0) ? 1 : 0;   // a saved deviate is pending
+    double dd[3] = {0.0, 0.0, 0.0};
+    if (p < a.np) {
         for (int m = 0; m < 3; ++m) {
             int g = 3 * p + m;
             double dev;
@@ -189,16 +199,16 @@ __global__ void __launch_bounds__(kChkThreads) k_bd_move(BdArgs a) {
                     dev = (hh & 1) ? v.y : v.x;
                 }
             }
-            double d = __dadd_rn(__dmul_rn(f1, a.forceo[3 * p + m]), __dmul_rn(f2, dev));
+            double d = __dadd_rn(__dmul_rn(f1, fo[m]), __dmul_rn(f2, dev));
             a.drostep[3 * p + m] = d;
             dd[m] = d;
-            double r = __dadd_rn(hro ? hro[3 * p + m] : a.ro[3 * p + m], d);
+            double r = __dadd_rn(r0[m], d);
             r = pbc_wrap(r, a.box.half[m], a.box.len[m], a.box.inv[m]);
             a.ro[3 * p + m] = r;
             if (hro) hro[3 * p + m] = r;
         }
     }
-    mg_chk_accum(p, a.np, dd[0], dd[1], dd[2], reset, a.chk.drosum, a.chk.r2out, a.chk.blkmax);
+    mg_chk_accum_from(p, a.np, dd[0], dd[1], dd[2], reset, sum0, a.chk.drosum, a.chk.r2out, a.chk.blkmax);
     __syncthreads();   // this block has read the state (rng, save)
     if (threadIdx.x == 0) {
         __threadfence();

@@ -312,9 +312,12 @@ constexpr int kChkThreads = 256;
 // cell-count scan: tiles of kScanTile cells, a block of kScanThreads per tile
 constexpr int kScanThreads = 512;
 constexpr int kScanTile = 4096;
-__device__ __forceinline__ void mg_chk_accum(int p, int np, double d0, double d1, double d2, bool reset,
-                                             double *__restrict__ drosum, double *__restrict__ r2out,
-                                             double *__restrict__ blkmax) {
+// as mg_chk_accum, with the particle's previous drosum already loaded into
+// s (not read on a reset), so that a move kernel can issue that load with
+// its other loads
+__device__ __forceinline__ void mg_chk_accum_from(int p, int np, double d0, double d1, double d2, bool reset,
+                                                  const double *s, double *__restrict__ drosum,
+                                                  double *__restrict__ r2out, double *__restrict__ blkmax) {
     __shared__ long long chk_red[kChkThreads / 32];
     double r2 = 0.0;
     if (p < np) {
@@ -324,9 +327,9 @@ __device__ __forceinline__ void mg_chk_accum(int p, int np, double d0, double d1
             s1 = 0.0 + d1;
             s2 = 0.0 + d2;
         } else {
-            s0 = __dadd_rn(drosum[3 * p], d0);
-            s1 = __dadd_rn(drosum[3 * p + 1], d1);
-            s2 = __dadd_rn(drosum[3 * p + 2], d2);
+            s0 = __dadd_rn(s[0], d0);
+            s1 = __dadd_rn(s[1], d1);
+            s2 = __dadd_rn(s[2], d2);
         }
         drosum[3 * p] = s0;
         drosum[3 * p + 1] = s1;
@@ -349,6 +352,18 @@ __device__ __forceinline__ void mg_chk_accum(int p, int np, double d0, double d1
         }
         if (threadIdx.x == 0) blkmax[blockIdx.x] = __longlong_as_double(x);
     }
+}
+
+__device__ __forceinline__ void mg_chk_accum(int p, int np, double d0, double d1, double d2, bool reset,
+                                             double *__restrict__ drosum, double *__restrict__ r2out,
+                                             double *__restrict__ blkmax) {
+    double s[3] = {0.0, 0.0, 0.0};
+    if (p < np && !reset) {
+        s[0] = drosum[3 * p];
+        s[1] = drosum[3 * p + 1];
+        s[2] = drosum[3 * p + 2];
+    }
+    mg_chk_accum_from(p, np, d0, d1, d2, reset, s, drosum, r2out, blkmax);
 }
 
 // the list check's device arrays, for move kernels that run its first pass

@@ -710,6 +710,15 @@ __global__ void k_plane_scatter(int np, BrickArgs b, const float *__restrict__ w
     constexpr int SR = spread_rec<ORDER>();
     __shared__ int s_start[129];
     const int nb = b.nbricks;   // planes
+    int i = blockIdx.x * blockDim.x + threadIdx.x;   // the record
+    // the record and its plane and rank first: they do not wait for the prefix
+    float v[RI::SB];
+    int pl = 0, rk = 0;
+    if (i < np) {
+        load_rec<float, RI::SB>(w + (size_t)i * spl_rec(ORDER), v);
+        pl = b.brick[i];
+        rk = b.rank[i];
+    }
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         int v[4], tot = 0;
@@ -736,11 +745,9 @@ __global__ void k_plane_scatter(int np, BrickArgs b, const float *__restrict__ w
     __syncthreads();
     if (blockIdx.x == 0)
         for (int k = threadIdx.x; k <= nb; k += blockDim.x) b.start[k] = s_start[k];
-    int i = blockIdx.x * blockDim.x + threadIdx.x;   // the record
     if (i >= np) return;
-    int dst = s_start[b.brick[i]] + b.rank[i];
-    float v[RI::SB], r[SR];
-    load_rec<float, RI::SB>(w + (size_t)i * spl_rec(ORDER), v);
+    int dst = s_start[pl] + rk;
+    float r[SR];
 #pragma unroll
     for (int k = 0; k < SR; ++k) r[k] = k < RI::SB ? v[k] : 0.f;
     store_rec<float, SR>(ws + (size_t)dst * SR, r);
