@@ -46,9 +46,30 @@ struct PolyArgs {
     const int *nneighpn, *jpnlist;
     double len[3], half[3], rcut2;
     double *force;
+    long long *ffx;   // k_twobody_p: atom forces in 64-bit fixed point (kPolyFx), converted after the pass
     double *part;   // [nblk][nptpt + 2]: u%twob(1:nptpt), virial
     int *err;
 };
+
+// The host-list atom-pair pass adds the atom forces of a particle's
+// neighbours from many warps.  It adds them as 64-bit integers at the scale
+// 2^36 (a resolution of 1.5e-11 in force units, a range of 1.3e8), so that
+// the sums do not depend on the order of the adds and every call gives the
+// same bits; a force beyond the range flags MG_ERR_NAN.
+constexpr double kPolyFx = 68719476736.0;   // 2^36
+__device__ __forceinline__ void poly_fx_add(long long *p, double v, int *err) {
+    double s = v * kPolyFx;
+    if (!(fabs(s) < 9.0e18)) {
+        mg_dev_error(err, MG_ERR_NAN, 0, 0, 0);
+        return;
+    }
+    atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)__double2ll_rn(s));
+}
+
+__global__ void k_poly_fx_out(const long long *__restrict__ ffx, size_t n, double *__restrict__ force) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) force[i] = (double)ffx[i] * (1.0 / kPolyFx);
+}
 
 // the record (0-based index into ubuf) where the search for r2 starts
 __device__ __forceinline__ int poly_search_start(const PolyArgs &a, int iatjat, double r2) {
@@ -128,9 +149,9 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
                     fj2 = __dsub_rn(fj2, fz);
                     vir = __dsub_rn(vir, __dmul_rn(fsum, ar2));
                 }
-                atomicAdd(&a.force[3 * ja], fj0);
-                atomicAdd(&a.force[3 * ja + 1], fj1);
-                atomicAdd(&a.force[3 * ja + 2], fj2);
+                poly_fx_add(&a.ffx[3 * ja], fj0, a.err);
+                poly_fx_add(&a.ffx[3 * ja + 1], fj1, a.err);
+                poly_fx_add(&a.ffx[3 * ja + 2], fj2, a.err);
             }
 #pragma unroll
             for (int k = 0; k < MG_MAX_NPTPT; ++k)   // static indices keep acc in registers
@@ -139,7 +160,7 @@ __global__ void __launch_bounds__(kPolyThreads) k_twobody_p(PolyArgs a) {
         for (int k = 0; k < 3 * (iaupp - ialow); ++k) {
             double v = fi[k];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) atomicAdd(&a.force[3 * ialow + k], v);
+            if (lane == 0) poly_fx_add(&a.ffx[3 * ialow + k], v, a.err);
         }
     }
     // block sums in a fixed order (thread 0 adds the block's values in turn)
@@ -684,6 +705,7 @@ struct mg_poly {
     int *d_bin_k = nullptr;
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
            *d_part = nullptr, *d_aza = nullptr;
+    long long *d_ffx = nullptr;   // the host-list pair pass's fixed-point atom forces
     std::vector<double> h_part;
     // rigid-body velocity Verlet (mg_poly_rigid_*): per particle
     // [0,3) ro, [3,7) qua, [7,10) rod, [10,13) rodd, [13,17) quad,
@@ -725,7 +747,7 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
     if (!c) return MG_OK;
     void *ptrs[] = {c->d_iptpn, c->d_iptpt, c->d_napt, c->d_ianpn, c->d_iatan, c->d_iatat, c->d_iubuflow,
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
-                    c->d_force, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
+                    c->d_force, c->d_ffx, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
                     c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to, c->d_bin_z0, c->d_bin_inv, c->d_bin_k,
                     c->d_rig, c->d_rig_io, c->d_dscr};
     for (void *q : ptrs)
@@ -790,6 +812,7 @@ extern "C" int mg_poly_create(const mg_poly_params *p, int32_t maxnneigh, mg_pol
     cudaError_t e = cudaMalloc(&c->d_ro, sizeof(double) * 3 * np);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_r, sizeof(double) * 3 * na);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_force, sizeof(double) * 3 * na);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_ffx, sizeof(long long) * 3 * na);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_nneigh, sizeof(int) * np);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_jpnlist, sizeof(int) * (size_t)maxnneigh * np);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int) * 4);
@@ -851,7 +874,7 @@ extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, c
     POLY_CUDA(c, cudaMemcpy(c->d_r, r, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
     POLY_CUDA(c, cudaMemcpy(c->d_nneigh, nneighpn, sizeof(int) * np, cudaMemcpyHostToDevice));
     POLY_CUDA(c, cudaMemcpy(c->d_jpnlist, jpnlist, sizeof(int) * (size_t)c->maxnneigh * np, cudaMemcpyHostToDevice));
-    POLY_CUDA(c, cudaMemset(c->d_force, 0, sizeof(double) * 3 * na));
+    POLY_CUDA(c, cudaMemset(c->d_ffx, 0, sizeof(long long) * 3 * na));
     POLY_CUDA(c, cudaMemset(c->d_err, 0, sizeof(int) * 4));
     PolyArgs a;
     a.np = np;
@@ -884,15 +907,18 @@ extern "C" int mg_poly_utwobody(mg_poly *c, const double *ro, const double *r, c
     }
     a.rcut2 = p.rcut * p.rcut;
     a.force = c->d_force;
+    a.ffx = c->d_ffx;
     a.part = c->d_part;
     a.err = c->d_err;
     size_t sm = sizeof(double) * (p.nptpt + 1) * kPolyThreads;
     k_twobody_p<<<c->nblk_w, kPolyThreads, sm>>>(a);
+    k_poly_fx_out<<<(unsigned)((3 * (size_t)na + 255) / 256), 256>>>(c->d_ffx, 3 * (size_t)na, c->d_force);
     POLY_CUDA(c, cudaGetLastError());
     int herr[4];
     POLY_CUDA(c, cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
     if (herr[0] == MG_ERR_TABLE_UNDERRUN)
         return poly_fail(c, herr[0], "r2 < r2umin for atoms %d and %d (atom-type pair %d)", herr[1], herr[2], herr[3]);
+    if (herr[0] == MG_ERR_NAN) return poly_fail(c, herr[0], "an atom force beyond the fixed-point range (|f| >= 1.3e8)");
     if (herr[0]) return poly_fail(c, herr[0], "ibuf > nbuf for atom-type pair %d", herr[1]);
     POLY_CUDA(c, cudaMemcpy(force, c->d_force, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost));
     POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->h_part.size(), cudaMemcpyDeviceToHost));

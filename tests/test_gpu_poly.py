@@ -2,9 +2,10 @@
 
 Rigid three-site waters and one-atom ions: u%twob per particle-type pair and
 the virial within 1e-10 relative, atom forces within 1e-10 of the largest
-(the GPU adds atom forces with atomics, so only the order of the additions
-differs), for the MD half list and the MC full list; an atom pair below its
-table reports MG_ERR_TABLE_UNDERRUN as the reference's Stop does.
+(the GPU adds the neighbours' atom forces as 64-bit fixed-point integers,
+the same bits on every call), for the MD half list and the MC full list; an
+atom pair below its table reports MG_ERR_TABLE_UNDERRUN as the reference's
+Stop does.
 """
 import numpy as np
 import pytest
@@ -32,6 +33,9 @@ def test_poly_utwobody_matches_oracle(seed, nw, ns, L, full, orc, gpu_lib):
         assert abs(g["u_twob"][k] - ref["u_twob"][k]) <= 1e-10 * abs(ref["u_twob"][0]), k
     assert abs(g["virial"] - ref["virial"]) <= 1e-10 * abs(ref["virial"])
     assert np.abs(g["force"] - ref["force"]).max() <= 1e-10 * np.abs(ref["force"]).max()
+    g2 = e.UTwoBodyP(nn, jl)   # integer sums: the same bits on every call
+    assert np.array_equal(g["force"], g2["force"]) and g["virial"] == g2["virial"]
+    assert np.array_equal(g["u_twob"], g2["u_twob"])
     e.close()
 
 
