@@ -504,19 +504,44 @@ __device__ __forceinline__ void dip_pair_terms(const double d[3], double qi, con
 struct DipArgs {
     const double *az, *dip;
     double *pot, *est, *efg;
+    // k_dipole_real: pot, est, efg (the same layout, 10 na values) in 64-bit
+    // fixed point at kDipFx, converted after the pass
+    long long *fx;
+    int na;
+    int *err;
     double ualpha, ualpha2, f1, f2, f3;
     int lewald;
 };
 
-__device__ __forceinline__ void dip_add_atomic(const DipArgs &q, int ia, const DipTerms &t) {
-    atomicAdd(&q.pot[ia], t.p);
-    for (int m = 0; m < 3; ++m) atomicAdd(&q.est[3 * ia + m], t.e[m]);
-    for (int m = 0; m < 6; ++m) atomicAdd(&q.efg[6 * ia + m], t.g[m]);
+// The real-space dipole pass adds the atoms' potentials, fields and field
+// gradients (charge units per A^k, k = 1, 2, 3) from many warps as 64-bit
+// integers at the scale 2^40 (resolution 9.1e-13, range 8.4e6), so that the
+// sums do not depend on the order of the adds; a value beyond the range
+// flags MG_ERR_NAN.
+constexpr double kDipFx = 1099511627776.0;   // 2^40
+__device__ __forceinline__ void dip_fx_add(long long *p, double v, int *err) {
+    double s = v * kDipFx;
+    if (!(fabs(s) < 9.0e18)) {
+        mg_dev_error(err, MG_ERR_NAN, 0, 0, 0);
+        return;
+    }
+    atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)__double2ll_rn(s));
+}
+
+__device__ __forceinline__ void dip_add_fx(const DipArgs &q, int ia, const DipTerms &t) {
+    dip_fx_add(&q.fx[ia], t.p, q.err);
+    for (int m = 0; m < 3; ++m) dip_fx_add(&q.fx[q.na + 3 * ia + m], t.e[m], q.err);
+    for (int m = 0; m < 6; ++m) dip_fx_add(&q.fx[4 * q.na + 6 * ia + m], t.g[m], q.err);
+}
+
+__global__ void k_dip_fx_out(const long long *__restrict__ fx, size_t n, double *__restrict__ out) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)fx[i] * (1.0 / kDipFx);
 }
 
 // UDipoleP: one warp per particle, lanes over its list row; for each of the
 // particle's atoms the lanes' sums are combined by shuffles, the partner
-// atoms' terms added with FP64 atomics; the virial per block
+// atoms' terms added as fixed-point integers; the virial per block
 __global__ void __launch_bounds__(kPolyThreads) k_dipole_real(PolyArgs a, DipArgs q) {
     __shared__ double red[kPolyThreads];
     double vir = 0.0;
@@ -564,7 +589,7 @@ __global__ void __launch_bounds__(kPolyThreads) k_dipole_real(PolyArgs a, DipArg
                     for (int m = 0; m < 3; ++m) acc.e[m] += oi.e[m];
                     for (int m = 0; m < 6; ++m) acc.g[m] += oi.g[m];
                     vir += vv;
-                    dip_add_atomic(q, ja, oj);
+                    dip_add_fx(q, ja, oj);
                 }
             }
             for (int o = 16; o > 0; o >>= 1) {
@@ -572,7 +597,7 @@ __global__ void __launch_bounds__(kPolyThreads) k_dipole_real(PolyArgs a, DipArg
                 for (int m = 0; m < 3; ++m) acc.e[m] += __shfl_xor_sync(0xffffffffu, acc.e[m], o);
                 for (int m = 0; m < 6; ++m) acc.g[m] += __shfl_xor_sync(0xffffffffu, acc.g[m], o);
             }
-            if (lane == 0) dip_add_atomic(q, ia, acc);
+            if (lane == 0) dip_add_fx(q, ia, acc);
         }
     }
     red[threadIdx.x] = vir;
@@ -706,6 +731,7 @@ struct mg_poly {
     double *d_ubuf = nullptr, *d_r2umin = nullptr, *d_ro = nullptr, *d_r = nullptr, *d_force = nullptr,
            *d_part = nullptr, *d_aza = nullptr;
     long long *d_ffx = nullptr;   // the host-list pair pass's fixed-point atom forces
+    long long *d_dfx = nullptr;   // the real-space dipole pass's fixed-point pot, est, efg
     std::vector<double> h_part;
     // rigid-body velocity Verlet (mg_poly_rigid_*): per particle
     // [0,3) ro, [3,7) qua, [7,10) rod, [10,13) rodd, [13,17) quad,
@@ -749,7 +775,7 @@ extern "C" int mg_poly_destroy(mg_poly *c) {
                     c->d_nneigh, c->d_jpnlist, c->d_err, c->d_ubuf, c->d_r2umin, c->d_ro, c->d_r,
                     c->d_force, c->d_ffx, c->d_part, c->d_aza, c->d_r2atat, c->d_tip, c->d_tatom0, c->d_tovl,
                     c->d_trotm, c->d_trtm, c->d_tdu, c->d_fo, c->d_to, c->d_bin_z0, c->d_bin_inv, c->d_bin_k,
-                    c->d_rig, c->d_rig_io, c->d_dscr};
+                    c->d_rig, c->d_rig_io, c->d_dscr, c->d_dfx};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     delete c;
@@ -1376,6 +1402,7 @@ namespace {
 int dip_scratch(mg_poly *c) {
     if (c->d_dscr) return MG_OK;
     POLY_CUDA(c, cudaMalloc(&c->d_dscr, sizeof(double) * (19 * (size_t)c->p.na + 8)));
+    POLY_CUDA(c, cudaMalloc(&c->d_dfx, sizeof(long long) * 10 * (size_t)c->p.na));
     return MG_OK;
 }
 
@@ -1388,6 +1415,9 @@ DipArgs dip_args(mg_poly *c) {
     q.pot = c->d_dscr + 3 * na;
     q.est = q.pot + na;
     q.efg = q.est + 3 * na;
+    q.fx = c->d_dfx;
+    q.na = p.na;
+    q.err = c->d_err;
     q.ualpha = p.ualpha;
     q.ualpha2 = p.ualpha * p.ualpha;
     q.lewald = p.ualpha > 0.0;
@@ -1448,10 +1478,16 @@ extern "C" int mg_poly_udipole_real(mg_poly *c, const double *ro, const double *
     POLY_CUDA(c, cudaMemcpy(c->d_dscr, dip, sizeof(double) * 3 * na, cudaMemcpyHostToDevice));
     POLY_CUDA(c, cudaMemcpy(c->d_nneigh, nneighpn, sizeof(int) * p.np, cudaMemcpyHostToDevice));
     POLY_CUDA(c, cudaMemcpy(c->d_jpnlist, jpnlist, sizeof(int) * (size_t)c->maxnneigh * p.np, cudaMemcpyHostToDevice));
-    POLY_CUDA(c, cudaMemset(q.pot, 0, sizeof(double) * 10 * na));   // pot, est, efg
+    POLY_CUDA(c, cudaMemset(q.fx, 0, sizeof(long long) * 10 * na));   // pot, est, efg
+    POLY_CUDA(c, cudaMemset(c->d_err, 0, sizeof(int) * 4));
     PolyArgs a = poly_args(c);
     k_dipole_real<<<c->nblk_w, kPolyThreads>>>(a, q);
+    k_dip_fx_out<<<(unsigned)((10 * na + 255) / 256), 256>>>(q.fx, 10 * na, q.pot);
     POLY_CUDA(c, cudaGetLastError());
+    int herr[4];
+    POLY_CUDA(c, cudaMemcpy(herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr[0])
+        return poly_fail(c, herr[0], "an atom potential, field or field gradient beyond the fixed-point range (8.4e6)");
     POLY_CUDA(c, cudaMemcpy(c->h_part.data(), c->d_part, sizeof(double) * c->nblk_w, cudaMemcpyDeviceToHost));
     double vir = 0.0;
     for (int b = 0; b < c->nblk_w; ++b) vir += c->h_part[b];

@@ -3,11 +3,12 @@ against the oracle: UDipole with standard Ewald (with and without the
 surface term) and SPME, UTotal of a dipole system, and rigid-body steps
 driven by it.
 
-FP64 throughout; the real-space pair loop adds the partner atoms' terms
-with FP64 atomics, so the order of the additions differs from the
-oracle's: potentials, fields, field gradients, forces and torques within
-1e-10 of their largest values, energies within 1e-10 of the atomic self
-term that the reciprocal sum cancels.
+FP64 arithmetic; the real-space pair loop adds the partner atoms' terms
+as 64-bit fixed-point integers (the same bits on every call), so the
+order and rounding of the additions differ from the oracle's: potentials,
+fields, field gradients, forces and torques within 1e-10 of their largest
+values, energies within 1e-10 of the atomic self term that the reciprocal
+sum cancels.
 """
 import numpy as np
 import pytest
@@ -50,6 +51,10 @@ def test_udipole_matches_oracle(ewald, lsurf, orc, gpu_lib):
     sc = _scale(s)
     assert abs(g["u_stat"] - ref["u_stat"]) <= 1e-10 * sc
     assert abs(g["virial"] - s.epsi_four_pi * ref["virelec"]) <= 1e-10 * sc
+    g2 = e.UDipole(nn, jl)   # integer sums in the pair loop: the same bits on every call
+    for k in ("potstat", "estat", "efg", "force", "torque"):
+        assert np.array_equal(g[k], g2[k]), k
+    assert g["u_stat"] == g2["u_stat"]
     e.close()
 
 
