@@ -547,7 +547,11 @@ int mg_poly_rigid_kick(mg_poly *c, const double *forceo, const double *torqueo, 
  * mg_poly_rigid_setup (and mg_poly_rigid_prime if wanted).  Returns the
  * last step's ro[3*np], ori[9*np] (column-major), rod[3*np], angvelo[3*np]
  * and uout[4] = u%tot, u%twob(0), u%rec, virial.  Charges only (no
- * dipoles). */
+ * dipoles).  The first step is launched kernel by kernel; with nstep > 1 the
+ * next one is captured on hc's stream into a CUDA graph (ha's streams joined
+ * by events) and replayed for the remaining steps, the same kernels in the
+ * same order, so the results do not depend on how the steps are split over
+ * calls.  With phase timing on either handle every step is launched. */
 int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const double *ra, int32_t nstep, double *ro,
                    double *ori, double *rod, double *angvelo, double *uout);
 /* the accelerations of the current state from forceo and torqueo (a kick

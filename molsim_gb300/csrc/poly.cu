@@ -1635,6 +1635,7 @@ extern "C" int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const do
     double *d_pi = d_ra + nra + p.npt, *d_pe = d_pi + c->nblk;
     cudaStream_t S = hc->st;
     cudaEvent_t e1 = nullptr, e2 = nullptr;
+    cudaGraphExec_t ge = nullptr;
     int st = MG_OK;
     auto ok = [&](cudaError_t e, const char *what) {
         if (e != cudaSuccess && st == MG_OK) st = poly_fail(c, MG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
@@ -1658,24 +1659,26 @@ extern "C" int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const do
         size_t sm = sizeof(double) * (p.nptpt + 1) * kPolyThreads;
         double ualpha2 = p.ualpha * p.ualpha;
         double ewaldfac1 = ewald ? (1.0 / (std::sqrt(3.1415926535897932) * p.ualpha)) * 2.0 * ualpha2 : 0.0;
-        for (int step = 0; step < nstep && st == MG_OK; ++step) {
+        // one step's launches on S (the atom handle's streams joined by events)
+        auto step_launch = [&]() -> bool {
             k_rigid_move<<<(np + 127) / 128, 128, 0, S>>>(np, c->rig_tstep, box, c->d_rig, hc->d_ro, d_ori, d_dro);
             k_place_atoms<<<(np + 127) / 128, 128, 0, S>>>(np, c->d_iptpn, c->d_ianpn, c->d_napt, d_off, d_ra,
                                                          hc->d_ro, d_ori, c->d_r);
             if (!ok(cudaGetLastError(), "move") || mg_lists_build(hc, false) != MG_OK) {
                 if (st == MG_OK) st = poly_fail(c, MG_ERR_STATE, "centres list: %s", hc->err.c_str());
-                break;
+                return false;
             }
             k_twobody_p_list<<<c->nblk_w, kPolyThreads, sm, S>>>(a, hc->d_perm, hc->d_nnb, hc->d_nbr);
             if (ewald) {
                 k_fold_atoms<<<(3 * na + 255) / 256, 256, 0, S>>>(na, c->d_r, box, ha->d_ro);
                 if (!ok(cudaEventRecord(e1, S), "event") || !ok(cudaStreamWaitEvent(ha->st, e1, 0), "wait"))
-                    break;
+                    return false;
                 if (mg_utotal_launch(ha) != MG_OK) {
                     st = poly_fail(c, MG_ERR_STATE, "atom handle: %s", ha->err.c_str());
-                    break;
+                    return false;
                 }
-                if (!ok(cudaEventRecord(e2, ha->st), "event") || !ok(cudaStreamWaitEvent(S, e2, 0), "wait")) break;
+                if (!ok(cudaEventRecord(e2, ha->st), "event") || !ok(cudaStreamWaitEvent(S, e2, 0), "wait"))
+                    return false;
                 k_add_scaled<<<(unsigned)((3 * (size_t)na + 255) / 256), 256, 0, S>>>(
                     3 * (size_t)na, ha->d_forceo, 1.0 / ha->force_fac, c->d_force);
                 PolyArgs ai = a;
@@ -1689,7 +1692,31 @@ extern "C" int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const do
             double *io = c->d_rig_io;
             k_rigid_kick<<<(np + 127) / 128, 128, 0, S>>>(np, c->rig_tstep, c->rig_tvvite, c->rig_nvvite, c->d_rig,
                                                          c->d_fo, c->d_to, io, io + 3 * np);
-            if (!ok(cudaGetLastError(), "step kernels")) break;
+            return ok(cudaGetLastError(), "step kernels");
+        };
+        // the first step as launched (it also makes any allocation the
+        // handles' passes do on first use); the others replay one captured
+        // step, so that a step costs one graph launch.  With phase timing on
+        // a handle, every step is launched as the first.
+        if (!step_launch()) break;
+        bool capture = nstep > 1 && !hc->timing && !(ha && ha->timing);
+        for (int step = 1; step < nstep && !capture && st == MG_OK; ++step)
+            if (!step_launch()) break;
+        if (st != MG_OK) break;
+        if (capture) {
+            cudaGraph_t g = nullptr;
+            if (!ok(cudaStreamBeginCapture(S, cudaStreamCaptureModeThreadLocal), "capture")) break;
+            bool launched = step_launch();
+            cudaError_t ce = cudaStreamEndCapture(S, &g);
+            if (!launched || !ok(ce, "capture")) {
+                if (g) cudaGraphDestroy(g);
+                break;
+            }
+            ce = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (!ok(ce, "graph instantiate")) break;
+            for (int step = 1; step < nstep; ++step)
+                if (!ok(cudaGraphLaunch(ge, S), "graph launch")) break;
         }
         if (st != MG_OK) break;
         // the last step's state and energies
@@ -1736,6 +1763,7 @@ extern "C" int mg_poly_md_run(mg_poly *c, mg_handle *hc, mg_handle *ha, const do
         uout[2] = urec;           // u%rec (atoms' reciprocal and self terms, molecular self term)
         uout[3] = vir + vmol;     // virial (with the molecular term)
     } while (false);
+    if (ge) cudaGraphExecDestroy(ge);
     if (e1) cudaEventDestroy(e1);
     if (e2) cudaEventDestroy(e2);
     cudaFree(d);

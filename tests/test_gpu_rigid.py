@@ -127,3 +127,29 @@ def test_device_md_run_matches_host_steps(ewald, orc, gpu_lib):
     assert abs(ra["virial"] - rb["virial"]) <= 1e-9 * max(abs(ra["virial"]), 1.0)
     ea.close()
     eb.close()
+
+
+def test_device_md_run_graph_replays_the_step(orc, gpu_lib):
+    """mg_poly_md_run launches its first step and replays one captured step
+    graph for the rest: one ten-step call and ten one-step calls (each step
+    launched as a first step) give the same bits."""
+    def system():
+        s = configs.water_ions(seed=52, nwater=150, nsalt=8, L=20.0, rcut=9.0)
+        s.relpermitt = 78.0
+        s.ewald, s.ualpha, s.order, s.nmesh = abi.MG_EWALD_SPM, 0.35, 6, 32
+        s = s.principal_axes()
+        s.build_table(orc.orc_pot_twobody_tab)
+        return s
+    a, b = system(), system()
+    v, w = _initial_velocities(a, seed=5)
+    ea, eb = _engine(a), _engine(b)
+    ea.RigidSetup(0.0005, v, w, prime=True)
+    eb.RigidSetup(0.0005, v, w, prime=True)
+    ra = ea.MDRun(10)
+    for _ in range(10):
+        rb = eb.MDRun(1)
+    assert np.array_equal(a.ro, b.ro) and np.array_equal(a.ori, b.ori)
+    assert np.array_equal(ra["rod"], rb["rod"])
+    assert ra["u_tot"] == rb["u_tot"] and ra["virial"] == rb["virial"]
+    ea.close()
+    eb.close()
