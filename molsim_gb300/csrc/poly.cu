@@ -7,12 +7,13 @@
 // pair adds the tabulated energy (the linear interval search from iubuflow
 // of its atom-type pair and the quintic in d = r^2 - z_low) to u%twob of the
 // particle-type pair, fsum*dr to the first atom's force and -fsum*dr to the
-// second's, and -fsum*r^2 to the virial.  FP64 throughout.
+// second's, and -fsum*r^2 to the virial.  FP64 arithmetic.
 //
-// One thread per particle walks its list row; the atom forces are added
-// with FP64 atomics (the order of the additions is not fixed, so forces
-// agree with the reference's sequential sums to rounding), the energies and
-// the virial are summed per block and the blocks in order on the host.
+// One warp per particle walks its list row; the neighbours' atom forces are
+// added as 64-bit fixed-point integers (the same bits on every call; they
+// agree with the reference's sequential FP64 sums to the fixed-point
+// resolution), the energies and the virial are summed per block and the
+// blocks in order on the host.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
