@@ -20,6 +20,16 @@ with its own DUTotal and MCUpdate.  Restated from mc.F90:
   GetRandomTrialPos of dtrancl2; after DUTotal the move is rejected without
   a Metropolis draw when a cluster member would come within radcl2 of a
   particle of the type outside the cluster (the cluster would change).
+- BrushCl2Move (mc.F90:3028-3158): the cluster of the chosen particle among
+  the particles of its type (radcl2, as SPartCl2Move), and the brush of
+  every cluster member: the chains ic = ip, ip + nppt, ip + 2 nppt, ... (ip
+  the member's particle number, nppt the number of particles of its type;
+  the reference grafts the chains cyclically on the particles of the first
+  type), whole, in segment order.  One GetRandomTrialPos of dtranbrush moves
+  all of them (the reference draws it with dtranbrush, not dtranbrushcl2);
+  after DUTotal the move is rejected without a Metropolis draw when a
+  cluster member would come within radcl2 of a particle of its type
+  outside the cluster.
 - PivotMove (mc.F90:1967-2172): the part of a chain on one side of a pivot
   bead ('short', 'lower' or 'upper'), unwrapped by UndoPBCChain
   (molaux.F90:1266-1325), rotated by alpha = drotpivot (Random - 1/2) about
@@ -33,7 +43,8 @@ with its own DUTotal and MCUpdate.  Restated from mc.F90:
 - Random (mollib.F90:2689-2709): Marsaglia's xorshift combined with
   Park-Miller, the generator every move draws from.
 
-The cluster moves' second shell (radcl1 > 0), the pivot's crosslinked
+The cluster moves' second shell (radcl1 > 0), the brush move's rotations
+of polyatomic particles, the pivot's crosslinked
 generations and the non-energetic weights (umbrella, MC weights) are not
 part of this path.
 """
@@ -167,12 +178,16 @@ class MoveParams:
     txmembcl2: str = "ipt"
     radcl2: float = 0.0
     dtrancl2: float = 0.0
+    pbrushcl2: float = 0.0
+    dtranbrush: float = 0.0
 
 
 @dataclass
 class MCStats:
-    trials: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0})
-    accepted: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0})
+    trials: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0,
+                                                             "brushcl2": 0})
+    accepted: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0,
+                                                               "brushcl2": 0})
     events: List[str] = field(default_factory=list)
 
 
@@ -194,10 +209,10 @@ class MCPass:
             raise ValueError(f"{len(plist)} move parameter sets for {npt} particle types")
         self.p = plist
         # cumulative probabilities (IOMC, CallMove's order): pspart, then
-        # pspartcl2, ppivot and pchain
+        # pspartcl2, ppivot, pchain and pbrushcl2
         self.cum = []
         for mp in plist:
-            tot = max(mp.pspart + mp.pspartcl2 + mp.ppivot + mp.pchain, 1e-15)
+            tot = max(mp.pspart + mp.pspartcl2 + mp.ppivot + mp.pchain + mp.pbrushcl2, 1e-15)
             a = mp.pspart / tot
             a2 = a + mp.pspartcl2 / tot
             b = a2 + mp.ppivot / tot
@@ -326,6 +341,51 @@ class MCPass:
             self.stats.events.append(f"cl2:{'a' if acc else ('o' if ovl else 'r')}{len(ips)}")
         return acc
 
+    def brushcl2(self, ipmove, mp):
+        """BrushCl2Move: the cluster of ipmove among its type and the chains
+        grafted on the cluster's members, moved together."""
+        ipt = int(self.s.iptpn[ipmove - 1])
+        of_type = np.flatnonzero(self.s.iptpn == ipt) + 1          # iplow .. ipupp
+        rc2 = mp.radcl2 ** 2
+        pos = self.ro[of_type - 1]
+        pairs = []
+        for a in range(len(of_type) - 1):
+            r2 = self._pbcr2(pos[a] - pos[a + 1:])
+            for b in np.flatnonzero(r2 < rc2):
+                pairs.append((a, a + 1 + b))
+        lab = clusters(len(of_type), pairs)
+        me = int(np.flatnonzero(of_type == ipmove)[0])
+        prim = of_type[lab == lab[me]]                              # the primary cluster, in particle order
+        nppt, nc = len(of_type), len(self.chains)
+        ips = [int(ip) for ip in prim]
+        for ip in prim:                                             # its brush: chains ip, ip + nppt, ... <= nc
+            for ic in range(int(ip), nc + 1, nppt):
+                ips.extend(self.chains[ic - 1])
+        ips = np.asarray(ips)
+        d = self._trial_translation(mp.dtranbrush)
+        rotm = self._pbc(self.ro[ips - 1] + d)
+        self.stats.trials["brushcl2"] += 1
+        du, ovl = self.e.DUTotal(ips, rotm)
+        if not ovl:
+            # a particle of the type outside the moving set within radcl2 of
+            # a moved cluster member: the cluster would change, rejected
+            outside = of_type[~np.isin(of_type, ips)]
+            for k in range(len(prim)):
+                if outside.size and (self._pbcr2(self.ro[outside - 1] - rotm[k]) < rc2).any():
+                    if self.record:
+                        self.stats.events.append("brushcl2:x")
+                    return False
+        acc = self._metropolis(ovl, du["du_tot"])
+        if acc:
+            self.e.MCUpdate()
+            self.ro[ips - 1] = rotm
+            self.drostep[ips - 1] += d
+            self.du_acc += du["du_tot"]
+            self.stats.accepted["brushcl2"] += 1
+        if self.record:
+            self.stats.events.append(f"brushcl2:{'a' if acc else ('o' if ovl else 'r')}{len(prim)}:{len(ips)}")
+        return acc
+
     def chain(self, ipmove, mp):
         ic = int(self.chain_of[ipmove])
         if ic < 0:
@@ -414,6 +474,8 @@ class MCPass:
                 self.spartcl2(ipmove, mp)
             elif pr < b:
                 self.pivot(ipmove, mp)
-            else:
+            elif pr < c or mp.pbrushcl2 <= 0.0:
                 self.chain(ipmove, mp)
+            else:
+                self.brushcl2(ipmove, mp)
         self.e.NList("step", self.drostep.reshape(-1))

@@ -116,6 +116,32 @@ def chain_system(seed=71, chains=4, nseg=10, **kw):
     return s
 
 
+def brush_system(seed=74, ngraft=6, chains=12, nseg=5, n=400, L=40.0, **kw):
+    """A brush for BrushCl2Move: ngraft grafting particles (a fourth type, a
+    copy of the divalent ion type) numbered first, then `chains` bonded
+    chains of nseg beads (chain ic grafted cyclically on particle
+    ((ic - 1) mod ngraft) + 1, as the reference's brush loop reads it), then
+    the other ions.  Built from small_system by moving the first ngraft
+    divalent ions to the front."""
+    s = configs.small_system(seed=seed, mode=abi.MG_MC, chains=chains, nseg=nseg, n=n, L=L, angle_kt=0.0, **kw)
+    nbead = chains * nseg
+    types = np.asarray(s.iptpn)
+    div = [i for i in range(nbead, s.np_) if types[i] == 3][:ngraft]
+    if len(div) < ngraft:
+        raise ValueError("not enough divalent ions to graft on")
+    rest = [i for i in range(nbead, s.np_) if i not in set(div)]
+    order = np.array(div + list(range(nbead)) + rest)
+    new_of = np.empty(s.np_, dtype=np.int64)
+    new_of[order] = np.arange(s.np_)
+    s.ro = np.asarray(s.ro)[order].copy()
+    s.iptpn = types[order].astype(np.int32)
+    s.species = list(s.species) + [dataclasses.replace(s.species[2], name="graft")]
+    s.iptpn[:ngraft] = len(s.species)
+    s.bond_ip = (new_of[np.asarray(s.bond_ip) - 1] + 1).astype(np.int32)
+    s.bond_jp = (new_of[np.asarray(s.bond_jp) - 1] + 1).astype(np.int32)
+    return s
+
+
 def centre_lists(ro, L, rlist, full=False):
     """A Verlet list of particle centres (nneighpn, jpnlist as NList stores
     it: 1-based, maxnneigh entries per particle): every pair within rlist

@@ -153,3 +153,42 @@ def test_cluster_moves_ucheck(memb, orc):
     u1 = _fresh(s, orc, mc.ro)
     assert abs((u0 + mc.du_acc) - u1) < 1e-9 * abs(u1)
     assert np.array_equal(e.GetPositions(), mc.ro)
+
+
+def test_brush_moves_ucheck(orc):
+    """BrushCl2Move (mc.F90:3028-3158) beside single-particle moves: a
+    grafting particle's cluster moves with every chain grafted on its
+    members, moves that would change the cluster are rejected, the bonds of
+    the moved chains keep their lengths, and the accepted du%tot add up to
+    the change of UTotal."""
+    from tests.helpers import brush_system
+    s = brush_system(txintlist=abi.MG_CELLLIST)
+    s.build_table(orc.orc_pot_twobody_tab)
+    e = Engine(s, lib=orc, prefix="orc_")
+    e.SetPositions(s.ro_flat())
+    e.NList("write")
+    u0 = e.UTotal()["u_tot"]
+    L = s.boxlen[0]
+
+    def bonds(ro):
+        d = ro[s.bond_jp - 1] - ro[s.bond_ip - 1]
+        d -= L * np.round(d / L)
+        return np.linalg.norm(d, axis=1)
+
+    b0 = bonds(s.ro)
+    ion_p = MoveParams(pspart=1.0, dtran=2.0)
+    still = MoveParams(pspart=0.0)   # type 2 holds the chain beads: they move only with their brush
+    graft_p = MoveParams(pspart=0.2, dtran=1.0, pbrushcl2=0.8, radcl2=14.0, dtranbrush=2.0)
+    mc = MCPass(e, s, iseed=23, params=[ion_p, still, ion_p, graft_p], record=True)
+    for _ in range(3):
+        mc.run_pass()
+    st = mc.stats
+    ev = [x for x in st.events if x.startswith("brushcl2:")]
+    assert st.trials["brushcl2"] > 5 and st.accepted["brushcl2"] > 0
+    moved = [x for x in ev if x[9] in "aro"]
+    # a member moves with its 2 chains of 5 beads: 11 particles per member
+    assert all(int(x.split(":")[2]) == 11 * int(x.split(":")[1][1:]) for x in moved)
+    assert np.abs(bonds(mc.ro) - b0).max() < 1e-9
+    u1 = _fresh(s, orc, mc.ro)
+    assert abs((u0 + mc.du_acc) - u1) < 1e-9 * abs(u1)
+    assert np.array_equal(e.GetPositions(), mc.ro)

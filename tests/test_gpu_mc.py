@@ -254,3 +254,32 @@ def test_cluster_passes_match_oracle(memb, orc, gpu_lib):
     assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
     u1 = gpu.UTotal()
     assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
+
+
+def test_brush_passes_match_oracle(orc, gpu_lib):
+    """MC passes with the brush cluster move BrushCl2Move (mc.F90:3028-3158):
+    grafting particles, clustered within radcl2, move together with every
+    chain grafted on them, beside single-particle moves of the ions, through
+    the oracle and through the GPU with the same Random stream: the same
+    moves are tried and accepted or rejected, positions agree bit for bit,
+    and the accepted du%tot add up to the GPU's UTotal."""
+    from molsim_gb300.mc import MCPass, MoveParams
+    from tests.helpers import brush_system
+    s = prepared(brush_system(txintlist=abi.MG_CELLLIST), orc)
+    ref, gpu, u_ref, u_gpu = _pair(s, orc)
+    ion_p = MoveParams(pspart=1.0, dtran=2.0)
+    still = MoveParams(pspart=0.0)   # type 2 holds the chain beads: they move only with their brush
+    graft_p = MoveParams(pspart=0.2, dtran=1.0, pbrushcl2=0.8, radcl2=14.0, dtranbrush=2.0)
+    runs = [MCPass(e, s, iseed=23, params=[ion_p, still, ion_p, graft_p], record=True) for e in (ref, gpu)]
+    for mc in runs:
+        for _ in range(3):
+            mc.run_pass()
+    a, b = runs
+    assert a.stats.events == b.stats.events
+    assert b.stats.trials["brushcl2"] > 5 and b.stats.accepted["brushcl2"] > 0
+    assert np.array_equal(a.ro, b.ro)
+    assert np.array_equal(gpu.GetPositions(), b.ro)
+    scale = abs(u_ref["u_tot"]) + abs(u_ref["u_rec"]) + 1.0
+    assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
+    u1 = gpu.UTotal()
+    assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
