@@ -20,6 +20,12 @@ with its own DUTotal and MCUpdate.  Restated from mc.F90:
   GetRandomTrialPos of dtrancl2; after DUTotal the move is rejected without
   a Metropolis draw when a cluster member would come within radcl2 of a
   particle of the type outside the cluster (the cluster would change).
+- BrushMove (mc.F90:2850-3019, lcl1brush = .false.): the chosen particle
+  and the chains grafted on it (as below), translated by one
+  GetRandomTrialPos of dtranbrush and rotated about the particle by alpha =
+  drotbrush (Random - 1/2) about a SphRandom axis (RotTranBrush: the chains
+  unwrapped from the particle by UndoPBCChain, RotateSetPart, then the
+  translation, rotm(ipmove) - ro(ipmove), added to every member).
 - BrushCl2Move (mc.F90:3028-3158): the cluster of the chosen particle among
   the particles of its type (radcl2, as SPartCl2Move), and the brush of
   every cluster member: the chains ic = ip, ip + nppt, ip + 2 nppt, ... (ip
@@ -178,6 +184,8 @@ class MoveParams:
     txmembcl2: str = "ipt"
     radcl2: float = 0.0
     dtrancl2: float = 0.0
+    pbrush: float = 0.0
+    drotbrush: float = 0.0        # degrees
     pbrushcl2: float = 0.0
     dtranbrush: float = 0.0
 
@@ -185,9 +193,9 @@ class MoveParams:
 @dataclass
 class MCStats:
     trials: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0,
-                                                             "brushcl2": 0})
+                                                             "brush": 0, "brushcl2": 0})
     accepted: Dict[str, int] = field(default_factory=lambda: {"spart": 0, "cl2": 0, "pivot": 0, "chain": 0,
-                                                               "brushcl2": 0})
+                                                               "brush": 0, "brushcl2": 0})
     events: List[str] = field(default_factory=list)
 
 
@@ -209,15 +217,16 @@ class MCPass:
             raise ValueError(f"{len(plist)} move parameter sets for {npt} particle types")
         self.p = plist
         # cumulative probabilities (IOMC, CallMove's order): pspart, then
-        # pspartcl2, ppivot, pchain and pbrushcl2
+        # pspartcl2, ppivot, pchain, pbrush and pbrushcl2
         self.cum = []
         for mp in plist:
-            tot = max(mp.pspart + mp.pspartcl2 + mp.ppivot + mp.pchain + mp.pbrushcl2, 1e-15)
+            tot = max(mp.pspart + mp.pspartcl2 + mp.ppivot + mp.pchain + mp.pbrush + mp.pbrushcl2, 1e-15)
             a = mp.pspart / tot
             a2 = a + mp.pspartcl2 / tot
             b = a2 + mp.ppivot / tot
             c = b + mp.pchain / tot
-            self.cum.append((a, a2, b, c, tot > 1e-15))
+            c2 = c + mp.pbrush / tot
+            self.cum.append((a, a2, b, c, c2, tot > 1e-15))
         self.L = np.asarray(system.boxlen, dtype=np.float64)
         self.half = 0.5 * self.L
         self.Li = 1.0 / self.L
@@ -341,6 +350,36 @@ class MCPass:
             self.stats.events.append(f"cl2:{'a' if acc else ('o' if ovl else 'r')}{len(ips)}")
         return acc
 
+    def _brush_chains(self, ip, nppt):
+        """The chains grafted on particle ip: ic = ip, ip + nppt, ... <= nc
+        (1-based chain numbers, the reference's brush loop)."""
+        return list(range(int(ip), len(self.chains) + 1, nppt))
+
+    def brush(self, ipmove, mp):
+        """BrushMove: the particle and its chains, translated and rotated."""
+        ipt = int(self.s.iptpn[ipmove - 1])
+        nppt = int(np.count_nonzero(self.s.iptpn == ipt))
+        ics = self._brush_chains(ipmove, nppt)
+        ips = [int(ipmove)]
+        for ic in ics:
+            ips.extend(self.chains[ic - 1])
+        ips = np.asarray(ips)
+        r0 = self.ro[ipmove - 1]
+        d = self._trial_translation(mp.dtranbrush)
+        dtr = (r0 + d) - r0                                  # rotm(ipmove) - ro(ipmove)
+        axis = self.rng.sphere()
+        alpha = (mp.drotbrush * (units.Pi / 180.0)) * (self.rng() - 0.5)   # drotbrush*sclang
+        v = {int(ipmove): r0.copy()}
+        for ic in ics:
+            v.update(self._undo_pbc_chain(ic - 1, ref=r0))
+        vaux = np.array([v[int(ip)] for ip in ips])
+        rot = axis_angle_matrix(axis, alpha)
+        rotm = r0 + (vaux - r0) @ rot.T
+        drotm = rotm - vaux
+        rotm = self._pbc(rotm + dtr)
+        drotm = drotm + dtr
+        return self._try("brush", ips, rotm, drotm)
+
     def brushcl2(self, ipmove, mp):
         """BrushCl2Move: the cluster of ipmove among its type and the chains
         grafted on the cluster's members, moved together."""
@@ -356,10 +395,10 @@ class MCPass:
         lab = clusters(len(of_type), pairs)
         me = int(np.flatnonzero(of_type == ipmove)[0])
         prim = of_type[lab == lab[me]]                              # the primary cluster, in particle order
-        nppt, nc = len(of_type), len(self.chains)
+        nppt = len(of_type)
         ips = [int(ip) for ip in prim]
-        for ip in prim:                                             # its brush: chains ip, ip + nppt, ... <= nc
-            for ic in range(int(ip), nc + 1, nppt):
+        for ip in prim:                                             # its brush
+            for ic in self._brush_chains(ip, nppt):
                 ips.extend(self.chains[ic - 1])
         ips = np.asarray(ips)
         d = self._trial_translation(mp.dtranbrush)
@@ -395,12 +434,13 @@ class MCPass:
         rotm = self._pbc(self.ro[ips - 1] + d)
         return self._try("chain", ips, rotm, np.tile(d, (len(ips), 1)))
 
-    def _undo_pbc_chain(self, ic):
-        """UndoPBCChain(ro(first segment), ic, +1): the chain made continuous
-        from its first segment."""
+    def _undo_pbc_chain(self, ic, ref=None):
+        """UndoPBCChain(rref, ic, +1) (molaux.F90:1266-1325): the chain made
+        continuous from its first segment, which takes the image nearest to
+        rref (by default the first segment itself)."""
         c = self.chains[ic]
         out = {}
-        ref = self.ro[c[0] - 1]
+        ref = self.ro[c[0] - 1] if ref is None else ref
         out[c[0]] = ref + self._pbc(self.ro[c[0] - 1] - ref)
         for jp, ip in zip(c[:-1], c[1:]):
             out[ip] = out[jp] + self._pbc(self.ro[ip - 1] - self.ro[jp - 1])
@@ -460,7 +500,7 @@ class MCPass:
             ipmove = ipass if self.isamp == 0 else 1 + int(np_ * self.rng())
             ipmove = max(1, min(ipmove, np_))
             ipt = int(self.s.iptpn[ipmove - 1]) - 1
-            a, a2, b, c, moving = self.cum[ipt]
+            a, a2, b, c, c2, moving = self.cum[ipt]
             if not moving:
                 continue
             mp = self.p[ipt]
@@ -474,8 +514,10 @@ class MCPass:
                 self.spartcl2(ipmove, mp)
             elif pr < b:
                 self.pivot(ipmove, mp)
-            elif pr < c or mp.pbrushcl2 <= 0.0:
+            elif pr < c or mp.pbrush + mp.pbrushcl2 <= 0.0:
                 self.chain(ipmove, mp)
+            elif pr < c2 or mp.pbrushcl2 <= 0.0:
+                self.brush(ipmove, mp)
             else:
                 self.brushcl2(ipmove, mp)
         self.e.NList("step", self.drostep.reshape(-1))

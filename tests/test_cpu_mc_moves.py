@@ -192,3 +192,57 @@ def test_brush_moves_ucheck(orc):
     u1 = _fresh(s, orc, mc.ro)
     assert abs((u0 + mc.du_acc) - u1) < 1e-9 * abs(u1)
     assert np.array_equal(e.GetPositions(), mc.ro)
+
+
+def test_brush_rotations_ucheck(orc):
+    """BrushMove (mc.F90:2850-3019): a grafting particle with the chains
+    grafted on it, translated and rotated about the particle; the bonds of
+    the moved chains keep their lengths, the distance from the particle to
+    every bead of its brush along the unwrapped chain is kept, and the
+    accepted du%tot add up to the change of UTotal."""
+    from tests.helpers import brush_system
+    s = brush_system(txintlist=abi.MG_CELLLIST)
+    s.build_table(orc.orc_pot_twobody_tab)
+    e = Engine(s, lib=orc, prefix="orc_")
+    e.SetPositions(s.ro_flat())
+    e.NList("write")
+    u0 = e.UTotal()["u_tot"]
+    L = s.boxlen[0]
+
+    def dist(ro, i, j):
+        d = ro[np.asarray(j) - 1] - ro[np.asarray(i) - 1]
+        d -= L * np.round(d / L)
+        return np.linalg.norm(d, axis=-1)
+
+    b0 = dist(s.ro, s.bond_ip, s.bond_jp)
+    ng = int(np.count_nonzero(s.iptpn == 4))
+    chains, _, _ = chains_from_bonds(s.np_, s.bond_ip, s.bond_jp)
+    graft = [(ic % ng) + 1 for ic in range(len(chains))]
+
+    def reach(ro, ic):
+        # the beads' distances to the grafting particle along the unwrapped
+        # chain (the minimum image from the particle to the first bead, then
+        # bond by bond): a rigid move keeps them, whatever the box
+        c = chains[ic]
+        pts = np.asarray(c) - 1
+        d = np.diff(ro[np.concatenate(([graft[ic] - 1], pts))], axis=0)
+        d -= L * np.round(d / L)
+        return np.linalg.norm(np.cumsum(d, axis=0), axis=1)
+
+    g0 = [reach(s.ro, ic) for ic in range(len(chains))]
+    ion_p = MoveParams(pspart=1.0, dtran=2.0)
+    still = MoveParams(pspart=0.0)   # type 2 holds the chain beads: they move only with their brush
+    # the grafting particles make only brush moves, so that their distances
+    # to the beads of their brushes are invariants
+    graft_p = MoveParams(pspart=0.0, pbrush=1.0, dtranbrush=1.0, drotbrush=10.0)
+    mc = MCPass(e, s, iseed=31, params=[ion_p, still, ion_p, graft_p], record=True)
+    for _ in range(3):
+        mc.run_pass()
+    st = mc.stats
+    assert st.trials["brush"] > 5 and st.accepted["brush"] > 1
+    assert np.abs(dist(mc.ro, s.bond_ip, s.bond_jp) - b0).max() < 1e-9
+    for ic in range(len(chains)):
+        assert np.abs(reach(mc.ro, ic) - g0[ic]).max() < 1e-9
+    u1 = _fresh(s, orc, mc.ro)
+    assert abs((u0 + mc.du_acc) - u1) < 1e-9 * abs(u1)
+    assert np.array_equal(e.GetPositions(), mc.ro)

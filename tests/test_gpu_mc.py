@@ -283,3 +283,31 @@ def test_brush_passes_match_oracle(orc, gpu_lib):
     assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
     u1 = gpu.UTotal()
     assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
+
+
+def test_brush_rotation_passes_match_oracle(orc, gpu_lib):
+    """MC passes with BrushMove (mc.F90:2850-3019): a grafting particle and
+    the chains grafted on it translated and rotated about the particle,
+    through the oracle and through the GPU with the same Random stream: the
+    same moves are accepted, positions agree bit for bit, and the accepted
+    du%tot add up to the GPU's UTotal."""
+    from molsim_gb300.mc import MCPass, MoveParams
+    from tests.helpers import brush_system
+    s = prepared(brush_system(txintlist=abi.MG_CELLLIST), orc)
+    ref, gpu, u_ref, u_gpu = _pair(s, orc)
+    ion_p = MoveParams(pspart=1.0, dtran=2.0)
+    still = MoveParams(pspart=0.0)   # type 2 holds the chain beads: they move only with their brush
+    graft_p = MoveParams(pspart=0.2, dtran=1.0, pbrush=0.8, dtranbrush=1.0, drotbrush=10.0)
+    runs = [MCPass(e, s, iseed=31, params=[ion_p, still, ion_p, graft_p], record=True) for e in (ref, gpu)]
+    for mc in runs:
+        for _ in range(3):
+            mc.run_pass()
+    a, b = runs
+    assert a.stats.events == b.stats.events
+    assert b.stats.accepted["brush"] > 1
+    assert np.array_equal(a.ro, b.ro)
+    assert np.array_equal(gpu.GetPositions(), b.ro)
+    scale = abs(u_ref["u_tot"]) + abs(u_ref["u_rec"]) + 1.0
+    assert abs(a.du_acc - b.du_acc) <= 1e-9 * scale
+    u1 = gpu.UTotal()
+    assert abs((u_gpu["u_tot"] + b.du_acc) - u1["u_tot"]) <= 1e-9 * scale
