@@ -116,12 +116,14 @@ def system_from_input(inp, cnf=None, seed=1, text=False):
 
     # particles (monoatomic: one atom type per particle type)
     npt = int(scalar(part, "npt", 1))
+    txelec = _lower(scalar(part, "txelec", "charge"))
+    if txelec == "pol":   # induced dipoles (UManyBodyP, energy.F90:2327-2497): not built
+        raise NotImplementedError("txelec = 'pol' (polarisation is not built)")
     natpt = array(part, "natpt", npt, 1, dtype=int)
     if (natpt != 1).any():
-        raise NotImplementedError("polyatomic particles (natpt > 1)")
-    txelec = _lower(scalar(part, "txelec", "charge"))
-    if txelec != "charge":   # particle.F90:307-321: weak charges, dipoles, polarisation, ...
-        raise NotImplementedError(f"txelec = {txelec!r} (the path treats fixed charges)")
+        raise NotImplementedError("polyatomic particles (natpt > 1): this reader builds monoatomic systems")
+    if txelec != "charge":   # particle.F90:307-321: weak charges, dipoles, ...
+        raise NotImplementedError(f"txelec = {txelec!r} (this reader builds fixed-charge systems)")
     for name in ("latweakcharge", "dipain", "polain"):
         if name in part:
             vals = part[name].values or []
